@@ -1,0 +1,1552 @@
+// ORACLE - TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of the hot path of vaishna77/Lippmann_Schwinger_Solver
+// (directory GMRES/): uniform quadtree, LFR/HFR interaction lists and
+// directional cones, adaptive Gauss-Legendre precomputations, nested cross
+// approximation (NCA), operator assembly, the ten DAFMM matvec phases with
+// per-box QR solves, the dense getMatrixEntry2 operator and GMRES.
+//
+// It is the checker for the GPU product and the timed CPU baseline. Nothing
+// in the product links or calls it. Each routine names the reference lines
+// it restates. Parity unpinned: the reference needs Eigen and Boost.Math,
+// which are absent, so it was never run here and ships no golden vectors.
+//
+// Arithmetic conventions that keep the restatement deterministic:
+//  * compiled with -ffp-contract=off, so no fused multiply-adds appear on
+//    any host (x86 or aarch64);
+//  * kernel entries, quadrature integrands and ACA updates use the same
+//    std::complex expression order as the reference source;
+//  * Bessel functions come from libstdc++ (std::cyl_bessel_j /
+//    std::cyl_neumann), called once per order like the reference's Boost
+//    calls (GMRES/G_FMM2DTree.hpp:73-100).
+
+#include "ls_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <set>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#include <omp.h>
+
+namespace ora {
+
+using cd = std::complex<double>;
+static const double PI = 3.1415926535897932384;  // GMRES/ACA.hpp:14
+static const cd I(0.0, 1.0);                       // GMRES/ACA.hpp:10
+
+struct Pt { double x, y; };
+struct Pair { int x, y; };
+
+// ---------------------------------------------------------------------------
+// Dense complex matrix, column major.
+struct CMat {
+  int r = 0, c = 0;
+  std::vector<cd> a;
+  CMat() {}
+  CMat(int rr, int cc) : r(rr), c(cc), a((size_t)rr * cc, cd(0.0, 0.0)) {}
+  cd& operator()(int i, int j) { return a[(size_t)j * r + i]; }
+  const cd& operator()(int i, int j) const { return a[(size_t)j * r + i]; }
+};
+
+// y += A * x (sequential column order).
+static void gemv_acc(const CMat& A, const cd* x, cd* y) {
+  for (int j = 0; j < A.c; ++j) {
+    const cd xj = x[j];
+    const cd* col = &A.a[(size_t)j * A.r];
+    for (int i = 0; i < A.r; ++i) y[i] += col[i] * xj;
+  }
+}
+
+static double vnorm(const std::vector<cd>& v) {
+  double s = 0.0;
+  for (const cd& z : v) s += std::norm(z);
+  return std::sqrt(s);
+}
+
+// ---------------------------------------------------------------------------
+// Householder QR with column pivoting (LAPACK xGEQP3 style with norm
+// downdating), standing in for Eigen::ColPivHouseholderQR used at
+// GMRES/G_FMM2DTree.hpp:2135, 2346, 3379, 3536 (Atilde) and
+// GMRES/GMRES.cpp:299 (least squares). solve() returns the basic solution
+// on the numerically nonzero pivots, the rest set to zero.
+struct ColPivQR {
+  int m = 0, n = 0, nzp = 0;
+  CMat qr;
+  std::vector<cd> tau;
+  std::vector<int> perm;  // perm[k] = original column placed at position k
+
+  void compute(const CMat& A) {
+    m = A.r; n = A.c;
+    qr = A;
+    const int size = std::min(m, n);
+    tau.assign(size, cd(0.0, 0.0));
+    perm.resize(n);
+    for (int j = 0; j < n; ++j) perm[j] = j;
+    std::vector<double> nu(n), nd(n);
+    double maxn = 0.0;
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < m; ++i) s += std::norm(qr(i, j));
+      nu[j] = nd[j] = std::sqrt(s);
+      maxn = std::max(maxn, nu[j]);
+    }
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double thr_helper = (maxn * eps) * (maxn * eps) / double(std::max(m, 1));
+    const double downdate_thr = std::sqrt(eps);
+    nzp = size;
+    std::vector<cd> tmp(n);
+    for (int k = 0; k < size; ++k) {
+      int p = k;
+      for (int j = k + 1; j < n; ++j) if (nu[j] > nu[p]) p = j;
+      if (nzp == size && nu[p] * nu[p] < thr_helper * double(m - k)) nzp = k;
+      if (p != k) {
+        for (int i = 0; i < m; ++i) std::swap(qr(i, k), qr(i, p));
+        std::swap(nu[k], nu[p]);
+        std::swap(nd[k], nd[p]);
+        std::swap(perm[k], perm[p]);
+      }
+      // Reflector for qr(k:m, k): H = I - tau v v^H with v = [1; ess].
+      cd c0 = qr(k, k);
+      double tail = 0.0;
+      for (int i = k + 1; i < m; ++i) tail += std::norm(qr(i, k));
+      double beta;
+      const double tiny = std::numeric_limits<double>::min();
+      if (tail <= tiny && c0.imag() * c0.imag() <= tiny) {
+        tau[k] = cd(0.0, 0.0);
+        beta = c0.real();
+        for (int i = k + 1; i < m; ++i) qr(i, k) = cd(0.0, 0.0);
+      } else {
+        beta = std::sqrt(std::norm(c0) + tail);
+        if (c0.real() >= 0.0) beta = -beta;
+        const cd d = c0 - beta;
+        for (int i = k + 1; i < m; ++i) qr(i, k) = qr(i, k) / d;
+        tau[k] = std::conj((beta - c0) / beta);
+      }
+      qr(k, k) = cd(beta, 0.0);
+      // Apply H to the trailing columns.
+      if (tau[k] != cd(0.0, 0.0)) {
+        for (int j = k + 1; j < n; ++j) {
+          cd t = qr(k, j);
+          for (int i = k + 1; i < m; ++i) t += std::conj(qr(i, k)) * qr(i, j);
+          tmp[j] = t;
+        }
+        for (int j = k + 1; j < n; ++j) {
+          qr(k, j) -= tau[k] * tmp[j];
+          for (int i = k + 1; i < m; ++i) qr(i, j) -= (tau[k] * qr(i, k)) * tmp[j];
+        }
+      }
+      // Column-norm downdating (LAPACK working note 176).
+      for (int j = k + 1; j < n; ++j) {
+        if (nu[j] != 0.0) {
+          double t = std::abs(qr(k, j)) / nu[j];
+          t = (1.0 + t) * (1.0 - t);
+          if (t < 0.0) t = 0.0;
+          const double ratio = nu[j] / nd[j];
+          const double t2 = t * ratio * ratio;
+          if (t2 <= downdate_thr) {
+            double s = 0.0;
+            for (int i = k + 1; i < m; ++i) s += std::norm(qr(i, j));
+            nd[j] = std::sqrt(s);
+            nu[j] = nd[j];
+          } else {
+            nu[j] *= std::sqrt(t);
+          }
+        }
+      }
+    }
+  }
+
+  // x (length n) = argmin |A x - b| on the nonzero pivots.
+  void solve(const cd* b, cd* x) const {
+    std::vector<cd> c(b, b + m);
+    for (int k = 0; k < nzp; ++k) {
+      if (tau[k] == cd(0.0, 0.0)) continue;
+      cd t = c[k];
+      for (int i = k + 1; i < m; ++i) t += std::conj(qr(i, k)) * c[i];
+      t *= tau[k];
+      c[k] -= t;
+      for (int i = k + 1; i < m; ++i) c[i] -= qr(i, k) * t;
+    }
+    for (int i = nzp - 1; i >= 0; --i) {
+      cd s = c[i];
+      for (int j = i + 1; j < nzp; ++j) s -= qr(i, j) * c[j];
+      c[i] = s / qr(i, i);
+    }
+    for (int j = 0; j < n; ++j) x[j] = cd(0.0, 0.0);
+    for (int k = 0; k < nzp; ++k) x[perm[k]] = c[k];
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Special functions.
+
+// GMRES/G_FMM2DTree.hpp:73-100: J_n, Y_n with the reflection rule for n < 0.
+static double besselJ(int n, double x) {
+  if (n >= 0) return std::cyl_bessel_j(double(n), x);
+  double t = std::cyl_bessel_j(double(-n), x);
+  return ((-n) % 2 == 0) ? t : -t;
+}
+static double besselY(int n, double x) {
+  if (n >= 0) return std::cyl_neumann(double(n), x);
+  double t = std::cyl_neumann(double(-n), x);
+  return ((-n) % 2 == 0) ? t : -t;
+}
+
+// GMRES/G_FMM2DTree.hpp:670-672 (and FarFieldInteraction.hpp:96-98).
+static double chebT(double x, int n) { return std::cos(n * std::acos(x)); }
+
+// Gauss-Legendre rule of order n on [-1, 1], computed by Newton iteration on
+// P_n in long double. Nodes are stored in the interleaved order of the
+// reference's table (GMRES/Gauss_Legendre_Nodes_and_Weights.hpp:17):
+// pairs (-t_i, +t_i) from the centre outwards (a zero node first when n is
+// odd).
+static void gauss_legendre(int n, std::vector<double>& nodes, std::vector<double>& weights) {
+  std::vector<long double> t, w;
+  for (int i = 1; i <= n; ++i) {
+    long double x = std::cos(PI * (i - 0.25L) / (n + 0.5L));
+    long double dp = 0.0L;
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1.0L, p1 = x;
+      for (int k = 2; k <= n; ++k) {
+        long double p2 = ((2.0L * k - 1.0L) * x * p1 - (k - 1.0L) * p0) / k;
+        p0 = p1; p1 = p2;
+      }
+      dp = n * (x * p1 - p0) / (x * x - 1.0L);
+      long double dx = p1 / dp;
+      x -= dx;
+      if (std::fabs((double)dx) < 1e-30) break;
+    }
+    {
+      long double p0 = 1.0L, p1 = x;
+      for (int k = 2; k <= n; ++k) {
+        long double p2 = ((2.0L * k - 1.0L) * x * p1 - (k - 1.0L) * p0) / k;
+        p0 = p1; p1 = p2;
+      }
+      dp = n * (x * p1 - p0) / (x * x - 1.0L);
+    }
+    t.push_back(x);
+    w.push_back(2.0L / ((1.0L - x * x) * dp * dp));
+  }
+  // t is descending from near +1; collect the non-negative roots ascending.
+  std::vector<std::pair<long double, long double>> pos;
+  for (int i = 0; i < n; ++i) if (t[i] >= 0.0L) pos.push_back({t[i], w[i]});
+  std::sort(pos.begin(), pos.end());
+  nodes.clear(); weights.clear();
+  for (auto& pw : pos) {
+    if (pw.first == 0.0L || std::fabs((double)pw.first) < 1e-300) {
+      nodes.push_back(0.0); weights.push_back((double)pw.second);
+    } else {
+      nodes.push_back(-(double)pw.first); weights.push_back((double)pw.second);
+      nodes.push_back((double)pw.first);  weights.push_back((double)pw.second);
+    }
+  }
+}
+
+// Rounds to 6 significant digits the way the reference's text round trip
+// does: Eigen's operator<< at the default stream precision (printf %g with
+// 6 digits) followed by operator>> (GMRES/G_FMM2DTree.hpp:1264-1270,
+// 1304-1315, 1868-1950).
+static double round6(double v) {
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%.6g", v);
+  return std::strtod(buf, nullptr);
+}
+static cd round6(cd v) { return cd(round6(v.real()), round6(v.imag())); }
+
+// ---------------------------------------------------------------------------
+// Adaptive 2-D Gauss-Legendre quadrature, GMRES/domain2D.hpp:7-138: each
+// panel is integrated with a 10x10 rule; a panel whose four children
+// reproduce its value within epsilon (absolute) becomes a leaf and
+// contributes its own (parent) value.
+template <class F>
+static cd adaptive_quad(const F& f, const std::vector<double>& gn, const std::vector<double>& gw,
+                        double eps) {
+  struct Panel { double xc, yc, xr, yr; cd val; };
+  const int nn = (int)gn.size();
+  auto integrate = [&](Panel& p) {
+    cd s(0.0, 0.0);
+    for (int m = 0; m < nn; ++m) {
+      const double px = p.xc + p.xr * gn[m];
+      for (int q = 0; q < nn; ++q) {
+        const double py = p.yc + p.yr * gn[q];
+        s += gw[m] * gw[q] * f(px, py);
+      }
+    }
+    s *= (p.xr * p.yr);
+    p.val = s;
+  };
+  Panel root{0.0, 0.0, 1.0, 1.0, cd(0.0, 0.0)};
+  integrate(root);
+  cd total(0.0, 0.0);
+  // Depth-first recursion in the reference's child order (0,1,2,3).
+  std::vector<Panel> stack;
+  stack.push_back(root);
+  // Explicit stack that reproduces the recursive visiting order: children
+  // are pushed in reverse so that child 0 is refined first.
+  while (!stack.empty()) {
+    Panel p = stack.back();
+    stack.pop_back();
+    const double xr = 0.5 * p.xr, yr = 0.5 * p.yr;
+    Panel ch[4] = {{p.xc - xr, p.yc - yr, xr, yr, cd()}, {p.xc + xr, p.yc - yr, xr, yr, cd()},
+                   {p.xc + xr, p.yc + yr, xr, yr, cd()}, {p.xc - xr, p.yc + yr, xr, yr, cd()}};
+    for (int l = 0; l < 4; ++l) integrate(ch[l]);
+    cd err = p.val;
+    for (int l = 0; l < 4; ++l) err -= ch[l].val;
+    if (std::abs(err) < eps) {
+      total += p.val;
+    } else {
+      for (int l = 3; l >= 0; --l) stack.push_back(ch[l]);
+    }
+  }
+  return total;
+}
+
+// ---------------------------------------------------------------------------
+// Tree data, restating FMM2DCone / FMM2DBox (GMRES/G_FMM2DTree.hpp:119-227).
+struct Node {  // either an LFR box or one cone of an HFR box
+  bool out_active = false, in_active = false;
+  std::vector<Pair> IL;
+  std::vector<int> out_charge, out_check, in_charge, in_check, user_check;
+  CMat out_Ar, M2M;
+  ColPivQR out_A, in_A;
+  std::vector<CMat> M2L;
+  CMat L2Lc[4];  // HFR: block per child (FMM2DCone::L2L[4])
+  std::vector<cd> out_charges, in_charges, in_potential;
+  bool has_out_charges = false;
+};
+
+struct Box {
+  double cx = 0, cy = 0, r = 0;
+  bool leaf = false;
+  std::vector<Pair> nbrs;
+  int colleague[9];
+  std::vector<int> chargeLoc;  // leaves only
+  Node lfr;                    // LFR data (also used for leaves)
+  CMat L2L;                    // LFR: block from the parent (FMM2DBox::L2L)
+  std::vector<Node> cones;     // HFR cones
+  std::vector<cd> multipoles;
+};
+
+struct Oracle {
+  ora_cfg cfg;
+  int nL = 0, rank = 0, nb = 0, S = 15, N = 0, level_LFR = 2;
+  double kappa = 0, L = 1;
+  std::vector<double> boxRadius, ConeAperture;
+  std::vector<int> nCones;
+  std::vector<std::vector<Box>> tree;
+  std::vector<Pt> grid;
+  std::vector<double> cheb1d;
+  std::vector<Pt> chebStd;
+  std::vector<Pair> bases;  // (a, b) per basis index
+  std::vector<double> gln, glw;
+  CMat Mleaf;               // (2S+1) x rank, leaf level
+  CMat nearB[9];            // colleague blocks at the leaf level
+  std::vector<double> Qpinv;  // nb x rank, row major
+
+  // --- contrast (GMRES/GMRES.cpp:5-117) ---
+  double contrast(Pt r) const {
+    switch (cfg.Qchoice) {
+      case 0: { double R2 = r.x * r.x + r.y * r.y; return 1.5 * std::exp(-160.0 * R2); }
+      case 1: {
+        static const double cxs[20] = {-1.17182014706864, -0.861066625441127, -1.14533939124057,
+          -0.856639124568525, -0.620066350133170, -0.457064031294315, -0.482782006538245,
+          -0.635070123186999, 0.108594058866164, -0.0315722590552472, -0.177274727610547,
+          0.0342987980936911, 0.369662097773613, 0.591444264226524, 0.401225715100565,
+          0.666822699314234, 1.10327781188617, 0.827519268441487, 0.873411278211136, 1.09482906183464};
+        static const double cys[20] = {-0.361066625441127, 0.0719520938231629, 0.354660608759432,
+          1.14336087543147, -1.12006635013317, -0.457064031294315, 0.364929876813001,
+          0.802261227250738, -0.394084977497864, -0.0315722590552472, 0.322725272389453,
+          1.03429879809369, -1.13033790222639, 0.0137164199764117, 0.401225715100565,
+          1.16682269931423, -0.345187707108795, -0.172480731558513, 0.373411278211136, 1.09482906183464};
+        double q = 0.0, a = 0.0013;
+        for (int i = 0; i < 20; ++i) {
+          double R2 = (r.x - cxs[i]) * (r.x - cxs[i]) + (r.y - cys[i]) * (r.y - cys[i]);
+          q += 1.5 * std::exp(-R2 / a);
+        }
+        return q;
+      }
+      case 2: {
+        double C = 0.4987;
+        double psi = 1.0 - (r.x - 0.15 * (1 - r.x * r.x)) * (r.x - 0.15 * (1 - r.x * r.x)) -
+                     C * (1.0 + 0.3 * r.x) * (1.0 + 0.3 * r.x) * r.y * r.y;
+        static const double aa[5] = {0.45, 0.195, 0.51, 0.195, 0.63};
+        static const double xx[5] = {0.8, 0.54, -0.14, -0.5, 0.18};
+        static const double yy[5] = {0.0, -0.28, 0.7, -0.01, 0.8};
+        if (psi <= 0.05) return 0.0;
+        double g = 0.0;
+        for (int i = 0; i < 5; ++i) {
+          double t = (r.x - xx[i]) * (r.x - xx[i]) + (r.y - yy[i]) * (r.y - yy[i]);
+          g += aa[i] * std::exp(-t / 0.01);
+        }
+        return -1.5 * (psi - 0.05) - g * std::cos(0.9 * r.y);
+      }
+      case 3: { double R2 = r.x * r.x + r.y * r.y; return 0.5 * std::erfc(5.0 * (R2 - 1.0)); }
+      case 4: {
+        double R = std::sqrt(r.x * r.x + r.y * r.y);
+        double th = std::atan2(r.y, r.x);
+        return (1.0 - std::pow(std::sin(0.5 * th), 500)) * std::exp(-2000 * (0.1 - R * R) * (0.1 - R * R));
+      }
+      case 5: {
+        double R = std::sqrt(r.x * r.x + r.y * r.y);
+        return 4 * (r.y - 0.1) * (1.0 - std::erf(25.0 * (R - 0.3)));
+      }
+      default: {  // seeded Gaussian bumps: sum_k a_k exp(-|x - c_k|^2 / w_k^2)
+        double q = 0.0;
+        for (int k = 0; k < cfg.n_bumps; ++k) {
+          double dx = r.x - cfg.bump_cx[k], dy = r.y - cfg.bump_cy[k];
+          double R2 = dx * dx + dy * dy;
+          q += cfg.bump_a[k] * std::exp(-R2 / (cfg.bump_w[k] * cfg.bump_w[k]));
+        }
+        return q;
+      }
+    }
+  }
+
+  // --- far-field kernel entry (GMRES/G_FMM2DTree.hpp:603-658) ---
+  // The Hankel vector h_n = (J_n + i Y_n) e^{i n theta} of target point i
+  // about the centre of leaf `leaf`; entries of all 36 sources of that leaf
+  // share it, so it is cached per (i, leaf) inside one ACA or block fill.
+  void hankel(int i, int leafk, cd* h) const {
+    const Pt ri = grid[i];
+    const Box& B = tree[nL][leafk];
+    const double th = std::atan2(ri.y - B.cy, ri.x - B.cx);
+    const double R2 = (ri.y - B.cy) * (ri.y - B.cy) + (ri.x - B.cx) * (ri.x - B.cx);
+    const double R = kappa * std::sqrt(R2);
+    for (int n = -S; n <= S; ++n) {
+      cd t = (besselJ(n, R) + I * besselY(n, R)) * std::exp(I * double(n) * th);
+      h[n + S] = t;
+    }
+  }
+  cd entry_from_h(int i, int j, const cd* h) const {
+    const int idx = j % rank;
+    cd s = 0.0 + 0.0 * I;
+    for (int n = -S; n <= S; ++n) s += Mleaf(n + S, idx) * h[n + S];
+    s *= I / 4.0;
+    if (cfg.findPhi) {
+      s *= kappa * kappa * (contrast(grid[i]));
+      if (i == j) s += 1.0;
+    }
+    return s;
+  }
+
+  struct HCache {
+    const Oracle* o;
+    std::unordered_map<long long, std::vector<cd>> m;
+    const cd* get(int i, int leafk) {
+      long long key = (long long)i * 1048576LL + leafk;
+      auto it = m.find(key);
+      if (it != m.end()) return it->second.data();
+      std::vector<cd> h(2 * o->S + 1);
+      o->hankel(i, leafk, h.data());
+      auto r = m.emplace(key, std::move(h));
+      return r.first->second.data();
+    }
+  };
+  cd entry(int i, int j, HCache& hc) const { return entry_from_h(i, j, hc.get(i, j / rank)); }
+  CMat getMatrix(const std::vector<int>& rows, const std::vector<int>& cols, HCache& hc) const {
+    CMat A((int)rows.size(), (int)cols.size());
+    for (int a = 0; a < A.r; ++a)
+      for (int b = 0; b < A.c; ++b) A(a, b) = entry(rows[a], cols[b], hc);
+    return A;
+  }
+
+  // --- NCA: ACA_only_nodes, GMRES/ACA.hpp:253-481 ---
+  static int argmax_abs(const std::vector<cd>& v, const std::set<int>& allowed) {
+    auto it = allowed.begin();
+    int idx = *it;
+    double mx = std::abs(v[idx]);
+    for (; it != allowed.end(); ++it)
+      if (std::abs(v[*it]) > mx) { idx = *it; mx = std::abs(v[idx]); }
+    return idx;
+  }
+  static cd dotc(const std::vector<cd>& a, const std::vector<cd>& b) {  // a^H b
+    cd s(0.0, 0.0);
+    for (size_t i = 0; i < a.size(); ++i) s += std::conj(a[i]) * b[i];
+    return s;
+  }
+  // Returns rank; row_bases / col_bases index rows / cols; Ar = K(pivot rows, cols).
+  int aca(const std::vector<int>& rows, const std::vector<int>& cols, double eps,
+          std::vector<int>& rb, std::vector<int>& cb, CMat* Ar, HCache& hc) const {
+    const int N1 = (int)rows.size(), N2 = (int)cols.size();
+    const int mn = std::min(N1, N2);
+    int rank_ = 0;
+    std::set<int> rrem, crem;
+    for (int l = 0; l < N1; ++l) rrem.insert(l);
+    for (int l = 0; l < N2; ++l) crem.insert(l);
+    std::vector<std::vector<cd>> U, V, Arows;
+    std::vector<cd> row(N2), col(N1), u, v;
+    auto getRow = [&](int ri) { std::vector<cd> r(N2); for (int k = 0; k < N2; ++k) r[k] = entry(rows[ri], cols[k], hc); return r; };
+    auto getCol = [&](int ci) { std::vector<cd> c(N1); for (int k = 0; k < N1; ++k) c[k] = entry(rows[k], cols[ci], hc); return c; };
+    int ri = 0, ci = 0;
+    if (N1 < N2) {
+      int l;
+      for (l = 0; l < N1; ++l) {
+        ri = l;
+        row = getRow(ri);
+        ci = argmax_abs(row, crem);
+        if (std::abs(row[ci]) > eps * std::pow(10, -1.0 * 0)) break;
+      }
+      if (l == N1) return 0;
+      v.resize(N2);
+      for (int s = 0; s < N2; ++s) v[s] = row[s] / row[ci];
+      rb.push_back(ri); cb.push_back(ci);
+      col = getCol(ci);
+      u = col;
+      U.push_back(u); V.push_back(v); Arows.push_back(row);
+      crem.erase(ci); rrem.erase(ri);
+      rank_ = 1;
+      double normS = 0.0, prev = 1000.0;
+      ri = argmax_abs(col, rrem);
+      while (std::abs(row[ci]) > eps * std::pow(10, -1.0 * 0) && std::abs(col[ri]) > eps &&
+             std::abs(prev - normS) >= eps * prev && rank_ < mn) {
+        rb.push_back(ri);
+        row = getRow(ri);
+        std::vector<cd> row_temp = row;
+        for (int l2 = 0; l2 < rank_; ++l2)
+          for (int s = 0; s < (int)V[l2].size(); ++s) row[s] -= U[l2][ri] * V[l2][s];
+        ci = argmax_abs(row, crem);
+        cb.push_back(ci);
+        for (int s = 0; s < (int)row.size(); ++s) v[s] = row[s] / row[ci];
+        col = getCol(ci);
+        for (int l2 = 0; l2 < rank_; ++l2)
+          for (int s = 0; s < (int)U[l2].size(); ++s) col[s] -= V[l2][ci] * U[l2][s];
+        u = col;
+        if (vnorm(u) < 1e-8 || vnorm(v) < 1e-8) { rb.pop_back(); cb.pop_back(); break; }
+        U.push_back(u); V.push_back(v); Arows.push_back(row_temp);
+        ++rank_;
+        crem.erase(ci); rrem.erase(ri);
+        if (rank_ != 2) prev = normS;
+        normS = std::pow(normS, 2) + std::pow(vnorm(u) * vnorm(v), 2);
+        for (int l2 = 0; l2 < rank_; ++l2) normS += 2 * std::abs(dotc(U[l2], u) * dotc(V[l2], v));
+        normS = std::sqrt(normS);
+        ri = argmax_abs(col, rrem);
+      }
+    } else {
+      int l;
+      for (l = 0; l < N2; ++l) {
+        ci = l;
+        col = getCol(ci);
+        ri = argmax_abs(col, rrem);
+        if (std::abs(col[ri]) > eps * std::pow(10, -1.0 * 0)) break;
+      }
+      if (l == N2) return 0;
+      cb.push_back(ci);
+      v.resize(N1);
+      for (int s = 0; s < N1; ++s) v[s] = col[s] / col[ri];
+      rb.push_back(ri);
+      row = getRow(ri);
+      u = row;
+      U.push_back(u); V.push_back(v); Arows.push_back(row);
+      rank_ = 1;
+      rrem.erase(ri); crem.erase(ci);
+      double normS = 0.0, prev = 1000.0;
+      ci = argmax_abs(row, crem);
+      while (std::abs(row[ci]) > eps * std::pow(10, -1.0 * 0) && std::abs(col[ri]) > eps &&
+             std::abs(prev - normS) >= eps * prev && rank_ < mn) {
+        cb.push_back(ci);
+        col = getCol(ci);
+        for (int l2 = 0; l2 < rank_; ++l2)
+          for (int s = 0; s < (int)V[l2].size(); ++s) col[s] -= U[l2][ci] * V[l2][s];
+        ri = argmax_abs(col, rrem);
+        rb.push_back(ri);
+        for (int s = 0; s < (int)col.size(); ++s) v[s] = col[s] / col[ri];
+        row = getRow(ri);
+        std::vector<cd> row_temp = row;
+        for (int l2 = 0; l2 < rank_; ++l2)
+          for (int s = 0; s < (int)U[l2].size(); ++s) row[s] -= V[l2][ri] * U[l2][s];
+        u = row;
+        if (vnorm(u) < 1e-8 || vnorm(v) < 1e-8) { cb.pop_back(); rb.pop_back(); break; }
+        U.push_back(u); V.push_back(v); Arows.push_back(row_temp);
+        ++rank_;
+        rrem.erase(ri); crem.erase(ci);
+        if (rank_ != 2) prev = normS;
+        normS = std::pow(normS, 2) + std::pow(vnorm(u) * vnorm(v), 2);
+        for (int l2 = 0; l2 < rank_; ++l2) normS += 2 * std::abs(dotc(U[l2], u) * dotc(V[l2], v));
+        normS = std::sqrt(normS);
+        ci = argmax_abs(row, crem);
+      }
+    }
+    if (Ar) {
+      *Ar = CMat(rank_, N2);
+      for (int a = 0; a < rank_; ++a)
+        for (int b = 0; b < N2; ++b) (*Ar)(a, b) = Arows[a][b];
+    }
+    return rank_;
+  }
+
+  // ------------------------------------------------------------------------
+  bool build(char* err, int errlen);
+  void precompute();
+  void interactions();
+  void nca();
+  void user_checks();
+  void assemble();
+  void matvec(const cd* x, cd* y);
+  void dense_matvec(const cd* x, cd* y);
+
+  bool lfr(int j) const { return j >= level_LFR; }
+};
+
+// GMRES/G_FMM2DTree.hpp:293-328 (ctor), 683-694 (Chebyshev nodes),
+// 833-941 (createTreeU / createUniformTree), 1150-1163 (leaf charge
+// locations), 1952-1974 (createCones).
+bool Oracle::build(char* err, int errlen) {
+  kappa = cfg.kappa;
+  L = cfg.L;
+  const int n1 = cfg.nChebNodes;
+  rank = n1 * n1;
+  nb = cfg.degreeOfBases * (cfg.degreeOfBases + 1) / 2;
+  if (cfg.nLevelsUniform < 2 || cfg.nLevelsUniform > 10) {
+    std::snprintf(err, errlen, "nLevelsUniform must be in [2, 10]");
+    return false;
+  }
+  if (cfg.yes2DFMM == 1) {
+    if (kappa == 0) level_LFR = 2;
+    else level_LFR = (int)std::floor(std::log(kappa * L / 0.35) / std::log(2.0));
+    if (level_LFR < 2) level_LFR = 2;
+  } else {
+    level_LFR = 2;
+  }
+  for (int k = 0; k < n1; ++k) cheb1d.push_back(-std::cos((k + 0.5) / n1 * PI));
+  for (int j = 0; j < n1; ++j)
+    for (int k = 0; k < n1; ++k) chebStd.push_back({cheb1d[k], cheb1d[j]});
+  nL = cfg.nLevelsUniform;
+  boxRadius.push_back(L);
+  for (int j = 1; j <= 10; ++j) boxRadius.push_back(boxRadius[j - 1] / 2.0);
+  if (level_LFR >= nL) level_LFR = nL - 1;
+  // Uniform tree: in the reference's depth-first construction the box
+  // index at each level equals its boxNumber (4 * parent + child).
+  tree.resize(nL + 1);
+  tree[0].resize(1);
+  tree[0][0].cx = 0.0; tree[0][0].cy = 0.0; tree[0][0].r = L;
+  for (int j = 0; j < nL; ++j) {
+    tree[j + 1].resize(tree[j].size() * 4);
+    for (size_t k = 0; k < tree[j].size(); ++k) {
+      const Box& P = tree[j][k];
+      for (int c = 0; c < 4; ++c) {
+        Box& B = tree[j + 1][4 * k + c];
+        B.r = 0.5 * P.r;
+        const double h = 0.5 * P.r;
+        B.cx = (c == 0 || c == 3) ? P.cx - h : P.cx + h;
+        B.cy = (c == 0 || c == 1) ? P.cy - h : P.cy + h;
+      }
+    }
+  }
+  for (auto& B : tree[nL]) B.leaf = true;
+  // Cones (createCones).
+  nCones.push_back((int)(cfg.nCones_LFR * std::pow(2.0, level_LFR - 1)));
+  ConeAperture.push_back(2 * PI / nCones[0]);
+  for (int j = 1; j <= level_LFR - 1; ++j) {
+    nCones.push_back((int)(nCones[j - 1] / 2.0));
+    ConeAperture.push_back(ConeAperture[j - 1] * 2.0);
+  }
+  for (int j = 0; j <= level_LFR - 1; ++j)
+    for (auto& B : tree[j]) B.cones.assign(nCones[j], Node());
+  // Leaf charge locations: DFS leaf order, node index row * n1 + col.
+  for (size_t k = 0; k < tree[nL].size(); ++k) {
+    Box& B = tree[nL][k];
+    const int start = (int)grid.size();
+    for (int i = 0; i < rank; ++i) B.chargeLoc.push_back(start + i);
+    for (int i = 0; i < rank; ++i)
+      grid.push_back({boxRadius[nL] * chebStd[i].x + B.cx, boxRadius[nL] * chebStd[i].y + B.cy});
+  }
+  N = (int)grid.size();
+  for (int d = 0; d < cfg.degreeOfBases; ++d)
+    for (int a = 0; a < d + 1; ++a) bases.push_back({a, d - a});
+  gauss_legendre(10, gln, glw);
+  return true;
+}
+
+// Q and its pseudo-inverse (FarFieldInteraction.hpp:138-150), far-field
+// moments C and M = C Q^+ (FarFieldInteraction.hpp:115-160), colleague
+// near blocks V (i r^2 / 4) Q^+ (NearFieldInteraction1.hpp:260-290,
+// G_FMM2DTree.hpp:1773-1805, 1815-1830). Only the leaf level of a uniform
+// tree is read by the matvec, so only that level is computed.
+void Oracle::precompute() {
+  // Q (rank x nb) and Q^+ via Householder QR of the full-column-rank Q.
+  CMat Q(rank, nb);
+  for (int i = 0; i < rank; ++i)
+    for (int l = 0; l < nb; ++l)
+      Q(i, l) = cd(chebT(chebStd[i].x, bases[l].x) * chebT(chebStd[i].y, bases[l].y), 0.0);
+  ColPivQR qr;
+  qr.compute(Q);
+  Qpinv.assign((size_t)nb * rank, 0.0);
+  std::vector<cd> e(rank), xs(nb);
+  for (int i = 0; i < rank; ++i) {
+    std::fill(e.begin(), e.end(), cd(0.0, 0.0));
+    e[i] = cd(1.0, 0.0);
+    qr.solve(e.data(), xs.data());
+    for (int l = 0; l < nb; ++l) Qpinv[(size_t)l * rank + i] = xs[l].real();
+  }
+  const double eps = 1e-7;
+  // Far-field moments at the leaf level.
+  const int nS = 2 * S + 1;
+  CMat C(nS, nb);
+  const double rj = boxRadius[nL];
+  {
+    std::vector<std::pair<int, int>> jobs;
+    for (int n = -S; n <= S; ++n)
+      for (int l = 0; l < nb; ++l) jobs.push_back({n, l});
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < (int)jobs.size(); ++t) {
+      const int n = jobs[t].first, l = jobs[t].second;
+      const int a = bases[l].x, b = bases[l].y;
+      auto f = [&](double px, double py) -> cd {
+        const double R2 = px * px + py * py;
+        const double normX = std::sqrt(R2);
+        const double argJ = kappa * rj * normX;
+        const double th = std::atan2(py, px);
+        return besselJ(n, argJ) * std::exp(-I * double(n) * th) * chebT(px, a) * chebT(py, b);
+      };
+      cd integral = adaptive_quad(f, gln, glw, eps);
+      C(n + S, l) = rj * rj * integral;
+    }
+  }
+  Mleaf = CMat(nS, rank);
+  for (int n = 0; n < nS; ++n)
+    for (int i = 0; i < rank; ++i) {
+      cd s(0.0, 0.0);
+      for (int l = 0; l < nb; ++l) s += C(n, l) * Qpinv[(size_t)l * rank + i];
+      Mleaf(n, i) = cfg.reference_rounding ? round6(s) : s;
+    }
+  // Colleague near blocks at the leaf level.
+  static const Pt Ncen[9] = {{-2, -2}, {0, -2}, {2, -2}, {2, 0}, {2, 2}, {0, 2}, {-2, 2}, {-2, 0}, {0, 0}};
+  const double rA = boxRadius[nL], rB = boxRadius[nL];
+  std::vector<CMat> V(9, CMat(rank, nb));
+  {
+    std::vector<std::pair<int, int>> jobs;
+    for (int q = 0; q < 9; ++q)
+      for (int i = 0; i < rank; ++i) jobs.push_back({q, i});
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < (int)jobs.size(); ++t) {
+      const int q = jobs[t].first, i = jobs[t].second;
+      const double cBx = Ncen[q].x * rA, cBy = Ncen[q].y * rA;
+      const double Ax = rA * chebStd[i].x + 0.0, Ay = rA * chebStd[i].y + 0.0;
+      const double Xx = (Ax - cBx) / rB, Xy = (Ay - cBy) / rB;
+      // H0 values cached per quadrature point; all bases reuse them.
+      std::unordered_map<unsigned long long, cd> h0;
+      auto key = [](double a, double b) {
+        unsigned long long ka, kb;
+        std::memcpy(&ka, &a, 8); std::memcpy(&kb, &b, 8);
+        return ka * 0x9E3779B97F4A7C15ULL ^ (kb + 0x632BE59BD9B4E019ULL + (ka << 6) + (ka >> 2));
+      };
+      for (int l = 0; l < nb; ++l) {
+        const int a = bases[l].x, b = bases[l].y;
+        auto f = [&](double px, double py) -> cd {
+          unsigned long long k = key(px, py);
+          auto it = h0.find(k);
+          cd H;
+          if (it != h0.end()) H = it->second;
+          else {
+            const double R2 = (Xx - px) * (Xx - px) + (Xy - py) * (Xy - py);
+            const double R = std::sqrt(R2);
+            const double arg = kappa * rB * R;
+            H = besselJ(0, arg) + I * besselY(0, arg);
+            h0.emplace(k, H);
+          }
+          return H * chebT(px, a) * chebT(py, b);
+        };
+        V[q](i, l) = adaptive_quad(f, gln, glw, eps);
+      }
+    }
+  }
+  for (int q = 0; q < 9; ++q) {
+    CMat Vt(rank, nb);
+    for (int i = 0; i < rank; ++i)
+      for (int l = 0; l < nb; ++l) Vt(i, l) = V[q](i, l) * I * rB * rB / 4.0;
+    nearB[q] = CMat(rank, rank);
+    for (int i = 0; i < rank; ++i)
+      for (int k = 0; k < rank; ++k) {
+        cd s(0.0, 0.0);
+        for (int l = 0; l < nb; ++l) s += Vt(i, l) * Qpinv[(size_t)l * rank + k];
+        nearB[q](i, k) = cfg.reference_rounding ? round6(s) : s;
+      }
+  }
+}
+
+// assign_Tree_Interactions (GMRES/G_FMM2DTree.hpp:1356-1498) for a uniform
+// tree, and the colleague table of getNeighbors (:1500-1601).
+void Oracle::interactions() {
+  const double epsR = std::pow(10, -8);  // epsilonRoundOff, :116
+  for (int c = 0; c < 4; ++c)
+    for (int n = 0; n < 4; ++n) tree[1][c].nbrs.push_back({1, n});
+  for (int j = 1; j <= nL - 1; ++j) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      for (int c = 0; c < 4; ++c) {
+        const int A = 4 * k + c;
+        Box& BA = tree[j + 1][A];
+        const Box& P = tree[j][k];
+        for (size_t n = 0; n < P.nbrs.size(); ++n) {
+          const int pnj = P.nbrs[n].x, pni = P.nbrs[n].y;
+          for (int nc = 0; nc < 4; ++nc) {
+            const int Bk = 4 * pni + nc;
+            const Box& BB = tree[pnj + 1][Bk];
+            const double dx = std::fabs(BA.cx - BB.cx), dy = std::fabs(BA.cy - BB.cy);
+            if (j + 1 >= level_LFR) {
+              const double lim = 3.0 * boxRadius[j + 1] + boxRadius[pnj + 1] - epsR;
+              if (dx >= lim || dy >= lim) BA.lfr.IL.push_back({pnj + 1, Bk});
+              else BA.nbrs.push_back({pnj + 1, Bk});
+            } else {
+              // HFR criterion, with the reference's y-test that omits the
+              // target radius (:1441-1442).
+              const double limx = kappa * boxRadius[j + 1] * boxRadius[j + 1] + boxRadius[j + 1] + boxRadius[pnj + 1] - epsR;
+              const double limy = kappa * boxRadius[j + 1] * boxRadius[j + 1] + boxRadius[pnj + 1] - epsR;
+              if (dx >= limx || dy >= limy) {
+                double arg = std::atan2(BA.cy - BB.cy, BA.cx - BB.cx);
+                arg = std::fmod(arg + 2 * PI + PI, 2 * PI);
+                const int cone = int(arg / ConeAperture[j + 1]);
+                BA.cones[cone].IL.push_back({pnj + 1, Bk});
+              } else {
+                BA.nbrs.push_back({pnj + 1, Bk});
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  // Colleague table at the leaf level.
+  double Nang[9];
+  static const Pt Ncen[9] = {{-2, -2}, {0, -2}, {2, -2}, {2, 0}, {2, 2}, {0, 2}, {-2, 2}, {-2, 0}, {0, 0}};
+  for (int i = 0; i < 9; ++i) Nang[i] = std::atan2(Ncen[i].y, Ncen[i].x);
+  for (auto& B : tree[nL]) {
+    for (int q = 0; q < 9; ++q) B.colleague[q] = -1;
+    for (const Pair& p : B.nbrs) {
+      const Box& O = tree[p.x][p.y];
+      const double ang = std::atan2(O.cy - B.cy, O.cx - B.cx);
+      if (std::fabs(O.cy - B.cy) < epsR && std::fabs(O.cx - B.cx) < epsR) { B.colleague[8] = p.y; continue; }
+      for (int q = 0; q < 8; ++q)
+        if (std::fabs(Nang[q] - ang) < epsR) { B.colleague[q] = p.y; break; }
+    }
+  }
+}
+
+// getNodes_LFR (:2062-2385) and getNodes_HFR (:3232-3571).
+void Oracle::nca() {
+  const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
+  for (int j = nL; j >= level_LFR; --j) {
+    // outgoing
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Box& B = tree[j][k];
+      HCache hc{this, {}};
+      std::vector<int> boxA;
+      if (B.leaf) boxA = B.chargeLoc;
+      else for (int c = 0; c < 4; ++c) { const Node& ch = tree[j + 1][4 * k + c].lfr; boxA.insert(boxA.end(), ch.out_charge.begin(), ch.out_charge.end()); }
+      std::vector<int> ILn;
+      for (const Pair& p : B.lfr.IL) {
+        const Box& O = tree[p.x][p.y];
+        if (O.leaf) ILn.insert(ILn.end(), O.chargeLoc.begin(), O.chargeLoc.end());
+        else for (int c = 0; c < 4; ++c) { const Node& ch = tree[p.x + 1][4 * p.y + c].lfr; ILn.insert(ILn.end(), ch.in_check.begin(), ch.in_check.end()); }
+      }
+      Node& nd = B.lfr;
+      if (!ILn.empty() && !boxA.empty()) {
+        nd.out_active = true;
+        std::vector<int> rb, cb;
+        const int rk = aca(ILn, boxA, tol, rb, cb, &nd.out_Ar, hc);
+        if (rk > 0) {
+          for (int r : rb) nd.out_check.push_back(ILn[r]);
+          for (int c : cb) nd.out_charge.push_back(boxA[c]);
+          nd.out_A.compute(getMatrix(nd.out_check, nd.out_charge, hc));
+        }
+      } else {
+        nd.out_active = false;
+        nd.out_charge = boxA;
+      }
+    }
+    // incoming
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Box& B = tree[j][k];
+      HCache hc{this, {}};
+      std::vector<int> boxA;
+      if (B.leaf) boxA = B.chargeLoc;
+      else for (int c = 0; c < 4; ++c) { const Node& ch = tree[j + 1][4 * k + c].lfr; boxA.insert(boxA.end(), ch.in_check.begin(), ch.in_check.end()); }
+      std::vector<int> ILn;
+      for (const Pair& p : B.lfr.IL) {
+        const Box& O = tree[p.x][p.y];
+        if (O.leaf) ILn.insert(ILn.end(), O.chargeLoc.begin(), O.chargeLoc.end());
+        else for (int c = 0; c < 4; ++c) { const Node& ch = tree[p.x + 1][4 * p.y + c].lfr; ILn.insert(ILn.end(), ch.out_charge.begin(), ch.out_charge.end()); }
+      }
+      Node& nd = B.lfr;
+      if (!ILn.empty() && !boxA.empty()) {
+        nd.in_active = true;
+        std::vector<int> rb, cb;
+        const int rk = aca(boxA, ILn, tol, rb, cb, nullptr, hc);
+        if (rk > 0) {
+          for (int r : rb) nd.in_check.push_back(boxA[r]);
+          for (int c : cb) nd.in_charge.push_back(ILn[c]);
+          if (!B.leaf) nd.in_A.compute(getMatrix(nd.in_check, nd.in_charge, hc));
+        }
+      } else {
+        nd.in_active = false;
+        nd.in_check = boxA;
+      }
+    }
+  }
+  for (int j = level_LFR - 1; j >= 2; --j) {
+    const int nc_ = nCones[j];
+    // Cone of IL box O pointing towards box B (:3335-3337).
+    auto coneOf = [&](const Box& B, const Pair& p) {
+      const Box& O = tree[p.x][p.y];
+      double arg = std::atan2(B.cy - O.cy, B.cx - O.cx);
+      double argB = std::fmod(arg + 2 * PI, 2 * PI);
+      return int(argB / ConeAperture[p.x]);
+    };
+    // children's nodes for cone `cone` (LFR children at level_LFR, else child cone cone/2)
+    auto childOut = [&](int jj, int kk, int cone, std::vector<int>& dst, bool charge) {
+      for (int c = 0; c < 4; ++c) {
+        const Box& ch = tree[jj + 1][4 * kk + c];
+        const Node& n = (jj == level_LFR - 1) ? ch.lfr : ch.cones[cone / 2];
+        const std::vector<int>& v = charge ? n.out_charge : n.in_check;
+        dst.insert(dst.end(), v.begin(), v.end());
+      }
+    };
+    auto childIn = [&](int jj, int kk, int cone, std::vector<int>& dst, bool charge) {
+      for (int c = 0; c < 4; ++c) {
+        const Box& ch = tree[jj + 1][4 * kk + c];
+        const Node& n = (jj == level_LFR - 1) ? ch.lfr : ch.cones[cone / 2];
+        const std::vector<int>& v = charge ? n.out_charge : n.in_check;
+        dst.insert(dst.end(), v.begin(), v.end());
+      }
+    };
+    // outgoing (:3322-3392)
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < (int)tree[j].size() * nc_; ++t) {
+      const int k = t / nc_, cone = t % nc_;
+      Box& B = tree[j][k];
+      HCache hc{this, {}};
+      std::vector<int> boxA, ILn;
+      childOut(j, k, cone, boxA, true);
+      for (const Pair& p : B.cones[cone].IL) {
+        const int coneB = coneOf(B, p);
+        childOut(p.x, p.y, coneB, ILn, false);
+      }
+      Node& nd = B.cones[cone];
+      if (!ILn.empty() && !boxA.empty()) {
+        nd.out_active = true;
+        std::vector<int> rb, cb;
+        const int rk = aca(ILn, boxA, tol, rb, cb, &nd.out_Ar, hc);
+        if (rk > 0) {
+          for (int r : rb) nd.out_check.push_back(ILn[r]);
+          for (int c : cb) nd.out_charge.push_back(boxA[c]);
+          nd.out_A.compute(getMatrix(nd.out_check, nd.out_charge, hc));
+        }
+      } else {
+        nd.out_active = false;
+        nd.out_charge = boxA;
+      }
+    }
+    // incoming (:3485-3546)
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < (int)tree[j].size() * nc_; ++t) {
+      const int k = t / nc_, cone = t % nc_;
+      Box& B = tree[j][k];
+      HCache hc{this, {}};
+      std::vector<int> boxA, ILn;
+      childIn(j, k, cone, boxA, false);
+      for (const Pair& p : B.cones[cone].IL) {
+        const int coneB = coneOf(B, p);
+        childIn(p.x, p.y, coneB, ILn, true);
+      }
+      Node& nd = B.cones[cone];
+      if (!ILn.empty() && !boxA.empty()) {
+        nd.in_active = true;
+        std::vector<int> rb, cb;
+        const int rk = aca(boxA, ILn, tol, rb, cb, nullptr, hc);
+        if (rk > 0) {
+          for (int r : rb) nd.in_check.push_back(boxA[r]);
+          for (int c : cb) nd.in_charge.push_back(ILn[c]);
+          nd.in_A.compute(getMatrix(nd.in_check, nd.in_charge, hc));
+        }
+      } else {
+        nd.in_active = false;
+        nd.in_check = boxA;
+      }
+    }
+  }
+}
+
+// getUserCheckPoints (:3146-3230).
+void Oracle::user_checks() {
+  for (int j = nL; j >= level_LFR; --j)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Box& B = tree[j][k];
+      if (B.leaf) B.lfr.user_check = B.chargeLoc;
+      else if (B.lfr.in_active) B.lfr.user_check = B.lfr.in_check;
+      else for (int c = 0; c < 4; ++c) { const auto& v = tree[j + 1][4 * k + c].lfr.user_check; B.lfr.user_check.insert(B.lfr.user_check.end(), v.begin(), v.end()); }
+    }
+  for (int j = level_LFR - 1; j >= 2; --j)
+    for (int k = 0; k < (int)tree[j].size(); ++k)
+      for (int cone = 0; cone < nCones[j]; ++cone) {
+        Node& nd = tree[j][k].cones[cone];
+        if (nd.in_active) nd.user_check = nd.in_check;
+        else for (int c = 0; c < 4; ++c) {
+          const Box& ch = tree[j + 1][4 * k + c];
+          const auto& v = (j + 1 == level_LFR) ? ch.lfr.user_check : ch.cones[cone / 2].user_check;
+          nd.user_check.insert(nd.user_check.end(), v.begin(), v.end());
+        }
+      }
+}
+
+// Assemble_HFR_M2M :3573-3622/:3804, Assemble_HFR_M2L :3829, Assemble_LFR_M2L
+// :2502, Assemble_LFR_L2L :2653/:2824, Assemble_HFR_L2L :3944/:4183.
+void Oracle::assemble() {
+  auto coneTo = [&](const Box& B, const Pair& p) {  // cone of source p pointing at B (:2524-2526)
+    const Box& O = tree[p.x][p.y];
+    double arg = std::atan2(B.cy - O.cy, B.cx - O.cx);
+    double argA = std::fmod(arg + 2 * PI, 2 * PI);
+    return int(argA / ConeAperture[p.x]);
+  };
+  // HFR M2M blocks
+  for (int j = level_LFR - 1; j >= 2; --j) {
+    const int nc_ = nCones[j];
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < (int)tree[j].size() * nc_; ++t) {
+      const int k = t / nc_, cone = t % nc_;
+      Node& nd = tree[j][k].cones[cone];
+      if (!nd.out_active) continue;
+      HCache hc{this, {}};
+      std::vector<int> src;
+      for (int c = 0; c < 4; ++c) {
+        const Box& ch = tree[j + 1][4 * k + c];
+        const Node& n = (j == level_LFR - 1) ? ch.lfr : ch.cones[cone / 2];
+        src.insert(src.end(), n.out_charge.begin(), n.out_charge.end());
+      }
+      if (!nd.out_check.empty() && !src.empty()) nd.M2M = getMatrix(nd.out_check, src, hc);
+    }
+  }
+  // HFR M2L blocks
+  for (int j = 2; j < level_LFR; ++j) {
+    const int nc_ = nCones[j];
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < (int)tree[j].size() * nc_; ++t) {
+      const int k = t / nc_, cone = t % nc_;
+      Box& B = tree[j][k];
+      Node& nd = B.cones[cone];
+      if (!nd.in_active) continue;
+      HCache hc{this, {}};
+      for (const Pair& p : nd.IL) {
+        const int cA = coneTo(B, p);
+        nd.M2L.push_back(getMatrix(nd.user_check, tree[p.x][p.y].cones[cA].out_charge, hc));
+      }
+    }
+  }
+  // LFR M2L blocks
+  for (int j = level_LFR; j <= nL; ++j) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Box& B = tree[j][k];
+      if (!B.lfr.in_active) continue;
+      HCache hc{this, {}};
+      const std::vector<int>& rows = B.leaf ? B.chargeLoc : B.lfr.user_check;
+      for (const Pair& p : B.lfr.IL) B.lfr.M2L.push_back(getMatrix(rows, tree[p.x][p.y].lfr.out_charge, hc));
+    }
+  }
+  // LFR L2L blocks (children of IL-active parents)
+  for (int j = level_LFR; j < nL; ++j) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Box& B = tree[j][k];
+      if (!B.lfr.in_active) continue;
+      HCache hc{this, {}};
+      for (int c = 0; c < 4; ++c) {
+        Box& ch = tree[j + 1][4 * k + c];
+        const std::vector<int>& rows = ch.leaf ? ch.chargeLoc : ch.lfr.user_check;
+        ch.L2L = getMatrix(rows, B.lfr.in_charge, hc);
+      }
+    }
+  }
+  // HFR L2L blocks
+  for (int j = 2; j < level_LFR; ++j) {
+    const int nc_ = nCones[j];
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < (int)tree[j].size() * nc_; ++t) {
+      const int k = t / nc_, cone = t % nc_;
+      Node& nd = tree[j][k].cones[cone];
+      if (!nd.in_active) continue;
+      HCache hc{this, {}};
+      for (int c = 0; c < 4; ++c) {
+        const Box& ch = tree[j + 1][4 * k + c];
+        const std::vector<int>& rows = (j == level_LFR - 1) ? ch.lfr.user_check : ch.cones[cone / 2].user_check;
+        if (!rows.empty() && !nd.in_charge.empty()) nd.L2Lc[c] = getMatrix(rows, nd.in_charge, hc);
+      }
+    }
+  }
+}
+
+// DFMM::MatVecProduct, GMRES/GMRES.cpp:201-254, i.e. the phases
+// assignLeafCharges :1139, LFR_M2M :2472, HFR_M2M :3772, LFR_M2L :2577,
+// HFR_M2L :3882, HFR_L2L :4208, LFR_L2L :2800,
+// evaluate_NearField_Using_Precomputations_LS :2884, collectPotential :3045.
+// (assign_NonLeaf_Charges :1976 only feeds near fields of non-leaf
+// neighbours, which a uniform tree does not have.)
+void Oracle::matvec(const cd* x, cd* y) {
+  for (int k = 0; k < (int)tree[nL].size(); ++k)
+    tree[nL][k].multipoles.assign(x + (size_t)k * rank, x + (size_t)(k + 1) * rank);
+  // LFR_M2M
+  for (int j = nL; j >= level_LFR; --j) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Box& B = tree[j][k];
+      Node& nd = B.lfr;
+      std::vector<cd> src;
+      if (B.leaf) src = B.multipoles;
+      else for (int c = 0; c < 4; ++c) { const auto& v = tree[j + 1][4 * k + c].lfr.out_charges; src.insert(src.end(), v.begin(), v.end()); }
+      if (nd.out_active) {
+        if (!nd.out_charge.empty()) {
+          std::vector<cd> u(nd.out_Ar.r, cd(0.0, 0.0));
+          gemv_acc(nd.out_Ar, src.data(), u.data());
+          nd.out_charges.assign(nd.out_Ar.r, cd(0.0, 0.0));
+          nd.out_A.solve(u.data(), nd.out_charges.data());
+        }
+      } else {
+        nd.out_charges = src;
+      }
+    }
+  }
+  // HFR_M2M
+  for (int j = level_LFR - 1; j >= 2; --j) {
+    const int nc_ = nCones[j];
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int t = 0; t < (int)tree[j].size() * nc_; ++t) {
+      const int k = t / nc_, cone = t % nc_;
+      Node& nd = tree[j][k].cones[cone];
+      std::vector<cd> src;
+      for (int c = 0; c < 4; ++c) {
+        const Box& ch = tree[j + 1][4 * k + c];
+        const auto& v = (j == level_LFR - 1) ? ch.lfr.out_charges : ch.cones[cone / 2].out_charges;
+        src.insert(src.end(), v.begin(), v.end());
+      }
+      if (nd.out_active) {
+        if (!nd.out_charge.empty() && !nd.out_check.empty() && !src.empty()) {
+          std::vector<cd> u(nd.M2M.r, cd(0.0, 0.0));
+          gemv_acc(nd.M2M, src.data(), u.data());
+          nd.out_charges.assign(nd.M2M.r, cd(0.0, 0.0));
+          nd.out_A.solve(u.data(), nd.out_charges.data());
+        }
+      } else {
+        nd.out_charges = src;
+      }
+    }
+  }
+  auto coneTo = [&](const Box& B, const Pair& p) {
+    const Box& O = tree[p.x][p.y];
+    double arg = std::atan2(B.cy - O.cy, B.cx - O.cx);
+    double argA = std::fmod(arg + 2 * PI, 2 * PI);
+    return int(argA / ConeAperture[p.x]);
+  };
+  // LFR_M2L
+  for (int j = level_LFR; j <= nL; ++j) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Box& B = tree[j][k];
+      Node& nd = B.lfr;
+      const int nrow = B.leaf ? rank : (int)nd.user_check.size();
+      nd.in_potential.assign(nrow, cd(0.0, 0.0));
+      if (!nd.in_active) continue;
+      for (size_t l = 0; l < nd.IL.size(); ++l) {
+        const Node& src = tree[nd.IL[l].x][nd.IL[l].y].lfr;
+        if (nd.M2L[l].c > 0 && nd.M2L[l].r > 0 && (int)src.out_charges.size() == nd.M2L[l].c)
+          gemv_acc(nd.M2L[l], src.out_charges.data(), nd.in_potential.data());
+      }
+    }
+  }
+  // HFR_M2L
+  for (int j = 2; j < level_LFR; ++j) {
+    const int nc_ = nCones[j];
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int t = 0; t < (int)tree[j].size() * nc_; ++t) {
+      const int k = t / nc_, cone = t % nc_;
+      Box& B = tree[j][k];
+      Node& nd = B.cones[cone];
+      nd.in_potential.assign(nd.user_check.size(), cd(0.0, 0.0));
+      if (!nd.in_active) continue;
+      for (size_t l = 0; l < nd.IL.size(); ++l) {
+        const int cA = coneTo(B, nd.IL[l]);
+        const Node& src = tree[nd.IL[l].x][nd.IL[l].y].cones[cA];
+        if (nd.M2L[l].r != 0 && nd.M2L[l].c != 0 && !src.out_charges.empty())
+          gemv_acc(nd.M2L[l], src.out_charges.data(), nd.in_potential.data());
+      }
+    }
+  }
+  // HFR_L2L (top down)
+  for (int j = 2; j < level_LFR; ++j) {
+    const int nc_ = nCones[j];
+    // Parent cones 2c, 2c+1 feed the same child cone; apply serially per box
+    // so that no two threads update one child.
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      for (int cone = 0; cone < nc_; ++cone) {
+        Node& nd = tree[j][k].cones[cone];
+        if (nd.in_active) {
+          if (nd.in_charge.empty()) continue;
+          nd.in_charges.assign(nd.in_charge.size(), cd(0.0, 0.0));
+          nd.in_A.solve(nd.in_potential.data(), nd.in_charges.data());
+          for (int c = 0; c < 4; ++c) {
+            Box& ch = tree[j + 1][4 * k + c];
+            std::vector<cd>& pot = (j == level_LFR - 1) ? ch.lfr.in_potential : ch.cones[cone / 2].in_potential;
+            const CMat& W = nd.L2Lc[c];
+            if (W.r != 0 && W.c != 0) gemv_acc(W, nd.in_charges.data(), pot.data());
+          }
+        } else {
+          int off = 0;
+          for (int c = 0; c < 4; ++c) {
+            Box& ch = tree[j + 1][4 * k + c];
+            std::vector<cd>& pot = (j == level_LFR - 1) ? ch.lfr.in_potential : ch.cones[cone / 2].in_potential;
+            const int len = (j == level_LFR - 1) ? (int)ch.lfr.user_check.size() : (int)ch.cones[cone / 2].user_check.size();
+            for (int i = 0; i < len; ++i) pot[i] += nd.in_potential[off + i];
+            off += len;
+          }
+        }
+      }
+    }
+  }
+  // LFR_L2L (top down)
+  for (int j = level_LFR; j < nL; ++j) {
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      Node& nd = tree[j][k].lfr;
+      if (nd.in_active) {
+        if (nd.in_charge.empty()) continue;
+        nd.in_charges.assign(nd.in_charge.size(), cd(0.0, 0.0));
+        nd.in_A.solve(nd.in_potential.data(), nd.in_charges.data());
+        for (int c = 0; c < 4; ++c) {
+          Box& ch = tree[j + 1][4 * k + c];
+          gemv_acc(ch.L2L, nd.in_charges.data(), ch.lfr.in_potential.data());
+        }
+      } else {
+        int off = 0;
+        for (int c = 0; c < 4; ++c) {
+          Box& ch = tree[j + 1][4 * k + c];
+          const int len = ch.leaf ? rank : (int)ch.lfr.user_check.size();
+          for (int i = 0; i < len; ++i) ch.lfr.in_potential[i] += nd.in_potential[off + i];
+          off += len;
+        }
+      }
+    }
+  }
+  // Near field (colleagues only in a uniform tree)
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < (int)tree[nL].size(); ++k) {
+    Box& B = tree[nL][k];
+    std::vector<double> cv(rank);
+    for (int i = 0; i < rank; ++i) cv[i] = kappa * kappa * (contrast(grid[B.chargeLoc[i]]));
+    CMat op(rank, rank);
+    for (int q = 0; q < 9; ++q) {
+      const int nk = B.colleague[q];
+      if (nk == -1) continue;
+      if (cfg.findPhi) {
+        for (int c = 0; c < rank; ++c)
+          for (int i = 0; i < rank; ++i) op(i, c) = cv[i] * nearB[q](i, c);
+        if (q == 8) for (int i = 0; i < rank; ++i) op(i, i) += 1.0;
+        gemv_acc(op, tree[nL][nk].multipoles.data(), B.lfr.in_potential.data());
+      } else {
+        gemv_acc(nearB[q], tree[nL][nk].multipoles.data(), B.lfr.in_potential.data());
+      }
+    }
+  }
+  for (int k = 0; k < (int)tree[nL].size(); ++k)
+    for (int i = 0; i < rank; ++i) y[(size_t)k * rank + i] = tree[nL][k].lfr.in_potential[i];
+}
+
+// Dense operator A(i,j) = getMatrixEntry2(i,j) (GMRES/G_FMM2DTree.hpp:518-601)
+// applied to x. For a uniform tree two leaves are neighbours exactly when
+// they are colleagues (getIfNeighbor :335-346).
+void Oracle::dense_matvec(const cd* x, cd* y) {
+  const int nLeaf = (int)tree[nL].size();
+  const double epsR = std::pow(10, -8);
+  const int nS = 2 * S + 1;
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int i = 0; i < N; ++i) {
+    const int li = i / rank, ii = i % rank;
+    const Box& Bi = tree[nL][li];
+    const double qi = contrast(grid[i]);
+    std::vector<cd> h(nS);
+    cd acc(0.0, 0.0);
+    for (int lj = 0; lj < nLeaf; ++lj) {
+      const Box& Bj = tree[nL][lj];
+      const double dxa = std::fabs(Bi.cx - Bj.cx), dya = std::fabs(Bi.cy - Bj.cy);
+      const double lim = 3.0 * boxRadius[nL] + boxRadius[nL] - epsR;
+      if (!(dxa >= lim || dya >= lim)) {
+        int q = -1;
+        for (int t = 0; t < 9; ++t) if (Bi.colleague[t] == lj) q = t;
+        for (int jj = 0; jj < rank; ++jj) {
+          const int j = lj * rank + jj;
+          cd e = nearB[q](ii, jj);
+          if (cfg.findPhi) {
+            e = e * kappa * kappa * qi;
+            if (i == j) e = 1.0 + e;
+          }
+          acc += e * x[j];
+        }
+      } else {
+        const Pt ri = grid[i];
+        const double th = std::atan2(ri.y - Bj.cy, ri.x - Bj.cx);
+        const double R2 = (ri.y - Bj.cy) * (ri.y - Bj.cy) + (ri.x - Bj.cx) * (ri.x - Bj.cx);
+        const double R = kappa * std::sqrt(R2);
+        for (int n = -S; n <= S; ++n)
+          h[n + S] = (besselJ(n, R) + I * besselY(n, R)) * std::exp(I * double(n) * th);
+        for (int jj = 0; jj < rank; ++jj) {
+          const int j = lj * rank + jj;
+          cd s = 0.0 + 0.0 * I;
+          for (int n = -S; n <= S; ++n) s += Mleaf(n + S, jj) * h[n + S];
+          s *= I / 4.0;
+          if (cfg.findPhi) {
+            s *= kappa * kappa * qi;
+            if (i == j) s += 1.0;
+          }
+          acc += s * x[j];
+        }
+      }
+    }
+    y[i] = acc;
+  }
+}
+
+}  // namespace ora
+
+// ---------------------------------------------------------------------------
+// C interface.
+using namespace ora;
+
+extern "C" {
+
+void* ora_create(const ora_cfg* cfg, char* err, int errlen) {
+  Oracle* o = new Oracle();
+  o->cfg = *cfg;
+  if (err && errlen > 0) err[0] = 0;
+  char dummy[8];
+  if (!err) { err = dummy; errlen = sizeof dummy; }
+  if (!o->build(err, errlen)) { delete o; return nullptr; }
+  o->precompute();
+  o->interactions();
+  o->nca();
+  o->user_checks();
+  o->assemble();
+  return o;
+}
+void ora_destroy(void* h) { delete (Oracle*)h; }
+int ora_N(void* h) { return ((Oracle*)h)->N; }
+int ora_nlevels(void* h) { return ((Oracle*)h)->nL; }
+int ora_level_lfr(void* h) { return ((Oracle*)h)->level_LFR; }
+int ora_rank(void* h) { return ((Oracle*)h)->rank; }
+void ora_points(void* h, double* xy) {
+  Oracle* o = (Oracle*)h;
+  for (int i = 0; i < o->N; ++i) { xy[2 * i] = o->grid[i].x; xy[2 * i + 1] = o->grid[i].y; }
+}
+void ora_contrast(void* h, double* q) {
+  Oracle* o = (Oracle*)h;
+  for (int i = 0; i < o->N; ++i) q[i] = o->contrast(o->grid[i]);
+}
+// RHSFunction, GMRES/GMRES.cpp:118-125, 361-364: b = -k^2 q(x) exp(i k x1).
+void ora_rhs(void* h, double* b) {
+  Oracle* o = (Oracle*)h;
+  for (int i = 0; i < o->N; ++i) {
+    const Pt r = o->grid[i];
+    cd inc = std::exp(I * o->kappa * r.x);
+    cd v = -1.0 * o->kappa * o->kappa * o->contrast(r) * inc;
+    b[2 * i] = v.real(); b[2 * i + 1] = v.imag();
+  }
+}
+void ora_get_M(void* h, double* M) {
+  Oracle* o = (Oracle*)h;
+  const int nS = 2 * o->S + 1;
+  for (int i = 0; i < o->rank; ++i)
+    for (int n = 0; n < nS; ++n) {
+      cd v = o->Mleaf(n, i);
+      M[2 * ((size_t)i * nS + n)] = v.real();
+      M[2 * ((size_t)i * nS + n) + 1] = v.imag();
+    }
+}
+void ora_get_near(void* h, double* B) {
+  Oracle* o = (Oracle*)h;
+  const int r = o->rank;
+  for (int q = 0; q < 9; ++q)
+    for (size_t t = 0; t < (size_t)r * r; ++t) {
+      B[2 * ((size_t)q * r * r + t)] = o->nearB[q].a[t].real();
+      B[2 * ((size_t)q * r * r + t) + 1] = o->nearB[q].a[t].imag();
+    }
+}
+// Flattened skeleton description, one record per node (level >= 2, box,
+// cone or -1): level, box, cone, out_active, in_active, then four counted
+// lists (out charge, out check, in charge, in check) and the counted
+// user-check list.
+long ora_skeleton_dump(void* h, int* buf, long cap) {
+  Oracle* o = (Oracle*)h;
+  long n = 0;
+  auto put = [&](int v) { if (n < cap && buf) buf[n] = v; ++n; };
+  auto putv = [&](const std::vector<int>& v) { put((int)v.size()); for (int x : v) put(x); };
+  for (int j = 2; j <= o->nL; ++j)
+    for (int k = 0; k < (int)o->tree[j].size(); ++k) {
+      const Box& B = o->tree[j][k];
+      if (j >= o->level_LFR) {
+        const Node& nd = B.lfr;
+        put(j); put(k); put(-1); put(nd.out_active); put(nd.in_active);
+        putv(nd.out_charge); putv(nd.out_check); putv(nd.in_charge); putv(nd.in_check); putv(nd.user_check);
+      } else {
+        for (int c = 0; c < o->nCones[j]; ++c) {
+          const Node& nd = B.cones[c];
+          put(j); put(k); put(c); put(nd.out_active); put(nd.in_active);
+          putv(nd.out_charge); putv(nd.out_check); putv(nd.in_charge); putv(nd.in_check); putv(nd.user_check);
+        }
+      }
+    }
+  return n;
+}
+void ora_matvec(void* h, const double* x, double* y) {
+  ((Oracle*)h)->matvec((const cd*)x, (cd*)y);
+}
+void ora_dense_matvec(void* h, const double* x, double* y) {
+  ((Oracle*)h)->dense_matvec((const cd*)x, (cd*)y);
+}
+
+// Tolerance-stopped GMRES with Givens rotations, classGMRES::gmres
+// (GMRES_Hybrid/include/gmres.hpp:6-119), written with the conjugate-linear
+// inner product h_i = q_i^H w and unitary complex rotations (the reference
+// conjugates h and uses a non-unitary rotation there). x0 = 0.
+int ora_gmres(void* h, const double* bd, int max_iter, double tol, double* xd, double* hist, int* iters) {
+  Oracle* o = (Oracle*)h;
+  const int N = o->N, m = max_iter;
+  const cd* b = (const cd*)bd;
+  cd* x = (cd*)xd;
+  std::vector<cd> r(b, b + N);
+  double bn = 0.0;
+  for (int i = 0; i < N; ++i) bn += std::norm(b[i]);
+  bn = std::sqrt(bn);
+  const double rn = bn;  // x0 = 0 so r = b
+  std::vector<std::vector<cd>> Q;
+  Q.push_back(std::vector<cd>(N));
+  for (int i = 0; i < N; ++i) Q[0][i] = r[i] / rn;
+  std::vector<std::vector<cd>> H;
+  std::vector<cd> cs(m), sn(m), beta(m + 1, cd(0.0, 0.0));
+  beta[0] = rn;
+  int K = m - 1, nh = 0;
+  if (hist) hist[nh++] = rn / bn;
+  std::vector<cd> w(N);
+  for (int k = 0; k < m; ++k) {
+    o->matvec(Q[k].data(), w.data());
+    std::vector<cd> hk(k + 2, cd(0.0, 0.0));
+    for (int i = 0; i <= k; ++i) {
+      cd s(0.0, 0.0);
+      for (int t = 0; t < N; ++t) s += std::conj(Q[i][t]) * w[t];
+      hk[i] = s;
+      for (int t = 0; t < N; ++t) w[t] -= s * Q[i][t];
+    }
+    double wn = 0.0;
+    for (int t = 0; t < N; ++t) wn += std::norm(w[t]);
+    wn = std::sqrt(wn);
+    hk[k + 1] = wn;
+    Q.push_back(std::vector<cd>(N));
+    for (int t = 0; t < N; ++t) Q[k + 1][t] = w[t] / wn;
+    for (int i = 0; i < k; ++i) {
+      cd t1 = std::conj(cs[i]) * hk[i] + std::conj(sn[i]) * hk[i + 1];
+      hk[i + 1] = -sn[i] * hk[i] + cs[i] * hk[i + 1];
+      hk[i] = t1;
+    }
+    const double nrm = std::sqrt(std::norm(hk[k]) + std::norm(hk[k + 1]));
+    cs[k] = hk[k] / nrm;
+    sn[k] = hk[k + 1] / nrm;
+    hk[k] = std::conj(cs[k]) * hk[k] + std::conj(sn[k]) * hk[k + 1];
+    hk[k + 1] = 0.0;
+    H.push_back(hk);
+    beta[k + 1] = -sn[k] * beta[k];
+    beta[k] = std::conj(cs[k]) * beta[k];
+    const double e = std::abs(beta[k + 1]) / bn;
+    if (hist) hist[nh++] = e;
+    if (e <= tol) { K = k; break; }
+  }
+  const int n = K + 1;
+  std::vector<cd> y(n);
+  for (int i = n - 1; i >= 0; --i) {
+    cd s = beta[i];
+    for (int j = i + 1; j < n; ++j) s -= H[j][i] * y[j];
+    y[i] = s / H[i][i];
+  }
+  for (int t = 0; t < N; ++t) x[t] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int t = 0; t < N; ++t) x[t] += Q[j][t] * y[j];
+  if (iters) *iters = n;
+  return 0;
+}
+
+// Fixed-m restarted GMRES, GMRES/GMRES.cpp:257-319: Arnoldi with modified
+// Gram-Schmidt, early exit when H(j+1,j) < 1e-8, least squares by
+// column-pivoted QR, x = x0 + V y, repeated `restarts` times.
+int ora_gmres_restarted(void* h, const double* bd, int m, int restarts, double* xd) {
+  Oracle* o = (Oracle*)h;
+  const int N = o->N;
+  const cd* b = (const cd*)bd;
+  cd* x = (cd*)xd;
+  std::vector<cd> x0(N, cd(0.0, 0.0)), out(N);
+  for (int rs = 0; rs < restarts; ++rs) {
+    int mm = m;
+    o->matvec(x0.data(), out.data());
+    std::vector<cd> r0(N);
+    for (int i = 0; i < N; ++i) r0[i] = b[i] - out[i];
+    double beta = 0.0;
+    for (int i = 0; i < N; ++i) beta += std::norm(r0[i]);
+    beta = std::sqrt(beta);
+    std::vector<std::vector<cd>> V(1, std::vector<cd>(N));
+    for (int i = 0; i < N; ++i) V[0][i] = r0[i] / beta;
+    CMat Hm(m + 1, m);
+    std::vector<cd> w(N);
+    for (int j = 0; j < m; ++j) {
+      o->matvec(V[j].data(), w.data());
+      for (int i = 0; i <= j; ++i) {
+        cd s(0.0, 0.0);
+        for (int t = 0; t < N; ++t) s += std::conj(V[i][t]) * w[t];
+        Hm(i, j) = s;
+        for (int t = 0; t < N; ++t) w[t] -= s * V[i][t];
+      }
+      double wn = 0.0;
+      for (int t = 0; t < N; ++t) wn += std::norm(w[t]);
+      Hm(j + 1, j) = std::sqrt(wn);
+      if (std::abs(Hm(j + 1, j)) < 1e-8) { mm = j + 1; break; }
+      V.push_back(std::vector<cd>(N));
+      for (int t = 0; t < N; ++t) V[j + 1][t] = w[t] / Hm(j + 1, j);
+    }
+    CMat Hs(mm + 1, mm);
+    for (int a = 0; a <= mm; ++a) for (int c = 0; c < mm; ++c) Hs(a, c) = Hm(a, c);
+    std::vector<cd> be1(mm + 1, cd(0.0, 0.0)), ym(mm);
+    be1[0] = beta;
+    ColPivQR qr;
+    qr.compute(Hs);
+    qr.solve(be1.data(), ym.data());
+    for (int t = 0; t < N; ++t) {
+      cd s = x0[t];
+      for (int c = 0; c < mm; ++c) s += V[c][t] * ym[c];
+      x[t] = s;
+    }
+    for (int t = 0; t < N; ++t) x0[t] = x[t];
+  }
+  return 0;
+}
+
+void ora_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }
+
+void ora_gauss_legendre(int n, double* nodes, double* weights) {
+  std::vector<double> gn, gw;
+  gauss_legendre(n, gn, gw);
+  for (int i = 0; i < n; ++i) { nodes[i] = gn[i]; weights[i] = gw[i]; }
+}
+void ora_bessel_jy(int n, double x, double* j, double* y) { *j = besselJ(n, x); *y = besselY(n, x); }
+void ora_colpiv_solve(int m, int n, const double* A, const double* b, double* x) {
+  CMat M(m, n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i)
+      M(i, j) = cd(A[2 * ((size_t)j * m + i)], A[2 * ((size_t)j * m + i) + 1]);
+  ColPivQR q;
+  q.compute(M);
+  q.solve((const cd*)b, (cd*)x);
+}
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+"""ORACLE - TEST INFRASTRUCTURE ONLY.
+
+ctypes front end of the CPU restatement of the reference DAFMM + GMRES path
+(oracle/ls_oracle.cpp). Only tests/, __graft_entry__.smoke() and the CPU
+baseline leg of bench.py import this module, and only as the checker or as
+the timed CPU baseline. Parity unpinned: the reference needs Eigen and
+Boost.Math, which are absent, so it cannot be compiled and run here.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libls_oracle.so")
+MAX_BUMPS = 8
+
+
+class OraCfg(ctypes.Structure):
+    _fields_ = [
+        ("nCones_LFR", ctypes.c_int),
+        ("nChebNodes", ctypes.c_int),
+        ("yes2DFMM", ctypes.c_int),
+        ("TOL_POW", ctypes.c_int),
+        ("degreeOfBases", ctypes.c_int),
+        ("nLevelsUniform", ctypes.c_int),
+        ("Qchoice", ctypes.c_int),
+        ("findPhi", ctypes.c_int),
+        ("reference_rounding", ctypes.c_int),
+        ("n_bumps", ctypes.c_int),
+        ("L", ctypes.c_double),
+        ("kappa", ctypes.c_double),
+        ("bump_cx", ctypes.c_double * MAX_BUMPS),
+        ("bump_cy", ctypes.c_double * MAX_BUMPS),
+        ("bump_a", ctypes.c_double * MAX_BUMPS),
+        ("bump_w", ctypes.c_double * MAX_BUMPS),
+    ]
+
+
+def build():
+    """Compiles the oracle with its Makefile (g++, OpenMP)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+        L.ora_create.restype = vp
+        L.ora_create.argtypes = [ctypes.POINTER(OraCfg), ctypes.c_char_p, ctypes.c_int]
+        L.ora_destroy.argtypes = [vp]
+        for name in ("ora_N", "ora_nlevels", "ora_level_lfr", "ora_rank"):
+            getattr(L, name).restype = ctypes.c_int
+            getattr(L, name).argtypes = [vp]
+        for name in ("ora_points", "ora_contrast", "ora_rhs", "ora_get_M", "ora_get_near"):
+            getattr(L, name).argtypes = [vp, dp]
+        L.ora_skeleton_dump.restype = ctypes.c_long
+        L.ora_skeleton_dump.argtypes = [vp, ip, ctypes.c_long]
+        L.ora_matvec.argtypes = [vp, dp, dp]
+        L.ora_dense_matvec.argtypes = [vp, dp, dp]
+        L.ora_gmres.restype = ctypes.c_int
+        L.ora_gmres.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp, dp, ip]
+        L.ora_gmres_restarted.restype = ctypes.c_int
+        L.ora_gmres_restarted.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, dp]
+        L.ora_set_threads.argtypes = [ctypes.c_int]
+        L.ora_gauss_legendre.argtypes = [ctypes.c_int, dp, dp]
+        L.ora_bessel_jy.argtypes = [ctypes.c_int, ctypes.c_double, dp, dp]
+        L.ora_colpiv_solve.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_cfg(d):
+    """Builds an OraCfg from a plain dict of the same field names."""
+    c = OraCfg()
+    for name, _ in OraCfg._fields_:
+        if name.startswith("bump_"):
+            vals = list(d.get(name, []))
+            arr = (ctypes.c_double * MAX_BUMPS)(*(vals + [0.0] * (MAX_BUMPS - len(vals))))
+            setattr(c, name, arr)
+        elif name in d:
+            setattr(c, name, d[name])
+    return c
+
+
+def set_threads(n):
+    lib().ora_set_threads(int(n))
+
+
+class Oracle:
+    """The reference DAFMM operator restated on the CPU (one per config)."""
+
+    def __init__(self, cfg):
+        L = lib()
+        self._cfg = make_cfg(cfg)
+        err = ctypes.create_string_buffer(256)
+        self._h = L.ora_create(ctypes.byref(self._cfg), err, 256)
+        if not self._h:
+            raise ValueError("oracle: " + err.value.decode())
+        self.N = L.ora_N(self._h)
+        self.nlevels = L.ora_nlevels(self._h)
+        self.level_lfr = L.ora_level_lfr(self._h)
+        self.rank = L.ora_rank(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ora_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def points(self):
+        a = np.empty((self.N, 2))
+        lib().ora_points(self._h, _dp(a))
+        return a
+
+    def contrast(self):
+        a = np.empty(self.N)
+        lib().ora_contrast(self._h, _dp(a))
+        return a
+
+    def rhs(self):
+        a = np.empty(self.N, dtype=np.complex128)
+        lib().ora_rhs(self._h, _dp(a))
+        return a
+
+    def far_moments(self):
+        """M at the leaf level, shape (rank, 31): M[i, n + 15] (column i)."""
+        a = np.empty((self.rank, 31), dtype=np.complex128)
+        lib().ora_get_M(self._h, _dp(a))
+        return a
+
+    def near_blocks(self):
+        """Colleague blocks, shape (9, rank, rank) in (row, col) order."""
+        a = np.empty((9, self.rank, self.rank), dtype=np.complex128)
+        lib().ora_get_near(self._h, _dp(a))
+        return np.ascontiguousarray(a.transpose(0, 2, 1))
+
+    def skeleton_dump(self):
+        n = lib().ora_skeleton_dump(self._h, None, 0)
+        a = np.empty(n, dtype=np.int32)
+        lib().ora_skeleton_dump(self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+        return a
+
+    def matvec(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.empty_like(x)
+        lib().ora_matvec(self._h, _dp(x), _dp(y))
+        return y
+
+    def dense_matvec(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.empty_like(x)
+        lib().ora_dense_matvec(self._h, _dp(x), _dp(y))
+        return y
+
+    def gmres(self, b, max_iter=400, tol=1e-10):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.empty_like(b)
+        hist = np.zeros(max_iter + 2)
+        it = ctypes.c_int(0)
+        lib().ora_gmres(self._h, _dp(b), max_iter, tol, _dp(x), _dp(hist), ctypes.byref(it))
+        return x, hist[: it.value + 1], it.value
+
+    def gmres_restarted(self, b, m, restarts):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.empty_like(b)
+        lib().ora_gmres_restarted(self._h, _dp(b), m, restarts, _dp(x))
+        return x
+
+
+def gauss_legendre(n):
+    nodes, w = np.empty(n), np.empty(n)
+    lib().ora_gauss_legendre(n, _dp(nodes), _dp(w))
+    return nodes, w
+
+
+def bessel_jy(n, x):
+    j, y = ctypes.c_double(), ctypes.c_double()
+    lib().ora_bessel_jy(n, x, ctypes.byref(j), ctypes.byref(y))
+    return j.value, y.value
+
+
+def colpiv_solve(A, b):
+    A = np.asfortranarray(A, dtype=np.complex128)
+    m, n = A.shape
+    b = np.ascontiguousarray(b, dtype=np.complex128)
+    x = np.empty(n, dtype=np.complex128)
+    Af = np.ascontiguousarray(A.T).reshape(-1)  # column-major flat
+    lib().ora_colpiv_solve(m, n, _dp(Af), _dp(b), _dp(x))
+    return x
