@@ -1,0 +1,156 @@
+/*
+ * ls_dafmm.h - C ABI of the GB300 DAFMM matvec + GMRES library
+ * (liblsdafmm.so, package lippmann_schwinger_solver_gb300).
+ *
+ * Drop-in boundary for the hot path of vaishna77/Lippmann_Schwinger_Solver:
+ * the operator that the reference's GMRES drives through the duck-typed
+ * `MatVecProduct(Vec&, Vec&)` member. Every entry point below names the
+ * reference interface it replaces. Plain pointers and sizes only; complex
+ * vectors are interleaved (re, im) doubles in the reference's leaf order
+ * (depth-first leaves, 36 Chebyshev nodes per leaf, node = row * n + col).
+ * All functions return LS_OK (0) or a negative LS_E_* code and never exit
+ * the process; ls_last_error() describes the last failure on this thread.
+ */
+#ifndef LS_DAFMM_H
+#define LS_DAFMM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ls_status;
+#define LS_OK 0
+#define LS_E_INVALID (-1)     /* bad argument or configuration */
+#define LS_E_CUDA (-2)        /* a CUDA call failed */
+#define LS_E_NOMEM (-3)       /* host or device allocation failed */
+#define LS_E_NOT_CONVERGED (-4)
+#define LS_E_STATE (-5)       /* handle used in the wrong state */
+#define LS_E_TIMEOUT (-6)     /* a bounded device wait gave up */
+
+#define LS_MAX_BUMPS 8
+
+/* Precision of the operator blocks and their accumulation. */
+#define LS_PREC_F64 0
+#define LS_PREC_F32 1
+
+/*
+ * Problem description. Replaces the positional argv of GMRES/GMRES.cpp:321-333
+ * (main), the inputsToDFMM struct (GMRES/GMRES.cpp:129-138), the global
+ * `kappa` (GMRES/G_FMM2DTree.hpp:3) and the contrast plugin selected by the
+ * global `Qchoice` (GMRES/GMRES.cpp:4, 100-117).
+ */
+typedef struct {
+  int nCones_LFR;          /* cones of a box at the finest HFR level (16) */
+  int nChebNodes;          /* Chebyshev nodes per leaf per direction (6) */
+  int yes2DFMM;            /* 1: directional DAFMM, 0: AFMM (level_LFR = 2) */
+  int TOL_POW;             /* NCA tolerance 10^-TOL_POW */
+  int degreeOfBases;       /* 6 -> 21 Chebyshev basis polynomials */
+  int nLevelsUniform;      /* depth of the uniform quadtree (2..10) */
+  int Qchoice;             /* 0..5 reference contrasts, 6 = Gaussian bumps */
+  int findPhi;             /* 1: I + k^2 q G (LS operator); 0: bare G */
+  int reference_rounding;  /* 1: M and near blocks rounded to 6 significant
+                              digits, as the reference's text cache does */
+  int n_bumps;             /* Qchoice 6: q(x) = sum_k a_k exp(-|x-c_k|^2/w_k^2) */
+  double L;                /* half side of the square domain */
+  double kappa;            /* wavenumber */
+  double bump_cx[LS_MAX_BUMPS];
+  double bump_cy[LS_MAX_BUMPS];
+  double bump_a[LS_MAX_BUMPS];
+  double bump_w[LS_MAX_BUMPS];
+} ls_config;
+
+typedef struct {
+  int N;                   /* unknowns = leaves * nChebNodes^2 */
+  int n_leaves;
+  int n_levels;
+  int level_LFR;
+  int rank;                /* nChebNodes^2 */
+  long long far_entries;   /* complex entries of all M2M/M2L/L2L blocks */
+  long long near_entries;  /* complex entries of the near blocks (shared) */
+  long long matvec_bytes;  /* algorithmic HBM bytes of one FP64 matvec */
+  long long matvec_flops;  /* real flops of one matvec */
+  long long device_bytes;  /* device memory held by the operator */
+  double assemble_seconds; /* host assembly wall time */
+  int max_rank;            /* largest NCA skeleton */
+  int n_kernels_per_matvec;/* CUDA kernel launches in one matvec */
+} ls_op_info_t;
+
+typedef struct ls_op ls_op;
+
+/*
+ * Builds the tree, interaction lists, cones, precomputations and NCA
+ * skeletons, assembles every block and uploads the operator to `device`.
+ * Replaces DFMM::DFMM + DFMM::FMMTreeInitialisation (GMRES/GMRES.cpp:152-199)
+ * for uniform trees (createUniformTree, GMRES/G_FMM2DTree.hpp:917).
+ * device < 0 assembles on the host only: geometry, precomputations and
+ * skeletons can be inspected, every device call returns LS_E_STATE.
+ */
+ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out);
+ls_status ls_op_destroy(ls_op* op);
+ls_status ls_op_info(const ls_op* op, ls_op_info_t* out);
+
+/* Chebyshev grid points (N x 2) in the operator's order; replaces
+ * DFMM::gridPoints (GMRES/GMRES.cpp:145, G_FMM2DTree.hpp:1150-1163). */
+ls_status ls_op_points(const ls_op* op, double* xy);
+/* q(x_i) at the grid points; userkernel::ContrastFunction (GMRES/GMRES.cpp:104). */
+ls_status ls_op_contrast(const ls_op* op, double* q);
+/* b_i = -kappa^2 q(x_i) exp(i kappa x_i1); userkernel::RHSFunction (GMRES/GMRES.cpp:122-125). */
+ls_status ls_op_rhs(const ls_op* op, double* b);
+
+/*
+ * y = A x on the device. x and y are device pointers to N complex values
+ * (2N doubles). Replaces DFMM::MatVecProduct (GMRES/GMRES.cpp:201-254).
+ * `stream` is a cudaStream_t (NULL = the operator's own stream). The call
+ * is asynchronous with respect to the host.
+ */
+ls_status ls_matvec(ls_op* op, const double* x, double* y, void* stream);
+/* Same product with FP32 blocks and FP32 accumulation (x, y stay FP64 on
+ * the boundary). Requires ls_op_enable_f32(). */
+ls_status ls_matvec_f32(ls_op* op, const double* x, double* y, void* stream);
+ls_status ls_op_enable_f32(ls_op* op);
+/* Host-buffer convenience: copies x in, runs ls_matvec, copies y out, syncs.
+ * This is the call a reference-style driver makes (Vec in, Vec out). */
+ls_status ls_matvec_host(ls_op* op, const double* x, double* y);
+
+/*
+ * Tolerance-stopped GMRES with Givens rotations, x0 = 0; replaces
+ * classGMRES::gmres (GMRES_Hybrid/include/gmres.hpp:54-119), with the
+ * conjugate-linear inner product and unitary complex rotations. b and x are
+ * HOST buffers of N complex values; history receives |r_k|/|b| estimates
+ * (max_iter + 1 entries, may be NULL). Returns LS_E_NOT_CONVERGED (with x
+ * filled) when max_iter is reached first.
+ */
+ls_status ls_gmres(ls_op* op, const double* b, int max_iter, double tol, double* x,
+                   double* history, int* n_iter, double* rel_residual);
+/* Fixed-m restarted GMRES (GMRES/GMRES.cpp:257-319, RestartedGMRES). */
+ls_status ls_gmres_restarted(ls_op* op, const double* b, int m, int restarts, double* x);
+
+/* Mixed precision: FP64 flexible GMRES whose inner solves use the FP32
+ * operator (needs ls_op_enable_f32). Stops on the FP64 true residual. */
+ls_status ls_gmres_mixed(ls_op* op, const double* b, int max_outer, int inner_iter,
+                         double tol, double* x, double* history, int* n_matvec,
+                         double* rel_residual);
+
+/* Times `iters` device matvecs (inputs resident) with CUDA events on the
+ * operator's stream after `warmup` untimed ones; writes the mean ms per
+ * matvec and the mean ms of the dominant kernel (M2L). precision: LS_PREC_*. */
+ls_status ls_time_matvec(ls_op* op, int precision, int warmup, int iters, float* ms_matvec,
+                         float* ms_m2l);
+
+/* Flattened NCA skeletons (one record per tree node: level, box, cone,
+ * out_active, in_active, then counted lists out-charge, out-check,
+ * in-charge, in-check, user-check). Returns the length; buf may be NULL. */
+long ls_op_skeleton_dump(const ls_op* op, int* buf, long cap);
+/* Leaf-level far-field moments M (rank x 31, complex) and colleague near
+ * blocks (9 x rank x rank, complex, row major) as used by the matvec. */
+ls_status ls_op_precomputations(const ls_op* op, double* M, double* near);
+
+const char* ls_last_error(void);
+const char* ls_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1260 @@
+// Host assembler of the DAFMM operator for a uniform quadtree.
+//
+// Builds, in this order, the pieces that the reference computes in
+// DFMM::FMMTreeInitialisation (GMRES/GMRES.cpp:161-199):
+//   * tree geometry, level_LFR and cones      G_FMM2DTree.hpp:293-328, 917-941, 1952-1974
+//   * interaction lists (LFR and per cone)    G_FMM2DTree.hpp:1356-1498
+//   * Chebyshev basis Q, Q^+, far moments M   FarFieldInteraction.hpp:115-160
+//   * colleague near blocks                   NearFieldInteraction1.hpp:260-290, G_FMM2DTree.hpp:1773-1830
+//   * NCA skeletons (ACA_only_nodes)          ACA.hpp:253-481, G_FMM2DTree.hpp:2062-2385, 3232-3571
+//   * user check points                       G_FMM2DTree.hpp:3146-3230
+//   * block fills                             G_FMM2DTree.hpp:2502, 2653, 2824, 3573-3880, 3944-4206
+// and then lays the operator out for the GPU: every phase of the matvec
+// becomes a list of gather-GEMV items over two flat buffers (skeleton
+// charges and skeleton potentials). The per-box QR solves of the reference
+// (Atilde^{-1}) are folded into the blocks: upward T = Atilde^{-1} Ar,
+// downward W = L2L Atilde^{-1}, so the device never solves a system.
+//
+// Kernel entries, quadrature integrands and the ACA updates use the same
+// floating-point expression order as the reference source (and the file
+// is compiled with -ffp-contract=off), so skeleton choices are
+// reproducible across hosts.
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <unordered_map>
+#include <vector>
+
+#include <omp.h>
+
+#include "ls_internal.h"
+
+namespace lsg {
+namespace {
+
+constexpr double kPi = 3.1415926535897932384;
+const cd kI(0.0, 1.0);
+constexpr int kSeries = 15;                 // FarFieldInteraction.hpp:55
+constexpr double kQuadEps = 1e-7;           // FarFieldInteraction.hpp:37, NearFieldInteraction1.hpp:199
+constexpr int kQuadOrder = 10;              // 10x10 Gauss-Legendre per panel
+
+// ---------------------------------------------------------------- special functions
+double bes_j(int n, double x) {
+  if (n >= 0) return std::cyl_bessel_j(double(n), x);
+  const double t = std::cyl_bessel_j(double(-n), x);
+  return ((-n) % 2 == 0) ? t : -t;
+}
+double bes_y(int n, double x) {
+  if (n >= 0) return std::cyl_neumann(double(n), x);
+  const double t = std::cyl_neumann(double(-n), x);
+  return ((-n) % 2 == 0) ? t : -t;
+}
+double cheb_t(double x, int n) { return std::cos(n * std::acos(x)); }
+
+// Gauss-Legendre nodes by Newton iteration on P_n in extended precision,
+// ordered as pairs (-t, +t) from the centre outwards.
+void gl_rule(int n, std::vector<double>& x, std::vector<double>& w) {
+  std::vector<std::pair<long double, long double>> pos;
+  for (int i = 1; i <= n; ++i) {
+    long double t = std::cos(kPi * (i - 0.25L) / (n + 0.5L));
+    long double d = 0.0L;
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1.0L, p1 = t;
+      for (int k = 2; k <= n; ++k) {
+        const long double p2 = ((2.0L * k - 1.0L) * t * p1 - (k - 1.0L) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      d = n * (t * p1 - p0) / (t * t - 1.0L);
+      const long double dt = p1 / d;
+      t -= dt;
+      if (std::fabs((double)dt) < 1e-30) break;
+    }
+    long double p0 = 1.0L, p1 = t;
+    for (int k = 2; k <= n; ++k) {
+      const long double p2 = ((2.0L * k - 1.0L) * t * p1 - (k - 1.0L) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    d = n * (t * p1 - p0) / (t * t - 1.0L);
+    if (t >= 0.0L) pos.push_back({t, 2.0L / ((1.0L - t * t) * d * d)});
+  }
+  std::sort(pos.begin(), pos.end());
+  x.clear();
+  w.clear();
+  for (auto& p : pos) {
+    if (std::fabs((double)p.first) < 1e-300) {
+      x.push_back(0.0);
+      w.push_back((double)p.second);
+    } else {
+      x.push_back(-(double)p.first);
+      w.push_back((double)p.second);
+      x.push_back((double)p.first);
+      w.push_back((double)p.second);
+    }
+  }
+}
+
+// 6-significant-digit round trip of the reference's text cache.
+double round6(double v) {
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%.6g", v);
+  return std::strtod(buf, nullptr);
+}
+
+// Adaptive quadrature on [-1,1]^2 (domain2D.hpp:46-138): a panel whose four
+// children reproduce its 10x10 value within eps becomes a leaf and
+// contributes its own value; leaves are summed in depth-first order.
+template <class F>
+cd quad2d(const F& f, const std::vector<double>& gx, const std::vector<double>& gw) {
+  struct P { double xc, yc, xr, yr; cd v; };
+  const int n = (int)gx.size();
+  auto integ = [&](P& p) {
+    cd s(0.0, 0.0);
+    for (int a = 0; a < n; ++a) {
+      const double x = p.xc + p.xr * gx[a];
+      for (int b = 0; b < n; ++b) {
+        const double y = p.yc + p.yr * gx[b];
+        s += gw[a] * gw[b] * f(x, y);
+      }
+    }
+    s *= (p.xr * p.yr);
+    p.v = s;
+  };
+  P root{0.0, 0.0, 1.0, 1.0, cd()};
+  integ(root);
+  cd total(0.0, 0.0);
+  std::vector<P> todo{root};
+  while (!todo.empty()) {
+    P p = todo.back();
+    todo.pop_back();
+    const double hx = 0.5 * p.xr, hy = 0.5 * p.yr;
+    P c[4] = {{p.xc - hx, p.yc - hy, hx, hy, cd()}, {p.xc + hx, p.yc - hy, hx, hy, cd()},
+              {p.xc + hx, p.yc + hy, hx, hy, cd()}, {p.xc - hx, p.yc + hy, hx, hy, cd()}};
+    for (auto& q : c) integ(q);
+    cd e = p.v;
+    for (auto& q : c) e -= q.v;
+    if (std::abs(e) < kQuadEps) total += p.v;
+    else for (int l = 3; l >= 0; --l) todo.push_back(c[l]);
+  }
+  return total;
+}
+
+// ---------------------------------------------------------------- small dense QR
+// Column-pivoted Householder QR (xGEQP3 with norm downdating); solve()
+// returns the basic least-squares solution on the nonzero pivots.
+struct PivQR {
+  int m = 0, n = 0, nz = 0;
+  std::vector<cd> a;  // column major m x n
+  std::vector<cd> tau;
+  std::vector<int> perm;
+  cd& at(int i, int j) { return a[(size_t)j * m + i]; }
+  const cd& at(int i, int j) const { return a[(size_t)j * m + i]; }
+
+  void factor(int rows, int cols, const std::vector<cd>& colmajor) {
+    m = rows;
+    n = cols;
+    a = colmajor;
+    const int sz = std::min(m, n);
+    tau.assign(sz, cd(0.0, 0.0));
+    perm.resize(n);
+    for (int j = 0; j < n; ++j) perm[j] = j;
+    std::vector<double> upd(n), dir(n);
+    double big = 0.0;
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int i = 0; i < m; ++i) s += std::norm(at(i, j));
+      upd[j] = dir[j] = std::sqrt(s);
+      big = std::max(big, upd[j]);
+    }
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double helper = (big * eps) * (big * eps) / double(std::max(m, 1));
+    const double dthr = std::sqrt(eps);
+    nz = sz;
+    std::vector<cd> t(n);
+    for (int k = 0; k < sz; ++k) {
+      int p = k;
+      for (int j = k + 1; j < n; ++j)
+        if (upd[j] > upd[p]) p = j;
+      if (nz == sz && upd[p] * upd[p] < helper * double(m - k)) nz = k;
+      if (p != k) {
+        for (int i = 0; i < m; ++i) std::swap(at(i, k), at(i, p));
+        std::swap(upd[k], upd[p]);
+        std::swap(dir[k], dir[p]);
+        std::swap(perm[k], perm[p]);
+      }
+      const cd c0 = at(k, k);
+      double tail = 0.0;
+      for (int i = k + 1; i < m; ++i) tail += std::norm(at(i, k));
+      double beta;
+      const double tiny = std::numeric_limits<double>::min();
+      if (tail <= tiny && c0.imag() * c0.imag() <= tiny) {
+        tau[k] = cd(0.0, 0.0);
+        beta = c0.real();
+        for (int i = k + 1; i < m; ++i) at(i, k) = cd(0.0, 0.0);
+      } else {
+        beta = std::sqrt(std::norm(c0) + tail);
+        if (c0.real() >= 0.0) beta = -beta;
+        const cd d = c0 - beta;
+        for (int i = k + 1; i < m; ++i) at(i, k) = at(i, k) / d;
+        tau[k] = std::conj((beta - c0) / beta);
+      }
+      at(k, k) = cd(beta, 0.0);
+      if (tau[k] != cd(0.0, 0.0)) {
+        for (int j = k + 1; j < n; ++j) {
+          cd s = at(k, j);
+          for (int i = k + 1; i < m; ++i) s += std::conj(at(i, k)) * at(i, j);
+          t[j] = s;
+        }
+        for (int j = k + 1; j < n; ++j) {
+          at(k, j) -= tau[k] * t[j];
+          for (int i = k + 1; i < m; ++i) at(i, j) -= (tau[k] * at(i, k)) * t[j];
+        }
+      }
+      for (int j = k + 1; j < n; ++j) {
+        if (upd[j] != 0.0) {
+          double r = std::abs(at(k, j)) / upd[j];
+          r = (1.0 + r) * (1.0 - r);
+          if (r < 0.0) r = 0.0;
+          const double q = upd[j] / dir[j];
+          if (r * q * q <= dthr) {
+            double s = 0.0;
+            for (int i = k + 1; i < m; ++i) s += std::norm(at(i, j));
+            dir[j] = std::sqrt(s);
+            upd[j] = dir[j];
+          } else {
+            upd[j] *= std::sqrt(r);
+          }
+        }
+      }
+    }
+  }
+
+  void solve(const cd* b, cd* x) const {
+    std::vector<cd> c(b, b + m);
+    for (int k = 0; k < nz; ++k) {
+      if (tau[k] == cd(0.0, 0.0)) continue;
+      cd s = c[k];
+      for (int i = k + 1; i < m; ++i) s += std::conj(at(i, k)) * c[i];
+      s *= tau[k];
+      c[k] -= s;
+      for (int i = k + 1; i < m; ++i) c[i] -= at(i, k) * s;
+    }
+    for (int i = nz - 1; i >= 0; --i) {
+      cd s = c[i];
+      for (int j = i + 1; j < nz; ++j) s -= at(i, j) * c[j];
+      c[i] = s / at(i, i);
+    }
+    for (int j = 0; j < n; ++j) x[j] = cd(0.0, 0.0);
+    for (int k = 0; k < nz; ++k) x[perm[k]] = c[k];
+  }
+};
+
+// ---------------------------------------------------------------- contrast plugin
+double contrast_fn(const ls_config& c, double x, double y) {
+  switch (c.Qchoice) {
+    case 0: {
+      const double R2 = x * x + y * y;
+      return 1.5 * std::exp(-160.0 * R2);
+    }
+    case 1: {
+      static const double cx[20] = {-1.17182014706864, -0.861066625441127, -1.14533939124057,
+        -0.856639124568525, -0.620066350133170, -0.457064031294315, -0.482782006538245,
+        -0.635070123186999, 0.108594058866164, -0.0315722590552472, -0.177274727610547,
+        0.0342987980936911, 0.369662097773613, 0.591444264226524, 0.401225715100565,
+        0.666822699314234, 1.10327781188617, 0.827519268441487, 0.873411278211136, 1.09482906183464};
+      static const double cy[20] = {-0.361066625441127, 0.0719520938231629, 0.354660608759432,
+        1.14336087543147, -1.12006635013317, -0.457064031294315, 0.364929876813001,
+        0.802261227250738, -0.394084977497864, -0.0315722590552472, 0.322725272389453,
+        1.03429879809369, -1.13033790222639, 0.0137164199764117, 0.401225715100565,
+        1.16682269931423, -0.345187707108795, -0.172480731558513, 0.373411278211136, 1.09482906183464};
+      double q = 0.0;
+      const double a = 0.0013;
+      for (int i = 0; i < 20; ++i) {
+        const double R2 = (x - cx[i]) * (x - cx[i]) + (y - cy[i]) * (y - cy[i]);
+        q += 1.5 * std::exp(-R2 / a);
+      }
+      return q;
+    }
+    case 2: {
+      const double C = 0.4987;
+      const double psi = 1.0 - (x - 0.15 * (1 - x * x)) * (x - 0.15 * (1 - x * x)) -
+                         C * (1.0 + 0.3 * x) * (1.0 + 0.3 * x) * y * y;
+      static const double aa[5] = {0.45, 0.195, 0.51, 0.195, 0.63};
+      static const double xs[5] = {0.8, 0.54, -0.14, -0.5, 0.18};
+      static const double ys[5] = {0.0, -0.28, 0.7, -0.01, 0.8};
+      if (psi <= 0.05) return 0.0;
+      double g = 0.0;
+      for (int i = 0; i < 5; ++i) {
+        const double t = (x - xs[i]) * (x - xs[i]) + (y - ys[i]) * (y - ys[i]);
+        g += aa[i] * std::exp(-t / 0.01);
+      }
+      return -1.5 * (psi - 0.05) - g * std::cos(0.9 * y);
+    }
+    case 3: {
+      const double R2 = x * x + y * y;
+      return 0.5 * std::erfc(5.0 * (R2 - 1.0));
+    }
+    case 4: {
+      const double R = std::sqrt(x * x + y * y);
+      const double th = std::atan2(y, x);
+      return (1.0 - std::pow(std::sin(0.5 * th), 500)) * std::exp(-2000 * (0.1 - R * R) * (0.1 - R * R));
+    }
+    case 5: {
+      const double R = std::sqrt(x * x + y * y);
+      return 4 * (y - 0.1) * (1.0 - std::erf(25.0 * (R - 0.3)));
+    }
+    default: {
+      double q = 0.0;
+      for (int k = 0; k < c.n_bumps; ++k) {
+        const double dx = x - c.bump_cx[k], dy = y - c.bump_cy[k];
+        const double R2 = dx * dx + dy * dy;
+        q += c.bump_a[k] * std::exp(-R2 / (c.bump_w[k] * c.bump_w[k]));
+      }
+      return q;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- the builder
+struct Node {
+  bool out_active = false, in_active = false;
+  std::vector<int> out_charge, out_check, in_charge, in_check, user_check;
+  std::vector<cd> Ar;  // rank_out x K, row major (pivot rows of the outgoing NCA)
+  std::vector<int> IL; // source boxes at the same level
+  // derived during packing
+  std::vector<int> fidx;   // gather indices of f_out in the charge buffer
+  long long own_charge = -1;
+  long long pot_off = -1;
+  bool pot_nonzero = false;
+};
+
+class Builder {
+ public:
+  explicit Builder(const ls_config& c) : cfg(c) {}
+  bool run(HostOperator& op, std::string& err);
+
+ private:
+  ls_config cfg;
+  int nL = 0, rank = 0, nb = 0, level_LFR = 2, N = 0;
+  double kappa = 0.0, L = 1.0;
+  std::vector<double> radius;         // boxRadius per level (0..10)
+  std::vector<int> nCones;
+  std::vector<double> aperture;
+  std::vector<std::vector<double>> cx, cy;  // box centres per level
+  std::vector<double> gx_, gy_;       // grid points
+  std::vector<double> kq_;            // kappa*kappa*q at grid points (entry scaling)
+  std::vector<double> cheb1;
+  std::vector<std::pair<int, int>> bases;
+  std::vector<double> gln, glw;
+  std::vector<cd> Mleaf;              // (2S+1) x rank, column major
+  std::vector<cd> near;               // 9 x rank x rank, row major
+  std::vector<std::vector<std::vector<int>>> nbrs;  // [level][box] same-level neighbours
+  std::vector<std::vector<Node>> nodes;             // [level][node]
+
+  bool is_lfr(int j) const { return j >= level_LFR; }
+  int nodes_at(int j) const { return is_lfr(j) ? (1 << (2 * j)) : (1 << (2 * j)) * nCones[j]; }
+  Node& lfr(int j, int k) { return nodes[j][k]; }
+  Node& cone(int j, int k, int c) { return nodes[j][(size_t)k * nCones[j] + c]; }
+  // Node through which box (j,k) exposes its data to direction `c` of a
+  // parent/IL relation: LFR boxes have one node, HFR boxes one per cone.
+  Node& child_node(int jchild, int kchild, int parent_cone) {
+    return is_lfr(jchild) ? lfr(jchild, kchild) : cone(jchild, kchild, parent_cone / 2);
+  }
+
+  // Far-field kernel entry (G_FMM2DTree.hpp:603-658) from a cached Hankel
+  // vector h_n = (J_n + i Y_n) e^{i n theta} of target i about leaf(j).
+  void hankel(int i, int leaf, cd* h) const {
+    const double px = gx_[i], py = gy_[i];
+    const double lx = cx[nL][leaf], ly = cy[nL][leaf];
+    const double th = std::atan2(py - ly, px - lx);
+    const double R2 = (py - ly) * (py - ly) + (px - lx) * (px - lx);
+    const double R = kappa * std::sqrt(R2);
+    double J[kSeries + 1], Y[kSeries + 1];
+    for (int n = 0; n <= kSeries; ++n) {
+      J[n] = std::cyl_bessel_j(double(n), R);
+      Y[n] = std::cyl_neumann(double(n), R);
+    }
+    for (int n = -kSeries; n <= kSeries; ++n) {
+      const int a = n < 0 ? -n : n;
+      const double sg = (n < 0 && (a % 2 == 1)) ? -1.0 : 1.0;
+      const double jn = sg == 1.0 ? J[a] : -J[a];
+      const double yn = sg == 1.0 ? Y[a] : -Y[a];
+      h[n + kSeries] = (jn + kI * yn) * std::exp(kI * double(n) * th);
+    }
+  }
+  struct HCache {
+    const Builder* b;
+    std::unordered_map<long long, std::vector<cd>> m;
+    const cd* get(int i, int leaf) {
+      const long long key = (long long)i * 1048576LL + leaf;
+      auto it = m.find(key);
+      if (it != m.end()) return it->second.data();
+      std::vector<cd> h(2 * kSeries + 1);
+      b->hankel(i, leaf, h.data());
+      return m.emplace(key, std::move(h)).first->second.data();
+    }
+  };
+  cd entry(int i, int j, HCache& hc) const {
+    const cd* h = hc.get(i, j / rank);
+    const int idx = j % rank;
+    const int nS = 2 * kSeries + 1;
+    cd s = 0.0 + 0.0 * kI;
+    for (int n = 0; n < nS; ++n) s += Mleaf[(size_t)idx * nS + n] * h[n];
+    s *= kI / 4.0;
+    if (cfg.findPhi) {
+      s *= kq_[i];
+      if (i == j) s += 1.0;
+    }
+    return s;
+  }
+  // Row-major block K(rows, cols).
+  void fill(const std::vector<int>& rows, const std::vector<int>& cols, HCache& hc, cd* out, int ld) const {
+    for (size_t a = 0; a < rows.size(); ++a)
+      for (size_t b = 0; b < cols.size(); ++b) out[a * ld + b] = entry(rows[a], cols[b], hc);
+  }
+  std::vector<cd> block_colmajor(const std::vector<int>& rows, const std::vector<int>& cols, HCache& hc) const {
+    std::vector<cd> A(rows.size() * cols.size());
+    for (size_t b = 0; b < cols.size(); ++b)
+      for (size_t a = 0; a < rows.size(); ++a) A[b * rows.size() + a] = entry(rows[a], cols[b], hc);
+    return A;
+  }
+
+  int aca(const std::vector<int>& rows, const std::vector<int>& cols, double eps, std::vector<int>& rb,
+          std::vector<int>& cb, std::vector<cd>* Ar, HCache& hc) const;
+
+  void geometry();
+  void precompute();
+  void interaction_lists();
+  void nca_level_lfr(int j);
+  void nca_level_hfr(int j);
+  void user_checks();
+  void pack(HostOperator& op);
+};
+
+static int argmax_remaining(const std::vector<cd>& v, const std::vector<char>& used) {
+  int idx = -1;
+  double mx = 0.0;
+  for (int i = 0; i < (int)v.size(); ++i) {
+    if (used[i]) continue;
+    if (idx < 0) { idx = i; mx = std::abs(v[i]); continue; }
+    if (std::abs(v[i]) > mx) { idx = i; mx = std::abs(v[idx]); }
+  }
+  return idx;
+}
+static double norm2(const std::vector<cd>& v) {
+  double s = 0.0;
+  for (const cd& z : v) s += std::norm(z);
+  return std::sqrt(s);
+}
+static cd cdot(const std::vector<cd>& a, const std::vector<cd>& b) {
+  cd s(0.0, 0.0);
+  for (size_t i = 0; i < a.size(); ++i) s += std::conj(a[i]) * b[i];
+  return s;
+}
+
+// Partially pivoted cross approximation that keeps only the pivots
+// (ACA_only_nodes, ACA.hpp:253-481). Row-first when there are fewer rows
+// than columns, column-first otherwise; ties go to the lowest index.
+int Builder::aca(const std::vector<int>& rows, const std::vector<int>& cols, double eps, std::vector<int>& rb,
+                 std::vector<int>& cb, std::vector<cd>* Ar, HCache& hc) const {
+  const int n1 = (int)rows.size(), n2 = (int)cols.size(), mn = std::min(n1, n2);
+  std::vector<char> rused(n1, 0), cused(n2, 0);
+  std::vector<std::vector<cd>> U, V, piv_rows;
+  std::vector<cd> row(n2), col(n1), u, v;
+  auto get_row = [&](int r) { std::vector<cd> o(n2); for (int k = 0; k < n2; ++k) o[k] = entry(rows[r], cols[k], hc); return o; };
+  auto get_col = [&](int c) { std::vector<cd> o(n1); for (int k = 0; k < n1; ++k) o[k] = entry(rows[k], cols[c], hc); return o; };
+  int rk = 0, ri = 0, ci = 0;
+  const double thr = eps * std::pow(10, -1.0 * 0);
+  if (n1 < n2) {
+    int l = 0;
+    for (; l < n1; ++l) {
+      ri = l;
+      row = get_row(ri);
+      ci = argmax_remaining(row, cused);
+      if (std::abs(row[ci]) > thr) break;
+    }
+    if (l == n1) return 0;
+    v.resize(n2);
+    for (int s = 0; s < n2; ++s) v[s] = row[s] / row[ci];
+    rb.push_back(ri);
+    cb.push_back(ci);
+    col = get_col(ci);
+    u = col;
+    U.push_back(u); V.push_back(v); piv_rows.push_back(row);
+    cused[ci] = 1; rused[ri] = 1;
+    rk = 1;
+    double nS = 0.0, prev = 1000.0;
+    ri = argmax_remaining(col, rused);
+    while (std::abs(row[ci]) > thr && std::abs(col[ri]) > eps && std::abs(prev - nS) >= eps * prev && rk < mn) {
+      rb.push_back(ri);
+      row = get_row(ri);
+      const std::vector<cd> raw = row;
+      for (int a = 0; a < rk; ++a)
+        for (size_t s = 0; s < V[a].size(); ++s) row[s] -= U[a][ri] * V[a][s];
+      ci = argmax_remaining(row, cused);
+      cb.push_back(ci);
+      for (size_t s = 0; s < row.size(); ++s) v[s] = row[s] / row[ci];
+      col = get_col(ci);
+      for (int a = 0; a < rk; ++a)
+        for (size_t s = 0; s < U[a].size(); ++s) col[s] -= V[a][ci] * U[a][s];
+      u = col;
+      if (norm2(u) < 1e-8 || norm2(v) < 1e-8) { rb.pop_back(); cb.pop_back(); break; }
+      U.push_back(u); V.push_back(v); piv_rows.push_back(raw);
+      ++rk;
+      cused[ci] = 1; rused[ri] = 1;
+      if (rk != 2) prev = nS;
+      nS = std::pow(nS, 2) + std::pow(norm2(u) * norm2(v), 2);
+      for (int a = 0; a < rk; ++a) nS += 2 * std::abs(cdot(U[a], u) * cdot(V[a], v));
+      nS = std::sqrt(nS);
+      ri = argmax_remaining(col, rused);
+    }
+  } else {
+    int l = 0;
+    for (; l < n2; ++l) {
+      ci = l;
+      col = get_col(ci);
+      ri = argmax_remaining(col, rused);
+      if (std::abs(col[ri]) > thr) break;
+    }
+    if (l == n2) return 0;
+    cb.push_back(ci);
+    v.resize(n1);
+    for (int s = 0; s < n1; ++s) v[s] = col[s] / col[ri];
+    rb.push_back(ri);
+    row = get_row(ri);
+    u = row;
+    U.push_back(u); V.push_back(v); piv_rows.push_back(row);
+    rk = 1;
+    rused[ri] = 1; cused[ci] = 1;
+    double nS = 0.0, prev = 1000.0;
+    ci = argmax_remaining(row, cused);
+    while (std::abs(row[ci]) > thr && std::abs(col[ri]) > eps && std::abs(prev - nS) >= eps * prev && rk < mn) {
+      cb.push_back(ci);
+      col = get_col(ci);
+      for (int a = 0; a < rk; ++a)
+        for (size_t s = 0; s < V[a].size(); ++s) col[s] -= U[a][ci] * V[a][s];
+      ri = argmax_remaining(col, rused);
+      rb.push_back(ri);
+      for (size_t s = 0; s < col.size(); ++s) v[s] = col[s] / col[ri];
+      row = get_row(ri);
+      const std::vector<cd> raw = row;
+      for (int a = 0; a < rk; ++a)
+        for (size_t s = 0; s < U[a].size(); ++s) row[s] -= V[a][ri] * U[a][s];
+      u = row;
+      if (norm2(u) < 1e-8 || norm2(v) < 1e-8) { cb.pop_back(); rb.pop_back(); break; }
+      U.push_back(u); V.push_back(v); piv_rows.push_back(raw);
+      ++rk;
+      rused[ri] = 1; cused[ci] = 1;
+      if (rk != 2) prev = nS;
+      nS = std::pow(nS, 2) + std::pow(norm2(u) * norm2(v), 2);
+      for (int a = 0; a < rk; ++a) nS += 2 * std::abs(cdot(U[a], u) * cdot(V[a], v));
+      nS = std::sqrt(nS);
+      ci = argmax_remaining(row, cused);
+    }
+  }
+  if (Ar) {
+    Ar->assign((size_t)rk * n2, cd(0.0, 0.0));
+    for (int a = 0; a < rk; ++a)
+      for (int b = 0; b < n2; ++b) (*Ar)[(size_t)a * n2 + b] = piv_rows[a][b];
+  }
+  return rk;
+}
+
+void Builder::geometry() {
+  kappa = cfg.kappa;
+  L = cfg.L;
+  const int n1 = cfg.nChebNodes;
+  rank = n1 * n1;
+  nb = cfg.degreeOfBases * (cfg.degreeOfBases + 1) / 2;
+  nL = cfg.nLevelsUniform;
+  if (cfg.yes2DFMM == 1) {
+    if (kappa == 0) level_LFR = 2;
+    else level_LFR = (int)std::floor(std::log(kappa * L / 0.35) / std::log(2.0));
+    if (level_LFR < 2) level_LFR = 2;
+  } else {
+    level_LFR = 2;
+  }
+  if (level_LFR >= nL) level_LFR = nL - 1;
+  radius.push_back(L);
+  for (int j = 1; j <= 10; ++j) radius.push_back(radius[j - 1] / 2.0);
+  cx.assign(nL + 1, {});
+  cy.assign(nL + 1, {});
+  cx[0] = {0.0};
+  cy[0] = {0.0};
+  std::vector<double> rr(1, L);
+  for (int j = 0; j < nL; ++j) {
+    const size_t nbx = cx[j].size();
+    cx[j + 1].resize(nbx * 4);
+    cy[j + 1].resize(nbx * 4);
+    const double h = 0.5 * radius[j];
+    // Child 0 (-,-), 1 (+,-), 2 (+,+), 3 (-,+); index 4k + c.
+    for (size_t k = 0; k < nbx; ++k) {
+      cx[j + 1][4 * k + 0] = cx[j][k] - h; cy[j + 1][4 * k + 0] = cy[j][k] - h;
+      cx[j + 1][4 * k + 1] = cx[j][k] + h; cy[j + 1][4 * k + 1] = cy[j][k] - h;
+      cx[j + 1][4 * k + 2] = cx[j][k] + h; cy[j + 1][4 * k + 2] = cy[j][k] + h;
+      cx[j + 1][4 * k + 3] = cx[j][k] - h; cy[j + 1][4 * k + 3] = cy[j][k] + h;
+    }
+  }
+  nCones.push_back((int)(cfg.nCones_LFR * std::pow(2.0, level_LFR - 1)));
+  aperture.push_back(2 * kPi / nCones[0]);
+  for (int j = 1; j <= level_LFR - 1; ++j) {
+    nCones.push_back((int)(nCones[j - 1] / 2.0));
+    aperture.push_back(aperture[j - 1] * 2.0);
+  }
+  for (int k = 0; k < n1; ++k) cheb1.push_back(-std::cos((k + 0.5) / n1 * kPi));
+  const int nleaf = 1 << (2 * nL);
+  N = nleaf * rank;
+  gx_.resize(N);
+  gy_.resize(N);
+  for (int t = 0; t < nleaf; ++t)
+    for (int r = 0; r < n1; ++r)
+      for (int c = 0; c < n1; ++c) {
+        const int i = t * rank + r * n1 + c;
+        gx_[i] = radius[nL] * cheb1[c] + cx[nL][t];
+        gy_[i] = radius[nL] * cheb1[r] + cy[nL][t];
+      }
+  kq_.resize(N);
+  for (int i = 0; i < N; ++i) kq_[i] = kappa * kappa * (contrast_fn(cfg, gx_[i], gy_[i]));
+  for (int d = 0; d < cfg.degreeOfBases; ++d)
+    for (int a = 0; a < d + 1; ++a) bases.push_back({a, d - a});
+  gl_rule(kQuadOrder, gln, glw);
+}
+
+void Builder::precompute() {
+  // Q (rank x nb) at the standard nodes and Q^+ from its QR.
+  std::vector<cd> Q((size_t)rank * nb);
+  const int n1 = cfg.nChebNodes;
+  for (int l = 0; l < nb; ++l)
+    for (int i = 0; i < rank; ++i) {
+      const double xs = cheb1[i % n1], ys = cheb1[i / n1];
+      Q[(size_t)l * rank + i] = cd(cheb_t(xs, bases[l].first) * cheb_t(ys, bases[l].second), 0.0);
+    }
+  PivQR qr;
+  qr.factor(rank, nb, Q);
+  std::vector<double> Qp((size_t)nb * rank);  // Qp[l * rank + i]
+  {
+    std::vector<cd> e(rank), s(nb);
+    for (int i = 0; i < rank; ++i) {
+      std::fill(e.begin(), e.end(), cd(0.0, 0.0));
+      e[i] = 1.0;
+      qr.solve(e.data(), s.data());
+      for (int l = 0; l < nb; ++l) Qp[(size_t)l * rank + i] = s[l].real();
+    }
+  }
+  const int nS = 2 * kSeries + 1;
+  const double rj = radius[nL];
+  // Far moments C (2S+1) x nb, then M = C Q^+ rounded like the text cache.
+  std::vector<cd> C((size_t)nS * nb);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int t = 0; t < nS * nb; ++t) {
+    const int n = t / nb - kSeries, l = t % nb;
+    const int a = bases[l].first, b = bases[l].second;
+    auto f = [&](double x, double y) -> cd {
+      const double R2 = x * x + y * y;
+      const double nx = std::sqrt(R2);
+      const double arg = kappa * rj * nx;
+      const double th = std::atan2(y, x);
+      return bes_j(n, arg) * std::exp(-kI * double(n) * th) * cheb_t(x, a) * cheb_t(y, b);
+    };
+    C[(size_t)(n + kSeries) * nb + l] = rj * rj * quad2d(f, gln, glw);
+  }
+  Mleaf.assign((size_t)nS * rank, cd(0.0, 0.0));
+  for (int n = 0; n < nS; ++n)
+    for (int i = 0; i < rank; ++i) {
+      cd s(0.0, 0.0);
+      for (int l = 0; l < nb; ++l) s += C[(size_t)n * nb + l] * Qp[(size_t)l * rank + i];
+      if (cfg.reference_rounding) s = cd(round6(s.real()), round6(s.imag()));
+      Mleaf[(size_t)i * nS + n] = s;
+    }
+  // Colleague near blocks: V(i,l) = int H0(k r |X_i - P|) T_a T_b dP, then
+  // V (i r^2 / 4) Q^+.
+  static const double ncx[9] = {-2, 0, 2, 2, 2, 0, -2, -2, 0};
+  static const double ncy[9] = {-2, -2, -2, 0, 2, 2, 2, 0, 0};
+  const double rA = radius[nL], rB = radius[nL];
+  std::vector<cd> V((size_t)9 * rank * nb);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int t = 0; t < 9 * rank; ++t) {
+    const int q = t / rank, i = t % rank;
+    const double bx = ncx[q] * rA, by = ncy[q] * rA;
+    const double ax = rA * cheb1[i % n1] + 0.0, ay = rA * cheb1[i / n1] + 0.0;
+    const double Xx = (ax - bx) / rB, Xy = (ay - by) / rB;
+    std::unordered_map<unsigned long long, cd> memo;
+    auto key = [](double a, double b) {
+      unsigned long long ka, kb;
+      std::memcpy(&ka, &a, 8);
+      std::memcpy(&kb, &b, 8);
+      return ka * 0x9E3779B97F4A7C15ULL ^ (kb + 0x632BE59BD9B4E019ULL + (ka << 6) + (ka >> 2));
+    };
+    for (int l = 0; l < nb; ++l) {
+      const int a = bases[l].first, b = bases[l].second;
+      auto f = [&](double x, double y) -> cd {
+        const unsigned long long kk = key(x, y);
+        auto it = memo.find(kk);
+        cd H;
+        if (it != memo.end()) {
+          H = it->second;
+        } else {
+          const double R2 = (Xx - x) * (Xx - x) + (Xy - y) * (Xy - y);
+          const double R = std::sqrt(R2);
+          const double arg = kappa * rB * R;
+          H = bes_j(0, arg) + kI * bes_y(0, arg);
+          memo.emplace(kk, H);
+        }
+        return H * cheb_t(x, a) * cheb_t(y, b);
+      };
+      V[((size_t)q * rank + i) * nb + l] = quad2d(f, gln, glw);
+    }
+  }
+  near.assign((size_t)9 * rank * rank, cd(0.0, 0.0));
+  for (int q = 0; q < 9; ++q)
+    for (int i = 0; i < rank; ++i)
+      for (int c = 0; c < rank; ++c) {
+        cd s(0.0, 0.0);
+        for (int l = 0; l < nb; ++l) {
+          const cd vt = V[((size_t)q * rank + i) * nb + l] * kI * rB * rB / 4.0;
+          s += vt * Qp[(size_t)l * rank + c];
+        }
+        if (cfg.reference_rounding) s = cd(round6(s.real()), round6(s.imag()));
+        near[((size_t)q * rank + i) * rank + c] = s;
+      }
+}
+
+// Interaction lists of the children of every box (assign_Child_Interaction,
+// G_FMM2DTree.hpp:1356-1461). In a uniform tree every neighbour is a
+// same-level box, so lists hold box indices of the same level.
+void Builder::interaction_lists() {
+  const double epsR = std::pow(10, -8);
+  nbrs.assign(nL + 1, {});
+  nodes.assign(nL + 1, {});
+  for (int j = 2; j <= nL; ++j) nodes[j].assign(nodes_at(j), Node());
+  nbrs[1].assign(4, {0, 1, 2, 3});
+  for (int j = 1; j <= nL - 1; ++j) {
+    const int J = j + 1;
+    nbrs[J].assign((size_t)1 << (2 * J), {});
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int k = 0; k < (1 << (2 * j)); ++k) {
+      for (int c = 0; c < 4; ++c) {
+        const int A = 4 * k + c;
+        for (int pn : nbrs[j][k]) {
+          for (int nc = 0; nc < 4; ++nc) {
+            const int B = 4 * pn + nc;
+            const double dx = std::fabs(cx[J][A] - cx[J][B]), dy = std::fabs(cy[J][A] - cy[J][B]);
+            if (J >= level_LFR) {
+              const double lim = 3.0 * radius[J] + radius[J] - epsR;
+              if (dx >= lim || dy >= lim) lfr(J, A).IL.push_back(B);
+              else nbrs[J][A].push_back(B);
+            } else {
+              const double limx = kappa * radius[J] * radius[J] + radius[J] + radius[J] - epsR;
+              const double limy = kappa * radius[J] * radius[J] + radius[J] - epsR;
+              if (dx >= limx || dy >= limy) {
+                double arg = std::atan2(cy[J][A] - cy[J][B], cx[J][A] - cx[J][B]);
+                arg = std::fmod(arg + 2 * kPi + kPi, 2 * kPi);
+                const int cn = int(arg / aperture[J]);
+                cone(J, A, cn).IL.push_back(B);
+              } else {
+                nbrs[J][A].push_back(B);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// Cone of source box `src` (level j) that points at box `dst`
+// (G_FMM2DTree.hpp:2524-2526, 3335-3337, 3863-3865).
+static inline int cone_towards(const std::vector<double>& cxj, const std::vector<double>& cyj, int dst, int src,
+                               double ap) {
+  const double arg = std::atan2(cyj[dst] - cyj[src], cxj[dst] - cxj[src]);
+  const double a = std::fmod(arg + 2 * kPi, 2 * kPi);
+  return int(a / ap);
+}
+
+void Builder::nca_level_lfr(int j) {
+  const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
+  const int nbx = 1 << (2 * j);
+  const bool leaf = (j == nL);
+  // outgoing
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < nbx; ++k) {
+    HCache hc{this, {}};
+    Node& nd = lfr(j, k);
+    std::vector<int> own, far;
+    if (leaf) for (int i = 0; i < rank; ++i) own.push_back(k * rank + i);
+    else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * k + c).out_charge; own.insert(own.end(), v.begin(), v.end()); }
+    for (int b : nd.IL) {
+      if (leaf) for (int i = 0; i < rank; ++i) far.push_back(b * rank + i);
+      else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * b + c).in_check; far.insert(far.end(), v.begin(), v.end()); }
+    }
+    if (!far.empty() && !own.empty()) {
+      nd.out_active = true;
+      std::vector<int> rb, cb;
+      if (aca(far, own, tol, rb, cb, &nd.Ar, hc) > 0) {
+        for (int r : rb) nd.out_check.push_back(far[r]);
+        for (int c : cb) nd.out_charge.push_back(own[c]);
+      }
+    } else {
+      nd.out_active = false;
+      nd.out_charge = own;
+    }
+  }
+  // incoming
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < nbx; ++k) {
+    HCache hc{this, {}};
+    Node& nd = lfr(j, k);
+    std::vector<int> own, far;
+    if (leaf) for (int i = 0; i < rank; ++i) own.push_back(k * rank + i);
+    else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * k + c).in_check; own.insert(own.end(), v.begin(), v.end()); }
+    for (int b : nd.IL) {
+      if (leaf) for (int i = 0; i < rank; ++i) far.push_back(b * rank + i);
+      else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * b + c).out_charge; far.insert(far.end(), v.begin(), v.end()); }
+    }
+    if (!far.empty() && !own.empty()) {
+      nd.in_active = true;
+      std::vector<int> rb, cb;
+      if (aca(own, far, tol, rb, cb, nullptr, hc) > 0) {
+        for (int r : rb) nd.in_check.push_back(own[r]);
+        for (int c : cb) nd.in_charge.push_back(far[c]);
+      }
+    } else {
+      nd.in_active = false;
+      nd.in_check = own;
+    }
+  }
+}
+
+void Builder::nca_level_hfr(int j) {
+  const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
+  const int nbx = 1 << (2 * j), nc = nCones[j];
+  auto gather = [&](int jj, int kk, int cn, bool charges, std::vector<int>& dst) {
+    for (int c = 0; c < 4; ++c) {
+      Node& ch = child_node(jj + 1, 4 * kk + c, cn);
+      const auto& v = charges ? ch.out_charge : ch.in_check;
+      dst.insert(dst.end(), v.begin(), v.end());
+    }
+  };
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int t = 0; t < nbx * nc; ++t) {
+    const int k = t / nc, cn = t % nc;
+    HCache hc{this, {}};
+    Node& nd = cone(j, k, cn);
+    std::vector<int> own, far;
+    gather(j, k, cn, true, own);
+    for (int b : nd.IL) gather(j, b, cone_towards(cx[j], cy[j], k, b, aperture[j]), false, far);
+    if (!far.empty() && !own.empty()) {
+      nd.out_active = true;
+      std::vector<int> rb, cb;
+      if (aca(far, own, tol, rb, cb, &nd.Ar, hc) > 0) {
+        for (int r : rb) nd.out_check.push_back(far[r]);
+        for (int c : cb) nd.out_charge.push_back(own[c]);
+      }
+    } else {
+      nd.out_active = false;
+      nd.out_charge = own;
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int t = 0; t < nbx * nc; ++t) {
+    const int k = t / nc, cn = t % nc;
+    HCache hc{this, {}};
+    Node& nd = cone(j, k, cn);
+    std::vector<int> own, far;
+    gather(j, k, cn, false, own);
+    for (int b : nd.IL) gather(j, b, cone_towards(cx[j], cy[j], k, b, aperture[j]), true, far);
+    if (!far.empty() && !own.empty()) {
+      nd.in_active = true;
+      std::vector<int> rb, cb;
+      if (aca(own, far, tol, rb, cb, nullptr, hc) > 0) {
+        for (int r : rb) nd.in_check.push_back(own[r]);
+        for (int c : cb) nd.in_charge.push_back(far[c]);
+      }
+    } else {
+      nd.in_active = false;
+      nd.in_check = own;
+    }
+  }
+}
+
+void Builder::user_checks() {
+  for (int j = nL; j >= level_LFR; --j)
+    for (int k = 0; k < (1 << (2 * j)); ++k) {
+      Node& nd = lfr(j, k);
+      if (j == nL) {
+        nd.user_check.clear();
+        for (int i = 0; i < rank; ++i) nd.user_check.push_back(k * rank + i);
+      } else if (nd.in_active) {
+        nd.user_check = nd.in_check;
+      } else {
+        for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * k + c).user_check; nd.user_check.insert(nd.user_check.end(), v.begin(), v.end()); }
+      }
+    }
+  for (int j = level_LFR - 1; j >= 2; --j)
+    for (int k = 0; k < (1 << (2 * j)); ++k)
+      for (int cn = 0; cn < nCones[j]; ++cn) {
+        Node& nd = cone(j, k, cn);
+        if (nd.in_active) nd.user_check = nd.in_check;
+        else for (int c = 0; c < 4; ++c) { const auto& v = child_node(j + 1, 4 * k + c, cn).user_check; nd.user_check.insert(nd.user_check.end(), v.begin(), v.end()); }
+      }
+}
+
+// Splits a block into warp items and appends it to a phase.
+static void add_task(GemvPhase& ph, const std::vector<cd>& rowmajor, int rows, int K, const std::vector<int>& idx,
+                     int out_off) {
+  if (rows <= 0 || K <= 0) return;
+  const long long a0 = (long long)ph.A.size();
+  const int i0 = (int)ph.idx.size();
+  ph.idx.insert(ph.idx.end(), idx.begin(), idx.end());
+  if (K >= kColsThreshold) {
+    ph.A.insert(ph.A.end(), rowmajor.begin(), rowmajor.end());
+    for (int r0 = 0; r0 < rows; r0 += kRowsPerItem) {
+      GemvItem it;
+      it.a_off = a0 + (long long)r0 * K;
+      it.idx_off = i0;
+      it.K = K;
+      it.nr = std::min(kRowsPerItem, rows - r0);
+      it.out_off = out_off + r0;
+      it.lda = K;
+      it.layout = 0;
+      ph.items.push_back(it);
+    }
+  } else {
+    // Column major so that a warp reading one column is coalesced.
+    for (int k = 0; k < K; ++k)
+      for (int r = 0; r < rows; ++r) ph.A.push_back(rowmajor[(size_t)r * K + k]);
+    for (int r0 = 0; r0 < rows; r0 += 32) {
+      GemvItem it;
+      it.a_off = a0 + r0;
+      it.idx_off = i0;
+      it.K = K;
+      it.nr = std::min(32, rows - r0);
+      it.out_off = out_off + r0;
+      it.lda = rows;
+      it.layout = 1;
+      ph.items.push_back(it);
+    }
+  }
+}
+
+static void sort_items(GemvPhase& ph) {
+  // Largest items first so that the grid-stride loop balances.
+  std::stable_sort(ph.items.begin(), ph.items.end(), [](const GemvItem& a, const GemvItem& b) {
+    return (long long)a.K * a.nr > (long long)b.K * b.nr;
+  });
+}
+
+void Builder::pack(HostOperator& op) {
+  const int nleaf = 1 << (2 * nL);
+  // ---- charge buffer: x, then own skeleton charges level by level.
+  long long S = N;
+  for (int j = nL; j >= 2; --j) {
+    for (auto& nd : nodes[j])
+      if (nd.out_active && !nd.out_charge.empty()) { nd.own_charge = S; S += (long long)nd.out_charge.size(); }
+  }
+  // f_out gather lists, bottom up.
+  for (int j = nL; j >= 2; --j) {
+    const int nbx = 1 << (2 * j);
+    const int ncn = is_lfr(j) ? 1 : nCones[j];
+    for (int k = 0; k < nbx; ++k)
+      for (int cn = 0; cn < ncn; ++cn) {
+        Node& nd = is_lfr(j) ? lfr(j, k) : cone(j, k, cn);
+        nd.fidx.clear();
+        if (nd.out_active) {
+          for (long long s = 0; s < (long long)nd.out_charge.size(); ++s) nd.fidx.push_back((int)(nd.own_charge + s));
+        } else if (j == nL) {
+          for (int i = 0; i < rank; ++i) nd.fidx.push_back(k * rank + i);
+        } else {
+          for (int c = 0; c < 4; ++c) {
+            const auto& v = child_node(j + 1, 4 * k + c, cn).fidx;
+            nd.fidx.insert(nd.fidx.end(), v.begin(), v.end());
+          }
+        }
+      }
+  }
+  // ---- potential buffer: leaves (N), then every non-leaf node with rows.
+  long long P = N;
+  for (int k = 0; k < nleaf; ++k) lfr(nL, k).pot_off = (long long)k * rank;
+  for (int j = 2; j < nL; ++j)
+    for (auto& nd : nodes[j])
+      if (!nd.user_check.empty()) { nd.pot_off = P; P += (long long)nd.user_check.size(); }
+  op.charges_len = S;
+  op.pots_len = P;
+
+  // ---- upward pass: T = Atilde^{-1} Ar for every node with a skeleton.
+  op.up.clear();
+  for (int j = nL; j >= 2; --j) {
+    GemvPhase ph;
+    const int nn = (int)nodes[j].size();
+    std::vector<std::vector<cd>> T(nn);
+    std::vector<std::vector<int>> src(nn);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < nn; ++t) {
+      Node& nd = nodes[j][t];
+      if (!(nd.out_active && !nd.out_charge.empty())) continue;
+      const int k = is_lfr(j) ? t : t / nCones[j];
+      const int cn = is_lfr(j) ? 0 : t % nCones[j];
+      std::vector<int> s;
+      if (j == nL) for (int i = 0; i < rank; ++i) s.push_back(k * rank + i);
+      else for (int c = 0; c < 4; ++c) { const auto& v = child_node(j + 1, 4 * k + c, cn).fidx; s.insert(s.end(), v.begin(), v.end()); }
+      const int r = (int)nd.out_charge.size(), K = (int)s.size();
+      if (K == 0) continue;
+      HCache hc{this, {}};
+      PivQR qr;
+      qr.factor(r, r, block_colmajor(nd.out_check, nd.out_charge, hc));
+      std::vector<cd> Tm((size_t)r * K), col(r), sol(r);
+      for (int c = 0; c < K; ++c) {
+        for (int a = 0; a < r; ++a) col[a] = nd.Ar[(size_t)a * K + c];
+        qr.solve(col.data(), sol.data());
+        for (int a = 0; a < r; ++a) Tm[(size_t)a * K + c] = sol[a];
+      }
+      T[t] = std::move(Tm);
+      src[t] = std::move(s);
+    }
+    for (int t = 0; t < nn; ++t)
+      if (!T[t].empty())
+        add_task(ph, T[t], (int)nodes[j][t].out_charge.size(), (int)src[t].size(), src[t], (int)nodes[j][t].own_charge);
+    sort_items(ph);
+    op.up.push_back(std::move(ph));
+  }
+
+  // ---- M2L: one task per node with an incoming interaction list.
+  {
+    struct Task { std::vector<cd> A; std::vector<int> idx; int rows = 0, K = 0; long long out = 0; };
+    std::vector<std::pair<int, int>> all;
+    for (int j = 2; j <= nL; ++j)
+      for (int t = 0; t < (int)nodes[j].size(); ++t) all.push_back({j, t});
+    std::vector<Task> tasks(all.size());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int u = 0; u < (int)all.size(); ++u) {
+      const int j = all[u].first, t = all[u].second;
+      Node& nd = nodes[j][t];
+      if (!nd.in_active || nd.user_check.empty()) continue;
+      const int k = is_lfr(j) ? t : t / nCones[j];
+      std::vector<const Node*> srcs;
+      for (int b : nd.IL) {
+        const Node& s = is_lfr(j) ? lfr(j, b) : cone(j, b, cone_towards(cx[j], cy[j], k, b, aperture[j]));
+        if (!s.out_charge.empty()) srcs.push_back(&s);
+      }
+      int K = 0;
+      for (const Node* s : srcs) K += (int)s->out_charge.size();
+      if (K == 0) continue;
+      const int rows = (int)nd.user_check.size();
+      HCache hc{this, {}};
+      Task& tk = tasks[u];
+      tk.A.resize((size_t)rows * K);
+      int c0 = 0;
+      for (const Node* s : srcs) {
+        fill(nd.user_check, s->out_charge, hc, tk.A.data() + c0, K);
+        tk.idx.insert(tk.idx.end(), s->fidx.begin(), s->fidx.end());
+        c0 += (int)s->out_charge.size();
+      }
+      tk.rows = rows;
+      tk.K = K;
+      tk.out = nd.pot_off;
+      nd.pot_nonzero = true;
+    }
+    GemvPhase ph;
+    for (auto& tk : tasks) {
+      if (tk.K == 0) continue;
+      add_task(ph, tk.A, tk.rows, tk.K, tk.idx, (int)tk.out);
+      std::vector<cd>().swap(tk.A);
+    }
+    sort_items(ph);
+    op.m2l = std::move(ph);
+  }
+
+  // ---- downward pass: child pulls W = L2L Atilde^{-1} (or a slice when the
+  // parent is a pass-through), parents in cone order.
+  op.down.clear();
+  for (int j = 2; j < nL; ++j) {
+    const int J = j + 1;
+    // QR of Atilde^T for every IL-active parent. W = L2L Atilde^{-1} is
+    // formed row by row by solving Atilde^T w^T = l^T: the rounding error of
+    // each row then lies along left singular vectors of Atilde with small
+    // singular values, which the parent's potential (in the range of
+    // Atilde) does not excite. An explicit inverse would not have this
+    // property and loses ~eps * cond(Atilde) in the product.
+    const int np = (int)nodes[j].size();
+    std::vector<PivQR> AT(np);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < np; ++t) {
+      Node& p = nodes[j][t];
+      if (!(p.in_active && !p.in_charge.empty() && p.pot_nonzero)) continue;
+      HCache hc{this, {}};
+      const int r = (int)p.in_charge.size();
+      const std::vector<cd> A = block_colmajor(p.in_check, p.in_charge, hc);
+      std::vector<cd> At((size_t)r * r);
+      for (int a = 0; a < r; ++a)
+        for (int c = 0; c < r; ++c) At[(size_t)c * r + a] = A[(size_t)a * r + c];  // At(a,c) = A(c,a)
+      AT[t].factor(r, r, At);
+    }
+    const int nch = (int)nodes[J].size();
+    struct Task { std::vector<cd> A; std::vector<int> idx; int rows = 0, K = 0; long long out = 0; bool any = false; };
+    std::vector<Task> tasks(nch);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int t = 0; t < nch; ++t) {
+      Node& X = nodes[J][t];
+      const int rows = (int)X.user_check.size();
+      if (rows == 0) continue;
+      const int kc = is_lfr(J) ? t : t / nCones[J];
+      const int cc = is_lfr(J) ? 0 : t % nCones[J];
+      const int kp = kc / 4, child = kc % 4;
+      std::vector<int> pcones;
+      if (is_lfr(j)) pcones.push_back(-1);
+      else for (int pc = 0; pc < nCones[j]; ++pc) if (is_lfr(J) || pc / 2 == cc) pcones.push_back(pc);
+      HCache hc{this, {}};
+      Task& tk = tasks[t];
+      std::vector<std::vector<cd>> cols_blocks;  // per term, row-major rows x w
+      std::vector<int> widths;
+      for (int pc : pcones) {
+        const int pt = (pc < 0) ? kp : kp * nCones[j] + pc;
+        Node& p = nodes[j][pt];
+        if (!p.pot_nonzero) continue;
+        if (p.in_active) {
+          if (p.in_charge.empty()) continue;
+          const int r = (int)p.in_charge.size();
+          std::vector<cd> Lb((size_t)rows * r);
+          fill(X.user_check, p.in_charge, hc, Lb.data(), r);
+          std::vector<cd> W((size_t)rows * r, cd(0.0, 0.0));
+          for (int a = 0; a < rows; ++a) AT[pt].solve(&Lb[(size_t)a * r], &W[(size_t)a * r]);
+          cols_blocks.push_back(std::move(W));
+          widths.push_back(r);
+          for (int m = 0; m < r; ++m) tk.idx.push_back((int)(p.pot_off + m));
+        } else {
+          // Pass-through: slice of the parent's potential for this child.
+          int off = 0;
+          for (int c = 0; c < child; ++c) off += (int)child_node(J, 4 * kp + c, pc < 0 ? 0 : pc).user_check.size();
+          std::vector<cd> Id((size_t)rows * rows, cd(0.0, 0.0));
+          for (int a = 0; a < rows; ++a) Id[(size_t)a * rows + a] = 1.0;
+          cols_blocks.push_back(std::move(Id));
+          widths.push_back(rows);
+          for (int m = 0; m < rows; ++m) tk.idx.push_back((int)(p.pot_off + off + m));
+        }
+      }
+      int K = 0;
+      for (int w : widths) K += w;
+      if (K == 0) continue;
+      tk.A.assign((size_t)rows * K, cd(0.0, 0.0));
+      int c0 = 0;
+      for (size_t b = 0; b < cols_blocks.size(); ++b) {
+        for (int a = 0; a < rows; ++a)
+          for (int c = 0; c < widths[b]; ++c) tk.A[(size_t)a * K + c0 + c] = cols_blocks[b][(size_t)a * widths[b] + c];
+        c0 += widths[b];
+      }
+      tk.rows = rows;
+      tk.K = K;
+      tk.out = X.pot_off;
+      tk.any = true;
+    }
+    GemvPhase ph;
+    ph.accumulate = 1;
+    for (int t = 0; t < nch; ++t) {
+      if (!tasks[t].any) continue;
+      nodes[J][t].pot_nonzero = true;
+      add_task(ph, tasks[t].A, tasks[t].rows, tasks[t].K, tasks[t].idx, (int)tasks[t].out);
+      std::vector<cd>().swap(tasks[t].A);
+    }
+    sort_items(ph);
+    op.down.push_back(std::move(ph));
+  }
+}
+
+bool Builder::run(HostOperator& op, std::string& err) {
+  const auto t0 = std::chrono::steady_clock::now();
+  if (cfg.nLevelsUniform < 2 || cfg.nLevelsUniform > 10) { err = "nLevelsUniform must be in [2, 10]"; return false; }
+  if (cfg.nChebNodes < 2 || cfg.nChebNodes > 8) { err = "nChebNodes must be in [2, 8]"; return false; }
+  if (cfg.degreeOfBases < 1 || cfg.degreeOfBases * (cfg.degreeOfBases + 1) / 2 > cfg.nChebNodes * cfg.nChebNodes) {
+    err = "degreeOfBases gives more basis polynomials than nodes"; return false;
+  }
+  if (!(cfg.L > 0.0) || !(cfg.kappa >= 0.0)) { err = "L must be > 0 and kappa >= 0"; return false; }
+  if (cfg.Qchoice < 0 || cfg.Qchoice > 6) { err = "Qchoice must be in [0, 6]"; return false; }
+  if (cfg.Qchoice == 6 && (cfg.n_bumps < 1 || cfg.n_bumps > LS_MAX_BUMPS)) { err = "n_bumps must be in [1, 8]"; return false; }
+  if (cfg.nCones_LFR < 1 || cfg.TOL_POW < 1 || cfg.TOL_POW > 16) { err = "nCones_LFR >= 1 and TOL_POW in [1, 16] required"; return false; }
+  if ((long long)(1LL << (2 * cfg.nLevelsUniform)) * cfg.nChebNodes * cfg.nChebNodes > (1LL << 28)) { err = "problem too large"; return false; }
+  geometry();
+  precompute();
+  interaction_lists();
+  for (int j = nL; j >= level_LFR; --j) nca_level_lfr(j);
+  for (int j = level_LFR - 1; j >= 2; --j) nca_level_hfr(j);
+  user_checks();
+  pack(op);
+  // Operator-level data for the near field and the C ABI.
+  op.cfg = cfg;
+  op.N = N;
+  op.n_leaves = 1 << (2 * nL);
+  op.rank = rank;
+  op.n_levels = nL;
+  op.level_LFR = level_LFR;
+  op.n_bases = nb;
+  op.px = gx_;
+  op.py = gy_;
+  op.q.resize(N);
+  for (int i = 0; i < N; ++i) op.q[i] = contrast_fn(cfg, gx_[i], gy_[i]);
+  op.kq = kq_;
+  op.nearB = near;
+  op.M.assign((size_t)rank * (2 * kSeries + 1), cd());
+  for (size_t i = 0; i < op.M.size(); ++i) op.M[i] = Mleaf[i];
+  // Colleague table of the leaves (getNeighbors, G_FMM2DTree.hpp:1567-1601):
+  // slot n <-> offset of N_centers[n] / 2 in box units.
+  static const int ox[9] = {-1, 0, 1, 1, 1, 0, -1, -1, 0};
+  static const int oy[9] = {-1, -1, -1, 0, 1, 1, 1, 0, 0};
+  const int nleaf = op.n_leaves;
+  op.colleague.assign((size_t)nleaf * 9, -1);
+  {
+    // grid coordinates of each leaf from its centre
+    const double w = 2.0 * radius[nL];
+    std::unordered_map<long long, int> at;
+    auto gidx = [&](double x, double y) { return std::llround((x + L) / w - 0.5) * 4194304LL + std::llround((y + L) / w - 0.5); };
+    for (int t = 0; t < nleaf; ++t) at[gidx(cx[nL][t], cy[nL][t])] = t;
+    for (int t = 0; t < nleaf; ++t) {
+      const long long gxi = std::llround((cx[nL][t] + L) / w - 0.5), gyi = std::llround((cy[nL][t] + L) / w - 0.5);
+      for (int q = 0; q < 9; ++q) {
+        auto it = at.find((gxi + ox[q]) * 4194304LL + (gyi + oy[q]));
+        if (it != at.end()) op.colleague[(size_t)t * 9 + q] = it->second;
+      }
+    }
+  }
+  // Skeleton dump (same record format as the CPU oracle).
+  op.skeleton_dump.clear();
+  int mr = 0;
+  auto put = [&](int v) { op.skeleton_dump.push_back(v); };
+  auto putv = [&](const std::vector<int>& v) { put((int)v.size()); for (int x : v) put(x); };
+  for (int j = 2; j <= nL; ++j)
+    for (int k = 0; k < (1 << (2 * j)); ++k) {
+      const int ncn = is_lfr(j) ? 1 : nCones[j];
+      for (int cn = 0; cn < ncn; ++cn) {
+        const Node& nd = is_lfr(j) ? lfr(j, k) : cone(j, k, cn);
+        put(j); put(k); put(is_lfr(j) ? -1 : cn); put(nd.out_active); put(nd.in_active);
+        putv(nd.out_charge); putv(nd.out_check); putv(nd.in_charge); putv(nd.in_check); putv(nd.user_check);
+        if (nd.out_active) mr = std::max(mr, (int)nd.out_charge.size());
+        if (nd.in_active) mr = std::max(mr, (int)nd.in_charge.size());
+      }
+    }
+  op.max_rank = mr;
+  op.assemble_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return true;
+}
+
+}  // namespace
+
+bool assemble(const ls_config& cfg, HostOperator& op, std::string& err) {
+  try {
+    Builder b(cfg);
+    return b.run(op, err);
+  } catch (const std::bad_alloc&) {
+    err = "host allocation failed during assembly";
+    return false;
+  } catch (const std::exception& e) {
+    err = std::string("assembly failed: ") + e.what();
+    return false;
+  }
+}
+
+}  // namespace lsg

@@ -1,0 +1,309 @@
+// extern "C" entry points of liblsdafmm.so (declared in include/ls_dafmm.h).
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "device.h"
+#include "ls_internal.h"
+
+struct ls_op {
+  lsg::HostOperator host;
+  lsg::DevOperator dev;
+  bool on_device = false;  // false: assembled on the host only (device < 0)
+};
+
+namespace lsg {
+static thread_local std::string t_last_error;
+void set_error(const std::string& msg) { t_last_error = msg; }
+}  // namespace lsg
+
+using namespace lsg;
+
+namespace {
+
+ls_status fail(ls_status code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+ls_status cuda_fail(cudaError_t e, const char* where) {
+  return fail(LS_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+extern "C" {
+
+ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
+  if (!cfg || !out) return fail(LS_E_INVALID, "ls_op_create: null argument");
+  *out = nullptr;
+  if (device >= 0) {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(LS_E_CUDA, "ls_op_create: no CUDA device available");
+    if (device >= ndev) return fail(LS_E_INVALID, "ls_op_create: device index out of range");
+  }
+  ls_op* op = new (std::nothrow) ls_op();
+  if (!op) return fail(LS_E_NOMEM, "ls_op_create: out of host memory");
+  std::string err;
+  if (!assemble(*cfg, op->host, err)) {
+    delete op;
+    return fail(LS_E_INVALID, "ls_op_create: " + err);
+  }
+  if (device < 0) {  // inspection only: skeletons, precomputations, geometry
+    *out = op;
+    return LS_OK;
+  }
+  op->on_device = true;
+  op->dev.device = device;
+  if (!dev_upload(op->host, op->dev, err)) {
+    dev_free(op->dev);
+    delete op;
+    return fail(LS_E_CUDA, "ls_op_create: " + err);
+  }
+  // Host copies of the blocks are no longer needed.
+  for (auto& p : op->host.up) { std::vector<cd>().swap(p.A); }
+  for (auto& p : op->host.down) { std::vector<cd>().swap(p.A); }
+  std::vector<cd>().swap(op->host.m2l.A);
+  *out = op;
+  return LS_OK;
+}
+
+ls_status ls_op_destroy(ls_op* op) {
+  if (!op) return LS_OK;
+  if (op->on_device) dev_free(op->dev);
+  delete op;
+  return LS_OK;
+}
+
+ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
+  if (!op || !o) return fail(LS_E_INVALID, "ls_op_info: null argument");
+  const HostOperator& h = op->host;
+  const DevOperator& d = op->dev;
+  std::memset(o, 0, sizeof(*o));
+  o->N = h.N;
+  o->n_leaves = h.n_leaves;
+  o->n_levels = h.n_levels;
+  o->level_LFR = h.level_LFR;
+  o->rank = h.rank;
+  long long far = 0;
+  if (op->on_device) {
+    for (auto& p : d.up) far += p.entries;
+    far += d.m2l.entries;
+    for (auto& p : d.down) far += p.entries;
+  } else {
+    for (auto& p : h.up) far += p.entries();
+    far += h.m2l.entries();
+    for (auto& p : h.down) far += p.entries();
+  }
+  o->far_entries = far;
+  o->near_entries = 9LL * h.rank * h.rank;
+  // Algorithmic bytes of one FP64 matvec: every far block once, the shared
+  // near blocks once, x read and y written once, every skeleton charge and
+  // potential written and read once, kappa^2 q read once.
+  const long long sk = (h.charges_len - h.N) + (h.pots_len - h.N);
+  o->matvec_bytes = 16LL * far + 16LL * o->near_entries + 16LL * 2 * h.N + 16LL * 2 * sk + 8LL * h.N;
+  long long nnz_near = 0;
+  for (int t = 0; t < h.n_leaves; ++t)
+    for (int q = 0; q < 9; ++q) nnz_near += h.colleague[(size_t)t * 9 + q] >= 0;
+  o->matvec_flops = 8LL * far + 8LL * nnz_near * h.rank * h.rank;
+  o->device_bytes = d.device_bytes;
+  o->assemble_seconds = h.assemble_seconds;
+  o->max_rank = h.max_rank;
+  o->n_kernels_per_matvec = d.launches_per_matvec;
+  return LS_OK;
+}
+
+ls_status ls_op_points(const ls_op* op, double* xy) {
+  if (!op || !xy) return fail(LS_E_INVALID, "ls_op_points: null argument");
+  for (int i = 0; i < op->host.N; ++i) { xy[2 * i] = op->host.px[i]; xy[2 * i + 1] = op->host.py[i]; }
+  return LS_OK;
+}
+
+ls_status ls_op_contrast(const ls_op* op, double* q) {
+  if (!op || !q) return fail(LS_E_INVALID, "ls_op_contrast: null argument");
+  std::memcpy(q, op->host.q.data(), sizeof(double) * op->host.N);
+  return LS_OK;
+}
+
+ls_status ls_op_rhs(const ls_op* op, double* b) {
+  if (!op || !b) return fail(LS_E_INVALID, "ls_op_rhs: null argument");
+  const HostOperator& h = op->host;
+  const double k = h.cfg.kappa;
+  for (int i = 0; i < h.N; ++i) {
+    const cd inc = std::exp(cd(0.0, 1.0) * k * h.px[i]);
+    const cd v = -1.0 * k * k * h.q[i] * inc;
+    b[2 * i] = v.real();
+    b[2 * i + 1] = v.imag();
+  }
+  return LS_OK;
+}
+
+ls_status ls_matvec(ls_op* op, const double* x, double* y, void* stream) {
+  if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_matvec: operator was assembled without a device");
+  cudaError_t e = dev_matvec(op->dev, (const double2*)x, (double2*)y, (cudaStream_t)stream, false);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_matvec");
+  return LS_OK;
+}
+
+ls_status ls_op_enable_f32(ls_op* op) {
+  if (!op) return fail(LS_E_INVALID, "ls_op_enable_f32: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_op_enable_f32: operator was assembled without a device");
+  std::string err;
+  if (!dev_enable_f32(op->dev, err)) return fail(LS_E_CUDA, "ls_op_enable_f32: " + err);
+  return LS_OK;
+}
+
+ls_status ls_matvec_f32(ls_op* op, const double* x, double* y, void* stream) {
+  if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_f32: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_f32: operator was assembled without a device");
+  if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_matvec_f32: call ls_op_enable_f32 first");
+  cudaError_t e = dev_matvec_f32(op->dev, (const double2*)x, (double2*)y, (cudaStream_t)stream, false);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_f32");
+  return LS_OK;
+}
+
+ls_status ls_matvec_host(ls_op* op, const double* x, double* y) {
+  if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_host: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_host: operator was assembled without a device");
+  DevOperator& d = op->dev;
+  cudaSetDevice(d.device);
+  const size_t bytes = (size_t)d.N * sizeof(double2);
+  cudaError_t e = cudaMemcpyAsync(d.xbuf, x, bytes, cudaMemcpyHostToDevice, d.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_host H2D");
+  if ((e = dev_matvec(d, d.xbuf, d.ybuf, d.stream, false)) != cudaSuccess) return cuda_fail(e, "ls_matvec_host");
+  if ((e = cudaMemcpyAsync(y, d.ybuf, bytes, cudaMemcpyDeviceToHost, d.stream)) != cudaSuccess)
+    return cuda_fail(e, "ls_matvec_host D2H");
+  if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_matvec_host sync");
+  return LS_OK;
+}
+
+ls_status ls_gmres(ls_op* op, const double* b, int max_iter, double tol, double* x, double* history, int* n_iter,
+                   double* rel_residual) {
+  if (!op || !b || !x) return fail(LS_E_INVALID, "ls_gmres: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_gmres: operator was assembled without a device");
+  if (max_iter < 1) return fail(LS_E_INVALID, "ls_gmres: max_iter must be >= 1");
+  DevOperator& d = op->dev;
+  cudaSetDevice(d.device);
+  const size_t bytes = (size_t)d.N * sizeof(double2);
+  cudaError_t e = cudaMemcpyAsync(d.xbuf, b, bytes, cudaMemcpyHostToDevice, d.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_gmres H2D");
+  std::vector<double> hist;
+  GmresResult res;
+  if ((e = dev_gmres(d, d.xbuf, d.ybuf, max_iter, tol, hist, res, false)) != cudaSuccess)
+    return cuda_fail(e, "ls_gmres");
+  if ((e = cudaMemcpyAsync(x, d.ybuf, bytes, cudaMemcpyDeviceToHost, d.stream)) != cudaSuccess)
+    return cuda_fail(e, "ls_gmres D2H");
+  if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_gmres sync");
+  if (history) for (size_t i = 0; i < hist.size() && i <= (size_t)max_iter; ++i) history[i] = hist[i];
+  if (n_iter) *n_iter = res.iters;
+  if (rel_residual) *rel_residual = res.rel_residual;
+  if (!res.converged) return fail(LS_E_NOT_CONVERGED, "ls_gmres: tolerance not reached within max_iter");
+  return LS_OK;
+}
+
+ls_status ls_gmres_restarted(ls_op* op, const double* b, int m, int restarts, double* x) {
+  if (!op || !b || !x) return fail(LS_E_INVALID, "ls_gmres_restarted: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_gmres_restarted: operator was assembled without a device");
+  if (m < 1 || restarts < 1) return fail(LS_E_INVALID, "ls_gmres_restarted: m and restarts must be >= 1");
+  DevOperator& d = op->dev;
+  cudaSetDevice(d.device);
+  const size_t bytes = (size_t)d.N * sizeof(double2);
+  cudaError_t e = cudaMemcpyAsync(d.xbuf, b, bytes, cudaMemcpyHostToDevice, d.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_gmres_restarted H2D");
+  if ((e = dev_gmres_restarted(d, d.xbuf, d.ybuf, m, restarts)) != cudaSuccess) return cuda_fail(e, "ls_gmres_restarted");
+  if ((e = cudaMemcpyAsync(x, d.ybuf, bytes, cudaMemcpyDeviceToHost, d.stream)) != cudaSuccess)
+    return cuda_fail(e, "ls_gmres_restarted D2H");
+  if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_gmres_restarted sync");
+  return LS_OK;
+}
+
+ls_status ls_gmres_mixed(ls_op* op, const double* b, int max_outer, int inner_iter, double tol, double* x,
+                         double* history, int* n_matvec, double* rel_residual) {
+  if (!op || !b || !x) return fail(LS_E_INVALID, "ls_gmres_mixed: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_gmres_mixed: operator was assembled without a device");
+  if (max_outer < 1 || inner_iter < 1) return fail(LS_E_INVALID, "ls_gmres_mixed: iteration counts must be >= 1");
+  if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_gmres_mixed: call ls_op_enable_f32 first");
+  DevOperator& d = op->dev;
+  cudaSetDevice(d.device);
+  const size_t bytes = (size_t)d.N * sizeof(double2);
+  cudaError_t e = cudaMemcpyAsync(d.xbuf, b, bytes, cudaMemcpyHostToDevice, d.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_gmres_mixed H2D");
+  std::vector<double> hist;
+  int nmv = 0;
+  double rr = 1.0;
+  if ((e = dev_gmres_mixed(d, d.xbuf, d.ybuf, max_outer, inner_iter, tol, hist, nmv, rr)) != cudaSuccess)
+    return cuda_fail(e, "ls_gmres_mixed");
+  if ((e = cudaMemcpyAsync(x, d.ybuf, bytes, cudaMemcpyDeviceToHost, d.stream)) != cudaSuccess)
+    return cuda_fail(e, "ls_gmres_mixed D2H");
+  if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_gmres_mixed sync");
+  if (history) for (size_t i = 0; i < hist.size() && i <= (size_t)max_outer; ++i) history[i] = hist[i];
+  if (n_matvec) *n_matvec = nmv;
+  if (rel_residual) *rel_residual = rr;
+  if (rr > tol) return fail(LS_E_NOT_CONVERGED, "ls_gmres_mixed: tolerance not reached");
+  return LS_OK;
+}
+
+ls_status ls_time_matvec(ls_op* op, int precision, int warmup, int iters, float* ms_matvec, float* ms_m2l) {
+  if (!op || iters < 1 || warmup < 0) return fail(LS_E_INVALID, "ls_time_matvec: bad argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_time_matvec: operator was assembled without a device");
+  DevOperator& d = op->dev;
+  if (precision == LS_PREC_F32 && !d.has_f32) return fail(LS_E_STATE, "ls_time_matvec: FP32 operator not enabled");
+  cudaSetDevice(d.device);
+  const bool f32 = precision == LS_PREC_F32;
+  cudaError_t e;
+  for (int i = 0; i < warmup; ++i) {
+    e = f32 ? dev_matvec_f32(d, d.xbuf, d.ybuf, d.stream, false) : dev_matvec(d, d.xbuf, d.ybuf, d.stream, false);
+    if (e != cudaSuccess) return cuda_fail(e, "ls_time_matvec warmup");
+  }
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_time_matvec sync");
+  float m2l_total = 0.0f;
+  float total = 0.0f;
+  for (int i = 0; i < iters; ++i) {
+    cudaEventRecord(a, d.stream);
+    e = f32 ? dev_matvec_f32(d, d.xbuf, d.ybuf, d.stream, true) : dev_matvec(d, d.xbuf, d.ybuf, d.stream, true);
+    if (e != cudaSuccess) return cuda_fail(e, "ls_time_matvec");
+    cudaEventRecord(b, d.stream);
+    if ((e = cudaEventSynchronize(b)) != cudaSuccess) return cuda_fail(e, "ls_time_matvec event");
+    float t = 0.0f, tm = 0.0f;
+    cudaEventElapsedTime(&t, a, b);
+    cudaEventElapsedTime(&tm, f32 ? d.ev[2] : d.ev[0], f32 ? d.ev[3] : d.ev[1]);
+    total += t;
+    m2l_total += tm;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (ms_matvec) *ms_matvec = total / iters;
+  if (ms_m2l) *ms_m2l = m2l_total / iters;
+  return LS_OK;
+}
+
+long ls_op_skeleton_dump(const ls_op* op, int* buf, long cap) {
+  if (!op) return -1;
+  const auto& v = op->host.skeleton_dump;
+  if (buf) {
+    const long n = std::min<long>(cap, (long)v.size());
+    std::memcpy(buf, v.data(), sizeof(int) * n);
+  }
+  return (long)v.size();
+}
+
+ls_status ls_op_precomputations(const ls_op* op, double* M, double* near) {
+  if (!op) return fail(LS_E_INVALID, "ls_op_precomputations: null argument");
+  if (M) std::memcpy(M, op->host.M.data(), op->host.M.size() * sizeof(cd));
+  if (near) std::memcpy(near, op->host.nearB.data(), op->host.nearB.size() * sizeof(cd));
+  return LS_OK;
+}
+
+const char* ls_last_error(void) { return t_last_error.c_str(); }
+const char* ls_version(void) { return "lsdafmm-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

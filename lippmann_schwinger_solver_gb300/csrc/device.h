@@ -1,0 +1,75 @@
+// Device-side operator state shared by matvec.cu, gmres.cu and capi.cpp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "ls_internal.h"
+
+namespace lsg {
+
+// One phase of gather-GEMV items resident on the device.
+template <class C>
+struct DevPhase {
+  C* A = nullptr;            // blocks (double2 or float2)
+  int* idx = nullptr;        // gather indices
+  GemvItem* items = nullptr;
+  int n_items = 0;
+  int accumulate = 0;
+  long long entries = 0;
+};
+
+struct DevOperator {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int N = 0, n_leaves = 0, rank = 0;
+  int find_phi = 1;
+  long long charges_len = 0, pots_len = 0;
+  // FP64 operator
+  std::vector<DevPhase<double2>> up, down;
+  DevPhase<double2> m2l;
+  double2* S = nullptr;      // charges: x then skeleton charges
+  double2* P = nullptr;      // potentials: leaves then skeleton potentials
+  double2* nearB = nullptr;  // 9 x rank x rank
+  double* kq = nullptr;      // kappa^2 q at the grid points
+  int* colleague = nullptr;  // n_leaves x 9
+  // FP32 operator (mixed precision), built on request
+  bool has_f32 = false;
+  std::vector<DevPhase<float2>> up32, down32;
+  DevPhase<float2> m2l32;
+  float2* S32 = nullptr;
+  float2* P32 = nullptr;
+  float2* nearB32 = nullptr;
+  float* kq32 = nullptr;
+  // scratch device vectors (N complex) for host-buffer calls
+  double2* xbuf = nullptr;
+  double2* ybuf = nullptr;
+  // events for phase timing
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  long long device_bytes = 0;
+  int launches_per_matvec = 0;
+};
+
+// matvec.cu
+bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err);
+void dev_free(DevOperator& d);
+bool dev_enable_f32(DevOperator& d, std::string& err);
+// y = A x; x, y device pointers (N complex). mark_m2l: record events around M2L.
+cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
+cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
+
+// gmres.cu
+struct GmresResult {
+  int iters = 0;
+  double rel_residual = 0.0;
+  bool converged = false;
+};
+cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter, double tol,
+                      std::vector<double>& hist, GmresResult& res, bool use_f32);
+cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, int m, int restarts);
+cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner,
+                            double tol, std::vector<double>& hist, int& n_matvec, double& relres);
+
+}  // namespace lsg

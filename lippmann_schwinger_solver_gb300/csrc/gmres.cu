@@ -1,0 +1,349 @@
+// GMRES driven by the device DAFMM matvec.
+//
+// The Krylov basis V (N x (m+1), column major) and all O(N) work live on
+// the device. Orthogonalisation is classical Gram-Schmidt applied twice
+// (CGS2): each pass is one multi-dot kernel (V^H w, deterministic
+// two-stage reduction) and one update kernel (w -= V h). The tiny
+// Hessenberg / Givens algebra runs on the host in FP64.
+//
+// Reference behaviour restated:
+//  * classGMRES::gmres (GMRES_Hybrid/include/gmres.hpp:54-119): x0 = 0,
+//    Givens-updated residual estimate |beta_{k+1}| / |b|, stop when it
+//    drops to the threshold; here with the conjugate-linear inner product
+//    and unitary complex rotations.
+//  * GMRES / RestartedGMRES (GMRES/GMRES.cpp:257-319): fixed m, early exit
+//    when H(j+1,j) < 1e-8, least squares on the (j+1) x j Hessenberg.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "device.h"
+
+namespace lsg {
+
+namespace {
+
+constexpr int kDotThreads = 256;
+constexpr int kDotBlocks = 240;  // partial sums per column
+
+// partial[col * gridDim.x + block] = sum_{rows in block} conj(V[row, col]) * w[row]
+__global__ void __launch_bounds__(kDotThreads) multidot_kernel(const double2* __restrict__ V, long long ldv,
+                                                               const double2* __restrict__ w, int n,
+                                                               double2* __restrict__ partial) {
+  const int col = blockIdx.y;
+  const double2* __restrict__ v = V + (size_t)col * ldv;
+  double sr = 0.0, si = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 a = v[i], b = w[i];
+    sr = fma(a.x, b.x, sr);
+    sr = fma(a.y, b.y, sr);
+    si = fma(a.x, b.y, si);
+    si = fma(-a.y, b.x, si);
+  }
+  __shared__ double shr[kDotThreads / 32], shi[kDotThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    si += __shfl_xor_sync(0xffffffffu, si, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { shr[wid] = sr; shi[wid] = si; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < kDotThreads / 32; ++k) { a += shr[k]; b += shi[k]; }
+    partial[(size_t)col * gridDim.x + blockIdx.x] = make_double2(a, b);
+  }
+}
+
+// out[col] (+)= sum_b partial[col * nb + b], fixed order.
+__global__ void reduce_partials_kernel(const double2* __restrict__ partial, int nb, int ncols,
+                                       double2* __restrict__ out, int accumulate) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncols) return;
+  double a = 0.0, b = 0.0;
+  for (int k = 0; k < nb; ++k) {
+    const double2 p = partial[(size_t)col * nb + k];
+    a += p.x;
+    b += p.y;
+  }
+  if (accumulate) { out[col].x += a; out[col].y += b; }
+  else out[col] = make_double2(a, b);
+}
+
+// w[i] += sign * sum_c V[i, c] * h[c]
+__global__ void __launch_bounds__(256) multi_axpy_kernel(double2* __restrict__ w, const double2* __restrict__ V,
+                                                         long long ldv, int ncols, const double2* __restrict__ h,
+                                                         int n, double sign) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double sr = 0.0, si = 0.0;
+    for (int c = 0; c < ncols; ++c) {
+      const double2 v = V[(size_t)c * ldv + i];
+      const double2 hc = h[c];
+      sr = fma(v.x, hc.x, sr);
+      sr = fma(-v.y, hc.y, sr);
+      si = fma(v.x, hc.y, si);
+      si = fma(v.y, hc.x, si);
+    }
+    double2 o = w[i];
+    o.x += sign * sr;
+    o.y += sign * si;
+    w[i] = o;
+  }
+}
+
+__global__ void scale_kernel(const double2* __restrict__ a, double2* __restrict__ b, double s, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = make_double2(a[i].x * s, a[i].y * s);
+}
+
+__global__ void sub_kernel(const double2* __restrict__ a, const double2* __restrict__ b, double2* __restrict__ c, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    c[i] = make_double2(a[i].x - b[i].x, a[i].y - b[i].y);
+}
+
+__global__ void add_inplace_kernel(double2* __restrict__ a, const double2* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    a[i].x += b[i].x;
+    a[i].y += b[i].y;
+  }
+}
+
+using cdh = std::complex<double>;
+
+struct Workspace {
+  double2* V = nullptr;
+  double2* w = nullptr;
+  double2* r = nullptr;
+  double2* partial = nullptr;
+  double2* h = nullptr;
+  int cap = 0;
+  ~Workspace() {
+    cudaFree(V); cudaFree(w); cudaFree(r); cudaFree(partial); cudaFree(h);
+  }
+  cudaError_t alloc(int n, int m) {
+    cap = m;
+    cudaError_t e;
+    if ((e = cudaMalloc(&V, (size_t)n * (m + 1) * sizeof(double2))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&w, (size_t)n * sizeof(double2))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&r, (size_t)n * sizeof(double2))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&partial, (size_t)kDotBlocks * (m + 2) * sizeof(double2))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&h, (size_t)(m + 2) * sizeof(double2))) != cudaSuccess) return e;
+    return cudaSuccess;
+  }
+};
+
+int grid_for(int n) { return std::min((n + 255) / 256, 152 * 8); }
+
+// h_dev[0:ncols) = V[:, 0:ncols)^H w
+void multidot(const double2* V, long long ldv, int ncols, const double2* w, int n, double2* partial, double2* h_dev,
+              int accumulate, cudaStream_t s) {
+  dim3 g(kDotBlocks, ncols);
+  multidot_kernel<<<g, kDotThreads, 0, s>>>(V, ldv, w, n, partial);
+  reduce_partials_kernel<<<(ncols + 127) / 128, 128, 0, s>>>(partial, kDotBlocks, ncols, h_dev, accumulate);
+}
+
+cudaError_t vnorm(const double2* w, int n, double2* partial, double2* h_dev, cudaStream_t s, double& out) {
+  multidot(w, n, 1, w, n, partial, h_dev, 0, s);
+  double2 hv;
+  cudaError_t e = cudaMemcpyAsync(&hv, h_dev, sizeof(double2), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+  out = std::sqrt(hv.x);
+  return cudaSuccess;
+}
+
+cudaError_t apply(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool f32) {
+  return f32 ? dev_matvec_f32(d, x, y, s, false) : dev_matvec(d, x, y, s, false);
+}
+
+// One Arnoldi cycle from x0 (device, may be null for x0 = 0). Writes the
+// updated solution into x. tol < 0 disables the residual stop; breakdown
+// exits when H(k+1,k) < brk.
+cudaError_t arnoldi_cycle(DevOperator& d, Workspace& ws, const double2* b, const double2* x0, double2* x, int m,
+                          double tol, double brk, double bnorm, std::vector<double>* hist, int& iters,
+                          bool& converged, bool f32) {
+  cudaStream_t s = d.stream;
+  const int n = d.N;
+  cudaError_t e;
+  // r = b - A x0
+  if (x0) {
+    if ((e = apply(d, x0, ws.w, s, f32)) != cudaSuccess) return e;
+    sub_kernel<<<grid_for(n), 256, 0, s>>>(b, ws.w, ws.r, n);
+  } else {
+    cudaMemcpyAsync(ws.r, b, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+  }
+  double beta = 0.0;
+  if ((e = vnorm(ws.r, n, ws.partial, ws.h, s, beta)) != cudaSuccess) return e;
+  if (hist && hist->empty()) hist->push_back(beta / bnorm);
+  converged = false;
+  iters = 0;
+  if (beta == 0.0) {
+    if (x != x0) {
+      if (x0) cudaMemcpyAsync(x, x0, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+      else cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), s);
+    }
+    converged = true;
+    return cudaStreamSynchronize(s);
+  }
+  scale_kernel<<<grid_for(n), 256, 0, s>>>(ws.r, ws.V, 1.0 / beta, n);
+  std::vector<std::vector<cdh>> H;  // columns, already rotated
+  std::vector<cdh> cs, sn, g(1, cdh(beta, 0.0));
+  std::vector<double2> hbuf(m + 2);
+  int K = 0;
+  for (int k = 0; k < m; ++k) {
+    double2* vk = ws.V + (size_t)k * n;
+    if ((e = apply(d, vk, ws.w, s, f32)) != cudaSuccess) return e;
+    // CGS2
+    multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h, 0, s);
+    multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h, n, -1.0);
+    cudaMemcpyAsync(hbuf.data(), ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    std::vector<cdh> hk(k + 2);
+    for (int i = 0; i <= k; ++i) hk[i] = cdh(hbuf[i].x, hbuf[i].y);
+    multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h, 0, s);
+    multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h, n, -1.0);
+    cudaMemcpyAsync(hbuf.data(), ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
+    double wn = 0.0;
+    if ((e = vnorm(ws.w, n, ws.partial, ws.h, s, wn)) != cudaSuccess) return e;
+    for (int i = 0; i <= k; ++i) hk[i] += cdh(hbuf[i].x, hbuf[i].y);
+    hk[k + 1] = wn;
+    const bool breakdown = (std::abs(hk[k + 1]) < brk);
+    if (!breakdown) scale_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V + (size_t)(k + 1) * n, 1.0 / wn, n);
+    // Givens rotations (unitary): G = [[conj(c), conj(s)], [-s, c]].
+    for (int i = 0; i < k; ++i) {
+      const cdh t = std::conj(cs[i]) * hk[i] + std::conj(sn[i]) * hk[i + 1];
+      hk[i + 1] = -sn[i] * hk[i] + cs[i] * hk[i + 1];
+      hk[i] = t;
+    }
+    const double nr = std::sqrt(std::norm(hk[k]) + std::norm(hk[k + 1]));
+    cdh c = nr == 0.0 ? cdh(1.0, 0.0) : hk[k] / nr;
+    cdh sv = nr == 0.0 ? cdh(0.0, 0.0) : hk[k + 1] / nr;
+    cs.push_back(c);
+    sn.push_back(sv);
+    hk[k] = std::conj(c) * hk[k] + std::conj(sv) * hk[k + 1];
+    hk[k + 1] = 0.0;
+    H.push_back(hk);
+    g.push_back(-sv * g[k]);
+    g[k] = std::conj(c) * g[k];
+    K = k + 1;
+    const double est = std::abs(g[k + 1]) / bnorm;
+    if (hist) hist->push_back(est);
+    if ((tol >= 0.0 && est <= tol) || breakdown) {
+      converged = tol >= 0.0 && est <= tol;
+      break;
+    }
+  }
+  // Back substitution R y = g, then x = x0 + V y.
+  std::vector<cdh> y(K);
+  for (int i = K - 1; i >= 0; --i) {
+    cdh sum = g[i];
+    for (int j = i + 1; j < K; ++j) sum -= H[j][i] * y[j];
+    y[i] = sum / H[i][i];
+  }
+  for (int i = 0; i < K; ++i) hbuf[i] = make_double2(y[i].real(), y[i].imag());
+  cudaMemcpyAsync(ws.h, hbuf.data(), (size_t)K * sizeof(double2), cudaMemcpyHostToDevice, s);
+  if (x0) {
+    if (x != x0) cudaMemcpyAsync(x, x0, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+  } else {
+    cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), s);
+  }
+  multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(x, ws.V, n, K, ws.h, n, 1.0);
+  iters = K;
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return cudaStreamSynchronize(s);
+}
+
+}  // namespace
+
+cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter, double tol,
+                      std::vector<double>& hist, GmresResult& res, bool use_f32) {
+  Workspace ws;
+  cudaError_t e = ws.alloc(d.N, max_iter);
+  if (e != cudaSuccess) return e;
+  double bn = 0.0;
+  if ((e = vnorm(b, d.N, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) return e;
+  if (bn == 0.0) {
+    cudaMemsetAsync(x, 0, (size_t)d.N * sizeof(double2), d.stream);
+    res.iters = 0; res.rel_residual = 0.0; res.converged = true;
+    hist.assign(1, 0.0);
+    return cudaStreamSynchronize(d.stream);
+  }
+  hist.clear();
+  int it = 0;
+  bool conv = false;
+  if ((e = arnoldi_cycle(d, ws, b, nullptr, x, max_iter, tol, 1e-300, bn, &hist, it, conv, use_f32)) != cudaSuccess) return e;
+  // True residual with the FP64 operator (the reference's "Err in GMRES").
+  if ((e = dev_matvec(d, x, ws.w, d.stream, false)) != cudaSuccess) return e;
+  sub_kernel<<<grid_for(d.N), 256, 0, d.stream>>>(b, ws.w, ws.r, d.N);
+  double rn = 0.0;
+  if ((e = vnorm(ws.r, d.N, ws.partial, ws.h, d.stream, rn)) != cudaSuccess) return e;
+  res.iters = it;
+  res.converged = conv;
+  res.rel_residual = rn / bn;
+  return cudaSuccess;
+}
+
+cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, int m, int restarts) {
+  Workspace ws;
+  cudaError_t e = ws.alloc(d.N, m);
+  if (e != cudaSuccess) return e;
+  double bn = 0.0;
+  if ((e = vnorm(b, d.N, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) return e;
+  if (bn == 0.0) bn = 1.0;
+  cudaMemsetAsync(x, 0, (size_t)d.N * sizeof(double2), d.stream);
+  for (int r = 0; r < restarts; ++r) {
+    int it = 0;
+    bool conv = false;
+    if ((e = arnoldi_cycle(d, ws, b, x, x, m, -1.0, 1e-8, bn, nullptr, it, conv, false)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Iterative refinement in FP64 around GMRES on the FP32 operator:
+//   r = b - A64 x ; solve A32 d = r to a loose tolerance ; x += d
+// until |b - A64 x| / |b| <= tol. The residual is always the FP64 one.
+cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner, double tol,
+                            std::vector<double>& hist, int& n_matvec, double& relres) {
+  const int n = d.N;
+  Workspace ws;
+  cudaError_t e = ws.alloc(n, inner);
+  if (e != cudaSuccess) return e;
+  double2 *r = nullptr, *dx = nullptr;
+  if ((e = cudaMalloc(&r, (size_t)n * sizeof(double2))) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&dx, (size_t)n * sizeof(double2))) != cudaSuccess) { cudaFree(r); return e; }
+  double bn = 0.0;
+  if ((e = vnorm(b, n, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) goto done;
+  hist.clear();
+  n_matvec = 0;
+  cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), d.stream);
+  cudaMemcpyAsync(r, b, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, d.stream);
+  relres = 1.0;
+  hist.push_back(1.0);
+  for (int o = 0; o < max_outer && relres > tol; ++o) {
+    int it = 0;
+    bool conv = false;
+    // Inner solve to roughly the FP32 operator accuracy.
+    const double inner_tol = std::max(tol / std::max(relres, 1e-300), 1e-6);
+    if ((e = arnoldi_cycle(d, ws, r, nullptr, dx, inner, inner_tol, 1e-300, std::max(relres * bn, 1e-300), nullptr, it,
+                           conv, true)) != cudaSuccess)
+      goto done;
+    n_matvec += it;
+    add_inplace_kernel<<<grid_for(n), 256, 0, d.stream>>>(x, dx, n);
+    if ((e = dev_matvec(d, x, ws.w, d.stream, false)) != cudaSuccess) goto done;
+    ++n_matvec;
+    sub_kernel<<<grid_for(n), 256, 0, d.stream>>>(b, ws.w, r, n);
+    double rn = 0.0;
+    if ((e = vnorm(r, n, ws.partial, ws.h, d.stream, rn)) != cudaSuccess) goto done;
+    relres = rn / bn;
+    hist.push_back(relres);
+  }
+done:
+  cudaFree(r);
+  cudaFree(dx);
+  return e;
+}
+
+}  // namespace lsg

@@ -1,0 +1,344 @@
+// DAFMM matvec on the GPU (sm_103a).
+//
+// y = A x runs as (GMRES/GMRES.cpp:201-254, DFMM::MatVecProduct):
+//   1. S[0:N) <- x                          (assignLeafCharges, G_FMM2DTree.hpp:1139)
+//   2. P <- 0
+//   3. upward, leaves first, one launch per level:
+//        S[own] = T * S[children]            (LFR_M2M :2472, HFR_M2M :3772)
+//   4. M2L, every level in one launch:
+//        P[node] = sum_IL M2L * S[source]     (LFR_M2L :2577, HFR_M2L :3882)
+//   5. downward, root side first, one launch per level:
+//        P[child] += W * P[parent]            (HFR_L2L :4208, LFR_L2L :2800)
+//   6. near field + identity, fused with the output write:
+//        y = P[0:N) + kappa^2 q .* sum_n B_n x_nb + x
+//                                            (evaluate_NearField_Using_Precomputations_LS :2884,
+//                                             collectPotential :3045)
+// Steps 3-5 share one gather-GEMV kernel. Each warp owns one output row
+// block, so every output element is written by exactly one warp and the
+// sums are deterministic (no atomics).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "device.h"
+
+namespace lsg {
+
+template <class C> struct Real;
+template <> struct Real<double2> { using T = double; };
+template <> struct Real<float2> { using T = float; };
+
+__device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
+
+// Gather-GEMV over a list of warp items (see GemvItem).
+template <class C>
+__global__ void __launch_bounds__(256) gemv_items_kernel(const GemvItem* __restrict__ items, int n_items,
+                                                         const C* __restrict__ A, const int* __restrict__ idx,
+                                                         const C* __restrict__ src, C* __restrict__ dst,
+                                                         int accumulate) {
+  using R = typename Real<C>::T;
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += nw) {
+    const GemvItem it = items[w];
+    const C* __restrict__ Ab = A + it.a_off;
+    const int* __restrict__ ib = idx + it.idx_off;
+    if (it.layout == 0) {
+      // Row major: lanes stride over the K columns, kRowsPerItem rows per warp.
+      R ar[kRowsPerItem], ai[kRowsPerItem];
+#pragma unroll
+      for (int r = 0; r < kRowsPerItem; ++r) { ar[r] = R(0); ai[r] = R(0); }
+      const int K = it.K, nr = it.nr;
+      for (int k = lane; k < K; k += 32) {
+        const C x = src[ib[k]];
+#pragma unroll
+        for (int r = 0; r < kRowsPerItem; ++r) {
+          if (r < nr) {
+            const C a = Ab[(size_t)r * K + k];
+            ar[r] = fma(a.x, x.x, ar[r]);
+            ar[r] = fma(-a.y, x.y, ar[r]);
+            ai[r] = fma(a.x, x.y, ai[r]);
+            ai[r] = fma(a.y, x.x, ai[r]);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kRowsPerItem; ++r) {
+        if (r < nr) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            ar[r] += __shfl_xor_sync(0xffffffffu, ar[r], o);
+            ai[r] += __shfl_xor_sync(0xffffffffu, ai[r], o);
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kRowsPerItem; ++r) {
+        if (r < nr && lane == r) {
+          C* out = dst + it.out_off + r;
+          if (accumulate) {
+            C o = *out;
+            o.x += ar[r];
+            o.y += ai[r];
+            *out = o;
+          } else {
+            *out = mk(ar[r], ai[r]);
+          }
+        }
+      }
+    } else {
+      // Column major: one lane per row, loop over the (few) columns.
+      if (lane < it.nr) {
+        R sr = R(0), si = R(0);
+        const C* __restrict__ col = Ab + lane;
+        const int K = it.K;
+        const int lda = it.lda;
+        for (int k = 0; k < K; ++k) {
+          const C x = src[ib[k]];
+          const C a = col[(size_t)k * lda];
+          sr = fma(a.x, x.x, sr);
+          sr = fma(-a.y, x.y, sr);
+          si = fma(a.x, x.y, si);
+          si = fma(a.y, x.x, si);
+        }
+        C* out = dst + it.out_off + lane;
+        if (accumulate) {
+          C o = *out;
+          o.x += sr;
+          o.y += si;
+          *out = o;
+        } else {
+          *out = mk(sr, si);
+        }
+      }
+    }
+  }
+}
+
+// Near field of every leaf (colleague blocks shared by all leaves of the
+// leaf level), fused with the far-field potential and the identity.
+template <class C>
+__global__ void __launch_bounds__(256) near_kernel(int n_out, int rank, const C* __restrict__ B,
+                                                   const typename Real<C>::T* __restrict__ kq,
+                                                   const int* __restrict__ coll, const C* __restrict__ x,
+                                                   const C* __restrict__ P, double2* __restrict__ y, int find_phi) {
+  using R = typename Real<C>::T;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_out) return;
+  const int leaf = t / rank, row = t - leaf * rank;
+  R ar = R(0), ai = R(0);
+#pragma unroll 1
+  for (int n = 0; n < 9; ++n) {
+    const int nb = coll[leaf * 9 + n];
+    if (nb < 0) continue;
+    const C* __restrict__ Bn = B + ((size_t)n * rank + row) * rank;
+    const C* __restrict__ xn = x + (size_t)nb * rank;
+    for (int c = 0; c < rank; ++c) {
+      const C a = Bn[c];
+      const C v = xn[c];
+      ar = fma(a.x, v.x, ar);
+      ar = fma(-a.y, v.y, ar);
+      ai = fma(a.x, v.y, ai);
+      ai = fma(a.y, v.x, ai);
+    }
+  }
+  const C p = P[t];
+  if (find_phi) {
+    const R s = kq[t];
+    const C xs = x[t];
+    y[t] = make_double2((double)(p.x + s * ar + xs.x), (double)(p.y + s * ai + xs.y));
+  } else {
+    y[t] = make_double2((double)(p.x + ar), (double)(p.y + ai));
+  }
+}
+
+__global__ void d2f_kernel(const double2* __restrict__ a, float2* __restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void d2f_real_kernel(const double* __restrict__ a, float* __restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+static int g_sm_count = 0;
+
+static int sm_count(int dev) {
+  if (g_sm_count == 0) {
+    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sm_count <= 0) g_sm_count = 148;
+  }
+  return g_sm_count;
+}
+
+template <class C>
+static void launch_gemv(const DevPhase<C>& ph, const C* src, C* dst, cudaStream_t s, int dev) {
+  if (ph.n_items == 0) return;
+  const int warps_per_block = 8;
+  int blocks = (ph.n_items + warps_per_block - 1) / warps_per_block;
+  blocks = std::min(blocks, sm_count(dev) * 8);
+  gemv_items_kernel<C><<<blocks, 256, 0, s>>>(ph.items, ph.n_items, ph.A, ph.idx, src, dst, ph.accumulate);
+}
+
+template <class T>
+static bool dmalloc(T** p, size_t n, long long& total, std::string& err) {
+  if (n == 0) { *p = nullptr; return true; }
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    err = std::string("cudaMalloc failed: ") + cudaGetErrorString(e);
+    *p = nullptr;
+    return false;
+  }
+  total += (long long)(n * sizeof(T));
+  return true;
+}
+
+static bool upload_phase(const GemvPhase& h, DevPhase<double2>& d, long long& total, std::string& err) {
+  d.n_items = (int)h.items.size();
+  d.accumulate = h.accumulate;
+  d.entries = (long long)h.A.size();
+  if (!dmalloc(&d.A, h.A.size(), total, err)) return false;
+  if (!dmalloc(&d.idx, h.idx.size(), total, err)) return false;
+  if (!dmalloc(&d.items, h.items.size(), total, err)) return false;
+  if (h.A.size() && cudaMemcpy(d.A, h.A.data(), h.A.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess) { err = "upload A"; return false; }
+  if (h.idx.size() && cudaMemcpy(d.idx, h.idx.data(), h.idx.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) { err = "upload idx"; return false; }
+  if (h.items.size() && cudaMemcpy(d.items, h.items.data(), h.items.size() * sizeof(GemvItem), cudaMemcpyHostToDevice) != cudaSuccess) { err = "upload items"; return false; }
+  return true;
+}
+
+bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
+  cudaError_t e = cudaSetDevice(d.device);
+  if (e != cudaSuccess) { err = std::string("cudaSetDevice: ") + cudaGetErrorString(e); return false; }
+  if ((e = cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+    return false;
+  }
+  for (auto& ev : d.ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) { err = "cudaEventCreate"; return false; }
+  d.N = h.N;
+  d.n_leaves = h.n_leaves;
+  d.rank = h.rank;
+  d.find_phi = h.cfg.findPhi;
+  d.charges_len = h.charges_len;
+  d.pots_len = h.pots_len;
+  long long& tot = d.device_bytes;
+  d.up.resize(h.up.size());
+  for (size_t i = 0; i < h.up.size(); ++i) if (!upload_phase(h.up[i], d.up[i], tot, err)) return false;
+  if (!upload_phase(h.m2l, d.m2l, tot, err)) return false;
+  d.down.resize(h.down.size());
+  for (size_t i = 0; i < h.down.size(); ++i) if (!upload_phase(h.down[i], d.down[i], tot, err)) return false;
+  if (!dmalloc(&d.S, (size_t)h.charges_len, tot, err)) return false;
+  if (!dmalloc(&d.P, (size_t)h.pots_len, tot, err)) return false;
+  if (!dmalloc(&d.nearB, h.nearB.size(), tot, err)) return false;
+  if (!dmalloc(&d.kq, h.kq.size(), tot, err)) return false;
+  if (!dmalloc(&d.colleague, h.colleague.size(), tot, err)) return false;
+  if (!dmalloc(&d.xbuf, (size_t)h.N, tot, err)) return false;
+  if (!dmalloc(&d.ybuf, (size_t)h.N, tot, err)) return false;
+  cudaMemcpy(d.nearB, h.nearB.data(), h.nearB.size() * sizeof(double2), cudaMemcpyHostToDevice);
+  cudaMemcpy(d.kq, h.kq.data(), h.kq.size() * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(d.colleague, h.colleague.data(), h.colleague.size() * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemset(d.xbuf, 0, (size_t)h.N * sizeof(double2));
+  cudaMemset(d.ybuf, 0, (size_t)h.N * sizeof(double2));
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return false; }
+  int launches = 1;  // near kernel
+  for (auto& p : d.up) launches += p.n_items > 0;
+  launches += d.m2l.n_items > 0;
+  for (auto& p : d.down) launches += p.n_items > 0;
+  d.launches_per_matvec = launches;
+  return true;
+}
+
+template <class C>
+static void free_phase(DevPhase<C>& p) {
+  cudaFree(p.A);
+  cudaFree(p.idx);
+  cudaFree(p.items);
+  p = DevPhase<C>();
+}
+
+void dev_free(DevOperator& d) {
+  cudaSetDevice(d.device);
+  for (auto& p : d.up) free_phase(p);
+  for (auto& p : d.down) free_phase(p);
+  free_phase(d.m2l);
+  // FP32 phases share idx / items with the FP64 phases; only A is theirs.
+  for (auto& p : d.up32) cudaFree(p.A);
+  for (auto& p : d.down32) cudaFree(p.A);
+  cudaFree(d.m2l32.A);
+  cudaFree(d.S); cudaFree(d.P); cudaFree(d.nearB); cudaFree(d.kq); cudaFree(d.colleague);
+  cudaFree(d.S32); cudaFree(d.P32); cudaFree(d.nearB32); cudaFree(d.kq32);
+  cudaFree(d.xbuf); cudaFree(d.ybuf);
+  for (auto& ev : d.ev) if (ev) cudaEventDestroy(ev);
+  if (d.stream) cudaStreamDestroy(d.stream);
+  d = DevOperator();
+}
+
+static bool f32_phase(const DevPhase<double2>& a, DevPhase<float2>& b, long long& tot, std::string& err) {
+  b.n_items = a.n_items;
+  b.accumulate = a.accumulate;
+  b.entries = a.entries;
+  if (!dmalloc(&b.A, (size_t)a.entries, tot, err)) return false;
+  b.idx = a.idx;      // shared with the FP64 phase
+  b.items = a.items;  // shared
+  if (a.entries) d2f_kernel<<<1024, 256>>>(a.A, b.A, a.entries);
+  return true;
+}
+
+bool dev_enable_f32(DevOperator& d, std::string& err) {
+  if (d.has_f32) return true;
+  cudaSetDevice(d.device);
+  long long& tot = d.device_bytes;
+  d.up32.resize(d.up.size());
+  for (size_t i = 0; i < d.up.size(); ++i) if (!f32_phase(d.up[i], d.up32[i], tot, err)) return false;
+  if (!f32_phase(d.m2l, d.m2l32, tot, err)) return false;
+  d.down32.resize(d.down.size());
+  for (size_t i = 0; i < d.down.size(); ++i) if (!f32_phase(d.down[i], d.down32[i], tot, err)) return false;
+  if (!dmalloc(&d.S32, (size_t)d.charges_len, tot, err)) return false;
+  if (!dmalloc(&d.P32, (size_t)d.pots_len, tot, err)) return false;
+  const long long nb = 9LL * d.rank * d.rank;
+  if (!dmalloc(&d.nearB32, (size_t)nb, tot, err)) return false;
+  if (!dmalloc(&d.kq32, (size_t)d.N, tot, err)) return false;
+  d2f_kernel<<<256, 256>>>(d.nearB, d.nearB32, nb);
+  d2f_real_kernel<<<256, 256>>>(d.kq, d.kq32, d.N);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { err = std::string("enable_f32: ") + cudaGetErrorString(e); return false; }
+  d.has_f32 = true;
+  return true;
+}
+
+cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
+  if (!s) s = d.stream;
+  cudaMemcpyAsync(d.S, x, (size_t)d.N * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+  cudaMemsetAsync(d.P, 0, (size_t)d.pots_len * sizeof(double2), s);
+  for (auto& ph : d.up) launch_gemv(ph, d.S, d.S, s, d.device);
+  if (mark_m2l) cudaEventRecord(d.ev[0], s);
+  launch_gemv(d.m2l, d.S, d.P, s, d.device);
+  if (mark_m2l) cudaEventRecord(d.ev[1], s);
+  for (auto& ph : d.down) launch_gemv(ph, d.P, d.P, s, d.device);
+  const int n = d.N;
+  near_kernel<double2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB, d.kq, d.colleague, d.S, d.P, y, d.find_phi);
+  return cudaGetLastError();
+}
+
+cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
+  if (!d.has_f32) return cudaErrorInvalidValue;
+  if (!s) s = d.stream;
+  d2f_kernel<<<256, 256, 0, s>>>(x, d.S32, d.N);
+  cudaMemsetAsync(d.P32, 0, (size_t)d.pots_len * sizeof(float2), s);
+  for (auto& ph : d.up32) launch_gemv(ph, d.S32, d.S32, s, d.device);
+  if (mark_m2l) cudaEventRecord(d.ev[2], s);
+  launch_gemv(d.m2l32, d.S32, d.P32, s, d.device);
+  if (mark_m2l) cudaEventRecord(d.ev[3], s);
+  for (auto& ph : d.down32) launch_gemv(ph, d.P32, d.P32, s, d.device);
+  const int n = d.N;
+  near_kernel<float2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB32, d.kq32, d.colleague, d.S32, d.P32, y, d.find_phi);
+  return cudaGetLastError();
+}
+
+}  // namespace lsg
