@@ -1,0 +1,300 @@
+"""Benchmark: FP64 DAFMM matvec throughput (matvec/s) on one GB300.
+
+Workload (the reference's scale configuration): uniform quadtree level 6
+(4,096 leaves, 6x6 Chebyshev nodes, N = 147,456), kappa = 40, contrast =
+3 Gaussian bumps drawn from numpy.random.default_rng(20261203) (centres
+U[-0.6,0.6]^2, amplitudes U[0.5,1.5], widths U[0.05,0.2]), NCA tolerance
+1e-10, 16 cones at the finest HFR level, degree-6 basis, 6-digit
+precomputation rounding as in the reference. One step = one matvec y = A x
+of the assembled operator over one synthetic input vector (re, im ~ U[-1,1]).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, all host threads) on the same workload; the reference itself needs
+Eigen and Boost.Math, which are not installed, so its own build is
+unavailable. N > 1 runs independent replicas (the path has no data-path
+collective), one per GPU, and reports the sum of their throughputs.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DAFMM matvec throughput, FP64 (plain method), N=147456, kappa=40"
+SEED = 20261203
+
+
+def workload_config(ls, level=6):
+    return ls.Config(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, TOL_POW=10, degreeOfBases=6, nLevelsUniform=level,
+                     Qchoice=6, findPhi=1, reference_rounding=1, L=1.0, kappa=40.0, bumps=ls.seeded_bumps(SEED))
+
+
+def input_vector(n):
+    rng = np.random.default_rng(SEED + 1)
+    return rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(ls, cfg, budget_s=25.0, threads=None):
+    """Times the oracle's matvec (CPU restatement of the reference phases)
+    on the same operator: as many matvecs as fit in budget_s, at least one."""
+    from oracle import oracle as ora
+
+    ora.build()
+    ncores = threads or os.cpu_count() or 1
+    ora.set_threads(ncores)
+    t0 = time.time()
+    o = ora.Oracle(cfg.as_dict())
+    t_asm = time.time() - t0
+    x = input_vector(o.N)
+    o.matvec(x)  # warm-up
+    n, t = 0, 0.0
+    while n < 1 or t < budget_s:
+        t1 = time.perf_counter()
+        o.matvec(x)
+        t += time.perf_counter() - t1
+        n += 1
+        if n >= 200:
+            break
+    o.close()
+    return {"value": n / t, "unit": "matvec/s", "cores": ncores, "kind": "port",
+            "sample": f"{n} oracle matvecs of the full workload operator (assembly {t_asm:.0f} s not timed)"}
+
+
+def run_reference(args):
+    """The CPU arm: the oracle restatement of the reference, all host threads."""
+    import lippmann_schwinger_solver_gb300 as ls
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg = workload_config(ls)
+    from oracle import oracle as ora
+
+    ora.build()
+    ncores = os.cpu_count() or 1
+    ora.set_threads(ncores)
+    o = ora.Oracle(cfg.as_dict())
+    x = input_vector(o.N)
+    for _ in range(max(1, min(args.warmup, 2))):
+        o.matvec(x)
+    steps = max(1, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.matvec(x)
+    dt = time.perf_counter() - t0
+    v = steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
+            "config": {"workload": "uniform level 6, N=147456, kappa=40, 3 seeded bumps, NCA tol 1e-10",
+                       "parallelism": "CPU threads"},
+            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": ncores, "kind": "port",
+                             "sample": f"{steps} matvecs of the full workload operator; reference build "
+                                       "unavailable (Eigen/Boost headers missing)"},
+            "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import lippmann_schwinger_solver_gb300 as ls
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    ls.build()
+    cfg = workload_config(ls, args.level)
+    op = ls.Operator(cfg, device=local)
+    info = op.info
+    n = op.N
+    x = input_vector(n)
+    xd = torch.from_numpy(x).to(f"cuda:{local}")
+    yd = torch.empty_like(xd)
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    # warm-up
+    for _ in range(max(3, args.warmup)):
+        op.matvec_device(xd.data_ptr(), yd.data_ptr(), sp)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        time.sleep(0.3)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            op.matvec_device(xd.data_ptr(), yd.data_ptr(), sp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        time.sleep(0.3)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1e3 / ms
+    # Dominant kernel (M2L) timed with events on the operator's own stream.
+    ms_mv, ms_m2l = op.time_matvec(warmup=3, iters=max(5, args.steps))
+    # End to end through the C ABI with host buffers (pinned).
+    xh = torch.from_numpy(x).pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    lib = ls.lib()
+    import ctypes
+
+    xp = ctypes.cast(xh.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    yp = ctypes.cast(yh.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    for _ in range(2):
+        lib.ls_matvec_host(op._h, xp, yp)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc = lib.ls_matvec_host(op._h, xp, yp)
+        if rc != 0:
+            raise RuntimeError(lib.ls_last_error().decode())
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    # The bench output must agree with the C ABI host path bit for bit.
+    assert np.array_equal(yh.numpy(), yd.cpu().numpy()), "device and host-buffer matvecs differ"
+    peak, peak_kind = load_peaks()
+    achieved = info["m2l_bytes"] / (ms_m2l * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "m2l_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(ls, cfg, budget_s=args.cpu_budget)
+    line = {
+        "metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
+        "config": {"workload": "uniform level %d, N=%d, kappa=40, 3 seeded bumps (seed %d), NCA tol 1e-10"
+                   % (args.level, n, SEED), "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2: %.0f MB of operator blocks streamed per matvec"
+                         % (info["far_entries"] * 16 / 1e6)},
+        "e2e": {"value": world / e2e_s, "unit": "matvec/s", "h2d_bytes_per_step": 16 * n,
+                "d2h_bytes_per_step": 16 * n},
+        "gpu_launches": info["n_kernels_per_matvec"] * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind, "kernel": "gemv_items_kernel<double2> (M2L)",
+                     "kernel_ms": ms_m2l, "kernel_gflops_fp64": info["m2l_flops"] / (ms_m2l * 1e-3) / 1e9},
+        "matvec": {"bytes": info["matvec_bytes"], "flops_fp64": info["matvec_flops"],
+                   "achieved_gbs": info["matvec_bytes"] / (ms * 1e-3) / 1e9,
+                   "achieved_fp64_tflops": info["matvec_flops"] / (ms * 1e-3) / 1e12,
+                   "assemble_s": info["assemble_seconds"], "device_bytes": info["device_bytes"],
+                   "far_entries": info["far_entries"], "max_rank": info["max_rank"]},
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    op.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=6)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -75,6 +75,9 @@ typedef struct {
   double assemble_seconds; /* host assembly wall time */
   int max_rank;            /* largest NCA skeleton */
   int n_kernels_per_matvec;/* CUDA kernel launches in one matvec */
+  long long m2l_entries;   /* complex entries of the M2L blocks */
+  long long m2l_bytes;     /* algorithmic bytes of the M2L kernel (FP64) */
+  long long m2l_flops;     /* real flops of the M2L kernel */
 } ls_op_info_t;
 
 typedef struct ls_op ls_op;

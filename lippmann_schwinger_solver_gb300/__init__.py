@@ -1,0 +1,378 @@
+"""GB300 DAFMM matvec + GMRES for the 2-D Lippmann-Schwinger equation.
+
+Python front end of liblsdafmm.so (C ABI in include/ls_dafmm.h). The
+classes mirror the reference's operator interface
+(vaishna77/Lippmann_Schwinger_Solver, GMRES/GMRES.cpp):
+
+* ``DFMM(inputs)`` with ``FMMTreeInitialisation()`` and
+  ``MatVecProduct(b)`` (GMRES/GMRES.cpp:140-255);
+* ``classGMRES().gmres(M, b, maxIterations, threshold)``
+  (GMRES_Hybrid/include/gmres.hpp:54-119);
+* ``RestartedGMRES(restart, S, m, inputs, b)`` (GMRES/GMRES.cpp:307-319);
+* ``userkernel`` contrast / incident / right-hand-side functions
+  (GMRES/GMRES.cpp:100-127).
+
+Every numerical call runs on the GPU through the CUDA library; there is no
+CPU implementation here. If the library is missing or no GPU is present the
+calls raise instead of falling back.
+"""
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblsdafmm.so")
+MAX_BUMPS = 8
+
+LS_OK = 0
+LS_E_INVALID = -1
+LS_E_CUDA = -2
+LS_E_NOMEM = -3
+LS_E_NOT_CONVERGED = -4
+LS_E_STATE = -5
+LS_E_TIMEOUT = -6
+LS_PREC_F64 = 0
+LS_PREC_F32 = 1
+
+# Every symbol declared in include/ls_dafmm.h.
+EXPORTED_SYMBOLS = (
+    "ls_op_create", "ls_op_destroy", "ls_op_info", "ls_op_points", "ls_op_contrast", "ls_op_rhs",
+    "ls_matvec", "ls_matvec_f32", "ls_op_enable_f32", "ls_matvec_host", "ls_gmres", "ls_gmres_restarted",
+    "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
+    "ls_version",
+)
+
+
+class LSError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{msg} (status {code})")
+        self.code = code
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [
+        ("nCones_LFR", ctypes.c_int),
+        ("nChebNodes", ctypes.c_int),
+        ("yes2DFMM", ctypes.c_int),
+        ("TOL_POW", ctypes.c_int),
+        ("degreeOfBases", ctypes.c_int),
+        ("nLevelsUniform", ctypes.c_int),
+        ("Qchoice", ctypes.c_int),
+        ("findPhi", ctypes.c_int),
+        ("reference_rounding", ctypes.c_int),
+        ("n_bumps", ctypes.c_int),
+        ("L", ctypes.c_double),
+        ("kappa", ctypes.c_double),
+        ("bump_cx", ctypes.c_double * MAX_BUMPS),
+        ("bump_cy", ctypes.c_double * MAX_BUMPS),
+        ("bump_a", ctypes.c_double * MAX_BUMPS),
+        ("bump_w", ctypes.c_double * MAX_BUMPS),
+    ]
+
+
+class _Info(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int),
+        ("n_leaves", ctypes.c_int),
+        ("n_levels", ctypes.c_int),
+        ("level_LFR", ctypes.c_int),
+        ("rank", ctypes.c_int),
+        ("far_entries", ctypes.c_longlong),
+        ("near_entries", ctypes.c_longlong),
+        ("matvec_bytes", ctypes.c_longlong),
+        ("matvec_flops", ctypes.c_longlong),
+        ("device_bytes", ctypes.c_longlong),
+        ("assemble_seconds", ctypes.c_double),
+        ("max_rank", ctypes.c_int),
+        ("n_kernels_per_matvec", ctypes.c_int),
+        ("m2l_entries", ctypes.c_longlong),
+        ("m2l_bytes", ctypes.c_longlong),
+        ("m2l_flops", ctypes.c_longlong),
+    ]
+
+
+@dataclasses.dataclass
+class Config:
+    """Problem description (ls_config). Defaults follow GMRES/Readme.md:43."""
+    nCones_LFR: int = 16
+    nChebNodes: int = 6
+    yes2DFMM: int = 1
+    TOL_POW: int = 8
+    degreeOfBases: int = 6
+    nLevelsUniform: int = 4
+    Qchoice: int = 0
+    findPhi: int = 1
+    reference_rounding: int = 1
+    L: float = 1.0
+    kappa: float = 10.0
+    bumps: tuple = ()  # ((cx, cy, a, w), ...) for Qchoice 6
+
+    def to_c(self):
+        c = _Config()
+        for f in ("nCones_LFR", "nChebNodes", "yes2DFMM", "TOL_POW", "degreeOfBases", "nLevelsUniform",
+                  "Qchoice", "findPhi", "reference_rounding"):
+            setattr(c, f, int(getattr(self, f)))
+        c.L = float(self.L)
+        c.kappa = float(self.kappa)
+        c.n_bumps = len(self.bumps)
+        for k, (bx, by, a, w) in enumerate(self.bumps):
+            c.bump_cx[k], c.bump_cy[k], c.bump_a[k], c.bump_w[k] = bx, by, a, w
+        return c
+
+    def as_dict(self):
+        d = {f.name: getattr(self, f.name) for f in dataclasses.fields(self) if f.name != "bumps"}
+        d["n_bumps"] = len(self.bumps)
+        d["bump_cx"] = [b[0] for b in self.bumps]
+        d["bump_cy"] = [b[1] for b in self.bumps]
+        d["bump_a"] = [b[2] for b in self.bumps]
+        d["bump_w"] = [b[3] for b in self.bumps]
+        return d
+
+
+def seeded_bumps(seed, n=3):
+    """Gaussian bumps q(x) = sum_k a_k exp(-|x-c_k|^2 / w_k^2) with centres
+    U[-0.6, 0.6]^2, amplitudes U[0.5, 1.5] and widths U[0.05, 0.2] drawn from
+    numpy.random.default_rng(seed)."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-0.6, 0.6, size=(n, 2))
+    a = rng.uniform(0.5, 1.5, size=n)
+    w = rng.uniform(0.05, 0.2, size=n)
+    return tuple((float(c[k, 0]), float(c[k, 1]), float(a[k]), float(w[k])) for k in range(n))
+
+
+_lib = None
+
+
+def build(verbose=False):
+    """Compiles liblsdafmm.so in-tree (nvcc for sm_103a + g++)."""
+    from . import _build
+    return _build.build(verbose=verbose)
+
+
+def lib():
+    """Loads liblsdafmm.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run lippmann_schwinger_solver_gb300.build() first")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+        L.ls_op_create.argtypes = [ctypes.POINTER(_Config), ctypes.c_int, ctypes.POINTER(vp)]
+        L.ls_op_destroy.argtypes = [vp]
+        L.ls_op_info.argtypes = [vp, ctypes.POINTER(_Info)]
+        for n in ("ls_op_points", "ls_op_contrast", "ls_op_rhs"):
+            getattr(L, n).argtypes = [vp, dp]
+        for n in ("ls_matvec", "ls_matvec_f32"):
+            getattr(L, n).argtypes = [vp, vp, vp, vp]
+        L.ls_op_enable_f32.argtypes = [vp]
+        L.ls_matvec_host.argtypes = [vp, dp, dp]
+        L.ls_gmres.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp, dp, ip, dp]
+        L.ls_gmres_restarted.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, dp]
+        L.ls_gmres_mixed.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, dp, ip, dp]
+        L.ls_time_matvec.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+        L.ls_op_skeleton_dump.restype = ctypes.c_long
+        L.ls_op_skeleton_dump.argtypes = [vp, ip, ctypes.c_long]
+        L.ls_op_precomputations.argtypes = [vp, dp, dp]
+        L.ls_last_error.restype = ctypes.c_char_p
+        L.ls_version.restype = ctypes.c_char_p
+        for n in EXPORTED_SYMBOLS:
+            if n not in ("ls_op_skeleton_dump", "ls_last_error", "ls_version"):
+                getattr(L, n).restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _check(code, what):
+    if code != LS_OK:
+        raise LSError(code, f"{what}: {lib().ls_last_error().decode()}")
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Operator:
+    """An assembled DAFMM operator resident on one GPU (ls_op)."""
+
+    def __init__(self, cfg, device=0):
+        if isinstance(cfg, dict):
+            cfg = Config(**cfg)
+        self.cfg = cfg
+        self._c = cfg.to_c()
+        h = ctypes.c_void_p()
+        _check(lib().ls_op_create(ctypes.byref(self._c), int(device), ctypes.byref(h)), "ls_op_create")
+        self._h = h
+        self.info = self._info()
+        self.N = self.info["N"]
+
+    def _info(self):
+        i = _Info()
+        _check(lib().ls_op_info(self._h, ctypes.byref(i)), "ls_op_info")
+        return {f: getattr(i, f) for f, _ in _Info._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ls_op_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # geometry / plugin
+    def points(self):
+        a = np.empty((self.N, 2))
+        _check(lib().ls_op_points(self._h, _dp(a)), "ls_op_points")
+        return a
+
+    def contrast(self):
+        a = np.empty(self.N)
+        _check(lib().ls_op_contrast(self._h, _dp(a)), "ls_op_contrast")
+        return a
+
+    def rhs(self):
+        a = np.empty(self.N, dtype=np.complex128)
+        _check(lib().ls_op_rhs(self._h, _dp(a)), "ls_op_rhs")
+        return a
+
+    # products
+    def matvec(self, x):
+        """y = A x for host vectors (copies in, computes on the GPU, copies out)."""
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        if x.shape != (self.N,):
+            raise ValueError(f"x must have shape ({self.N},)")
+        y = np.empty_like(x)
+        _check(lib().ls_matvec_host(self._h, _dp(x), _dp(y)), "ls_matvec_host")
+        return y
+
+    def matvec_device(self, x_ptr, y_ptr, stream=0, precision=LS_PREC_F64):
+        """y = A x for device pointers (e.g. torch complex128 tensors' data_ptr())."""
+        f = lib().ls_matvec if precision == LS_PREC_F64 else lib().ls_matvec_f32
+        _check(f(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), ctypes.c_void_p(stream)), "ls_matvec")
+
+    def enable_f32(self):
+        _check(lib().ls_op_enable_f32(self._h), "ls_op_enable_f32")
+
+    def gmres(self, b, max_iter=400, tol=1e-10, raise_on_fail=False):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.empty_like(b)
+        hist = np.full(max_iter + 1, np.nan)
+        it = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        code = lib().ls_gmres(self._h, _dp(b), int(max_iter), float(tol), _dp(x), _dp(hist), ctypes.byref(it),
+                              ctypes.byref(rr))
+        if code not in (LS_OK, LS_E_NOT_CONVERGED) or (raise_on_fail and code != LS_OK):
+            _check(code, "ls_gmres")
+        return x, hist[: it.value + 1], it.value, rr.value, code
+
+    def gmres_restarted(self, b, m, restarts):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.empty_like(b)
+        _check(lib().ls_gmres_restarted(self._h, _dp(b), int(m), int(restarts), _dp(x)), "ls_gmres_restarted")
+        return x
+
+    def gmres_mixed(self, b, max_outer=10, inner_iter=200, tol=1e-8):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.empty_like(b)
+        hist = np.full(max_outer + 1, np.nan)
+        nmv = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        code = lib().ls_gmres_mixed(self._h, _dp(b), int(max_outer), int(inner_iter), float(tol), _dp(x), _dp(hist),
+                                    ctypes.byref(nmv), ctypes.byref(rr))
+        if code not in (LS_OK, LS_E_NOT_CONVERGED):
+            _check(code, "ls_gmres_mixed")
+        return x, hist[~np.isnan(hist)], nmv.value, rr.value, code
+
+    def time_matvec(self, warmup=3, iters=20, precision=LS_PREC_F64):
+        a, b = ctypes.c_float(), ctypes.c_float()
+        _check(lib().ls_time_matvec(self._h, int(precision), int(warmup), int(iters), ctypes.byref(a),
+                                    ctypes.byref(b)), "ls_time_matvec")
+        return a.value, b.value
+
+    # inspection
+    def skeleton_dump(self):
+        n = lib().ls_op_skeleton_dump(self._h, None, 0)
+        a = np.empty(n, dtype=np.int32)
+        lib().ls_op_skeleton_dump(self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+        return a
+
+    def precomputations(self):
+        r = self.info["rank"]
+        M = np.empty((r, 31), dtype=np.complex128)
+        B = np.empty((9, r, r), dtype=np.complex128)
+        _check(lib().ls_op_precomputations(self._h, _dp(M), _dp(B)), "ls_op_precomputations")
+        return M, B
+
+
+# --------------------------------------------------------------------------
+# Reference-shaped interface (GMRES/GMRES.cpp, GMRES_Hybrid/include/gmres.hpp)
+
+
+@dataclasses.dataclass
+class inputsToDFMM:  # noqa: N801 - reference name (GMRES/GMRES.cpp:129-138)
+    nCones_LFR: int = 16
+    nChebNodes: int = 6
+    L: float = 1.0
+    yes2DFMM: int = 1
+    TOL_POW: int = 8
+    degreeOfBases: int = 6
+    treeAdaptivity: int = 5
+    nLevelsUniform: int = 4
+
+
+class userkernel:  # noqa: N801 - reference name (GMRES/GMRES.cpp:100-127)
+    """Contrast / incidence / right-hand side plugin. Qchoice 0..5 are the
+    reference contrasts; Qchoice 6 are Gaussian bumps."""
+
+    def __init__(self, kappa, Qchoice=0, bumps=()):
+        self.kappa, self.Qchoice, self.bumps = kappa, Qchoice, tuple(bumps)
+
+    def IncidenceFunction(self, xy):
+        return np.exp(1j * self.kappa * np.asarray(xy)[..., 0])
+
+
+class DFMM:
+    """Drop-in for the reference's DFMM adapter (GMRES/GMRES.cpp:140-255)."""
+
+    def __init__(self, inputs, kernel, findPhi=True, reference_rounding=True, device=0):
+        self.inputs, self.mykernel = inputs, kernel
+        self.cfg = Config(nCones_LFR=inputs.nCones_LFR, nChebNodes=inputs.nChebNodes, yes2DFMM=inputs.yes2DFMM,
+                          TOL_POW=inputs.TOL_POW, degreeOfBases=inputs.degreeOfBases,
+                          nLevelsUniform=inputs.nLevelsUniform, Qchoice=kernel.Qchoice, findPhi=int(findPhi),
+                          reference_rounding=int(reference_rounding), L=inputs.L, kappa=kernel.kappa,
+                          bumps=kernel.bumps)
+        self.device = device
+        self.K = None
+
+    def FMMTreeInitialisation(self):
+        self.K = Operator(self.cfg, self.device)
+        self.N = self.K.N
+        self.gridPoints = self.K.points()
+
+    def MatVecProduct(self, b):
+        return self.K.matvec(b)
+
+    def RHS(self):
+        return self.K.rhs()
+
+
+class classGMRES:  # noqa: N801 - reference name
+    def gmres(self, M, b, maxIterations, threshold):
+        """Returns (x, error, noOfIterations, e) like classGMRES::gmres."""
+        x, hist, it, _, _ = M.K.gmres(b, maxIterations, threshold)
+        return x, float(hist[-1]), it, list(hist)
+
+
+def RestartedGMRES(restart, S, m, inputs, b):  # noqa: N802 - reference name
+    return S.K.gmres_restarted(b, m, restart)

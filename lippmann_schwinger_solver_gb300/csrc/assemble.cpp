@@ -1061,8 +1061,10 @@ void Builder::pack(HostOperator& op) {
       nd.pot_nonzero = true;
     }
     GemvPhase ph;
+    op.m2l_rows = 0;
     for (auto& tk : tasks) {
       if (tk.K == 0) continue;
+      op.m2l_rows += tk.rows;
       add_task(ph, tk.A, tk.rows, tk.K, tk.idx, (int)tk.out);
       std::vector<cd>().swap(tk.A);
     }

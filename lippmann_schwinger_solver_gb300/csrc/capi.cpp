@@ -115,6 +115,11 @@ ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
   o->assemble_seconds = h.assemble_seconds;
   o->max_rank = h.max_rank;
   o->n_kernels_per_matvec = d.launches_per_matvec;
+  // M2L: every block once (16 B per complex entry), every source charge of
+  // the charge buffer once, every potential it writes once.
+  o->m2l_entries = op->on_device ? d.m2l.entries : h.m2l.entries();
+  o->m2l_bytes = 16LL * o->m2l_entries + 16LL * h.charges_len + 16LL * h.m2l_rows;
+  o->m2l_flops = 8LL * o->m2l_entries;
   return LS_OK;
 }
 

@@ -52,6 +52,7 @@ struct HostOperator {
   long long pots_len = 0;            // leaf potentials (N) + skeleton potentials
   std::vector<GemvPhase> up;         // M2M, leaves first, then coarser levels
   GemvPhase m2l;                     // all levels in one launch
+  long long m2l_rows = 0;            // potential rows written by M2L
   std::vector<GemvPhase> down;       // L2L, coarse to fine
   std::vector<int> skeleton_dump;
   int max_rank = 0;
