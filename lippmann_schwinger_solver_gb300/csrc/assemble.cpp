@@ -978,12 +978,40 @@ void Builder::pack(HostOperator& op) {
         }
       }
   }
-  // ---- potential buffer: leaves (N), then every non-leaf node with rows.
+  // ---- which potentials can be nonzero: a node's potential is nonzero
+  // when it has an M2L term with at least one source charge, or when a
+  // parent with a nonzero potential passes something down (top down).
+  for (int j = 2; j <= nL; ++j) {
+    const int nn = (int)nodes[j].size();
+    for (int t = 0; t < nn; ++t) {
+      Node& X = nodes[j][t];
+      X.pot_nonzero = false;
+      if (X.user_check.empty()) continue;
+      const int k = is_lfr(j) ? t : t / nCones[j];
+      if (X.in_active) {
+        for (int b : X.IL) {
+          const Node& src = is_lfr(j) ? lfr(j, b) : cone(j, b, cone_towards(cx[j], cy[j], k, b, aperture[j]));
+          if (!src.out_charge.empty()) { X.pot_nonzero = true; break; }
+        }
+      }
+      if (X.pot_nonzero || j == 2) continue;
+      const int cc = is_lfr(j) ? 0 : t % nCones[j];
+      const int kp = k / 4, jp = j - 1;
+      const int npc = is_lfr(jp) ? 1 : nCones[jp];
+      for (int pc = 0; pc < npc && !X.pot_nonzero; ++pc) {
+        if (!is_lfr(jp) && !is_lfr(j) && pc / 2 != cc) continue;
+        const Node& p = is_lfr(jp) ? lfr(jp, kp) : cone(jp, kp, pc);
+        if (p.pot_nonzero && (!p.in_active || !p.in_charge.empty())) X.pot_nonzero = true;
+      }
+    }
+  }
+  // ---- potential buffer: leaves (N), then every other node whose
+  // potential can be nonzero.
   long long P = N;
   for (int k = 0; k < nleaf; ++k) lfr(nL, k).pot_off = (long long)k * rank;
   for (int j = 2; j < nL; ++j)
     for (auto& nd : nodes[j])
-      if (!nd.user_check.empty()) { nd.pot_off = P; P += (long long)nd.user_check.size(); }
+      if (nd.pot_nonzero && !nd.user_check.empty()) { nd.pot_off = P; P += (long long)nd.user_check.size(); }
   op.charges_len = S;
   op.pots_len = P;
 
@@ -1058,7 +1086,6 @@ void Builder::pack(HostOperator& op) {
       tk.rows = rows;
       tk.K = K;
       tk.out = nd.pot_off;
-      nd.pot_nonzero = true;
     }
     GemvPhase ph;
     op.m2l_rows = 0;
@@ -1159,7 +1186,6 @@ void Builder::pack(HostOperator& op) {
     ph.accumulate = 1;
     for (int t = 0; t < nch; ++t) {
       if (!tasks[t].any) continue;
-      nodes[J][t].pot_nonzero = true;
       add_task(ph, tasks[t].A, tasks[t].rows, tasks[t].K, tasks[t].idx, (int)tasks[t].out);
       std::vector<cd>().swap(tasks[t].A);
     }
