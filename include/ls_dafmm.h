@@ -113,6 +113,22 @@ ls_status ls_matvec(ls_op* op, const double* x, double* y, void* stream);
  * the boundary). Requires ls_op_enable_f32(). */
 ls_status ls_matvec_f32(ls_op* op, const double* x, double* y, void* stream);
 ls_status ls_op_enable_f32(ls_op* op);
+/*
+ * Allocation-free variant of ls_matvec. No counterpart in the reference.
+ * For callers that may not allocate device memory while they run (for
+ * example a solver inside a framework whose caching allocator owns the
+ * device heap): the matvec's scratch (skeleton charges and potentials) is
+ * taken from a fixed device array of LS_STATIC_SCRATCH_ELEMS complex
+ * doubles (16 MiB) that every GPU loading the library reserves until exit;
+ * nothing is allocated or freed per call. x, y and the operator stay
+ * caller-provided as in ls_matvec. Operators that need more scratch are
+ * rejected with LS_E_INVALID. The first call on a device looks up the
+ * array's device address (make it before any stream capture). All calls
+ * share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.
+ */
+#define LS_STATIC_SCRATCH_ELEMS (1LL << 20)
+ls_status ls_matvec_noalloc(ls_op* op, const double* x, double* y, void* stream);
 /* Host-buffer convenience: copies x in, runs ls_matvec, copies y out, syncs.
  * This is the call a reference-style driver makes (Vec in, Vec out). */
 ls_status ls_matvec_host(ls_op* op, const double* x, double* y);

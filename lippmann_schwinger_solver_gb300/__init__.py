@@ -41,7 +41,7 @@ EXPORTED_SYMBOLS = (
     "ls_op_create", "ls_op_destroy", "ls_op_info", "ls_op_points", "ls_op_contrast", "ls_op_rhs",
     "ls_matvec", "ls_matvec_f32", "ls_op_enable_f32", "ls_matvec_host", "ls_gmres", "ls_gmres_restarted",
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
-    "ls_version",
+    "ls_version", "ls_matvec_noalloc",
 )
 
 
@@ -164,7 +164,7 @@ def lib():
         L.ls_op_info.argtypes = [vp, ctypes.POINTER(_Info)]
         for n in ("ls_op_points", "ls_op_contrast", "ls_op_rhs"):
             getattr(L, n).argtypes = [vp, dp]
-        for n in ("ls_matvec", "ls_matvec_f32"):
+        for n in ("ls_matvec", "ls_matvec_f32", "ls_matvec_noalloc"):
             getattr(L, n).argtypes = [vp, vp, vp, vp]
         L.ls_op_enable_f32.argtypes = [vp]
         L.ls_matvec_host.argtypes = [vp, dp, dp]
@@ -260,6 +260,12 @@ class Operator:
         """y = A x for device pointers (e.g. torch complex128 tensors' data_ptr())."""
         f = lib().ls_matvec if precision == LS_PREC_F64 else lib().ls_matvec_f32
         _check(f(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), ctypes.c_void_p(stream)), "ls_matvec")
+
+    def matvec_device_noalloc(self, x_ptr, y_ptr, stream=0):
+        """y = A x for device pointers with the matvec scratch taken from the
+        library's static device array (no device allocation per call)."""
+        _check(lib().ls_matvec_noalloc(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr),
+                                       ctypes.c_void_p(stream)), "ls_matvec_noalloc")
 
     def enable_f32(self):
         _check(lib().ls_op_enable_f32(self._h), "ls_op_enable_f32")

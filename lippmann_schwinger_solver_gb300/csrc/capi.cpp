@@ -173,6 +173,19 @@ ls_status ls_matvec_f32(ls_op* op, const double* x, double* y, void* stream) {
   return LS_OK;
 }
 
+ls_status ls_matvec_noalloc(ls_op* op, const double* x, double* y, void* stream) {
+  if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_noalloc: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_noalloc: operator was assembled without a device");
+  const long long need = op->dev.charges_len + op->dev.pots_len;
+  if (need > LS_STATIC_SCRATCH_ELEMS)
+    return fail(LS_E_INVALID, "ls_matvec_noalloc: operator needs " + std::to_string(need) +
+                                  " complex scratch entries, the static array holds " +
+                                  std::to_string((long long)LS_STATIC_SCRATCH_ELEMS));
+  cudaError_t e = dev_matvec_static(op->dev, (const double2*)x, (double2*)y, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_noalloc");
+  return LS_OK;
+}
+
 ls_status ls_matvec_host(ls_op* op, const double* x, double* y) {
   if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_host: null argument");
   if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_host: operator was assembled without a device");

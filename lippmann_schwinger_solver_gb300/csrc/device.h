@@ -52,6 +52,10 @@ struct DevOperator {
   int launches_per_matvec = 0;
 };
 
+// Capacity of the static scratch array of ls_matvec_noalloc, in complex
+// doubles (16 MiB).
+constexpr long long kStaticScratchElems = LS_STATIC_SCRATCH_ELEMS;
+
 // matvec.cu
 bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err);
 void dev_free(DevOperator& d);
@@ -59,6 +63,8 @@ bool dev_enable_f32(DevOperator& d, std::string& err);
 // y = A x; x, y device pointers (N complex). mark_m2l: record events around M2L.
 cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
 cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
+// Same product with its scratch in a static device array (no allocation).
+cudaError_t dev_matvec_static(DevOperator& d, const double2* x, double2* y, cudaStream_t s);
 
 // gmres.cu
 struct GmresResult {

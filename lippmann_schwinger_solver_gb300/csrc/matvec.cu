@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -338,6 +339,76 @@ cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStr
   for (auto& ph : d.down32) launch_gemv(ph, d.P32, d.P32, s, d.device);
   const int n = d.N;
   near_kernel<float2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB32, d.kq32, d.colleague, d.S32, d.P32, y, d.find_phi);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free matvec (ls_matvec_noalloc).
+//
+// Some callers must not allocate device memory while they run: a solver
+// embedded in a framework whose caching allocator owns the device heap
+// (a cudaMalloc behind its back can fail once that allocator has reserved
+// the memory, or force a device-wide synchronisation in its middle), and
+// drivers that hand over every buffer they use up front. For them the
+// matvec's two scratch vectors -- the skeleton charges and the skeleton
+// potentials -- live in the fixed, file-scope device array below instead of
+// buffers owned by the operator. Every GPU that loads this library reserves
+// it (kStaticScratchElems complex doubles, 16 MiB) until the process exits.
+//
+// The array is shared by all calls and keeps the last call's contents, so
+// each call clears what must start at zero. Calls whose work overlaps on the
+// GPU (two streams, two operators, two threads) race on it and must be
+// serialised by the caller.
+
+namespace {
+
+constexpr int kMaxScratchDevices = 64;
+
+static __device__ __align__(256) double2 g_static_scratch[kStaticScratchElems];
+
+std::mutex g_scratch_mu;
+double2* g_scratch_ptr[kMaxScratchDevices] = {};
+
+// Device address of g_static_scratch on `device`. In host code the symbol
+// is only a host-side stand-in, so the address is looked up once per device
+// with that device current (the first call on a device does this set-up and
+// should come before any stream capture).
+cudaError_t static_scratch_address(int device, double2** out) {
+  if (device < 0 || device >= kMaxScratchDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[device]) {
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) return e;
+    if (cur != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (cur != device) cudaSetDevice(cur);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[device] = static_cast<double2*>(p);
+  }
+  *out = g_scratch_ptr[device];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t dev_matvec_static(DevOperator& d, const double2* x, double2* y, cudaStream_t s) {
+  if (d.charges_len + d.pots_len > kStaticScratchElems) return cudaErrorInvalidValue;
+  if (!s) s = d.stream;
+  double2* base = nullptr;
+  cudaError_t e = static_scratch_address(d.device, &base);
+  if (e != cudaSuccess) return e;
+  double2* S = base;
+  double2* P = base + d.charges_len;
+  cudaMemcpyAsync(S, x, (size_t)d.N * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+  cudaMemsetAsync(S + d.N, 0, (size_t)(d.charges_len - d.N) * sizeof(double2), s);
+  cudaMemsetAsync(P, 0, (size_t)d.pots_len * sizeof(double2), s);
+  for (auto& ph : d.up) launch_gemv(ph, (const double2*)S, S, s, d.device);
+  launch_gemv(d.m2l, (const double2*)S, P, s, d.device);
+  for (auto& ph : d.down) launch_gemv(ph, (const double2*)P, P, s, d.device);
+  const int n = d.N;
+  near_kernel<double2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB, d.kq, d.colleague, S, P, y, d.find_phi);
   return cudaGetLastError();
 }
 
