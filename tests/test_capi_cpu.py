@@ -1,0 +1,109 @@
+"""The C ABI library without a GPU: it loads, exports every symbol declared
+in include/ls_dafmm.h, and its host assembly (device < 0) reproduces the
+oracle's precomputations and NCA skeletons exactly. No compute call runs."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import CFG_BUMPS, CFG_C1, CFG_HFR, CFG_L3_K10, full_cfg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    text = open(os.path.join(ROOT, "include", "ls_dafmm.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ls_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(ls):
+    L = ls.lib()
+    names = _declared()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(ls.EXPORTED_SYMBOLS)
+    assert b"sm_103a" in L.ls_version()
+
+
+@pytest.mark.parametrize("base,over", [
+    (CFG_L3_K10, {}),
+    (CFG_C1, {}),
+    (CFG_C1, {"findPhi": 0}),
+    (CFG_C1, {"yes2DFMM": 0}),
+    (CFG_HFR, {}),
+    (CFG_BUMPS, {"nLevelsUniform": 3}),
+    (CFG_L3_K10, {"Qchoice": 4, "TOL_POW": 6}),
+    (CFG_L3_K10, {"Qchoice": 1}),
+])
+def test_host_assembly_matches_oracle(ls, ora, base, over):
+    cfg = full_cfg(base, **over)
+    op = ls.Operator(cfg, device=-1)
+    ref = ora.Oracle(cfg.as_dict())
+    assert op.N == ref.N
+    assert op.info["level_LFR"] == ref.level_lfr
+    assert np.array_equal(op.skeleton_dump(), ref.skeleton_dump())
+    M, B = op.precomputations()
+    assert np.array_equal(M, ref.far_moments())
+    assert np.array_equal(B, ref.near_blocks())
+    assert np.array_equal(op.points(), ref.points())
+    assert np.array_equal(op.contrast(), ref.contrast())
+    assert np.array_equal(op.rhs(), ref.rhs())
+    op.close()
+
+
+def test_host_only_operator_refuses_device_calls(ls):
+    op = ls.Operator(full_cfg(CFG_L3_K10), device=-1)
+    x = np.zeros(op.N, dtype=np.complex128)
+    with pytest.raises(ls.LSError) as ei:
+        op.matvec(x)
+    assert ei.value.code == ls.LS_E_STATE
+    with pytest.raises(ls.LSError) as ei:
+        op.gmres(x, 5, 1e-3)
+    assert ei.value.code == ls.LS_E_STATE
+    with pytest.raises(ls.LSError) as ei:
+        op.enable_f32()
+    assert ei.value.code == ls.LS_E_STATE
+    info = op.info
+    assert info["far_entries"] > 0 and info["matvec_flops"] > 8 * info["far_entries"]
+    assert info["m2l_entries"] <= info["far_entries"]
+    op.close()
+
+
+@pytest.mark.parametrize("over,msg", [
+    ({"nLevelsUniform": 1}, "nLevelsUniform"),
+    ({"nLevelsUniform": 11}, "nLevelsUniform"),
+    ({"nChebNodes": 1}, "nChebNodes"),
+    ({"degreeOfBases": 9}, "degreeOfBases"),
+    ({"Qchoice": 7}, "Qchoice"),
+    ({"L": 0.0}, "L must"),
+    ({"TOL_POW": 0}, "TOL_POW"),
+])
+def test_invalid_configurations_are_rejected(ls, over, msg):
+    with pytest.raises(ls.LSError) as ei:
+        ls.Operator(full_cfg(CFG_L3_K10, **over), device=-1)
+    assert ei.value.code == ls.LS_E_INVALID
+    assert msg in str(ei.value)
+
+
+def test_bumps_contrast_needs_bumps(ls):
+    with pytest.raises(ls.LSError) as ei:
+        ls.Operator(ls.Config(Qchoice=6, nLevelsUniform=3), device=-1)
+    assert ei.value.code == ls.LS_E_INVALID
+
+
+def test_seeded_bumps_are_reproducible(ls):
+    a = ls.seeded_bumps(20261203)
+    assert a == ls.seeded_bumps(20261203)
+    for cx, cy, amp, w in a:
+        assert -0.6 <= cx <= 0.6 and -0.6 <= cy <= 0.6 and 0.5 <= amp <= 1.5 and 0.05 <= w <= 0.2
+
+
+def test_null_handles_do_not_crash(ls):
+    L = ls.lib()
+    assert L.ls_op_destroy(None) == 0
+    assert L.ls_op_info(None, None) == ls.LS_E_INVALID
+    assert L.ls_matvec(None, None, None, None) == ls.LS_E_INVALID
+    assert L.ls_op_skeleton_dump(None, None, 0) == -1

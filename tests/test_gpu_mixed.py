@@ -1,0 +1,45 @@
+"""FP32 operator (FP32 blocks, FP32 accumulation) and the FP64 iterative
+refinement around it (mixed-precision configuration)."""
+import numpy as np
+import pytest
+
+from conftest import CFG_BUMPS, CFG_C1, full_cfg
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_f32_matvec_error_is_single_precision(ls, ora):
+    torch = pytest.importorskip("torch")
+    cfg = full_cfg(CFG_BUMPS)
+    op = ls.Operator(cfg, device=0)
+    op.enable_f32()
+    x = np.random.default_rng(4).uniform(-1, 1, op.N) + 1j * np.random.default_rng(5).uniform(-1, 1, op.N)
+    xt = torch.from_numpy(x).cuda()
+    y32 = torch.empty_like(xt)
+    op.matvec_device(xt.data_ptr(), y32.data_ptr(), 0, precision=ls.LS_PREC_F32)
+    torch.cuda.synchronize()
+    y64 = op.matvec(x)
+    e = _rel(y32.cpu().numpy(), y64)
+    # FP32 storage and accumulation of blocks: ~1e-7 relative, far above FP64.
+    assert 1e-12 < e <= 2e-6
+    op.close()
+
+
+def test_mixed_refinement_reaches_fp64_residual(ls, ora):
+    cfg = full_cfg(CFG_C1)
+    op = ls.Operator(cfg, device=0)
+    op.enable_f32()
+    b = op.rhs()
+    x, hist, nmv, relres, code = op.gmres_mixed(b, max_outer=10, inner_iter=100, tol=1e-10)
+    assert code == ls.LS_OK
+    ref = ora.Oracle(cfg.as_dict())
+    rr = np.linalg.norm(b - ref.matvec(x)) / np.linalg.norm(b)
+    assert rr <= 2e-10
+    assert abs(rr - relres) <= 1e-11
+    x64, _, it64, _, _ = op.gmres(b, 200, 1e-10)
+    assert _rel(x, x64) <= 1e-8
+    op.close()

@@ -107,3 +107,14 @@ def test_empty_and_invalid(ls):
     with pytest.raises(ValueError):
         op.matvec(np.zeros(3, dtype=np.complex128))
     op.close()
+
+
+@pytest.mark.parametrize("name", ["l3_k10_gauss", "l4_k10_gauss", "l4_k24_flatbump"])
+def test_matvec_matches_golden_fixtures(ls, name):
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    d = eval(str(g["cfg"]))  # dict literal written by tests/golden/make_golden.py
+    op = ls.Operator(ls.Config(**{k: v for k, v in d.items()}), device=0)
+    assert _rel(op.matvec(g["x"]), g["y"]) <= TOL_PARITY
+    op.close()
