@@ -36,8 +36,61 @@ template <> struct Real<float2> { using T = float; };
 __device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
 __device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
 
-// Gather-GEMV over a list of warp items (see GemvItem).
-template <class C>
+// Streaming loads for the operator blocks: every block entry is read once
+// per matvec, so it should not displace the gathered charges from L2.
+__device__ __forceinline__ double2 ld_stream(const double2* p) { return __ldcs(p); }
+__device__ __forceinline__ float2 ld_stream(const float2* p) { return __ldcs(p); }
+
+// Warp reduction of kRowsPerItem complex partial sums (2 * kRowsPerItem
+// reals per lane) that halves the values each lane carries at every step:
+// after offsets 16, 8, 4 a lane holds 3 of the 24 values, summed over the 8
+// lanes that share its bits 2..4, and offsets 2, 1 finish the sum. It needs
+// 12 + 6 + 3 + 3 + 3 = 27 additions per lane instead of 5 * 24 = 120.
+// On return the lanes with (lane & 3) == 0 hold values base..base+2 with
+// base = 12 * bit4 + 6 * bit3 + 3 * bit2; value v is row v / 2, part v % 2.
+template <class R>
+__device__ __forceinline__ void transpose_reduce24(R (&v)[24], int lane, R (&out)[3]) {
+  static_assert(kRowsPerItem == 12, "reduction written for 12 rows");
+  R w[12];
+  {
+    const bool hi = lane & 16;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+      const R send = hi ? v[i] : v[i + 12];
+      const R keep = hi ? v[i + 12] : v[i];
+      w[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+  }
+  R u[6];
+  {
+    const bool hi = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const R send = hi ? w[i] : w[i + 6];
+      const R keep = hi ? w[i + 6] : w[i];
+      u[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+  }
+  {
+    const bool hi = lane & 4;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const R send = hi ? u[i] : u[i + 3];
+      const R keep = hi ? u[i + 3] : u[i];
+      out[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    out[i] += __shfl_xor_sync(0xffffffffu, out[i], 2);
+    out[i] += __shfl_xor_sync(0xffffffffu, out[i], 1);
+  }
+}
+
+// Gather-GEMV over a list of warp items (see GemvItem). PHASE only names the
+// instantiation (0 upward, 1 M2L, 2 downward) so that profilers can tell the
+// launches apart.
+template <class C, int PHASE>
 __global__ void __launch_bounds__(256) gemv_items_kernel(const GemvItem* __restrict__ items, int n_items,
                                                          const C* __restrict__ A, const int* __restrict__ idx,
                                                          const C* __restrict__ src, C* __restrict__ dst,
@@ -51,44 +104,54 @@ __global__ void __launch_bounds__(256) gemv_items_kernel(const GemvItem* __restr
     const int* __restrict__ ib = idx + it.idx_off;
     if (it.layout == 0) {
       // Row major: lanes stride over the K columns, kRowsPerItem rows per warp.
-      R ar[kRowsPerItem], ai[kRowsPerItem];
+      R v[2 * kRowsPerItem];
 #pragma unroll
-      for (int r = 0; r < kRowsPerItem; ++r) { ar[r] = R(0); ai[r] = R(0); }
+      for (int r = 0; r < 2 * kRowsPerItem; ++r) v[r] = R(0);
       const int K = it.K, nr = it.nr;
-      for (int k = lane; k < K; k += 32) {
-        const C x = src[ib[k]];
+      int k = lane;
+      for (; k + 32 < K; k += 64) {
+        const C x0 = src[ib[k]];
+        const C x1 = src[ib[k + 32]];
 #pragma unroll
         for (int r = 0; r < kRowsPerItem; ++r) {
           if (r < nr) {
-            const C a = Ab[(size_t)r * K + k];
-            ar[r] = fma(a.x, x.x, ar[r]);
-            ar[r] = fma(-a.y, x.y, ar[r]);
-            ai[r] = fma(a.x, x.y, ai[r]);
-            ai[r] = fma(a.y, x.x, ai[r]);
+            const C a0 = ld_stream(Ab + (size_t)r * K + k);
+            const C a1 = ld_stream(Ab + (size_t)r * K + k + 32);
+            v[2 * r] = fma(a0.x, x0.x, v[2 * r]);
+            v[2 * r] = fma(-a0.y, x0.y, v[2 * r]);
+            v[2 * r + 1] = fma(a0.x, x0.y, v[2 * r + 1]);
+            v[2 * r + 1] = fma(a0.y, x0.x, v[2 * r + 1]);
+            v[2 * r] = fma(a1.x, x1.x, v[2 * r]);
+            v[2 * r] = fma(-a1.y, x1.y, v[2 * r]);
+            v[2 * r + 1] = fma(a1.x, x1.y, v[2 * r + 1]);
+            v[2 * r + 1] = fma(a1.y, x1.x, v[2 * r + 1]);
           }
         }
       }
+      if (k < K) {
+        const C x0 = src[ib[k]];
 #pragma unroll
-      for (int r = 0; r < kRowsPerItem; ++r) {
-        if (r < nr) {
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            ar[r] += __shfl_xor_sync(0xffffffffu, ar[r], o);
-            ai[r] += __shfl_xor_sync(0xffffffffu, ai[r], o);
+        for (int r = 0; r < kRowsPerItem; ++r) {
+          if (r < nr) {
+            const C a0 = ld_stream(Ab + (size_t)r * K + k);
+            v[2 * r] = fma(a0.x, x0.x, v[2 * r]);
+            v[2 * r] = fma(-a0.y, x0.y, v[2 * r]);
+            v[2 * r + 1] = fma(a0.x, x0.y, v[2 * r + 1]);
+            v[2 * r + 1] = fma(a0.y, x0.x, v[2 * r + 1]);
           }
         }
       }
+      R out[3];
+      transpose_reduce24(v, lane, out);
+      if ((lane & 3) == 0) {
+        const int base = 12 * ((lane >> 4) & 1) + 6 * ((lane >> 3) & 1) + 3 * ((lane >> 2) & 1);
+        R* d = reinterpret_cast<R*>(dst + it.out_off);
 #pragma unroll
-      for (int r = 0; r < kRowsPerItem; ++r) {
-        if (r < nr && lane == r) {
-          C* out = dst + it.out_off + r;
-          if (accumulate) {
-            C o = *out;
-            o.x += ar[r];
-            o.y += ai[r];
-            *out = o;
-          } else {
-            *out = mk(ar[r], ai[r]);
+        for (int t = 0; t < 3; ++t) {
+          const int vv = base + t;
+          if ((vv >> 1) < nr) {
+            if (accumulate) d[vv] += out[t];
+            else d[vv] = out[t];
           }
         }
       }
@@ -101,7 +164,7 @@ __global__ void __launch_bounds__(256) gemv_items_kernel(const GemvItem* __restr
         const int lda = it.lda;
         for (int k = 0; k < K; ++k) {
           const C x = src[ib[k]];
-          const C a = col[(size_t)k * lda];
+          const C a = ld_stream(col + (size_t)k * lda);
           sr = fma(a.x, x.x, sr);
           sr = fma(-a.y, x.y, sr);
           si = fma(a.x, x.y, si);
@@ -177,13 +240,13 @@ static int sm_count(int dev) {
   return g_sm_count;
 }
 
-template <class C>
+template <int PHASE, class C>
 static void launch_gemv(const DevPhase<C>& ph, const C* src, C* dst, cudaStream_t s, int dev) {
   if (ph.n_items == 0) return;
   const int warps_per_block = 8;
   int blocks = (ph.n_items + warps_per_block - 1) / warps_per_block;
   blocks = std::min(blocks, sm_count(dev) * 8);
-  gemv_items_kernel<C><<<blocks, 256, 0, s>>>(ph.items, ph.n_items, ph.A, ph.idx, src, dst, ph.accumulate);
+  gemv_items_kernel<C, PHASE><<<blocks, 256, 0, s>>>(ph.items, ph.n_items, ph.A, ph.idx, src, dst, ph.accumulate);
 }
 
 template <class T>
@@ -317,11 +380,11 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
   if (!s) s = d.stream;
   cudaMemcpyAsync(d.S, x, (size_t)d.N * sizeof(double2), cudaMemcpyDeviceToDevice, s);
   cudaMemsetAsync(d.P, 0, (size_t)d.pots_len * sizeof(double2), s);
-  for (auto& ph : d.up) launch_gemv(ph, d.S, d.S, s, d.device);
+  for (auto& ph : d.up) launch_gemv<0>(ph, (const double2*)d.S, d.S, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[0], s);
-  launch_gemv(d.m2l, d.S, d.P, s, d.device);
+  launch_gemv<1>(d.m2l, (const double2*)d.S, d.P, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
-  for (auto& ph : d.down) launch_gemv(ph, d.P, d.P, s, d.device);
+  for (auto& ph : d.down) launch_gemv<2>(ph, (const double2*)d.P, d.P, s, d.device);
   const int n = d.N;
   near_kernel<double2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB, d.kq, d.colleague, d.S, d.P, y, d.find_phi);
   return cudaGetLastError();
@@ -332,11 +395,11 @@ cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStr
   if (!s) s = d.stream;
   d2f_kernel<<<256, 256, 0, s>>>(x, d.S32, d.N);
   cudaMemsetAsync(d.P32, 0, (size_t)d.pots_len * sizeof(float2), s);
-  for (auto& ph : d.up32) launch_gemv(ph, d.S32, d.S32, s, d.device);
+  for (auto& ph : d.up32) launch_gemv<0>(ph, (const float2*)d.S32, d.S32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[2], s);
-  launch_gemv(d.m2l32, d.S32, d.P32, s, d.device);
+  launch_gemv<1>(d.m2l32, (const float2*)d.S32, d.P32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[3], s);
-  for (auto& ph : d.down32) launch_gemv(ph, d.P32, d.P32, s, d.device);
+  for (auto& ph : d.down32) launch_gemv<2>(ph, (const float2*)d.P32, d.P32, s, d.device);
   const int n = d.N;
   near_kernel<float2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB32, d.kq32, d.colleague, d.S32, d.P32, y, d.find_phi);
   return cudaGetLastError();
@@ -404,9 +467,9 @@ cudaError_t dev_matvec_static(DevOperator& d, const double2* x, double2* y, cuda
   cudaMemcpyAsync(S, x, (size_t)d.N * sizeof(double2), cudaMemcpyDeviceToDevice, s);
   cudaMemsetAsync(S + d.N, 0, (size_t)(d.charges_len - d.N) * sizeof(double2), s);
   cudaMemsetAsync(P, 0, (size_t)d.pots_len * sizeof(double2), s);
-  for (auto& ph : d.up) launch_gemv(ph, (const double2*)S, S, s, d.device);
-  launch_gemv(d.m2l, (const double2*)S, P, s, d.device);
-  for (auto& ph : d.down) launch_gemv(ph, (const double2*)P, P, s, d.device);
+  for (auto& ph : d.up) launch_gemv<0>(ph, (const double2*)S, S, s, d.device);
+  launch_gemv<1>(d.m2l, (const double2*)S, P, s, d.device);
+  for (auto& ph : d.down) launch_gemv<2>(ph, (const double2*)P, P, s, d.device);
   const int n = d.N;
   near_kernel<double2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB, d.kq, d.colleague, S, P, y, d.find_phi);
   return cudaGetLastError();

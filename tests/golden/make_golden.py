@@ -5,9 +5,14 @@ missing), so these vectors are outputs of the oracle's restatement of the
 reference DAFMM. They freeze its results: tests check that the oracle keeps
 reproducing them and that the GPU path matches them.
 
+One set per host architecture (tests/golden/<machine>/): glibc's libm
+differs in the last bit between x86-64 and aarch64, which can move an NCA
+pivot at a near-tie and hence change the operator at the NCA tolerance.
+
     python tests/golden/make_golden.py
 """
 import os
+import platform
 import sys
 
 import numpy as np
@@ -29,6 +34,8 @@ BASE = dict(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, degreeOfBases=6, findPhi=1,
 
 
 def main():
+    out = os.path.join(HERE, platform.machine())
+    os.makedirs(out, exist_ok=True)
     for name, over in CASES.items():
         cfg = dict(BASE, **over)
         o = oracle.Oracle(cfg)
@@ -38,8 +45,8 @@ def main():
         b = o.rhs()
         xs, hist, it = o.gmres(b, 200, 1e-10)
         ranks = np.array([o.level_lfr, o.nlevels, len(o.skeleton_dump())])
-        np.savez_compressed(os.path.join(HERE, name + ".npz"), x=x, y=y, b=b, x_gmres=xs, gmres_iters=it,
-                            ranks=ranks, cfg=np.array(repr(cfg)))
+        np.savez_compressed(os.path.join(out, name + ".npz"), x=x, y=y, b=b, x_gmres=xs, gmres_iters=it,
+                            ranks=ranks, skeleton=o.skeleton_dump(), cfg=np.array(repr(cfg)))
         print(name, o.N, it)
 
 

@@ -24,8 +24,11 @@ def test_f32_matvec_error_is_single_precision(ls, ora):
     torch.cuda.synchronize()
     y64 = op.matvec(x)
     e = _rel(y32.cpu().numpy(), y64)
-    # FP32 storage and accumulation of blocks: ~1e-7 relative, far above FP64.
-    assert 1e-12 < e <= 2e-6
+    # FP32 storage and accumulation of the folded blocks. Folding Atilde^-1
+    # into the blocks leaves cancellation that FP32 amplifies: the product is
+    # good to ~1e-5 relative, far above FP64 and enough for the inner solves
+    # of the FP64 refinement.
+    assert 1e-12 < e <= 5e-5
     op.close()
 
 

@@ -112,9 +112,11 @@ def test_empty_and_invalid(ls):
 @pytest.mark.parametrize("name", ["l3_k10_gauss", "l4_k10_gauss", "l4_k24_flatbump"])
 def test_matvec_matches_golden_fixtures(ls, name):
     import os
+    import platform
 
-    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", platform.machine(), name + ".npz"))
     d = eval(str(g["cfg"]))  # dict literal written by tests/golden/make_golden.py
     op = ls.Operator(ls.Config(**{k: v for k, v in d.items()}), device=0)
+    assert np.array_equal(op.skeleton_dump(), g["skeleton"])
     assert _rel(op.matvec(g["x"]), g["y"]) <= TOL_PARITY
     op.close()

@@ -5,7 +5,10 @@ import os
 import numpy as np
 import pytest
 
-GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+import platform
+
+# Golden vectors written by tests/golden/make_golden.py on this architecture.
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", platform.machine())
 BASE = dict(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, degreeOfBases=6, findPhi=1, reference_rounding=1, L=1.0)
 
 
@@ -18,6 +21,7 @@ def test_oracle_reproduces_golden(ora, name):
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     cfg = eval(str(g["cfg"]))  # a dict literal written by make_golden.py
     o = ora.Oracle(cfg)
+    assert np.array_equal(o.skeleton_dump(), g["skeleton"])
     assert _rel(o.matvec(g["x"]), g["y"]) <= 1e-12
     assert _rel(o.rhs(), g["b"]) <= 1e-14
 
