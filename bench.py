@@ -107,6 +107,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(value, dist, device=None):
+    """The slowest rank's value (timings of replicas are reported as the max
+    over ranks, so that whole-job throughput = ranks * steps / max time)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(value)
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, ms_per_step):
+    """Whole-job matvec/s of `world` independent replicas whose slowest
+    step takes ms_per_step."""
+    return world * 1e3 / ms_per_step
+
+
 def cpu_baseline(ls, cfg, budget_s=25.0, threads=None):
     """Times the oracle's matvec (CPU restatement of the reference phases)
     on the same operator: as many matvecs as fit in budget_s, at least one."""
@@ -209,12 +227,8 @@ def run_ours(args):
         ev1.record(stream)
         torch.cuda.synchronize()
         time.sleep(0.3)
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1e3 / ms
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, f"cuda:{local}")
+    value = replica_throughput(world, ms)
     # Dominant kernel (M2L) timed with events on the operator's own stream.
     ms_mv, ms_m2l = op.time_matvec(warmup=3, iters=max(5, args.steps))
     # End to end through the C ABI with host buffers (pinned).
@@ -234,13 +248,27 @@ def run_ours(args):
         rc = lib.ls_matvec_host(op._h, xp, yp)
         if rc != 0:
             raise RuntimeError(lib.ls_last_error().decode())
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, f"cuda:{local}")
     # The bench output must agree with the C ABI host path bit for bit.
     assert np.array_equal(yh.numpy(), yd.cpu().numpy()), "device and host-buffer matvecs differ"
+    # Solve time to a true relative residual of 1e-8: plain FP64 GMRES, and
+    # the FP64 refinement around the FP32 operator (residual always FP64).
+    solve = None
+    if not args.no_solve:
+        b = op.rhs()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, hist64, it64, rr64, code64 = op.gmres(b, max_iter=args.max_iter, tol=1e-8)
+        t64 = time.perf_counter() - t0
+        op.enable_f32()
+        ms32, m2l32 = op.time_matvec(warmup=3, iters=max(5, args.steps), precision=ls.LS_PREC_F32)
+        t0 = time.perf_counter()
+        _, histm, nmv, rrm, codem = op.gmres_mixed(b, max_outer=20, inner_iter=args.max_iter, tol=1e-8)
+        tm = time.perf_counter() - t0
+        solve = {"tol": 1e-8, "fp64_gmres_s": t64, "fp64_iters": it64, "fp64_true_residual": rr64,
+                 "fp64_converged": code64 == 0, "mixed_s": tm, "mixed_matvecs": nmv, "mixed_true_residual": rrm,
+                 "mixed_converged": codem == 0, "speedup_mixed_vs_fp64": t64 / tm if tm > 0 else None,
+                 "f32_matvec_per_s": 1e3 / ms32, "f32_m2l_ms": m2l32}
     peak, peak_kind = load_peaks()
     achieved = info["m2l_bytes"] / (ms_m2l * 1e-3) / 1e9
     traffic = None
@@ -271,6 +299,7 @@ def run_ours(args):
                    "assemble_s": info["assemble_seconds"], "device_bytes": info["device_bytes"],
                    "far_entries": info["far_entries"], "max_rank": info["max_rank"]},
         "clocks": clk.summary(),
+        "solve": solve,
         "cpu_baseline": cpu,
     }
     if rank == 0:
@@ -289,6 +318,8 @@ def main():
     ap.add_argument("--level", type=int, default=6)
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--max-iter", type=int, default=400)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1,0 +1,149 @@
+// ls_dafmm.hpp - C++ facade over the C ABI (ls_dafmm.h) with the reference's
+// tree / matvec / GMRES API surface (vaishna77/Lippmann_Schwinger_Solver):
+//
+//   inputsToDFMM                 GMRES/GMRES.cpp:129-138
+//   userkernel                   GMRES/GMRES.cpp:100-127 (contrast choice, plane wave, RHS)
+//   DFMM                         GMRES/GMRES.cpp:140-255 (FMMTreeInitialisation, MatVecProduct)
+//   GMRES / RestartedGMRES       GMRES/GMRES.cpp:257-319
+//   classGMRES::gmres            GMRES_Hybrid/include/gmres.hpp:54-119
+//
+// Vec is std::vector<std::complex<double>> (contiguous interleaved complex,
+// the layout of the reference's Eigen::VectorXcd). Header only; link with
+// -llsdafmm. Errors throw ls::Error carrying the C ABI status and message.
+#pragma once
+
+#include <complex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ls_dafmm.h"
+
+namespace ls {
+
+using Vec = std::vector<std::complex<double>>;
+
+struct pts2D {
+  double x, y;
+};
+
+class Error : public std::runtime_error {
+ public:
+  Error(ls_status s, const std::string& what) : std::runtime_error(what), status(s) {}
+  ls_status status;
+};
+
+inline void check(ls_status s, const char* where) {
+  if (s != LS_OK) throw Error(s, std::string(where) + ": " + ls_last_error());
+}
+
+struct inputsToDFMM {
+  int nCones_LFR = 16;
+  int nChebNodes = 6;
+  double L = 1.0;
+  int yes2DFMM = 1;
+  int TOL_POW = 8;
+  int degreeOfBases = 6;
+  int treeAdaptivity = 5;  // unused: the tree is uniform
+  int nLevelsUniform = 4;
+};
+
+// Contrast plugin: Qchoice 0..5 as in the reference, 6 = Gaussian bumps.
+struct userkernel {
+  double kappa = 10.0;
+  int Qchoice = 0;
+  std::vector<double> bump_cx, bump_cy, bump_a, bump_w;
+  std::complex<double> IncidenceFunction(const pts2D r) const {
+    return std::exp(std::complex<double>(0.0, 1.0) * kappa * r.x);
+  }
+};
+
+class DFMM {
+ public:
+  inputsToDFMM inputs;
+  userkernel kernel;
+  std::vector<pts2D> gridPoints;
+  bool findPhi = true;
+  int device = 0;
+  ls_op* op = nullptr;
+  int N = 0;
+
+  DFMM(const inputsToDFMM& in, const userkernel& k) : inputs(in), kernel(k) {}
+  DFMM(const DFMM&) = delete;
+  DFMM& operator=(const DFMM&) = delete;
+  ~DFMM() { ls_op_destroy(op); }
+
+  ls_config config() const {
+    ls_config c{};
+    c.nCones_LFR = inputs.nCones_LFR;
+    c.nChebNodes = inputs.nChebNodes;
+    c.yes2DFMM = inputs.yes2DFMM;
+    c.TOL_POW = inputs.TOL_POW;
+    c.degreeOfBases = inputs.degreeOfBases;
+    c.nLevelsUniform = inputs.nLevelsUniform;
+    c.Qchoice = kernel.Qchoice;
+    c.findPhi = findPhi ? 1 : 0;
+    c.reference_rounding = 1;
+    c.L = inputs.L;
+    c.kappa = kernel.kappa;
+    c.n_bumps = (int)kernel.bump_cx.size();
+    for (int i = 0; i < c.n_bumps && i < LS_MAX_BUMPS; ++i) {
+      c.bump_cx[i] = kernel.bump_cx[i];
+      c.bump_cy[i] = kernel.bump_cy[i];
+      c.bump_a[i] = kernel.bump_a[i];
+      c.bump_w[i] = kernel.bump_w[i];
+    }
+    return c;
+  }
+
+  void FMMTreeInitialisation() {
+    ls_config c = config();
+    check(ls_op_create(&c, device, &op), "ls_op_create");
+    ls_op_info_t info;
+    check(ls_op_info(op, &info), "ls_op_info");
+    N = info.N;
+    std::vector<double> xy(2 * (size_t)N);
+    check(ls_op_points(op, xy.data()), "ls_op_points");
+    gridPoints.resize(N);
+    for (int i = 0; i < N; ++i) gridPoints[i] = {xy[2 * i], xy[2 * i + 1]};
+  }
+
+  void MatVecProduct(const Vec& b, Vec& output) {
+    output.resize(b.size());
+    check(ls_matvec_host(op, reinterpret_cast<const double*>(b.data()), reinterpret_cast<double*>(output.data())),
+          "ls_matvec_host");
+  }
+
+  Vec RHS() const {
+    Vec b(N);
+    check(ls_op_rhs(op, reinterpret_cast<double*>(b.data())), "ls_op_rhs");
+    return b;
+  }
+};
+
+// Fixed-m GMRES with `restart` cycles, x0 = 0 (GMRES/GMRES.cpp:307-319).
+inline void RestartedGMRES(int restart, DFMM* S, int m, const inputsToDFMM&, const Vec& b, Vec& solution) {
+  solution.resize(b.size());
+  check(ls_gmres_restarted(S->op, reinterpret_cast<const double*>(b.data()), m, restart,
+                           reinterpret_cast<double*>(solution.data())),
+        "ls_gmres_restarted");
+}
+
+class classGMRES {
+ public:
+  // Tolerance-stopped GMRES (GMRES_Hybrid/include/gmres.hpp:54): fills x,
+  // the final residual estimate, the iteration count and the history.
+  void gmres(DFMM* M, const Vec& b, int maxIterations, double threshold, Vec& x, double& error, int& noOfIterations,
+             std::vector<double>& e) {
+    x.resize(b.size());
+    e.assign(maxIterations + 1, 0.0);
+    double rel = 0.0;
+    const ls_status s = ls_gmres(M->op, reinterpret_cast<const double*>(b.data()), maxIterations, threshold,
+                                 reinterpret_cast<double*>(x.data()), e.data(), &noOfIterations, &rel);
+    if (s != LS_OK && s != LS_E_NOT_CONVERGED) check(s, "ls_gmres");
+    e.resize(noOfIterations + 1);
+    error = e.empty() ? rel : e.back();
+  }
+};
+
+}  // namespace ls

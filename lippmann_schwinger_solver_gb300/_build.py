@@ -12,6 +12,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblsdafmm.so")
+DRIVER = os.path.join(PKG, "gmres_driver")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -73,6 +74,16 @@ def build(verbose=False, force=False):
         r = subprocess.run(link, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(link) + "\n" + r.stdout + r.stderr)
+    # Reference-style C++ driver over the facade (include/ls_dafmm.hpp).
+    src = os.path.join(PKG, "examples", "gmres_driver.cpp")
+    hpp = os.path.join(ROOT, "include", "ls_dafmm.hpp")
+    if force or not os.path.exists(DRIVER) or max(os.path.getmtime(src), os.path.getmtime(hpp),
+                                                   os.path.getmtime(LIB)) > os.path.getmtime(DRIVER):
+        cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), src, "-o", DRIVER, "-L" + PKG,
+               "-llsdafmm", "-Wl,-rpath," + PKG]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
     return LIB
 
 
