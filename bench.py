@@ -291,7 +291,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": 16 * n},
         "gpu_launches": info["n_kernels_per_matvec"] * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_kind, "kernel": "gemv_items_kernel<double2> (M2L)",
+                     "traffic": traffic, "peak_source": peak_kind, "kernel": "gemv_tiles_kernel<double2, 1> (M2L)",
                      "kernel_ms": ms_m2l, "kernel_gflops_fp64": info["m2l_flops"] / (ms_m2l * 1e-3) / 1e9},
         "matvec": {"bytes": info["matvec_bytes"], "flops_fp64": info["matvec_flops"],
                    "achieved_gbs": info["matvec_bytes"] / (ms * 1e-3) / 1e9,

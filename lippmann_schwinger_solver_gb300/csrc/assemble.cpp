@@ -354,6 +354,9 @@ class Builder {
   std::vector<double> gln, glw;
   std::vector<cd> Mleaf;              // (2S+1) x rank, column major
   std::vector<cd> near;               // 9 x rank x rank, row major
+  std::vector<cd> nearVt;             // 9 x rank x nb, row major (factor of near)
+  std::vector<cd> nearE;              // 9 x rank x rank, rounding residual of near
+  std::vector<double> Qpinv;          // nb x rank, row major
   std::vector<std::vector<std::vector<int>>> nbrs;  // [level][box] same-level neighbours
   std::vector<std::vector<Node>> nodes;             // [level][node]
 
@@ -712,17 +715,27 @@ void Builder::precompute() {
     }
   }
   near.assign((size_t)9 * rank * rank, cd(0.0, 0.0));
+  // Factored form for the device: B_q = Vt_q Q^+ + E_q, with Vt_q = V_q (i r^2/4)
+  // (rank x nb) and E_q the residual of the 6-digit rounding (0 without it).
+  nearVt.assign((size_t)9 * rank * nb, cd(0.0, 0.0));
+  nearE.assign((size_t)9 * rank * rank, cd(0.0, 0.0));
+  Qpinv = Qp;
   for (int q = 0; q < 9; ++q)
-    for (int i = 0; i < rank; ++i)
+    for (int i = 0; i < rank; ++i) {
+      for (int l = 0; l < nb; ++l)
+        nearVt[((size_t)q * rank + i) * nb + l] = V[((size_t)q * rank + i) * nb + l] * kI * rB * rB / 4.0;
       for (int c = 0; c < rank; ++c) {
         cd s(0.0, 0.0);
         for (int l = 0; l < nb; ++l) {
           const cd vt = V[((size_t)q * rank + i) * nb + l] * kI * rB * rB / 4.0;
           s += vt * Qp[(size_t)l * rank + c];
         }
+        const cd exact = s;
         if (cfg.reference_rounding) s = cd(round6(s.real()), round6(s.imag()));
         near[((size_t)q * rank + i) * rank + c] = s;
+        nearE[((size_t)q * rank + i) * rank + c] = s - exact;
       }
+    }
 }
 
 // Interaction lists of the children of every box (assign_Child_Interaction,
@@ -905,49 +918,84 @@ void Builder::user_checks() {
       }
 }
 
-// Splits a block into warp items and appends it to a phase.
+// Appends a row-major block (rows x K) with its gather list to a phase.
 static void add_task(GemvPhase& ph, const std::vector<cd>& rowmajor, int rows, int K, const std::vector<int>& idx,
                      int out_off) {
   if (rows <= 0 || K <= 0) return;
-  const long long a0 = (long long)ph.A.size();
-  const int i0 = (int)ph.idx.size();
-  ph.idx.insert(ph.idx.end(), idx.begin(), idx.end());
-  if (K >= kColsThreshold) {
-    ph.A.insert(ph.A.end(), rowmajor.begin(), rowmajor.end());
-    for (int r0 = 0; r0 < rows; r0 += kRowsPerItem) {
-      GemvItem it;
-      it.a_off = a0 + (long long)r0 * K;
-      it.idx_off = i0;
-      it.K = K;
-      it.nr = std::min(kRowsPerItem, rows - r0);
-      it.out_off = out_off + r0;
-      it.lda = K;
-      it.layout = 0;
-      ph.items.push_back(it);
-    }
-  } else {
-    // Column major so that a warp reading one column is coalesced.
-    for (int k = 0; k < K; ++k)
-      for (int r = 0; r < rows; ++r) ph.A.push_back(rowmajor[(size_t)r * K + k]);
-    for (int r0 = 0; r0 < rows; r0 += 32) {
-      GemvItem it;
-      it.a_off = a0 + r0;
-      it.idx_off = i0;
-      it.K = K;
-      it.nr = std::min(32, rows - r0);
-      it.out_off = out_off + r0;
-      it.lda = rows;
-      it.layout = 1;
-      ph.items.push_back(it);
-    }
-  }
+  const long long a0 = (long long)ph.stageA.size();
+  const int i0 = (int)ph.stageIdx.size();
+  ph.stageA.insert(ph.stageA.end(), rowmajor.begin(), rowmajor.begin() + (size_t)rows * K);
+  ph.stageIdx.insert(ph.stageIdx.end(), idx.begin(), idx.end());
+  for (int r = 0; r < rows; ++r) ph.rows.push_back({a0 + (long long)r * K, K, i0, out_off + r});
+  ph.nnz += (long long)rows * K;
 }
 
-static void sort_items(GemvPhase& ph) {
-  // Largest items first so that the grid-stride loop balances.
-  std::stable_sort(ph.items.begin(), ph.items.end(), [](const GemvItem& a, const GemvItem& b) {
-    return (long long)a.K * a.nr > (long long)b.K * b.nr;
+// Column slices per row: long rows are split so that a warp covers fewer
+// rows and the grid has enough warps to hide memory latency. `min_s` is
+// the phase-wide minimum that gives the launch at least ~7,300 warps (one
+// full wave of 48 warps on each of 152 SMs); slices are never shorter than
+// 4 columns.
+static int slices_for(int K, int min_s) {
+  int s = K >= 128 ? 4 : (K >= 48 ? 2 : 1);
+  while (s < min_s && K >= 8 * s) s *= 2;
+  return s;
+}
+
+// Packs the staged rows into tiles (see GemvTile), longest rows first
+// (stable, so that the rows of one block stay together and share their
+// gathers).
+static void finalize(GemvPhase& ph) {
+  std::stable_sort(ph.rows.begin(), ph.rows.end(), [](const GemvPhase::Row& a, const GemvPhase::Row& b) {
+    return a.K > b.K;
   });
+  // First pass: tile boundaries and sizes.
+  struct T { size_t r0; int rows, S, qmax; };
+  std::vector<T> tl;
+  long long total = 0;
+  const long long want_warps = 152LL * 48;
+  int min_s = 1;
+  while (min_s < 8 && (long long)ph.rows.size() * min_s < want_warps * kTileLanes) min_s *= 2;
+  for (size_t r0 = 0; r0 < ph.rows.size();) {
+    const int K = ph.rows[r0].K;
+    const int S = slices_for(K, min_s);
+    const int R = kTileLanes / S;
+    const int rows = (int)std::min<size_t>(R, ph.rows.size() - r0);
+    const int qmax = (K + S - 1) / S;
+    tl.push_back({r0, rows, S, qmax});
+    total += (long long)qmax * kTileLanes;
+    r0 += rows;
+  }
+  ph.A.assign((size_t)total, cd(0.0, 0.0));
+  ph.idx.assign((size_t)total, 0);
+  ph.out.assign(ph.rows.size(), 0);
+  ph.klen.assign(tl.size() * kTileLanes, 0);
+  ph.tiles.clear();
+  long long off = 0;
+  for (size_t t = 0; t < tl.size(); ++t) {
+    const T& d = tl[t];
+    const int R = kTileLanes / d.S;
+    int log2s = 0;
+    while ((1 << log2s) < d.S) ++log2s;
+    for (int r = 0; r < d.rows; ++r) {
+      const GemvPhase::Row& row = ph.rows[d.r0 + r];
+      ph.out[d.r0 + r] = row.out;
+      for (int sl = 0; sl < d.S; ++sl) {
+        const int lane = sl * R + r;
+        int q = 0;
+        for (int k = sl; k < row.K; k += d.S, ++q) {
+          const size_t pos = (size_t)(off + (long long)q * kTileLanes + lane);
+          ph.A[pos] = ph.stageA[(size_t)(row.a + k)];
+          ph.idx[pos] = ph.stageIdx[(size_t)row.idx + k];
+        }
+        ph.klen[t * kTileLanes + lane] = q;
+      }
+    }
+    ph.tiles.push_back({off, d.qmax, d.rows, log2s, (int)(t * kTileLanes), (int)d.r0, 0});
+    off += (long long)d.qmax * kTileLanes;
+  }
+  std::vector<cd>().swap(ph.stageA);
+  std::vector<int>().swap(ph.stageIdx);
+  std::vector<GemvPhase::Row>().swap(ph.rows);
 }
 
 void Builder::pack(HostOperator& op) {
@@ -1048,7 +1096,7 @@ void Builder::pack(HostOperator& op) {
     for (int t = 0; t < nn; ++t)
       if (!T[t].empty())
         add_task(ph, T[t], (int)nodes[j][t].out_charge.size(), (int)src[t].size(), src[t], (int)nodes[j][t].own_charge);
-    sort_items(ph);
+    finalize(ph);
     op.up.push_back(std::move(ph));
   }
 
@@ -1095,7 +1143,7 @@ void Builder::pack(HostOperator& op) {
       add_task(ph, tk.A, tk.rows, tk.K, tk.idx, (int)tk.out);
       std::vector<cd>().swap(tk.A);
     }
-    sort_items(ph);
+    finalize(ph);
     op.m2l = std::move(ph);
   }
 
@@ -1189,7 +1237,7 @@ void Builder::pack(HostOperator& op) {
       add_task(ph, tasks[t].A, tasks[t].rows, tasks[t].K, tasks[t].idx, (int)tasks[t].out);
       std::vector<cd>().swap(tasks[t].A);
     }
-    sort_items(ph);
+    finalize(ph);
     op.down.push_back(std::move(ph));
   }
 }
@@ -1227,6 +1275,9 @@ bool Builder::run(HostOperator& op, std::string& err) {
   for (int i = 0; i < N; ++i) op.q[i] = contrast_fn(cfg, gx_[i], gy_[i]);
   op.kq = kq_;
   op.nearB = near;
+  op.nearVt = nearVt;
+  op.nearE = nearE;
+  op.Qpinv = Qpinv;
   op.M.assign((size_t)rank * (2 * kSeries + 1), cd());
   for (size_t i = 0; i < op.M.size(); ++i) op.M[i] = Mleaf[i];
   // Colleague table of the leaves (getNeighbors, G_FMM2DTree.hpp:1567-1601):

@@ -65,10 +65,14 @@ ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
     delete op;
     return fail(LS_E_CUDA, "ls_op_create: " + err);
   }
-  // Host copies of the blocks are no longer needed.
-  for (auto& p : op->host.up) { std::vector<cd>().swap(p.A); }
-  for (auto& p : op->host.down) { std::vector<cd>().swap(p.A); }
-  std::vector<cd>().swap(op->host.m2l.A);
+  // Host copies of the tiles are no longer needed.
+  auto drop = [](GemvPhase& p) {
+    std::vector<cd>().swap(p.A);
+    std::vector<int>().swap(p.idx);
+  };
+  for (auto& p : op->host.up) drop(p);
+  for (auto& p : op->host.down) drop(p);
+  drop(op->host.m2l);
   *out = op;
   return LS_OK;
 }

@@ -13,12 +13,15 @@ namespace lsg {
 // One phase of gather-GEMV items resident on the device.
 template <class C>
 struct DevPhase {
-  C* A = nullptr;            // blocks (double2 or float2)
-  int* idx = nullptr;        // gather indices
-  GemvItem* items = nullptr;
-  int n_items = 0;
+  C* A = nullptr;            // tiles (double2 or float2)
+  int* idx = nullptr;        // gather indices (same positions as A)
+  int* out = nullptr;        // output element per row
+  int* klen = nullptr;       // length per row
+  GemvTile* tiles = nullptr;
+  int n_tiles = 0;
   int accumulate = 0;
-  long long entries = 0;
+  long long entries = 0;     // true block entries (without tile padding)
+  long long stored = 0;      // stored elements (with padding)
 };
 
 struct DevOperator {
@@ -35,6 +38,13 @@ struct DevOperator {
   double2* nearB = nullptr;  // 9 x rank x rank
   double* kq = nullptr;      // kappa^2 q at the grid points
   int* colleague = nullptr;  // n_leaves x 9
+  // Factored near field: B_q = Vt_q Q^+ + E_q (E_q: 6-digit rounding residual)
+  int n_bases = 0;
+  double2* nearVt = nullptr; // 9 x rank x n_bases
+  double* Qp = nullptr;      // n_bases x rank
+  float2* nearE = nullptr;   // 9 x rank x rank (FP32)
+  double2* cbuf = nullptr;   // n_leaves x n_bases: Q^+ x per leaf
+  float2* x32 = nullptr;     // N: x in FP32 for the E_q term
   // FP32 operator (mixed precision), built on request
   bool has_f32 = false;
   std::vector<DevPhase<float2>> up32, down32;

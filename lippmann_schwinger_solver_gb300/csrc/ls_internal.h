@@ -13,30 +13,41 @@ namespace lsg {
 
 using cd = std::complex<double>;
 
-// One warp-sized unit of a gather-GEMV phase:
-//   dst[out_off + r] (=|+=) sum_k A[r, k] * src[idx[idx_off + k]],  r < nr.
-// Blocks with K >= kColsThreshold are stored row major (lanes stride over
-// K); narrower blocks are stored column major (one lane per row).
-struct GemvItem {
-  long long a_off;   // element offset of row 0 of this item in A
-  int idx_off;       // offset of the gather list in idx
-  int K;             // columns
-  int nr;            // rows handled by this item
-  int out_off;       // output element offset
-  int lda;           // row-major: K; column-major: total rows of the block
-  int layout;        // 0 = row major (lanes over K), 1 = column major (lane per row)
+// One warp tile of a gather-GEMV phase. Rows of all blocks of a phase are
+// sorted by length and packed R = 32 / S to a tile; each row is split into
+// S interleaved column slices (S = 4 for long rows, 1 for short ones), so
+// lane l = s * R + r sums columns k = q * S + s of row r. Element (q, l)
+// sits at a_off + 32 q + l in A and idx: every warp load is one contiguous
+// line. After the loop the S slice sums are combined with shuffles and the
+// lanes of slice 0 write:
+//   dst[out[row_base + r]] (=|+=) sum_k A(r, k) * src[idx(r, k)]
+struct GemvTile {
+  long long a_off;  // first element of the tile in A / idx
+  int qmax;         // steps of the longest lane
+  int rows;         // rows in the tile (<= R)
+  int log2s;        // S = 1 << log2s column slices per row
+  int lane_base;    // offset of the tile's 32 lane lengths in qlen
+  int row_base;     // offset of the tile's rows in out
+  int pad;
 };
 
-constexpr int kRowsPerItem = 12;   // rows per warp item in the row-major kernel
-constexpr int kColsThreshold = 64; // K below this uses the lane-per-row kernel
+constexpr int kTileLanes = 32;
 
 // A phase (or one tree level of a phase) in device-ready form.
 struct GemvPhase {
-  std::vector<cd> A;            // concatenated blocks
-  std::vector<int> idx;         // gather indices into the source buffer
-  std::vector<GemvItem> items;
+  std::vector<cd> A;            // tiles, column interleaved (zero padded)
+  std::vector<int> idx;         // gather indices, same positions as A
+  std::vector<int> out;         // output element of each row
+  std::vector<int> klen;        // steps of each lane (32 per tile)
+  std::vector<GemvTile> tiles;
   int accumulate = 0;           // 0: overwrite, 1: accumulate into dst
-  long long entries() const { return (long long)A.size(); }
+  long long nnz = 0;            // true (unpadded) block entries
+  // Staging before packing: blocks row major, one record per row.
+  struct Row { long long a; int K; int idx; int out; };
+  std::vector<cd> stageA;
+  std::vector<int> stageIdx;
+  std::vector<Row> rows;
+  long long entries() const { return nnz; }
 };
 
 // Host-side intermediate representation of an assembled operator.
@@ -46,6 +57,9 @@ struct HostOperator {
   std::vector<double> px, py, q;     // grid points and contrast
   std::vector<int> colleague;        // n_leaves x 9, -1 = none
   std::vector<cd> nearB;             // 9 x rank x rank, row major
+  std::vector<cd> nearVt;            // 9 x rank x n_bases: B_q = Vt_q Q^+ + E_q
+  std::vector<cd> nearE;             // 9 x rank x rank: residual of the 6-digit rounding
+  std::vector<double> Qpinv;         // n_bases x rank: Q^+
   std::vector<cd> M;                 // rank x 31 (leaf level), row major
   std::vector<double> kq;            // kappa^2 q at the grid points
   long long charges_len = 0;         // x (N) + skeleton charges

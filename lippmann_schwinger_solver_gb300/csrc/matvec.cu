@@ -41,144 +41,56 @@ __device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b
 __device__ __forceinline__ double2 ld_stream(const double2* p) { return __ldcs(p); }
 __device__ __forceinline__ float2 ld_stream(const float2* p) { return __ldcs(p); }
 
-// Warp reduction of kRowsPerItem complex partial sums (2 * kRowsPerItem
-// reals per lane) that halves the values each lane carries at every step:
-// after offsets 16, 8, 4 a lane holds 3 of the 24 values, summed over the 8
-// lanes that share its bits 2..4, and offsets 2, 1 finish the sum. It needs
-// 12 + 6 + 3 + 3 + 3 = 27 additions per lane instead of 5 * 24 = 120.
-// On return the lanes with (lane & 3) == 0 hold values base..base+2 with
-// base = 12 * bit4 + 6 * bit3 + 3 * bit2; value v is row v / 2, part v % 2.
-template <class R>
-__device__ __forceinline__ void transpose_reduce24(R (&v)[24], int lane, R (&out)[3]) {
-  static_assert(kRowsPerItem == 12, "reduction written for 12 rows");
-  R w[12];
-  {
-    const bool hi = lane & 16;
-#pragma unroll
-    for (int i = 0; i < 12; ++i) {
-      const R send = hi ? v[i] : v[i + 12];
-      const R keep = hi ? v[i + 12] : v[i];
-      w[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-  }
-  R u[6];
-  {
-    const bool hi = lane & 8;
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      const R send = hi ? w[i] : w[i + 6];
-      const R keep = hi ? w[i + 6] : w[i];
-      u[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-  }
-  {
-    const bool hi = lane & 4;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const R send = hi ? u[i] : u[i + 3];
-      const R keep = hi ? u[i + 3] : u[i];
-      out[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    out[i] += __shfl_xor_sync(0xffffffffu, out[i], 2);
-    out[i] += __shfl_xor_sync(0xffffffffu, out[i], 1);
-  }
-}
-
-// Gather-GEMV over a list of warp items (see GemvItem). PHASE only names the
-// instantiation (0 upward, 1 M2L, 2 downward) so that profilers can tell the
-// launches apart.
+// Gather-GEMV over warp tiles (see GemvTile): lane l = s * R + r sums the
+// columns of slice s of row r, 4 steps at a time to keep 4 independent
+// loads of A, idx and the gathered source in flight; the S slices are then
+// combined with shuffles. PHASE only names the instantiation (0 upward,
+// 1 M2L, 2 downward) so that profilers can tell the launches apart.
 template <class C, int PHASE>
-__global__ void __launch_bounds__(256) gemv_items_kernel(const GemvItem* __restrict__ items, int n_items,
-                                                         const C* __restrict__ A, const int* __restrict__ idx,
-                                                         const C* __restrict__ src, C* __restrict__ dst,
-                                                         int accumulate) {
+__global__ void __launch_bounds__(256, 3) gemv_tiles_kernel(const GemvTile* __restrict__ tiles, int n_tiles,
+                                                            const C* __restrict__ A, const int* __restrict__ idx,
+                                                            const int* __restrict__ out, const int* __restrict__ qlen,
+                                                            const C* __restrict__ src, C* __restrict__ dst,
+                                                            int accumulate) {
   using R = typename Real<C>::T;
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_items; w += nw) {
-    const GemvItem it = items[w];
-    const C* __restrict__ Ab = A + it.a_off;
-    const int* __restrict__ ib = idx + it.idx_off;
-    if (it.layout == 0) {
-      // Row major: lanes stride over the K columns, kRowsPerItem rows per warp.
-      R v[2 * kRowsPerItem];
-#pragma unroll
-      for (int r = 0; r < 2 * kRowsPerItem; ++r) v[r] = R(0);
-      const int K = it.K, nr = it.nr;
-      int k = lane;
-      for (; k + 32 < K; k += 64) {
-        const C x0 = src[ib[k]];
-        const C x1 = src[ib[k + 32]];
-#pragma unroll
-        for (int r = 0; r < kRowsPerItem; ++r) {
-          if (r < nr) {
-            const C a0 = ld_stream(Ab + (size_t)r * K + k);
-            const C a1 = ld_stream(Ab + (size_t)r * K + k + 32);
-            v[2 * r] = fma(a0.x, x0.x, v[2 * r]);
-            v[2 * r] = fma(-a0.y, x0.y, v[2 * r]);
-            v[2 * r + 1] = fma(a0.x, x0.y, v[2 * r + 1]);
-            v[2 * r + 1] = fma(a0.y, x0.x, v[2 * r + 1]);
-            v[2 * r] = fma(a1.x, x1.x, v[2 * r]);
-            v[2 * r] = fma(-a1.y, x1.y, v[2 * r]);
-            v[2 * r + 1] = fma(a1.x, x1.y, v[2 * r + 1]);
-            v[2 * r + 1] = fma(a1.y, x1.x, v[2 * r + 1]);
-          }
-        }
-      }
-      if (k < K) {
-        const C x0 = src[ib[k]];
-#pragma unroll
-        for (int r = 0; r < kRowsPerItem; ++r) {
-          if (r < nr) {
-            const C a0 = ld_stream(Ab + (size_t)r * K + k);
-            v[2 * r] = fma(a0.x, x0.x, v[2 * r]);
-            v[2 * r] = fma(-a0.y, x0.y, v[2 * r]);
-            v[2 * r + 1] = fma(a0.x, x0.y, v[2 * r + 1]);
-            v[2 * r + 1] = fma(a0.y, x0.x, v[2 * r + 1]);
-          }
-        }
-      }
-      R out[3];
-      transpose_reduce24(v, lane, out);
-      if ((lane & 3) == 0) {
-        const int base = 12 * ((lane >> 4) & 1) + 6 * ((lane >> 3) & 1) + 3 * ((lane >> 2) & 1);
-        R* d = reinterpret_cast<R*>(dst + it.out_off);
-#pragma unroll
-        for (int t = 0; t < 3; ++t) {
-          const int vv = base + t;
-          if ((vv >> 1) < nr) {
-            if (accumulate) d[vv] += out[t];
-            else d[vv] = out[t];
-          }
-        }
-      }
-    } else {
-      // Column major: one lane per row, loop over the (few) columns.
-      if (lane < it.nr) {
-        R sr = R(0), si = R(0);
-        const C* __restrict__ col = Ab + lane;
-        const int K = it.K;
-        const int lda = it.lda;
-        for (int k = 0; k < K; ++k) {
-          const C x = src[ib[k]];
-          const C a = ld_stream(col + (size_t)k * lda);
-          sr = fma(a.x, x.x, sr);
-          sr = fma(-a.y, x.y, sr);
-          si = fma(a.x, x.y, si);
-          si = fma(a.y, x.x, si);
-        }
-        C* out = dst + it.out_off + lane;
-        if (accumulate) {
-          C o = *out;
-          o.x += sr;
-          o.y += si;
-          *out = o;
-        } else {
-          *out = mk(sr, si);
-        }
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_tiles; w += nw) {
+    const GemvTile t = tiles[w];
+    const int ql = qlen[t.lane_base + lane];
+    const C* __restrict__ a = A + t.a_off + lane;
+    const int* __restrict__ ix = idx + t.a_off + lane;
+    R sr = R(0), si = R(0);
+    int q = 0;
+    for (; q + 4 <= ql; q += 4) {
+      const int i0 = ix[32 * q], i1 = ix[32 * (q + 1)], i2 = ix[32 * (q + 2)], i3 = ix[32 * (q + 3)];
+      const C a0 = ld_stream(a + 32 * q), a1 = ld_stream(a + 32 * (q + 1));
+      const C a2 = ld_stream(a + 32 * (q + 2)), a3 = ld_stream(a + 32 * (q + 3));
+      const C x0 = src[i0], x1 = src[i1], x2 = src[i2], x3 = src[i3];
+      sr = fma(a0.x, x0.x, sr); sr = fma(-a0.y, x0.y, sr); si = fma(a0.x, x0.y, si); si = fma(a0.y, x0.x, si);
+      sr = fma(a1.x, x1.x, sr); sr = fma(-a1.y, x1.y, sr); si = fma(a1.x, x1.y, si); si = fma(a1.y, x1.x, si);
+      sr = fma(a2.x, x2.x, sr); sr = fma(-a2.y, x2.y, sr); si = fma(a2.x, x2.y, si); si = fma(a2.y, x2.x, si);
+      sr = fma(a3.x, x3.x, sr); sr = fma(-a3.y, x3.y, sr); si = fma(a3.x, x3.y, si); si = fma(a3.y, x3.x, si);
+    }
+    for (; q < ql; ++q) {
+      const C a0 = ld_stream(a + 32 * q);
+      const C x0 = src[ix[32 * q]];
+      sr = fma(a0.x, x0.x, sr); sr = fma(-a0.y, x0.y, sr); si = fma(a0.x, x0.y, si); si = fma(a0.y, x0.x, si);
+    }
+    // Combine the slices: lanes r, r + R, r + 2R, ... (R = 32 >> log2s).
+    for (int o = 16; o >= (32 >> t.log2s); o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane < t.rows) {
+      C* o = dst + out[t.row_base + lane];
+      if (accumulate) {
+        C v = *o;
+        v.x += sr;
+        v.y += si;
+        *o = v;
+      } else {
+        *o = mk(sr, si);
       }
     }
   }
@@ -221,6 +133,94 @@ __global__ void __launch_bounds__(256) near_kernel(int n_out, int rank, const C*
   }
 }
 
+// Near field, factored form (FP64 path). The colleague blocks are
+// B_q = Vt_q Q^+ + E_q: Vt_q (rank x n_bases) and Q^+ come from the
+// quadrature (NearFieldInteraction1 V times i r^2/4, and the Chebyshev
+// pseudo-inverse), E_q is what the reference's 6-digit rounding of B_q
+// added (|E_q| <= 5e-7 |B_q|, zero without the rounding). The product
+// B_q x = Vt_q (Q^+ x) + E_q x then needs Q^+ x once per leaf and
+// rank x n_bases FP64 multiply-adds per colleague instead of rank x rank;
+// E_q x is accumulated in FP32, which keeps its absolute error near
+// 3e-14 |B_q| |x|.
+//
+// Pass 1: c_s = Q^+ x_s for every leaf s (one thread per (s, j < n_bases)),
+// and x in FP32 (grid-stride over the N points).
+__global__ void __launch_bounds__(256) near_coeff_kernel(int n_leaves, int rank, int nb, const double* __restrict__ Qp,
+                                                         const double2* __restrict__ x, double2* __restrict__ c,
+                                                         float2* __restrict__ x32) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = n_leaves * rank;
+  for (int i = t; i < n; i += gridDim.x * blockDim.x) {
+    const double2 xv = x[i];
+    x32[i] = make_float2((float)xv.x, (float)xv.y);
+  }
+  if (t >= n_leaves * nb) return;
+  const int s = t / nb, j = t - s * nb;
+  const double* __restrict__ q = Qp + (size_t)j * rank;
+  const double2* __restrict__ xs = x + (size_t)s * rank;
+  double cr = 0.0, ci = 0.0;
+  for (int i = 0; i < rank; ++i) {
+    const double w = q[i];
+    const double2 v = xs[i];
+    cr = fma(w, v.x, cr);
+    ci = fma(w, v.y, ci);
+  }
+  c[t] = make_double2(cr, ci);
+}
+
+// Pass 2: y = P + kappa^2 q .* sum_q (Vt_q c_nb(q) + E_q x_nb(q)) + x.
+__global__ void __launch_bounds__(256) near_factored_kernel(int n_out, int rank, int nb,
+                                                            const double2* __restrict__ Vt,
+                                                            const float2* __restrict__ E,
+                                                            const double* __restrict__ kq,
+                                                            const int* __restrict__ coll,
+                                                            const double2* __restrict__ c,
+                                                            const float2* __restrict__ x32,
+                                                            const double2* __restrict__ x,
+                                                            const double2* __restrict__ P, double2* __restrict__ y,
+                                                            int find_phi) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_out) return;
+  const int leaf = t / rank, row = t - leaf * rank;
+  double ar = 0.0, ai = 0.0;
+#pragma unroll 1
+  for (int n = 0; n < 9; ++n) {
+    const int nbx = coll[leaf * 9 + n];
+    if (nbx < 0) continue;
+    const double2* __restrict__ v = Vt + ((size_t)n * rank + row) * nb;
+    const double2* __restrict__ cc = c + (size_t)nbx * nb;
+    for (int l = 0; l < nb; ++l) {
+      const double2 a = v[l];
+      const double2 b = cc[l];
+      ar = fma(a.x, b.x, ar);
+      ar = fma(-a.y, b.y, ar);
+      ai = fma(a.x, b.y, ai);
+      ai = fma(a.y, b.x, ai);
+    }
+    const float2* __restrict__ e = E + ((size_t)n * rank + row) * rank;
+    const float2* __restrict__ xs = x32 + (size_t)nbx * rank;
+    float er = 0.0f, ei = 0.0f;
+    for (int k = 0; k < rank; ++k) {
+      const float2 a = e[k];
+      const float2 b = xs[k];
+      er = fmaf(a.x, b.x, er);
+      er = fmaf(-a.y, b.y, er);
+      ei = fmaf(a.x, b.y, ei);
+      ei = fmaf(a.y, b.x, ei);
+    }
+    ar += (double)er;
+    ai += (double)ei;
+  }
+  const double2 p = P[t];
+  if (find_phi) {
+    const double s = kq[t];
+    const double2 xs = x[t];
+    y[t] = make_double2(p.x + s * ar + xs.x, p.y + s * ai + xs.y);
+  } else {
+    y[t] = make_double2(p.x + ar, p.y + ai);
+  }
+}
+
 __global__ void d2f_kernel(const double2* __restrict__ a, float2* __restrict__ b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     b[i] = make_float2((float)a[i].x, (float)a[i].y);
@@ -242,11 +242,12 @@ static int sm_count(int dev) {
 
 template <int PHASE, class C>
 static void launch_gemv(const DevPhase<C>& ph, const C* src, C* dst, cudaStream_t s, int dev) {
-  if (ph.n_items == 0) return;
+  if (ph.n_tiles == 0) return;
   const int warps_per_block = 8;
-  int blocks = (ph.n_items + warps_per_block - 1) / warps_per_block;
+  int blocks = (ph.n_tiles + warps_per_block - 1) / warps_per_block;
   blocks = std::min(blocks, sm_count(dev) * 8);
-  gemv_items_kernel<C, PHASE><<<blocks, 256, 0, s>>>(ph.items, ph.n_items, ph.A, ph.idx, src, dst, ph.accumulate);
+  gemv_tiles_kernel<C, PHASE><<<blocks, 256, 0, s>>>(ph.tiles, ph.n_tiles, ph.A, ph.idx, ph.out, ph.klen, src, dst,
+                                                     ph.accumulate);
 }
 
 template <class T>
@@ -262,17 +263,28 @@ static bool dmalloc(T** p, size_t n, long long& total, std::string& err) {
   return true;
 }
 
-static bool upload_phase(const GemvPhase& h, DevPhase<double2>& d, long long& total, std::string& err) {
-  d.n_items = (int)h.items.size();
-  d.accumulate = h.accumulate;
-  d.entries = (long long)h.A.size();
-  if (!dmalloc(&d.A, h.A.size(), total, err)) return false;
-  if (!dmalloc(&d.idx, h.idx.size(), total, err)) return false;
-  if (!dmalloc(&d.items, h.items.size(), total, err)) return false;
-  if (h.A.size() && cudaMemcpy(d.A, h.A.data(), h.A.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess) { err = "upload A"; return false; }
-  if (h.idx.size() && cudaMemcpy(d.idx, h.idx.data(), h.idx.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) { err = "upload idx"; return false; }
-  if (h.items.size() && cudaMemcpy(d.items, h.items.data(), h.items.size() * sizeof(GemvItem), cudaMemcpyHostToDevice) != cudaSuccess) { err = "upload items"; return false; }
+template <class T>
+static bool upload(T** d, const std::vector<T>& h, long long& total, std::string& err) {
+  if (!dmalloc(d, h.size(), total, err)) return false;
+  if (h.size() && cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) {
+    err = "upload failed";
+    return false;
+  }
   return true;
+}
+
+static bool upload_phase(const GemvPhase& h, DevPhase<double2>& d, long long& total, std::string& err) {
+  d.n_tiles = (int)h.tiles.size();
+  d.accumulate = h.accumulate;
+  d.entries = h.nnz;
+  d.stored = (long long)h.A.size();
+  if (!dmalloc(&d.A, h.A.size(), total, err)) return false;
+  if (h.A.size() && cudaMemcpy(d.A, h.A.data(), h.A.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess) {
+    err = "upload A";
+    return false;
+  }
+  return upload(&d.idx, h.idx, total, err) && upload(&d.out, h.out, total, err) &&
+         upload(&d.klen, h.klen, total, err) && upload(&d.tiles, h.tiles, total, err);
 }
 
 bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
@@ -306,14 +318,27 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
   cudaMemcpy(d.nearB, h.nearB.data(), h.nearB.size() * sizeof(double2), cudaMemcpyHostToDevice);
   cudaMemcpy(d.kq, h.kq.data(), h.kq.size() * sizeof(double), cudaMemcpyHostToDevice);
   cudaMemcpy(d.colleague, h.colleague.data(), h.colleague.size() * sizeof(int), cudaMemcpyHostToDevice);
+  {
+    d.n_bases = h.n_bases;
+    std::vector<float2> e32(h.nearE.size());
+    for (size_t i = 0; i < e32.size(); ++i) e32[i] = make_float2((float)h.nearE[i].real(), (float)h.nearE[i].imag());
+    if (!dmalloc(&d.nearVt, h.nearVt.size(), tot, err)) return false;
+    if (!dmalloc(&d.Qp, h.Qpinv.size(), tot, err)) return false;
+    if (!dmalloc(&d.nearE, e32.size(), tot, err)) return false;
+    if (!dmalloc(&d.cbuf, (size_t)h.n_leaves * h.n_bases, tot, err)) return false;
+    if (!dmalloc(&d.x32, (size_t)h.N, tot, err)) return false;
+    cudaMemcpy(d.nearVt, h.nearVt.data(), h.nearVt.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    cudaMemcpy(d.Qp, h.Qpinv.data(), h.Qpinv.size() * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(d.nearE, e32.data(), e32.size() * sizeof(float2), cudaMemcpyHostToDevice);
+  }
   cudaMemset(d.xbuf, 0, (size_t)h.N * sizeof(double2));
   cudaMemset(d.ybuf, 0, (size_t)h.N * sizeof(double2));
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return false; }
-  int launches = 1;  // near kernel
-  for (auto& p : d.up) launches += p.n_items > 0;
-  launches += d.m2l.n_items > 0;
-  for (auto& p : d.down) launches += p.n_items > 0;
+  int launches = 2;  // near coefficient + near kernels
+  for (auto& p : d.up) launches += p.n_tiles > 0;
+  launches += d.m2l.n_tiles > 0;
+  for (auto& p : d.down) launches += p.n_tiles > 0;
   d.launches_per_matvec = launches;
   return true;
 }
@@ -322,7 +347,9 @@ template <class C>
 static void free_phase(DevPhase<C>& p) {
   cudaFree(p.A);
   cudaFree(p.idx);
-  cudaFree(p.items);
+  cudaFree(p.out);
+  cudaFree(p.klen);
+  cudaFree(p.tiles);
   p = DevPhase<C>();
 }
 
@@ -331,11 +358,12 @@ void dev_free(DevOperator& d) {
   for (auto& p : d.up) free_phase(p);
   for (auto& p : d.down) free_phase(p);
   free_phase(d.m2l);
-  // FP32 phases share idx / items with the FP64 phases; only A is theirs.
+  // FP32 phases share idx / out / klen / tiles with the FP64 phases; only A is theirs.
   for (auto& p : d.up32) cudaFree(p.A);
   for (auto& p : d.down32) cudaFree(p.A);
   cudaFree(d.m2l32.A);
   cudaFree(d.S); cudaFree(d.P); cudaFree(d.nearB); cudaFree(d.kq); cudaFree(d.colleague);
+  cudaFree(d.nearVt); cudaFree(d.Qp); cudaFree(d.nearE); cudaFree(d.cbuf); cudaFree(d.x32);
   cudaFree(d.S32); cudaFree(d.P32); cudaFree(d.nearB32); cudaFree(d.kq32);
   cudaFree(d.xbuf); cudaFree(d.ybuf);
   for (auto& ev : d.ev) if (ev) cudaEventDestroy(ev);
@@ -344,13 +372,16 @@ void dev_free(DevOperator& d) {
 }
 
 static bool f32_phase(const DevPhase<double2>& a, DevPhase<float2>& b, long long& tot, std::string& err) {
-  b.n_items = a.n_items;
+  b.n_tiles = a.n_tiles;
   b.accumulate = a.accumulate;
   b.entries = a.entries;
-  if (!dmalloc(&b.A, (size_t)a.entries, tot, err)) return false;
-  b.idx = a.idx;      // shared with the FP64 phase
-  b.items = a.items;  // shared
-  if (a.entries) d2f_kernel<<<1024, 256>>>(a.A, b.A, a.entries);
+  b.stored = a.stored;
+  if (!dmalloc(&b.A, (size_t)a.stored, tot, err)) return false;
+  b.idx = a.idx;  // shared with the FP64 phase
+  b.out = a.out;
+  b.klen = a.klen;
+  b.tiles = a.tiles;
+  if (a.stored) d2f_kernel<<<1024, 256>>>(a.A, b.A, a.stored);
   return true;
 }
 
@@ -386,7 +417,10 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down) launch_gemv<2>(ph, (const double2*)d.P, d.P, s, d.device);
   const int n = d.N;
-  near_kernel<double2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB, d.kq, d.colleague, d.S, d.P, y, d.find_phi);
+  near_coeff_kernel<<<(d.n_leaves * d.n_bases + 255) / 256, 256, 0, s>>>(d.n_leaves, d.rank, d.n_bases, d.Qp, d.S,
+                                                                         d.cbuf, d.x32);
+  near_factored_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.n_bases, d.nearVt, d.nearE, d.kq, d.colleague,
+                                                       d.cbuf, d.x32, d.S, d.P, y, d.find_phi);
   return cudaGetLastError();
 }
 
