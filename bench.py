@@ -210,9 +210,12 @@ def run_ours(args):
     yd = torch.empty_like(xd)
     stream = torch.cuda.Stream(device=local)
     sp = stream.cuda_stream
+    prec = ls.LS_PREC_F32 if args.precision == "f32" else ls.LS_PREC_F64
+    if prec == ls.LS_PREC_F32:
+        op.enable_f32()
     # warm-up
     for _ in range(max(3, args.warmup)):
-        op.matvec_device(xd.data_ptr(), yd.data_ptr(), sp)
+        op.matvec_device(xd.data_ptr(), yd.data_ptr(), sp, precision=prec)
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
@@ -223,14 +226,20 @@ def run_ours(args):
         time.sleep(0.3)
         ev0.record(stream)
         for _ in range(args.steps):
-            op.matvec_device(xd.data_ptr(), yd.data_ptr(), sp)
+            op.matvec_device(xd.data_ptr(), yd.data_ptr(), sp, precision=prec)
         ev1.record(stream)
         torch.cuda.synchronize()
         time.sleep(0.3)
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, f"cuda:{local}")
     value = replica_throughput(world, ms)
     # Dominant kernel (M2L) timed with events on the operator's own stream.
-    ms_mv, ms_m2l = op.time_matvec(warmup=3, iters=max(5, args.steps))
+    ms_mv, ms_m2l = op.time_matvec(warmup=3, iters=max(5, args.steps), precision=prec)
+    if prec == ls.LS_PREC_F32:
+        # Profiling / reference run of the FP32 operator: one JSON line, no e2e.
+        print(json.dumps({"metric": "DAFMM matvec throughput, FP32 operator", "value": world * 1e3 / ms,
+                          "unit": "matvec/s", "ms_per_step": ms, "m2l_ms": ms_m2l, "n_gpus": world}), flush=True)
+        op.close()
+        return
     # End to end through the C ABI with host buffers (pinned).
     xh = torch.from_numpy(x).pin_memory()
     yh = torch.empty_like(xh).pin_memory()
@@ -320,6 +329,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--max-iter", type=int, default=400)
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32"],
+                    help="operator precision of the timed loop (f32: profiling run of the FP32 operator)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -382,3 +382,28 @@ class classGMRES:  # noqa: N801 - reference name
 
 def RestartedGMRES(restart, S, m, inputs, b):  # noqa: N802 - reference name
     return S.K.gmres_restarted(b, m, restart)
+
+
+def scattered_field(cfg, phi, device=0):
+    """Scattered and total field from the solved density (GMRES/GMRES.cpp:581-597).
+
+    A second operator with findPhi = 0 (the bare volume potential G, no
+    q scaling and no identity) is assembled on the same tree. It gives
+    u_scat = G phi and u_tot = u_inc + u_scat, where u_inc = exp(i kappa x1).
+    It also returns the residual of the Lippmann-Schwinger identity
+    phi / kappa^2 + q u_tot = 0, the check that
+    GMRES_Hybrid/LippmannSchwinger/main/hybridTrueValidation_gmres.cpp:227-232
+    prints, as an absolute 2-norm.
+    """
+    if isinstance(cfg, dict):
+        cfg = Config(**cfg)
+    g = Config(**{**dataclasses.asdict(cfg), "findPhi": 0})
+    with Operator(g, device) as op2:
+        phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        u_scat = op2.matvec(phi)
+        pts = op2.points()
+        q = op2.contrast()
+    u_inc = np.exp(1j * cfg.kappa * pts[:, 0])
+    u_tot = u_inc + u_scat
+    err = np.linalg.norm(phi / cfg.kappa ** 2 + q * u_tot)
+    return u_scat, u_tot, float(err)

@@ -221,6 +221,53 @@ __global__ void __launch_bounds__(256) near_factored_kernel(int n_out, int rank,
   }
 }
 
+// Near field of the FP32 operator. The 9 colleague blocks (9 x rank x rank
+// float2, 93 KB at rank 36) are staged once per thread block in shared
+// memory, transposed so that the threads of one leaf (one per row) read
+// consecutive words; the block then walks groups of leaves. y stays FP64 on
+// the boundary.
+__global__ void __launch_bounds__(256) near32_smem_kernel(int n_leaves, int rank, const float2* __restrict__ B,
+                                                          const float* __restrict__ kq, const int* __restrict__ coll,
+                                                          const float2* __restrict__ x, const float2* __restrict__ P,
+                                                          double2* __restrict__ y, int find_phi) {
+  extern __shared__ float2 sB[];  // [n][c][row]
+  const int rr = rank * rank;
+  for (int i = threadIdx.x; i < 9 * rr; i += blockDim.x) {
+    const int n = i / rr, rem = i - n * rr, row = rem / rank, c = rem - row * rank;
+    sB[(n * rank + c) * rank + row] = B[i];
+  }
+  __syncthreads();
+  const int per = blockDim.x / rank;  // leaves handled together
+  const int local = threadIdx.x / rank, row = threadIdx.x - local * rank;
+  if (local >= per) return;
+  for (int leaf = blockIdx.x * per + local; leaf < n_leaves; leaf += gridDim.x * per) {
+    float ar = 0.0f, ai = 0.0f;
+    for (int n = 0; n < 9; ++n) {
+      const int nb = coll[leaf * 9 + n];
+      if (nb < 0) continue;
+      const float2* __restrict__ xn = x + (size_t)nb * rank;
+      const float2* __restrict__ bn = sB + (size_t)n * rr + row;
+      for (int c = 0; c < rank; ++c) {
+        const float2 a = bn[c * rank];
+        const float2 v = xn[c];
+        ar = fmaf(a.x, v.x, ar);
+        ar = fmaf(-a.y, v.y, ar);
+        ai = fmaf(a.x, v.y, ai);
+        ai = fmaf(a.y, v.x, ai);
+      }
+    }
+    const int t = leaf * rank + row;
+    const float2 p = P[t];
+    if (find_phi) {
+      const float s = kq[t];
+      const float2 xs = x[t];
+      y[t] = make_double2((double)(p.x + s * ar + xs.x), (double)(p.y + s * ai + xs.y));
+    } else {
+      y[t] = make_double2((double)(p.x + ar), (double)(p.y + ai));
+    }
+  }
+}
+
 __global__ void d2f_kernel(const double2* __restrict__ a, float2* __restrict__ b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     b[i] = make_float2((float)a[i].x, (float)a[i].y);
@@ -400,6 +447,8 @@ bool dev_enable_f32(DevOperator& d, std::string& err) {
   if (!dmalloc(&d.nearB32, (size_t)nb, tot, err)) return false;
   if (!dmalloc(&d.kq32, (size_t)d.N, tot, err)) return false;
   d2f_kernel<<<256, 256>>>(d.nearB, d.nearB32, nb);
+  if (nb * sizeof(float2) <= 200 * 1024)
+    cudaFuncSetAttribute(near32_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(nb * sizeof(float2)));
   d2f_real_kernel<<<256, 256>>>(d.kq, d.kq32, d.N);
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { err = std::string("enable_f32: ") + cudaGetErrorString(e); return false; }
@@ -434,8 +483,17 @@ cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStr
   launch_gemv<1>(d.m2l32, (const float2*)d.S32, d.P32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[3], s);
   for (auto& ph : d.down32) launch_gemv<2>(ph, (const float2*)d.P32, d.P32, s, d.device);
-  const int n = d.N;
-  near_kernel<float2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB32, d.kq32, d.colleague, d.S32, d.P32, y, d.find_phi);
+  const size_t smem = (size_t)9 * d.rank * d.rank * sizeof(float2);
+  if (smem <= 200 * 1024) {
+    const int per = 256 / d.rank;
+    const int blocks = std::min((d.n_leaves + per - 1) / per, sm_count(d.device) * 2);
+    near32_smem_kernel<<<blocks, per * d.rank, smem, s>>>(d.n_leaves, d.rank, d.nearB32, d.kq32, d.colleague, d.S32,
+                                                           d.P32, y, d.find_phi);
+  } else {  // blocks too large for shared memory (nChebNodes 8)
+    const int n = d.N;
+    near_kernel<float2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB32, d.kq32, d.colleague, d.S32, d.P32, y,
+                                                        d.find_phi);
+  }
   return cudaGetLastError();
 }
 
