@@ -440,6 +440,11 @@ class Builder {
   void pack(HostOperator& op);
 };
 
+// First index of the largest |v| among the unused ones (strict >, so ties
+// go to the lowest index, ACA.hpp:153-166). With every index used the
+// reference dereferences begin() of an empty std::set, which reads the
+// set's element count (0) with libstdc++: index 0, after which the ACA loop
+// ends on rank == min(rows, cols).
 static int argmax_remaining(const std::vector<cd>& v, const std::vector<char>& used) {
   int idx = -1;
   double mx = 0.0;
@@ -448,7 +453,7 @@ static int argmax_remaining(const std::vector<cd>& v, const std::vector<char>& u
     if (idx < 0) { idx = i; mx = std::abs(v[i]); continue; }
     if (std::abs(v[i]) > mx) { idx = i; mx = std::abs(v[idx]); }
   }
-  return idx;
+  return idx < 0 ? 0 : idx;
 }
 static double norm2(const std::vector<cd>& v) {
   double s = 0.0;
