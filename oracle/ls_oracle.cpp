@@ -8,8 +8,11 @@
 //
 // It is the checker for the GPU product and the timed CPU baseline. Nothing
 // in the product links or calls it. Each routine names the reference lines
-// it restates. Parity unpinned: the reference needs Eigen and Boost.Math,
-// which are absent, so it was never run here and ships no golden vectors.
+// it restates. The reference needs Eigen and Boost.Math, which are absent,
+// so it was never run here, and it ships no golden vectors. The pin to its
+// printed output goes through ls_oracle_adaptive.cpp, which reproduces the
+// reference's published assembly log and, on a uniform tree, this file's
+// skeletons exactly.
 //
 // Arithmetic conventions that keep the restatement deterministic:
 //  * compiled with -ffp-contract=off, so no fused multiply-adds appear on

@@ -7,13 +7,18 @@
  * this library, and only as the checker or as the CPU baseline; the
  * product never links, loads or calls it.
  *
- * Parity status: parity unpinned. The reference needs Eigen and
- * Boost.Math, which are absent, so it cannot be compiled and run here, and
- * the reference ships no golden vectors or known-answer tests. The oracle
- * is pinned instead by independent checks (Bessel functions and
- * Gauss-Legendre rules against scipy/numpy, quadrature against scipy
- * integration, the DAFMM matvec against the dense getMatrixEntry2
- * operator) -- see tests/test_oracle_*.py.
+ * Parity status: pinned to the reference's own printed output. The
+ * reference needs Eigen and Boost.Math, which are absent, so it cannot be
+ * compiled and run here, and it ships no golden vectors or known-answer
+ * tests. Its README (GMRES/Readme.md:43-60, 103-113) publishes the assembly
+ * log of its default adaptive run: tree depth, level_LFR, number of points,
+ * boxes per level and the largest NCA rank per level and direction. The
+ * adaptive-tree restatement (ls_oracle_adaptive.cpp) reproduces all of
+ * them, and on a uniform tree it reproduces this oracle's skeletons point
+ * for point (tests/test_oracle_pinned.py). The numerical pieces are checked
+ * independently: Bessel functions and Gauss-Legendre rules against
+ * scipy/numpy, quadrature against scipy integration, the DAFMM matvec
+ * against the dense getMatrixEntry2 operator (tests/test_oracle_*.py).
  */
 #ifndef LS_ORACLE_H
 #define LS_ORACLE_H
@@ -68,6 +73,15 @@ void ora_set_threads(int n);
 void ora_gauss_legendre(int n, double* nodes, double* weights);
 void ora_bessel_jy(int n, double x, double* j, double* y);
 void ora_colpiv_solve(int m, int n, const double* A, const double* b, double* x);
+
+/* Adaptive tree (ls_oracle_adaptive.cpp): builds the contrast-adapted tree,
+ * its 2:1 level restriction, interaction lists and NCA skeletons, and
+ * reports the per-level statistics the reference prints while assembling.
+ * head = {nLevels, level_LFR, N, records}; 7 ints per record. */
+int ora_adaptive_report(const ora_cfg* cfg, int treeAdaptivity, int* head, int* rec, int cap);
+/* Skeleton node sets of the same build (treeAdaptivity < 0: uniform tree of
+ * nLevelsUniform levels); j, k, cone, then four length-prefixed lists. */
+long ora_adaptive_skeletons(const ora_cfg* cfg, int treeAdaptivity, int* buf, long cap);
 
 #ifdef __cplusplus
 }

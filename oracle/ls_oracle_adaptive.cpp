@@ -1,0 +1,667 @@
+// ORACLE - TEST INFRASTRUCTURE ONLY.
+//
+// Adaptive-tree restatement of the reference's operator construction up to
+// the nested cross approximation, for pinning the oracle to the numbers the
+// reference itself prints. The reference's default path builds an
+// adaptive tree (GMRES/GMRES.cpp:165 createAdaptiveTree + :166
+// makeLevelRestriction_Tree). While it assembles it prints, per level, the
+// tree size and the largest NCA rank with the matrix shape that produced it
+// (GMRES/G_FMM2DTree.hpp:2238, 2384, 3418, 3570). GMRES/Readme.md:43-60
+// publishes that output for one run; tests/test_oracle_pinned.py compares
+// this restatement with it.
+//
+// Restated: createTree :773-831 (resolveContrast :739-754, get_S :675-681,
+// get_Transfer_Matrix :725-737), createAdaptiveTree :891-915,
+// makeLevelRestriction_Tree :1019-1129 (with assign_Tree_Interactions_LFR
+// :966-1017 and getFutureGeneration_LFR :943-964), createCones :1952-1974,
+// assign_Child_Interaction :1356-1498, assignLeafChargeLocations
+// :1150-1163, FarFieldInteraction::evaluateM (levels 0..nLevels, 6-digit
+// text round trip), getMatrixEntry :603-658 and getNodes_LFR :2062-2385 /
+// getNodes_HFR :3232-3571 with the getParticlesFromChildren* helpers.
+
+#include "ora_common.hpp"
+
+#include <omp.h>
+
+namespace ora {
+namespace adaptive {
+
+struct Cone {
+  std::vector<Pair> IL;
+  std::vector<int> oc, ochk, ic, ichk;  // outgoing charge/check, incoming charge/check points
+  int o_rows = 0, o_cols = 0, o_rank = -1, i_rows = 0, i_cols = 0, i_rank = -1;  // for the printed statistics
+};
+
+struct ABox {
+  int level = 0, boxNumber = 0, parentNumber = -1;
+  double radius = 0;
+  Pt c{0, 0};
+  bool leaf = false;
+  std::vector<Pair> nbrs, IL;
+  std::vector<Cone> cones;
+  std::vector<int> chargeLoc;
+  std::vector<int> oc, ochk, ic, ichk;
+  int o_rows = 0, o_cols = 0, o_rank = -1, i_rows = 0, i_cols = 0, i_rank = -1;
+};
+
+struct LevelStat {
+  char dir;  // 'O' outgoing, 'I' incoming
+  int j, nboxes, kmax, rows, cols, rank;
+  bool hfr;
+};
+
+struct AOracle {
+  ora_cfg cfg;
+  int treeAdaptivity = 5;
+  double kappa = 0, L = 1, epsTree = 1e-5;
+  int n1 = 6, rank = 36, nb = 21, S = 15, nLevels = 0, level_LFR = 2;
+  std::vector<std::vector<ABox>> tree;
+  std::vector<std::vector<int>> indexTree;
+  std::vector<Pair> leafNodes;
+  std::vector<double> boxRadius, ConeAperture;
+  std::vector<int> nCones;
+  std::vector<double> cheb1d;
+  std::vector<Pt> chebStd, chebChild;
+  std::vector<double> L2L[4];  // rank x rank, row major
+  std::vector<Pt> grid;
+  std::vector<CMat> M;         // per level: (2S+1) x rank
+  std::vector<LevelStat> stats;
+
+  double contrast(Pt r) const { return contrast_value(cfg, r); }
+  int child_index(int J, int boxNumber) const {
+    const auto& v = indexTree[J];
+    return (int)(std::find(v.begin(), v.end(), boxNumber) - v.begin());
+  }
+
+  // ---- tree creation ------------------------------------------------------
+  void cheb_setup() {
+    n1 = cfg.nChebNodes;
+    rank = n1 * n1;
+    for (int k = 0; k < n1; ++k) cheb1d.push_back(-std::cos((k + 0.5) / n1 * PI));
+    for (int j = 0; j < n1; ++j)
+      for (int k = 0; k < n1; ++k) chebStd.push_back({cheb1d[k], cheb1d[j]});
+    const double sx[4] = {-0.5, 0.5, 0.5, -0.5}, sy[4] = {-0.5, -0.5, 0.5, 0.5};
+    for (int c = 0; c < 4; ++c)
+      for (int j = 0; j < rank; ++j) chebChild.push_back({0.5 * chebStd[j].x + sx[c], 0.5 * chebStd[j].y + sy[c]});
+    auto getS = [&](double x, double y) {
+      double s = 0.5;
+      for (int k = 1; k < n1; ++k) s += chebT(x, k) * chebT(y, k);
+      return 2.0 / n1 * s;
+    };
+    for (int l = 0; l < 4; ++l) {
+      L2L[l].assign((size_t)rank * rank, 0.0);
+      for (int j = 0; j < rank; ++j)
+        for (int k = 0; k < rank; ++k)
+          L2L[l][(size_t)j * rank + k] = getS(chebStd[k].x, chebChild[j + l * rank].x) *
+                                         getS(chebStd[k].y, chebChild[j + l * rank].y);
+    }
+  }
+  // Max error of the Chebyshev interpolant of q from the box's nodes to its
+  // children's nodes (resolveContrast :739-754).
+  double resolve_contrast(const ABox& B) const {
+    std::vector<double> qn(rank), approx(4 * rank), truth(4 * rank);
+    for (int i = 0; i < rank; ++i) qn[i] = contrast({B.radius * chebStd[i].x + B.c.x, B.radius * chebStd[i].y + B.c.y});
+    for (int c = 0; c < 4; ++c)
+      for (int j = 0; j < rank; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < rank; ++k) s += L2L[c][(size_t)j * rank + k] * qn[k];
+        approx[c * rank + j] = s;
+      }
+    for (int i = 0; i < 4 * rank; ++i)
+      truth[i] = contrast({B.radius * chebChild[i].x + B.c.x, B.radius * chebChild[i].y + B.c.y});
+    double e = 0.0;
+    for (int i = 0; i < 4 * rank; ++i) e = std::max(e, std::fabs(truth[i] - approx[i]));
+    return e;
+  }
+  void add_children(int j, int k) {
+    if ((int)tree.size() == j + 1) { tree.emplace_back(); indexTree.emplace_back(); }
+    const ABox P = tree[j][k];
+    const double h = 0.5 * P.radius;
+    for (int c = 0; c < 4; ++c) {
+      ABox B;
+      B.level = j + 1;
+      B.boxNumber = P.boxNumber * 4 + c;
+      B.parentNumber = P.boxNumber;
+      B.radius = 0.5 * P.radius;
+      B.c.x = (c == 0 || c == 3) ? P.c.x - h : P.c.x + h;
+      B.c.y = (c == 0 || c == 1) ? P.c.y - h : P.c.y + h;
+      tree[j + 1].push_back(B);
+      indexTree[j + 1].push_back(B.boxNumber);
+    }
+  }
+  // Uniform tree (createTreeU :833-889): boxes split until the level
+  // nLevelsUniform, and further while a box spans more than three wavelengths.
+  void create_tree_uniform(int j, int k) {
+    const bool c3 = kappa * tree[j][k].radius <= 2 * PI * 3.0;
+    if (c3 && j == cfg.nLevelsUniform) {
+      tree[j][k].leaf = true;
+      leafNodes.push_back({j, k});
+    } else {
+      if ((int)tree.size() == j + 1) { tree.emplace_back(); indexTree.emplace_back(); }
+      const int n = (int)tree[j + 1].size();
+      add_children(j, k);
+      for (int c = 0; c < 4; ++c) create_tree_uniform(j + 1, n + c);
+    }
+  }
+  void create_tree(int j, int k) {
+    const double err = resolve_contrast(tree[j][k]);
+    const bool c1 = err < epsTree;
+    const bool c3 = kappa * tree[j][k].radius / 2 / PI <= 1.0;
+    if (c1 && c3) {
+      tree[j][k].leaf = true;
+      leafNodes.push_back({j, k});
+    } else {
+      if ((int)tree.size() == j + 1) { tree.emplace_back(); indexTree.emplace_back(); }
+      const int n = (int)tree[j + 1].size();
+      add_children(j, k);
+      for (int c = 0; c < 4; ++c) create_tree(j + 1, n + c);
+    }
+  }
+  bool adjacent(int bj, int bk, int nj, int nk) const {
+    const double epsR = std::pow(10, -8);
+    const ABox& A = tree[bj][bk];
+    const ABox& O = tree[nj][nk];
+    return !(std::fabs(A.c.x - O.c.x) >= 3.0 * boxRadius[bj] + boxRadius[nj] - epsR ||
+             std::fabs(A.c.y - O.c.y) >= 3.0 * boxRadius[bj] + boxRadius[nj] - epsR);
+  }
+  // Leaf descendants of (pnj, pni) adjacent to (bj, bk) (getFutureGeneration_LFR).
+  void future_generation(int bj, int bk, int pnj, int pni, std::vector<Pair>& out) const {
+    if (tree[pnj][pni].leaf) {
+      if (adjacent(bj, bk, pnj, pni)) out.push_back({pnj, pni});
+    } else {
+      for (int nc = 0; nc < 4; ++nc) {
+        const int idx = child_index(pnj + 1, 4 * tree[pnj][pni].boxNumber + nc);
+        future_generation(bj, bk, pnj + 1, idx, out);
+      }
+    }
+  }
+  void level_restriction() {
+    for (int pass = 0; pass < nLevels; ++pass) {
+      std::vector<std::vector<std::vector<Pair>>> nb(nLevels + 1);
+      for (int j = 0; j <= nLevels; ++j) nb[j].assign(tree[j].size(), {});
+      for (int c = 0; c < 4; ++c)
+        for (int n = 0; n < 4; ++n) nb[1][c].push_back({1, n});
+      for (int j = 1; j <= nLevels - 1; ++j)
+        for (int k = 0; k < (int)tree[j].size(); ++k) {
+          if (tree[j][k].leaf) continue;
+          for (int c = 0; c < 4; ++c) {
+            const int A = child_index(j + 1, 4 * tree[j][k].boxNumber + c);
+            for (const Pair& p : nb[j][k]) {
+              std::vector<Pair> fg;
+              future_generation(j + 1, A, p.x, p.y, fg);
+              nb[j + 1][A].insert(nb[j + 1][A].end(), fg.begin(), fg.end());
+            }
+          }
+        }
+      std::vector<Pair> old = leafNodes;
+      auto index_of = [&](Pair p) {
+        for (size_t l = 0; l < leafNodes.size(); ++l)
+          if (leafNodes[l].x == p.x && leafNodes[l].y == p.y) return (int)l;
+        return -1;
+      };
+      auto refine = [&](int l, Pair leaf) {
+        old[l].x = -1;
+        tree[leaf.x][leaf.y].leaf = false;
+        const int n0 = (int)tree.size() > leaf.x + 1 ? (int)tree[leaf.x + 1].size() : 0;
+        add_children(leaf.x, leaf.y);
+        for (int c = 0; c < 4; ++c) {
+          tree[leaf.x + 1][n0 + c].leaf = true;
+          leafNodes.push_back({leaf.x + 1, n0 + c});
+        }
+      };
+      for (size_t l = 0; l < old.size(); ++l) {
+        const Pair leaf = leafNodes[l];
+        const int j = leaf.x, k = leaf.y;
+        for (const Pair& p : nb[j][k]) {
+          if (j - p.x >= 2) {
+            const int id = index_of(p);
+            if (old[id].x != -1) refine(id, p);
+          } else if (p.x - j >= 2) {
+            if (old[l].x != -1) refine((int)l, leaf);
+          }
+        }
+      }
+      int cnt = 0;
+      for (size_t l = 0; l < old.size(); ++l)
+        if (old[l].x == -1) { leafNodes.erase(leafNodes.begin() + l - cnt); ++cnt; }
+    }
+  }
+
+  // ---- interaction lists (assign_Child_Interaction :1356-1461) -------------
+  void child_interactions(int c, int j, int k) {
+    const double epsR = std::pow(10, -8);
+    const int A = child_index(j + 1, 4 * tree[j][k].boxNumber + c);
+    ABox& BA = tree[j + 1][A];
+    const std::vector<Pair> pn = tree[j][k].nbrs;
+    for (const Pair& p : pn) {
+      const int pnj = p.x, pni = p.y;
+      const int pnn = tree[pnj][pni].boxNumber;
+      if (j + 1 >= level_LFR || (j + 1 < level_LFR && BA.leaf)) {
+        if (tree[pnj][pni].leaf) {
+          if (!adjacent(j + 1, A, pnj, pni)) BA.IL.push_back({pnj, pni});
+          else BA.nbrs.push_back({pnj, pni});
+        } else {
+          for (int nc = 0; nc < 4; ++nc) {
+            const int Bk = child_index(pnj + 1, 4 * pnn + nc);
+            if (!adjacent(j + 1, A, pnj + 1, Bk)) {
+              BA.IL.push_back({pnj + 1, Bk});
+            } else if (!BA.leaf) {
+              BA.nbrs.push_back({pnj + 1, Bk});
+            } else {
+              std::vector<Pair> fg;
+              future_generation(j + 1, A, pnj + 1, Bk, fg);
+              BA.nbrs.insert(BA.nbrs.end(), fg.begin(), fg.end());
+            }
+          }
+        }
+      } else {
+        const double r = boxRadius[j + 1];
+        if (tree[pnj][pni].leaf) {
+          const ABox& O = tree[pnj][pni];
+          if (std::fabs(BA.c.x - O.c.x) >= kappa * r * r + r + boxRadius[pnj] - epsR ||
+              std::fabs(BA.c.y - O.c.y) >= kappa * r * r + r + boxRadius[pnj] - epsR) {
+            double arg = std::atan2(BA.c.y - O.c.y, BA.c.x - O.c.x);
+            arg = std::fmod(arg + 2 * PI + PI, 2 * PI);
+            BA.cones[int(arg / ConeAperture[j + 1])].IL.push_back({pnj, pni});
+          } else {
+            BA.nbrs.push_back({pnj, pni});
+          }
+        } else {
+          for (int nc = 0; nc < 4; ++nc) {
+            const int Bk = child_index(pnj + 1, 4 * pnn + nc);
+            const ABox& O = tree[pnj + 1][Bk];
+            if (std::fabs(BA.c.x - O.c.x) >= kappa * r * r + r + boxRadius[pnj + 1] - epsR ||
+                std::fabs(BA.c.y - O.c.y) >= kappa * r * r + boxRadius[pnj + 1] - epsR) {
+              double arg = std::atan2(BA.c.y - O.c.y, BA.c.x - O.c.x);
+              arg = std::fmod(arg + 2 * PI + PI, 2 * PI);
+              BA.cones[int(arg / ConeAperture[j + 1])].IL.push_back({pnj + 1, Bk});
+            } else {
+              BA.nbrs.push_back({pnj + 1, Bk});
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // ---- far-field entries --------------------------------------------------
+  void precompute_M() {
+    std::vector<double> gln, glw;
+    gauss_legendre(10, gln, glw);
+    std::vector<Pair> bases;
+    for (int d = 0; d < cfg.degreeOfBases; ++d)
+      for (int a = 0; a < d + 1; ++a) bases.push_back({a, d - a});
+    nb = (int)bases.size();
+    CMat Q(rank, nb);
+    for (int i = 0; i < rank; ++i)
+      for (int l = 0; l < nb; ++l) Q(i, l) = cd(chebT(chebStd[i].x, bases[l].x) * chebT(chebStd[i].y, bases[l].y), 0.0);
+    ColPivQR qr;
+    qr.compute(Q);
+    std::vector<double> Qp((size_t)nb * rank);
+    std::vector<cd> e(rank), xs(nb);
+    for (int i = 0; i < rank; ++i) {
+      std::fill(e.begin(), e.end(), cd(0.0, 0.0));
+      e[i] = cd(1.0, 0.0);
+      qr.solve(e.data(), xs.data());
+      for (int l = 0; l < nb; ++l) Qp[(size_t)l * rank + i] = xs[l].real();
+    }
+    const int nS = 2 * S + 1;
+    M.assign(nLevels + 1, CMat());
+    std::vector<char> has_leaf(nLevels + 1, 0);
+    for (const Pair& lf : leafNodes) has_leaf[lf.x] = 1;
+    for (int j = 0; j <= nLevels; ++j) {
+      if (!has_leaf[j]) continue;  // only leaf levels enter getMatrixEntry
+      const double rj = boxRadius[j];
+      CMat C(nS, nb);
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int t = 0; t < nS * nb; ++t) {
+        const int n = t / nb - S, l = t % nb;
+        const int a = bases[l].x, b = bases[l].y;
+        auto f = [&](double px, double py) -> cd {
+          const double R2 = px * px + py * py;
+          const double normX = std::sqrt(R2);
+          const double argJ = kappa * rj * normX;
+          const double th = std::atan2(py, px);
+          return besselJ(n, argJ) * std::exp(-I * double(n) * th) * chebT(px, a) * chebT(py, b);
+        };
+        C(n + S, l) = rj * rj * adaptive_quad(f, gln, glw, 1e-7);
+      }
+      M[j] = CMat(nS, rank);
+      for (int n = 0; n < nS; ++n)
+        for (int i = 0; i < rank; ++i) {
+          cd s(0.0, 0.0);
+          for (int l = 0; l < nb; ++l) s += C(n, l) * Qp[(size_t)l * rank + i];
+          M[j](n, i) = cfg.reference_rounding ? round6(s) : s;
+        }
+    }
+  }
+  struct HCache {
+    const AOracle* o;
+    std::unordered_map<long long, std::vector<cd>> m;
+    const cd* get(int i, int leaf) {
+      const long long key = (long long)i * 1048576LL + leaf;
+      auto it = m.find(key);
+      if (it != m.end()) return it->second.data();
+      std::vector<cd> h(2 * o->S + 1);
+      const Pt ri = o->grid[i];
+      const ABox& B = o->tree[o->leafNodes[leaf].x][o->leafNodes[leaf].y];
+      const double th = std::atan2(ri.y - B.c.y, ri.x - B.c.x);
+      const double R2 = (ri.y - B.c.y) * (ri.y - B.c.y) + (ri.x - B.c.x) * (ri.x - B.c.x);
+      const double R = o->kappa * std::sqrt(R2);
+      for (int n = -o->S; n <= o->S; ++n) h[n + o->S] = (besselJ(n, R) + I * besselY(n, R)) * std::exp(I * double(n) * th);
+      return m.emplace(key, std::move(h)).first->second.data();
+    }
+  };
+  cd entry(int i, int j, HCache& hc) const {
+    const int l = j / rank, idx = j % rank;
+    const cd* h = hc.get(i, l);
+    const CMat& Ml = M[leafNodes[l].x];
+    cd s = 0.0 + 0.0 * I;
+    for (int n = -S; n <= S; ++n) s += Ml(n + S, idx) * h[n + S];
+    s *= I / 4.0;
+    if (cfg.findPhi) {
+      s *= kappa * kappa * (contrast(grid[i]));
+      if (i == j) s += 1.0;
+    }
+    return s;
+  }
+
+  // ---- node sets (getParticlesFromChildren*) -------------------------------
+  bool lfr_child(int J, int K) const { return J >= level_LFR || (J < level_LFR && tree[J][K].leaf); }
+  template <class Get>
+  void gather_children(int j, int k, bool all_cones, int cone, const Get& get, std::vector<int>& out) const {
+    const int J = j + 1;
+    for (int c = 0; c < 4; ++c) {
+      const int K = child_index(J, 4 * tree[j][k].boxNumber + c);
+      const ABox& ch = tree[J][K];
+      if (all_cones) {
+        if (lfr_child(J, K)) { const auto& v = get(ch); out.insert(out.end(), v.begin(), v.end()); }
+        else for (size_t q = 0; q < ch.cones.size(); ++q) { const auto& v = get(ch.cones[q]); out.insert(out.end(), v.begin(), v.end()); }
+      } else {
+        if (j == level_LFR - 1 || ch.leaf) { const auto& v = get(ch); out.insert(out.end(), v.begin(), v.end()); }
+        else { const auto& v = get(ch.cones[cone / 2]); out.insert(out.end(), v.begin(), v.end()); }
+      }
+    }
+  }
+  // LFR helpers: children as LFR boxes (or all their cones when HFR).
+  std::vector<int> lfr_nodes(int j, int k, int what) const {  // what: 0 oc, 1 ichk
+    if (tree[j][k].leaf) return tree[j][k].chargeLoc;
+    std::vector<int> out;
+    if (what == 0) gather_children(j, k, true, 0, [](const auto& n) -> const std::vector<int>& { return n.oc; }, out);
+    else gather_children(j, k, true, 0, [](const auto& n) -> const std::vector<int>& { return n.ichk; }, out);
+    return out;
+  }
+  std::vector<int> hfr_nodes(int j, int k, int cone, int what) const {
+    if (tree[j][k].leaf) return tree[j][k].chargeLoc;
+    std::vector<int> out;
+    if (what == 0) gather_children(j, k, false, cone, [](const auto& n) -> const std::vector<int>& { return n.oc; }, out);
+    else gather_children(j, k, false, cone, [](const auto& n) -> const std::vector<int>& { return n.ichk; }, out);
+    return out;
+  }
+
+  void lfr_box(int j, int k, double tol, bool outgoing) {
+    ABox& B = tree[j][k];
+    HCache hc{this, {}};
+    std::vector<int> own = lfr_nodes(j, k, outgoing ? 0 : 1);
+    std::vector<int> far;
+    for (const Pair& p : B.IL) {
+      std::vector<int> v = lfr_nodes(p.x, p.y, outgoing ? 1 : 0);
+      far.insert(far.end(), v.begin(), v.end());
+    }
+    std::vector<int> rb, cb;
+    auto E = [&](int i, int jj) { return entry(i, jj, hc); };
+    if (outgoing) {
+      B.o_rows = (int)far.size();
+      B.o_cols = (int)own.size();
+      if (!far.empty() && !own.empty()) {
+        B.o_rank = aca_nodes(far, own, tol, rb, cb, nullptr, E);
+        if (B.o_rank > 0) {
+          for (int r : rb) B.ochk.push_back(far[r]);
+          for (int c : cb) B.oc.push_back(own[c]);
+        }
+      } else {
+        B.oc = own;
+      }
+    } else {
+      B.i_rows = (int)own.size();
+      B.i_cols = (int)far.size();
+      if (!far.empty() && !own.empty()) {
+        B.i_rank = aca_nodes(own, far, tol, rb, cb, nullptr, E);
+        if (B.i_rank > 0) {
+          for (int r : rb) B.ichk.push_back(own[r]);
+          for (int c : cb) B.ic.push_back(far[c]);
+        }
+      } else {
+        B.ichk = own;
+      }
+    }
+  }
+  void hfr_cone(int j, int k, int cone, double tol, bool outgoing) {
+    ABox& B = tree[j][k];
+    Cone& C = B.cones[cone];
+    HCache hc{this, {}};
+    std::vector<int> own = hfr_nodes(j, k, cone, outgoing ? 0 : 1);
+    std::vector<int> far;
+    for (const Pair& p : C.IL) {
+      const ABox& O = tree[p.x][p.y];
+      const double arg = std::atan2(B.c.y - O.c.y, B.c.x - O.c.x);
+      const int coneB = int(std::fmod(arg + 2 * PI, 2 * PI) / ConeAperture[p.x]);
+      std::vector<int> v = hfr_nodes(p.x, p.y, coneB, outgoing ? 1 : 0);
+      far.insert(far.end(), v.begin(), v.end());
+    }
+    std::vector<int> rb, cb;
+    auto E = [&](int i, int jj) { return entry(i, jj, hc); };
+    if (outgoing) {
+      C.o_rows = (int)far.size();
+      C.o_cols = (int)own.size();
+      if (!far.empty() && !own.empty()) {
+        C.o_rank = aca_nodes(far, own, tol, rb, cb, nullptr, E);
+        if (C.o_rank > 0) {
+          for (int r : rb) C.ochk.push_back(far[r]);
+          for (int c : cb) C.oc.push_back(own[c]);
+        }
+      } else {
+        C.oc = own;
+      }
+    } else {
+      C.i_rows = (int)own.size();
+      C.i_cols = (int)far.size();
+      if (!far.empty() && !own.empty()) {
+        C.i_rank = aca_nodes(own, far, tol, rb, cb, nullptr, E);
+        if (C.i_rank > 0) {
+          for (int r : rb) C.ichk.push_back(own[r]);
+          for (int c : cb) C.ic.push_back(far[c]);
+        }
+      } else {
+        C.ichk = own;
+      }
+    }
+  }
+
+  // Replays the reference's per-level bookkeeping in box order: rows / cols
+  // are those of the last cone handled for the box; the rank is that of the
+  // last ACA that ran (the variable is not reset when a cone has no
+  // interaction list).
+  void record(char dir, int j, bool hfr_level, int& stale_rank) {
+    int rankPerLevel = 0, rows_cp = -1, cols_cp = -1, kmax = -1;
+    for (int k = 0; k < (int)tree[j].size(); ++k) {
+      const ABox& B = tree[j][k];
+      int rows = 0, cols = 0;
+      if (B.leaf || !hfr_level) {
+        rows = dir == 'O' ? B.o_rows : B.i_rows;
+        cols = dir == 'O' ? B.o_cols : B.i_cols;
+        const int rk = dir == 'O' ? B.o_rank : B.i_rank;
+        if (rk >= 0) stale_rank = rk;
+      } else {
+        for (const Cone& C : B.cones) {
+          rows = dir == 'O' ? C.o_rows : C.i_rows;
+          cols = dir == 'O' ? C.o_cols : C.i_cols;
+          const int rk = dir == 'O' ? C.o_rank : C.i_rank;
+          if (rk >= 0) stale_rank = rk;
+        }
+      }
+      if (rankPerLevel < stale_rank) {
+        rankPerLevel = stale_rank;
+        rows_cp = rows;
+        cols_cp = cols;
+        kmax = k;
+      }
+    }
+    stats.push_back({dir, j, (int)tree[j].size(), kmax, rows_cp, cols_cp, rankPerLevel, hfr_level});
+  }
+
+  void run() {
+    kappa = cfg.kappa;
+    L = cfg.L;
+    epsTree = std::pow(10, -treeAdaptivity);
+    if (cfg.yes2DFMM == 1) {
+      if (kappa == 0) level_LFR = 2;
+      else level_LFR = (int)std::floor(std::log(kappa * L / 0.35) / std::log(2.0));
+      if (level_LFR < 2) level_LFR = 2;
+    } else {
+      level_LFR = 2;
+    }
+    cheb_setup();
+    tree.assign(1, {});
+    indexTree.assign(1, {0});
+    ABox root;
+    root.radius = L;
+    tree[0].push_back(root);
+    if (treeAdaptivity < 0) create_tree_uniform(0, 0);
+    else create_tree(0, 0);
+    nLevels = (int)tree.size() - 1;
+    boxRadius.push_back(L);
+    for (int j = 1; j <= 10; ++j) boxRadius.push_back(boxRadius[j - 1] / 2.0);
+    if (level_LFR >= nLevels) level_LFR = nLevels - 1;
+    level_restriction();
+    // createCones
+    nCones.push_back((int)(cfg.nCones_LFR * std::pow(2.0, level_LFR - 1)));
+    ConeAperture.push_back(2 * PI / nCones[0]);
+    for (int j = 1; j <= level_LFR - 1; ++j) {
+      nCones.push_back((int)(nCones[j - 1] / 2.0));
+      ConeAperture.push_back(ConeAperture[j - 1] * 2.0);
+    }
+    for (int j = 0; j <= level_LFR - 1; ++j)
+      for (auto& B : tree[j])
+        if (!B.leaf) B.cones.assign(nCones[j], Cone());
+    // assign_Tree_Interactions
+    for (int c = 0; c < 4; ++c)
+      for (int n = 0; n < 4; ++n) tree[1][c].nbrs.push_back({1, n});
+    for (int j = 1; j <= nLevels - 1; ++j)
+      for (int k = 0; k < (int)tree[j].size(); ++k)
+        if (!tree[j][k].leaf)
+          for (int c = 0; c < 4; ++c) child_interactions(c, j, k);
+    // assignLeafChargeLocations
+    for (const Pair& lf : leafNodes) {
+      ABox& B = tree[lf.x][lf.y];
+      const int start = (int)grid.size();
+      for (int i = 0; i < rank; ++i) B.chargeLoc.push_back(start + i);
+      for (int i = 0; i < rank; ++i)
+        grid.push_back({boxRadius[lf.x] * chebStd[i].x + B.c.x, boxRadius[lf.x] * chebStd[i].y + B.c.y});
+    }
+    precompute_M();
+    // NCA, levels fine to coarse; boxes of a level are independent.
+    const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
+    int stale_o = 0, stale_i = 0;
+    for (int j = nLevels; j >= level_LFR; --j) {
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) lfr_box(j, k, tol, true);
+      record('O', j, false, stale_o);
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) lfr_box(j, k, tol, false);
+      record('I', j, false, stale_i);
+    }
+    int stale_ho = 0, stale_hi = 0;
+    for (int j = level_LFR - 1; j >= 2; --j) {
+      const int nbx = (int)tree[j].size();
+      std::vector<std::pair<int, int>> work;
+      for (int k = 0; k < nbx; ++k) {
+        if (tree[j][k].leaf) work.push_back({k, -1});
+        else for (int c = 0; c < nCones[j]; ++c) work.push_back({k, c});
+      }
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int t = 0; t < (int)work.size(); ++t) {
+        if (work[t].second < 0) lfr_box(j, work[t].first, tol, true);
+        else hfr_cone(j, work[t].first, work[t].second, tol, true);
+      }
+      record('O', j, true, stale_ho);
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int t = 0; t < (int)work.size(); ++t) {
+        if (work[t].second < 0) lfr_box(j, work[t].first, tol, false);
+        else hfr_cone(j, work[t].first, work[t].second, tol, false);
+      }
+      record('I', j, true, stale_hi);
+    }
+  }
+};
+
+}  // namespace adaptive
+}  // namespace ora
+
+extern "C" {
+
+// treeAdaptivity >= 0: the adaptive tree with epsilonTree = 10^-treeAdaptivity
+// (createAdaptiveTree); treeAdaptivity < 0: the uniform tree of
+// cfg->nLevelsUniform levels (createUniformTree).
+//
+// Builds the adaptive tree and its NCA skeletons and reports what the
+// reference prints while assembling. head[0..3] = nLevels, level_LFR, N,
+// number of level records; each record (7 ints) = direction (0 'O',
+// 1 'I'), level j, boxes at the level, box of the largest rank (-1 for LFR
+// levels), rows, cols, largest rank. Returns the number of ints written to
+// rec (capacity cap), or -1 on a bad configuration.
+int ora_adaptive_report(const ora_cfg* cfg, int treeAdaptivity, int* head, int* rec, int cap) {
+  using namespace ora::adaptive;
+  if (!cfg || cfg->nChebNodes < 2) return -1;
+  AOracle o;
+  o.cfg = *cfg;
+  o.treeAdaptivity = treeAdaptivity;
+  o.run();
+  head[0] = o.nLevels;
+  head[1] = o.level_LFR;
+  head[2] = (int)o.grid.size();
+  head[3] = (int)o.stats.size();
+  int n = 0;
+  for (const LevelStat& s : o.stats) {
+    const int v[7] = {s.dir == 'O' ? 0 : 1, s.j, s.nboxes, s.hfr ? s.kmax : -1, s.rows, s.cols, s.rank};
+    for (int t = 0; t < 7; ++t) {
+      if (n < cap) rec[n] = v[t];
+      ++n;
+    }
+  }
+  return n;
+}
+
+// Skeleton node sets after the NCA: per box of levels 2..nLevels (per cone
+// for non-leaf boxes of HFR levels, cone -1 otherwise) the ints j, k, cone,
+// then the outgoing charge, outgoing check, incoming charge and incoming
+// check point lists, each as a length followed by the global point indices.
+// Returns the number of ints (written up to cap).
+long ora_adaptive_skeletons(const ora_cfg* cfg, int treeAdaptivity, int* buf, long cap) {
+  using namespace ora::adaptive;
+  if (!cfg || cfg->nChebNodes < 2) return -1;
+  AOracle o;
+  o.cfg = *cfg;
+  o.treeAdaptivity = treeAdaptivity;
+  o.run();
+  long n = 0;
+  auto put = [&](int v) { if (n < cap && buf) buf[n] = v; ++n; };
+  auto putv = [&](const std::vector<int>& v) { put((int)v.size()); for (int x : v) put(x); };
+  for (int j = 2; j <= o.nLevels; ++j)
+    for (int k = 0; k < (int)o.tree[j].size(); ++k) {
+      const ABox& B = o.tree[j][k];
+      if (j >= o.level_LFR || B.leaf) {
+        put(j); put(k); put(-1);
+        putv(B.oc); putv(B.ochk); putv(B.ic); putv(B.ichk);
+      } else {
+        for (int c = 0; c < (int)B.cones.size(); ++c) {
+          const Cone& C = B.cones[c];
+          put(j); put(k); put(c);
+          putv(C.oc); putv(C.ochk); putv(C.ic); putv(C.ichk);
+        }
+      }
+    }
+  return n;
+}
+
+}  // extern "C"

@@ -3,8 +3,10 @@
 ctypes front end of the CPU restatement of the reference DAFMM + GMRES path
 (oracle/ls_oracle.cpp). Only tests/, __graft_entry__.smoke() and the CPU
 baseline leg of bench.py import this module, and only as the checker or as
-the timed CPU baseline. Parity unpinned: the reference needs Eigen and
-Boost.Math, which are absent, so it cannot be compiled and run here.
+the timed CPU baseline. The reference needs Eigen and Boost.Math, which are
+absent, so it cannot be compiled and run here; the oracle is pinned to the
+assembly log the reference's README publishes through the adaptive-tree
+restatement (oracle/ls_oracle_adaptive.cpp, tests/test_oracle_pinned.py).
 """
 import ctypes
 import os
@@ -73,6 +75,10 @@ def lib():
         L.ora_gauss_legendre.argtypes = [ctypes.c_int, dp, dp]
         L.ora_bessel_jy.argtypes = [ctypes.c_int, ctypes.c_double, dp, dp]
         L.ora_colpiv_solve.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp]
+        L.ora_adaptive_report.restype = ctypes.c_int
+        L.ora_adaptive_report.argtypes = [ctypes.POINTER(OraCfg), ctypes.c_int, ip, ip, ctypes.c_int]
+        L.ora_adaptive_skeletons.restype = ctypes.c_long
+        L.ora_adaptive_skeletons.argtypes = [ctypes.POINTER(OraCfg), ctypes.c_int, ip, ctypes.c_long]
         _lib = L
     return _lib
 
@@ -204,3 +210,52 @@ def colpiv_solve(A, b):
     Af = np.ascontiguousarray(A.T).reshape(-1)  # column-major flat
     lib().ora_colpiv_solve(m, n, _dp(Af), _dp(b), _dp(x))
     return x
+
+
+def adaptive_report(cfg, tree_adaptivity):
+    """Adaptive-tree assembly statistics (ls_oracle_adaptive.cpp).
+
+    Returns {"nLevels", "level_LFR", "N", "levels": [...]}; each level entry
+    is one line the reference prints while choosing NCA skeletons
+    (GMRES/G_FMM2DTree.hpp:2238, 2384, 3418, 3570): direction "O"/"I",
+    level j, Nboxes, k (HFR levels only, else None), rows, cols, Crank."""
+    c = make_cfg(cfg)
+    head = (ctypes.c_int * 4)()
+    cap = 7 * 64
+    rec = (ctypes.c_int * cap)()
+    n = lib().ora_adaptive_report(ctypes.byref(c), int(tree_adaptivity), head, rec, cap)
+    if n < 0:
+        raise ValueError("ora_adaptive_report: invalid configuration")
+    levels = []
+    for r in range(min(n, cap) // 7):
+        d, j, nb, k, rows, cols, rk = rec[7 * r:7 * r + 7]
+        levels.append({"dir": "OI"[d], "j": j, "Nboxes": nb, "k": None if k < 0 else k,
+                       "rows": rows, "cols": cols, "Crank": rk})
+    return {"nLevels": head[0], "level_LFR": head[1], "N": head[2], "levels": levels}
+
+
+def _parse_skeletons(buf, n_lists, skip):
+    out, p = {}, 0
+    while p < len(buf):
+        key = (int(buf[p]), int(buf[p + 1]), int(buf[p + 2]))
+        p += 3 + skip
+        lists = []
+        for _ in range(n_lists):
+            m = int(buf[p])
+            lists.append(buf[p + 1:p + 1 + m].tolist())
+            p += 1 + m
+        out[key] = lists
+    return out
+
+
+def adaptive_skeletons(cfg, tree_adaptivity):
+    """{(j, k, cone): [out_charge, out_check, in_charge, in_check]} of the
+    adaptive restatement; tree_adaptivity < 0 builds the uniform tree."""
+    c = make_cfg(cfg)
+    n = lib().ora_adaptive_skeletons(ctypes.byref(c), int(tree_adaptivity), None, 0)
+    if n < 0:
+        raise ValueError("ora_adaptive_skeletons: invalid configuration")
+    buf = np.empty(n, dtype=np.int32)
+    lib().ora_adaptive_skeletons(ctypes.byref(c), int(tree_adaptivity),
+                                 buf.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+    return _parse_skeletons(buf, 4, 0)
