@@ -35,13 +35,15 @@ LS_E_STATE = -5
 LS_E_TIMEOUT = -6
 LS_PREC_F64 = 0
 LS_PREC_F32 = 1
+LS_F64_NATIVE = 0
+LS_F64_DOUBLE_FLOAT = 1
 
 # Every symbol declared in include/ls_dafmm.h.
 EXPORTED_SYMBOLS = (
     "ls_op_create", "ls_op_destroy", "ls_op_info", "ls_op_points", "ls_op_contrast", "ls_op_rhs",
     "ls_matvec", "ls_matvec_f32", "ls_op_enable_f32", "ls_matvec_host", "ls_gmres", "ls_gmres_restarted",
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
-    "ls_version", "ls_matvec_noalloc",
+    "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels",
 )
 
 
@@ -167,6 +169,7 @@ def lib():
         for n in ("ls_matvec", "ls_matvec_f32", "ls_matvec_noalloc"):
             getattr(L, n).argtypes = [vp, vp, vp, vp]
         L.ls_op_enable_f32.argtypes = [vp]
+        L.ls_op_set_f64_kernels.argtypes = [vp, ctypes.c_int]
         L.ls_matvec_host.argtypes = [vp, dp, dp]
         L.ls_gmres.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp, dp, ip, dp]
         L.ls_gmres_restarted.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, dp]
@@ -269,6 +272,10 @@ class Operator:
 
     def enable_f32(self):
         _check(lib().ls_op_enable_f32(self._h), "ls_op_enable_f32")
+
+    def set_f64_kernels(self, kernels):
+        """LS_F64_NATIVE or LS_F64_DOUBLE_FLOAT behind every FP64 entry point."""
+        _check(lib().ls_op_set_f64_kernels(self._h, int(kernels)), "ls_op_set_f64_kernels")
 
     def gmres(self, b, max_iter=400, tol=1e-10, raise_on_fail=False):
         b = np.ascontiguousarray(b, dtype=np.complex128)

@@ -118,7 +118,7 @@ ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
   o->device_bytes = d.device_bytes;
   o->assemble_seconds = h.assemble_seconds;
   o->max_rank = h.max_rank;
-  o->n_kernels_per_matvec = d.launches_per_matvec;
+  o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 1 : 0);
   // M2L: every block once (16 B per complex entry), every source charge of
   // the charge buffer once, every potential it writes once.
   o->m2l_entries = op->on_device ? d.m2l.entries : h.m2l.entries();
@@ -165,6 +165,19 @@ ls_status ls_op_enable_f32(ls_op* op) {
   if (!op->on_device) return fail(LS_E_STATE, "ls_op_enable_f32: operator was assembled without a device");
   std::string err;
   if (!dev_enable_f32(op->dev, err)) return fail(LS_E_CUDA, "ls_op_enable_f32: " + err);
+  return LS_OK;
+}
+
+ls_status ls_op_set_f64_kernels(ls_op* op, int kernels) {
+  if (!op) return fail(LS_E_INVALID, "ls_op_set_f64_kernels: null argument");
+  if (kernels != LS_F64_NATIVE && kernels != LS_F64_DOUBLE_FLOAT)
+    return fail(LS_E_INVALID, "ls_op_set_f64_kernels: unknown kernel choice " + std::to_string(kernels));
+  if (!op->on_device) return fail(LS_E_STATE, "ls_op_set_f64_kernels: operator was assembled without a device");
+  if (kernels == LS_F64_DOUBLE_FLOAT) {
+    std::string err;
+    if (!dev_enable_df(op->dev, err)) return fail(LS_E_CUDA, "ls_op_set_f64_kernels: " + err);
+  }
+  op->dev.f64_kernels = kernels;
   return LS_OK;
 }
 

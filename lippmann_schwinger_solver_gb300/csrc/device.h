@@ -40,9 +40,9 @@ struct DevOperator {
   int* colleague = nullptr;  // n_leaves x 9
   // Factored near field: B_q = Vt_q Q^+ + E_q (E_q: 6-digit rounding residual)
   int n_bases = 0;
-  double2* nearVt = nullptr; // 9 x rank x n_bases
+  double2* nearVt = nullptr; // [q][l][row]: 9 x n_bases x rank (transposed)
   double* Qp = nullptr;      // n_bases x rank
-  float2* nearE = nullptr;   // 9 x rank x rank (FP32)
+  float2* nearE = nullptr;   // [q][k][row]: 9 x rank x rank (FP32, transposed)
   double2* cbuf = nullptr;   // n_leaves x n_bases: Q^+ x per leaf
   float2* x32 = nullptr;     // N: x in FP32 for the E_q term
   // FP32 operator (mixed precision), built on request
@@ -53,6 +53,18 @@ struct DevOperator {
   float2* P32 = nullptr;
   float2* nearB32 = nullptr;
   float* kq32 = nullptr;
+  // Double-float form of the FP64 operator (matvec_df.cu), built on request.
+  // f64_kernels selects what the FP64 entry points run: LS_F64_NATIVE or
+  // LS_F64_DOUBLE_FLOAT.
+  int f64_kernels = LS_F64_NATIVE;
+  bool has_df = false;
+  std::vector<DevPhase<float4>> up_df, down_df;
+  DevPhase<float4> m2l_df;
+  float4* S_df = nullptr;    // (re_hi, im_hi, re_lo, im_lo)
+  float4* P_df = nullptr;
+  float4* Vt_df = nullptr;
+  float2* Qp_df = nullptr;   // (hi, lo)
+  float4* c_df = nullptr;
   // scratch device vectors (N complex) for host-buffer calls
   double2* xbuf = nullptr;
   double2* ybuf = nullptr;
@@ -75,6 +87,11 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
 cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
 // Same product with its scratch in a static device array (no allocation).
 cudaError_t dev_matvec_static(DevOperator& d, const double2* x, double2* y, cudaStream_t s);
+
+// matvec_df.cu
+bool dev_enable_df(DevOperator& d, std::string& err);
+void dev_free_df(DevOperator& d);
+cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
 
 // gmres.cu
 struct GmresResult {

@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(256) near_coeff_kernel(int n_leaves, int rank,
 }
 
 // Pass 2: y = P + kappa^2 q .* sum_q (Vt_q c_nb(q) + E_q x_nb(q)) + x.
-__global__ void __launch_bounds__(256) near_factored_kernel(int n_out, int rank, int nb,
+__global__ void __launch_bounds__(256, 4) near_factored_kernel(int n_out, int rank, int nb,
                                                             const double2* __restrict__ Vt,
                                                             const float2* __restrict__ E,
                                                             const double* __restrict__ kq,
@@ -187,21 +187,21 @@ __global__ void __launch_bounds__(256) near_factored_kernel(int n_out, int rank,
   for (int n = 0; n < 9; ++n) {
     const int nbx = coll[leaf * 9 + n];
     if (nbx < 0) continue;
-    const double2* __restrict__ v = Vt + ((size_t)n * rank + row) * nb;
+    const double2* __restrict__ v = Vt + (size_t)n * nb * rank + row;
     const double2* __restrict__ cc = c + (size_t)nbx * nb;
     for (int l = 0; l < nb; ++l) {
-      const double2 a = v[l];
+      const double2 a = v[(size_t)l * rank];
       const double2 b = cc[l];
       ar = fma(a.x, b.x, ar);
       ar = fma(-a.y, b.y, ar);
       ai = fma(a.x, b.y, ai);
       ai = fma(a.y, b.x, ai);
     }
-    const float2* __restrict__ e = E + ((size_t)n * rank + row) * rank;
+    const float2* __restrict__ e = E + (size_t)n * rank * rank + row;
     const float2* __restrict__ xs = x32 + (size_t)nbx * rank;
     float er = 0.0f, ei = 0.0f;
     for (int k = 0; k < rank; ++k) {
-      const float2 a = e[k];
+      const float2 a = e[(size_t)k * rank];
       const float2 b = xs[k];
       er = fmaf(a.x, b.x, er);
       er = fmaf(-a.y, b.y, er);
@@ -367,14 +367,25 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
   cudaMemcpy(d.colleague, h.colleague.data(), h.colleague.size() * sizeof(int), cudaMemcpyHostToDevice);
   {
     d.n_bases = h.n_bases;
+    // Device layouts are transposed so that the threads of one leaf (one per
+    // row) read consecutive words: Vt as [q][l][row], E as [q][k][row].
+    const int R = h.rank, NB = h.n_bases;
     std::vector<float2> e32(h.nearE.size());
-    for (size_t i = 0; i < e32.size(); ++i) e32[i] = make_float2((float)h.nearE[i].real(), (float)h.nearE[i].imag());
+    std::vector<cd> vt(h.nearVt.size());
+    for (int q = 0; q < 9; ++q)
+      for (int i = 0; i < R; ++i) {
+        for (int k = 0; k < R; ++k) {
+          const cd v = h.nearE[((size_t)q * R + i) * R + k];
+          e32[((size_t)q * R + k) * R + i] = make_float2((float)v.real(), (float)v.imag());
+        }
+        for (int l = 0; l < NB; ++l) vt[((size_t)q * NB + l) * R + i] = h.nearVt[((size_t)q * R + i) * NB + l];
+      }
     if (!dmalloc(&d.nearVt, h.nearVt.size(), tot, err)) return false;
     if (!dmalloc(&d.Qp, h.Qpinv.size(), tot, err)) return false;
     if (!dmalloc(&d.nearE, e32.size(), tot, err)) return false;
     if (!dmalloc(&d.cbuf, (size_t)h.n_leaves * h.n_bases, tot, err)) return false;
     if (!dmalloc(&d.x32, (size_t)h.N, tot, err)) return false;
-    cudaMemcpy(d.nearVt, h.nearVt.data(), h.nearVt.size() * sizeof(double2), cudaMemcpyHostToDevice);
+    cudaMemcpy(d.nearVt, vt.data(), vt.size() * sizeof(double2), cudaMemcpyHostToDevice);
     cudaMemcpy(d.Qp, h.Qpinv.data(), h.Qpinv.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(d.nearE, e32.data(), e32.size() * sizeof(float2), cudaMemcpyHostToDevice);
   }
@@ -413,6 +424,7 @@ void dev_free(DevOperator& d) {
   cudaFree(d.nearVt); cudaFree(d.Qp); cudaFree(d.nearE); cudaFree(d.cbuf); cudaFree(d.x32);
   cudaFree(d.S32); cudaFree(d.P32); cudaFree(d.nearB32); cudaFree(d.kq32);
   cudaFree(d.xbuf); cudaFree(d.ybuf);
+  dev_free_df(d);
   for (auto& ev : d.ev) if (ev) cudaEventDestroy(ev);
   if (d.stream) cudaStreamDestroy(d.stream);
   d = DevOperator();
@@ -457,6 +469,7 @@ bool dev_enable_f32(DevOperator& d, std::string& err) {
 }
 
 cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
+  if (d.f64_kernels == LS_F64_DOUBLE_FLOAT) return dev_matvec_df(d, x, y, s, mark_m2l);
   if (!s) s = d.stream;
   cudaMemcpyAsync(d.S, x, (size_t)d.N * sizeof(double2), cudaMemcpyDeviceToDevice, s);
   cudaMemsetAsync(d.P, 0, (size_t)d.pots_len * sizeof(double2), s);
