@@ -935,68 +935,89 @@ static void add_task(GemvPhase& ph, const std::vector<cd>& rowmajor, int rows, i
   ph.nnz += (long long)rows * K;
 }
 
-// Column slices per row: long rows are split so that a warp covers fewer
-// rows and the grid has enough warps to hide memory latency. `min_s` is
-// the phase-wide minimum that gives the launch at least ~7,300 warps (one
-// full wave of 48 warps on each of 152 SMs); slices are never shorter than
-// 4 columns.
-static int slices_for(int K, int min_s) {
-  int s = K >= 128 ? 4 : (K >= 48 ? 2 : 1);
-  while (s < min_s && K >= 8 * s) s *= 2;
-  return s;
+// Packs the staged blocks into warp tiles (see GemvTile). A tile holds R
+// rows of ONE block, R a power of two, so its rows share their gather list
+// and the tile stores one index per column slice and step (S = 32 / R per
+// step) instead of one per element. A block of r rows is cut into tiles of
+// R = 16, 8, ... rows (largest first) so that no rows are padded, except
+// that R never drops below r_min: slices must keep at least 4 columns
+// (R >= 128 / K), and the last tile of a block pads up to r_min. r_max
+// (at most 8) keeps at least ~14,600 tiles per phase (two waves of 48
+// warps on each of 152 SMs): fewer, longer warps leave too few loads in
+// flight to cover HBM latency. Blocks go longest first (stable, so
+// neighbouring blocks keep their order).
+static int pow2_ceil(int v) {
+  int p = 1;
+  while (p < v) p <<= 1;
+  return p;
 }
 
-// Packs the staged rows into tiles (see GemvTile), longest rows first
-// (stable, so that the rows of one block stay together and share their
-// gathers).
 static void finalize(GemvPhase& ph) {
-  std::stable_sort(ph.rows.begin(), ph.rows.end(), [](const GemvPhase::Row& a, const GemvPhase::Row& b) {
-    return a.K > b.K;
-  });
-  // First pass: tile boundaries and sizes.
-  struct T { size_t r0; int rows, S, qmax; };
+  struct Block { size_t r0; int rows, K; };
+  std::vector<Block> blocks;
+  for (size_t r = 0; r < ph.rows.size();) {
+    size_t e = r + 1;
+    while (e < ph.rows.size() && ph.rows[e].idx == ph.rows[r].idx) ++e;
+    blocks.push_back({r, (int)(e - r), ph.rows[r].K});
+    r = e;
+  }
+  std::stable_sort(blocks.begin(), blocks.end(), [](const Block& a, const Block& b) { return a.K > b.K; });
+  const long long want_tiles = 152LL * 96;
+  int r_max = 8;
+  while (r_max > 1 && (long long)ph.rows.size() < want_tiles * r_max) r_max >>= 1;
+  struct T { size_t r0; int rows, S, qmax, K; };
   std::vector<T> tl;
-  long long total = 0;
-  const long long want_warps = 152LL * 48;
-  int min_s = 1;
-  while (min_s < 8 && (long long)ph.rows.size() * min_s < want_warps * kTileLanes) min_s *= 2;
-  for (size_t r0 = 0; r0 < ph.rows.size();) {
-    const int K = ph.rows[r0].K;
-    const int S = slices_for(K, min_s);
-    const int R = kTileLanes / S;
-    const int rows = (int)std::min<size_t>(R, ph.rows.size() - r0);
-    const int qmax = (K + S - 1) / S;
-    tl.push_back({r0, rows, S, qmax});
-    total += (long long)qmax * kTileLanes;
-    r0 += rows;
+  long long total = 0, total_idx = 0;
+  for (const Block& b : blocks) {
+    const int r_min = std::min(kTileLanes, pow2_ceil((128 + b.K - 1) / b.K));
+    const int rcap = std::max(r_max, r_min);
+    for (int done = 0; done < b.rows;) {
+      const int rem = b.rows - done;
+      int R = 1;
+      while (R * 2 <= std::min(rem, rcap)) R *= 2;
+      R = std::max(R, r_min);
+      const int rows = std::min(R, rem);
+      const int S = kTileLanes / R;
+      const int qmax = (b.K + S - 1) / S;
+      tl.push_back({b.r0 + (size_t)done, rows, S, qmax, b.K});
+      total += (long long)qmax * kTileLanes;
+      total_idx += (long long)qmax * S;
+      done += rows;
+    }
   }
   ph.A.assign((size_t)total, cd(0.0, 0.0));
-  ph.idx.assign((size_t)total, 0);
+  ph.idx.assign((size_t)total_idx, 0);
   ph.out.assign(ph.rows.size(), 0);
   ph.klen.assign(tl.size() * kTileLanes, 0);
   ph.tiles.clear();
-  long long off = 0;
+  long long off = 0, ioff = 0;
+  int row_base = 0;
   for (size_t t = 0; t < tl.size(); ++t) {
     const T& d = tl[t];
     const int R = kTileLanes / d.S;
     int log2s = 0;
     while ((1 << log2s) < d.S) ++log2s;
+    const GemvPhase::Row& first = ph.rows[d.r0];
+    for (int q = 0; q < d.qmax; ++q)
+      for (int sl = 0; sl < d.S; ++sl) {
+        const int k = q * d.S + sl;
+        if (k < d.K) ph.idx[(size_t)(ioff + (long long)q * d.S + sl)] = ph.stageIdx[(size_t)first.idx + k];
+      }
     for (int r = 0; r < d.rows; ++r) {
       const GemvPhase::Row& row = ph.rows[d.r0 + r];
-      ph.out[d.r0 + r] = row.out;
+      ph.out[(size_t)row_base + r] = row.out;
       for (int sl = 0; sl < d.S; ++sl) {
         const int lane = sl * R + r;
         int q = 0;
-        for (int k = sl; k < row.K; k += d.S, ++q) {
-          const size_t pos = (size_t)(off + (long long)q * kTileLanes + lane);
-          ph.A[pos] = ph.stageA[(size_t)(row.a + k)];
-          ph.idx[pos] = ph.stageIdx[(size_t)row.idx + k];
-        }
+        for (int k = sl; k < row.K; k += d.S, ++q)
+          ph.A[(size_t)(off + (long long)q * kTileLanes + lane)] = ph.stageA[(size_t)(row.a + k)];
         ph.klen[t * kTileLanes + lane] = q;
       }
     }
-    ph.tiles.push_back({off, d.qmax, d.rows, log2s, (int)(t * kTileLanes), (int)d.r0, 0});
+    ph.tiles.push_back({off, ioff, d.qmax, d.rows, log2s, (int)(t * kTileLanes), row_base});
     off += (long long)d.qmax * kTileLanes;
+    ioff += (long long)d.qmax * d.S;
+    row_base += d.rows;
   }
   std::vector<cd>().swap(ph.stageA);
   std::vector<int>().swap(ph.stageIdx);

@@ -24,6 +24,8 @@ struct DevPhase {
   long long stored = 0;      // stored elements (with padding)
 };
 
+struct GmresWorkspace;  // gmres.cu: Krylov basis and scratch, kept between solves
+
 struct DevOperator {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -51,8 +53,9 @@ struct DevOperator {
   DevPhase<float2> m2l32;
   float2* S32 = nullptr;
   float2* P32 = nullptr;
-  float2* nearB32 = nullptr;
+  float2* nearB32 = nullptr;  // [q][k][row]: 9 x rank x rank (transposed)
   float* kq32 = nullptr;
+  float2* Z32 = nullptr;      // near field, pass 1: [leaf][q][row]
   // Double-float form of the FP64 operator (matvec_df.cu), built on request.
   // f64_kernels selects what the FP64 entry points run: LS_F64_NATIVE or
   // LS_F64_DOUBLE_FLOAT.
@@ -65,9 +68,12 @@ struct DevOperator {
   float4* Vt_df = nullptr;
   float2* Qp_df = nullptr;   // (hi, lo)
   float4* c_df = nullptr;
+  float4* Z_df = nullptr;    // near field, pass 1: [leaf][q][row] contribution of a leaf
+  float2* ZE_df = nullptr;   // same for the E_q term (FP32)
   // scratch device vectors (N complex) for host-buffer calls
   double2* xbuf = nullptr;
   double2* ybuf = nullptr;
+  GmresWorkspace* gws = nullptr;
   // events for phase timing
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   long long device_bytes = 0;
@@ -94,6 +100,7 @@ void dev_free_df(DevOperator& d);
 cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
 
 // gmres.cu
+void dev_free_gmres(DevOperator& d);
 struct GmresResult {
   int iters = 0;
   double rel_residual = 0.0;

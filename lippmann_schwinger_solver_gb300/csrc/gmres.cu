@@ -24,10 +24,67 @@
 
 namespace lsg {
 
-namespace {
-
 constexpr int kDotThreads = 256;
 constexpr int kDotBlocks = 240;  // partial sums per column
+
+struct GmresWorkspace {
+  double2* V = nullptr;
+  double2* w = nullptr;
+  double2* r = nullptr;
+  double2* dx = nullptr;   // correction of the mixed-precision refinement
+  double2* res = nullptr;  // residual of the mixed-precision refinement
+  double2* partial = nullptr;
+  double2* h = nullptr;   // first CGS pass, then scratch
+  double2* h2 = nullptr;  // second CGS pass
+  double2* nrm = nullptr; // |w|^2
+  int n = 0, cap = -1;
+  void release() {
+    cudaFree(V); cudaFree(w); cudaFree(r); cudaFree(dx); cudaFree(res); cudaFree(partial); cudaFree(h); cudaFree(h2);
+    cudaFree(nrm);
+    V = w = r = dx = res = partial = h = h2 = nrm = nullptr;
+    n = 0;
+    cap = -1;
+  }
+  // Buffers for n-vectors and up to m Arnoldi steps; kept between solves
+  // and grown only when a solve needs more.
+  cudaError_t ensure(int n_, int m) {
+    if (n_ == n && m <= cap) return cudaSuccess;
+    release();
+    const size_t nb = (size_t)n_ * sizeof(double2);
+    cudaError_t e = cudaMalloc(&V, nb * (m + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&w, nb);
+    if (e == cudaSuccess) e = cudaMalloc(&r, nb);
+    if (e == cudaSuccess) e = cudaMalloc(&dx, nb);
+    if (e == cudaSuccess) e = cudaMalloc(&res, nb);
+    if (e == cudaSuccess) e = cudaMalloc(&partial, (size_t)kDotBlocks * (m + 2) * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&h, (size_t)(m + 2) * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&h2, (size_t)(m + 2) * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&nrm, sizeof(double2));
+    if (e != cudaSuccess) {
+      release();
+      return e;
+    }
+    n = n_;
+    cap = m;
+    return cudaSuccess;
+  }
+};
+
+GmresWorkspace& workspace(DevOperator& d) {
+  if (!d.gws) d.gws = new GmresWorkspace();
+  return *d.gws;
+}
+
+void dev_free_gmres(DevOperator& d) {
+  if (d.gws) {
+    d.gws->release();
+    delete d.gws;
+    d.gws = nullptr;
+  }
+}
+
+namespace {
+
 
 // partial[col * gridDim.x + block] = sum_{rows in block} conj(V[row, col]) * w[row]
 __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const double2* __restrict__ V, long long ldv,
@@ -113,27 +170,15 @@ __global__ void add_inplace_kernel(double2* __restrict__ a, const double2* __res
 
 using cdh = std::complex<double>;
 
-struct Workspace {
-  double2* V = nullptr;
-  double2* w = nullptr;
-  double2* r = nullptr;
-  double2* partial = nullptr;
-  double2* h = nullptr;
-  int cap = 0;
-  ~Workspace() {
-    cudaFree(V); cudaFree(w); cudaFree(r); cudaFree(partial); cudaFree(h);
-  }
-  cudaError_t alloc(int n, int m) {
-    cap = m;
-    cudaError_t e;
-    if ((e = cudaMalloc(&V, (size_t)n * (m + 1) * sizeof(double2))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&w, (size_t)n * sizeof(double2))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&r, (size_t)n * sizeof(double2))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&partial, (size_t)kDotBlocks * (m + 2) * sizeof(double2))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&h, (size_t)(m + 2) * sizeof(double2))) != cudaSuccess) return e;
-    return cudaSuccess;
-  }
-};
+// b = a / sqrt(nrm->x), or zeros when the norm is zero (breakdown; the
+// vector is then never used).
+__global__ void scale_by_norm_kernel(const double2* __restrict__ a, double2* __restrict__ b,
+                                     const double2* __restrict__ nrm, int n) {
+  const double nn = nrm->x;
+  const double s = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = make_double2(a[i].x * s, a[i].y * s);
+}
 
 int grid_for(int n) { return std::min((n + 255) / 256, 152 * 8); }
 
@@ -162,7 +207,7 @@ cudaError_t apply(DevOperator& d, const double2* x, double2* y, cudaStream_t s, 
 // One Arnoldi cycle from x0 (device, may be null for x0 = 0). Writes the
 // updated solution into x. tol < 0 disables the residual stop; breakdown
 // exits when H(k+1,k) < brk.
-cudaError_t arnoldi_cycle(DevOperator& d, Workspace& ws, const double2* b, const double2* x0, double2* x, int m,
+cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const double2* b, const double2* x0, double2* x, int m,
                           double tol, double brk, double bnorm, std::vector<double>* hist, int& iters,
                           bool& converged, bool f32) {
   cudaStream_t s = d.stream;
@@ -191,27 +236,28 @@ cudaError_t arnoldi_cycle(DevOperator& d, Workspace& ws, const double2* b, const
   scale_kernel<<<grid_for(n), 256, 0, s>>>(ws.r, ws.V, 1.0 / beta, n);
   std::vector<std::vector<cdh>> H;  // columns, already rotated
   std::vector<cdh> cs, sn, g(1, cdh(beta, 0.0));
-  std::vector<double2> hbuf(m + 2);
+  std::vector<double2> hbuf(m + 2), hbuf2(m + 2);
   int K = 0;
   for (int k = 0; k < m; ++k) {
     double2* vk = ws.V + (size_t)k * n;
     if ((e = apply(d, vk, ws.w, s, f32)) != cudaSuccess) return e;
-    // CGS2
+    // CGS2, both passes and the norm on the device; one copy back per step.
     multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h, 0, s);
     multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h, n, -1.0);
+    multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h2, 0, s);
+    multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h2, n, -1.0);
+    multidot(ws.w, n, 1, ws.w, n, ws.partial, ws.nrm, 0, s);
+    scale_by_norm_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V + (size_t)(k + 1) * n, ws.nrm, n);
     cudaMemcpyAsync(hbuf.data(), ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hbuf2.data(), ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
+    double2 nv;
+    cudaMemcpyAsync(&nv, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     std::vector<cdh> hk(k + 2);
-    for (int i = 0; i <= k; ++i) hk[i] = cdh(hbuf[i].x, hbuf[i].y);
-    multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h, 0, s);
-    multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h, n, -1.0);
-    cudaMemcpyAsync(hbuf.data(), ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    double wn = 0.0;
-    if ((e = vnorm(ws.w, n, ws.partial, ws.h, s, wn)) != cudaSuccess) return e;
-    for (int i = 0; i <= k; ++i) hk[i] += cdh(hbuf[i].x, hbuf[i].y);
+    for (int i = 0; i <= k; ++i) hk[i] = cdh(hbuf[i].x + hbuf2[i].x, hbuf[i].y + hbuf2[i].y);
+    const double wn = std::sqrt(nv.x);
     hk[k + 1] = wn;
     const bool breakdown = (std::abs(hk[k + 1]) < brk);
-    if (!breakdown) scale_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V + (size_t)(k + 1) * n, 1.0 / wn, n);
     // Givens rotations (unitary): G = [[conj(c), conj(s)], [-s, c]].
     for (int i = 0; i < k; ++i) {
       const cdh t = std::conj(cs[i]) * hk[i] + std::conj(sn[i]) * hk[i + 1];
@@ -260,8 +306,8 @@ cudaError_t arnoldi_cycle(DevOperator& d, Workspace& ws, const double2* b, const
 
 cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter, double tol,
                       std::vector<double>& hist, GmresResult& res, bool use_f32) {
-  Workspace ws;
-  cudaError_t e = ws.alloc(d.N, max_iter);
+  GmresWorkspace& ws = workspace(d);
+  cudaError_t e = ws.ensure(d.N, max_iter);
   if (e != cudaSuccess) return e;
   double bn = 0.0;
   if ((e = vnorm(b, d.N, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) return e;
@@ -287,8 +333,8 @@ cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter
 }
 
 cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, int m, int restarts) {
-  Workspace ws;
-  cudaError_t e = ws.alloc(d.N, m);
+  GmresWorkspace& ws = workspace(d);
+  cudaError_t e = ws.ensure(d.N, m);
   if (e != cudaSuccess) return e;
   double bn = 0.0;
   if ((e = vnorm(b, d.N, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) return e;
@@ -308,12 +354,12 @@ cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, in
 cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner, double tol,
                             std::vector<double>& hist, int& n_matvec, double& relres) {
   const int n = d.N;
-  Workspace ws;
-  cudaError_t e = ws.alloc(n, inner);
+  GmresWorkspace& ws = workspace(d);
+  cudaError_t e = ws.ensure(n, inner);
   if (e != cudaSuccess) return e;
-  double2 *r = nullptr, *dx = nullptr;
-  if ((e = cudaMalloc(&r, (size_t)n * sizeof(double2))) != cudaSuccess) return e;
-  if ((e = cudaMalloc(&dx, (size_t)n * sizeof(double2))) != cudaSuccess) { cudaFree(r); return e; }
+  // r and dx must survive the inner cycles, which use ws.r and ws.w.
+  double2* r = ws.res;
+  double2* dx = ws.dx;
   double bn = 0.0;
   if ((e = vnorm(b, n, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) goto done;
   hist.clear();
@@ -341,8 +387,6 @@ cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int ma
     hist.push_back(relres);
   }
 done:
-  cudaFree(r);
-  cudaFree(dx);
   return e;
 }
 

@@ -13,16 +13,17 @@ namespace lsg {
 
 using cd = std::complex<double>;
 
-// One warp tile of a gather-GEMV phase. Rows of all blocks of a phase are
-// sorted by length and packed R = 32 / S to a tile; each row is split into
-// S interleaved column slices (S = 4 for long rows, 1 for short ones), so
-// lane l = s * R + r sums columns k = q * S + s of row r. Element (q, l)
-// sits at a_off + 32 q + l in A and idx: every warp load is one contiguous
-// line. After the loop the S slice sums are combined with shuffles and the
-// lanes of slice 0 write:
-//   dst[out[row_base + r]] (=|+=) sum_k A(r, k) * src[idx(r, k)]
+// One warp tile of a gather-GEMV phase: R = 32 / S rows of one block, each
+// split into S interleaved column slices, so lane l = s * R + r sums the
+// columns k = q * S + s of row r. Element (q, l) sits at a_off + 32 q + l in
+// A: every warp load is one contiguous line. The rows of a tile share their
+// gather list, stored once per slice and step: column k = q * S + s of the
+// tile gathers src[idx[i_off + q * S + s]]. After the loop the S slice sums
+// are combined with shuffles and the lanes of slice 0 write:
+//   dst[out[row_base + r]] (=|+=) sum_k A(r, k) * src[idx(k)]
 struct GemvTile {
-  long long a_off;  // first element of the tile in A / idx
+  long long a_off;  // first element of the tile in A
+  long long i_off;  // first gather index of the tile in idx
   int qmax;         // steps of the longest lane
   int rows;         // rows in the tile (<= R)
   int log2s;        // S = 1 << log2s column slices per row
@@ -36,7 +37,7 @@ constexpr int kTileLanes = 32;
 // A phase (or one tree level of a phase) in device-ready form.
 struct GemvPhase {
   std::vector<cd> A;            // tiles, column interleaved (zero padded)
-  std::vector<int> idx;         // gather indices, same positions as A
+  std::vector<int> idx;         // gather indices, one per tile, step and slice
   std::vector<int> out;         // output element of each row
   std::vector<int> klen;        // steps of each lane (32 per tile)
   std::vector<GemvTile> tiles;

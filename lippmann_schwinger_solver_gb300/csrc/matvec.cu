@@ -59,11 +59,12 @@ __global__ void __launch_bounds__(256, 3) gemv_tiles_kernel(const GemvTile* __re
     const GemvTile t = tiles[w];
     const int ql = qlen[t.lane_base + lane];
     const C* __restrict__ a = A + t.a_off + lane;
-    const int* __restrict__ ix = idx + t.a_off + lane;
+    const int S = 1 << t.log2s;
+    const int* __restrict__ ix = idx + t.i_off + (lane >> (5 - t.log2s));  // slice s = lane / R
     R sr = R(0), si = R(0);
     int q = 0;
     for (; q + 4 <= ql; q += 4) {
-      const int i0 = ix[32 * q], i1 = ix[32 * (q + 1)], i2 = ix[32 * (q + 2)], i3 = ix[32 * (q + 3)];
+      const int i0 = ix[S * q], i1 = ix[S * (q + 1)], i2 = ix[S * (q + 2)], i3 = ix[S * (q + 3)];
       const C a0 = ld_stream(a + 32 * q), a1 = ld_stream(a + 32 * (q + 1));
       const C a2 = ld_stream(a + 32 * (q + 2)), a3 = ld_stream(a + 32 * (q + 3));
       const C x0 = src[i0], x1 = src[i1], x2 = src[i2], x3 = src[i3];
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(256, 3) gemv_tiles_kernel(const GemvTile* __re
     }
     for (; q < ql; ++q) {
       const C a0 = ld_stream(a + 32 * q);
-      const C x0 = src[ix[32 * q]];
+      const C x0 = src[ix[S * q]];
       sr = fma(a0.x, x0.x, sr); sr = fma(-a0.y, x0.y, sr); si = fma(a0.x, x0.y, si); si = fma(a0.y, x0.x, si);
     }
     // Combine the slices: lanes r, r + R, r + 2R, ... (R = 32 >> log2s).
@@ -221,50 +222,86 @@ __global__ void __launch_bounds__(256, 4) near_factored_kernel(int n_out, int ra
   }
 }
 
-// Near field of the FP32 operator. The 9 colleague blocks (9 x rank x rank
-// float2, 93 KB at rank 36) are staged once per thread block in shared
-// memory, transposed so that the threads of one leaf (one per row) read
-// consecutive words; the block then walks groups of leaves. y stays FP64 on
-// the boundary.
-__global__ void __launch_bounds__(256) near32_smem_kernel(int n_leaves, int rank, const float2* __restrict__ B,
-                                                          const float* __restrict__ kq, const int* __restrict__ coll,
-                                                          const float2* __restrict__ x, const float2* __restrict__ P,
-                                                          double2* __restrict__ y, int find_phi) {
-  extern __shared__ float2 sB[];  // [n][c][row]
-  const int rr = rank * rank;
-  for (int i = threadIdx.x; i < 9 * rr; i += blockDim.x) {
-    const int n = i / rr, rem = i - n * rr, row = rem / rank, c = rem - row * rank;
-    sB[(n * rank + c) * rank + row] = B[i];
+// Near field of the FP32 operator in two passes (as the double-float path,
+// matvec_df.cu). Pass 1: Z32[s][q][row] = B_q(row, :) x_s for every leaf s
+// and direction q; a block takes kNearSources32 leaves (their x staged in
+// shared memory), thread (q, row) keeps one accumulator per leaf, and the
+// blocks are read transposed ([q][k][row]) so the threads of a direction
+// read consecutive words. Pass 2 gathers the nine contributions of every
+// output row and adds P and the identity; y stays FP64 on the boundary.
+constexpr int kNearSources32 = 8;
+
+__global__ void __launch_bounds__(576, 1) near_gemm32_kernel(int n_leaves, int rank, const float2* __restrict__ BT,
+                                                          const float2* __restrict__ x, float2* __restrict__ Z) {
+  constexpr int NS = kNearSources32;
+  extern __shared__ float2 sx32[];  // [j][k]
+  const int s0 = blockIdx.x * NS;
+  for (int i = threadIdx.x; i < NS * rank; i += blockDim.x) {
+    const int j = i / rank;
+    sx32[i] = s0 + j < n_leaves ? x[(size_t)s0 * rank + i] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const int per = blockDim.x / rank;  // leaves handled together
-  const int local = threadIdx.x / rank, row = threadIdx.x - local * rank;
-  if (local >= per) return;
-  for (int leaf = blockIdx.x * per + local; leaf < n_leaves; leaf += gridDim.x * per) {
-    float ar = 0.0f, ai = 0.0f;
-    for (int n = 0; n < 9; ++n) {
-      const int nb = coll[leaf * 9 + n];
-      if (nb < 0) continue;
-      const float2* __restrict__ xn = x + (size_t)nb * rank;
-      const float2* __restrict__ bn = sB + (size_t)n * rr + row;
-      for (int c = 0; c < rank; ++c) {
-        const float2 a = bn[c * rank];
-        const float2 v = xn[c];
-        ar = fmaf(a.x, v.x, ar);
-        ar = fmaf(-a.y, v.y, ar);
-        ai = fmaf(a.x, v.y, ai);
-        ai = fmaf(a.y, v.x, ai);
-      }
+  const int qr = threadIdx.x;
+  if (qr >= 9 * rank) return;
+  const int q = qr / rank, row = qr - q * rank;
+  float ar[NS], ai[NS];
+#pragma unroll
+  for (int j = 0; j < NS; ++j) ar[j] = ai[j] = 0.f;
+  const float2* __restrict__ b = BT + (size_t)q * rank * rank + row;
+  for (int k = 0; k < rank; ++k) {
+    const float2 a = b[(size_t)k * rank];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      const float2 v = sx32[j * rank + k];
+      ar[j] = fmaf(a.x, v.x, ar[j]);
+      ar[j] = fmaf(-a.y, v.y, ar[j]);
+      ai[j] = fmaf(a.x, v.y, ai[j]);
+      ai[j] = fmaf(a.y, v.x, ai[j]);
     }
-    const int t = leaf * rank + row;
-    const float2 p = P[t];
-    if (find_phi) {
-      const float s = kq[t];
-      const float2 xs = x[t];
-      y[t] = make_double2((double)(p.x + s * ar + xs.x), (double)(p.y + s * ai + xs.y));
-    } else {
-      y[t] = make_double2((double)(p.x + ar), (double)(p.y + ai));
-    }
+  }
+  const size_t per = (size_t)9 * rank;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    if (s0 + j >= n_leaves) break;
+    Z[(size_t)(s0 + j) * per + qr] = make_float2(ar[j], ai[j]);
+  }
+}
+
+__global__ void __launch_bounds__(256) near_gather32_kernel(int n_out, int rank, const float2* __restrict__ Z,
+                                                            const float* __restrict__ kq,
+                                                            const int* __restrict__ coll,
+                                                            const float2* __restrict__ x,
+                                                            const float2* __restrict__ P, double2* __restrict__ y,
+                                                            int find_phi) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_out) return;
+  const int leaf = t / rank, row = t - leaf * rank;
+  float ar = 0.f, ai = 0.f;
+  const size_t per = (size_t)9 * rank;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const int nbx = coll[leaf * 9 + q];
+    if (nbx < 0) continue;
+    const float2 z = Z[(size_t)nbx * per + (size_t)q * rank + row];
+    ar += z.x;
+    ai += z.y;
+  }
+  const float2 p = P[t];
+  if (find_phi) {
+    const float s = kq[t];
+    const float2 xs = x[t];
+    y[t] = make_double2((double)(p.x + s * ar + xs.x), (double)(p.y + s * ai + xs.y));
+  } else {
+    y[t] = make_double2((double)(p.x + ar), (double)(p.y + ai));
+  }
+}
+
+// [q][row][k] (FP64) -> [q][k][row] (FP32)
+__global__ void near_transpose32_kernel(const double2* __restrict__ B, float2* __restrict__ BT, int rank) {
+  const int n = 9 * rank * rank;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int q = i / (rank * rank), rem = i - q * rank * rank, row = rem / rank, k = rem - row * rank;
+    BT[((size_t)q * rank + k) * rank + row] = make_float2((float)B[i].x, (float)B[i].y);
   }
 }
 
@@ -422,9 +459,10 @@ void dev_free(DevOperator& d) {
   cudaFree(d.m2l32.A);
   cudaFree(d.S); cudaFree(d.P); cudaFree(d.nearB); cudaFree(d.kq); cudaFree(d.colleague);
   cudaFree(d.nearVt); cudaFree(d.Qp); cudaFree(d.nearE); cudaFree(d.cbuf); cudaFree(d.x32);
-  cudaFree(d.S32); cudaFree(d.P32); cudaFree(d.nearB32); cudaFree(d.kq32);
+  cudaFree(d.S32); cudaFree(d.P32); cudaFree(d.nearB32); cudaFree(d.kq32); cudaFree(d.Z32);
   cudaFree(d.xbuf); cudaFree(d.ybuf);
   dev_free_df(d);
+  dev_free_gmres(d);
   for (auto& ev : d.ev) if (ev) cudaEventDestroy(ev);
   if (d.stream) cudaStreamDestroy(d.stream);
   d = DevOperator();
@@ -458,9 +496,8 @@ bool dev_enable_f32(DevOperator& d, std::string& err) {
   const long long nb = 9LL * d.rank * d.rank;
   if (!dmalloc(&d.nearB32, (size_t)nb, tot, err)) return false;
   if (!dmalloc(&d.kq32, (size_t)d.N, tot, err)) return false;
-  d2f_kernel<<<256, 256>>>(d.nearB, d.nearB32, nb);
-  if (nb * sizeof(float2) <= 200 * 1024)
-    cudaFuncSetAttribute(near32_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(nb * sizeof(float2)));
+  if (!dmalloc(&d.Z32, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
+  near_transpose32_kernel<<<64, 256>>>(d.nearB, d.nearB32, d.rank);
   d2f_real_kernel<<<256, 256>>>(d.kq, d.kq32, d.N);
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { err = std::string("enable_f32: ") + cudaGetErrorString(e); return false; }
@@ -478,11 +515,10 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
   launch_gemv<1>(d.m2l, (const double2*)d.S, d.P, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down) launch_gemv<2>(ph, (const double2*)d.P, d.P, s, d.device);
-  const int n = d.N;
   near_coeff_kernel<<<(d.n_leaves * d.n_bases + 255) / 256, 256, 0, s>>>(d.n_leaves, d.rank, d.n_bases, d.Qp, d.S,
                                                                          d.cbuf, d.x32);
-  near_factored_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.n_bases, d.nearVt, d.nearE, d.kq, d.colleague,
-                                                       d.cbuf, d.x32, d.S, d.P, y, d.find_phi);
+  near_factored_kernel<<<(d.N + 255) / 256, 256, 0, s>>>(d.N, d.rank, d.n_bases, d.nearVt, d.nearE, d.kq,
+                                                         d.colleague, d.cbuf, d.x32, d.S, d.P, y, d.find_phi);
   return cudaGetLastError();
 }
 
@@ -496,17 +532,12 @@ cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStr
   launch_gemv<1>(d.m2l32, (const float2*)d.S32, d.P32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[3], s);
   for (auto& ph : d.down32) launch_gemv<2>(ph, (const float2*)d.P32, d.P32, s, d.device);
-  const size_t smem = (size_t)9 * d.rank * d.rank * sizeof(float2);
-  if (smem <= 200 * 1024) {
-    const int per = 256 / d.rank;
-    const int blocks = std::min((d.n_leaves + per - 1) / per, sm_count(d.device) * 2);
-    near32_smem_kernel<<<blocks, per * d.rank, smem, s>>>(d.n_leaves, d.rank, d.nearB32, d.kq32, d.colleague, d.S32,
-                                                           d.P32, y, d.find_phi);
-  } else {  // blocks too large for shared memory (nChebNodes 8)
-    const int n = d.N;
-    near_kernel<float2><<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.nearB32, d.kq32, d.colleague, d.S32, d.P32, y,
-                                                        d.find_phi);
-  }
+  const int nthr = (9 * d.rank + 31) / 32 * 32;
+  near_gemm32_kernel<<<(d.n_leaves + kNearSources32 - 1) / kNearSources32, nthr,
+                       (size_t)kNearSources32 * d.rank * sizeof(float2), s>>>(d.n_leaves, d.rank, d.nearB32, d.S32,
+                                                                              d.Z32);
+  near_gather32_kernel<<<(d.N + 255) / 256, 256, 0, s>>>(d.N, d.rank, d.Z32, d.kq32, d.colleague, d.S32, d.P32, y,
+                                                         d.find_phi);
   return cudaGetLastError();
 }
 

@@ -114,11 +114,12 @@ __global__ void __launch_bounds__(256, 3) gemv_df_kernel(const GemvTile* __restr
     const GemvTile t = tiles[w];
     const int ql = qlen[t.lane_base + lane];
     const float4* __restrict__ a = A + t.a_off + lane;
-    const int* __restrict__ ix = idx + t.a_off + lane;
+    const int S = 1 << t.log2s;
+    const int* __restrict__ ix = idx + t.i_off + (lane >> (5 - t.log2s));  // slice s = lane / R
     float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
     int q = 0;
     for (; q + 4 <= ql; q += 4) {
-      const int i0 = ix[32 * q], i1 = ix[32 * (q + 1)], i2 = ix[32 * (q + 2)], i3 = ix[32 * (q + 3)];
+      const int i0 = ix[S * q], i1 = ix[S * (q + 1)], i2 = ix[S * (q + 2)], i3 = ix[S * (q + 3)];
       const float4 a0 = __ldcs(a + 32 * q), a1 = __ldcs(a + 32 * (q + 1));
       const float4 a2 = __ldcs(a + 32 * (q + 2)), a3 = __ldcs(a + 32 * (q + 3));
       const float4 x0 = src[i0], x1 = src[i1], x2 = src[i2], x3 = src[i3];
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(256, 3) gemv_df_kernel(const GemvTile* __restr
       cmac(rh, rl, ih, il, a2, x2);
       cmac(rh, rl, ih, il, a3, x3);
     }
-    for (; q < ql; ++q) cmac(rh, rl, ih, il, __ldcs(a + 32 * q), src[ix[32 * q]]);
+    for (; q < ql; ++q) cmac(rh, rl, ih, il, __ldcs(a + 32 * q), src[ix[S * q]]);
     for (int o = 16; o >= (32 >> t.log2s); o >>= 1) {
       const float rh2 = __shfl_xor_sync(0xffffffffu, rh, o), rl2 = __shfl_xor_sync(0xffffffffu, rl, o);
       const float ih2 = __shfl_xor_sync(0xffffffffu, ih, o), il2 = __shfl_xor_sync(0xffffffffu, il, o);
@@ -171,41 +172,101 @@ __global__ void __launch_bounds__(256) near_coeff_df_kernel(int n_leaves, int ra
   c[t] = pack(rh, rl, ih, il);
 }
 
-// y = P + kappa^2 q .* sum_q (Vt_q c_nb(q) + E_q x_nb(q)) + x; the E_q term
-// in FP32 as in the FP64 path, the final sum in FP64 with x read from the
-// caller's FP64 input.
-__global__ void __launch_bounds__(256) near_factored_df_kernel(int n_out, int rank, int nb,
-                                                               const float4* __restrict__ Vt,
-                                                               const float2* __restrict__ E,
-                                                               const double* __restrict__ kq,
-                                                               const int* __restrict__ coll,
-                                                               const float4* __restrict__ c,
-                                                               const float2* __restrict__ x32,
-                                                               const double2* __restrict__ x,
-                                                               const float4* __restrict__ P,
-                                                               double2* __restrict__ y, int find_phi) {
+// Near field in two passes (the colleague blocks are shared by all leaves,
+// so the product is a GEMM with a gathered epilogue).
+//
+// Pass 1: for every leaf s and direction q, the contribution of s to the
+// colleague that sees it in direction q:
+//   Z[s][q][row]  = Vt_q(row, :) c_s      (double-float)
+//   ZE[s][q][row] = E_q(row, :) x32_s      (FP32, the rounding residual)
+// A block takes kNearSources leaves; thread (q, row) keeps one accumulator
+// per leaf, so every factor entry it loads serves kNearSources products and
+// each thread has that many independent dependency chains. The leaves'
+// coefficients are staged in shared memory (broadcast reads).
+constexpr int kNearSources = 8;
+
+__global__ void __launch_bounds__(576) near_gemm_df_kernel(int n_leaves, int rank, int nb,
+                                                           const float4* __restrict__ Vt,
+                                                           const float2* __restrict__ E,
+                                                           const float4* __restrict__ c,
+                                                           const float2* __restrict__ x32,
+                                                           float4* __restrict__ Z, float2* __restrict__ ZE) {
+  constexpr int NS = kNearSources;
+  extern __shared__ float4 sc[];                    // [j][l]: c of source j
+  float2* sx = reinterpret_cast<float2*>(sc + NS * nb);  // [j][k]: x32 of source j
+  const int s0 = blockIdx.x * NS;
+  for (int i = threadIdx.x; i < NS * nb; i += blockDim.x) {
+    const int j = i / nb;
+    sc[i] = s0 + j < n_leaves ? c[(size_t)s0 * nb + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (int i = threadIdx.x; i < NS * rank; i += blockDim.x) {
+    const int j = i / rank;
+    sx[i] = s0 + j < n_leaves ? x32[(size_t)s0 * rank + i] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int qr = threadIdx.x;
+  if (qr >= 9 * rank) return;
+  const int q = qr / rank, row = qr - q * rank;
+  float h[NS][4];
+  float er[NS], ei[NS];
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    h[j][0] = h[j][1] = h[j][2] = h[j][3] = 0.f;
+    er[j] = ei[j] = 0.f;
+  }
+  const float4* __restrict__ v = Vt + (size_t)q * nb * rank + row;
+  for (int l = 0; l < nb; ++l) {
+    const float4 a = v[(size_t)l * rank];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) cmac(h[j][0], h[j][1], h[j][2], h[j][3], a, sc[j * nb + l]);
+  }
+  const float2* __restrict__ e = E + (size_t)q * rank * rank + row;
+  for (int k = 0; k < rank; ++k) {
+    const float2 a = e[(size_t)k * rank];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      const float2 b = sx[j * rank + k];
+      er[j] = fmaf(a.x, b.x, er[j]);
+      er[j] = fmaf(-a.y, b.y, er[j]);
+      ei[j] = fmaf(a.x, b.y, ei[j]);
+      ei[j] = fmaf(a.y, b.x, ei[j]);
+    }
+  }
+  const size_t per = (size_t)9 * rank;
+#pragma unroll
+  for (int j = 0; j < NS; ++j) {
+    if (s0 + j >= n_leaves) break;
+    Z[(size_t)(s0 + j) * per + qr] = pack(h[j][0], h[j][1], h[j][2], h[j][3]);
+    ZE[(size_t)(s0 + j) * per + qr] = make_float2(er[j], ei[j]);
+  }
+}
+
+// Pass 2: y = P + kappa^2 q .* sum_q (Z + ZE)[nb(q)][q][row] + x, one
+// thread per output; the double-float partials are added in q order, the
+// final sum is formed in FP64 with x read from the caller's FP64 input.
+__global__ void __launch_bounds__(256) near_gather_df_kernel(int n_out, int rank, const float4* __restrict__ Z,
+                                                             const float2* __restrict__ ZE,
+                                                             const double* __restrict__ kq,
+                                                             const int* __restrict__ coll,
+                                                             const double2* __restrict__ x,
+                                                             const float4* __restrict__ P,
+                                                             double2* __restrict__ y, int find_phi) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out) return;
   const int leaf = t / rank, row = t - leaf * rank;
-  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-  float er = 0.f, ei = 0.f;
-#pragma unroll 1
-  for (int n = 0; n < 9; ++n) {
-    const int nbx = coll[leaf * 9 + n];
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f, er = 0.f, ei = 0.f;
+  const size_t per = (size_t)9 * rank;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const int nbx = coll[leaf * 9 + q];
     if (nbx < 0) continue;
-    const float4* __restrict__ v = Vt + (size_t)n * nb * rank + row;
-    const float4* __restrict__ cc = c + (size_t)nbx * nb;
-    for (int l = 0; l < nb; ++l) cmac(rh, rl, ih, il, v[(size_t)l * rank], cc[l]);
-    const float2* __restrict__ e = E + (size_t)n * rank * rank + row;
-    const float2* __restrict__ xs = x32 + (size_t)nbx * rank;
-    for (int k = 0; k < rank; ++k) {
-      const float2 a = e[(size_t)k * rank];
-      const float2 b = xs[k];
-      er = fmaf(a.x, b.x, er);
-      er = fmaf(-a.y, b.y, er);
-      ei = fmaf(a.x, b.y, ei);
-      ei = fmaf(a.y, b.x, ei);
-    }
+    const size_t o = (size_t)nbx * per + (size_t)q * rank + row;
+    const float4 z = Z[o];
+    dd_add(rh, rl, z.x, z.z);
+    dd_add(ih, il, z.y, z.w);
+    const float2 w = ZE[o];
+    er += w.x;
+    ei += w.y;
   }
   const double ar = ((double)rh + (double)rl) + (double)er;
   const double ai = ((double)ih + (double)il) + (double)ei;
@@ -283,6 +344,8 @@ bool dev_enable_df(DevOperator& d, std::string& err) {
   if (!dalloc(&d.Vt_df, (size_t)nvt, tot, err)) return false;
   if (!dalloc(&d.Qp_df, (size_t)nqp, tot, err)) return false;
   if (!dalloc(&d.c_df, (size_t)d.n_leaves * d.n_bases, tot, err)) return false;
+  if (!dalloc(&d.Z_df, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
+  if (!dalloc(&d.ZE_df, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
   split_kernel<<<64, 256>>>(d.nearVt, d.Vt_df, nvt);
   split_real_kernel<<<16, 256>>>(d.Qp, d.Qp_df, nqp);
   const cudaError_t e = cudaDeviceSynchronize();
@@ -296,10 +359,12 @@ void dev_free_df(DevOperator& d) {
   for (auto& p : d.down_df) cudaFree(p.A);
   cudaFree(d.m2l_df.A);
   cudaFree(d.S_df); cudaFree(d.P_df); cudaFree(d.Vt_df); cudaFree(d.Qp_df); cudaFree(d.c_df);
+  cudaFree(d.Z_df); cudaFree(d.ZE_df);
   d.up_df.clear();
   d.down_df.clear();
   d.m2l_df = DevPhase<float4>();
   d.S_df = nullptr; d.P_df = nullptr; d.Vt_df = nullptr; d.Qp_df = nullptr; d.c_df = nullptr;
+  d.Z_df = nullptr; d.ZE_df = nullptr;
   d.has_df = false;
 }
 
@@ -316,8 +381,14 @@ cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStre
   for (auto& ph : d.down_df) launch_df<2>(ph, (const float4*)d.P_df, d.P_df, s, d.device);
   near_coeff_df_kernel<<<(d.n_leaves * d.n_bases + 255) / 256, 256, 0, s>>>(d.n_leaves, d.rank, d.n_bases, d.Qp_df,
                                                                             d.S_df, d.c_df, d.x32);
-  near_factored_df_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.n_bases, d.Vt_df, d.nearE, d.kq, d.colleague,
-                                                          d.c_df, d.x32, x, d.P_df, y, d.find_phi);
+  {
+    const int nthr = (9 * d.rank + 31) / 32 * 32;
+    const size_t smem = (size_t)kNearSources * (d.n_bases * sizeof(float4) + d.rank * sizeof(float2));
+    near_gemm_df_kernel<<<(d.n_leaves + kNearSources - 1) / kNearSources, nthr, smem, s>>>(
+        d.n_leaves, d.rank, d.n_bases, d.Vt_df, d.nearE, d.c_df, d.x32, d.Z_df, d.ZE_df);
+    near_gather_df_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.Z_df, d.ZE_df, d.kq, d.colleague, x, d.P_df,
+                                                          y, d.find_phi);
+  }
   return cudaGetLastError();
 }
 
