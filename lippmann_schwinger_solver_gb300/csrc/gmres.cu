@@ -24,8 +24,8 @@
 
 namespace lsg {
 
-constexpr int kDotThreads = 256;
-constexpr int kDotBlocks = 240;  // partial sums per column
+constexpr int kDotThreads = 128;
+constexpr int kDotBlocks = 304;  // row chunks: partial sums per column (2 per SM)
 
 struct GmresWorkspace {
   double2* V = nullptr;
@@ -37,11 +37,17 @@ struct GmresWorkspace {
   double2* h = nullptr;   // first CGS pass, then scratch
   double2* h2 = nullptr;  // second CGS pass
   double2* nrm = nullptr; // |w|^2
+  cudaEvent_t copied = nullptr;  // step coefficients are on the host
+  double2* pinned = nullptr;     // host: h (m+2), h2 (m+2), |w|^2 (1); page-locked so copies stay asynchronous
   int n = 0, cap = -1;
   void release() {
     cudaFree(V); cudaFree(w); cudaFree(r); cudaFree(dx); cudaFree(res); cudaFree(partial); cudaFree(h); cudaFree(h2);
     cudaFree(nrm);
     V = w = r = dx = res = partial = h = h2 = nrm = nullptr;
+    if (copied) cudaEventDestroy(copied);
+    copied = nullptr;
+    if (pinned) cudaFreeHost(pinned);
+    pinned = nullptr;
     n = 0;
     cap = -1;
   }
@@ -60,6 +66,8 @@ struct GmresWorkspace {
     if (e == cudaSuccess) e = cudaMalloc(&h, (size_t)(m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&h2, (size_t)(m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&nrm, sizeof(double2));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost(&pinned, (size_t)(2 * (m + 2) + 1) * sizeof(double2));
     if (e != cudaSuccess) {
       release();
       return e;
@@ -86,57 +94,123 @@ void dev_free_gmres(DevOperator& d) {
 namespace {
 
 
-// partial[col * gridDim.x + block] = sum_{rows in block} conj(V[row, col]) * w[row]
-__global__ void __launch_bounds__(kDotThreads) multidot_kernel(const double2* __restrict__ V, long long ldv,
+// partial[col * gridDim.x + block] = sum_{rows of block} conj(V[row, col]) * w[row].
+// Block (x, y) owns a contiguous chunk of rows and the columns
+// 8y .. 8y+7: each thread keeps eight sums, so it has eight independent
+// loads of V in flight per row. GB300's FP64 pipe is narrow, so the warp
+// reduction of the eight sums is a transposing butterfly: at each of the
+// first three shuffle steps a lane keeps half of its columns and adds the
+// partner's half, which leaves each group of four lanes one column (18
+// FP64 adds per lane instead of 80). All orders are fixed: deterministic.
+constexpr int kDotCols = 8;
+
+__device__ __forceinline__ double2 shfl2(double2 v, int o) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+}
+
+__global__ void __launch_bounds__(kDotThreads) multidot_kernel(const double2* __restrict__ V, long long ldv, int ncols,
                                                                const double2* __restrict__ w, int n,
                                                                double2* __restrict__ partial) {
-  const int col = blockIdx.y;
-  const double2* __restrict__ v = V + (size_t)col * ldv;
-  double sr = 0.0, si = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double2 a = v[i], b = w[i];
-    sr = fma(a.x, b.x, sr);
-    sr = fma(a.y, b.y, sr);
-    si = fma(a.x, b.y, si);
-    si = fma(-a.y, b.x, si);
-  }
-  __shared__ double shr[kDotThreads / 32], shi[kDotThreads / 32];
-  for (int o = 16; o > 0; o >>= 1) {
-    sr += __shfl_xor_sync(0xffffffffu, sr, o);
-    si += __shfl_xor_sync(0xffffffffu, si, o);
+  __shared__ double2 red[kDotThreads / 32][kDotCols];
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int r0 = blockIdx.x * chunk;
+  const int len = max(0, min(chunk, n - r0));
+  const int c0 = blockIdx.y * kDotCols;
+  const int nc = min(kDotCols, ncols - c0);
+  double2 acc[kDotCols];
+#pragma unroll
+  for (int j = 0; j < kDotCols; ++j) acc[j] = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    const double2 b = w[r0 + i];
+    double2 a[kDotCols];
+#pragma unroll
+    for (int j = 0; j < kDotCols; ++j)  // all loads first, so that they are in flight together
+      a[j] = j < nc ? V[(size_t)(c0 + j) * ldv + r0 + i] : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int j = 0; j < kDotCols; ++j) {
+      acc[j].x = fma(a[j].x, b.x, acc[j].x);
+      acc[j].x = fma(a[j].y, b.y, acc[j].x);
+      acc[j].y = fma(a[j].x, b.y, acc[j].y);
+      acc[j].y = fma(-a[j].y, b.x, acc[j].y);
+    }
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) { shr[wid] = sr; shi[wid] = si; }
+  // Butterfly: after the steps 16, 8, 4 lane l holds column
+  // 4 * bit4(l) + 2 * bit3(l) + bit2(l); steps 2 and 1 finish its sum.
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const bool hi = lane & 16;
+    const double2 keep = hi ? acc[j + 4] : acc[j];
+    const double2 got = shfl2(hi ? acc[j] : acc[j + 4], 16);
+    acc[j] = make_double2(keep.x + got.x, keep.y + got.y);
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const bool hi = lane & 8;
+    const double2 keep = hi ? acc[j + 2] : acc[j];
+    const double2 got = shfl2(hi ? acc[j] : acc[j + 2], 8);
+    acc[j] = make_double2(keep.x + got.x, keep.y + got.y);
+  }
+  {
+    const bool hi = lane & 4;
+    const double2 keep = hi ? acc[1] : acc[0];
+    const double2 got = shfl2(hi ? acc[0] : acc[1], 4);
+    acc[0] = make_double2(keep.x + got.x, keep.y + got.y);
+  }
+  for (int o = 2; o > 0; o >>= 1) {
+    const double2 got = shfl2(acc[0], o);
+    acc[0] = make_double2(acc[0].x + got.x, acc[0].y + got.y);
+  }
+  if ((lane & 3) == 0) red[wid][((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1)] = acc[0];
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < nc) {
     double a = 0.0, b = 0.0;
-    for (int k = 0; k < kDotThreads / 32; ++k) { a += shr[k]; b += shi[k]; }
-    partial[(size_t)col * gridDim.x + blockIdx.x] = make_double2(a, b);
+    for (int k = 0; k < kDotThreads / 32; ++k) { a += red[k][threadIdx.x].x; b += red[k][threadIdx.x].y; }
+    partial[(size_t)(c0 + threadIdx.x) * gridDim.x + blockIdx.x] = make_double2(a, b);
   }
 }
 
-// out[col] (+)= sum_b partial[col * nb + b], fixed order.
+// out[col] (+)= sum_b partial[col * nb + b]: one warp per column, lanes
+// stride over the partials, then a fixed shuffle tree (deterministic).
 __global__ void reduce_partials_kernel(const double2* __restrict__ partial, int nb, int ncols,
                                        double2* __restrict__ out, int accumulate) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (col >= ncols) return;
   double a = 0.0, b = 0.0;
-  for (int k = 0; k < nb; ++k) {
+  for (int k = lane; k < nb; k += 32) {
     const double2 p = partial[(size_t)col * nb + k];
     a += p.x;
     b += p.y;
   }
-  if (accumulate) { out[col].x += a; out[col].y += b; }
-  else out[col] = make_double2(a, b);
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    if (accumulate) { out[col].x += a; out[col].y += b; }
+    else out[col] = make_double2(a, b);
+  }
 }
 
-// w[i] += sign * sum_c V[i, c] * h[c]
+// w[i] += sign * sum_c V[i, c] * h[c]; the column loop is unrolled by 4 so
+// that four independent loads of V are in flight per thread.
 __global__ void __launch_bounds__(256) multi_axpy_kernel(double2* __restrict__ w, const double2* __restrict__ V,
                                                          long long ldv, int ncols, const double2* __restrict__ h,
                                                          int n, double sign) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double sr = 0.0, si = 0.0;
-    for (int c = 0; c < ncols; ++c) {
+    int c = 0;
+    for (; c + 4 <= ncols; c += 4) {
+      const double2 v0 = V[(size_t)c * ldv + i], v1 = V[(size_t)(c + 1) * ldv + i];
+      const double2 v2 = V[(size_t)(c + 2) * ldv + i], v3 = V[(size_t)(c + 3) * ldv + i];
+      const double2 h0 = h[c], h1 = h[c + 1], h2 = h[c + 2], h3 = h[c + 3];
+      sr = fma(v0.x, h0.x, sr); sr = fma(-v0.y, h0.y, sr); si = fma(v0.x, h0.y, si); si = fma(v0.y, h0.x, si);
+      sr = fma(v1.x, h1.x, sr); sr = fma(-v1.y, h1.y, sr); si = fma(v1.x, h1.y, si); si = fma(v1.y, h1.x, si);
+      sr = fma(v2.x, h2.x, sr); sr = fma(-v2.y, h2.y, sr); si = fma(v2.x, h2.y, si); si = fma(v2.y, h2.x, si);
+      sr = fma(v3.x, h3.x, sr); sr = fma(-v3.y, h3.y, sr); si = fma(v3.x, h3.y, si); si = fma(v3.y, h3.x, si);
+    }
+    for (; c < ncols; ++c) {
       const double2 v = V[(size_t)c * ldv + i];
       const double2 hc = h[c];
       sr = fma(v.x, hc.x, sr);
@@ -185,9 +259,9 @@ int grid_for(int n) { return std::min((n + 255) / 256, 152 * 8); }
 // h_dev[0:ncols) = V[:, 0:ncols)^H w
 void multidot(const double2* V, long long ldv, int ncols, const double2* w, int n, double2* partial, double2* h_dev,
               int accumulate, cudaStream_t s) {
-  dim3 g(kDotBlocks, ncols);
-  multidot_kernel<<<g, kDotThreads, 0, s>>>(V, ldv, w, n, partial);
-  reduce_partials_kernel<<<(ncols + 127) / 128, 128, 0, s>>>(partial, kDotBlocks, ncols, h_dev, accumulate);
+  multidot_kernel<<<dim3(kDotBlocks, (ncols + kDotCols - 1) / kDotCols), kDotThreads, 0, s>>>(V, ldv, ncols, w, n,
+                                                                                              partial);
+  reduce_partials_kernel<<<(ncols * 32 + 255) / 256, 256, 0, s>>>(partial, kDotBlocks, ncols, h_dev, accumulate);
 }
 
 cudaError_t vnorm(const double2* w, int n, double2* partial, double2* h_dev, cudaStream_t s, double& out) {
@@ -236,11 +310,14 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const double2* b, 
   scale_kernel<<<grid_for(n), 256, 0, s>>>(ws.r, ws.V, 1.0 / beta, n);
   std::vector<std::vector<cdh>> H;  // columns, already rotated
   std::vector<cdh> cs, sn, g(1, cdh(beta, 0.0));
-  std::vector<double2> hbuf(m + 2), hbuf2(m + 2);
+  std::vector<double2> hbuf(m + 2);
   int K = 0;
+  // The product A v_{k+1} only needs v_{k+1} = w / |w|, which the device
+  // forms itself, so it is queued before the host waits for step k's
+  // coefficients: the host's Givens work and the wait hide behind it. A
+  // converged or broken-down cycle leaves one unused product behind.
+  if ((e = apply(d, ws.V, ws.w, s, f32)) != cudaSuccess) return e;
   for (int k = 0; k < m; ++k) {
-    double2* vk = ws.V + (size_t)k * n;
-    if ((e = apply(d, vk, ws.w, s, f32)) != cudaSuccess) return e;
     // CGS2, both passes and the norm on the device; one copy back per step.
     multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h, 0, s);
     multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h, n, -1.0);
@@ -248,14 +325,18 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const double2* b, 
     multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h2, n, -1.0);
     multidot(ws.w, n, 1, ws.w, n, ws.partial, ws.nrm, 0, s);
     scale_by_norm_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V + (size_t)(k + 1) * n, ws.nrm, n);
-    cudaMemcpyAsync(hbuf.data(), ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(hbuf2.data(), ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    double2 nv;
-    cudaMemcpyAsync(&nv, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    double2* hp = ws.pinned;
+    double2* hp2 = ws.pinned + (m + 2);
+    double2* np = ws.pinned + 2 * (m + 2);
+    cudaMemcpyAsync(hp, ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hp2, ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(np, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
+    if ((e = cudaEventRecord(ws.copied, s)) != cudaSuccess) return e;
+    if (k + 1 < m && (e = apply(d, ws.V + (size_t)(k + 1) * n, ws.w, s, f32)) != cudaSuccess) return e;
+    if ((e = cudaEventSynchronize(ws.copied)) != cudaSuccess) return e;
     std::vector<cdh> hk(k + 2);
-    for (int i = 0; i <= k; ++i) hk[i] = cdh(hbuf[i].x + hbuf2[i].x, hbuf[i].y + hbuf2[i].y);
-    const double wn = std::sqrt(nv.x);
+    for (int i = 0; i <= k; ++i) hk[i] = cdh(hp[i].x + hp2[i].x, hp[i].y + hp2[i].y);
+    const double wn = std::sqrt(np->x);
     hk[k + 1] = wn;
     const bool breakdown = (std::abs(hk[k + 1]) < brk);
     // Givens rotations (unitary): G = [[conj(c), conj(s)], [-s, c]].
