@@ -230,7 +230,7 @@ ls_status ls_gmres(ls_op* op, const double* b, int max_iter, double tol, double*
   if (e != cudaSuccess) return cuda_fail(e, "ls_gmres H2D");
   std::vector<double> hist;
   GmresResult res;
-  if ((e = dev_gmres(d, d.xbuf, d.ybuf, max_iter, tol, hist, res, false)) != cudaSuccess)
+  if ((e = dev_gmres(d, d.xbuf, d.ybuf, max_iter, tol, hist, res)) != cudaSuccess)
     return cuda_fail(e, "ls_gmres");
   if ((e = cudaMemcpyAsync(x, d.ybuf, bytes, cudaMemcpyDeviceToHost, d.stream)) != cudaSuccess)
     return cuda_fail(e, "ls_gmres D2H");

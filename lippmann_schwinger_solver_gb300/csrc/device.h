@@ -91,6 +91,8 @@ bool dev_enable_f32(DevOperator& d, std::string& err);
 // y = A x; x, y device pointers (N complex). mark_m2l: record events around M2L.
 cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
 cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
+// The FP32 operator with FP32 vectors on both sides (inner solves of ls_gmres_mixed).
+cudaError_t dev_matvec_f32v(DevOperator& d, const float2* x, float2* y, cudaStream_t s);
 // Same product with its scratch in a static device array (no allocation).
 cudaError_t dev_matvec_static(DevOperator& d, const double2* x, double2* y, cudaStream_t s);
 
@@ -107,7 +109,7 @@ struct GmresResult {
   bool converged = false;
 };
 cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter, double tol,
-                      std::vector<double>& hist, GmresResult& res, bool use_f32);
+                      std::vector<double>& hist, GmresResult& res);
 cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, int m, int restarts);
 cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner,
                             double tol, std::vector<double>& hist, int& n_matvec, double& relres);

@@ -6,6 +6,11 @@
 // two-stage reduction) and one update kernel (w -= V h). The tiny
 // Hessenberg / Givens algebra runs on the host in FP64.
 //
+// The Arnoldi cycle is written once for the element type of its basis:
+// double2 for the FP64 solvers, float2 for the inner solves of the
+// mixed-precision refinement, whose corrections only need the accuracy of
+// the FP32 operator they are solved with.
+//
 // Reference behaviour restated:
 //  * classGMRES::gmres (GMRES_Hybrid/include/gmres.hpp:54-119): x0 = 0,
 //    Givens-updated residual estimate |beta_{k+1}| / |b|, stop when it
@@ -26,24 +31,67 @@ namespace lsg {
 
 constexpr int kDotThreads = 128;
 constexpr int kDotBlocks = 304;  // row chunks: partial sums per column (2 per SM)
+constexpr int kDotCols = 8;      // columns per multi-dot block
 
-struct GmresWorkspace {
-  double2* V = nullptr;
-  double2* w = nullptr;
-  double2* r = nullptr;
-  double2* dx = nullptr;   // correction of the mixed-precision refinement
-  double2* res = nullptr;  // residual of the mixed-precision refinement
-  double2* partial = nullptr;
-  double2* h = nullptr;   // first CGS pass, then scratch
-  double2* h2 = nullptr;  // second CGS pass
-  double2* nrm = nullptr; // |w|^2
-  cudaEvent_t copied = nullptr;  // step coefficients are on the host
-  double2* pinned = nullptr;     // host: h (m+2), h2 (m+2), |w|^2 (1); page-locked so copies stay asynchronous
+template <class T> struct Cx;
+template <> struct Cx<double2> {
+  using R = double;
+  static __host__ __device__ double2 make(double a, double b) { return make_double2(a, b); }
+};
+template <> struct Cx<float2> {
+  using R = float;
+  static __host__ __device__ float2 make(float a, float b) { return make_float2(a, b); }
+};
+
+// Krylov basis V (n x (m+1)) and two n-vectors of one element type.
+template <class T>
+struct Basis {
+  T* V = nullptr;
+  T* w = nullptr;
+  T* r = nullptr;
   int n = 0, cap = -1;
   void release() {
-    cudaFree(V); cudaFree(w); cudaFree(r); cudaFree(dx); cudaFree(res); cudaFree(partial); cudaFree(h); cudaFree(h2);
-    cudaFree(nrm);
-    V = w = r = dx = res = partial = h = h2 = nrm = nullptr;
+    cudaFree(V); cudaFree(w); cudaFree(r);
+    V = w = r = nullptr;
+    n = 0;
+    cap = -1;
+  }
+  cudaError_t ensure(int n_, int m) {
+    if (n_ == n && m <= cap) return cudaSuccess;
+    release();
+    const size_t nb = (size_t)n_ * sizeof(T);
+    cudaError_t e = cudaMalloc(&V, nb * (m + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&w, nb);
+    if (e == cudaSuccess) e = cudaMalloc(&r, nb);
+    if (e != cudaSuccess) {
+      release();
+      return e;
+    }
+    n = n_;
+    cap = m;
+    return cudaSuccess;
+  }
+};
+
+struct GmresWorkspace {
+  Basis<double2> b64;
+  Basis<float2> b32;
+  // Mixed-precision refinement: FP64 residual, FP32 right-hand side and correction.
+  double2* res = nullptr;
+  float2* res32 = nullptr;
+  float2* dx32 = nullptr;
+  // Coefficients: per-block partial sums, CGS passes, |w|^2 (all FP64).
+  double2* partial = nullptr;
+  double2* h = nullptr;
+  double2* h2 = nullptr;
+  double2* nrm = nullptr;
+  cudaEvent_t copied = nullptr;  // a step's coefficients are on the host
+  double2* pinned = nullptr;     // host: h (m+2), h2 (m+2), |w|^2; page-locked so copies stay asynchronous
+  int n = 0, cap = -1;
+  void release_small() {
+    cudaFree(res); cudaFree(res32); cudaFree(dx32); cudaFree(partial); cudaFree(h); cudaFree(h2); cudaFree(nrm);
+    res = partial = h = h2 = nrm = nullptr;
+    res32 = dx32 = nullptr;
     if (copied) cudaEventDestroy(copied);
     copied = nullptr;
     if (pinned) cudaFreeHost(pinned);
@@ -51,17 +99,19 @@ struct GmresWorkspace {
     n = 0;
     cap = -1;
   }
-  // Buffers for n-vectors and up to m Arnoldi steps; kept between solves
-  // and grown only when a solve needs more.
+  void release() {
+    b64.release();
+    b32.release();
+    release_small();
+  }
+  // Coefficient buffers for up to m Arnoldi steps on n-vectors; kept
+  // between solves and grown only when a solve needs more.
   cudaError_t ensure(int n_, int m) {
     if (n_ == n && m <= cap) return cudaSuccess;
-    release();
-    const size_t nb = (size_t)n_ * sizeof(double2);
-    cudaError_t e = cudaMalloc(&V, nb * (m + 1));
-    if (e == cudaSuccess) e = cudaMalloc(&w, nb);
-    if (e == cudaSuccess) e = cudaMalloc(&r, nb);
-    if (e == cudaSuccess) e = cudaMalloc(&dx, nb);
-    if (e == cudaSuccess) e = cudaMalloc(&res, nb);
+    release_small();
+    cudaError_t e = cudaMalloc(&res, (size_t)n_ * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&res32, (size_t)n_ * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&dx32, (size_t)n_ * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&partial, (size_t)kDotBlocks * (m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&h, (size_t)(m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&h2, (size_t)(m + 2) * sizeof(double2));
@@ -69,7 +119,7 @@ struct GmresWorkspace {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost(&pinned, (size_t)(2 * (m + 2) + 1) * sizeof(double2));
     if (e != cudaSuccess) {
-      release();
+      release_small();
       return e;
     }
     n = n_;
@@ -93,6 +143,12 @@ void dev_free_gmres(DevOperator& d) {
 
 namespace {
 
+// (x, y) <- (kx + partner's x, ky + partner's y) for the lane l ^ o.
+template <class R>
+__device__ __forceinline__ void shfl_add(R& x, R& y, R kx, R ky, int o) {
+  x = kx + __shfl_xor_sync(0xffffffffu, x, o);
+  y = ky + __shfl_xor_sync(0xffffffffu, y, o);
+}
 
 // partial[col * gridDim.x + block] = sum_{rows of block} conj(V[row, col]) * w[row].
 // Block (x, y) owns a contiguous chunk of rows and the columns
@@ -101,37 +157,33 @@ namespace {
 // reduction of the eight sums is a transposing butterfly: at each of the
 // first three shuffle steps a lane keeps half of its columns and adds the
 // partner's half, which leaves each group of four lanes one column (18
-// FP64 adds per lane instead of 80). All orders are fixed: deterministic.
-constexpr int kDotCols = 8;
-
-__device__ __forceinline__ double2 shfl2(double2 v, int o) {
-  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
-}
-
-__global__ void __launch_bounds__(kDotThreads) multidot_kernel(const double2* __restrict__ V, long long ldv, int ncols,
-                                                               const double2* __restrict__ w, int n,
+// adds per lane instead of 80). All orders are fixed: deterministic.
+template <class T>
+__global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restrict__ V, long long ldv, int ncols,
+                                                               const T* __restrict__ w, int n,
                                                                double2* __restrict__ partial) {
-  __shared__ double2 red[kDotThreads / 32][kDotCols];
+  using R = typename Cx<T>::R;
+  __shared__ T red[kDotThreads / 32][kDotCols];
   const int chunk = (n + gridDim.x - 1) / gridDim.x;
   const int r0 = blockIdx.x * chunk;
   const int len = max(0, min(chunk, n - r0));
   const int c0 = blockIdx.y * kDotCols;
   const int nc = min(kDotCols, ncols - c0);
-  double2 acc[kDotCols];
+  R ar[kDotCols], ai[kDotCols];
 #pragma unroll
-  for (int j = 0; j < kDotCols; ++j) acc[j] = make_double2(0.0, 0.0);
+  for (int j = 0; j < kDotCols; ++j) ar[j] = ai[j] = R(0);
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
-    const double2 b = w[r0 + i];
-    double2 a[kDotCols];
+    const T b = w[r0 + i];
+    T a[kDotCols];
 #pragma unroll
     for (int j = 0; j < kDotCols; ++j)  // all loads first, so that they are in flight together
-      a[j] = j < nc ? V[(size_t)(c0 + j) * ldv + r0 + i] : make_double2(0.0, 0.0);
+      a[j] = j < nc ? V[(size_t)(c0 + j) * ldv + r0 + i] : Cx<T>::make(R(0), R(0));
 #pragma unroll
     for (int j = 0; j < kDotCols; ++j) {
-      acc[j].x = fma(a[j].x, b.x, acc[j].x);
-      acc[j].x = fma(a[j].y, b.y, acc[j].x);
-      acc[j].y = fma(a[j].x, b.y, acc[j].y);
-      acc[j].y = fma(-a[j].y, b.x, acc[j].y);
+      ar[j] = fma(a[j].x, b.x, ar[j]);
+      ar[j] = fma(a[j].y, b.y, ar[j]);
+      ai[j] = fma(a[j].x, b.y, ai[j]);
+      ai[j] = fma(-a[j].y, b.x, ai[j]);
     }
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -140,40 +192,49 @@ __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const double2* __
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const bool hi = lane & 16;
-    const double2 keep = hi ? acc[j + 4] : acc[j];
-    const double2 got = shfl2(hi ? acc[j] : acc[j + 4], 16);
-    acc[j] = make_double2(keep.x + got.x, keep.y + got.y);
+    R sx = hi ? ar[j] : ar[j + 4], sy = hi ? ai[j] : ai[j + 4];
+    shfl_add(sx, sy, hi ? ar[j + 4] : ar[j], hi ? ai[j + 4] : ai[j], 16);
+    ar[j] = sx;
+    ai[j] = sy;
   }
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
     const bool hi = lane & 8;
-    const double2 keep = hi ? acc[j + 2] : acc[j];
-    const double2 got = shfl2(hi ? acc[j] : acc[j + 2], 8);
-    acc[j] = make_double2(keep.x + got.x, keep.y + got.y);
+    R sx = hi ? ar[j] : ar[j + 2], sy = hi ? ai[j] : ai[j + 2];
+    shfl_add(sx, sy, hi ? ar[j + 2] : ar[j], hi ? ai[j + 2] : ai[j], 8);
+    ar[j] = sx;
+    ai[j] = sy;
   }
   {
     const bool hi = lane & 4;
-    const double2 keep = hi ? acc[1] : acc[0];
-    const double2 got = shfl2(hi ? acc[0] : acc[1], 4);
-    acc[0] = make_double2(keep.x + got.x, keep.y + got.y);
+    R sx = hi ? ar[0] : ar[1], sy = hi ? ai[0] : ai[1];
+    shfl_add(sx, sy, hi ? ar[1] : ar[0], hi ? ai[1] : ai[0], 4);
+    ar[0] = sx;
+    ai[0] = sy;
   }
   for (int o = 2; o > 0; o >>= 1) {
-    const double2 got = shfl2(acc[0], o);
-    acc[0] = make_double2(acc[0].x + got.x, acc[0].y + got.y);
+    R sx = ar[0], sy = ai[0];
+    shfl_add(sx, sy, ar[0], ai[0], o);
+    ar[0] = sx;
+    ai[0] = sy;
   }
-  if ((lane & 3) == 0) red[wid][((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1)] = acc[0];
+  if ((lane & 3) == 0)
+    red[wid][((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1)] = Cx<T>::make(ar[0], ai[0]);
   __syncthreads();
   if (threadIdx.x < nc) {
     double a = 0.0, b = 0.0;
-    for (int k = 0; k < kDotThreads / 32; ++k) { a += red[k][threadIdx.x].x; b += red[k][threadIdx.x].y; }
+    for (int k = 0; k < kDotThreads / 32; ++k) {
+      a += (double)red[k][threadIdx.x].x;
+      b += (double)red[k][threadIdx.x].y;
+    }
     partial[(size_t)(c0 + threadIdx.x) * gridDim.x + blockIdx.x] = make_double2(a, b);
   }
 }
 
-// out[col] (+)= sum_b partial[col * nb + b]: one warp per column, lanes
-// stride over the partials, then a fixed shuffle tree (deterministic).
+// out[col] = sum_b partial[col * nb + b]: one warp per column, lanes stride
+// over the partials, then a fixed shuffle tree (deterministic).
 __global__ void reduce_partials_kernel(const double2* __restrict__ partial, int nb, int ncols,
-                                       double2* __restrict__ out, int accumulate) {
+                                       double2* __restrict__ out) {
   const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (col >= ncols) return;
@@ -187,152 +248,177 @@ __global__ void reduce_partials_kernel(const double2* __restrict__ partial, int 
     a += __shfl_xor_sync(0xffffffffu, a, o);
     b += __shfl_xor_sync(0xffffffffu, b, o);
   }
-  if (lane == 0) {
-    if (accumulate) { out[col].x += a; out[col].y += b; }
-    else out[col] = make_double2(a, b);
-  }
+  if (lane == 0) out[col] = make_double2(a, b);
 }
 
 // w[i] += sign * sum_c V[i, c] * h[c]; the column loop is unrolled by 4 so
 // that four independent loads of V are in flight per thread.
-__global__ void __launch_bounds__(256) multi_axpy_kernel(double2* __restrict__ w, const double2* __restrict__ V,
-                                                         long long ldv, int ncols, const double2* __restrict__ h,
-                                                         int n, double sign) {
+template <class T>
+__global__ void __launch_bounds__(256) multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, long long ldv,
+                                                         int ncols, const double2* __restrict__ h, int n,
+                                                         double sign) {
+  using R = typename Cx<T>::R;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double sr = 0.0, si = 0.0;
+    R sr = R(0), si = R(0);
     int c = 0;
     for (; c + 4 <= ncols; c += 4) {
-      const double2 v0 = V[(size_t)c * ldv + i], v1 = V[(size_t)(c + 1) * ldv + i];
-      const double2 v2 = V[(size_t)(c + 2) * ldv + i], v3 = V[(size_t)(c + 3) * ldv + i];
-      const double2 h0 = h[c], h1 = h[c + 1], h2 = h[c + 2], h3 = h[c + 3];
-      sr = fma(v0.x, h0.x, sr); sr = fma(-v0.y, h0.y, sr); si = fma(v0.x, h0.y, si); si = fma(v0.y, h0.x, si);
-      sr = fma(v1.x, h1.x, sr); sr = fma(-v1.y, h1.y, sr); si = fma(v1.x, h1.y, si); si = fma(v1.y, h1.x, si);
-      sr = fma(v2.x, h2.x, sr); sr = fma(-v2.y, h2.y, sr); si = fma(v2.x, h2.y, si); si = fma(v2.y, h2.x, si);
-      sr = fma(v3.x, h3.x, sr); sr = fma(-v3.y, h3.y, sr); si = fma(v3.x, h3.y, si); si = fma(v3.y, h3.x, si);
+      T v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = V[(size_t)(c + j) * ldv + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const R hx = (R)h[c + j].x, hy = (R)h[c + j].y;
+        sr = fma(v[j].x, hx, sr);
+        sr = fma(-v[j].y, hy, sr);
+        si = fma(v[j].x, hy, si);
+        si = fma(v[j].y, hx, si);
+      }
     }
     for (; c < ncols; ++c) {
-      const double2 v = V[(size_t)c * ldv + i];
-      const double2 hc = h[c];
-      sr = fma(v.x, hc.x, sr);
-      sr = fma(-v.y, hc.y, sr);
-      si = fma(v.x, hc.y, si);
-      si = fma(v.y, hc.x, si);
+      const T v = V[(size_t)c * ldv + i];
+      const R hx = (R)h[c].x, hy = (R)h[c].y;
+      sr = fma(v.x, hx, sr);
+      sr = fma(-v.y, hy, sr);
+      si = fma(v.x, hy, si);
+      si = fma(v.y, hx, si);
     }
-    double2 o = w[i];
-    o.x += sign * sr;
-    o.y += sign * si;
+    T o = w[i];
+    o.x += (R)sign * sr;
+    o.y += (R)sign * si;
     w[i] = o;
   }
 }
 
-__global__ void scale_kernel(const double2* __restrict__ a, double2* __restrict__ b, double s, int n) {
+template <class T>
+__global__ void scale_kernel(const T* __restrict__ a, T* __restrict__ b, double s, int n) {
+  using R = typename Cx<T>::R;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = make_double2(a[i].x * s, a[i].y * s);
+    b[i] = Cx<T>::make(a[i].x * (R)s, a[i].y * (R)s);
 }
 
-__global__ void sub_kernel(const double2* __restrict__ a, const double2* __restrict__ b, double2* __restrict__ c, int n) {
+// b = a / sqrt(nrm->x), or zeros when the norm is zero (breakdown; the
+// vector is then never used).
+template <class T>
+__global__ void scale_by_norm_kernel(const T* __restrict__ a, T* __restrict__ b, const double2* __restrict__ nrm,
+                                     int n) {
+  using R = typename Cx<T>::R;
+  const double nn = nrm->x;
+  const R s = nn > 0.0 ? (R)(1.0 / sqrt(nn)) : R(0);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    c[i] = make_double2(a[i].x - b[i].x, a[i].y - b[i].y);
+    b[i] = Cx<T>::make(a[i].x * s, a[i].y * s);
 }
 
-__global__ void add_inplace_kernel(double2* __restrict__ a, const double2* __restrict__ b, int n) {
+template <class T>
+__global__ void sub_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ c, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    c[i] = Cx<T>::make(a[i].x - b[i].x, a[i].y - b[i].y);
+}
+
+__global__ void to_f32_kernel(const double2* __restrict__ a, float2* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+// a += b, with b widened to FP64
+__global__ void add_f32_kernel(double2* __restrict__ a, const float2* __restrict__ b, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    a[i].x += b[i].x;
-    a[i].y += b[i].y;
+    a[i].x += (double)b[i].x;
+    a[i].y += (double)b[i].y;
   }
 }
 
 using cdh = std::complex<double>;
 
-// b = a / sqrt(nrm->x), or zeros when the norm is zero (breakdown; the
-// vector is then never used).
-__global__ void scale_by_norm_kernel(const double2* __restrict__ a, double2* __restrict__ b,
-                                     const double2* __restrict__ nrm, int n) {
-  const double nn = nrm->x;
-  const double s = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = make_double2(a[i].x * s, a[i].y * s);
-}
-
 int grid_for(int n) { return std::min((n + 255) / 256, 152 * 8); }
 
 // h_dev[0:ncols) = V[:, 0:ncols)^H w
-void multidot(const double2* V, long long ldv, int ncols, const double2* w, int n, double2* partial, double2* h_dev,
-              int accumulate, cudaStream_t s) {
-  multidot_kernel<<<dim3(kDotBlocks, (ncols + kDotCols - 1) / kDotCols), kDotThreads, 0, s>>>(V, ldv, ncols, w, n,
-                                                                                              partial);
-  reduce_partials_kernel<<<(ncols * 32 + 255) / 256, 256, 0, s>>>(partial, kDotBlocks, ncols, h_dev, accumulate);
+template <class T>
+void multidot(const T* V, long long ldv, int ncols, const T* w, int n, double2* partial, double2* h_dev,
+              cudaStream_t s) {
+  multidot_kernel<T><<<dim3(kDotBlocks, (ncols + kDotCols - 1) / kDotCols), kDotThreads, 0, s>>>(V, ldv, ncols, w, n,
+                                                                                                 partial);
+  reduce_partials_kernel<<<(ncols * 32 + 255) / 256, 256, 0, s>>>(partial, kDotBlocks, ncols, h_dev);
 }
 
-cudaError_t vnorm(const double2* w, int n, double2* partial, double2* h_dev, cudaStream_t s, double& out) {
-  multidot(w, n, 1, w, n, partial, h_dev, 0, s);
+template <class T>
+cudaError_t vnorm(const T* w, int n, GmresWorkspace& ws, cudaStream_t s, double& out) {
+  multidot(w, n, 1, w, n, ws.partial, ws.nrm, s);
   double2 hv;
-  cudaError_t e = cudaMemcpyAsync(&hv, h_dev, sizeof(double2), cudaMemcpyDeviceToHost, s);
+  cudaError_t e = cudaMemcpyAsync(&hv, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return e;
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
   out = std::sqrt(hv.x);
   return cudaSuccess;
 }
 
-cudaError_t apply(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool f32) {
-  return f32 ? dev_matvec_f32(d, x, y, s, false) : dev_matvec(d, x, y, s, false);
+// y = A x with the operator that matches the basis element type: the FP64
+// operator (native or double-float kernels) for double2, the FP32 operator
+// for float2.
+cudaError_t apply(DevOperator& d, const double2* x, double2* y, cudaStream_t s) {
+  return dev_matvec(d, x, y, s, false);
 }
+cudaError_t apply(DevOperator& d, const float2* x, float2* y, cudaStream_t s) {
+  return dev_matvec_f32v(d, x, y, s);
+}
+
+Basis<double2>& basis(GmresWorkspace& ws, const double2*) { return ws.b64; }
+Basis<float2>& basis(GmresWorkspace& ws, const float2*) { return ws.b32; }
 
 // One Arnoldi cycle from x0 (device, may be null for x0 = 0). Writes the
 // updated solution into x. tol < 0 disables the residual stop; breakdown
 // exits when H(k+1,k) < brk.
-cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const double2* b, const double2* x0, double2* x, int m,
-                          double tol, double brk, double bnorm, std::vector<double>* hist, int& iters,
-                          bool& converged, bool f32) {
+template <class T>
+cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const T* x0, T* x, int m, double tol,
+                          double brk, double bnorm, std::vector<double>* hist, int& iters, bool& converged) {
+  Basis<T>& B = basis(ws, b);
   cudaStream_t s = d.stream;
   const int n = d.N;
   cudaError_t e;
   // r = b - A x0
   if (x0) {
-    if ((e = apply(d, x0, ws.w, s, f32)) != cudaSuccess) return e;
-    sub_kernel<<<grid_for(n), 256, 0, s>>>(b, ws.w, ws.r, n);
+    if ((e = apply(d, x0, B.w, s)) != cudaSuccess) return e;
+    sub_kernel<T><<<grid_for(n), 256, 0, s>>>(b, B.w, B.r, n);
   } else {
-    cudaMemcpyAsync(ws.r, b, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(B.r, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   }
   double beta = 0.0;
-  if ((e = vnorm(ws.r, n, ws.partial, ws.h, s, beta)) != cudaSuccess) return e;
+  if ((e = vnorm(B.r, n, ws, s, beta)) != cudaSuccess) return e;
   if (hist && hist->empty()) hist->push_back(beta / bnorm);
   converged = false;
   iters = 0;
   if (beta == 0.0) {
     if (x != x0) {
-      if (x0) cudaMemcpyAsync(x, x0, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
-      else cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), s);
+      if (x0) cudaMemcpyAsync(x, x0, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, s);
+      else cudaMemsetAsync(x, 0, (size_t)n * sizeof(T), s);
     }
     converged = true;
     return cudaStreamSynchronize(s);
   }
-  scale_kernel<<<grid_for(n), 256, 0, s>>>(ws.r, ws.V, 1.0 / beta, n);
+  scale_kernel<T><<<grid_for(n), 256, 0, s>>>(B.r, B.V, 1.0 / beta, n);
   std::vector<std::vector<cdh>> H;  // columns, already rotated
   std::vector<cdh> cs, sn, g(1, cdh(beta, 0.0));
-  std::vector<double2> hbuf(m + 2);
   int K = 0;
   // The product A v_{k+1} only needs v_{k+1} = w / |w|, which the device
   // forms itself, so it is queued before the host waits for step k's
   // coefficients: the host's Givens work and the wait hide behind it. A
   // converged or broken-down cycle leaves one unused product behind.
-  if ((e = apply(d, ws.V, ws.w, s, f32)) != cudaSuccess) return e;
+  if ((e = apply(d, B.V, B.w, s)) != cudaSuccess) return e;
+  double2* hp = ws.pinned;
+  double2* hp2 = ws.pinned + (m + 2);
+  double2* np = ws.pinned + 2 * (m + 2);
   for (int k = 0; k < m; ++k) {
     // CGS2, both passes and the norm on the device; one copy back per step.
-    multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h, 0, s);
-    multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h, n, -1.0);
-    multidot(ws.V, n, k + 1, ws.w, n, ws.partial, ws.h2, 0, s);
-    multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V, n, k + 1, ws.h2, n, -1.0);
-    multidot(ws.w, n, 1, ws.w, n, ws.partial, ws.nrm, 0, s);
-    scale_by_norm_kernel<<<grid_for(n), 256, 0, s>>>(ws.w, ws.V + (size_t)(k + 1) * n, ws.nrm, n);
-    double2* hp = ws.pinned;
-    double2* hp2 = ws.pinned + (m + 2);
-    double2* np = ws.pinned + 2 * (m + 2);
+    multidot(B.V, n, k + 1, B.w, n, ws.partial, ws.h, s);
+    multi_axpy_kernel<T><<<grid_for(n), 256, 0, s>>>(B.w, B.V, n, k + 1, ws.h, n, -1.0);
+    multidot(B.V, n, k + 1, B.w, n, ws.partial, ws.h2, s);
+    multi_axpy_kernel<T><<<grid_for(n), 256, 0, s>>>(B.w, B.V, n, k + 1, ws.h2, n, -1.0);
+    multidot(B.w, n, 1, B.w, n, ws.partial, ws.nrm, s);
+    scale_by_norm_kernel<T><<<grid_for(n), 256, 0, s>>>(B.w, B.V + (size_t)(k + 1) * n, ws.nrm, n);
     cudaMemcpyAsync(hp, ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hp2, ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(np, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
     if ((e = cudaEventRecord(ws.copied, s)) != cudaSuccess) return e;
-    if (k + 1 < m && (e = apply(d, ws.V + (size_t)(k + 1) * n, ws.w, s, f32)) != cudaSuccess) return e;
+    if (k + 1 < m && (e = apply(d, B.V + (size_t)(k + 1) * n, B.w, s)) != cudaSuccess) return e;
     if ((e = cudaEventSynchronize(ws.copied)) != cudaSuccess) return e;
     std::vector<cdh> hk(k + 2);
     for (int i = 0; i <= k; ++i) hk[i] = cdh(hp[i].x + hp2[i].x, hp[i].y + hp2[i].y);
@@ -370,14 +456,15 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const double2* b, 
     for (int j = i + 1; j < K; ++j) sum -= H[j][i] * y[j];
     y[i] = sum / H[i][i];
   }
+  std::vector<double2> hbuf(K + 1);
   for (int i = 0; i < K; ++i) hbuf[i] = make_double2(y[i].real(), y[i].imag());
   cudaMemcpyAsync(ws.h, hbuf.data(), (size_t)K * sizeof(double2), cudaMemcpyHostToDevice, s);
   if (x0) {
-    if (x != x0) cudaMemcpyAsync(x, x0, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+    if (x != x0) cudaMemcpyAsync(x, x0, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   } else {
-    cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), s);
+    cudaMemsetAsync(x, 0, (size_t)n * sizeof(T), s);
   }
-  multi_axpy_kernel<<<grid_for(n), 256, 0, s>>>(x, ws.V, n, K, ws.h, n, 1.0);
+  multi_axpy_kernel<T><<<grid_for(n), 256, 0, s>>>(x, B.V, n, K, ws.h, n, 1.0);
   iters = K;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return cudaStreamSynchronize(s);
@@ -386,12 +473,13 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const double2* b, 
 }  // namespace
 
 cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter, double tol,
-                      std::vector<double>& hist, GmresResult& res, bool use_f32) {
+                      std::vector<double>& hist, GmresResult& res) {
   GmresWorkspace& ws = workspace(d);
   cudaError_t e = ws.ensure(d.N, max_iter);
+  if (e == cudaSuccess) e = ws.b64.ensure(d.N, max_iter);
   if (e != cudaSuccess) return e;
   double bn = 0.0;
-  if ((e = vnorm(b, d.N, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) return e;
+  if ((e = vnorm(b, d.N, ws, d.stream, bn)) != cudaSuccess) return e;
   if (bn == 0.0) {
     cudaMemsetAsync(x, 0, (size_t)d.N * sizeof(double2), d.stream);
     res.iters = 0; res.rel_residual = 0.0; res.converged = true;
@@ -401,12 +489,13 @@ cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter
   hist.clear();
   int it = 0;
   bool conv = false;
-  if ((e = arnoldi_cycle(d, ws, b, nullptr, x, max_iter, tol, 1e-300, bn, &hist, it, conv, use_f32)) != cudaSuccess) return e;
+  if ((e = arnoldi_cycle<double2>(d, ws, b, nullptr, x, max_iter, tol, 1e-300, bn, &hist, it, conv)) != cudaSuccess)
+    return e;
   // True residual with the FP64 operator (the reference's "Err in GMRES").
-  if ((e = dev_matvec(d, x, ws.w, d.stream, false)) != cudaSuccess) return e;
-  sub_kernel<<<grid_for(d.N), 256, 0, d.stream>>>(b, ws.w, ws.r, d.N);
+  if ((e = dev_matvec(d, x, ws.b64.w, d.stream, false)) != cudaSuccess) return e;
+  sub_kernel<double2><<<grid_for(d.N), 256, 0, d.stream>>>(b, ws.b64.w, ws.b64.r, d.N);
   double rn = 0.0;
-  if ((e = vnorm(ws.r, d.N, ws.partial, ws.h, d.stream, rn)) != cudaSuccess) return e;
+  if ((e = vnorm(ws.b64.r, d.N, ws, d.stream, rn)) != cudaSuccess) return e;
   res.iters = it;
   res.converged = conv;
   res.rel_residual = rn / bn;
@@ -416,33 +505,35 @@ cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter
 cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, int m, int restarts) {
   GmresWorkspace& ws = workspace(d);
   cudaError_t e = ws.ensure(d.N, m);
+  if (e == cudaSuccess) e = ws.b64.ensure(d.N, m);
   if (e != cudaSuccess) return e;
   double bn = 0.0;
-  if ((e = vnorm(b, d.N, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) return e;
+  if ((e = vnorm(b, d.N, ws, d.stream, bn)) != cudaSuccess) return e;
   if (bn == 0.0) bn = 1.0;
   cudaMemsetAsync(x, 0, (size_t)d.N * sizeof(double2), d.stream);
   for (int r = 0; r < restarts; ++r) {
     int it = 0;
     bool conv = false;
-    if ((e = arnoldi_cycle(d, ws, b, x, x, m, -1.0, 1e-8, bn, nullptr, it, conv, false)) != cudaSuccess) return e;
+    if ((e = arnoldi_cycle<double2>(d, ws, b, x, x, m, -1.0, 1e-8, bn, nullptr, it, conv)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
 // Iterative refinement in FP64 around GMRES on the FP32 operator:
-//   r = b - A64 x ; solve A32 d = r to a loose tolerance ; x += d
-// until |b - A64 x| / |b| <= tol. The residual is always the FP64 one.
+//   r = b - A64 x ; solve A32 d = r in FP32 to a loose tolerance ; x += d
+// until |b - A64 x| / |b| <= tol. The residual is always the FP64 one; the
+// inner Arnoldi basis and its orthogonalisation are FP32.
 cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner, double tol,
                             std::vector<double>& hist, int& n_matvec, double& relres) {
   const int n = d.N;
   GmresWorkspace& ws = workspace(d);
   cudaError_t e = ws.ensure(n, inner);
+  if (e == cudaSuccess) e = ws.b32.ensure(n, inner);
+  if (e == cudaSuccess && ws.b64.n != n) e = ws.b64.ensure(n, 1);
   if (e != cudaSuccess) return e;
-  // r and dx must survive the inner cycles, which use ws.r and ws.w.
   double2* r = ws.res;
-  double2* dx = ws.dx;
   double bn = 0.0;
-  if ((e = vnorm(b, n, ws.partial, ws.h, d.stream, bn)) != cudaSuccess) goto done;
+  if ((e = vnorm(b, n, ws, d.stream, bn)) != cudaSuccess) return e;
   hist.clear();
   n_matvec = 0;
   cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), d.stream);
@@ -454,21 +545,21 @@ cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int ma
     bool conv = false;
     // Inner solve to roughly the FP32 operator accuracy.
     const double inner_tol = std::max(tol / std::max(relres, 1e-300), 1e-6);
-    if ((e = arnoldi_cycle(d, ws, r, nullptr, dx, inner, inner_tol, 1e-300, std::max(relres * bn, 1e-300), nullptr, it,
-                           conv, true)) != cudaSuccess)
-      goto done;
+    to_f32_kernel<<<grid_for(n), 256, 0, d.stream>>>(r, ws.res32, n);
+    if ((e = arnoldi_cycle<float2>(d, ws, ws.res32, nullptr, ws.dx32, inner, inner_tol, 1e-300,
+                                   std::max(relres * bn, 1e-300), nullptr, it, conv)) != cudaSuccess)
+      return e;
     n_matvec += it;
-    add_inplace_kernel<<<grid_for(n), 256, 0, d.stream>>>(x, dx, n);
-    if ((e = dev_matvec(d, x, ws.w, d.stream, false)) != cudaSuccess) goto done;
+    add_f32_kernel<<<grid_for(n), 256, 0, d.stream>>>(x, ws.dx32, n);
+    if ((e = dev_matvec(d, x, ws.b64.w, d.stream, false)) != cudaSuccess) return e;
     ++n_matvec;
-    sub_kernel<<<grid_for(n), 256, 0, d.stream>>>(b, ws.w, r, n);
+    sub_kernel<double2><<<grid_for(n), 256, 0, d.stream>>>(b, ws.b64.w, r, n);
     double rn = 0.0;
-    if ((e = vnorm(r, n, ws.partial, ws.h, d.stream, rn)) != cudaSuccess) goto done;
+    if ((e = vnorm(r, n, ws, d.stream, rn)) != cudaSuccess) return e;
     relres = rn / bn;
     hist.push_back(relres);
   }
-done:
-  return e;
+  return cudaSuccess;
 }
 
 }  // namespace lsg

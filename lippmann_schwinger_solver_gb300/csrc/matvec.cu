@@ -267,11 +267,15 @@ __global__ void __launch_bounds__(576, 1) near_gemm32_kernel(int n_leaves, int r
   }
 }
 
+__device__ __forceinline__ void store_out(double2* y, int t, float a, float b) { y[t] = make_double2((double)a, (double)b); }
+__device__ __forceinline__ void store_out(float2* y, int t, float a, float b) { y[t] = make_float2(a, b); }
+
+template <class Y>
 __global__ void __launch_bounds__(256) near_gather32_kernel(int n_out, int rank, const float2* __restrict__ Z,
                                                             const float* __restrict__ kq,
                                                             const int* __restrict__ coll,
                                                             const float2* __restrict__ x,
-                                                            const float2* __restrict__ P, double2* __restrict__ y,
+                                                            const float2* __restrict__ P, Y* __restrict__ y,
                                                             int find_phi) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out) return;
@@ -290,9 +294,9 @@ __global__ void __launch_bounds__(256) near_gather32_kernel(int n_out, int rank,
   if (find_phi) {
     const float s = kq[t];
     const float2 xs = x[t];
-    y[t] = make_double2((double)(p.x + s * ar + xs.x), (double)(p.y + s * ai + xs.y));
+    store_out(y, t, p.x + s * ar + xs.x, p.y + s * ai + xs.y);
   } else {
-    y[t] = make_double2((double)(p.x + ar), (double)(p.y + ai));
+    store_out(y, t, p.x + ar, p.y + ai);
   }
 }
 
@@ -522,10 +526,9 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
   return cudaGetLastError();
 }
 
-cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
-  if (!d.has_f32) return cudaErrorInvalidValue;
-  if (!s) s = d.stream;
-  d2f_kernel<<<256, 256, 0, s>>>(x, d.S32, d.N);
+// Phases of the FP32 operator after x has been placed in S32.
+template <class Y>
+static cudaError_t f32_phases(DevOperator& d, Y* y, cudaStream_t s, bool mark_m2l) {
   cudaMemsetAsync(d.P32, 0, (size_t)d.pots_len * sizeof(float2), s);
   for (auto& ph : d.up32) launch_gemv<0>(ph, (const float2*)d.S32, d.S32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[2], s);
@@ -536,9 +539,23 @@ cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStr
   near_gemm32_kernel<<<(d.n_leaves + kNearSources32 - 1) / kNearSources32, nthr,
                        (size_t)kNearSources32 * d.rank * sizeof(float2), s>>>(d.n_leaves, d.rank, d.nearB32, d.S32,
                                                                               d.Z32);
-  near_gather32_kernel<<<(d.N + 255) / 256, 256, 0, s>>>(d.N, d.rank, d.Z32, d.kq32, d.colleague, d.S32, d.P32, y,
-                                                         d.find_phi);
+  near_gather32_kernel<Y><<<(d.N + 255) / 256, 256, 0, s>>>(d.N, d.rank, d.Z32, d.kq32, d.colleague, d.S32, d.P32, y,
+                                                            d.find_phi);
   return cudaGetLastError();
+}
+
+cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
+  if (!d.has_f32) return cudaErrorInvalidValue;
+  if (!s) s = d.stream;
+  d2f_kernel<<<256, 256, 0, s>>>(x, d.S32, d.N);
+  return f32_phases(d, y, s, mark_m2l);
+}
+
+cudaError_t dev_matvec_f32v(DevOperator& d, const float2* x, float2* y, cudaStream_t s) {
+  if (!d.has_f32) return cudaErrorInvalidValue;
+  if (!s) s = d.stream;
+  cudaMemcpyAsync(d.S32, x, (size_t)d.N * sizeof(float2), cudaMemcpyDeviceToDevice, s);
+  return f32_phases(d, y, s, false);
 }
 
 // ---------------------------------------------------------------------------

@@ -182,10 +182,15 @@ __global__ void __launch_bounds__(256) near_coeff_df_kernel(int n_leaves, int ra
 // A block takes kNearSources leaves; thread (q, row) keeps one accumulator
 // per leaf, so every factor entry it loads serves kNearSources products and
 // each thread has that many independent dependency chains. The leaves'
-// coefficients are staged in shared memory (broadcast reads).
-constexpr int kNearSources = 8;
+// coefficients are staged in shared memory (broadcast reads). Four leaves
+// per block and three blocks per SM measured fastest on GB300 (69 us at
+// level 6, against 82 us for eight leaves and two blocks).
+constexpr int kNearSources = 4;
 
-__global__ void __launch_bounds__(576) near_gemm_df_kernel(int n_leaves, int rank, int nb,
+constexpr int kNearThreads = 352;    // threads of a near-field GEMM block (loop over 9 * rank outputs)
+constexpr int kNearMinBlocks = 3;    // resident blocks per SM the register budget must allow
+
+__global__ void __launch_bounds__(kNearThreads, kNearMinBlocks) near_gemm_df_kernel(int n_leaves, int rank, int nb,
                                                            const float4* __restrict__ Vt,
                                                            const float2* __restrict__ E,
                                                            const float4* __restrict__ c,
@@ -204,40 +209,40 @@ __global__ void __launch_bounds__(576) near_gemm_df_kernel(int n_leaves, int ran
     sx[i] = s0 + j < n_leaves ? x32[(size_t)s0 * rank + i] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const int qr = threadIdx.x;
-  if (qr >= 9 * rank) return;
-  const int q = qr / rank, row = qr - q * rank;
-  float h[NS][4];
-  float er[NS], ei[NS];
-#pragma unroll
-  for (int j = 0; j < NS; ++j) {
-    h[j][0] = h[j][1] = h[j][2] = h[j][3] = 0.f;
-    er[j] = ei[j] = 0.f;
-  }
-  const float4* __restrict__ v = Vt + (size_t)q * nb * rank + row;
-  for (int l = 0; l < nb; ++l) {
-    const float4 a = v[(size_t)l * rank];
-#pragma unroll
-    for (int j = 0; j < NS; ++j) cmac(h[j][0], h[j][1], h[j][2], h[j][3], a, sc[j * nb + l]);
-  }
-  const float2* __restrict__ e = E + (size_t)q * rank * rank + row;
-  for (int k = 0; k < rank; ++k) {
-    const float2 a = e[(size_t)k * rank];
+  for (int qr = threadIdx.x; qr < 9 * rank; qr += blockDim.x) {
+    const int q = qr / rank, row = qr - q * rank;
+    float h[NS][4];
+    float er[NS], ei[NS];
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      const float2 b = sx[j * rank + k];
-      er[j] = fmaf(a.x, b.x, er[j]);
-      er[j] = fmaf(-a.y, b.y, er[j]);
-      ei[j] = fmaf(a.x, b.y, ei[j]);
-      ei[j] = fmaf(a.y, b.x, ei[j]);
+      h[j][0] = h[j][1] = h[j][2] = h[j][3] = 0.f;
+      er[j] = ei[j] = 0.f;
     }
-  }
-  const size_t per = (size_t)9 * rank;
+    const float4* __restrict__ v = Vt + (size_t)q * nb * rank + row;
+    for (int l = 0; l < nb; ++l) {
+      const float4 a = v[(size_t)l * rank];
 #pragma unroll
-  for (int j = 0; j < NS; ++j) {
-    if (s0 + j >= n_leaves) break;
-    Z[(size_t)(s0 + j) * per + qr] = pack(h[j][0], h[j][1], h[j][2], h[j][3]);
-    ZE[(size_t)(s0 + j) * per + qr] = make_float2(er[j], ei[j]);
+      for (int j = 0; j < NS; ++j) cmac(h[j][0], h[j][1], h[j][2], h[j][3], a, sc[j * nb + l]);
+    }
+    const float2* __restrict__ e = E + (size_t)q * rank * rank + row;
+    for (int k = 0; k < rank; ++k) {
+      const float2 a = e[(size_t)k * rank];
+#pragma unroll
+      for (int j = 0; j < NS; ++j) {
+        const float2 b = sx[j * rank + k];
+        er[j] = fmaf(a.x, b.x, er[j]);
+        er[j] = fmaf(-a.y, b.y, er[j]);
+        ei[j] = fmaf(a.x, b.y, ei[j]);
+        ei[j] = fmaf(a.y, b.x, ei[j]);
+      }
+    }
+    const size_t per = (size_t)9 * rank;
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      if (s0 + j >= n_leaves) break;
+      Z[(size_t)(s0 + j) * per + qr] = pack(h[j][0], h[j][1], h[j][2], h[j][3]);
+      ZE[(size_t)(s0 + j) * per + qr] = make_float2(er[j], ei[j]);
+    }
   }
 }
 
@@ -382,9 +387,8 @@ cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStre
   near_coeff_df_kernel<<<(d.n_leaves * d.n_bases + 255) / 256, 256, 0, s>>>(d.n_leaves, d.rank, d.n_bases, d.Qp_df,
                                                                             d.S_df, d.c_df, d.x32);
   {
-    const int nthr = (9 * d.rank + 31) / 32 * 32;
     const size_t smem = (size_t)kNearSources * (d.n_bases * sizeof(float4) + d.rank * sizeof(float2));
-    near_gemm_df_kernel<<<(d.n_leaves + kNearSources - 1) / kNearSources, nthr, smem, s>>>(
+    near_gemm_df_kernel<<<(d.n_leaves + kNearSources - 1) / kNearSources, kNearThreads, smem, s>>>(
         d.n_leaves, d.rank, d.n_bases, d.Vt_df, d.nearE, d.c_df, d.x32, d.Z_df, d.ZE_df);
     near_gather_df_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.Z_df, d.ZE_df, d.kq, d.colleague, x, d.P_df,
                                                           y, d.find_phi);
