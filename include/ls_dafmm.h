@@ -167,6 +167,21 @@ ls_status ls_gmres_mixed(ls_op* op, const double* b, int max_outer, int inner_it
                          double tol, double* x, double* history, int* n_matvec,
                          double* rel_residual);
 
+/*
+ * Many right-hand sides on one operator (e.g. the incident fields of many
+ * directions on one scatterer). No single counterpart in the reference,
+ * which runs one GMRES per right-hand side (GMRES/GMRES.cpp:336-470).
+ * Solves A x_j = b_j for j < nrhs with the mixed-precision refinement of
+ * ls_gmres_mixed, kBatchRhs (8) columns at a time: the inner FP32 GMRES of
+ * the columns share every operator apply, and each column stops on its own
+ * FP64 true residual. B and X are host arrays of nrhs columns of N complex
+ * values (column j at 2 * N * j doubles). n_matvec counts FP32 block
+ * applies plus FP64 residual products; rel_residuals (nrhs, may be NULL)
+ * gets each column's final FP64 relative residual. Needs
+ * ls_op_enable_f32(); LS_E_NOT_CONVERGED when a column misses tol.
+ */
+ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_outer, int inner_iter, double tol,
+                                 double* X, int* n_matvec, double* rel_residuals);
 /* Times `iters` device matvecs (inputs resident) with CUDA events on the
  * operator's stream after `warmup` untimed ones; writes the mean ms per
  * matvec and the mean ms of the dominant kernel (M2L). precision: LS_PREC_*. */

@@ -43,7 +43,7 @@ EXPORTED_SYMBOLS = (
     "ls_op_create", "ls_op_destroy", "ls_op_info", "ls_op_points", "ls_op_contrast", "ls_op_rhs",
     "ls_matvec", "ls_matvec_f32", "ls_op_enable_f32", "ls_matvec_host", "ls_gmres", "ls_gmres_restarted",
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
-    "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels",
+    "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched",
 )
 
 
@@ -170,6 +170,8 @@ def lib():
             getattr(L, n).argtypes = [vp, vp, vp, vp]
         L.ls_op_enable_f32.argtypes = [vp]
         L.ls_op_set_f64_kernels.argtypes = [vp, ctypes.c_int]
+        L.ls_gmres_mixed_batched.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp,
+                                             ip, dp]
         L.ls_matvec_host.argtypes = [vp, dp, dp]
         L.ls_gmres.argtypes = [vp, dp, ctypes.c_int, ctypes.c_double, dp, dp, ip, dp]
         L.ls_gmres_restarted.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, dp]
@@ -306,6 +308,34 @@ class Operator:
         if code not in (LS_OK, LS_E_NOT_CONVERGED):
             _check(code, "ls_gmres_mixed")
         return x, hist[~np.isnan(hist)], nmv.value, rr.value, code
+
+    def gmres_mixed_batched(self, B, max_outer=10, inner_iter=100, tol=1e-8):
+        """Solves A X = B for the columns of B (N x nrhs) with the batched
+        mixed-precision refinement (needs enable_f32()). Returns (X, number of
+        FP32 block applies + FP64 residual products, per-column FP64 relative
+        residuals, status)."""
+        B = np.asfortranarray(B, dtype=np.complex128)
+        if B.ndim != 2 or B.shape[0] != self.N:
+            raise ValueError("B must be N x nrhs")
+        nrhs = B.shape[1]
+        X = np.empty_like(B, order="F")
+        rr = np.empty(nrhs)
+        nmv = ctypes.c_int(0)
+        code = lib().ls_gmres_mixed_batched(self._h, int(nrhs), _dp(B), int(max_outer), int(inner_iter), float(tol),
+                                            _dp(X), ctypes.byref(nmv), rr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        if code not in (LS_OK, LS_E_NOT_CONVERGED):
+            _check(code, "ls_gmres_mixed_batched")
+        return X, nmv.value, rr, code
+
+    def rhs_angles(self, thetas):
+        """Right-hand sides -kappa^2 q exp(i kappa (x cos t + y sin t)) for the
+        incidence directions t (GMRES/GMRES.cpp:119-126 for t = 0), N x len(t)."""
+        xy = self.points()
+        q = self.contrast()
+        k = self.cfg.kappa
+        t = np.asarray(thetas, dtype=float)
+        phase = np.outer(xy[:, 0], np.cos(t)) + np.outer(xy[:, 1], np.sin(t))
+        return np.asfortranarray(-(k * k) * q[:, None] * np.exp(1j * k * phase))
 
     def time_matvec(self, warmup=3, iters=20, precision=LS_PREC_F64):
         a, b = ctypes.c_float(), ctypes.c_float()

@@ -118,7 +118,8 @@ ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
   o->device_bytes = d.device_bytes;
   o->assemble_seconds = h.assemble_seconds;
   o->max_rank = h.max_rank;
-  o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 1 : 0);
+  // double-float: + the split of x and the near-field gather
+  o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 2 : 0);
   // M2L: every block once (16 B per complex entry), every source charge of
   // the charge buffer once, every potential it writes once.
   o->m2l_entries = op->on_device ? d.m2l.entries : h.m2l.entries();
@@ -281,6 +282,42 @@ ls_status ls_gmres_mixed(ls_op* op, const double* b, int max_outer, int inner_it
   if (n_matvec) *n_matvec = nmv;
   if (rel_residual) *rel_residual = rr;
   if (rr > tol) return fail(LS_E_NOT_CONVERGED, "ls_gmres_mixed: tolerance not reached");
+  return LS_OK;
+}
+
+ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_outer, int inner_iter, double tol,
+                                 double* X, int* n_matvec, double* rel_residuals) {
+  if (!op || !B || !X) return fail(LS_E_INVALID, "ls_gmres_mixed_batched: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_gmres_mixed_batched: operator was assembled without a device");
+  if (nrhs < 1 || max_outer < 1 || inner_iter < 1)
+    return fail(LS_E_INVALID, "ls_gmres_mixed_batched: nrhs and iteration counts must be >= 1");
+  if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_gmres_mixed_batched: call ls_op_enable_f32 first");
+  DevOperator& d = op->dev;
+  cudaSetDevice(d.device);
+  const size_t bytes = (size_t)d.N * nrhs * sizeof(double2);
+  double2 *db = nullptr, *dx = nullptr;
+  cudaError_t e = cudaMalloc(&db, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&dx, bytes);
+  if (e != cudaSuccess) {
+    cudaFree(db);
+    return cuda_fail(e, "ls_gmres_mixed_batched alloc");
+  }
+  std::vector<double> rr;
+  int nmv = 0;
+  if ((e = cudaMemcpyAsync(db, B, bytes, cudaMemcpyHostToDevice, d.stream)) == cudaSuccess)
+    e = dev_gmres_mixed_batch(d, nrhs, db, dx, max_outer, inner_iter, tol, nmv, rr);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(X, dx, bytes, cudaMemcpyDeviceToHost, d.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d.stream);
+  cudaFree(db);
+  cudaFree(dx);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_gmres_mixed_batched");
+  if (n_matvec) *n_matvec = nmv;
+  bool ok = true;
+  for (int j = 0; j < nrhs; ++j) {
+    if (rel_residuals) rel_residuals[j] = rr[j];
+    ok = ok && rr[j] <= tol;
+  }
+  if (!ok) return fail(LS_E_NOT_CONVERGED, "ls_gmres_mixed_batched: a column did not reach the tolerance");
   return LS_OK;
 }
 

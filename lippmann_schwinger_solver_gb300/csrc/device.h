@@ -14,9 +14,9 @@ namespace lsg {
 template <class C>
 struct DevPhase {
   C* A = nullptr;            // tiles (double2 or float2)
-  int* idx = nullptr;        // gather indices (same positions as A)
+  int* idx = nullptr;        // gather indices, one per tile, step and slice
   int* out = nullptr;        // output element per row
-  int* klen = nullptr;       // length per row
+  int* klen = nullptr;       // steps per lane
   GemvTile* tiles = nullptr;
   int n_tiles = 0;
   int accumulate = 0;
@@ -25,6 +25,10 @@ struct DevPhase {
 };
 
 struct GmresWorkspace;  // gmres.cu: Krylov basis and scratch, kept between solves
+struct BatchWorkspace;  // batched.cu: state of the many-right-hand-side solver
+
+// Right-hand sides handled together by the batched solver (batched.cu).
+constexpr int kBatchRhs = 8;
 
 struct DevOperator {
   int device = 0;
@@ -74,6 +78,7 @@ struct DevOperator {
   double2* xbuf = nullptr;
   double2* ybuf = nullptr;
   GmresWorkspace* gws = nullptr;
+  BatchWorkspace* bws = nullptr;
   // events for phase timing
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   long long device_bytes = 0;
@@ -100,6 +105,18 @@ cudaError_t dev_matvec_static(DevOperator& d, const double2* x, double2* y, cuda
 bool dev_enable_df(DevOperator& d, std::string& err);
 void dev_free_df(DevOperator& d);
 cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
+
+// batched.cu
+void dev_free_batch(DevOperator& d);
+// y_j = A32 x_j for the kBatchRhs vectors of a block stored rhs-minor
+// (element (i, j) at i * kBatchRhs + j); FP32 operator.
+cudaError_t dev_matvec_f32_batch(DevOperator& d, const float2* x, float2* y, cudaStream_t s);
+// Mixed-precision refinement for nrhs right-hand sides (device arrays,
+// column j at b + j * N), solved kBatchRhs at a time with a shared FP32
+// operator apply. n_matvec counts FP32 block applies and FP64 residual
+// products; relres gets each column's final FP64 relative residual.
+cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, double2* x, int max_outer, int inner,
+                                  double tol, int& n_matvec, std::vector<double>& relres);
 
 // gmres.cu
 void dev_free_gmres(DevOperator& d);

@@ -467,6 +467,7 @@ void dev_free(DevOperator& d) {
   cudaFree(d.xbuf); cudaFree(d.ybuf);
   dev_free_df(d);
   dev_free_gmres(d);
+  dev_free_batch(d);
   for (auto& ev : d.ev) if (ev) cudaEventDestroy(ev);
   if (d.stream) cudaStreamDestroy(d.stream);
   d = DevOperator();

@@ -1,0 +1,50 @@
+"""Many right-hand sides on one operator (ls_gmres_mixed_batched).
+
+Each column is judged by its own FP64 true residual, like ls_gmres_mixed;
+the batched solution must agree with the single-vector FP64 GMRES solution
+to the accuracy both solves carry (residual 1e-8, relative solution
+difference bound 1e-5 written below).
+"""
+import numpy as np
+import pytest
+
+from conftest import CFG_C1, CFG_HFR, full_cfg
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("base,kernels", [(CFG_C1, 0), (CFG_HFR, 1)])
+def test_batched_solve_matches_single_solves(ls, base, kernels):
+    op = ls.Operator(full_cfg(base), device=0)
+    op.enable_f32()
+    op.set_f64_kernels(kernels)
+    thetas = np.linspace(0.0, 2 * np.pi, 11, endpoint=False)  # one full block of 8 and a partial one
+    B = op.rhs_angles(thetas)
+    assert np.allclose(B[:, 0], op.rhs(), rtol=1e-14, atol=0)
+    X, nmv, rr, code = op.gmres_mixed_batched(B, max_outer=20, inner_iter=200, tol=1e-8)
+    assert code == 0
+    assert nmv > 0
+    assert np.all(rr <= 1e-8)
+    op.set_f64_kernels(ls.LS_F64_NATIVE)
+    for j in (0, 3, 8, 10):
+        r = B[:, j] - op.matvec(X[:, j])
+        assert np.linalg.norm(r) / np.linalg.norm(B[:, j]) <= 1.5e-8
+        xs, _, _, rs, cs = op.gmres(B[:, j], max_iter=400, tol=1e-10)
+        assert cs == 0
+        assert _rel(X[:, j], xs) <= 1e-5
+    op.close()
+
+
+def test_batched_rejects_bad_input(ls):
+    op = ls.Operator(full_cfg(CFG_C1), device=0)
+    B = op.rhs_angles([0.0, 1.0])
+    with pytest.raises(ls.LSError):  # FP32 operator not enabled
+        op.gmres_mixed_batched(B)
+    op.enable_f32()
+    with pytest.raises(ValueError):
+        op.gmres_mixed_batched(B[:-1])
+    op.close()
