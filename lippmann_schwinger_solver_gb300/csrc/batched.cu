@@ -390,14 +390,20 @@ __global__ void __launch_bounds__(256) multi_axpy_block_kernel(float2* __restric
   }
 }
 
-// b[i][j] = a[i][j] / sqrt(nrm[j]), zero for a zero norm.
+// b[i][j] = a[i][j] / sqrt(nrm[j]), zero for a zero norm. The NR factors
+// are formed once per thread block (FP64 divides are slow on GB300).
 __global__ void scale_block_kernel(const float2* __restrict__ a, float2* __restrict__ b,
                                    const double2* __restrict__ nrm, int n) {
+  __shared__ float f[NR];
+  if (threadIdx.x < NR) {
+    const double nn = nrm[threadIdx.x].x;
+    f[threadIdx.x] = nn > 0.0 ? (float)(1.0 / sqrt(nn)) : 0.f;
+  }
+  __syncthreads();
   const long long tot = (long long)n * NR;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (long long)gridDim.x * blockDim.x) {
-    const double nn = nrm[e % NR].x;
-    const float s = nn > 0.0 ? (float)(1.0 / sqrt(nn)) : 0.f;
+    const float s = f[e % NR];
     b[e] = make_float2(a[e].x * s, a[e].y * s);
   }
 }

@@ -302,8 +302,13 @@ template <class T>
 __global__ void scale_by_norm_kernel(const T* __restrict__ a, T* __restrict__ b, const double2* __restrict__ nrm,
                                      int n) {
   using R = typename Cx<T>::R;
-  const double nn = nrm->x;
-  const R s = nn > 0.0 ? (R)(1.0 / sqrt(nn)) : R(0);
+  __shared__ R f;  // formed once per thread block (FP64 divides are slow on GB300)
+  if (threadIdx.x == 0) {
+    const double nn = nrm->x;
+    f = nn > 0.0 ? (R)(1.0 / sqrt(nn)) : R(0);
+  }
+  __syncthreads();
+  const R s = f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     b[i] = Cx<T>::make(a[i].x * s, a[i].y * s);
 }
