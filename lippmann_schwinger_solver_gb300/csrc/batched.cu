@@ -359,7 +359,7 @@ __global__ void reduce_block_partials_kernel(const double2* __restrict__ partial
 }
 
 // w[i][j] += sign * sum_c V[c][i][j] * h[c][j]
-__global__ void __launch_bounds__(256) multi_axpy_block_kernel(float2* __restrict__ w, const float2* __restrict__ V,
+__global__ void __launch_bounds__(256, 4) multi_axpy_block_kernel(float2* __restrict__ w, const float2* __restrict__ V,
                                                                int n, int ncols, const double2* __restrict__ h,
                                                                float sign) {
   const long long tot = (long long)n * NR;
