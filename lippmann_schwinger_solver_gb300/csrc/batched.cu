@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "device.h"
+#include "launch.h"
 
 namespace lsg {
 
@@ -140,6 +141,7 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
                                                             const int* __restrict__ qlen,
                                                             const float2* __restrict__ src, float2* __restrict__ dst,
                                                             int accumulate) {
+  pdl_enter();
   constexpr int NV = NR / 2;  // float4 per gathered point
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -215,6 +217,7 @@ __global__ void __launch_bounds__(352, 2) near_gemm_block_kernel(int n_leaves, i
                                                                  const float2* __restrict__ BT,
                                                                  const float2* __restrict__ x,
                                                                  float2* __restrict__ Z) {
+  pdl_enter();
   constexpr int NS = kBatchNearSources;
   constexpr int NV = NR / 2;
   extern __shared__ float4 sx4[];  // [s][k][p]
@@ -262,6 +265,7 @@ __global__ void __launch_bounds__(256) near_gather_block_kernel(int n_out, int r
                                                                 const float2* __restrict__ x,
                                                                 const float2* __restrict__ P,
                                                                 float2* __restrict__ y, int find_phi) {
+  pdl_enter();
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (long long)n_out * NR) return;
   const int t = (int)(e / NR), j = (int)(e - (long long)t * NR);
@@ -292,6 +296,7 @@ __global__ void __launch_bounds__(256) near_gather_block_kernel(int n_out, int r
 __global__ void __launch_bounds__(kBDotThreads) multidot_block_kernel(const float2* __restrict__ V, int n,
                                                                       const float2* __restrict__ w,
                                                                       double2* __restrict__ partial) {
+  pdl_enter();
   constexpr int NV = NR / 2;
   __shared__ float red[kBDotThreads / 32][2 * NR];
   const int chunk = (n + gridDim.x - 1) / gridDim.x;
@@ -342,6 +347,7 @@ __global__ void __launch_bounds__(kBDotThreads) multidot_block_kernel(const floa
 // out[c] = sum_b partial[c * nb + b], one warp per entry (fixed order).
 __global__ void reduce_block_partials_kernel(const double2* __restrict__ partial, int nb, int nent,
                                              double2* __restrict__ out) {
+  pdl_enter();
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= nent) return;
@@ -362,6 +368,7 @@ __global__ void reduce_block_partials_kernel(const double2* __restrict__ partial
 __global__ void __launch_bounds__(256, 4) multi_axpy_block_kernel(float2* __restrict__ w, const float2* __restrict__ V,
                                                                int n, int ncols, const double2* __restrict__ h,
                                                                float sign) {
+  pdl_enter();
   const long long tot = (long long)n * NR;
   const long long stride = (long long)n * NR;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
@@ -394,6 +401,7 @@ __global__ void __launch_bounds__(256, 4) multi_axpy_block_kernel(float2* __rest
 // are formed once per thread block (FP64 divides are slow on GB300).
 __global__ void scale_block_kernel(const float2* __restrict__ a, float2* __restrict__ b,
                                    const double2* __restrict__ nrm, int n) {
+  pdl_enter();
   __shared__ float f[NR];
   if (threadIdx.x < NR) {
     const double nn = nrm[threadIdx.x].x;
@@ -410,6 +418,7 @@ __global__ void scale_block_kernel(const float2* __restrict__ a, float2* __restr
 
 // r32[i][j] = (float) r[j * n + i] for active columns, 0 otherwise.
 __global__ void pack_block_kernel(const double2* __restrict__ r, float2* __restrict__ r32, int n, unsigned active) {
+  pdl_enter();
   const long long tot = (long long)n * NR;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (long long)gridDim.x * blockDim.x) {
@@ -426,6 +435,7 @@ __global__ void pack_block_kernel(const double2* __restrict__ r, float2* __restr
 // x[j * n + i] += dx[i][j] for active columns.
 __global__ void unpack_add_block_kernel(double2* __restrict__ x, const float2* __restrict__ dx, int n, int ncols,
                                         unsigned active) {
+  pdl_enter();
   const long long tot = (long long)n * ncols;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (long long)gridDim.x * blockDim.x) {
@@ -439,6 +449,7 @@ __global__ void unpack_add_block_kernel(double2* __restrict__ x, const float2* _
 
 __global__ void sub64_kernel(const double2* __restrict__ a, const double2* __restrict__ b, double2* __restrict__ c,
                              int n) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     c[i] = make_double2(a[i].x - b[i].x, a[i].y - b[i].y);
 }
@@ -446,6 +457,7 @@ __global__ void sub64_kernel(const double2* __restrict__ a, const double2* __res
 // partial[col * gridDim.x + block] = |A[:, col]|^2 over the block's rows (FP64 columns, leading dimension n).
 __global__ void __launch_bounds__(kBDotThreads) colnorm_kernel(const double2* __restrict__ A, int n,
                                                                double2* __restrict__ partial) {
+  pdl_enter();
   __shared__ double red[kBDotThreads / 32];
   const int chunk = (n + gridDim.x - 1) / gridDim.x;
   const int r0 = blockIdx.x * chunk;
@@ -483,14 +495,14 @@ void launch_block(const DevPhase<float2>& ph, const float2* src, float2* dst, cu
   if (ph.n_tiles == 0) return;
   int blocks = (ph.n_tiles + 7) / 8;
   blocks = std::min(blocks, sms_b(dev) * 8);
-  gemv_block_kernel<PHASE><<<blocks, 256, 0, s>>>(ph.tiles, ph.n_tiles, ph.A, ph.idx, ph.out, ph.klen, src, dst,
+  launch_pdl(gemv_block_kernel<PHASE>, blocks, 256, 0, s, ph.tiles, ph.n_tiles, ph.A, ph.idx, ph.out, ph.klen, src, dst,
                                                   ph.accumulate);
 }
 
 // |columns|^2 of an n x ncols FP64 array into out (host), ncols <= NR.
 cudaError_t colnorms(const double2* A, int n, int ncols, BatchWorkspace& B, cudaStream_t s, double* out) {
-  colnorm_kernel<<<dim3(kBDotBlocks, ncols), kBDotThreads, 0, s>>>(A, n, B.partial);
-  reduce_block_partials_kernel<<<(ncols * 32 + 255) / 256, 256, 0, s>>>(B.partial, kBDotBlocks, ncols, B.nrm);
+  launch_pdl(colnorm_kernel, dim3(kBDotBlocks, ncols), kBDotThreads, 0, s, A, n, B.partial);
+  launch_pdl(reduce_block_partials_kernel, (ncols * 32 + 255) / 256, 256, 0, s, B.partial, kBDotBlocks, ncols, B.nrm);
   std::vector<double2> v(ncols);
   cudaError_t e = cudaMemcpyAsync(v.data(), B.nrm, (size_t)ncols * sizeof(double2), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return e;
@@ -501,8 +513,8 @@ cudaError_t colnorms(const double2* A, int n, int ncols, BatchWorkspace& B, cuda
 
 void block_multidot(const float2* V, int n, int ncols, const float2* w, BatchWorkspace& B, double2* h,
                     cudaStream_t s) {
-  multidot_block_kernel<<<dim3(kBDotBlocks, ncols), kBDotThreads, 0, s>>>(V, n, w, B.partial);
-  reduce_block_partials_kernel<<<(ncols * NR * 32 + 255) / 256, 256, 0, s>>>(B.partial, kBDotBlocks, ncols * NR, h);
+  launch_pdl(multidot_block_kernel, dim3(kBDotBlocks, ncols), kBDotThreads, 0, s, V, n, w, B.partial);
+  launch_pdl(reduce_block_partials_kernel, (ncols * NR * 32 + 255) / 256, 256, 0, s, B.partial, kBDotBlocks, ncols * NR, h);
 }
 
 using cdh = std::complex<double>;
@@ -542,7 +554,7 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<
   }
   cudaMemsetAsync(B.dx, 0, blk * sizeof(float2), s);
   if (!any) return cudaStreamSynchronize(s);
-  scale_block_kernel<<<grid_n((long long)blk), 256, 0, s>>>(B.rhs, B.V, B.nrm, n);
+  launch_pdl(scale_block_kernel, grid_n((long long)blk), 256, 0, s, B.rhs, B.V, B.nrm, n);
   if ((e = dev_matvec_f32_batch(d, B.V, B.w, s)) != cudaSuccess) return e;
   ++applies;
   double2* hp = B.pinned;
@@ -552,11 +564,11 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<
   for (int k = 0; k < m; ++k) {
     const float2* Vk = B.V;
     block_multidot(Vk, n, k + 1, B.w, B, B.h, s);
-    multi_axpy_block_kernel<<<grid_n((long long)blk), 256, 0, s>>>(B.w, B.V, n, k + 1, B.h, -1.f);
+    launch_pdl(multi_axpy_block_kernel, grid_n((long long)blk), 256, 0, s, B.w, B.V, n, k + 1, B.h, -1.f);
     block_multidot(Vk, n, k + 1, B.w, B, B.h2, s);
-    multi_axpy_block_kernel<<<grid_n((long long)blk), 256, 0, s>>>(B.w, B.V, n, k + 1, B.h2, -1.f);
+    launch_pdl(multi_axpy_block_kernel, grid_n((long long)blk), 256, 0, s, B.w, B.V, n, k + 1, B.h2, -1.f);
     block_multidot(B.w, n, 1, B.w, B, B.nrm, s);
-    scale_block_kernel<<<grid_n((long long)blk), 256, 0, s>>>(B.w, B.V + (size_t)(k + 1) * blk, B.nrm, n);
+    launch_pdl(scale_block_kernel, grid_n((long long)blk), 256, 0, s, B.w, B.V + (size_t)(k + 1) * blk, B.nrm, n);
     cudaMemcpyAsync(hp, B.h, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hp2, B.h2, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(np, B.nrm, (size_t)NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
@@ -613,7 +625,7 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<
   }
   if (kmax > 0) {
     cudaMemcpyAsync(B.h, y.data(), y.size() * sizeof(double2), cudaMemcpyHostToDevice, s);
-    multi_axpy_block_kernel<<<grid_n((long long)blk), 256, 0, s>>>(B.dx, B.V, n, kmax, B.h, 1.f);
+    launch_pdl(multi_axpy_block_kernel, grid_n((long long)blk), 256, 0, s, B.dx, B.V, n, kmax, B.h, 1.f);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return cudaStreamSynchronize(s);
@@ -633,9 +645,9 @@ cudaError_t dev_matvec_f32_batch(DevOperator& d, const float2* x, float2* y, cud
   launch_block<1>(d.m2l32, (const float2*)B.S, B.P, s, d.device);
   for (auto& ph : d.down32) launch_block<2>(ph, (const float2*)B.P, B.P, s, d.device);
   const int NS = kBatchNearSources;
-  near_gemm_block_kernel<<<(d.n_leaves + NS - 1) / NS, 352, (size_t)NS * d.rank * NR * sizeof(float2), s>>>(
+  launch_pdl(near_gemm_block_kernel, (d.n_leaves + NS - 1) / NS, 352, (size_t)NS * d.rank * NR * sizeof(float2), s, 
       d.n_leaves, d.rank, d.nearB32, B.S, B.Z);
-  near_gather_block_kernel<<<(int)(((long long)d.N * NR + 255) / 256), 256, 0, s>>>(d.N, d.rank, B.Z, d.kq32,
+  launch_pdl(near_gather_block_kernel, (int)(((long long)d.N * NR + 255) / 256), 256, 0, s, d.N, d.rank, B.Z, d.kq32,
                                                                                    d.colleague, B.S, B.P, y,
                                                                                    d.find_phi);
   return cudaGetLastError();
@@ -677,17 +689,17 @@ cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, do
         rs[j].tol = rs[j].done ? 0.0 : std::max(tol / std::max(rel[j], 1e-300), 1e-6);
         rs[j].bnorm = rs[j].done ? 1.0 : std::max(rel[j] * bn[j], 1e-300);
       }
-      pack_block_kernel<<<grid_n((long long)n * NR), 256, 0, s>>>(B.res, B.rhs, n, active);
+      launch_pdl(pack_block_kernel, grid_n((long long)n * NR), 256, 0, s, B.res, B.rhs, n, active);
       int applies = 0;
       if ((e = block_arnoldi(d, B, inner, rs, applies)) != cudaSuccess) return e;
       n_matvec += applies;
-      unpack_add_block_kernel<<<grid_n((long long)n * nb), 256, 0, s>>>(xb, B.dx, n, nb, active);
+      launch_pdl(unpack_add_block_kernel, grid_n((long long)n * nb), 256, 0, s, xb, B.dx, n, nb, active);
       // FP64 residuals of the active columns.
       for (int j = 0; j < nb; ++j) {
         if (!((active >> j) & 1u)) continue;
         if ((e = dev_matvec(d, xb + (size_t)j * n, B.tmp, s, false)) != cudaSuccess) return e;
         ++n_matvec;
-        sub64_kernel<<<grid_n(n), 256, 0, s>>>(bb + (size_t)j * n, B.tmp, B.res + (size_t)j * n, n);
+        launch_pdl(sub64_kernel, grid_n(n), 256, 0, s, bb + (size_t)j * n, B.tmp, B.res + (size_t)j * n, n);
       }
       double rn2[NR] = {};
       if ((e = colnorms(B.res, n, nb, B, s, rn2)) != cudaSuccess) return e;

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "device.h"
+#include "launch.h"
 
 namespace lsg {
 
@@ -162,6 +163,7 @@ template <class T>
 __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restrict__ V, long long ldv, int ncols,
                                                                const T* __restrict__ w, int n,
                                                                double2* __restrict__ partial) {
+  pdl_enter();
   using R = typename Cx<T>::R;
   __shared__ T red[kDotThreads / 32][kDotCols];
   const int chunk = (n + gridDim.x - 1) / gridDim.x;
@@ -235,6 +237,7 @@ __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restri
 // over the partials, then a fixed shuffle tree (deterministic).
 __global__ void reduce_partials_kernel(const double2* __restrict__ partial, int nb, int ncols,
                                        double2* __restrict__ out) {
+  pdl_enter();
   const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (col >= ncols) return;
@@ -257,6 +260,7 @@ template <class T>
 __global__ void __launch_bounds__(256) multi_axpy_kernel(T* __restrict__ w, const T* __restrict__ V, long long ldv,
                                                          int ncols, const double2* __restrict__ h, int n,
                                                          double sign) {
+  pdl_enter();
   using R = typename Cx<T>::R;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     R sr = R(0), si = R(0);
@@ -291,6 +295,7 @@ __global__ void __launch_bounds__(256) multi_axpy_kernel(T* __restrict__ w, cons
 
 template <class T>
 __global__ void scale_kernel(const T* __restrict__ a, T* __restrict__ b, double s, int n) {
+  pdl_enter();
   using R = typename Cx<T>::R;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     b[i] = Cx<T>::make(a[i].x * (R)s, a[i].y * (R)s);
@@ -301,6 +306,7 @@ __global__ void scale_kernel(const T* __restrict__ a, T* __restrict__ b, double 
 template <class T>
 __global__ void scale_by_norm_kernel(const T* __restrict__ a, T* __restrict__ b, const double2* __restrict__ nrm,
                                      int n) {
+  pdl_enter();
   using R = typename Cx<T>::R;
   __shared__ R f;  // formed once per thread block (FP64 divides are slow on GB300)
   if (threadIdx.x == 0) {
@@ -315,17 +321,20 @@ __global__ void scale_by_norm_kernel(const T* __restrict__ a, T* __restrict__ b,
 
 template <class T>
 __global__ void sub_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ c, int n) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     c[i] = Cx<T>::make(a[i].x - b[i].x, a[i].y - b[i].y);
 }
 
 __global__ void to_f32_kernel(const double2* __restrict__ a, float2* __restrict__ b, int n) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     b[i] = make_float2((float)a[i].x, (float)a[i].y);
 }
 
 // a += b, with b widened to FP64
 __global__ void add_f32_kernel(double2* __restrict__ a, const float2* __restrict__ b, int n) {
+  pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     a[i].x += (double)b[i].x;
     a[i].y += (double)b[i].y;
@@ -340,9 +349,9 @@ int grid_for(int n) { return std::min((n + 255) / 256, 152 * 8); }
 template <class T>
 void multidot(const T* V, long long ldv, int ncols, const T* w, int n, double2* partial, double2* h_dev,
               cudaStream_t s) {
-  multidot_kernel<T><<<dim3(kDotBlocks, (ncols + kDotCols - 1) / kDotCols), kDotThreads, 0, s>>>(V, ldv, ncols, w, n,
+  launch_pdl(multidot_kernel<T>, dim3(kDotBlocks, (ncols + kDotCols - 1) / kDotCols), kDotThreads, 0, s, V, ldv, ncols, w, n,
                                                                                                  partial);
-  reduce_partials_kernel<<<(ncols * 32 + 255) / 256, 256, 0, s>>>(partial, kDotBlocks, ncols, h_dev);
+  launch_pdl(reduce_partials_kernel, (ncols * 32 + 255) / 256, 256, 0, s, partial, kDotBlocks, ncols, h_dev);
 }
 
 template <class T>
@@ -382,7 +391,7 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
   // r = b - A x0
   if (x0) {
     if ((e = apply(d, x0, B.w, s)) != cudaSuccess) return e;
-    sub_kernel<T><<<grid_for(n), 256, 0, s>>>(b, B.w, B.r, n);
+    launch_pdl(sub_kernel<T>, grid_for(n), 256, 0, s, b, B.w, B.r, n);
   } else {
     cudaMemcpyAsync(B.r, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, s);
   }
@@ -399,7 +408,7 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
     converged = true;
     return cudaStreamSynchronize(s);
   }
-  scale_kernel<T><<<grid_for(n), 256, 0, s>>>(B.r, B.V, 1.0 / beta, n);
+  launch_pdl(scale_kernel<T>, grid_for(n), 256, 0, s, B.r, B.V, 1.0 / beta, n);
   std::vector<std::vector<cdh>> H;  // columns, already rotated
   std::vector<cdh> cs, sn, g(1, cdh(beta, 0.0));
   int K = 0;
@@ -414,11 +423,11 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
   for (int k = 0; k < m; ++k) {
     // CGS2, both passes and the norm on the device; one copy back per step.
     multidot(B.V, n, k + 1, B.w, n, ws.partial, ws.h, s);
-    multi_axpy_kernel<T><<<grid_for(n), 256, 0, s>>>(B.w, B.V, n, k + 1, ws.h, n, -1.0);
+    launch_pdl(multi_axpy_kernel<T>, grid_for(n), 256, 0, s, B.w, B.V, n, k + 1, ws.h, n, -1.0);
     multidot(B.V, n, k + 1, B.w, n, ws.partial, ws.h2, s);
-    multi_axpy_kernel<T><<<grid_for(n), 256, 0, s>>>(B.w, B.V, n, k + 1, ws.h2, n, -1.0);
+    launch_pdl(multi_axpy_kernel<T>, grid_for(n), 256, 0, s, B.w, B.V, n, k + 1, ws.h2, n, -1.0);
     multidot(B.w, n, 1, B.w, n, ws.partial, ws.nrm, s);
-    scale_by_norm_kernel<T><<<grid_for(n), 256, 0, s>>>(B.w, B.V + (size_t)(k + 1) * n, ws.nrm, n);
+    launch_pdl(scale_by_norm_kernel<T>, grid_for(n), 256, 0, s, B.w, B.V + (size_t)(k + 1) * n, ws.nrm, n);
     cudaMemcpyAsync(hp, ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hp2, ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(np, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
@@ -469,7 +478,7 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
   } else {
     cudaMemsetAsync(x, 0, (size_t)n * sizeof(T), s);
   }
-  multi_axpy_kernel<T><<<grid_for(n), 256, 0, s>>>(x, B.V, n, K, ws.h, n, 1.0);
+  launch_pdl(multi_axpy_kernel<T>, grid_for(n), 256, 0, s, x, B.V, n, K, ws.h, n, 1.0);
   iters = K;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return cudaStreamSynchronize(s);
@@ -498,7 +507,7 @@ cudaError_t dev_gmres(DevOperator& d, const double2* b, double2* x, int max_iter
     return e;
   // True residual with the FP64 operator (the reference's "Err in GMRES").
   if ((e = dev_matvec(d, x, ws.b64.w, d.stream, false)) != cudaSuccess) return e;
-  sub_kernel<double2><<<grid_for(d.N), 256, 0, d.stream>>>(b, ws.b64.w, ws.b64.r, d.N);
+  launch_pdl(sub_kernel<double2>, grid_for(d.N), 256, 0, d.stream, b, ws.b64.w, ws.b64.r, d.N);
   double rn = 0.0;
   if ((e = vnorm(ws.b64.r, d.N, ws, d.stream, rn)) != cudaSuccess) return e;
   res.iters = it;
@@ -550,15 +559,15 @@ cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int ma
     bool conv = false;
     // Inner solve to roughly the FP32 operator accuracy.
     const double inner_tol = std::max(tol / std::max(relres, 1e-300), 1e-6);
-    to_f32_kernel<<<grid_for(n), 256, 0, d.stream>>>(r, ws.res32, n);
+    launch_pdl(to_f32_kernel, grid_for(n), 256, 0, d.stream, r, ws.res32, n);
     if ((e = arnoldi_cycle<float2>(d, ws, ws.res32, nullptr, ws.dx32, inner, inner_tol, 1e-300,
                                    std::max(relres * bn, 1e-300), nullptr, it, conv)) != cudaSuccess)
       return e;
     n_matvec += it;
-    add_f32_kernel<<<grid_for(n), 256, 0, d.stream>>>(x, ws.dx32, n);
+    launch_pdl(add_f32_kernel, grid_for(n), 256, 0, d.stream, x, ws.dx32, n);
     if ((e = dev_matvec(d, x, ws.b64.w, d.stream, false)) != cudaSuccess) return e;
     ++n_matvec;
-    sub_kernel<double2><<<grid_for(n), 256, 0, d.stream>>>(b, ws.b64.w, r, n);
+    launch_pdl(sub_kernel<double2>, grid_for(n), 256, 0, d.stream, b, ws.b64.w, r, n);
     double rn = 0.0;
     if ((e = vnorm(r, n, ws, d.stream, rn)) != cudaSuccess) return e;
     relres = rn / bn;

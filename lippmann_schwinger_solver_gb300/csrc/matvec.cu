@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "device.h"
+#include "launch.h"
 
 namespace lsg {
 
@@ -52,6 +53,7 @@ __global__ void __launch_bounds__(256, 3) gemv_tiles_kernel(const GemvTile* __re
                                                             const int* __restrict__ out, const int* __restrict__ qlen,
                                                             const C* __restrict__ src, C* __restrict__ dst,
                                                             int accumulate) {
+  pdl_enter();
   using R = typename Real<C>::T;
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -149,6 +151,7 @@ __global__ void __launch_bounds__(256) near_kernel(int n_out, int rank, const C*
 __global__ void __launch_bounds__(256) near_coeff_kernel(int n_leaves, int rank, int nb, const double* __restrict__ Qp,
                                                          const double2* __restrict__ x, double2* __restrict__ c,
                                                          float2* __restrict__ x32) {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = n_leaves * rank;
   for (int i = t; i < n; i += gridDim.x * blockDim.x) {
@@ -180,6 +183,7 @@ __global__ void __launch_bounds__(256, 4) near_factored_kernel(int n_out, int ra
                                                             const double2* __restrict__ x,
                                                             const double2* __restrict__ P, double2* __restrict__ y,
                                                             int find_phi) {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out) return;
   const int leaf = t / rank, row = t - leaf * rank;
@@ -233,6 +237,7 @@ constexpr int kNearSources32 = 8;
 
 __global__ void __launch_bounds__(576, 1) near_gemm32_kernel(int n_leaves, int rank, const float2* __restrict__ BT,
                                                           const float2* __restrict__ x, float2* __restrict__ Z) {
+  pdl_enter();
   constexpr int NS = kNearSources32;
   extern __shared__ float2 sx32[];  // [j][k]
   const int s0 = blockIdx.x * NS;
@@ -277,6 +282,7 @@ __global__ void __launch_bounds__(256) near_gather32_kernel(int n_out, int rank,
                                                             const float2* __restrict__ x,
                                                             const float2* __restrict__ P, Y* __restrict__ y,
                                                             int find_phi) {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out) return;
   const int leaf = t / rank, row = t - leaf * rank;
@@ -309,6 +315,25 @@ __global__ void near_transpose32_kernel(const double2* __restrict__ B, float2* _
   }
 }
 
+// First kernel of a matvec: S[0:n) = x (converted to the operator's type)
+// and P = 0.
+__device__ __forceinline__ double2 conv(double2 v, double2*) { return v; }
+__device__ __forceinline__ float2 conv(double2 v, float2*) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ float2 conv(float2 v, float2*) { return v; }
+
+template <class X, class C>
+__global__ void load_zero_kernel(const X* __restrict__ x, C* __restrict__ S, long long n, C* __restrict__ P,
+                                 long long np) {
+  pdl_enter();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
+    S[i] = conv(x[i], (C*)nullptr);
+  C z;
+  z.x = 0;
+  z.y = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += stride) P[i] = z;
+}
+
 __global__ void d2f_kernel(const double2* __restrict__ a, float2* __restrict__ b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     b[i] = make_float2((float)a[i].x, (float)a[i].y);
@@ -334,8 +359,8 @@ static void launch_gemv(const DevPhase<C>& ph, const C* src, C* dst, cudaStream_
   const int warps_per_block = 8;
   int blocks = (ph.n_tiles + warps_per_block - 1) / warps_per_block;
   blocks = std::min(blocks, sm_count(dev) * 8);
-  gemv_tiles_kernel<C, PHASE><<<blocks, 256, 0, s>>>(ph.tiles, ph.n_tiles, ph.A, ph.idx, ph.out, ph.klen, src, dst,
-                                                     ph.accumulate);
+  launch_pdl(gemv_tiles_kernel<C, PHASE>, blocks, 256, 0, s, ph.tiles, ph.n_tiles, ph.A, ph.idx, ph.out, ph.klen,
+             src, dst, ph.accumulate);
 }
 
 template <class T>
@@ -513,49 +538,49 @@ bool dev_enable_f32(DevOperator& d, std::string& err) {
 cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
   if (d.f64_kernels == LS_F64_DOUBLE_FLOAT) return dev_matvec_df(d, x, y, s, mark_m2l);
   if (!s) s = d.stream;
-  cudaMemcpyAsync(d.S, x, (size_t)d.N * sizeof(double2), cudaMemcpyDeviceToDevice, s);
-  cudaMemsetAsync(d.P, 0, (size_t)d.pots_len * sizeof(double2), s);
+  launch_pdl(load_zero_kernel<double2, double2>, (unsigned)sm_count(d.device) * 4, 256, 0, s, x, d.S, (long long)d.N,
+             d.P, d.pots_len);
   for (auto& ph : d.up) launch_gemv<0>(ph, (const double2*)d.S, d.S, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[0], s);
   launch_gemv<1>(d.m2l, (const double2*)d.S, d.P, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down) launch_gemv<2>(ph, (const double2*)d.P, d.P, s, d.device);
-  near_coeff_kernel<<<(d.n_leaves * d.n_bases + 255) / 256, 256, 0, s>>>(d.n_leaves, d.rank, d.n_bases, d.Qp, d.S,
-                                                                         d.cbuf, d.x32);
-  near_factored_kernel<<<(d.N + 255) / 256, 256, 0, s>>>(d.N, d.rank, d.n_bases, d.nearVt, d.nearE, d.kq,
-                                                         d.colleague, d.cbuf, d.x32, d.S, d.P, y, d.find_phi);
+  launch_pdl(near_coeff_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
+             d.n_bases, d.Qp, d.S, d.cbuf, d.x32);
+  launch_pdl(near_factored_kernel, (unsigned)((d.N + 255) / 256), 256, 0, s, d.N, d.rank, d.n_bases, d.nearVt,
+             d.nearE, d.kq, d.colleague, d.cbuf, d.x32, d.S, d.P, y, d.find_phi);
   return cudaGetLastError();
 }
 
 // Phases of the FP32 operator after x has been placed in S32.
 template <class Y>
 static cudaError_t f32_phases(DevOperator& d, Y* y, cudaStream_t s, bool mark_m2l) {
-  cudaMemsetAsync(d.P32, 0, (size_t)d.pots_len * sizeof(float2), s);
   for (auto& ph : d.up32) launch_gemv<0>(ph, (const float2*)d.S32, d.S32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[2], s);
   launch_gemv<1>(d.m2l32, (const float2*)d.S32, d.P32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[3], s);
   for (auto& ph : d.down32) launch_gemv<2>(ph, (const float2*)d.P32, d.P32, s, d.device);
   const int nthr = (9 * d.rank + 31) / 32 * 32;
-  near_gemm32_kernel<<<(d.n_leaves + kNearSources32 - 1) / kNearSources32, nthr,
-                       (size_t)kNearSources32 * d.rank * sizeof(float2), s>>>(d.n_leaves, d.rank, d.nearB32, d.S32,
-                                                                              d.Z32);
-  near_gather32_kernel<Y><<<(d.N + 255) / 256, 256, 0, s>>>(d.N, d.rank, d.Z32, d.kq32, d.colleague, d.S32, d.P32, y,
-                                                            d.find_phi);
+  launch_pdl(near_gemm32_kernel, (unsigned)((d.n_leaves + kNearSources32 - 1) / kNearSources32), (unsigned)nthr,
+             (size_t)kNearSources32 * d.rank * sizeof(float2), s, d.n_leaves, d.rank, d.nearB32, d.S32, d.Z32);
+  launch_pdl(near_gather32_kernel<Y>, (unsigned)((d.N + 255) / 256), 256, 0, s, d.N, d.rank, d.Z32, d.kq32,
+             d.colleague, d.S32, d.P32, y, d.find_phi);
   return cudaGetLastError();
 }
 
 cudaError_t dev_matvec_f32(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
   if (!d.has_f32) return cudaErrorInvalidValue;
   if (!s) s = d.stream;
-  d2f_kernel<<<256, 256, 0, s>>>(x, d.S32, d.N);
+  launch_pdl(load_zero_kernel<double2, float2>, (unsigned)sm_count(d.device) * 4, 256, 0, s, x, d.S32,
+             (long long)d.N, d.P32, d.pots_len);
   return f32_phases(d, y, s, mark_m2l);
 }
 
 cudaError_t dev_matvec_f32v(DevOperator& d, const float2* x, float2* y, cudaStream_t s) {
   if (!d.has_f32) return cudaErrorInvalidValue;
   if (!s) s = d.stream;
-  cudaMemcpyAsync(d.S32, x, (size_t)d.N * sizeof(float2), cudaMemcpyDeviceToDevice, s);
+  launch_pdl(load_zero_kernel<float2, float2>, (unsigned)sm_count(d.device) * 4, 256, 0, s, x, d.S32,
+             (long long)d.N, d.P32, d.pots_len);
   return f32_phases(d, y, s, false);
 }
 

@@ -30,6 +30,7 @@
 #include <string>
 
 #include "device.h"
+#include "launch.h"
 
 namespace lsg {
 namespace {
@@ -94,6 +95,16 @@ __global__ void split_kernel(const double2* __restrict__ a, float4* __restrict__
     b[i] = split(a[i]);
 }
 
+// First kernel of a matvec: S[0:n) = split(x) and P = 0.
+__global__ void split_zero_kernel(const double2* __restrict__ x, float4* __restrict__ S, long long n,
+                                  float4* __restrict__ P, long long np) {
+  pdl_enter();
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) S[i] = split(x[i]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += stride)
+    P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 __global__ void split_real_kernel(const double* __restrict__ a, float2* __restrict__ b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float h = __double2float_rn(a[i]);
@@ -108,6 +119,7 @@ __global__ void __launch_bounds__(256, 3) gemv_df_kernel(const GemvTile* __restr
                                                          const int* __restrict__ out, const int* __restrict__ qlen,
                                                          const float4* __restrict__ src, float4* __restrict__ dst,
                                                          int accumulate) {
+  pdl_enter();
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_tiles; w += nw) {
@@ -152,6 +164,7 @@ __global__ void __launch_bounds__(256) near_coeff_df_kernel(int n_leaves, int ra
                                                             const float2* __restrict__ Qp,
                                                             const float4* __restrict__ x, float4* __restrict__ c,
                                                             float2* __restrict__ x32) {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = n_leaves * rank;
   for (int i = t; i < n; i += gridDim.x * blockDim.x) {
@@ -196,6 +209,7 @@ __global__ void __launch_bounds__(kNearThreads, kNearMinBlocks) near_gemm_df_ker
                                                            const float4* __restrict__ c,
                                                            const float2* __restrict__ x32,
                                                            float4* __restrict__ Z, float2* __restrict__ ZE) {
+  pdl_enter();
   constexpr int NS = kNearSources;
   extern __shared__ float4 sc[];                    // [j][l]: c of source j
   float2* sx = reinterpret_cast<float2*>(sc + NS * nb);  // [j][k]: x32 of source j
@@ -256,6 +270,7 @@ __global__ void __launch_bounds__(256) near_gather_df_kernel(int n_out, int rank
                                                              const double2* __restrict__ x,
                                                              const float4* __restrict__ P,
                                                              double2* __restrict__ y, int find_phi) {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_out) return;
   const int leaf = t / rank, row = t - leaf * rank;
@@ -300,8 +315,8 @@ void launch_df(const DevPhase<float4>& ph, const float4* src, float4* dst, cudaS
   if (ph.n_tiles == 0) return;
   int blocks = (ph.n_tiles + 7) / 8;
   blocks = std::min(blocks, sms(dev) * 8);
-  gemv_df_kernel<PHASE><<<blocks, 256, 0, s>>>(ph.tiles, ph.n_tiles, ph.A, ph.idx, ph.out, ph.klen, src, dst,
-                                               ph.accumulate);
+  launch_pdl(gemv_df_kernel<PHASE>, blocks, 256, 0, s, ph.tiles, ph.n_tiles, ph.A, ph.idx, ph.out, ph.klen, src,
+             dst, ph.accumulate);
 }
 
 template <class T>
@@ -377,21 +392,21 @@ cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStre
   if (!d.has_df) return cudaErrorInvalidValue;
   if (!s) s = d.stream;
   const int n = d.N;
-  split_kernel<<<std::min((n + 255) / 256, sms(d.device) * 4), 256, 0, s>>>(x, d.S_df, n);
-  cudaMemsetAsync(d.P_df, 0, (size_t)d.pots_len * sizeof(float4), s);
+  launch_pdl(split_zero_kernel, (unsigned)sms(d.device) * 4, 256, 0, s, x, d.S_df, (long long)n, d.P_df,
+             d.pots_len);
   for (auto& ph : d.up_df) launch_df<0>(ph, (const float4*)d.S_df, d.S_df, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[0], s);
   launch_df<1>(d.m2l_df, (const float4*)d.S_df, d.P_df, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down_df) launch_df<2>(ph, (const float4*)d.P_df, d.P_df, s, d.device);
-  near_coeff_df_kernel<<<(d.n_leaves * d.n_bases + 255) / 256, 256, 0, s>>>(d.n_leaves, d.rank, d.n_bases, d.Qp_df,
-                                                                            d.S_df, d.c_df, d.x32);
+  launch_pdl(near_coeff_df_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
+             d.n_bases, d.Qp_df, d.S_df, d.c_df, d.x32);
   {
     const size_t smem = (size_t)kNearSources * (d.n_bases * sizeof(float4) + d.rank * sizeof(float2));
-    near_gemm_df_kernel<<<(d.n_leaves + kNearSources - 1) / kNearSources, kNearThreads, smem, s>>>(
-        d.n_leaves, d.rank, d.n_bases, d.Vt_df, d.nearE, d.c_df, d.x32, d.Z_df, d.ZE_df);
-    near_gather_df_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, d.rank, d.Z_df, d.ZE_df, d.kq, d.colleague, x, d.P_df,
-                                                          y, d.find_phi);
+    launch_pdl(near_gemm_df_kernel, (unsigned)((d.n_leaves + kNearSources - 1) / kNearSources), kNearThreads, smem, s,
+               d.n_leaves, d.rank, d.n_bases, d.Vt_df, d.nearE, d.c_df, d.x32, d.Z_df, d.ZE_df);
+    launch_pdl(near_gather_df_kernel, (unsigned)((n + 255) / 256), 256, 0, s, n, d.rank, d.Z_df, d.ZE_df, d.kq,
+               d.colleague, x, d.P_df, y, d.find_phi);
   }
   return cudaGetLastError();
 }
