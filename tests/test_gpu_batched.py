@@ -8,7 +8,7 @@ difference bound 1e-5 written below).
 import numpy as np
 import pytest
 
-from conftest import CFG_C1, CFG_HFR, full_cfg
+from conftest import CFG_C1, CFG_HFR, CFG_L3_K10, full_cfg
 
 pytestmark = pytest.mark.gpu
 
@@ -17,9 +17,9 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("base,kernels", [(CFG_C1, 0), (CFG_HFR, 1)])
-def test_batched_solve_matches_single_solves(ls, base, kernels):
-    op = ls.Operator(full_cfg(base), device=0)
+@pytest.mark.parametrize("base,over,kernels", [(CFG_C1, {}, 0), (CFG_HFR, {}, 1), (CFG_L3_K10, {"nChebNodes": 8}, 1)])
+def test_batched_solve_matches_single_solves(ls, base, over, kernels):
+    op = ls.Operator(full_cfg(base, **over), device=0)
     op.enable_f32()
     op.set_f64_kernels(kernels)
     thetas = np.linspace(0.0, 2 * np.pi, 11, endpoint=False)  # one full block of 8 and a partial one

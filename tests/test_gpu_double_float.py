@@ -39,6 +39,7 @@ def _x(n, seed):
         (CFG_C1, {"findPhi": 0}),
         (CFG_HFR, {}),
         (CFG_BUMPS, {}),
+        (CFG_L3_K10, {"nChebNodes": 8}),
     ],
 )
 def test_double_float_matches_oracle_and_native(ls, ora, base, over):

@@ -3,7 +3,7 @@ refinement around it (mixed-precision configuration)."""
 import numpy as np
 import pytest
 
-from conftest import CFG_BUMPS, CFG_C1, full_cfg
+from conftest import CFG_BUMPS, CFG_C1, CFG_L3_K10, full_cfg
 
 pytestmark = pytest.mark.gpu
 
@@ -12,9 +12,10 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def test_f32_matvec_error_is_single_precision(ls, ora):
+@pytest.mark.parametrize("base,over", [(CFG_BUMPS, {}), (CFG_L3_K10, {"nChebNodes": 8})])
+def test_f32_matvec_error_is_single_precision(ls, ora, base, over):
     torch = pytest.importorskip("torch")
-    cfg = full_cfg(CFG_BUMPS)
+    cfg = full_cfg(base, **over)
     op = ls.Operator(cfg, device=0)
     op.enable_f32()
     x = np.random.default_rng(4).uniform(-1, 1, op.N) + 1j * np.random.default_rng(5).uniform(-1, 1, op.N)

@@ -34,6 +34,7 @@ def _x(n, seed):
         (CFG_BUMPS, {}),
         (CFG_L3_K10, {"Qchoice": 2}),
         (CFG_L3_K10, {"Qchoice": 5, "nChebNodes": 5, "degreeOfBases": 5}),
+        (CFG_L3_K10, {"nChebNodes": 8}),  # rank 64: the largest leaf, near-field GEMMs loop over 576 outputs
     ],
 )
 def test_matvec_matches_oracle(ls, ora, base, over):
