@@ -12,6 +12,8 @@
 // -llsdafmm. Errors throw ls::Error carrying the C ABI status and message.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <complex>
 #include <stdexcept>
 #include <string>
@@ -118,6 +120,45 @@ class DFMM {
     Vec b(N);
     check(ls_op_rhs(op, reinterpret_cast<double*>(b.data())), "ls_op_rhs");
     return b;
+  }
+
+  // Kernels behind the FP64 products (LS_F64_NATIVE or LS_F64_DOUBLE_FLOAT).
+  void setF64Kernels(int kernels) { check(ls_op_set_f64_kernels(op, kernels), "ls_op_set_f64_kernels"); }
+
+  // Right-hand sides for plane waves from the directions thetas (radians):
+  // -kappa^2 q(x) exp(i kappa (x1 cos t + x2 sin t)); t = 0 is RHS().
+  std::vector<Vec> RHSAngles(const std::vector<double>& thetas) const {
+    std::vector<double> q(N);
+    check(ls_op_contrast(op, q.data()), "ls_op_contrast");
+    std::vector<Vec> out;
+    const double k = kernel.kappa;
+    for (double t : thetas) {
+      Vec b(N);
+      for (int i = 0; i < N; ++i) {
+        const double ph = k * (gridPoints[i].x * std::cos(t) + gridPoints[i].y * std::sin(t));
+        b[i] = -k * k * q[i] * std::exp(std::complex<double>(0.0, ph));
+      }
+      out.push_back(std::move(b));
+    }
+    return out;
+  }
+
+  // Solves for all right-hand sides together (mixed precision, FP64 residual
+  // per column). Returns the number of FP32 block applies plus FP64 products.
+  int SolveBatched(const std::vector<Vec>& B, std::vector<Vec>& X, double tol = 1e-8, int max_outer = 20,
+                   int inner = 100) {
+    check(ls_op_enable_f32(op), "ls_op_enable_f32");
+    const int nrhs = (int)B.size();
+    std::vector<std::complex<double>> flatB((size_t)N * nrhs), flatX((size_t)N * nrhs);
+    for (int j = 0; j < nrhs; ++j) std::copy(B[j].begin(), B[j].end(), flatB.begin() + (size_t)j * N);
+    int nmv = 0;
+    std::vector<double> rr(nrhs);
+    check(ls_gmres_mixed_batched(op, nrhs, reinterpret_cast<const double*>(flatB.data()), max_outer, inner, tol,
+                                 reinterpret_cast<double*>(flatX.data()), &nmv, rr.data()),
+          "ls_gmres_mixed_batched");
+    X.assign(nrhs, Vec(N));
+    for (int j = 0; j < nrhs; ++j) std::copy(flatX.begin() + (size_t)j * N, flatX.begin() + (size_t)(j + 1) * N, X[j].begin());
+    return nmv;
   }
 };
 

@@ -1,8 +1,11 @@
 // Reference-style driver through the C++ facade: the same steps as
 // GMRES/GMRES.cpp main (build the operator, b = RHS, GMRES, report the
-// residual of the solution with one more matvec). Prints one JSON line.
+// residual of the solution with one more matvec), then ten incidence
+// directions solved together and the double-float kernels behind the same
+// product. Prints one JSON line.
 //
 //   gmres_driver <nLevelsUniform> <kappa> <TOL_POW> <Qchoice>
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -42,9 +45,36 @@ int main(int argc, char** argv) {
       dx += std::norm(x[i] - xr[i]);
       xn += std::norm(x[i]);
     }
+    // Several incidence directions at once, each checked with one FP64 product.
+    std::vector<double> thetas;
+    for (int m = 0; m < 10; ++m) thetas.push_back(2.0 * 3.141592653589793 * m / 10.0);
+    std::vector<ls::Vec> Bs = S.RHSAngles(thetas), Xs;
+    const int nmv = S.SolveBatched(Bs, Xs, 1e-8);
+    double worst = 0.0;
+    for (size_t j = 0; j < Bs.size(); ++j) {
+      ls::Vec Ax2;
+      S.MatVecProduct(Xs[j], Ax2);
+      double rj = 0.0, bj = 0.0;
+      for (int i = 0; i < S.N; ++i) {
+        rj += std::norm(Bs[j][i] - Ax2[i]);
+        bj += std::norm(Bs[j][i]);
+      }
+      worst = std::max(worst, std::sqrt(rj / bj));
+    }
+    // The double-float kernels behind MatVecProduct.
+    S.setF64Kernels(LS_F64_DOUBLE_FLOAT);
+    ls::Vec Axd;
+    S.MatVecProduct(x, Axd);
+    S.setF64Kernels(LS_F64_NATIVE);
+    double dd = 0.0, an = 0.0;
+    for (int i = 0; i < S.N; ++i) {
+      dd += std::norm(Axd[i] - Ax[i]);
+      an += std::norm(Ax[i]);
+    }
     std::printf("{\"N\": %d, \"iters\": %d, \"estimate\": %.3e, \"residual\": %.3e, \"restarted_vs_tol\": %.3e, "
+                "\"batched_max_residual\": %.3e, \"batched_applies\": %d, \"double_float_vs_native\": %.3e, "
                 "\"assemble_s\": %.3f, \"gmres_s\": %.4f}\n",
-                S.N, it, err, std::sqrt(rn / bn), std::sqrt(dx / xn),
+                S.N, it, err, std::sqrt(rn / bn), std::sqrt(dx / xn), worst, nmv, std::sqrt(dd / an),
                 std::chrono::duration<double>(t1 - t0).count(), std::chrono::duration<double>(t2 - t1).count());
   } catch (const ls::Error& e) {
     std::fprintf(stderr, "error %d: %s\n", e.status, e.what());

@@ -18,3 +18,6 @@ def test_reference_style_cpp_driver(ls):
     assert r["estimate"] <= 1e-10
     assert r["residual"] <= 2e-10
     assert r["restarted_vs_tol"] <= 1e-6
+    assert r["batched_max_residual"] <= 1.5e-8
+    assert r["batched_applies"] > 0
+    assert r["double_float_vs_native"] <= 2e-11
