@@ -44,6 +44,16 @@ def input_vector(n):
     return rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
 
 
+def traffic_per_launch(kernels):
+    """DRAM bytes of one M2L launch at the benchmark size, from the ncu capture
+    summarised in profiles/ (None when absent)."""
+    tp = os.path.join(ROOT, "profiles", "m2l_traffic.json")
+    if not os.path.exists(tp):
+        return None
+    with open(tp) as f:
+        return json.load(f).get(kernels, {}).get("bytes_per_launch")
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -273,9 +283,16 @@ def run_ours(args):
     op.matvec_device(xd.data_ptr(), yo.data_ptr(), sp)
     torch.cuda.synchronize()
     y_main = yd.cpu().numpy()
-    alt = {"f64_kernels": "native" if other == ls.LS_F64_NATIVE else "double-float",
+    other_name = "native" if other == ls.LS_F64_NATIVE else "double-float"
+    peak_o, peak_kind_o = load_peaks()
+    achieved_o = info["m2l_bytes"] / (m2l_o * 1e-3) / 1e9
+    alt = {"f64_kernels": other_name,
            "matvec_per_s": 1e3 / ms_o, "ms_per_step": ms_o, "m2l_ms": m2l_o,
-           "m2l_achieved_gbs": info["m2l_bytes"] / (m2l_o * 1e-3) / 1e9,
+           "roofline": {"bound": "hbm", "achieved": achieved_o, "peak": peak_o, "unit": "GB/s",
+                        "frac": achieved_o / peak_o, "traffic": traffic_per_launch(other_name),
+                        "peak_source": peak_kind_o,
+                        "kernel": "gemv_df_kernel<1> (M2L)" if other_name == "double-float"
+                        else "gemv_tiles_kernel<double2, 1> (M2L)"},
            "rel_l2_vs_timed": float(np.linalg.norm(yo.cpu().numpy() - y_main) / np.linalg.norm(y_main))}
     op.set_f64_kernels(ls.LS_F64_DOUBLE_FLOAT if df_kernels else ls.LS_F64_NATIVE)
     # Solve time to a true relative residual of 1e-8: plain FP64 GMRES, and
@@ -321,11 +338,7 @@ def run_ours(args):
                  "speedup_batched_vs_sequential": ts / tb}
     peak, peak_kind = load_peaks()
     achieved = info["m2l_bytes"] / (ms_m2l * 1e-3) / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "m2l_traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            traffic = json.load(f).get(args.f64_kernels, {}).get("bytes_per_launch")
+    traffic = traffic_per_launch(args.f64_kernels)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(ls, cfg, budget_s=args.cpu_budget)
