@@ -942,10 +942,12 @@ static void add_task(GemvPhase& ph, const std::vector<cd>& rowmajor, int rows, i
 // R = 16, 8, ... rows (largest first) so that no rows are padded, except
 // that R never drops below r_min: slices must keep at least 4 columns
 // (R >= 128 / K), and the last tile of a block pads up to r_min. r_max
-// (at most 8) keeps at least ~14,600 tiles per phase (two waves of 48
-// warps on each of 152 SMs): fewer, longer warps leave too few loads in
-// flight to cover HBM latency. Blocks go longest first (stable, so
-// neighbouring blocks keep their order).
+// (at most 8) keeps at least ~7,300 tiles per phase (one wave of 48 warps
+// on each of 152 SMs): fewer, longer warps leave too few loads in flight to
+// cover HBM latency, more and shorter ones spend their time in the slice
+// combination (measured on GB300: 96 warps per SM was 3-8% slower, 32 and
+// 24 slower again, rows up to 16 slower for FP32 and double-float). Blocks
+// go longest first (stable, so neighbouring blocks keep their order).
 static int pow2_ceil(int v) {
   int p = 1;
   while (p < v) p <<= 1;
@@ -962,7 +964,7 @@ static void finalize(GemvPhase& ph) {
     r = e;
   }
   std::stable_sort(blocks.begin(), blocks.end(), [](const Block& a, const Block& b) { return a.K > b.K; });
-  const long long want_tiles = 152LL * 96;
+  const long long want_tiles = 152LL * 48;
   int r_max = 8;
   while (r_max > 1 && (long long)ph.rows.size() < want_tiles * r_max) r_max >>= 1;
   struct T { size_t r0; int rows, S, qmax, K; };

@@ -118,8 +118,8 @@ ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
   o->device_bytes = d.device_bytes;
   o->assemble_seconds = h.assemble_seconds;
   o->max_rank = h.max_rank;
-  // double-float: + the split of x and the near-field gather
-  o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 2 : 0);
+  // double-float: the near field takes a GEMM and a gather kernel
+  o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 1 : 0);
   // M2L: every block once (16 B per complex entry), every source charge of
   // the charge buffer once, every potential it writes once.
   o->m2l_entries = op->on_device ? d.m2l.entries : h.m2l.entries();

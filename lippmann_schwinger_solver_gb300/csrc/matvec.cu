@@ -459,7 +459,7 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
   cudaMemset(d.ybuf, 0, (size_t)h.N * sizeof(double2));
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return false; }
-  int launches = 2;  // near coefficient + near kernels
+  int launches = 3;  // load of x, near coefficients, near field
   for (auto& p : d.up) launches += p.n_tiles > 0;
   launches += d.m2l.n_tiles > 0;
   for (auto& p : d.down) launches += p.n_tiles > 0;
