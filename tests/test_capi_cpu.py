@@ -66,6 +66,15 @@ def test_host_only_operator_refuses_device_calls(ls):
     with pytest.raises(ls.LSError) as ei:
         op.enable_f32()
     assert ei.value.code == ls.LS_E_STATE
+    with pytest.raises(ls.LSError) as ei:
+        op.set_f64_kernels(ls.LS_F64_DOUBLE_FLOAT)
+    assert ei.value.code == ls.LS_E_STATE
+    with pytest.raises(ls.LSError) as ei:  # an unknown kernel choice is rejected first
+        op.set_f64_kernels(5)
+    assert ei.value.code == ls.LS_E_INVALID
+    with pytest.raises(ls.LSError) as ei:
+        op.gmres_mixed_batched(np.zeros((op.N, 3), dtype=np.complex128))
+    assert ei.value.code == ls.LS_E_STATE
     info = op.info
     assert info["far_entries"] > 0 and info["matvec_flops"] > 8 * info["far_entries"]
     assert info["m2l_entries"] <= info["far_entries"]
