@@ -57,7 +57,7 @@ typedef struct {
   int yes2DFMM;            /* 1: directional DAFMM, 0: AFMM (level_LFR = 2) */
   int TOL_POW;             /* NCA tolerance 10^-TOL_POW */
   int degreeOfBases;       /* 6 -> 21 Chebyshev basis polynomials */
-  int nLevelsUniform;      /* depth of the uniform quadtree (2..10) */
+  int nLevelsUniform;      /* depth of the uniform quadtree (3..10) */
   int Qchoice;             /* 0..5 reference contrasts, 6 = Gaussian bumps */
   int findPhi;             /* 1: I + k^2 q G (LS operator); 0: bare G */
   int reference_rounding;  /* 1: M and near blocks rounded to 6 significant

@@ -45,6 +45,18 @@ EXPORTED_SYMBOLS = (
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched",
 )
+# Every symbol declared in include/ls_fno.h (learned preconditioner).
+FNO_SYMBOLS = (
+    "ls_fno_create", "ls_fno_destroy", "ls_fno_num_params", "ls_fno_get_params", "ls_fno_set_params",
+    "ls_fno_get_grads", "ls_fno_forward", "ls_fno_loss_grad", "ls_fno_adam_step", "ls_fno_make_batch",
+    "ls_op_grid_sample", "ls_op_grid_weights", "ls_op_grid_contrast", "ls_fgmres_nn",
+)
+LS_NN_GUESS = 1
+LS_NN_PRECOND = 2
+FNO_IN_CHANNELS = 6
+FNO_OUT_CHANNELS = 2
+FNO_WIDTH = 32
+FNO_KAPPA_SCALE = 40.0
 
 
 class LSError(RuntimeError):
@@ -93,6 +105,16 @@ class _Info(ctypes.Structure):
         ("m2l_bytes", ctypes.c_longlong),
         ("m2l_flops", ctypes.c_longlong),
     ]
+
+
+class _FnoConfig(ctypes.Structure):
+    _fields_ = [("grid", ctypes.c_int), ("modes", ctypes.c_int), ("layers", ctypes.c_int),
+                ("proj_width", ctypes.c_int)]
+
+
+class _NnReport(ctypes.Structure):
+    _fields_ = [("n_matvec", ctypes.c_int), ("n_precond", ctypes.c_int), ("outer", ctypes.c_int),
+                ("fell_back", ctypes.c_int), ("guess_residual", ctypes.c_double), ("rel_residual", ctypes.c_double)]
 
 
 @dataclasses.dataclass
@@ -183,7 +205,22 @@ def lib():
         L.ls_op_precomputations.argtypes = [vp, dp, dp]
         L.ls_last_error.restype = ctypes.c_char_p
         L.ls_version.restype = ctypes.c_char_p
-        for n in EXPORTED_SYMBOLS:
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.ls_fno_create.argtypes = [ctypes.POINTER(_FnoConfig), ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
+        L.ls_fno_destroy.argtypes = [vp]
+        L.ls_fno_num_params.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        for n in ("ls_fno_get_params", "ls_fno_set_params", "ls_fno_get_grads"):
+            getattr(L, n).argtypes = [vp, fp]
+        L.ls_fno_forward.argtypes = [vp, ctypes.c_int, vp, vp, vp]
+        L.ls_fno_loss_grad.argtypes = [vp, ctypes.c_int, vp, vp, fp, vp]
+        L.ls_fno_adam_step.argtypes = [vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, vp]
+        L.ls_fno_make_batch.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int] + [vp] * 9
+        L.ls_op_grid_sample.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, vp]
+        L.ls_op_grid_weights.argtypes = [vp, ctypes.c_int, fp, ip]
+        L.ls_op_grid_contrast.argtypes = [vp, ctypes.c_int, fp]
+        L.ls_fgmres_nn.argtypes = [vp, vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, dp,
+                                   ctypes.POINTER(_NnReport)]
+        for n in EXPORTED_SYMBOLS + FNO_SYMBOLS:
             if n not in ("ls_op_skeleton_dump", "ls_last_error", "ls_version"):
                 getattr(L, n).restype = ctypes.c_int
         _lib = L
@@ -343,6 +380,40 @@ class Operator:
                                     ctypes.byref(b)), "ls_time_matvec")
         return a.value, b.value
 
+    # grid resampling and the learned preconditioner (include/ls_fno.h)
+    def grid_weights(self, grid):
+        """Host weight rows [G*G, rank] and leaf [G*G] of the nodes -> grid map."""
+        w = np.empty((grid * grid, self.info["rank"]), dtype=np.float32)
+        leaf = np.empty(grid * grid, dtype=np.int32)
+        _check(lib().ls_op_grid_weights(self._h, int(grid), w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                        leaf.ctypes.data_as(ctypes.POINTER(ctypes.c_int))), "ls_op_grid_weights")
+        return w, leaf
+
+    def grid_contrast(self, grid):
+        q = np.empty(grid * grid, dtype=np.float32)
+        _check(lib().ls_op_grid_contrast(self._h, int(grid), q.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+               "ls_op_grid_contrast")
+        return q
+
+    def grid_sample_device(self, grid, nvec, x_ptr, out_ptr, stream=0):
+        """out[v][G*G] (complex64) from nvec complex128 vectors at x_ptr (device)."""
+        _check(lib().ls_op_grid_sample(self._h, int(grid), int(nvec), ctypes.c_void_p(x_ptr), ctypes.c_void_p(out_ptr),
+                                       ctypes.c_void_p(stream)), "ls_op_grid_sample")
+
+    def fgmres_nn(self, net, b, flags=LS_NN_GUESS | LS_NN_PRECOND, max_outer=10, inner_iter=100, tol=1e-8):
+        """Mixed-precision flexible GMRES with the network as initial guess
+        and right preconditioner (ls_fgmres_nn). Returns (x, FP64 residual
+        history, report dict, status)."""
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.empty_like(b)
+        hist = np.full(max_outer + 2, np.nan)
+        rep = _NnReport()
+        code = lib().ls_fgmres_nn(self._h, net._h if net is not None else None, _dp(b), int(flags), int(max_outer),
+                                  int(inner_iter), float(tol), _dp(x), _dp(hist), ctypes.byref(rep))
+        if code not in (LS_OK, LS_E_NOT_CONVERGED):
+            _check(code, "ls_fgmres_nn")
+        return x, hist[~np.isnan(hist)], {f: getattr(rep, f) for f, _ in _NnReport._fields_}, code
+
     # inspection
     def skeleton_dump(self):
         n = lib().ls_op_skeleton_dump(self._h, None, 0)
@@ -444,3 +515,120 @@ def scattered_field(cfg, phi, device=0):
     u_tot = u_inc + u_scat
     err = np.linalg.norm(phi / cfg.kappa ** 2 + q * u_tot)
     return u_scat, u_tot, float(err)
+
+
+# ---------------------------------------------------------------- learned preconditioner
+
+def fno_layout(grid=128, modes=24, layers=4, proj_width=128):
+    """Offsets of the parameter groups in the flat FP32 vector (include/ls_fno.h)."""
+    W, o, lay = FNO_WIDTH, 0, {}
+
+    def take(name, n):
+        nonlocal o
+        lay[name] = (o, n)
+        o += n
+    take("lift_w", W * FNO_IN_CHANNELS)
+    take("lift_b", W)
+    for l in range(layers):
+        take(f"spec{l}", 2 * (2 * modes) * modes * W * W)
+        take(f"pw_w{l}", W * W)
+        take(f"pw_b{l}", W)
+    take("p1_w", proj_width * W)
+    take("p1_b", proj_width)
+    take("p2_w", FNO_OUT_CHANNELS * proj_width)
+    take("p2_b", FNO_OUT_CHANNELS)
+    lay["total"] = o
+    return lay
+
+
+_FNO_MAGIC = b"LSFNO001"
+
+
+class FNO:
+    """Spectral neural operator on one GPU (ls_fno): hand-written CUDA
+    forward, backward and Adam. Device buffers are passed as integer
+    addresses (e.g. torch tensors' data_ptr())."""
+
+    def __init__(self, grid=128, modes=24, layers=4, proj_width=128, device=0, seed=0):
+        self.shape = dict(grid=grid, modes=modes, layers=layers, proj_width=proj_width)
+        c = _FnoConfig(grid, modes, layers, proj_width)
+        h = ctypes.c_void_p()
+        _check(lib().ls_fno_create(ctypes.byref(c), int(device), int(seed), ctypes.byref(h)), "ls_fno_create")
+        self._h = h
+        n = ctypes.c_longlong()
+        _check(lib().ls_fno_num_params(self._h, ctypes.byref(n)), "ls_fno_num_params")
+        self.n_params = n.value
+        self.device = device
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ls_fno_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _fp(self, a):
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def get_params(self):
+        p = np.empty(self.n_params, dtype=np.float32)
+        _check(lib().ls_fno_get_params(self._h, self._fp(p)), "ls_fno_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        if p.shape != (self.n_params,):
+            raise ValueError(f"expected {self.n_params} parameters")
+        _check(lib().ls_fno_set_params(self._h, self._fp(p)), "ls_fno_set_params")
+
+    def get_grads(self):
+        g = np.empty(self.n_params, dtype=np.float32)
+        _check(lib().ls_fno_get_grads(self._h, self._fp(g)), "ls_fno_get_grads")
+        return g
+
+    def forward_device(self, batch, in_ptr, out_ptr, stream=0):
+        _check(lib().ls_fno_forward(self._h, int(batch), ctypes.c_void_p(in_ptr), ctypes.c_void_p(out_ptr),
+                                    ctypes.c_void_p(stream)), "ls_fno_forward")
+
+    def loss_grad_device(self, batch, in_ptr, target_ptr, want_loss=True, stream=0):
+        loss = ctypes.c_float(float("nan"))
+        _check(lib().ls_fno_loss_grad(self._h, int(batch), ctypes.c_void_p(in_ptr), ctypes.c_void_p(target_ptr),
+                                      ctypes.byref(loss) if want_loss else None, ctypes.c_void_p(stream)),
+               "ls_fno_loss_grad")
+        return loss.value if want_loss else None
+
+    def adam_step(self, lr, beta1=0.9, beta2=0.999, eps=1e-8, stream=0):
+        _check(lib().ls_fno_adam_step(self._h, float(lr), float(beta1), float(beta2), float(eps),
+                                      ctypes.c_void_p(stream)), "ls_fno_adam_step")
+
+    def make_batch_device(self, batch, n_basis, n_scatterers, F, PHI, Q, kappa, scatterer, coef, inp, target,
+                          stream=0):
+        args = [ctypes.c_void_p(a) for a in (F, PHI, Q, kappa, scatterer, coef, inp, target, stream)]
+        _check(lib().ls_fno_make_batch(self._h, int(batch), int(n_basis), int(n_scatterers), *args),
+               "ls_fno_make_batch")
+
+    def save(self, path, half=True):
+        """Weights file: magic, 5 int32 (grid, modes, layers, proj_width,
+        dtype 0 = float32 / 1 = float16), then the flat parameters."""
+        p = self.get_params()
+        hdr = np.array([self.shape["grid"], self.shape["modes"], self.shape["layers"], self.shape["proj_width"],
+                        1 if half else 0], dtype="<i4")
+        with open(path, "wb") as f:
+            f.write(_FNO_MAGIC)
+            f.write(hdr.tobytes())
+            f.write(p.astype("<f2" if half else "<f4").tobytes())
+
+    @classmethod
+    def load(cls, path, device=0):
+        with open(path, "rb") as f:
+            if f.read(8) != _FNO_MAGIC:
+                raise ValueError(f"{path}: not a network weights file")
+            g, m, l, pw, dt = np.frombuffer(f.read(20), dtype="<i4")
+            p = np.frombuffer(f.read(), dtype="<f2" if dt == 1 else "<f4").astype(np.float32)
+        net = cls(grid=int(g), modes=int(m), layers=int(l), proj_width=int(pw), device=device)
+        net.set_params(p)
+        return net

@@ -17,7 +17,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CXX_SOURCES = ["assemble.cpp", "capi.cpp"]
-CU_SOURCES = ["matvec.cu", "matvec_df.cu", "gmres.cu", "batched.cu"]
+CU_SOURCES = ["matvec.cu", "matvec_df.cu", "gmres.cu", "batched.cu", "fno.cu", "nn_precond.cu"]
 
 
 def _nvcc():
@@ -46,7 +46,7 @@ def _stale(target, deps):
         return True
     t = os.path.getmtime(target)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
-    headers.append(os.path.join(ROOT, "include", "ls_dafmm.h"))
+    headers += [os.path.join(ROOT, "include", "ls_dafmm.h"), os.path.join(ROOT, "include", "ls_fno.h")]
     return any(os.path.getmtime(d) > t for d in list(deps) + headers)
 
 

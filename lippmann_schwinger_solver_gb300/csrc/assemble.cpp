@@ -1272,7 +1272,9 @@ void Builder::pack(HostOperator& op) {
 
 bool Builder::run(HostOperator& op, std::string& err) {
   const auto t0 = std::chrono::steady_clock::now();
-  if (cfg.nLevelsUniform < 2 || cfg.nLevelsUniform > 10) { err = "nLevelsUniform must be in [2, 10]"; return false; }
+  // Depth 2 would put level_LFR = min(max(., 2), nLevels - 1) below the
+  // coarsest far-field level 2, which the level structure does not allow.
+  if (cfg.nLevelsUniform < 3 || cfg.nLevelsUniform > 10) { err = "nLevelsUniform must be in [3, 10]"; return false; }
   if (cfg.nChebNodes < 2 || cfg.nChebNodes > 8) { err = "nChebNodes must be in [2, 8]"; return false; }
   if (cfg.degreeOfBases < 1 || cfg.degreeOfBases * (cfg.degreeOfBases + 1) / 2 > cfg.nChebNodes * cfg.nChebNodes) {
     err = "degreeOfBases gives more basis polynomials than nodes"; return false;
@@ -1363,5 +1365,7 @@ bool assemble(const ls_config& cfg, HostOperator& op, std::string& err) {
     return false;
   }
 }
+
+double contrast_at(const ls_config& cfg, double x, double y) { return contrast_fn(cfg, x, y); }
 
 }  // namespace lsg

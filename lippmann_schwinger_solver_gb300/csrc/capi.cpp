@@ -3,17 +3,38 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
 
+#include "../../include/ls_fno.h"
 #include "device.h"
 #include "ls_internal.h"
+#include "nn_precond.h"
 
 struct ls_op {
   lsg::HostOperator host;
   lsg::DevOperator dev;
   bool on_device = false;  // false: assembled on the host only (device < 0)
+  // Network preconditioner of the last ls_fgmres_nn (built for nn_net).
+  std::unique_ptr<lsg::NnPrecond> nn;
+  const void* nn_net = nullptr;
+  // Nodes -> grid sampler of the last ls_op_grid_sample.
+  std::unique_ptr<lsg::GridSampler> sampler;
+  ~ls_op() {
+    if (nn) nn->release();
+    if (sampler) sampler->release();
+  }
+};
+
+struct ls_fno {
+  lsg::FnoNet net;
+  float* ssq = nullptr;  // per-sample |f|^2 of ls_fno_make_batch
+  ~ls_fno() {
+    cudaFree(ssq);
+    net.release();
+  }
 };
 
 namespace lsg {
@@ -79,7 +100,12 @@ ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
 
 ls_status ls_op_destroy(ls_op* op) {
   if (!op) return LS_OK;
-  if (op->on_device) dev_free(op->dev);
+  if (op->on_device) {
+    cudaSetDevice(op->dev.device);
+    if (op->nn) op->nn->release();
+    if (op->sampler) op->sampler->release();
+    dev_free(op->dev);
+  }
   delete op;
   return LS_OK;
 }
@@ -372,6 +398,211 @@ ls_status ls_op_precomputations(const ls_op* op, double* M, double* near) {
   if (!op) return fail(LS_E_INVALID, "ls_op_precomputations: null argument");
   if (M) std::memcpy(M, op->host.M.data(), op->host.M.size() * sizeof(cd));
   if (near) std::memcpy(near, op->host.nearB.data(), op->host.nearB.size() * sizeof(cd));
+  return LS_OK;
+}
+
+// ------------------------------------------------------------------ learned preconditioner (ls_fno.h)
+
+ls_status ls_fno_create(const ls_fno_config* cfg, int device, unsigned long long seed, ls_fno** out) {
+  if (!cfg || !out) return fail(LS_E_INVALID, "ls_fno_create: null argument");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(LS_E_CUDA, "ls_fno_create: no CUDA device available");
+  if (device < 0 || device >= ndev) return fail(LS_E_INVALID, "ls_fno_create: device index out of range");
+  ls_fno* f = new (std::nothrow) ls_fno();
+  if (!f) return fail(LS_E_NOMEM, "ls_fno_create: out of host memory");
+  FnoShape sh;
+  sh.grid = cfg->grid;
+  sh.modes = cfg->modes;
+  sh.layers = cfg->layers;
+  sh.proj = cfg->proj_width;
+  std::string err;
+  if (!f->net.init(device, sh, seed, err)) {
+    delete f;
+    return fail(err.rfind("device", 0) == 0 ? LS_E_CUDA : LS_E_INVALID, "ls_fno_create: " + err);
+  }
+  if ((e = cudaMalloc(&f->ssq, kFnoMaxBatch * sizeof(float))) != cudaSuccess) {
+    delete f;
+    return cuda_fail(e, "ls_fno_create");
+  }
+  *out = f;
+  return LS_OK;
+}
+
+ls_status ls_fno_destroy(ls_fno* net) {
+  if (!net) return LS_OK;
+  cudaSetDevice(net->net.device);
+  delete net;
+  return LS_OK;
+}
+
+ls_status ls_fno_num_params(const ls_fno* net, long long* n) {
+  if (!net || !n) return fail(LS_E_INVALID, "ls_fno_num_params: null argument");
+  *n = net->net.lay.total;
+  return LS_OK;
+}
+
+namespace {
+ls_status fno_copy(const ls_fno* net, float* host, const float* dev_src, float* dev_dst, const float* host_src,
+                   const char* where) {
+  if (!net || !(host || host_src)) return fail(LS_E_INVALID, std::string(where) + ": null argument");
+  cudaSetDevice(net->net.device);
+  const size_t bytes = (size_t)net->net.lay.total * sizeof(float);
+  cudaError_t e = cudaDeviceSynchronize();  // the net's kernels may be on any stream
+  if (e == cudaSuccess) e = dev_dst ? cudaMemcpy(dev_dst, host_src, bytes, cudaMemcpyHostToDevice)
+                                    : cudaMemcpy(host, dev_src, bytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, where);
+  return LS_OK;
+}
+cudaStream_t fno_stream(const ls_fno*, void* stream) { return static_cast<cudaStream_t>(stream); }
+}  // namespace
+
+ls_status ls_fno_get_params(const ls_fno* net, float* host) {
+  return fno_copy(net, host, net ? net->net.params : nullptr, nullptr, nullptr, "ls_fno_get_params");
+}
+ls_status ls_fno_set_params(ls_fno* net, const float* host) {
+  if (!net || !host) return fail(LS_E_INVALID, "ls_fno_set_params: null argument");
+  return fno_copy(net, nullptr, nullptr, net->net.params, host, "ls_fno_set_params");
+}
+ls_status ls_fno_get_grads(const ls_fno* net, float* host) {
+  return fno_copy(net, host, net ? net->net.grads : nullptr, nullptr, nullptr, "ls_fno_get_grads");
+}
+
+ls_status ls_fno_forward(ls_fno* net, int batch, const float* in, float* out, void* stream) {
+  if (!net || !in || !out) return fail(LS_E_INVALID, "ls_fno_forward: null argument");
+  if (batch < 1 || batch > kFnoMaxBatch) return fail(LS_E_INVALID, "ls_fno_forward: batch out of range");
+  cudaSetDevice(net->net.device);
+  cudaError_t e = net->net.forward(batch, in, out, nullptr, fno_stream(net, stream));
+  if (e != cudaSuccess) return cuda_fail(e, "ls_fno_forward");
+  return LS_OK;
+}
+
+ls_status ls_fno_loss_grad(ls_fno* net, int batch, const float* in, const float* target, float* loss, void* stream) {
+  if (!net || !in || !target) return fail(LS_E_INVALID, "ls_fno_loss_grad: null argument");
+  if (batch < 1 || batch > kFnoMaxBatch) return fail(LS_E_INVALID, "ls_fno_loss_grad: batch out of range");
+  cudaSetDevice(net->net.device);
+  cudaStream_t s = fno_stream(net, stream);
+  cudaError_t e = net->net.loss_grad(batch, in, target, s);
+  if (e == cudaSuccess && loss) {
+    e = cudaMemcpyAsync(loss, net->net.loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "ls_fno_loss_grad");
+  return LS_OK;
+}
+
+ls_status ls_fno_adam_step(ls_fno* net, float lr, float beta1, float beta2, float eps, void* stream) {
+  if (!net) return fail(LS_E_INVALID, "ls_fno_adam_step: null argument");
+  if (!(lr > 0.f) || !(beta1 >= 0.f && beta1 < 1.f) || !(beta2 >= 0.f && beta2 < 1.f) || !(eps > 0.f))
+    return fail(LS_E_INVALID, "ls_fno_adam_step: bad hyper-parameters");
+  cudaSetDevice(net->net.device);
+  cudaError_t e = net->net.adam(lr, beta1, beta2, eps, fno_stream(net, stream));
+  if (e != cudaSuccess) return cuda_fail(e, "ls_fno_adam_step");
+  return LS_OK;
+}
+
+ls_status ls_fno_make_batch(ls_fno* net, int batch, int n_basis, int n_scatterers, const float* F, const float* PHI,
+                            const float* Q, const float* kappa, const int* scatterer, const float* coef, float* in,
+                            float* target, void* stream) {
+  if (!net || !F || !PHI || !Q || !kappa || !scatterer || !coef || !in || !target)
+    return fail(LS_E_INVALID, "ls_fno_make_batch: null argument");
+  if (batch < 1 || batch > kFnoMaxBatch || n_basis < 1 || n_basis > 64 || n_scatterers < 1)
+    return fail(LS_E_INVALID, "ls_fno_make_batch: batch must be in [1, 64], n_basis in [1, 64], n_scatterers >= 1");
+  cudaSetDevice(net->net.device);
+  cudaError_t e = fno_make_batch(net->net.shape.grid, batch, n_basis, n_scatterers, reinterpret_cast<const float2*>(F),
+                                 reinterpret_cast<const float2*>(PHI), Q, kappa, scatterer,
+                                 reinterpret_cast<const float2*>(coef), in, target, net->ssq, fno_stream(net, stream));
+  if (e != cudaSuccess) return cuda_fail(e, "ls_fno_make_batch");
+  return LS_OK;
+}
+
+namespace {
+bool valid_grid(int g) { return g >= 8 && g <= 1024 && (g & (g - 1)) == 0; }
+}  // namespace
+
+ls_status ls_op_grid_weights(const ls_op* op, int grid, float* w, int* leaf) {
+  if (!op || !w || !leaf) return fail(LS_E_INVALID, "ls_op_grid_weights: null argument");
+  if (!valid_grid(grid)) return fail(LS_E_INVALID, "ls_op_grid_weights: grid must be a power of two in [8, 1024]");
+  std::vector<float> hw;
+  std::vector<int> hl;
+  grid_sampling_weights(op->host, grid, hw, hl);
+  std::memcpy(w, hw.data(), hw.size() * sizeof(float));
+  std::memcpy(leaf, hl.data(), hl.size() * sizeof(int));
+  return LS_OK;
+}
+
+ls_status ls_op_grid_contrast(const ls_op* op, int grid, float* q) {
+  if (!op || !q) return fail(LS_E_INVALID, "ls_op_grid_contrast: null argument");
+  if (!valid_grid(grid)) return fail(LS_E_INVALID, "ls_op_grid_contrast: grid must be a power of two in [8, 1024]");
+  std::vector<float> hq;
+  grid_contrast(op->host.cfg, grid, hq);
+  std::memcpy(q, hq.data(), hq.size() * sizeof(float));
+  return LS_OK;
+}
+
+ls_status ls_op_grid_sample(ls_op* op, int grid, int nvec, const double* x, float* out, void* stream) {
+  if (!op || !x || !out) return fail(LS_E_INVALID, "ls_op_grid_sample: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_op_grid_sample: operator was assembled without a device");
+  if (!valid_grid(grid) || nvec < 1 || nvec > 65535)
+    return fail(LS_E_INVALID, "ls_op_grid_sample: bad grid or vector count");
+  DevOperator& d = op->dev;
+  cudaSetDevice(d.device);
+  std::string err;
+  if (!op->sampler || op->sampler->G != grid) {
+    if (!op->sampler) op->sampler.reset(new GridSampler());
+    if (!op->sampler->init(op->host, grid, err)) return fail(LS_E_CUDA, "ls_op_grid_sample: " + err);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = op->sampler->sample(reinterpret_cast<const double2*>(x), nvec, d.N, reinterpret_cast<float2*>(out), s);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_op_grid_sample");
+  return LS_OK;
+}
+
+ls_status ls_fgmres_nn(ls_op* op, ls_fno* net, const double* b, int flags, int max_outer, int inner_iter, double tol,
+                       double* x, double* history, ls_nn_report* report) {
+  if (!op || !b || !x) return fail(LS_E_INVALID, "ls_fgmres_nn: null argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_fgmres_nn: operator was assembled without a device");
+  if (max_outer < 1 || inner_iter < 1 || flags < 0 || flags > (LS_NN_GUESS | LS_NN_PRECOND))
+    return fail(LS_E_INVALID, "ls_fgmres_nn: bad iteration counts or flags");
+  if (flags && !net) return fail(LS_E_INVALID, "ls_fgmres_nn: flags need a network");
+  DevOperator& d = op->dev;
+  if (!d.has_f32) return fail(LS_E_STATE, "ls_fgmres_nn: call ls_op_enable_f32 first");
+  if (flags && net->net.device != d.device) return fail(LS_E_INVALID, "ls_fgmres_nn: network on another device");
+  cudaSetDevice(d.device);
+  std::string err;
+  Precond32* M = nullptr;
+  if (flags) {
+    if (!op->nn || op->nn_net != net) {
+      if (!op->nn) op->nn.reset(new NnPrecond());
+      op->nn_net = nullptr;
+      if (!op->nn->init(op->host, &net->net, err)) return fail(LS_E_CUDA, "ls_fgmres_nn: " + err);
+      op->nn_net = net;
+    }
+    M = op->nn.get();
+  }
+  const size_t bytes = (size_t)d.N * sizeof(double2);
+  cudaError_t e = cudaMemcpyAsync(d.xbuf, b, bytes, cudaMemcpyHostToDevice, d.stream);
+  std::vector<double> hist;
+  FlexReport rep;
+  double rr = 1.0;
+  if (e == cudaSuccess)
+    e = dev_gmres_mixed_flex(d, d.xbuf, d.ybuf, (flags & LS_NN_PRECOND) ? M : nullptr,
+                             (flags & LS_NN_GUESS) ? M : nullptr, max_outer, inner_iter, tol, hist, rep, rr);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(x, d.ybuf, bytes, cudaMemcpyDeviceToHost, d.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_fgmres_nn");
+  if (history)
+    for (size_t i = 0; i < hist.size() && i < (size_t)max_outer + 2; ++i) history[i] = hist[i];
+  if (report) {
+    report->n_matvec = rep.n_matvec;
+    report->n_precond = rep.n_precond;
+    report->outer = (int)hist.size() - 1;
+    report->fell_back = rep.fell_back ? 1 : 0;
+    report->guess_residual = rep.guess_residual;
+    report->rel_residual = rr;
+  }
+  if (!(rr <= tol)) return fail(LS_E_NOT_CONVERGED, "ls_fgmres_nn: tolerance not reached");
   return LS_OK;
 }
 

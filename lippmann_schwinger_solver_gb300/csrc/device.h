@@ -131,4 +131,27 @@ cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, in
 cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner,
                             double tol, std::vector<double>& hist, int& n_matvec, double& relres);
 
+// A right preconditioner z = M(v) on FP32 vectors of the operator's size,
+// queued on stream s without waiting on the host. M may be nonlinear
+// (flexible GMRES keeps each z).
+struct Precond32 {
+  virtual ~Precond32() = default;
+  virtual cudaError_t apply(const float2* v, float2* z, cudaStream_t s) = 0;
+};
+struct FlexReport {
+  int n_matvec = 0;       // FP32 operator applies + FP64 residual products
+  int n_precond = 0;      // applications of M (the initial guess included)
+  double guess_residual = 1.0;  // |b - A x0| / |b| of the initial guess (1 without one)
+  bool fell_back = false; // M was dropped after an outer step that did not reduce the residual
+};
+// dev_gmres_mixed with flexible inner GMRES right-preconditioned by M (may be
+// null), starting from x0 = guess(b) when guess is given (kept only if it
+// beats x0 = 0). The residual is the FP64 one throughout. M is turned off
+// for the remaining steps, so that the solve ends as plain dev_gmres_mixed
+// would, when an outer step (at most 16 preconditioned inner steps) did not
+// halve the residual.
+cudaError_t dev_gmres_mixed_flex(DevOperator& d, const double2* b, double2* x, Precond32* M, Precond32* guess,
+                                 int max_outer, int inner, double tol, std::vector<double>& hist, FlexReport& rep,
+                                 double& relres);
+
 }  // namespace lsg

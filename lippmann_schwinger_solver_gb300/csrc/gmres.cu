@@ -33,6 +33,7 @@ namespace lsg {
 constexpr int kDotThreads = 128;
 constexpr int kDotBlocks = 304;  // row chunks: partial sums per column (2 per SM)
 constexpr int kDotCols = 8;      // columns per multi-dot block
+constexpr int kFlexInner = 16;   // steps of a right-preconditioned inner cycle
 
 template <class T> struct Cx;
 template <> struct Cx<double2> {
@@ -50,12 +51,22 @@ struct Basis {
   T* V = nullptr;
   T* w = nullptr;
   T* r = nullptr;
-  int n = 0, cap = -1;
+  T* Z = nullptr;  // flexible GMRES: preconditioned directions z_k = M(v_k)
+  int n = 0, cap = -1, zcap = -1;
   void release() {
-    cudaFree(V); cudaFree(w); cudaFree(r);
-    V = w = r = nullptr;
+    cudaFree(V); cudaFree(w); cudaFree(r); cudaFree(Z);
+    V = w = r = Z = nullptr;
     n = 0;
-    cap = -1;
+    cap = zcap = -1;
+  }
+  cudaError_t ensure_z(int m) {
+    if (Z && m <= zcap) return cudaSuccess;
+    cudaFree(Z);
+    Z = nullptr;
+    zcap = -1;
+    cudaError_t e = cudaMalloc(&Z, (size_t)n * sizeof(T) * (m + 1));
+    if (e == cudaSuccess) zcap = m;
+    return e;
   }
   cudaError_t ensure(int n_, int m) {
     if (n_ == n && m <= cap) return cudaSuccess;
@@ -378,16 +389,31 @@ cudaError_t apply(DevOperator& d, const float2* x, float2* y, cudaStream_t s) {
 Basis<double2>& basis(GmresWorkspace& ws, const double2*) { return ws.b64; }
 Basis<float2>& basis(GmresWorkspace& ws, const float2*) { return ws.b32; }
 
+cudaError_t precondition(Precond32* M, const float2* v, float2* z, cudaStream_t s) { return M->apply(v, z, s); }
+cudaError_t precondition(Precond32*, const double2*, double2*, cudaStream_t) { return cudaErrorNotSupported; }
+
 // One Arnoldi cycle from x0 (device, may be null for x0 = 0). Writes the
 // updated solution into x. tol < 0 disables the residual stop; breakdown
-// exits when H(k+1,k) < brk.
+// exits when H(k+1,k) < brk. With M (FP32 bases only) the cycle is flexible
+// GMRES: step k applies A to z_k = M(v_k), keeps z_k, and the update is
+// x = x0 + Z y instead of x0 + V y.
 template <class T>
 cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const T* x0, T* x, int m, double tol,
-                          double brk, double bnorm, std::vector<double>* hist, int& iters, bool& converged) {
+                          double brk, double bnorm, std::vector<double>* hist, int& iters, bool& converged,
+                          Precond32* M = nullptr) {
   Basis<T>& B = basis(ws, b);
   cudaStream_t s = d.stream;
   const int n = d.N;
   cudaError_t e;
+  if (M && (e = B.ensure_z(m)) != cudaSuccess) return e;
+  // w = A v_k, or w = A M(v_k) with z_k kept.
+  auto product = [&](int k) -> cudaError_t {
+    const T* v = B.V + (size_t)k * n;
+    if (!M) return apply(d, v, B.w, s);
+    T* z = B.Z + (size_t)k * n;
+    cudaError_t pe = precondition(M, v, z, s);
+    return pe != cudaSuccess ? pe : apply(d, z, B.w, s);
+  };
   // r = b - A x0
   if (x0) {
     if ((e = apply(d, x0, B.w, s)) != cudaSuccess) return e;
@@ -416,7 +442,7 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
   // forms itself, so it is queued before the host waits for step k's
   // coefficients: the host's Givens work and the wait hide behind it. A
   // converged or broken-down cycle leaves one unused product behind.
-  if ((e = apply(d, B.V, B.w, s)) != cudaSuccess) return e;
+  if ((e = product(0)) != cudaSuccess) return e;
   double2* hp = ws.pinned;
   double2* hp2 = ws.pinned + (m + 2);
   double2* np = ws.pinned + 2 * (m + 2);
@@ -432,7 +458,7 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
     cudaMemcpyAsync(hp2, ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(np, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
     if ((e = cudaEventRecord(ws.copied, s)) != cudaSuccess) return e;
-    if (k + 1 < m && (e = apply(d, B.V + (size_t)(k + 1) * n, B.w, s)) != cudaSuccess) return e;
+    if (k + 1 < m && (e = product(k + 1)) != cudaSuccess) return e;
     if ((e = cudaEventSynchronize(ws.copied)) != cudaSuccess) return e;
     std::vector<cdh> hk(k + 2);
     for (int i = 0; i <= k; ++i) hk[i] = cdh(hp[i].x + hp2[i].x, hp[i].y + hp2[i].y);
@@ -478,7 +504,7 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
   } else {
     cudaMemsetAsync(x, 0, (size_t)n * sizeof(T), s);
   }
-  launch_pdl(multi_axpy_kernel<T>, grid_for(n), 256, 0, s, x, B.V, n, K, ws.h, n, 1.0);
+  launch_pdl(multi_axpy_kernel<T>, grid_for(n), 256, 0, s, x, M ? B.Z : B.V, n, K, ws.h, n, 1.0);
   iters = K;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return cudaStreamSynchronize(s);
@@ -536,9 +562,12 @@ cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, in
 // Iterative refinement in FP64 around GMRES on the FP32 operator:
 //   r = b - A64 x ; solve A32 d = r in FP32 to a loose tolerance ; x += d
 // until |b - A64 x| / |b| <= tol. The residual is always the FP64 one; the
-// inner Arnoldi basis and its orthogonalisation are FP32.
-cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner, double tol,
-                            std::vector<double>& hist, int& n_matvec, double& relres) {
+// inner Arnoldi basis and its orthogonalisation are FP32. With a right
+// preconditioner M the inner solves are flexible GMRES on A32 M, and with
+// guess the iteration starts from x0 = guess(b) instead of 0.
+cudaError_t dev_gmres_mixed_flex(DevOperator& d, const double2* b, double2* x, Precond32* M, Precond32* guess,
+                                 int max_outer, int inner, double tol, std::vector<double>& hist, FlexReport& rep,
+                                 double& relres) {
   const int n = d.N;
   GmresWorkspace& ws = workspace(d);
   cudaError_t e = ws.ensure(n, inner);
@@ -549,31 +578,66 @@ cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int ma
   double bn = 0.0;
   if ((e = vnorm(b, n, ws, d.stream, bn)) != cudaSuccess) return e;
   hist.clear();
-  n_matvec = 0;
+  rep = FlexReport();
   cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), d.stream);
   cudaMemcpyAsync(r, b, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, d.stream);
   relres = 1.0;
-  hist.push_back(1.0);
-  for (int o = 0; o < max_outer && relres > tol; ++o) {
-    int it = 0;
-    bool conv = false;
-    // Inner solve to roughly the FP32 operator accuracy.
-    const double inner_tol = std::max(tol / std::max(relres, 1e-300), 1e-6);
-    launch_pdl(to_f32_kernel, grid_for(n), 256, 0, d.stream, r, ws.res32, n);
-    if ((e = arnoldi_cycle<float2>(d, ws, ws.res32, nullptr, ws.dx32, inner, inner_tol, 1e-300,
-                                   std::max(relres * bn, 1e-300), nullptr, it, conv)) != cudaSuccess)
-      return e;
-    n_matvec += it;
+  if (guess && bn > 0.0) {
+    // x0 = guess(b) in FP32; kept only if it beats x0 = 0.
+    launch_pdl(to_f32_kernel, grid_for(n), 256, 0, d.stream, b, ws.res32, n);
+    if ((e = guess->apply(ws.res32, ws.dx32, d.stream)) != cudaSuccess) return e;
+    ++rep.n_precond;
     launch_pdl(add_f32_kernel, grid_for(n), 256, 0, d.stream, x, ws.dx32, n);
     if ((e = dev_matvec(d, x, ws.b64.w, d.stream, false)) != cudaSuccess) return e;
-    ++n_matvec;
+    ++rep.n_matvec;
     launch_pdl(sub_kernel<double2>, grid_for(n), 256, 0, d.stream, b, ws.b64.w, r, n);
     double rn = 0.0;
     if ((e = vnorm(r, n, ws, d.stream, rn)) != cudaSuccess) return e;
+    rep.guess_residual = rn / bn;
+    if (rep.guess_residual < 1.0) {
+      relres = rep.guess_residual;
+    } else {
+      cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), d.stream);
+      cudaMemcpyAsync(r, b, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, d.stream);
+    }
+  }
+  hist.push_back(relres);
+  for (int o = 0; o < max_outer && relres > tol; ++o) {
+    int it = 0;
+    bool conv = false;
+    Precond32* Mo = rep.fell_back ? nullptr : M;
+    // Inner solve to roughly the FP32 operator accuracy. A preconditioned
+    // cycle is capped at kFlexInner steps: a useful M converges well within
+    // them, and a useless one costs no more than that before the outer test
+    // below drops it.
+    const double inner_tol = std::max(tol / std::max(relres, 1e-300), 1e-6);
+    const int m_inner = Mo ? std::min(inner, kFlexInner) : inner;
+    launch_pdl(to_f32_kernel, grid_for(n), 256, 0, d.stream, r, ws.res32, n);
+    if ((e = arnoldi_cycle<float2>(d, ws, ws.res32, nullptr, ws.dx32, m_inner, inner_tol, 1e-300,
+                                   std::max(relres * bn, 1e-300), nullptr, it, conv, Mo)) != cudaSuccess)
+      return e;
+    rep.n_matvec += it;
+    if (Mo) rep.n_precond += it;
+    launch_pdl(add_f32_kernel, grid_for(n), 256, 0, d.stream, x, ws.dx32, n);
+    if ((e = dev_matvec(d, x, ws.b64.w, d.stream, false)) != cudaSuccess) return e;
+    ++rep.n_matvec;
+    launch_pdl(sub_kernel<double2>, grid_for(n), 256, 0, d.stream, b, ws.b64.w, r, n);
+    double rn = 0.0;
+    if ((e = vnorm(r, n, ws, d.stream, rn)) != cudaSuccess) return e;
+    const double prev = relres;
     relres = rn / bn;
     hist.push_back(relres);
+    if (Mo && relres > 0.5 * prev) rep.fell_back = true;
   }
   return cudaSuccess;
+}
+
+cudaError_t dev_gmres_mixed(DevOperator& d, const double2* b, double2* x, int max_outer, int inner, double tol,
+                            std::vector<double>& hist, int& n_matvec, double& relres) {
+  FlexReport rep;
+  cudaError_t e = dev_gmres_mixed_flex(d, b, x, nullptr, nullptr, max_outer, inner, tol, hist, rep, relres);
+  n_matvec = rep.n_matvec;
+  return e;
 }
 
 }  // namespace lsg

@@ -76,6 +76,8 @@ struct HostOperator {
 
 // assemble.cpp
 bool assemble(const ls_config& cfg, HostOperator& op, std::string& err);
+// The contrast plugin q(x, y) selected by cfg (userkernel::ContrastFunction).
+double contrast_at(const ls_config& cfg, double x, double y);
 
 // Thread-local last error message used by the C ABI.
 void set_error(const std::string& msg);

@@ -83,6 +83,7 @@ def test_host_only_operator_refuses_device_calls(ls):
 
 @pytest.mark.parametrize("over,msg", [
     ({"nLevelsUniform": 1}, "nLevelsUniform"),
+    ({"nLevelsUniform": 2}, "nLevelsUniform"),
     ({"nLevelsUniform": 11}, "nLevelsUniform"),
     ({"nChebNodes": 1}, "nChebNodes"),
     ({"degreeOfBases": 9}, "degreeOfBases"),

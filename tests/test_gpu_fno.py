@@ -1,0 +1,207 @@
+"""Learned preconditioner on the GPU against the oracle (oracle/fno_oracle.py):
+network forward, loss and every parameter group's gradient, the Adam step,
+the training-batch construction, the device grid resampling, and the
+network-preconditioned flexible GMRES (convergence, fallback, and its
+initial guess recomputed from the oracle's network and resampling).
+
+Tolerances: the kernels compute in FP32 and the oracle in FP64; relative L2
+1e-5 for the forward pass and 1e-4 per gradient group (sums over 2 x 128^2
+points with float atomics)."""
+import numpy as np
+import pytest
+
+from conftest import CFG_BUMPS, CFG_C1, full_cfg
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+SHAPES = [dict(grid=128, modes=24, layers=4, proj_width=128), dict(grid=32, modes=6, layers=2, proj_width=64)]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _inputs(G, B, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, (B, G * G, 6)).astype(np.float32)
+    t = rng.uniform(-1, 1, (B, G * G, 2)).astype(np.float32)
+    return x, t
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_forward_matches_oracle(ls, shape):
+    from oracle import fno_oracle as fo
+    net = ls.FNO(**shape, seed=3)
+    G, B = shape["grid"], 2
+    x, _ = _inputs(G, B, 0)
+    xd = torch.from_numpy(x).cuda()
+    od = torch.empty((B, G * G, 2), device="cuda")
+    net.forward_device(B, xd.data_ptr(), od.data_ptr(), stream=_stream())
+    torch.cuda.synchronize()
+    ref = fo.forward(net.get_params(), x, G, shape["modes"], shape["layers"], shape["proj_width"])
+    assert rel(od.cpu().numpy(), ref) < 1e-5
+    net.close()
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_loss_and_gradients_match_oracle(ls, shape):
+    from oracle import fno_oracle as fo
+    net = ls.FNO(**shape, seed=4)
+    G, B = shape["grid"], 2
+    x, t = _inputs(G, B, 1)
+    xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+    loss = net.loss_grad_device(B, xd.data_ptr(), td.data_ptr(), stream=_stream())
+    g = net.get_grads()
+    lref, gref = fo.loss_and_grad(net.get_params(), x, t, G, shape["modes"], shape["layers"], shape["proj_width"])
+    lay = ls.fno_layout(**shape)
+    errs = {name: rel(g[v[0]:v[0] + v[1]], gref[v[0]:v[0] + v[1]]) for name, v in lay.items() if name != "total"}
+    assert abs(loss - lref) / lref < 1e-5, (loss, lref)
+    for name, e in errs.items():
+        assert e < 1e-4, (name, errs)
+    net.close()
+
+
+def test_adam_step_matches_oracle(ls):
+    from oracle import fno_oracle as fo
+    shape = SHAPES[1]
+    net = ls.FNO(**shape, seed=5)
+    G, B = shape["grid"], 2
+    x, t = _inputs(G, B, 2)
+    xd, td = torch.from_numpy(x).cuda(), torch.from_numpy(t).cuda()
+    p = net.get_params().astype(np.float64)
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for step in (1, 2):
+        net.loss_grad_device(B, xd.data_ptr(), td.data_ptr(), stream=_stream())
+        g = net.get_grads().astype(np.float64)
+        net.adam_step(1e-3, stream=_stream())
+        torch.cuda.synchronize()
+        p, m, v = fo.adam(p, g, m, v, step, 1e-3)
+        assert rel(net.get_params(), p) < 1e-6
+    net.close()
+
+
+def test_training_batch_matches_oracle(ls):
+    from oracle import fno_oracle as fo
+    G, S, nb, B = 32, 3, 5, 4
+    net = ls.FNO(grid=G, modes=6, layers=1, proj_width=32)
+    rng = np.random.default_rng(6)
+    F = (rng.standard_normal((S, nb, G * G)) + 1j * rng.standard_normal((S, nb, G * G))).astype(np.complex64)
+    PHI = (rng.standard_normal((S, nb, G * G)) + 1j * rng.standard_normal((S, nb, G * G))).astype(np.complex64)
+    Q = rng.uniform(0, 1.5, (S, G * G)).astype(np.float32)
+    kap = rng.uniform(0.25, 1.0, S).astype(np.float32)
+    sidx = np.array([2, 0, 1, 2], dtype=np.int32)
+    coef = (rng.standard_normal((B, nb)) + 1j * rng.standard_normal((B, nb))).astype(np.complex64)
+    dev = [torch.from_numpy(a).cuda() for a in (F, PHI, Q, kap, sidx, coef)]
+    inp = torch.empty((B, G * G, 6), device="cuda")
+    tgt = torch.empty((B, G * G, 2), device="cuda")
+    net.make_batch_device(B, nb, S, *[d.data_ptr() for d in dev], inp.data_ptr(), tgt.data_ptr(), stream=_stream())
+    torch.cuda.synchronize()
+    ri, rt = fo.make_batch(F.astype(complex), PHI.astype(complex), Q, kap, sidx, coef.astype(complex), G)
+    assert rel(inp.cpu().numpy(), ri) < 1e-5
+    assert rel(tgt.cpu().numpy(), rt) < 1e-5
+    with pytest.raises(ls.LSError):
+        net.make_batch_device(B, 65, S, *[d.data_ptr() for d in dev], inp.data_ptr(), tgt.data_ptr())
+    # an out-of-range scatterer index gives a zero sample, never a read outside F
+    sidx2 = torch.from_numpy(np.array([0, 7, -1, 1], dtype=np.int32)).cuda()
+    net.make_batch_device(B, nb, S, dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), dev[3].data_ptr(),
+                          sidx2.data_ptr(), dev[5].data_ptr(), inp.data_ptr(), tgt.data_ptr(), stream=_stream())
+    torch.cuda.synchronize()
+    assert float(tgt[1].abs().max()) == 0.0 and float(tgt[2].abs().max()) == 0.0
+    assert float(tgt[0].abs().max()) > 0.0
+    net.close()
+
+
+def test_device_grid_sampling_matches_oracle(ls):
+    from oracle import fno_oracle as fo
+    cfg = full_cfg(CFG_BUMPS, nLevelsUniform=3)
+    op = ls.Operator(cfg, device=0)
+    G = 64
+    rng = np.random.default_rng(7)
+    X = rng.standard_normal((3, op.N)) + 1j * rng.standard_normal((3, op.N))
+    xd = torch.from_numpy(X).cuda()
+    out = torch.empty((3, G * G), dtype=torch.complex64, device="cuda")
+    op.grid_sample_device(G, 3, xd.data_ptr(), out.data_ptr(), stream=_stream())
+    torch.cuda.synchronize()
+    pts = op.points()
+    for v in range(3):
+        ref = fo.grid_sample(pts, X[v], cfg.L, G)
+        assert rel(out[v].cpu().numpy(), ref) < 2e-6
+    op.close()
+
+
+def _solve_pair(ls, op, net, b, flags):
+    x0, h0, n0, rr0, c0 = op.gmres_mixed(b, max_outer=10, inner_iter=100, tol=1e-8)
+    x1, h1, rep, c1 = op.fgmres_nn(net, b, flags=flags, max_outer=10, inner_iter=100, tol=1e-8)
+    return (x0, h0, n0, rr0, c0), (x1, h1, rep, c1)
+
+
+def test_fgmres_without_network_is_mixed_gmres(ls):
+    op = ls.Operator(full_cfg(CFG_C1), device=0)
+    op.enable_f32()
+    b = op.rhs()
+    (x0, h0, n0, rr0, c0), (x1, h1, rep, c1) = _solve_pair(ls, op, None, b, 0)
+    assert c0 == c1 == ls.LS_OK
+    assert rep["n_precond"] == 0 and rep["guess_residual"] == 1.0 and rep["fell_back"] == 0
+    assert rep["n_matvec"] == n0
+    assert np.allclose(h0, h1, rtol=1e-12, atol=0)
+    assert rel(x1, x0) < 1e-14
+    op.close()
+
+
+def test_untrained_network_preconditioner_still_converges(ls):
+    """A random network is a poor preconditioner: the solve must still reach
+    the FP64 tolerance, the plain iteration taking over if the net stalls."""
+    op = ls.Operator(full_cfg(CFG_C1), device=0)
+    op.enable_f32()
+    net = ls.FNO(seed=11)
+    b = op.rhs()
+    x, hist, rep, code = op.fgmres_nn(net, b, flags=ls.LS_NN_GUESS | ls.LS_NN_PRECOND, max_outer=12,
+                                      inner_iter=100, tol=1e-8)
+    assert code == ls.LS_OK and rep["rel_residual"] <= 1e-8
+    r = b - op.matvec(x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.5e-8
+    assert rep["n_precond"] >= 1
+    assert hist[0] == (rep["guess_residual"] if rep["guess_residual"] < 1.0 else 1.0)
+    op.close()
+    net.close()
+
+
+def test_initial_guess_matches_oracle_composition(ls):
+    """x0 = b + grid->nodes(net(q, sample(b) / rms) * rms): the residual of
+    the library's guess equals the residual of the same map built from the
+    oracle's resampling and network."""
+    from oracle import fno_oracle as fo
+    cfg = full_cfg(CFG_C1)
+    op = ls.Operator(cfg, device=0)
+    op.enable_f32()
+    shape = SHAPES[0]
+    net = ls.FNO(**shape, seed=12)
+    b = op.rhs()
+    _, hist, rep, code = op.fgmres_nn(net, b, flags=ls.LS_NN_GUESS, max_outer=1, inner_iter=2, tol=1e-8)
+    G = shape["grid"]
+    pts = op.points()
+    f = fo.grid_sample(pts, b, cfg.L, G)
+    ix, iy = np.divmod(np.arange(G * G), G)
+    feats = np.zeros((1, G * G, 6))
+    feats[0, :, 0] = op.grid_contrast(G)
+    feats[0, :, 1], feats[0, :, 2] = f.real, f.imag
+    feats[0, :, 3] = cfg.kappa / ls.FNO_KAPPA_SCALE
+    feats[0, :, 4] = -1 + (2 * ix + 1) / G
+    feats[0, :, 5] = -1 + (2 * iy + 1) / G
+    out = fo.forward(net.get_params(), feats, G, shape["modes"], shape["layers"], shape["proj_width"],
+                     ssq=np.array([np.sum(np.abs(f) ** 2)]))
+    x0 = b + fo.grid_to_nodes(pts, out[0, :, 0] + 1j * out[0, :, 1], cfg.L, G)
+    r0 = np.linalg.norm(b - op.matvec(x0)) / np.linalg.norm(b)
+    assert rep["n_precond"] == 1
+    if r0 < 1.0:
+        assert abs(rep["guess_residual"] - r0) / r0 < 1e-4
+    else:  # a guess worse than zero is discarded
+        assert hist[0] == 1.0 and rep["guess_residual"] >= 1.0
+    op.close()
+    net.close()
