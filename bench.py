@@ -34,6 +34,9 @@ METRIC = "DAFMM matvec throughput, FP64 (plain method), N=147456, kappa=40"
 SEED = 20261203
 
 
+FNO_WEIGHTS = os.path.join(ROOT, "lippmann_schwinger_solver_gb300", "weights", "fno_k10_40.lsfno")
+
+
 def workload_config(ls, level=6):
     return ls.Config(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, TOL_POW=10, degreeOfBases=6, nLevelsUniform=level,
                      Qchoice=6, findPhi=1, reference_rounding=1, L=1.0, kappa=40.0, bumps=ls.seeded_bumps(SEED))
@@ -300,19 +303,40 @@ def run_ours(args):
     solve = None
     if not args.no_solve:
         b = op.rhs()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        _, hist64, it64, rr64, code64 = op.gmres(b, max_iter=args.max_iter, tol=1e-8)
-        t64 = time.perf_counter() - t0
+
+        def timed(fn):
+            fn()  # first call: workspaces, preconditioner set-up
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = fn()
+            return time.perf_counter() - t0, r
+        t64, (_, hist64, it64, rr64, code64) = timed(lambda: op.gmres(b, max_iter=args.max_iter, tol=1e-8))
         op.enable_f32()
         ms32, m2l32 = op.time_matvec(warmup=3, iters=max(5, args.steps), precision=ls.LS_PREC_F32)
-        t0 = time.perf_counter()
-        _, histm, nmv, rrm, codem = op.gmres_mixed(b, max_outer=20, inner_iter=args.max_iter, tol=1e-8)
-        tm = time.perf_counter() - t0
+        tm, (_, histm, nmv, rrm, codem) = timed(
+            lambda: op.gmres_mixed(b, max_outer=20, inner_iter=args.max_iter, tol=1e-8))
         solve = {"tol": 1e-8, "fp64_gmres_s": t64, "fp64_iters": it64, "fp64_true_residual": rr64,
                  "fp64_converged": code64 == 0, "mixed_s": tm, "mixed_matvecs": nmv, "mixed_true_residual": rrm,
                  "mixed_converged": codem == 0, "speedup_mixed_vs_fp64": t64 / tm if tm > 0 else None,
                  "f32_matvec_per_s": 1e3 / ms32, "f32_m2l_ms": m2l32}
+        # The learned preconditioner: mixed-precision flexible GMRES with the
+        # trained spectral neural operator as initial guess and right
+        # preconditioner (the BASELINE metric's NN-FGMRES leg).
+        if not args.no_nn and os.path.exists(FNO_WEIGHTS):
+            net = ls.FNO.load(FNO_WEIGHTS, device=local)
+            nn = {"weights": os.path.relpath(FNO_WEIGHTS, ROOT), "params": net.n_params}
+            for name, flags in (("nn", ls.LS_NN_GUESS | ls.LS_NN_PRECOND), ("nn_guess_only", ls.LS_NN_GUESS),
+                                ("nn_precond_only", ls.LS_NN_PRECOND)):
+                tn, (_, hn, rep, coden) = timed(
+                    lambda: op.fgmres_nn(net, b, flags=flags, max_outer=20, inner_iter=args.max_iter, tol=1e-8))
+                nn[name] = {"s": tn, "converged": coden == 0, "true_residual": rep["rel_residual"],
+                            "fp32_applies_and_fp64_products": rep["n_matvec"], "network_applies": rep["n_precond"],
+                            "guess_residual": rep["guess_residual"], "fell_back": bool(rep["fell_back"]),
+                            "history": [float(v) for v in hn]}
+            nn["speedup_nn_vs_fp64"] = t64 / nn["nn"]["s"]
+            nn["speedup_nn_vs_mixed"] = tm / nn["nn"]["s"]
+            solve["nn_fgmres"] = nn
+            net.close()
     # Many incidence directions on the scatterer (64 plane waves): the
     # batched mixed-precision solve against the same solves one at a time.
     batch = None
@@ -377,6 +401,33 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_fno_forward(args):
+    """Times `args.fno_forward` batch-1 forward passes of the trained
+    network (the preconditioner's unit of work) with CUDA events; one JSON
+    line. Also the command that the network's ncu launch lists profile."""
+    import torch
+
+    import lippmann_schwinger_solver_gb300 as ls
+    net = ls.FNO.load(FNO_WEIGHTS)
+    G = net.shape["grid"]
+    st = torch.cuda.current_stream().cuda_stream
+    x = torch.randn(1, G * G, ls.FNO_IN_CHANNELS, device="cuda")
+    o = torch.empty(1, G * G, ls.FNO_OUT_CHANNELS, device="cuda")
+    for _ in range(2):
+        net.forward_device(1, x.data_ptr(), o.data_ptr(), stream=st)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.fno_forward):
+        net.forward_device(1, x.data_ptr(), o.data_ptr(), stream=st)
+    b.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"metric": "spectral neural operator forward, batch 1", "unit": "ms",
+                      "value": a.elapsed_time(b) / args.fno_forward, "passes": args.fno_forward,
+                      "grid": G, "params": net.n_params}), flush=True)
+    net.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,6 +439,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the many-direction batched solve")
+    ap.add_argument("--no-nn", action="store_true", help="skip the learned-preconditioner solve")
     ap.add_argument("--angles", type=int, default=64, help="incidence directions of the batched solve")
     ap.add_argument("--max-iter", type=int, default=400)
     ap.add_argument("--f64-kernels", default="native", choices=["native", "double-float"],
@@ -395,8 +447,12 @@ def main():
                          "error-free transformations (same operator)")
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"],
                     help="operator precision of the timed loop (f32: profiling run of the FP32 operator)")
+    ap.add_argument("--fno-forward", type=int, default=0,
+                    help="only time this many batch-1 forward passes of the trained network")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.fno_forward > 0:
+        run_fno_forward(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

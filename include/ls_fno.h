@@ -105,9 +105,11 @@ typedef struct {
  * inner FP32 flexible GMRES on the FP32 operator, right-preconditioned by
  * the net (flags & LS_NN_PRECOND), starting from net(b) (flags &
  * LS_NN_GUESS). The stopping test is always the FP64 true residual. The net
- * is dropped, returning the solve to plain GMRES, when an outer step (at
- * most 16 preconditioned inner steps) does not halve the residual; a guess
- * worse than x0 = 0 is discarded.
+ * preconditions only outer steps that must reduce the residual by more than
+ * 1e3 (looser targets take a few plain steps, cheaper than network
+ * applications); it is dropped, returning the solve to plain GMRES, when
+ * an outer step (at most 24 preconditioned inner steps) does not halve the
+ * residual; a guess worse than x0 = 0 is discarded.
  * With flags = 0 this is ls_gmres_mixed. b, x: host, N complex. history
  * (max_outer + 2 entries, may be NULL) gets the FP64 residual after the
  * guess and after each outer step. Needs ls_op_enable_f32(); net and

@@ -146,10 +146,11 @@ struct FlexReport {
 };
 // dev_gmres_mixed with flexible inner GMRES right-preconditioned by M (may be
 // null), starting from x0 = guess(b) when guess is given (kept only if it
-// beats x0 = 0). The residual is the FP64 one throughout. M is turned off
-// for the remaining steps, so that the solve ends as plain dev_gmres_mixed
-// would, when an outer step (at most 16 preconditioned inner steps) did not
-// halve the residual.
+// beats x0 = 0). The residual is the FP64 one throughout. M is used only in
+// outer steps whose inner target is a reduction below 1e-3 (looser ones
+// take a few plain steps), and it is turned off for the remaining steps,
+// so that the solve ends as plain dev_gmres_mixed would, when an outer step
+// (at most 24 preconditioned inner steps) did not halve the residual.
 cudaError_t dev_gmres_mixed_flex(DevOperator& d, const double2* b, double2* x, Precond32* M, Precond32* guess,
                                  int max_outer, int inner, double tol, std::vector<double>& hist, FlexReport& rep,
                                  double& relres);

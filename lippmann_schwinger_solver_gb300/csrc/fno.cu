@@ -77,7 +77,10 @@ __global__ void r2c_kernel(int G, int M, int scaled, const float* __restrict__ x
   for (int i = threadIdx.x; i < G; i += blockDim.x) ts[i] = tw[i];
   __syncthreads();
   const int c = threadIdx.x & 31;
-  for (int ky = threadIdx.x >> 5; ky < M; ky += blockDim.x >> 5) {
+  // The kept ky are split over gridDim.y blocks (small batches fill the GPU).
+  const int k_lo = (int)(((long long)blockIdx.y * M) / gridDim.y);
+  const int k_hi = (int)(((long long)(blockIdx.y + 1) * M) / gridDim.y);
+  for (int ky = k_lo + (threadIdx.x >> 5); ky < k_hi; ky += blockDim.x >> 5) {
     float ar = 0.f, ai = 0.f;
     for (int y = 0; y < G; ++y) {
       const float2 t = ts[(ky * y) & (G - 1)];
@@ -197,7 +200,11 @@ __global__ void c2r_kernel(int G, int M, int fwd, const float2* __restrict__ Gin
   float2* gs = reinterpret_cast<float2*>(smf + G * 32);   // [M][32]
   float2* ts = gs + M * 32;                               // [G]
   const long long r = blockIdx.x;
-  for (int i = threadIdx.x; i < G * 32; i += blockDim.x) hs[i] = hin[r * G * 32 + i];
+  // The outputs y of the row are split over gridDim.y blocks; each stages
+  // only its own rows of hin.
+  const int y_lo = (int)(((long long)blockIdx.y * G) / gridDim.y);
+  const int y_hi = (int)(((long long)(blockIdx.y + 1) * G) / gridDim.y);
+  for (int i = threadIdx.x; i < (y_hi - y_lo) * 32; i += blockDim.x) hs[i] = hin[(r * G + y_lo) * 32 + i];
   for (int i = threadIdx.x; i < M * 32; i += blockDim.x) {
     float2 g = Gin[r * M * 32 + i];
     if (fwd) {
@@ -216,14 +223,14 @@ __global__ void c2r_kernel(int G, int M, int fwd, const float2* __restrict__ Gin
   __syncthreads();
   const int c = threadIdx.x & 31;
   const float bc = bias ? bias[c] : 0.f;
-  for (int y = threadIdx.x >> 5; y < G; y += blockDim.x >> 5) {
+  for (int y = y_lo + (threadIdx.x >> 5); y < y_hi; y += blockDim.x >> 5) {
     float acc = bc;
     for (int ky = 0; ky < M; ++ky) {
       const float2 t = ts[(ky * y) & (G - 1)];
       const float2 g = gs[ky * 32 + c];
       acc = fmaf(t.x, g.x, fmaf(-t.y, g.y, acc));
     }
-    const float* hr = hs + y * 32;
+    const float* hr = hs + (y - y_lo) * 32;
 #pragma unroll 8
     for (int i = 0; i < 32; ++i) acc = fmaf(ps[c][i], hr[i], acc);
     const long long o = (r * G + y) * 32 + c;
@@ -507,6 +514,13 @@ int wgrad_blocks(long long P) { return (int)std::min<long long>((P + kWgradChunk
 // Blocks per (sample, ky) of the x-DFT: a batch of one has only M blocks,
 // so their outputs are split to put about two blocks on every SM.
 dim3 xdft_grid(int B, int M) { return dim3((unsigned)(B * M), (unsigned)std::max(1, std::min(8, 304 / (B * M)))); }
+// Rows of the y-transforms (B G of them) split in the same way.
+dim3 row_grid(int B, int G, int most) {
+  return dim3((unsigned)(B * G), (unsigned)std::max(1, std::min(most, 608 / (B * G))));
+}
+// Blocks of the projection kernels: at least 8 points per warp, so that
+// each block's copy of the projection weights serves many points.
+unsigned proj_blocks(long long P) { return (unsigned)std::min<long long>((P + 63) / 64, 152LL * 8); }
 
 }  // namespace
 
@@ -600,6 +614,7 @@ void FnoNet::release() {
   H1 = O = G1 = nullptr;
   u = out = dout = dz = dh0 = dh1 = du = sums = nullptr;
   cap = 0;
+  ++generation;
   cudaFree(params); cudaFree(grads); cudaFree(adam_m); cudaFree(adam_v); cudaFree(tw); cudaFree(loss);
   params = grads = adam_m = adam_v = loss = nullptr;
   tw = nullptr;
@@ -607,6 +622,7 @@ void FnoNet::release() {
 
 cudaError_t FnoNet::ensure(int batch) {
   if (batch <= cap) return cudaSuccess;
+  ++generation;
   for (float* p : h) cudaFree(p);
   for (float* p : z) cudaFree(p);
   for (float2* p : H2) cudaFree(p);
@@ -655,16 +671,17 @@ cudaError_t FnoNet::forward(int B, const float* in, float* outp, const float* ss
   const size_t sm_xa = (size_t)G * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const size_t sm_xs = (size_t)2 * M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const size_t sm_c2r = (size_t)G * 32 * sizeof(float) + (size_t)M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
-  const int r2c_threads = 32 * std::min(M, 32);
+  const dim3 rg = row_grid(B, G, 2);
+  const int r2c_threads = 32 * std::min(32, (M + (int)rg.y - 1) / (int)rg.y);
   for (int l = 0; l < L; ++l) {
-    r2c_kernel<<<(unsigned)(B * G), r2c_threads, sm_r2c, s>>>(G, M, 0, h[l], nullptr, nullptr, tw, H1);
+    r2c_kernel<<<rg, r2c_threads, sm_r2c, s>>>(G, M, 0, h[l], nullptr, nullptr, tw, H1);
     xdft_kernel<<<xdft_grid(B, M), 256, sm_xa, s>>>(G, M, 1, H1, tw, H2[l]);
     mix_kernel<<<(unsigned)NM, 256, (size_t)B * 32 * sizeof(float2), s>>>(B, NM, 0, H2[l], reinterpret_cast<const float2*>(w + lay.spec[l]), O);
     xdft_kernel<<<xdft_grid(B, M), 256, sm_xs, s>>>(G, M, 0, O, tw, G1);
-    c2r_kernel<<<(unsigned)(B * G), 512, sm_c2r, s>>>(G, M, 1, G1, tw, h[l], w + lay.pw_w[l], w + lay.pw_b[l], z[l], h[l + 1], l + 1 < L ? 1 : 0);
+    c2r_kernel<<<row_grid(B, G, 4), 512, sm_c2r, s>>>(G, M, 1, G1, tw, h[l], w + lay.pw_w[l], w + lay.pw_b[l], z[l], h[l + 1], l + 1 < L ? 1 : 0);
     launches += 5;
   }
-  const unsigned pblocks = (unsigned)std::min<long long>((P + 7) / 8, 152LL * 16);
+  const unsigned pblocks = proj_blocks(P);
   proj_kernel<<<pblocks, 256, 0, s>>>(P, shape.proj, (int)GG, h[L], w + lay.p1_w, w + lay.p1_b, w + lay.p2_w, w + lay.p2_b, ssq, ssq ? nullptr : u, outp);
   ++launches;
   return cudaGetLastError();
@@ -686,7 +703,7 @@ cudaError_t FnoNet::loss_grad(int B, const float* in, const float* target, cudaS
   loss_sums_kernel<<<dim3((unsigned)std::min<long long>((n_per + 255) / 256, 64), (unsigned)B), 256, 0, s>>>(n_per, out, target, sums);
   loss_grad_kernel<<<(unsigned)std::min<long long>((B * n_per + 255) / 256, 152LL * 8), 256, 0, s>>>(B, n_per, out, target, sums, dout, loss);
   // Projection.
-  const unsigned pblocks = (unsigned)std::min<long long>((P + 7) / 8, 152LL * 16);
+  const unsigned pblocks = proj_blocks(P);
   const unsigned wb = (unsigned)wgrad_blocks(P);
   proj_bwd_kernel<<<pblocks, 256, 0, s>>>(P, PW, u, dout, w + lay.p1_w, w + lay.p2_w, du, dh0);
   wgrad_kernel<<<wb, 1024, 0, s>>>(P, kFnoOut, PW, dout, u, 1, gw + lay.p2_w, gw + lay.p2_b);
@@ -696,7 +713,8 @@ cudaError_t FnoNet::loss_grad(int B, const float* in, const float* target, cudaS
   const size_t sm_xa = (size_t)G * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const size_t sm_xs = (size_t)2 * M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const size_t sm_c2r = (size_t)G * 32 * sizeof(float) + (size_t)M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
-  const int r2c_threads = 32 * std::min(M, 32);
+  const dim3 rg = row_grid(B, G, 2);
+  const int r2c_threads = 32 * std::min(32, (M + (int)rg.y - 1) / (int)rg.y);
   float* dhA = dh0;
   float* dhB = dh1;
   for (int l = L - 1; l >= 0; --l) {
@@ -704,10 +722,10 @@ cudaError_t FnoNet::loss_grad(int B, const float* in, const float* target, cudaS
     // adjoint; the last layer has no activation), then dG1 = c2r^T dz.
     const float* dzl;
     if (l + 1 < L) {
-      r2c_kernel<<<(unsigned)(B * G), r2c_threads, sm_r2c, s>>>(G, M, 1, dhA, z[l], dz, tw, H1);
+      r2c_kernel<<<rg, r2c_threads, sm_r2c, s>>>(G, M, 1, dhA, z[l], dz, tw, H1);
       dzl = dz;
     } else {
-      r2c_kernel<<<(unsigned)(B * G), r2c_threads, sm_r2c, s>>>(G, M, 1, dhA, nullptr, nullptr, tw, H1);
+      r2c_kernel<<<rg, r2c_threads, sm_r2c, s>>>(G, M, 1, dhA, nullptr, nullptr, tw, H1);
       dzl = dhA;
     }
     wgrad_kernel<<<wb, 1024, 0, s>>>(P, kFnoWidth, kFnoWidth, dzl, h[l], 0, gw + lay.pw_w[l], gw + lay.pw_b[l]);
@@ -716,7 +734,7 @@ cudaError_t FnoNet::loss_grad(int B, const float* in, const float* target, cudaS
     mix_kernel<<<(unsigned)NM, 256, (size_t)B * 32 * sizeof(float2), s>>>(B, NM, 1, O, reinterpret_cast<const float2*>(w + lay.spec[l]), H2[l]);  // dH2 (H2[l] no longer needed)
     xdft_kernel<<<xdft_grid(B, M), 256, sm_xs, s>>>(G, M, 0, H2[l], tw, G1);  // dH1 = dft_x^T dH2
     // dh[l] = r2c^T dH1 + Wpw^T dz
-    c2r_kernel<<<(unsigned)(B * G), 512, sm_c2r, s>>>(G, M, 0, G1, tw, dzl, w + lay.pw_w[l], nullptr, nullptr, dhB, 0);
+    c2r_kernel<<<row_grid(B, G, 4), 512, sm_c2r, s>>>(G, M, 0, G1, tw, dzl, w + lay.pw_w[l], nullptr, nullptr, dhB, 0);
     std::swap(dhA, dhB);
   }
   wgrad_kernel<<<wb, 1024, 0, s>>>(P, kFnoWidth, kFnoIn, dhA, in, 0, gw + lay.lift_w, gw + lay.lift_b);

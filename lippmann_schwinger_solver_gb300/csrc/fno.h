@@ -55,8 +55,10 @@ struct FnoNet {
   float* adam_v = nullptr;
   int adam_t = 0;
   float2* tw = nullptr;  // cos/sin(2 pi k / G), k < G
-  // Activations and gradients for up to `cap` samples.
+  // Activations and gradients for up to `cap` samples; `generation` counts
+  // their reallocations (a captured launch sequence is valid for one).
   int cap = 0;
+  unsigned long long generation = 0;
   std::vector<float*> h;  // layers + 1 inputs/outputs of the Fourier layers, [P][32]
   std::vector<float*> z;  // pre-activations, [P][32]
   std::vector<float2*> H2;// spectral inputs of each layer, [B][2M*M][32]

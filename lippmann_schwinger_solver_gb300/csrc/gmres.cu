@@ -33,7 +33,11 @@ namespace lsg {
 constexpr int kDotThreads = 128;
 constexpr int kDotBlocks = 304;  // row chunks: partial sums per column (2 per SM)
 constexpr int kDotCols = 8;      // columns per multi-dot block
-constexpr int kFlexInner = 16;   // steps of a right-preconditioned inner cycle
+constexpr int kFlexInner = 24;   // steps of a right-preconditioned inner cycle
+// Inner targets at or above this relative reduction are left to plain
+// GMRES: a few unpreconditioned steps reach them for less than the
+// network's applications would cost.
+constexpr double kFlexPlainTol = 1e-3;
 
 template <class T> struct Cx;
 template <> struct Cx<double2> {
@@ -605,12 +609,12 @@ cudaError_t dev_gmres_mixed_flex(DevOperator& d, const double2* b, double2* x, P
   for (int o = 0; o < max_outer && relres > tol; ++o) {
     int it = 0;
     bool conv = false;
-    Precond32* Mo = rep.fell_back ? nullptr : M;
     // Inner solve to roughly the FP32 operator accuracy. A preconditioned
     // cycle is capped at kFlexInner steps: a useful M converges well within
     // them, and a useless one costs no more than that before the outer test
     // below drops it.
     const double inner_tol = std::max(tol / std::max(relres, 1e-300), 1e-6);
+    Precond32* Mo = (rep.fell_back || inner_tol >= kFlexPlainTol) ? nullptr : M;
     const int m_inner = Mo ? std::min(inner, kFlexInner) : inner;
     launch_pdl(to_f32_kernel, grid_for(n), 256, 0, d.stream, r, ws.res32, n);
     if ((e = arnoldi_cycle<float2>(d, ws, ws.res32, nullptr, ws.dx32, m_inner, inner_tol, 1e-300,

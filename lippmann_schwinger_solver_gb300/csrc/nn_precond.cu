@@ -229,6 +229,8 @@ bool NnPrecond::init(const HostOperator& h, FnoNet* n, std::string& err) {
 }
 
 void NnPrecond::release() {
+  if (fwd) cudaGraphExecDestroy(fwd);
+  fwd = nullptr;
   gs.release();
   cudaFree(nodes);
   cudaFree(in);
@@ -239,12 +241,43 @@ void NnPrecond::release() {
   N = 0;
 }
 
+cudaError_t NnPrecond::capture() {
+  if (fwd) cudaGraphExecDestroy(fwd);
+  fwd = nullptr;
+  cudaError_t e = net->ensure(1);  // no allocation may happen while capturing
+  if (e != cudaSuccess) return e;
+  cudaStream_t cs = nullptr;
+  if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  cudaGraph_t g = nullptr;
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    const cudaError_t fe = net->forward(1, in, out, ssq, cs);
+    e = cudaStreamEndCapture(cs, &g);
+    if (fe != cudaSuccess) e = fe;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&fwd, g, 0);
+  if (g) cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    fwd = nullptr;
+    cudaGetLastError();
+    return e;
+  }
+  fwd_generation = net->generation;
+  return cudaSuccess;
+}
+
 cudaError_t NnPrecond::apply(const float2* v, float2* z, cudaStream_t s) {
   const int G = gs.G, GG = G * G;
   cudaError_t e;
   // ssq is zero here: set at init and cleared by the last kernel of every application.
   nodes_to_grid_kernel<float2><<<dim3((unsigned)((GG + 255) / 256), 1), 256, 0, s>>>(GG, gs.rank, gs.w, gs.leaf, v, 0, in, kFnoIn, 1, 0, ssq);
-  if ((e = net->forward(1, in, out, ssq, s)) != cudaSuccess) return e;
+  if (!fwd || fwd_generation != net->generation || net->cap < 1) capture();
+  if (fwd && fwd_generation == net->generation) {
+    if ((e = cudaGraphLaunch(fwd, s)) != cudaSuccess) return e;
+  } else if ((e = net->forward(1, in, out, ssq, s)) != cudaSuccess) {
+    return e;
+  }
   grid_to_nodes_kernel<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(N, G, nodes, out, v, z, ssq);
   ++applies;
   return cudaGetLastError();

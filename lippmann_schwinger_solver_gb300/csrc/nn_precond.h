@@ -53,6 +53,12 @@ struct NnPrecond : Precond32 {
   float* out = nullptr;     // [G*G][2]
   float* ssq = nullptr;     // |sampled field|^2
   int applies = 0;
+  // The network's forward pass on (in, out) captured once as a CUDA graph
+  // and replayed by every application (its ~22 launches cost more than
+  // their kernels for one sample); recaptured when the net's buffers move.
+  cudaGraphExec_t fwd = nullptr;
+  unsigned long long fwd_generation = 0;
+  cudaError_t capture();
   bool init(const HostOperator& h, FnoNet* net, std::string& err);
   void release();
   cudaError_t apply(const float2* v, float2* z, cudaStream_t s) override;

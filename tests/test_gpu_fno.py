@@ -7,6 +7,8 @@ initial guess recomputed from the oracle's network and resampling).
 Tolerances: the kernels compute in FP32 and the oracle in FP64; relative L2
 1e-5 for the forward pass and 1e-4 per gradient group (sums over 2 x 128^2
 points with float atomics)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -204,4 +206,37 @@ def test_initial_guess_matches_oracle_composition(ls):
     else:  # a guess worse than zero is discarded
         assert hist[0] == 1.0 and rep["guess_residual"] >= 1.0
     op.close()
+    net.close()
+
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "lippmann_schwinger_solver_gb300",
+                       "weights", "fno_k10_40.lsfno")
+
+
+@pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained network weights")
+def test_trained_network_gain_over_plain_mixed_gmres(ls):
+    """What the trained network gains over the method without it, on
+    scatterers it was not trained on (kappa and bumps drawn with another
+    seed): the preconditioned solve reaches the same FP64 tolerance with
+    fewer FP32 operator applies, and its initial guess beats x0 = 0."""
+    from lippmann_schwinger_solver_gb300 import fno_train as ft
+    net = ls.FNO.load(WEIGHTS)
+    rng = np.random.default_rng(4242)
+    plain_total = nn_total = 0
+    for trial in range(3):
+        kappa, bumps = ft.scatterer(rng)
+        op = ls.Operator(ft.operator_config(kappa, bumps, 4, 8), device=0)
+        op.enable_f32()
+        b = op.rhs_angles([0.3])[:, 0]
+        _, _, n_plain, rr_plain, c_plain = op.gmres_mixed(b, max_outer=12, inner_iter=100, tol=1e-8)
+        x, hist, rep, code = op.fgmres_nn(net, b, flags=ls.LS_NN_GUESS | ls.LS_NN_PRECOND, max_outer=12,
+                                          inner_iter=100, tol=1e-8)
+        assert c_plain == ls.LS_OK and code == ls.LS_OK
+        r = b - op.matvec(x)
+        assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.5e-8
+        assert rep["guess_residual"] < 1.0 and not rep["fell_back"]
+        plain_total += n_plain
+        nn_total += rep["n_matvec"]
+        op.close()
+    assert nn_total <= 0.7 * plain_total, (nn_total, plain_total)
     net.close()
