@@ -34,6 +34,9 @@ namespace lsg {
 namespace {
 
 constexpr int kWgradChunk = 32;  // points staged per step of the weight-gradient reduction
+constexpr int kXWarps = 8;       // warps of an x-DFT block (the input sum is split over them)
+constexpr int kXOut = 16;        // most outputs of one x-DFT block (accumulators per lane)
+constexpr int kC2rRows = 4;      // y rows per warp step of the c2r synthesis
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float x) {
@@ -93,40 +96,60 @@ __global__ void r2c_kernel(int G, int M, int scaled, const float* __restrict__ x
   }
 }
 
-// Along x for one (sample, ky); kept frequency of mode m: m < M ? m : G - 2M + m.
+// Along x for one (sample, ky) and one chunk of outputs (blockIdx.y); the
+// kept frequency of mode m is m < M ? m : G - 2M + m.
 // analysis:  out[b][m][ky][c] = sum_x e^{-2 pi i f_m x / G} in[b][x][ky][c]
 // synthesis: out[b][x][ky][c] = sum_m e^{+2 pi i f_m x / G} in[b][m][ky][c]
-__global__ void xdft_kernel(int G, int M, int analysis, const float2* __restrict__ in,
-                            const float2* __restrict__ tw, float2* __restrict__ out) {
-  extern __shared__ float2 smc[];
+// The sum over inputs is split over the block's warps: each warp reads its
+// own input rows (one coalesced 256-byte row per step) and keeps one
+// accumulator pair per output of the chunk, so its FMA chains are
+// independent; the warps' partial sums are added in shared memory.
+__global__ void __launch_bounds__(kXWarps * 32) xdft_kernel(int G, int M, int analysis, const float2* __restrict__ in,
+                                                            const float2* __restrict__ tw, float2* __restrict__ out) {
+  __shared__ float2 ts[256];
+  __shared__ float2 part[kXWarps][kXOut][32];
   const int NI = analysis ? G : 2 * M, NO = analysis ? 2 * M : G;
-  float2* ins = smc;            // [NI][32]
-  float2* ts = smc + NI * 32;   // [G]
   const int b = blockIdx.x / M, ky = blockIdx.x - b * M;
-  for (int i = threadIdx.x; i < NI * 32; i += blockDim.x) {
-    const int j = i >> 5, c = i & 31;
-    ins[i] = in[(((long long)b * NI + j) * M + ky) * 32 + c];
-  }
+  const int oc = (NO + gridDim.y - 1) / gridDim.y;
+  const int o_lo = blockIdx.y * oc;
+  const int no = min(oc, NO - o_lo);
+  if (no <= 0) return;  // block-uniform
   for (int i = threadIdx.x; i < G; i += blockDim.x) ts[i] = tw[i];
   __syncthreads();
-  const int c = threadIdx.x & 31;
+  const int c = threadIdx.x & 31, w = threadIdx.x >> 5;
   const float sg = analysis ? -1.f : 1.f;
-  // Outputs split over gridDim.y blocks (small batches fill the GPU).
-  const int o_lo = (int)(((long long)blockIdx.y * NO) / gridDim.y);
-  const int o_hi = (int)(((long long)(blockIdx.y + 1) * NO) / gridDim.y);
-  for (int o = o_lo + (threadIdx.x >> 5); o < o_hi; o += blockDim.x >> 5) {
-    float ar = 0.f, ai = 0.f;
-    for (int j = 0; j < NI; ++j) {
-      const int xx = analysis ? j : o;
-      const int m = analysis ? o : j;
-      const int f = m < M ? m : G - 2 * M + m;
-      const float2 t = ts[(f * xx) & (G - 1)];
-      const float ti = sg * t.y;
-      const float2 v = ins[j * 32 + c];
-      ar = fmaf(t.x, v.x, fmaf(-ti, v.y, ar));
-      ai = fmaf(t.x, v.y, fmaf(ti, v.x, ai));
+  float ar[kXOut], ai[kXOut];
+#pragma unroll
+  for (int k = 0; k < kXOut; ++k) ar[k] = ai[k] = 0.f;
+  const int j_lo = (w * NI) / kXWarps, j_hi = ((w + 1) * NI) / kXWarps;
+#pragma unroll 2
+  for (int j = j_lo; j < j_hi; ++j) {
+    const float2 v = in[(((long long)b * NI + j) * M + ky) * 32 + c];
+#pragma unroll
+    for (int k = 0; k < kXOut; ++k) {
+      if (k < no) {
+        const int o = o_lo + k;
+        const int m = analysis ? o : j;
+        const int f = m < M ? m : G - 2 * M + m;
+        const float2 t = ts[(f * (analysis ? j : o)) & (G - 1)];
+        const float ti = sg * t.y;
+        ar[k] = fmaf(t.x, v.x, fmaf(-ti, v.y, ar[k]));
+        ai[k] = fmaf(t.x, v.y, fmaf(ti, v.x, ai[k]));
+      }
     }
-    out[(((long long)b * NO + o) * M + ky) * 32 + c] = make_float2(ar, ai);
+  }
+#pragma unroll
+  for (int k = 0; k < kXOut; ++k)
+    if (k < no) part[w][k][c] = make_float2(ar[k], ai[k]);
+  __syncthreads();
+  for (int i = threadIdx.x; i < no * 32; i += blockDim.x) {
+    const int k = i >> 5, cc = i & 31;
+    float2 acc = part[0][k][cc];
+    for (int ww = 1; ww < kXWarps; ++ww) {
+      acc.x += part[ww][k][cc].x;
+      acc.y += part[ww][k][cc].y;
+    }
+    out[(((long long)b * NO + o_lo + k) * M + ky) * 32 + cc] = acc;
   }
 }
 
@@ -223,19 +246,38 @@ __global__ void c2r_kernel(int G, int M, int fwd, const float2* __restrict__ Gin
   __syncthreads();
   const int c = threadIdx.x & 31;
   const float bc = bias ? bias[c] : 0.f;
-  for (int y = y_lo + (threadIdx.x >> 5); y < y_hi; y += blockDim.x >> 5) {
-    float acc = bc;
+  // Each warp step produces kC2rRows rows: every spectral coefficient and
+  // pointwise weight read from shared memory serves that many outputs.
+  const int step = (blockDim.x >> 5) * kC2rRows;
+  for (int y0 = y_lo + (threadIdx.x >> 5) * kC2rRows; y0 < y_hi; y0 += step) {
+    float acc[kC2rRows];
+#pragma unroll
+    for (int q = 0; q < kC2rRows; ++q) acc[q] = bc;
     for (int ky = 0; ky < M; ++ky) {
-      const float2 t = ts[(ky * y) & (G - 1)];
       const float2 g = gs[ky * 32 + c];
-      acc = fmaf(t.x, g.x, fmaf(-t.y, g.y, acc));
+#pragma unroll
+      for (int q = 0; q < kC2rRows; ++q) {
+        const float2 t = ts[(ky * (y0 + q)) & (G - 1)];
+        acc[q] = fmaf(t.x, g.x, fmaf(-t.y, g.y, acc[q]));
+      }
     }
-    const float* hr = hs + (y - y_lo) * 32;
 #pragma unroll 8
-    for (int i = 0; i < 32; ++i) acc = fmaf(ps[c][i], hr[i], acc);
-    const long long o = (r * G + y) * 32 + c;
-    if (z_out) z_out[o] = acc;
-    h_out[o] = act ? gelu(acc) : acc;
+    for (int i = 0; i < 32; ++i) {
+      const float pc = ps[c][i];
+#pragma unroll
+      for (int q = 0; q < kC2rRows; ++q) {
+        const int yy = min(y0 + q, y_hi - 1) - y_lo;
+        acc[q] = fmaf(pc, hs[yy * 32 + i], acc[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kC2rRows; ++q) {
+      if (y0 + q < y_hi) {
+        const long long o = (r * G + y0 + q) * 32 + c;
+        if (z_out) z_out[o] = acc[q];
+        h_out[o] = act ? gelu(acc[q]) : acc[q];
+      }
+    }
   }
 }
 
@@ -511,9 +553,13 @@ struct Rng {
 
 int wgrad_blocks(long long P) { return (int)std::min<long long>((P + kWgradChunk - 1) / kWgradChunk, 152 * 2); }
 
-// Blocks per (sample, ky) of the x-DFT: a batch of one has only M blocks,
-// so their outputs are split to put about two blocks on every SM.
-dim3 xdft_grid(int B, int M) { return dim3((unsigned)(B * M), (unsigned)std::max(1, std::min(8, 304 / (B * M)))); }
+// Blocks per (sample, ky) of the x-DFT: at least enough output chunks for
+// kXOut accumulators, and for a batch of one (only M blocks otherwise)
+// enough to put about two blocks on every SM.
+dim3 xdft_grid(int B, int M, int NO) {
+  const int need = (NO + kXOut - 1) / kXOut;
+  return dim3((unsigned)(B * M), (unsigned)std::max(need, std::min(NO, 304 / (B * M))));
+}
 // Rows of the y-transforms (B G of them) split in the same way.
 dim3 row_grid(int B, int G, int most) {
   return dim3((unsigned)(B * G), (unsigned)std::max(1, std::min(most, 608 / (B * G))));
@@ -668,17 +714,15 @@ cudaError_t FnoNet::forward(int B, const float* in, float* outp, const float* ss
   lift_kernel<<<(unsigned)((P * kFnoWidth + 255) / 256), 256, 0, s>>>(P, (int)GG, in, w + lay.lift_w, w + lay.lift_b, ssq, h[0]);
   ++launches;
   const size_t sm_r2c = (size_t)G * 32 * sizeof(float) + (size_t)G * sizeof(float2);
-  const size_t sm_xa = (size_t)G * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
-  const size_t sm_xs = (size_t)2 * M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const size_t sm_c2r = (size_t)G * 32 * sizeof(float) + (size_t)M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const dim3 rg = row_grid(B, G, 2);
   const int r2c_threads = 32 * std::min(32, (M + (int)rg.y - 1) / (int)rg.y);
   for (int l = 0; l < L; ++l) {
     r2c_kernel<<<rg, r2c_threads, sm_r2c, s>>>(G, M, 0, h[l], nullptr, nullptr, tw, H1);
-    xdft_kernel<<<xdft_grid(B, M), 256, sm_xa, s>>>(G, M, 1, H1, tw, H2[l]);
+    xdft_kernel<<<xdft_grid(B, M, 2 * M), kXWarps * 32, 0, s>>>(G, M, 1, H1, tw, H2[l]);
     mix_kernel<<<(unsigned)NM, 256, (size_t)B * 32 * sizeof(float2), s>>>(B, NM, 0, H2[l], reinterpret_cast<const float2*>(w + lay.spec[l]), O);
-    xdft_kernel<<<xdft_grid(B, M), 256, sm_xs, s>>>(G, M, 0, O, tw, G1);
-    c2r_kernel<<<row_grid(B, G, 4), 512, sm_c2r, s>>>(G, M, 1, G1, tw, h[l], w + lay.pw_w[l], w + lay.pw_b[l], z[l], h[l + 1], l + 1 < L ? 1 : 0);
+    xdft_kernel<<<xdft_grid(B, M, G), kXWarps * 32, 0, s>>>(G, M, 0, O, tw, G1);
+    c2r_kernel<<<row_grid(B, G, 4), 256, sm_c2r, s>>>(G, M, 1, G1, tw, h[l], w + lay.pw_w[l], w + lay.pw_b[l], z[l], h[l + 1], l + 1 < L ? 1 : 0);
     launches += 5;
   }
   const unsigned pblocks = proj_blocks(P);
@@ -710,8 +754,6 @@ cudaError_t FnoNet::loss_grad(int B, const float* in, const float* target, cudaS
   wgrad_kernel<<<wb, 1024, 0, s>>>(P, PW, kFnoWidth, du, h[L], 0, gw + lay.p1_w, gw + lay.p1_b);
   // Fourier layers, last to first. dhA = dL/dh[l + 1] on entry.
   const size_t sm_r2c = (size_t)G * 32 * sizeof(float) + (size_t)G * sizeof(float2);
-  const size_t sm_xa = (size_t)G * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
-  const size_t sm_xs = (size_t)2 * M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const size_t sm_c2r = (size_t)G * 32 * sizeof(float) + (size_t)M * 32 * sizeof(float2) + (size_t)G * sizeof(float2);
   const dim3 rg = row_grid(B, G, 2);
   const int r2c_threads = 32 * std::min(32, (M + (int)rg.y - 1) / (int)rg.y);
@@ -729,12 +771,12 @@ cudaError_t FnoNet::loss_grad(int B, const float* in, const float* target, cudaS
       dzl = dhA;
     }
     wgrad_kernel<<<wb, 1024, 0, s>>>(P, kFnoWidth, kFnoWidth, dzl, h[l], 0, gw + lay.pw_w[l], gw + lay.pw_b[l]);
-    xdft_kernel<<<xdft_grid(B, M), 256, sm_xa, s>>>(G, M, 1, H1, tw, O);  // dO = idft_x^T dG1
+    xdft_kernel<<<xdft_grid(B, M, 2 * M), kXWarps * 32, 0, s>>>(G, M, 1, H1, tw, O);  // dO = idft_x^T dG1
     mix_wgrad_kernel<<<(unsigned)NM, 256, (size_t)2 * B * 32 * sizeof(float2), s>>>(B, NM, H2[l], O, reinterpret_cast<float2*>(gw + lay.spec[l]));
     mix_kernel<<<(unsigned)NM, 256, (size_t)B * 32 * sizeof(float2), s>>>(B, NM, 1, O, reinterpret_cast<const float2*>(w + lay.spec[l]), H2[l]);  // dH2 (H2[l] no longer needed)
-    xdft_kernel<<<xdft_grid(B, M), 256, sm_xs, s>>>(G, M, 0, H2[l], tw, G1);  // dH1 = dft_x^T dH2
+    xdft_kernel<<<xdft_grid(B, M, G), kXWarps * 32, 0, s>>>(G, M, 0, H2[l], tw, G1);  // dH1 = dft_x^T dH2
     // dh[l] = r2c^T dH1 + Wpw^T dz
-    c2r_kernel<<<row_grid(B, G, 4), 512, sm_c2r, s>>>(G, M, 0, G1, tw, dzl, w + lay.pw_w[l], nullptr, nullptr, dhB, 0);
+    c2r_kernel<<<row_grid(B, G, 4), 256, sm_c2r, s>>>(G, M, 0, G1, tw, dzl, w + lay.pw_w[l], nullptr, nullptr, dhB, 0);
     std::swap(dhA, dhB);
   }
   wgrad_kernel<<<wb, 1024, 0, s>>>(P, kFnoWidth, kFnoIn, dhA, in, 0, gw + lay.lift_w, gw + lay.lift_b);
