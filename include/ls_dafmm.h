@@ -188,6 +188,23 @@ ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_o
 ls_status ls_time_matvec(ls_op* op, int precision, int warmup, int iters, float* ms_matvec,
                          float* ms_m2l);
 
+/*
+ * Density at arbitrary points by the reference's Chebyshev-Q+ interpolation
+ * (GMRES_Hybrid/LippmannSchwinger/main/hybridTrueValidation_gmres.cpp:
+ * 187-219, the "Psi_non_grid" loop): in the leaf that contains (x, y),
+ * c = Q^+ phi_leaf and psi = sum_l c_l T_a(l)(x') T_b(l)(y') with
+ * x' = (x - centre) / radius. Host buffers: xy (npts x 2), phi (N complex),
+ * psi (npts complex). Points outside [-L, L]^2 give LS_E_INVALID (the
+ * reference runs off the end of its leaf list there); points on the upper
+ * edges belong to the last leaf. Works for host-only operators.
+ */
+ls_status ls_op_interpolate(const ls_op* op, int npts, const double* xy, const double* phi, double* psi);
+
+/* Writes n complex values to `path`, one per line as "(re,im)" with six
+ * significant digits: the text of the reference's result files
+ * (GMRES/GMRES.cpp:391-397, `myfile0 << Phi(l) << endl`). */
+ls_status ls_write_result(const char* path, int n, const double* v);
+
 /* Flattened NCA skeletons (one record per tree node: level, box, cone,
  * out_active, in_active, then counted lists out-charge, out-check,
  * in-charge, in-check, user-check). Returns the length; buf may be NULL. */

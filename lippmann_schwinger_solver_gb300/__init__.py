@@ -43,7 +43,8 @@ EXPORTED_SYMBOLS = (
     "ls_op_create", "ls_op_destroy", "ls_op_info", "ls_op_points", "ls_op_contrast", "ls_op_rhs",
     "ls_matvec", "ls_matvec_f32", "ls_op_enable_f32", "ls_matvec_host", "ls_gmres", "ls_gmres_restarted",
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
-    "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched",
+    "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
+    "ls_write_result",
 )
 # Every symbol declared in include/ls_fno.h (learned preconditioner).
 FNO_SYMBOLS = (
@@ -203,6 +204,8 @@ def lib():
         L.ls_op_skeleton_dump.restype = ctypes.c_long
         L.ls_op_skeleton_dump.argtypes = [vp, ip, ctypes.c_long]
         L.ls_op_precomputations.argtypes = [vp, dp, dp]
+        L.ls_op_interpolate.argtypes = [vp, ctypes.c_int, dp, dp, dp]
+        L.ls_write_result.argtypes = [ctypes.c_char_p, ctypes.c_int, dp]
         L.ls_last_error.restype = ctypes.c_char_p
         L.ls_version.restype = ctypes.c_char_p
         fp = ctypes.POINTER(ctypes.c_float)
@@ -380,6 +383,17 @@ class Operator:
                                     ctypes.byref(b)), "ls_time_matvec")
         return a.value, b.value
 
+    def interpolate(self, xy, phi):
+        """The density phi (nodes) at the points xy (n x 2) by the
+        reference's Chebyshev-Q+ interpolation (ls_op_interpolate)."""
+        xy = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        if phi.shape != (self.N,):
+            raise ValueError(f"phi must have shape ({self.N},)")
+        out = np.empty(len(xy), dtype=np.complex128)
+        _check(lib().ls_op_interpolate(self._h, len(xy), _dp(xy), _dp(phi), _dp(out)), "ls_op_interpolate")
+        return out
+
     # grid resampling and the learned preconditioner (include/ls_fno.h)
     def grid_weights(self, grid):
         """Host weight rows [G*G, rank] and leaf [G*G] of the nodes -> grid map."""
@@ -490,6 +504,13 @@ class classGMRES:  # noqa: N801 - reference name
 
 def RestartedGMRES(restart, S, m, inputs, b):  # noqa: N802 - reference name
     return S.K.gmres_restarted(b, m, restart)
+
+
+def write_result(path, v):
+    """Writes complex values one per line as "(re,im)" with six significant
+    digits, the reference's result-file text (GMRES/GMRES.cpp:391-397)."""
+    v = np.ascontiguousarray(v, dtype=np.complex128)
+    _check(lib().ls_write_result(os.fsencode(path), len(v), _dp(v)), "ls_write_result")
 
 
 def scattered_field(cfg, phi, device=0):

@@ -2,7 +2,9 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
+#include <fstream>
 #include <memory>
 #include <new>
 #include <string>
@@ -398,6 +400,37 @@ ls_status ls_op_precomputations(const ls_op* op, double* M, double* near) {
   if (!op) return fail(LS_E_INVALID, "ls_op_precomputations: null argument");
   if (M) std::memcpy(M, op->host.M.data(), op->host.M.size() * sizeof(cd));
   if (near) std::memcpy(near, op->host.nearB.data(), op->host.nearB.size() * sizeof(cd));
+  return LS_OK;
+}
+
+ls_status ls_op_interpolate(const ls_op* op, int npts, const double* xy, const double* phi, double* psi) {
+  if (!op || npts < 0 || (npts > 0 && (!xy || !phi || !psi)))
+    return fail(LS_E_INVALID, "ls_op_interpolate: bad argument");
+  const HostOperator& h = op->host;
+  const double L = h.cfg.L;
+  for (int i = 0; i < npts; ++i)
+    if (!(std::fabs(xy[2 * i]) <= L && std::fabs(xy[2 * i + 1]) <= L))
+      return fail(LS_E_INVALID, "ls_op_interpolate: point " + std::to_string(i) + " outside [-L, L]^2");
+  const LeafInterpolator li(h);
+  const cd* ph = reinterpret_cast<const cd*>(phi);
+  std::vector<double> w(h.rank);
+  for (int i = 0; i < npts; ++i) {
+    const int t = li.row(xy[2 * i], xy[2 * i + 1], w.data());
+    cd s(0.0, 0.0);
+    for (int r = 0; r < h.rank; ++r) s += w[r] * ph[(size_t)t * h.rank + r];
+    psi[2 * i] = s.real();
+    psi[2 * i + 1] = s.imag();
+  }
+  return LS_OK;
+}
+
+ls_status ls_write_result(const char* path, int n, const double* v) {
+  if (!path || n < 0 || (n > 0 && !v)) return fail(LS_E_INVALID, "ls_write_result: bad argument");
+  std::ofstream f(path);
+  if (!f) return fail(LS_E_INVALID, std::string("ls_write_result: cannot open ") + path);
+  for (int i = 0; i < n; ++i) f << cd(v[2 * i], v[2 * i + 1]) << '\n';
+  f.close();
+  if (!f) return fail(LS_E_INVALID, std::string("ls_write_result: write to ") + path + " failed");
   return LS_OK;
 }
 

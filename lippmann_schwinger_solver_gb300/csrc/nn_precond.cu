@@ -102,13 +102,16 @@ double cheb_t(double x, int n) {
 
 }  // namespace
 
-void grid_sampling_weights(const HostOperator& h, int G, std::vector<float>& w, std::vector<int>& leaf) {
-  const double L = h.cfg.L;
-  const int nl = h.n_leaves, rank = h.rank, side = 1 << h.cfg.nLevelsUniform;
-  const double rad = L / side;
+LeafInterpolator::LeafInterpolator(const HostOperator& h) : op(h) {
+  L = h.cfg.L;
+  rank = h.rank;
+  side = 1 << h.cfg.nLevelsUniform;
+  rad = L / side;
+  const int nl = h.n_leaves;
   // Leaf centres (mean of their nodes) and the leaf at each cell of the leaf grid.
-  std::vector<double> cx(nl), cy(nl);
-  std::vector<int> table((size_t)side * side, 0);
+  cx.assign(nl, 0.0);
+  cy.assign(nl, 0.0);
+  table.assign((size_t)side * side, 0);
   for (int t = 0; t < nl; ++t) {
     double sx = 0.0, sy = 0.0;
     for (int r = 0; r < rank; ++r) {
@@ -117,32 +120,42 @@ void grid_sampling_weights(const HostOperator& h, int G, std::vector<float>& w, 
     }
     cx[t] = sx / rank;
     cy[t] = sy / rank;
-    const int lx = std::min(std::max((int)std::floor((cx[t] + L) / (2 * rad)), 0), side - 1);
-    const int ly = std::min(std::max((int)std::floor((cy[t] + L) / (2 * rad)), 0), side - 1);
-    table[(size_t)lx * side + ly] = t;
+    table[(size_t)cell(cx[t]) * side + cell(cy[t])] = t;
   }
-  std::vector<std::pair<int, int>> bases;
   for (int d = 0; d < h.cfg.degreeOfBases; ++d)
     for (int a = 0; a < d + 1; ++a) bases.push_back({a, d - a});
+}
+
+int LeafInterpolator::cell(double v) const {
+  return std::min(std::max((int)std::floor((v + L) / (2 * rad)), 0), side - 1);
+}
+
+int LeafInterpolator::row(double x, double y, double* w) const {
+  const int t = table[(size_t)cell(x) * side + cell(y)];
+  const double Px = (x - cx[t]) / rad, Py = (y - cy[t]) / rad;
   const int nb = (int)bases.size();
+  double tb[64];
+  for (int l = 0; l < nb && l < 64; ++l) tb[l] = cheb_t(Px, bases[l].first) * cheb_t(Py, bases[l].second);
+  for (int r = 0; r < rank; ++r) {
+    double s = 0.0;
+    for (int l = 0; l < nb; ++l) s += tb[l] * op.Qpinv[(size_t)l * rank + r];
+    w[r] = s;
+  }
+  return t;
+}
+
+void grid_sampling_weights(const HostOperator& h, int G, std::vector<float>& w, std::vector<int>& leaf) {
+  const LeafInterpolator li(h);
+  const double L = h.cfg.L;
+  const int rank = h.rank;
   w.assign((size_t)G * G * rank, 0.f);
   leaf.assign((size_t)G * G, 0);
-  std::vector<double> tb(nb);
+  std::vector<double> row(rank);
   for (int ix = 0; ix < G; ++ix)
     for (int iy = 0; iy < G; ++iy) {
       const int g = ix * G + iy;
-      const double x = L * (-1.0 + (2.0 * ix + 1.0) / G), y = L * (-1.0 + (2.0 * iy + 1.0) / G);
-      const int lx = std::min(std::max((int)std::floor((x + L) / (2 * rad)), 0), side - 1);
-      const int ly = std::min(std::max((int)std::floor((y + L) / (2 * rad)), 0), side - 1);
-      const int t = table[(size_t)lx * side + ly];
-      leaf[g] = t;
-      const double Px = (x - cx[t]) / rad, Py = (y - cy[t]) / rad;
-      for (int l = 0; l < nb; ++l) tb[l] = cheb_t(Px, bases[l].first) * cheb_t(Py, bases[l].second);
-      for (int r = 0; r < rank; ++r) {
-        double s = 0.0;
-        for (int l = 0; l < nb; ++l) s += tb[l] * h.Qpinv[(size_t)l * rank + r];
-        w[(size_t)g * rank + r] = (float)s;
-      }
+      leaf[g] = li.row(L * (-1.0 + (2.0 * ix + 1.0) / G), L * (-1.0 + (2.0 * iy + 1.0) / G), row.data());
+      for (int r = 0; r < rank; ++r) w[(size_t)g * rank + r] = (float)row[r];
     }
 }
 

@@ -33,6 +33,22 @@ struct GridSampler {
   cudaError_t sample(const double2* x, int nvec, long long N, float2* out, cudaStream_t s) const;
 };
 
+// Host side of the reference's Chebyshev-Q+ interpolation at arbitrary
+// points (hybridTrueValidation_gmres.cpp:187-219): the containing leaf of a
+// uniform tree (points on the domain's upper edges go to the last leaf) and
+// the row w with psi(x, y) = sum_r w[r] phi[leaf * rank + r].
+struct LeafInterpolator {
+  const HostOperator& op;
+  double L = 1.0, rad = 1.0;
+  int rank = 0, side = 1;
+  std::vector<double> cx, cy;
+  std::vector<int> table;
+  std::vector<std::pair<int, int>> bases;
+  explicit LeafInterpolator(const HostOperator& h);
+  int cell(double v) const;
+  int row(double x, double y, double* w) const;  // returns the leaf
+};
+
 // Host computation of the weight rows and leaf of every grid point.
 void grid_sampling_weights(const HostOperator& h, int grid, std::vector<float>& w, std::vector<int>& leaf);
 // q at the grid points (host), from the operator's contrast plugin.
