@@ -5,10 +5,14 @@
 // the channel-last activations are read and written as whole 128-byte rows.
 //
 // The kernels are launched one after another without programmatic
-// dependent launch: with it, the backward pass read stale values of a
-// buffer that the kernel two launches earlier had read and the preceding
-// kernel had rewritten (the weight gradients of the GELU layers came out
-// wrong on GB300 while each kernel alone was correct).
+// dependent launch. With it, an earlier version of these kernels read, in
+// the backward pass, stale values of a buffer that the kernel two launches
+// before had read and the preceding kernel had rewritten: the weight
+// gradients of the GELU layers came out wrong on GB300 although each kernel
+// alone was correct. The present kernels measured correct with it too, but
+// the failure depended on which kernels shared the SMs, so plain launches
+// are kept (the forward pass of the preconditioner is replayed as a CUDA
+// graph instead).
 //
 // Spectral convolution of one layer, forward:
 //   H1 = r2c_y(h)        [B][G][M][32]    y-DFT, kept ky < M
