@@ -25,6 +25,7 @@
 // to the per-ky weights, dft_x and idft_x likewise, and mix's adjoint uses
 // the conjugate transpose of each mode's weight matrix.
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -542,6 +543,234 @@ __global__ void features_kernel(int G, int B, int S, const float* __restrict__ Q
   target[t * 2 + 1] *= sc;
 }
 
+// ---------------------------------------------------------------------------
+// The forward pass of ONE sample in one cooperative launch (the
+// preconditioner's case, where 22 separate launches cost more than their
+// work). The network is walked in alternating phases separated by grid-wide
+// barriers:
+//   row phase p (one grid row x per block): for p = 0 the lift of the row;
+//     for p >= 1 the y-synthesis of G1 + pointwise path + bias (+ GELU) of
+//     layer p-1; then, while p < L, the y-DFT of the new row into H1, and at
+//     p = L the projection of the row's points.
+//   column phase p (one kept ky per block): x-DFT of the H1 column, the
+//     per-mode channel mixing of layer p, and the x-synthesis into G1.
+// A row needs only its own previous values and G1 row, and a column only
+// its H1 column, so one barrier after each phase suffices (2 L in all).
+// Same arithmetic as the separate kernels above, in the same order per
+// output, except that the x-DFT sums run unsplit.
+struct Fwd1Args {
+  int G, M, L, PW;
+  const float* in;    // [G*G][6]
+  const float* ssq;   // |field|^2 of the sample (may be null)
+  float* out;         // [G*G][2]
+  float* h;           // [G*G][32], updated row by row
+  float2* H1;         // [G][M][32]
+  float2* G1;         // [G][M][32]
+  const float2* tw;
+  const float* lift_w;
+  const float* lift_b;
+  const float2* spec[8];
+  const float* pw_w[8];
+  const float* pw_b[8];
+  const float* p1_w;
+  const float* p1_b;
+  const float* p2_w;
+  const float* p2_b;
+};
+
+constexpr int kF1Threads = 512;
+
+// Shared floats of the fused kernel: twiddles, then the larger of the row
+// phase (two rows, a G1 row, pointwise weights, projection weights) and the
+// column phase (an H1 column and two mode columns).
+size_t fwd1_smem_floats(int G, int M) {
+  const size_t row = 2 * (size_t)G * 32 + 2 * (size_t)M * 32 + 32 * 33 + 128 * 33 + 128 + 256;
+  const size_t col = 2 * ((size_t)G * 32 + 2 * (2 * (size_t)M) * 32);
+  return 2 * (size_t)G + std::max(row, col);
+}
+
+__global__ void __launch_bounds__(kF1Threads, 1) forward1_kernel(Fwd1Args a) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ float smf[];
+  const int G = a.G, M = a.M, L = a.L, PW = a.PW, NM2 = 2 * M;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  float2* ts = reinterpret_cast<float2*>(smf);
+  float* region = smf + 2 * G;
+  const float GG = (float)G * (float)G;
+  const float sc_in = a.ssq ? rsqrtf(fmaxf(a.ssq[0] / GG, 1e-30f)) : 1.f;
+  const float sc_out = a.ssq ? sqrtf(fmaxf(a.ssq[0] / GG, 1e-30f)) : 1.f;
+  for (int i = tid; i < G; i += nt) ts[i] = a.tw[i];
+  __syncthreads();
+  for (int p = 0; p <= L; ++p) {
+    // ---------------- row phase
+    for (int r = blockIdx.x; r < G; r += gridDim.x) {
+      float* hs_old = region;
+      float* hs_new = region + G * 32;
+      float2* gs = reinterpret_cast<float2*>(region + 2 * G * 32);
+      float* ps = region + 2 * G * 32 + 2 * M * 32;  // [32][33]
+      float* q1s = ps + 32 * 33;                      // [128][33]
+      float* b1s = q1s + 128 * 33;
+      float* q2s = b1s + 128;                         // [2][128]
+      const long long row0 = (long long)r * G;
+      if (p == 0) {
+        for (int i = tid; i < G * 32; i += nt) {
+          const int y = i >> 5, c = i & 31;
+          const float* x = a.in + (row0 + y) * kFnoIn;
+          float acc = a.lift_b[c];
+#pragma unroll
+          for (int j = 0; j < kFnoIn; ++j)
+            acc = fmaf(a.lift_w[c * kFnoIn + j], (j == 1 || j == 2) ? x[j] * sc_in : x[j], acc);
+          hs_new[i] = acc;
+        }
+      } else {
+        const int l = p - 1;
+        for (int i = tid; i < G * 32; i += nt) hs_old[i] = a.h[row0 * 32 + i];
+        for (int i = tid; i < M * 32; i += nt) {
+          float2 g = a.G1[(long long)r * M * 32 + i];
+          const float sk = ((i >> 5) ? 2.f : 1.f) / GG;
+          g.x *= sk;
+          g.y *= sk;
+          gs[i] = g;
+        }
+        for (int i = tid; i < 1024; i += nt) ps[(i >> 5) * 33 + (i & 31)] = a.pw_w[l][i];
+        if (p == L) {
+          for (int i = tid; i < PW * 32; i += nt) q1s[(i >> 5) * 33 + (i & 31)] = a.p1_w[i];
+          for (int i = tid; i < PW; i += nt) {
+            b1s[i] = a.p1_b[i];
+            q2s[i] = a.p2_w[i];
+            q2s[128 + i] = a.p2_w[PW + i];
+          }
+        }
+        __syncthreads();
+        const float bc = a.pw_b[l][lane];
+        const bool act = p < L;
+        for (int y0 = warp * kC2rRows; y0 < G; y0 += nw * kC2rRows) {
+          float acc[kC2rRows];
+#pragma unroll
+          for (int q = 0; q < kC2rRows; ++q) acc[q] = bc;
+          for (int ky = 0; ky < M; ++ky) {
+            const float2 g = gs[ky * 32 + lane];
+#pragma unroll
+            for (int q = 0; q < kC2rRows; ++q) {
+              const float2 t = ts[(ky * (y0 + q)) & (G - 1)];
+              acc[q] = fmaf(t.x, g.x, fmaf(-t.y, g.y, acc[q]));
+            }
+          }
+#pragma unroll 8
+          for (int i = 0; i < 32; ++i) {
+            const float pc = ps[lane * 33 + i];
+#pragma unroll
+            for (int q = 0; q < kC2rRows; ++q) acc[q] = fmaf(pc, hs_old[min(y0 + q, G - 1) * 32 + i], acc[q]);
+          }
+#pragma unroll
+          for (int q = 0; q < kC2rRows; ++q)
+            if (y0 + q < G) hs_new[(y0 + q) * 32 + lane] = act ? gelu(acc[q]) : acc[q];
+        }
+      }
+      __syncthreads();
+      if (p < L) {
+        for (int i = tid; i < G * 32; i += nt) a.h[row0 * 32 + i] = hs_new[i];
+        for (int item = tid; item < M * 32; item += nt) {
+          const int ky = item >> 5, c = item & 31;
+          float ar = 0.f, ai = 0.f;
+          for (int y = 0; y < G; ++y) {
+            const float2 t = ts[(ky * y) & (G - 1)];
+            const float v = hs_new[y * 32 + c];
+            ar = fmaf(t.x, v, ar);
+            ai = fmaf(-t.y, v, ai);
+          }
+          a.H1[((long long)r * M + ky) * 32 + c] = make_float2(ar, ai);
+        }
+      } else {
+        const int nk = PW >> 5;
+        for (int y = warp; y < G; y += nw) {
+          const float hv = hs_new[y * 32 + lane];
+          float uj[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) uj[k] = k < nk ? b1s[lane + 32 * k] : 0.f;
+          for (int i = 0; i < 32; ++i) {
+            const float hb = __shfl_sync(0xffffffffu, hv, i);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              if (k < nk) uj[k] = fmaf(q1s[(lane + 32 * k) * 33 + i], hb, uj[k]);
+          }
+          float o0 = 0.f, o1 = 0.f;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (k < nk) {
+              const float gv = gelu(uj[k]);
+              o0 = fmaf(q2s[lane + 32 * k], gv, o0);
+              o1 = fmaf(q2s[128 + lane + 32 * k], gv, o1);
+            }
+          }
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) {
+            o0 += __shfl_xor_sync(0xffffffffu, o0, off);
+            o1 += __shfl_xor_sync(0xffffffffu, o1, off);
+          }
+          if (lane == 0) {
+            a.out[(row0 + y) * 2] = (o0 + a.p2_b[0]) * sc_out;
+            a.out[(row0 + y) * 2 + 1] = (o1 + a.p2_b[1]) * sc_out;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (p == L) break;
+    grid.sync();
+    // ---------------- column phase (layer p)
+    for (int ky = blockIdx.x; ky < M; ky += gridDim.x) {
+      float2* ins = reinterpret_cast<float2*>(region);  // [G][32]
+      float2* h2s = ins + G * 32;                          // [2M][32]
+      float2* os = h2s + NM2 * 32;                         // [2M][32]
+      for (int i = tid; i < G * 32; i += nt) ins[i] = a.H1[((long long)(i >> 5) * M + ky) * 32 + (i & 31)];
+      __syncthreads();
+      for (int item = tid; item < NM2 * 32; item += nt) {
+        const int m = item >> 5, c = item & 31;
+        const int f = m < M ? m : G - 2 * M + m;
+        float ar = 0.f, ai = 0.f;
+        for (int x = 0; x < G; ++x) {
+          const float2 t = ts[(f * x) & (G - 1)];
+          const float2 v = ins[x * 32 + c];
+          ar = fmaf(t.x, v.x, fmaf(t.y, v.y, ar));
+          ai = fmaf(t.x, v.y, fmaf(-t.y, v.x, ai));
+        }
+        h2s[item] = make_float2(ar, ai);
+      }
+      __syncthreads();
+      for (int item = tid; item < NM2 * 32; item += nt) {
+        const int m = item >> 5, o = item & 31;
+        const float2* wm = a.spec[p] + (long long)(m * M + ky) * 1024 + o;
+        float ar = 0.f, ai = 0.f;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const float2 v = h2s[m * 32 + i];
+          const float2 w = wm[i * 32];
+          ar = fmaf(v.x, w.x, fmaf(-v.y, w.y, ar));
+          ai = fmaf(v.x, w.y, fmaf(v.y, w.x, ai));
+        }
+        os[item] = make_float2(ar, ai);
+      }
+      __syncthreads();
+      for (int item = tid; item < G * 32; item += nt) {
+        const int x = item >> 5, c = item & 31;
+        float ar = 0.f, ai = 0.f;
+        for (int m = 0; m < NM2; ++m) {
+          const int f = m < M ? m : G - 2 * M + m;
+          const float2 t = ts[(f * x) & (G - 1)];
+          const float2 v = os[m * 32 + c];
+          ar = fmaf(t.x, v.x, fmaf(-t.y, v.y, ar));
+          ai = fmaf(t.x, v.y, fmaf(t.y, v.x, ai));
+        }
+        a.G1[((long long)x * M + ky) * 32 + c] = make_float2(ar, ai);
+      }
+      __syncthreads();
+    }
+    grid.sync();
+  }
+}
+
 // Host-side uniform numbers for the initial weights (splitmix64).
 struct Rng {
   uint64_t s;
@@ -708,6 +937,70 @@ cudaError_t FnoNet::ensure(int batch) {
 }
 
 cudaError_t FnoNet::forward(int B, const float* in, float* outp, const float* ssq, cudaStream_t s) {
+  if (B == 1 && fused_ok()) {
+    const cudaError_t e = forward1(in, outp, ssq, s);
+    if (e == cudaSuccess) return e;
+    cudaGetLastError();  // not launchable here: separate kernels
+    fused = -1;
+  }
+  return forward_layers(B, in, outp, ssq, s);
+}
+
+bool FnoNet::fused_ok() {
+  if (fused == 0) {
+    int coop = 0, nsm = 0, per_sm = 0;
+    const size_t smem = fwd1_smem_floats(shape.grid, shape.modes) * sizeof(float);
+    fused = -1;
+    if (shape.grid <= 128 && shape.layers <= 8 && shape.proj <= 128 &&
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) == cudaSuccess && coop &&
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess &&
+        cudaFuncSetAttribute(forward1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+            cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward1_kernel, kF1Threads, smem) == cudaSuccess &&
+        per_sm >= 1) {
+      fused_blocks = nsm * per_sm;
+      fused = 1;
+    }
+    cudaGetLastError();
+  }
+  return fused == 1;
+}
+
+cudaError_t FnoNet::forward1(const float* in, float* outp, const float* ssq, cudaStream_t s) {
+  cudaError_t e = ensure(1);
+  if (e != cudaSuccess) return e;
+  Fwd1Args a = {};
+  a.G = shape.grid;
+  a.M = shape.modes;
+  a.L = shape.layers;
+  a.PW = shape.proj;
+  a.in = in;
+  a.ssq = ssq;
+  a.out = outp;
+  a.h = h[0];
+  a.H1 = H1;
+  a.G1 = G1;
+  a.tw = tw;
+  a.lift_w = params + lay.lift_w;
+  a.lift_b = params + lay.lift_b;
+  for (int l = 0; l < shape.layers; ++l) {
+    a.spec[l] = reinterpret_cast<const float2*>(params + lay.spec[l]);
+    a.pw_w[l] = params + lay.pw_w[l];
+    a.pw_b[l] = params + lay.pw_b[l];
+  }
+  a.p1_w = params + lay.p1_w;
+  a.p1_b = params + lay.p1_b;
+  a.p2_w = params + lay.p2_w;
+  a.p2_b = params + lay.p2_b;
+  void* args[] = {&a};
+  const size_t smem = fwd1_smem_floats(shape.grid, shape.modes) * sizeof(float);
+  const int blocks = std::min(fused_blocks, std::max(shape.grid, shape.modes));
+  launches = 1;
+  return cudaLaunchCooperativeKernel((const void*)forward1_kernel, dim3((unsigned)blocks), dim3(kF1Threads), args,
+                                     smem, s);
+}
+
+cudaError_t FnoNet::forward_layers(int B, const float* in, float* outp, const float* ssq, cudaStream_t s) {
   if (B < 1 || B > kFnoMaxBatch) return cudaErrorInvalidValue;
   cudaError_t e = ensure(B);
   if (e != cudaSuccess) return e;
@@ -738,7 +1031,7 @@ cudaError_t FnoNet::forward(int B, const float* in, float* outp, const float* ss
 cudaError_t FnoNet::loss_grad(int B, const float* in, const float* target, cudaStream_t s) {
   if (B < 1 || B > kFnoMaxBatch) return cudaErrorInvalidValue;
   cudaError_t e = ensure(B);
-  if (e == cudaSuccess) e = forward(B, in, out, nullptr, s);
+  if (e == cudaSuccess) e = forward_layers(B, in, out, nullptr, s);  // keeps what the backward pass reads
   if (e != cudaSuccess) return e;
   const int G = shape.grid, M = shape.modes, L = shape.layers, NM = 2 * M * M, PW = shape.proj;
   const long long GG = (long long)G * G, P = B * GG;

@@ -76,8 +76,15 @@ struct FnoNet {
   // out[b][x][y][2] = net(in[b][x][y][6]). ssq (device, one float per sample,
   // may be null): the field channels are divided by sqrt(ssq/G^2) on input
   // and the outputs multiplied by it, which makes the net's linear use scale
-  // invariant (the preconditioner's case).
+  // invariant (the preconditioner's case). A single sample runs as one
+  // cooperative launch (forward1) where the device allows it.
   cudaError_t forward(int batch, const float* in, float* out, const float* ssq, cudaStream_t s);
+  // The layer-by-layer kernels (the training forward: keeps z and u).
+  cudaError_t forward_layers(int batch, const float* in, float* out, const float* ssq, cudaStream_t s);
+  cudaError_t forward1(const float* in, float* out, const float* ssq, cudaStream_t s);
+  bool fused_ok();
+  int fused = 0;         // 0: not checked, 1: forward1 available, -1: not available
+  int fused_blocks = 0;  // co-resident blocks of forward1
   // Forward, loss = mean_b |o_b - t_b|^2 / |t_b|^2 (device scalar), backward
   // into grads (overwritten).
   cudaError_t loss_grad(int batch, const float* in, const float* target, cudaStream_t s);

@@ -285,11 +285,16 @@ cudaError_t NnPrecond::apply(const float2* v, float2* z, cudaStream_t s) {
   cudaError_t e;
   // ssq is zero here: set at init and cleared by the last kernel of every application.
   nodes_to_grid_kernel<float2><<<dim3((unsigned)((GG + 255) / 256), 1), 256, 0, s>>>(GG, gs.rank, gs.w, gs.leaf, v, 0, in, kFnoIn, 1, 0, ssq);
-  if (!fwd || fwd_generation != net->generation || net->cap < 1) capture();
-  if (fwd && fwd_generation == net->generation) {
-    if ((e = cudaGraphLaunch(fwd, s)) != cudaSuccess) return e;
-  } else if ((e = net->forward(1, in, out, ssq, s)) != cudaSuccess) {
-    return e;
+  if (net->fused_ok()) {
+    // One cooperative launch for the whole network.
+    if ((e = net->forward(1, in, out, ssq, s)) != cudaSuccess) return e;
+  } else {
+    if (!fwd || fwd_generation != net->generation || net->cap < 1) capture();
+    if (fwd && fwd_generation == net->generation) {
+      if ((e = cudaGraphLaunch(fwd, s)) != cudaSuccess) return e;
+    } else if ((e = net->forward(1, in, out, ssq, s)) != cudaSuccess) {
+      return e;
+    }
   }
   grid_to_nodes_kernel<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(N, G, nodes, out, v, z, ssq);
   ++applies;

@@ -69,9 +69,11 @@ struct NnPrecond : Precond32 {
   float* out = nullptr;     // [G*G][2]
   float* ssq = nullptr;     // |sampled field|^2
   int applies = 0;
-  // The network's forward pass on (in, out) captured once as a CUDA graph
-  // and replayed by every application (its ~22 launches cost more than
-  // their kernels for one sample); recaptured when the net's buffers move.
+  // Where the fused single-sample pass (one cooperative launch) is not
+  // available, the network's layer-by-layer forward pass on (in, out) is
+  // captured once as a CUDA graph and replayed by every application (its
+  // 22 launches cost more than their kernels for one sample); recaptured
+  // when the net's buffers move.
   cudaGraphExec_t fwd = nullptr;
   unsigned long long fwd_generation = 0;
   cudaError_t capture();

@@ -36,10 +36,11 @@ def _inputs(G, B, seed):
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-def test_forward_matches_oracle(ls, shape):
+@pytest.mark.parametrize("B", [1, 2])  # one sample: the fused cooperative pass
+def test_forward_matches_oracle(ls, shape, B):
     from oracle import fno_oracle as fo
     net = ls.FNO(**shape, seed=3)
-    G, B = shape["grid"], 2
+    G = shape["grid"]
     x, _ = _inputs(G, B, 0)
     xd = torch.from_numpy(x).cuda()
     od = torch.empty((B, G * G, 2), device="cuda")
