@@ -132,3 +132,16 @@ def test_host_only_operator_refuses_device_grid_calls(ls):
         op.fgmres_nn(None, b, flags=0)
     assert e.value.code == ls.LS_E_STATE
     op.close()
+
+
+def test_many_scatterer_specs_are_seeded_and_in_range():
+    from lippmann_schwinger_solver_gb300 import scatterers as sc
+    a = sc.scatterer_specs(32, 20261203)
+    assert a == sc.scatterer_specs(32, 20261203)
+    assert {lv for lv, _, _ in a} == {4, 5, 6}
+    for lv, k, bumps in a:
+        assert 10.0 <= k <= 60.0 and 1 <= len(bumps) <= 4
+        for cx, cy, amp, w in bumps:
+            assert -0.6 <= cx <= 0.6 and -0.6 <= cy <= 0.6 and 0.5 <= amp <= 1.5 and 0.05 <= w <= 0.2
+    cfg = sc.config(*a[0])
+    assert cfg.Qchoice == 6 and cfg.nLevelsUniform == a[0][0] and cfg.kappa == a[0][1]

@@ -48,3 +48,22 @@ def test_batched_rejects_bad_input(ls):
     with pytest.raises(ValueError):
         op.gmres_mixed_batched(B[:-1])
     op.close()
+
+
+def test_many_scatterers_pipeline(ls):
+    """Several scatterers of different size and wavenumber, each with many
+    directions; assembly of the next overlaps the solve of the current one.
+    Every direction of every scatterer meets the FP64 tolerance, and the
+    solutions equal those of the same solve run alone."""
+    from lippmann_schwinger_solver_gb300 import scatterers as sc
+    specs = [(3, 12.0, ((0.1, -0.2, 1.0, 0.15),)), (4, 30.0, ((-0.3, 0.2, 0.8, 0.1), (0.4, 0.1, 1.2, 0.07)))]
+    recs, total, sols = sc.solve_many(specs, angles=16, tol=1e-8, keep_solutions=True)
+    assert total["all_converged"] and total["max_true_residual"] <= 1e-8
+    assert [r["N"] for r in recs] == [2304, 9216]
+    op = ls.Operator(sc.config(*specs[1]), device=0)
+    op.enable_f32()
+    B = op.rhs_angles(2 * np.pi * np.arange(16) / 16)
+    X, _, rr, code = op.gmres_mixed_batched(B, max_outer=20, inner_iter=100, tol=1e-8)
+    assert code == ls.LS_OK
+    assert np.linalg.norm(X - sols[1]) / np.linalg.norm(X) < 1e-12
+    op.close()
