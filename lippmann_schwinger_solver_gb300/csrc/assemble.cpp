@@ -44,6 +44,47 @@ constexpr double kQuadEps = 1e-7;           // FarFieldInteraction.hpp:37, NearF
 constexpr int kQuadOrder = 10;              // 10x10 Gauss-Legendre per panel
 
 // ---------------------------------------------------------------- special functions
+// J_n(x), Y_n(x) for n = 0 .. nmax (nmax < 64) for the far-field Hankel
+// series, from four library calls instead of one per order: J_0, J_1, Y_0,
+// Y_1 from libstdc++; Y_n by forward recurrence (Y is the dominant
+// solution); J_n by forward recurrence when x > nmax (stable below the
+// turning point), else by Miller's backward recurrence from order
+// 2((max(nmax, x) + 20 + sqrt(60 max)) / 2), scaled to whichever of J_0, J_1
+// is larger in magnitude (they never vanish together). Against libstdc++'s
+// per-order values for x in [0.3, 250], n <= 15: J within 5e-14 and Y
+// within 1e-13 of max_n |.|. The CPU oracle performs exactly the same
+// operations, so the two assemblers still pick the same skeletons.
+void bessel_jy_orders(int nmax, double x, double* J, double* Y) {
+  const double j0 = std::cyl_bessel_j(0.0, x), j1 = std::cyl_bessel_j(1.0, x);
+  Y[0] = std::cyl_neumann(0.0, x);
+  if (nmax >= 1) Y[1] = std::cyl_neumann(1.0, x);
+  for (int n = 1; n < nmax; ++n) Y[n + 1] = (2.0 * n / x) * Y[n] - Y[n - 1];
+  J[0] = j0;
+  if (nmax >= 1) J[1] = j1;
+  if (x > nmax) {
+    for (int n = 1; n < nmax; ++n) J[n + 1] = (2.0 * n / x) * J[n] - J[n - 1];
+    return;
+  }
+  const int base = nmax > (int)x ? nmax : (int)x;
+  const int m = 2 * ((base + 20 + (int)std::sqrt(60.0 * base)) / 2);
+  double F[64];
+  double fp = 0.0, f = 1.0;
+  for (int j = m; j > 0; --j) {
+    const double fm = (2.0 * j / x) * f - fp;
+    fp = f;
+    f = fm;
+    if (std::fabs(f) > 1e10) {
+      f *= 1e-10;
+      fp *= 1e-10;
+      for (int i = j + 1; i <= nmax; ++i) F[i] *= 1e-10;
+    }
+    if (j <= nmax) F[j] = fp;
+  }
+  F[0] = f;
+  const double s = (std::fabs(j0) >= std::fabs(j1) || nmax < 1) ? j0 / F[0] : j1 / F[1];
+  for (int i = 0; i <= nmax; ++i) J[i] = F[i] * s;
+}
+
 double bes_j(int n, double x) {
   if (n >= 0) return std::cyl_bessel_j(double(n), x);
   const double t = std::cyl_bessel_j(double(-n), x);
@@ -379,10 +420,7 @@ class Builder {
     const double R2 = (py - ly) * (py - ly) + (px - lx) * (px - lx);
     const double R = kappa * std::sqrt(R2);
     double J[kSeries + 1], Y[kSeries + 1];
-    for (int n = 0; n <= kSeries; ++n) {
-      J[n] = std::cyl_bessel_j(double(n), R);
-      Y[n] = std::cyl_neumann(double(n), R);
-    }
+    bessel_jy_orders(kSeries, R, J, Y);
     for (int n = -kSeries; n <= kSeries; ++n) {
       const int a = n < 0 ? -n : n;
       const double sg = (n < 0 && (a % 2 == 1)) ? -1.0 : 1.0;

@@ -20,7 +20,10 @@
 //  * kernel entries, quadrature integrands and ACA updates use the same
 //    std::complex expression order as the reference source;
 //  * Bessel functions come from libstdc++ (std::cyl_bessel_j /
-//    std::cyl_neumann), called once per order like the reference's Boost
+//    std::cyl_neumann). The far-field Hankel series takes J_0, J_1, Y_0, Y_1
+//    from it and the other orders by recurrence (bessel_jy_orders, shared
+//    with the library's assembler); elsewhere they are called once per order
+//    like the reference's Boost
 //    calls (GMRES/G_FMM2DTree.hpp:73-100).
 
 #include "ora_common.hpp"
@@ -94,8 +97,15 @@ struct Oracle {
     const double th = std::atan2(ri.y - B.cy, ri.x - B.cx);
     const double R2 = (ri.y - B.cy) * (ri.y - B.cy) + (ri.x - B.cx) * (ri.x - B.cx);
     const double R = kappa * std::sqrt(R2);
+    double J[64], Y[64];
+    bessel_jy_orders(S, R, J, Y);
     for (int n = -S; n <= S; ++n) {
-      cd t = (besselJ(n, R) + I * besselY(n, R)) * std::exp(I * double(n) * th);
+      // reflection J_{-n} = (-1)^n J_n, Y_{-n} = (-1)^n Y_n (G_FMM2DTree.hpp:73-100)
+      const int a = n < 0 ? -n : n;
+      const double sg = (n < 0 && (a % 2 == 1)) ? -1.0 : 1.0;
+      const double jn = sg == 1.0 ? J[a] : -J[a];
+      const double yn = sg == 1.0 ? Y[a] : -Y[a];
+      cd t = (jn + I * yn) * std::exp(I * double(n) * th);
       h[n + S] = t;
     }
   }
@@ -1095,6 +1105,7 @@ void ora_gauss_legendre(int n, double* nodes, double* weights) {
   for (int i = 0; i < n; ++i) { nodes[i] = gn[i]; weights[i] = gw[i]; }
 }
 void ora_bessel_jy(int n, double x, double* j, double* y) { *j = besselJ(n, x); *y = besselY(n, x); }
+void ora_bessel_jy_orders(int nmax, double x, double* j, double* y) { bessel_jy_orders(nmax, x, j, y); }
 void ora_colpiv_solve(int m, int n, const double* A, const double* b, double* x) {
   CMat M(m, n);
   for (int j = 0; j < n; ++j)

@@ -72,6 +72,8 @@ void ora_set_threads(int n);
 /* Stand-alone helpers exposed for unit tests of the restated math. */
 void ora_gauss_legendre(int n, double* nodes, double* weights);
 void ora_bessel_jy(int n, double x, double* j, double* y);
+/* J_0..J_nmax, Y_0..Y_nmax by the recurrences of the far-field Hankel series. */
+void ora_bessel_jy_orders(int nmax, double x, double* j, double* y);
 void ora_colpiv_solve(int m, int n, const double* A, const double* b, double* x);
 
 /* Adaptive tree (ls_oracle_adaptive.cpp): builds the contrast-adapted tree,
@@ -82,6 +84,10 @@ int ora_adaptive_report(const ora_cfg* cfg, int treeAdaptivity, int* head, int* 
 /* Skeleton node sets of the same build (treeAdaptivity < 0: uniform tree of
  * nLevelsUniform levels); j, k, cone, then four length-prefixed lists. */
 long ora_adaptive_skeletons(const ora_cfg* cfg, int treeAdaptivity, int* buf, long cap);
+/* Far-field Bessel orders of the adaptive restatement: 1 = one library call
+ * per order (the reference's pattern), 0 (default) = the recurrence shared
+ * with the uniform oracle and the library. */
+void ora_adaptive_set_per_order_bessel(int on);
 
 #ifdef __cplusplus
 }

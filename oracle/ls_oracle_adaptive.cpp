@@ -25,6 +25,13 @@
 
 namespace ora {
 namespace adaptive {
+// Far-field Bessel orders: one library call per order (the reference's
+// calling pattern, what the printed-log pin is checked with) or the
+// recurrence shared with the uniform oracle and the library.
+bool g_per_order_bessel = false;
+}  // namespace adaptive
+
+namespace adaptive {
 
 struct Cone {
   std::vector<Pair> IL;
@@ -348,7 +355,21 @@ struct AOracle {
       const double th = std::atan2(ri.y - B.c.y, ri.x - B.c.x);
       const double R2 = (ri.y - B.c.y) * (ri.y - B.c.y) + (ri.x - B.c.x) * (ri.x - B.c.x);
       const double R = o->kappa * std::sqrt(R2);
-      for (int n = -o->S; n <= o->S; ++n) h[n + o->S] = (besselJ(n, R) + I * besselY(n, R)) * std::exp(I * double(n) * th);
+      if (g_per_order_bessel) {
+        // one library call per order, as the reference calls Boost
+        for (int n = -o->S; n <= o->S; ++n)
+          h[n + o->S] = (besselJ(n, R) + I * besselY(n, R)) * std::exp(I * double(n) * th);
+      } else {
+        double J[64], Y[64];
+        bessel_jy_orders(o->S, R, J, Y);
+        for (int n = -o->S; n <= o->S; ++n) {
+          const int a = n < 0 ? -n : n;
+          const double sg = (n < 0 && (a % 2 == 1)) ? -1.0 : 1.0;
+          const double jn = sg == 1.0 ? J[a] : -J[a];
+          const double yn = sg == 1.0 ? Y[a] : -Y[a];
+          h[n + o->S] = (jn + I * yn) * std::exp(I * double(n) * th);
+        }
+      }
       return m.emplace(key, std::move(h)).first->second.data();
     }
   };
@@ -599,6 +620,10 @@ struct AOracle {
 }  // namespace ora
 
 extern "C" {
+
+// Far-field Bessel orders of the adaptive restatement: 1 = one library call
+// per order (the reference's pattern), 0 = the shared recurrence.
+void ora_adaptive_set_per_order_bessel(int on) { ora::adaptive::g_per_order_bessel = on != 0; }
 
 // treeAdaptivity >= 0: the adaptive tree with epsilonTree = 10^-treeAdaptivity
 // (createAdaptiveTree); treeAdaptivity < 0: the uniform tree of

@@ -187,6 +187,47 @@ inline double besselY(int n, double x) {
   return ((-n) % 2 == 0) ? t : -t;
 }
 
+// J_n(x) and Y_n(x) for n = 0 .. nmax (nmax <= 62) for the far-field
+// Hankel series, from four library calls instead of one per order:
+// J_0, J_1, Y_0, Y_1 from libstdc++; Y_n by forward recurrence (Y is the
+// dominant solution); J_n by forward recurrence when x > nmax (below the
+// turning point the recurrence is stable), else by Miller's backward
+// recurrence from order 2((max(nmax, x) + 20 + sqrt(60 max)) / 2), scaled to
+// whichever of J_0, J_1 is larger in magnitude (they never vanish
+// together). Against libstdc++'s per-order values for x in [0.3, 250],
+// n <= 15: J within 5e-14 and Y within 1e-13 of max_n |.|. Both this oracle
+// and the library's assembler use exactly these operations.
+inline void bessel_jy_orders(int nmax, double x, double* J, double* Y) {
+  const double j0 = std::cyl_bessel_j(0.0, x), j1 = std::cyl_bessel_j(1.0, x);
+  Y[0] = std::cyl_neumann(0.0, x);
+  if (nmax >= 1) Y[1] = std::cyl_neumann(1.0, x);
+  for (int n = 1; n < nmax; ++n) Y[n + 1] = (2.0 * n / x) * Y[n] - Y[n - 1];
+  J[0] = j0;
+  if (nmax >= 1) J[1] = j1;
+  if (x > nmax) {
+    for (int n = 1; n < nmax; ++n) J[n + 1] = (2.0 * n / x) * J[n] - J[n - 1];
+    return;
+  }
+  const int base = nmax > (int)x ? nmax : (int)x;
+  const int m = 2 * ((base + 20 + (int)std::sqrt(60.0 * base)) / 2);
+  double F[64];
+  double fp = 0.0, f = 1.0;
+  for (int j = m; j > 0; --j) {
+    const double fm = (2.0 * j / x) * f - fp;
+    fp = f;
+    f = fm;
+    if (std::fabs(f) > 1e10) {
+      f *= 1e-10;
+      fp *= 1e-10;
+      for (int i = j + 1; i <= nmax; ++i) F[i] *= 1e-10;
+    }
+    if (j <= nmax) F[j] = fp;
+  }
+  F[0] = f;
+  const double s = (std::fabs(j0) >= std::fabs(j1) || nmax < 1) ? j0 / F[0] : j1 / F[1];
+  for (int i = 0; i <= nmax; ++i) J[i] = F[i] * s;
+}
+
 // GMRES/G_FMM2DTree.hpp:670-672 (and FarFieldInteraction.hpp:96-98).
 inline double chebT(double x, int n) { return std::cos(n * std::acos(x)); }
 

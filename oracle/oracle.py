@@ -77,6 +77,10 @@ def lib():
         L.ora_colpiv_solve.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp]
         L.ora_adaptive_report.restype = ctypes.c_int
         L.ora_adaptive_report.argtypes = [ctypes.POINTER(OraCfg), ctypes.c_int, ip, ip, ctypes.c_int]
+        L.ora_bessel_jy_orders.argtypes = [ctypes.c_int, ctypes.c_double, dp, dp]
+        L.ora_bessel_jy_orders.restype = None
+        L.ora_adaptive_set_per_order_bessel.argtypes = [ctypes.c_int]
+        L.ora_adaptive_set_per_order_bessel.restype = None
         L.ora_adaptive_skeletons.restype = ctypes.c_long
         L.ora_adaptive_skeletons.argtypes = [ctypes.POINTER(OraCfg), ctypes.c_int, ip, ctypes.c_long]
         _lib = L
@@ -212,18 +216,25 @@ def colpiv_solve(A, b):
     return x
 
 
-def adaptive_report(cfg, tree_adaptivity):
+def adaptive_report(cfg, tree_adaptivity, per_order_bessel=True):
     """Adaptive-tree assembly statistics (ls_oracle_adaptive.cpp).
 
     Returns {"nLevels", "level_LFR", "N", "levels": [...]}; each level entry
     is one line the reference prints while choosing NCA skeletons
     (GMRES/G_FMM2DTree.hpp:2238, 2384, 3418, 3570): direction "O"/"I",
-    level j, Nboxes, k (HFR levels only, else None), rows, cols, Crank."""
+    level j, Nboxes, k (HFR levels only, else None), rows, cols, Crank.
+    per_order_bessel: far-field Bessel orders from one library call each, as
+    the reference calls Boost (default), or from the recurrence that the
+    uniform oracle and the library use."""
     c = make_cfg(cfg)
     head = (ctypes.c_int * 4)()
     cap = 7 * 64
     rec = (ctypes.c_int * cap)()
-    n = lib().ora_adaptive_report(ctypes.byref(c), int(tree_adaptivity), head, rec, cap)
+    lib().ora_adaptive_set_per_order_bessel(1 if per_order_bessel else 0)
+    try:
+        n = lib().ora_adaptive_report(ctypes.byref(c), int(tree_adaptivity), head, rec, cap)
+    finally:
+        lib().ora_adaptive_set_per_order_bessel(0)
     if n < 0:
         raise ValueError("ora_adaptive_report: invalid configuration")
     levels = []
@@ -248,14 +259,28 @@ def _parse_skeletons(buf, n_lists, skip):
     return out
 
 
-def adaptive_skeletons(cfg, tree_adaptivity):
+def adaptive_skeletons(cfg, tree_adaptivity, per_order_bessel=False):
     """{(j, k, cone): [out_charge, out_check, in_charge, in_check]} of the
-    adaptive restatement; tree_adaptivity < 0 builds the uniform tree."""
+    adaptive restatement; tree_adaptivity < 0 builds the uniform tree.
+    per_order_bessel as in adaptive_report (default: the shared recurrence,
+    the method of the uniform oracle)."""
     c = make_cfg(cfg)
-    n = lib().ora_adaptive_skeletons(ctypes.byref(c), int(tree_adaptivity), None, 0)
-    if n < 0:
-        raise ValueError("ora_adaptive_skeletons: invalid configuration")
-    buf = np.empty(n, dtype=np.int32)
-    lib().ora_adaptive_skeletons(ctypes.byref(c), int(tree_adaptivity),
-                                 buf.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+    lib().ora_adaptive_set_per_order_bessel(1 if per_order_bessel else 0)
+    try:
+        n = lib().ora_adaptive_skeletons(ctypes.byref(c), int(tree_adaptivity), None, 0)
+        if n < 0:
+            raise ValueError("ora_adaptive_skeletons: invalid configuration")
+        buf = np.empty(n, dtype=np.int32)
+        lib().ora_adaptive_skeletons(ctypes.byref(c), int(tree_adaptivity),
+                                     buf.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+    finally:
+        lib().ora_adaptive_set_per_order_bessel(0)
     return _parse_skeletons(buf, 4, 0)
+
+
+def bessel_jy_orders(nmax, x):
+    """J_0..J_nmax(x), Y_0..Y_nmax(x) by the far-field recurrences."""
+    J = np.empty(nmax + 1)
+    Y = np.empty(nmax + 1)
+    lib().ora_bessel_jy_orders(int(nmax), float(x), _dp(J), _dp(Y))
+    return J, Y
