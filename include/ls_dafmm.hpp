@@ -15,11 +15,15 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstdint>
+#include <cstring>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "ls_dafmm.h"
+#include "ls_fno.h"
 
 namespace ls {
 
@@ -143,6 +147,21 @@ class DFMM {
     return out;
   }
 
+  // The density phi at other points, by the reference's Chebyshev-Q+
+  // interpolation (hybridTrueValidation_gmres.cpp:187-219, "Psi_non_grid").
+  Vec Interpolate(const std::vector<pts2D>& pts, const Vec& phi) const {
+    std::vector<double> xy(2 * pts.size());
+    for (size_t i = 0; i < pts.size(); ++i) {
+      xy[2 * i] = pts[i].x;
+      xy[2 * i + 1] = pts[i].y;
+    }
+    Vec out(pts.size());
+    check(ls_op_interpolate(op, (int)pts.size(), xy.data(), reinterpret_cast<const double*>(phi.data()),
+                            reinterpret_cast<double*>(out.data())),
+          "ls_op_interpolate");
+    return out;
+  }
+
   // Solves for all right-hand sides together (mixed precision, FP64 residual
   // per column). Returns the number of FP32 block applies plus FP64 products.
   int SolveBatched(const std::vector<Vec>& B, std::vector<Vec>& X, double tol = 1e-8, int max_outer = 20,
@@ -161,6 +180,88 @@ class DFMM {
     return nmv;
   }
 };
+
+// Writes v as the reference's result files do (GMRES/GMRES.cpp:391-397):
+// one "(re,im)" per line, six significant digits.
+inline void WriteResult(const std::string& path, const Vec& v) {
+  check(ls_write_result(path.c_str(), (int)v.size(), reinterpret_cast<const double*>(v.data())), "ls_write_result");
+}
+
+// The learned preconditioner (include/ls_fno.h): a spectral neural operator
+// read from a weights file ("LSFNO001", five int32: grid, modes, layers,
+// proj_width, dtype 0 = float32 / 1 = float16, then the parameters), used
+// as initial guess and right preconditioner of the mixed-precision flexible
+// GMRES. No counterpart in the reference, whose GMRES is unpreconditioned.
+class LearnedPreconditioner {
+ public:
+  ls_fno* net = nullptr;
+
+  LearnedPreconditioner(const std::string& path, int device = 0) {
+    std::ifstream f(path, std::ios::binary);
+    char magic[8];
+    int32_t hdr[5];
+    if (!f.read(magic, 8) || std::memcmp(magic, "LSFNO001", 8) != 0 ||
+        !f.read(reinterpret_cast<char*>(hdr), sizeof hdr))
+      throw Error(LS_E_INVALID, path + ": not a network weights file");
+    ls_fno_config c{hdr[0], hdr[1], hdr[2], hdr[3]};
+    check(ls_fno_create(&c, device, 0, &net), "ls_fno_create");
+    long long n = 0;
+    check(ls_fno_num_params(net, &n), "ls_fno_num_params");
+    std::vector<float> p((size_t)n);
+    if (hdr[4] == 1) {
+      std::vector<uint16_t> h((size_t)n);
+      if (!f.read(reinterpret_cast<char*>(h.data()), (std::streamsize)(2 * n))) throw Error(LS_E_INVALID, path + ": short");
+      for (long long i = 0; i < n; ++i) p[(size_t)i] = half_to_float(h[(size_t)i]);
+    } else if (!f.read(reinterpret_cast<char*>(p.data()), (std::streamsize)(4 * n))) {
+      throw Error(LS_E_INVALID, path + ": short");
+    }
+    check(ls_fno_set_params(net, p.data()), "ls_fno_set_params");
+  }
+  LearnedPreconditioner(const LearnedPreconditioner&) = delete;
+  LearnedPreconditioner& operator=(const LearnedPreconditioner&) = delete;
+  ~LearnedPreconditioner() { ls_fno_destroy(net); }
+
+  // Solves S x = b to the FP64 relative residual tol (flags: LS_NN_GUESS,
+  // LS_NN_PRECOND); returns the solver's report.
+  ls_nn_report Solve(class DFMM* S, const Vec& b, Vec& x, double tol = 1e-8,
+                     int flags = LS_NN_GUESS | LS_NN_PRECOND, int max_outer = 20, int inner = 400);
+
+  // IEEE 754 binary16 -> binary32.
+  static float half_to_float(uint16_t h) {
+    const uint32_t sign = (uint32_t)(h & 0x8000u) << 16;
+    int e = (h >> 10) & 0x1f;
+    uint32_t m = h & 0x3ffu, bits;
+    if (e == 0x1f) {
+      bits = sign | 0x7f800000u | (m << 13);
+    } else if (e != 0) {
+      bits = sign | ((uint32_t)(e - 15 + 127) << 23) | (m << 13);
+    } else if (m == 0) {
+      bits = sign;
+    } else {  // subnormal: normalise
+      e = -14;
+      while (!(m & 0x400u)) {
+        m <<= 1;
+        --e;
+      }
+      m &= 0x3ffu;
+      bits = sign | ((uint32_t)(e + 127) << 23) | (m << 13);
+    }
+    float out;
+    std::memcpy(&out, &bits, sizeof out);
+    return out;
+  }
+};
+
+inline ls_nn_report LearnedPreconditioner::Solve(DFMM* S, const Vec& b, Vec& x, double tol, int flags, int max_outer,
+                                                 int inner) {
+  check(ls_op_enable_f32(S->op), "ls_op_enable_f32");
+  x.resize(b.size());
+  ls_nn_report rep{};
+  const ls_status s = ls_fgmres_nn(S->op, net, reinterpret_cast<const double*>(b.data()), flags, max_outer, inner,
+                                   tol, reinterpret_cast<double*>(x.data()), nullptr, &rep);
+  if (s != LS_OK && s != LS_E_NOT_CONVERGED) check(s, "ls_fgmres_nn");
+  return rep;
+}
 
 // Fixed-m GMRES with `restart` cycles, x0 = 0 (GMRES/GMRES.cpp:307-319).
 inline void RestartedGMRES(int restart, DFMM* S, int m, const inputsToDFMM&, const Vec& b, Vec& solution) {

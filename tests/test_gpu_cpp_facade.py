@@ -9,11 +9,20 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_reference_style_cpp_driver(ls):
-    exe = os.path.join(os.path.dirname(ls.LIB_PATH), "gmres_driver")
-    out = subprocess.run([exe, "4", "10", "8", "0"], capture_output=True, text=True, timeout=600)
+def test_reference_style_cpp_driver(ls, tmp_path):
+    pkg = os.path.dirname(ls.LIB_PATH)
+    exe = os.path.join(pkg, "gmres_driver")
+    result = tmp_path / "Phi_1_10"
+    weights = os.path.join(pkg, "weights", "fno_k10_40.lsfno")
+    args = [exe, "4", "10", "8", "0", str(result)] + ([weights] if os.path.exists(weights) else [])
+    out = subprocess.run(args, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr
     r = json.loads(out.stdout.strip().splitlines()[-1])
+    lines = result.read_text().splitlines()
+    assert len(lines) == r["N"] and lines[0].startswith("(") and lines[0].endswith(")")
+    assert r["interpolation_error"] <= 1e-12
+    if os.path.exists(weights):
+        assert r["nn_residual"] <= 1.5e-8 and r["nn_network_applies"] >= 1
     assert r["N"] == 9216
     assert r["estimate"] <= 1e-10
     assert r["residual"] <= 2e-10
