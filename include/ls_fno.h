@@ -23,7 +23,8 @@
  * [proj][32], [proj], [2][proj], [2].
  * All device pointers are on the net's (operator's) device. `stream` is the
  * cudaStream_t the work is queued on, NULL being CUDA's default stream, so
- * that buffers written on the caller's stream are read in order.
+ * that buffers written on the caller's stream are read in order. A net keeps
+ * its activations in its own buffers: use one net from one stream at a time.
  */
 #ifndef LS_FNO_H
 #define LS_FNO_H

@@ -606,7 +606,9 @@ ls_status ls_fgmres_nn(ls_op* op, ls_fno* net, const double* b, int flags, int m
   std::string err;
   Precond32* M = nullptr;
   if (flags) {
-    if (!op->nn || op->nn_net != net) {
+    // Rebuilt for another net, or for one with another grid (a new net may
+    // reuse a destroyed one's address).
+    if (!op->nn || op->nn_net != net || op->nn->gs.G != net->net.shape.grid) {
       if (!op->nn) op->nn.reset(new NnPrecond());
       op->nn_net = nullptr;
       if (!op->nn->init(op->host, &net->net, err)) return fail(LS_E_CUDA, "ls_fgmres_nn: " + err);
