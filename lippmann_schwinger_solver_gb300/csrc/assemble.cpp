@@ -992,7 +992,29 @@ static int pow2_ceil(int v) {
   return p;
 }
 
-static void finalize(GemvPhase& ph) {
+// Tile knobs of one phase kind ("UP", "M2L", "DOWN"): the largest rows per
+// tile (1, 2, 4 or 8) and the warps per SM that the tile count aims at.
+// Defaults 8 and 48; the environment variable LS_TILE_<kind> = "rows,warps"
+// overrides them (set by lippmann_schwinger_solver_gb300.autotune, which
+// times the candidates on the GPU).
+struct TileKnobs {
+  int rows = 8;
+  int warps = 48;
+};
+
+static TileKnobs tile_knobs(const char* kind) {
+  TileKnobs k;
+  const std::string name = std::string("LS_TILE_") + kind;
+  const char* v = std::getenv(name.c_str());
+  int r = 0, w = 0;
+  if (v && std::sscanf(v, "%d,%d", &r, &w) == 2 && (r == 1 || r == 2 || r == 4 || r == 8) && w >= 1 && w <= 1024) {
+    k.rows = r;
+    k.warps = w;
+  }
+  return k;
+}
+
+static void finalize(GemvPhase& ph, const char* kind) {
   struct Block { size_t r0; int rows, K; };
   std::vector<Block> blocks;
   for (size_t r = 0; r < ph.rows.size();) {
@@ -1002,8 +1024,9 @@ static void finalize(GemvPhase& ph) {
     r = e;
   }
   std::stable_sort(blocks.begin(), blocks.end(), [](const Block& a, const Block& b) { return a.K > b.K; });
-  const long long want_tiles = 152LL * 48;
-  int r_max = 8;
+  const TileKnobs kn = tile_knobs(kind);
+  const long long want_tiles = 152LL * kn.warps;
+  int r_max = kn.rows;
   while (r_max > 1 && (long long)ph.rows.size() < want_tiles * r_max) r_max >>= 1;
   struct T { size_t r0; int rows, S, qmax, K; };
   std::vector<T> tl;
@@ -1162,7 +1185,7 @@ void Builder::pack(HostOperator& op) {
     for (int t = 0; t < nn; ++t)
       if (!T[t].empty())
         add_task(ph, T[t], (int)nodes[j][t].out_charge.size(), (int)src[t].size(), src[t], (int)nodes[j][t].own_charge);
-    finalize(ph);
+    finalize(ph, "UP");
     op.up.push_back(std::move(ph));
   }
 
@@ -1209,7 +1232,7 @@ void Builder::pack(HostOperator& op) {
       add_task(ph, tk.A, tk.rows, tk.K, tk.idx, (int)tk.out);
       std::vector<cd>().swap(tk.A);
     }
-    finalize(ph);
+    finalize(ph, "M2L");
     op.m2l = std::move(ph);
   }
 
@@ -1303,7 +1326,7 @@ void Builder::pack(HostOperator& op) {
       add_task(ph, tasks[t].A, tasks[t].rows, tasks[t].K, tasks[t].idx, (int)tasks[t].out);
       std::vector<cd>().swap(tasks[t].A);
     }
-    finalize(ph);
+    finalize(ph, "DOWN");
     op.down.push_back(std::move(ph));
   }
 }
