@@ -171,7 +171,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cfg = workload_config(ls)
+    cfg = workload_config(ls, args.level)
     from oracle import oracle as ora
 
     ora.build()
@@ -190,8 +190,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
-            "config": {"workload": "uniform level 6, N=147456, kappa=40, 3 seeded bumps, NCA tol 1e-10",
-                       "parallelism": "CPU threads"},
+            "config": {"workload": "uniform level %d, N=%d, kappa=40, 3 seeded bumps (seed %d), NCA tol 1e-10"
+                                   % (args.level, o.N, SEED), "parallelism": "CPU threads"},
             "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": ncores, "kind": "port",
                              "sample": f"{steps} matvecs of the full workload operator; reference build "
                                        "unavailable (Eigen/Boost headers missing)"},
