@@ -145,3 +145,18 @@ def test_many_scatterer_specs_are_seeded_and_in_range():
             assert -0.6 <= cx <= 0.6 and -0.6 <= cy <= 0.6 and 0.5 <= amp <= 1.5 and 0.05 <= w <= 0.2
     cfg = sc.config(*a[0])
     assert cfg.Qchoice == 6 and cfg.nLevelsUniform == a[0][0] and cfg.kappa == a[0][1]
+
+
+def test_training_data_generators(ls):
+    from lippmann_schwinger_solver_gb300 import fno_train as ft
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        kappa, bumps = ft.scatterer(rng)
+        assert 10.0 <= kappa <= 40.0 and 1 <= len(bumps) <= 4
+    op = ls.Operator(ft.operator_config(20.0, [(0.1, 0.2, 1.0, 0.1)], 3, 8), device=-1)
+    B = ft.off_shell_rhs(op, 20.0, 5, np.random.default_rng(4))
+    assert B.shape == (op.N, 5) and B.flags["F_CONTIGUOUS"]
+    q = op.contrast()
+    # each column is -kappa^2 q times a unit-modulus wave
+    assert np.allclose(np.abs(B), (20.0 ** 2) * np.abs(q)[:, None], rtol=1e-12, atol=1e-300)
+    op.close()

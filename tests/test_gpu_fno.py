@@ -241,3 +241,23 @@ def test_trained_network_gain_over_plain_mixed_gmres(ls):
         op.close()
     assert nn_total <= 0.7 * plain_total, (nn_total, plain_total)
     net.close()
+
+
+def test_training_pipeline_reduces_the_loss(ls):
+    """Solver-generated data -> GPU batches -> the network's own forward,
+    backward and Adam kernels: a short run lowers the training loss, and
+    the saved weights load back identically."""
+    from lippmann_schwinger_solver_gb300 import fno_train as ft
+    data = ft.generate(2, 4, 3, 32, seed=5, off_shell=4, log=lambda s: None)
+    assert all(r["max_residual"] <= 1e-6 for r in data["records"])
+    net = ls.FNO(grid=32, modes=6, layers=2, proj_width=64, seed=2)
+    hist = ft.train(net, data, 60, batch=8, lr=3e-3, log_every=20, log=lambda s: None)
+    assert hist[-1][1] < 0.7 * hist[0][1], hist
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "w.lsfno")
+        net.save(path, half=False)
+        back = ls.FNO.load(path)
+        assert np.array_equal(back.get_params(), net.get_params())
+        back.close()
+    net.close()
