@@ -584,6 +584,11 @@ cudaError_t dev_gmres_mixed_flex(DevOperator& d, const double2* b, double2* x, P
   hist.clear();
   rep = FlexReport();
   cudaMemsetAsync(x, 0, (size_t)n * sizeof(double2), d.stream);
+  if (bn == 0.0) {  // b = 0: x = 0 exactly
+    relres = 0.0;
+    hist.push_back(0.0);
+    return cudaStreamSynchronize(d.stream);
+  }
   cudaMemcpyAsync(r, b, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, d.stream);
   relres = 1.0;
   if (guess && bn > 0.0) {

@@ -261,3 +261,17 @@ def test_training_pipeline_reduces_the_loss(ls):
         assert np.array_equal(back.get_params(), net.get_params())
         back.close()
     net.close()
+
+
+def test_zero_right_hand_side(ls):
+    """b = 0 gives x = 0 exactly, with and without the network."""
+    op = ls.Operator(full_cfg(CFG_C1), device=0)
+    op.enable_f32()
+    z = np.zeros(op.N, dtype=np.complex128)
+    x, h, n, rr, code = op.gmres_mixed(z)
+    assert code == ls.LS_OK and rr == 0.0 and not np.any(x)
+    net = ls.FNO(grid=32, modes=6, layers=2, proj_width=64)
+    x, h, rep, code = op.fgmres_nn(net, z)
+    assert code == ls.LS_OK and rep["rel_residual"] == 0.0 and not np.any(x)
+    net.close()
+    op.close()
