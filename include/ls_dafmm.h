@@ -30,6 +30,7 @@ typedef int ls_status;
 #define LS_E_TIMEOUT (-6)     /* a bounded device wait gave up */
 
 #define LS_MAX_BUMPS 8
+#define LS_ASSEMBLE_STAGES 6
 
 /* Precision of the operator blocks and their accumulation. */
 #define LS_PREC_F64 0
@@ -88,6 +89,11 @@ typedef struct {
   long long m2l_entries;   /* complex entries of the M2L blocks */
   long long m2l_bytes;     /* algorithmic bytes of the M2L kernel (FP64) */
   long long m2l_flops;     /* real flops of the M2L kernel */
+  /* Host assembly wall time by stage, seconds: [0] tree geometry and leaf
+     quadrature, [1] precomputations (Chebyshev fits, near blocks, leaf
+     multipoles), [2] interaction lists, [3] NCA skeletons of every level,
+     [4] user checks, [5] block fill, folding and tile packing. */
+  double assemble_stage_seconds[LS_ASSEMBLE_STAGES];
 } ls_op_info_t;
 
 typedef struct ls_op ls_op;

@@ -105,6 +105,7 @@ class _Info(ctypes.Structure):
         ("m2l_entries", ctypes.c_longlong),
         ("m2l_bytes", ctypes.c_longlong),
         ("m2l_flops", ctypes.c_longlong),
+        ("assemble_stage_seconds", ctypes.c_double * 6),
     ]
 
 
@@ -256,7 +257,9 @@ class Operator:
     def _info(self):
         i = _Info()
         _check(lib().ls_op_info(self._h, ctypes.byref(i)), "ls_op_info")
-        return {f: getattr(i, f) for f, _ in _Info._fields_}
+        out = {f: getattr(i, f) for f, _ in _Info._fields_}
+        out["assemble_stage_seconds"] = list(out["assemble_stage_seconds"])
+        return out
 
     def close(self):
         if getattr(self, "_h", None):

@@ -21,12 +21,16 @@
 // reproducible across hosts.
 
 #include <algorithm>
+#include <array>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <limits>
+#include <mutex>
 #include <unordered_map>
 #include <vector>
 
@@ -362,6 +366,111 @@ double contrast_fn(const ls_config& c, double x, double y) {
   }
 }
 
+// ---------------------------------------------------------------- Hankel table
+// Far-field Hankel vectors shared by every task of one assembly. A vector is
+// a function of the two doubles (px - lx, py - ly) alone, so the table is
+// keyed on their bit patterns: a hit returns exactly the vector the caller
+// would have computed, and the skeletons and blocks do not depend on which
+// thread filled a slot first. On a uniform tree the leaf centres are dyadic
+// and a Chebyshev node's offset from its leaf centre rounds the same way in
+// every box of one binade, so few distinct keys occur: at level 5 (kappa 40)
+// 178 thousand against 7.4 million vectors that per-task caches compute.
+using HankelVec = std::array<cd, 2 * kSeries + 1>;
+
+class HankelTable {
+ public:
+  struct Key {
+    uint64_t x, y;
+    bool operator==(const Key& o) const { return x == o.x && y == o.y; }
+  };
+  static Key key(double rx, double ry) {
+    Key k;
+    std::memcpy(&k.x, &rx, sizeof(double));
+    std::memcpy(&k.y, &ry, sizeof(double));
+    return k;
+  }
+  static uint64_t hash(const Key& k) {
+    uint64_t h = k.x * 0x9E3779B97F4A7C15ULL ^ (k.y + 0xC2B2AE3D27D4EB4FULL + (k.x << 6) + (k.x >> 2));
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ULL;
+    return h ^ (h >> 29);
+  }
+  // Stored vector for `k`, or nullptr.
+  const cd* find(const Key& k) {
+    const uint64_t h = hash(k);
+    Shard& sh = shards_[h >> (64 - kShardBits)];
+    std::lock_guard<std::mutex> lk(sh.mu);
+    if (sh.keys.empty()) return nullptr;
+    for (size_t p = h & sh.mask;; p = (p + 1) & sh.mask) {
+      if (sh.keys[p].x == kEmpty) return nullptr;
+      if (sh.keys[p] == k) return sh.vals[p];
+    }
+  }
+  // Stores `v` under `k` unless the table is full; returns the stored vector
+  // (a concurrent insert of the same key keeps the first, bit-identical one)
+  // or nullptr when full. Pointers stay valid until clear().
+  const cd* insert(const Key& k, const HankelVec& v) {
+    const uint64_t h = hash(k);
+    Shard& sh = shards_[h >> (64 - kShardBits)];
+    std::lock_guard<std::mutex> lk(sh.mu);
+    if (sh.keys.empty()) sh.rehash(1024);
+    size_t p = h & sh.mask;
+    for (;; p = (p + 1) & sh.mask) {
+      if (sh.keys[p].x == kEmpty) break;
+      if (sh.keys[p] == k) return sh.vals[p];
+    }
+    if (size_.load(std::memory_order_relaxed) >= kCap) return nullptr;
+    sh.store.push_back(v);
+    sh.keys[p] = k;
+    sh.vals[p] = sh.store.back().data();
+    size_.fetch_add(1, std::memory_order_relaxed);
+    if (2 * sh.store.size() > sh.mask) sh.rehash(2 * (sh.mask + 1));
+    return sh.store.back().data();
+  }
+  void clear() {
+    for (Shard& sh : shards_) {
+      std::vector<Key>().swap(sh.keys);
+      std::vector<const cd*>().swap(sh.vals);
+      std::deque<HankelVec>().swap(sh.store);
+      sh.mask = 0;
+    }
+    size_.store(0);
+  }
+
+ private:
+  // The bits of a relative position: never a NaN, so all-ones marks a free slot.
+  static constexpr uint64_t kEmpty = ~0ULL;
+  static constexpr int kShardBits = 8;
+  // At most 4 million vectors (about 2.1 GB of host memory); beyond that the
+  // tasks keep what they compute to themselves.
+  static constexpr size_t kCap = size_t(1) << 22;
+  // Open addressing with linear probing over a deque of vectors, so a rehash
+  // moves keys and pointers but never a vector.
+  struct Shard {
+    std::mutex mu;
+    std::vector<Key> keys;
+    std::vector<const cd*> vals;
+    std::deque<HankelVec> store;
+    size_t mask = 0;
+    void rehash(size_t cap) {
+      std::vector<Key> nk(cap, Key{kEmpty, kEmpty});
+      std::vector<const cd*> nv(cap, nullptr);
+      for (size_t q = 0; q < keys.size(); ++q) {
+        if (keys[q].x == kEmpty) continue;
+        size_t p = hash(keys[q]) & (cap - 1);
+        while (nk[p].x != kEmpty) p = (p + 1) & (cap - 1);
+        nk[p] = keys[q];
+        nv[p] = vals[q];
+      }
+      keys.swap(nk);
+      vals.swap(nv);
+      mask = cap - 1;
+    }
+  };
+  Shard shards_[1 << kShardBits];
+  std::atomic<size_t> size_{0};
+};
+
 // ---------------------------------------------------------------- the builder
 struct Node {
   bool out_active = false, in_active = false;
@@ -400,6 +509,7 @@ class Builder {
   std::vector<double> Qpinv;          // nb x rank, row major
   std::vector<std::vector<std::vector<int>>> nbrs;  // [level][box] same-level neighbours
   std::vector<std::vector<Node>> nodes;             // [level][node]
+  mutable HankelTable htab;                         // shared by NCA and block fills
 
   bool is_lfr(int j) const { return j >= level_LFR; }
   int nodes_at(int j) const { return is_lfr(j) ? (1 << (2 * j)) : (1 << (2 * j)) * nCones[j]; }
@@ -411,13 +521,11 @@ class Builder {
     return is_lfr(jchild) ? lfr(jchild, kchild) : cone(jchild, kchild, parent_cone / 2);
   }
 
-  // Far-field kernel entry (G_FMM2DTree.hpp:603-658) from a cached Hankel
-  // vector h_n = (J_n + i Y_n) e^{i n theta} of target i about leaf(j).
-  void hankel(int i, int leaf, cd* h) const {
-    const double px = gx_[i], py = gy_[i];
-    const double lx = cx[nL][leaf], ly = cy[nL][leaf];
-    const double th = std::atan2(py - ly, px - lx);
-    const double R2 = (py - ly) * (py - ly) + (px - lx) * (px - lx);
+  // Far-field Hankel vector h_n = (J_n + i Y_n) e^{i n theta}, n = -15..15,
+  // of a target at (rx, ry) from a leaf centre (G_FMM2DTree.hpp:603-658).
+  void hankel_rel(double rx, double ry, cd* h) const {
+    const double th = std::atan2(ry, rx);
+    const double R2 = ry * ry + rx * rx;
     const double R = kappa * std::sqrt(R2);
     double J[kSeries + 1], Y[kSeries + 1];
     bessel_jy_orders(kSeries, R, J, Y);
@@ -429,24 +537,76 @@ class Builder {
       h[n + kSeries] = (jn + kI * yn) * std::exp(kI * double(n) * th);
     }
   }
+  // Per-task cache of target i about leaf(j), over the shared table: open
+  // addressing on the key i * 2^20 + leaf (-1 marks a free slot).
   struct HCache {
     const Builder* b;
-    std::unordered_map<long long, std::vector<cd>> m;
+    std::vector<long long> keys;
+    std::vector<const cd*> vals;
+    size_t used = 0;
+    std::deque<HankelVec> own;  // vectors the full table did not take
+    long long last_key = -1;    // rows and columns visit a leaf's points in runs
+    const cd* last = nullptr;
+    static size_t slot(long long key, size_t mask) {
+      uint64_t h = (uint64_t)key * 0x9E3779B97F4A7C15ULL;
+      return (size_t)(h ^ (h >> 32)) & mask;
+    }
+    void grow() {
+      const size_t cap = keys.empty() ? 4096 : 2 * keys.size();
+      std::vector<long long> nk(cap, -1);
+      std::vector<const cd*> nv(cap, nullptr);
+      for (size_t q = 0; q < keys.size(); ++q) {
+        if (keys[q] < 0) continue;
+        size_t p = slot(keys[q], cap - 1);
+        while (nk[p] >= 0) p = (p + 1) & (cap - 1);
+        nk[p] = keys[q];
+        nv[p] = vals[q];
+      }
+      keys.swap(nk);
+      vals.swap(nv);
+    }
     const cd* get(int i, int leaf) {
       const long long key = (long long)i * 1048576LL + leaf;
-      auto it = m.find(key);
-      if (it != m.end()) return it->second.data();
-      std::vector<cd> h(2 * kSeries + 1);
-      b->hankel(i, leaf, h.data());
-      return m.emplace(key, std::move(h)).first->second.data();
+      if (key == last_key) return last;
+      last_key = key;
+      if (2 * (used + 1) > keys.size()) grow();
+      const size_t mask = keys.size() - 1;
+      size_t p = slot(key, mask);
+      for (; keys[p] >= 0; p = (p + 1) & mask)
+        if (keys[p] == key) return last = vals[p];
+      const double rx = b->gx_[i] - b->cx[b->nL][leaf], ry = b->gy_[i] - b->cy[b->nL][leaf];
+      const HankelTable::Key k = HankelTable::key(rx, ry);
+      const cd* h = b->htab.find(k);
+      if (!h) {
+        HankelVec v;
+        b->hankel_rel(rx, ry, v.data());
+        h = b->htab.insert(k, v);
+        if (!h) {
+          own.push_back(v);
+          h = own.back().data();
+        }
+      }
+      keys[p] = key;
+      vals[p] = h;
+      ++used;
+      return last = h;
     }
   };
   cd entry(int i, int j, HCache& hc) const {
     const cd* h = hc.get(i, j / rank);
     const int idx = j % rank;
     const int nS = 2 * kSeries + 1;
-    cd s = 0.0 + 0.0 * kI;
-    for (int n = 0; n < nS; ++n) s += Mleaf[(size_t)idx * nS + n] * h[n];
+    const cd* m = &Mleaf[(size_t)idx * nS];
+    // sum_n M_n h_n in real arithmetic with the operand order of the complex
+    // product, (a + ib)(c + id) = (ac - bd) + i(ad + bc), so the sum equals
+    // the std::complex one bit for bit without its per-product NaN checks.
+    double sr = 0.0, si = 0.0;
+    for (int n = 0; n < nS; ++n) {
+      const double a = m[n].real(), b = m[n].imag(), c = h[n].real(), d = h[n].imag();
+      sr += a * c - b * d;
+      si += a * d + b * c;
+    }
+    cd s(sr, si);
     s *= kI / 4.0;
     if (cfg.findPhi) {
       s *= kq_[i];
@@ -1345,13 +1505,26 @@ bool Builder::run(HostOperator& op, std::string& err) {
   if (cfg.Qchoice == 6 && (cfg.n_bumps < 1 || cfg.n_bumps > LS_MAX_BUMPS)) { err = "n_bumps must be in [1, 8]"; return false; }
   if (cfg.nCones_LFR < 1 || cfg.TOL_POW < 1 || cfg.TOL_POW > 16) { err = "nCones_LFR >= 1 and TOL_POW in [1, 16] required"; return false; }
   if ((long long)(1LL << (2 * cfg.nLevelsUniform)) * cfg.nChebNodes * cfg.nChebNodes > (1LL << 28)) { err = "problem too large"; return false; }
+  auto lap = [t = t0]() mutable {
+    const auto now = std::chrono::steady_clock::now();
+    const double s = std::chrono::duration<double>(now - t).count();
+    t = now;
+    return s;
+  };
   geometry();
+  op.stage_seconds[0] = lap();
   precompute();
+  op.stage_seconds[1] = lap();
   interaction_lists();
+  op.stage_seconds[2] = lap();
   for (int j = nL; j >= level_LFR; --j) nca_level_lfr(j);
   for (int j = level_LFR - 1; j >= 2; --j) nca_level_hfr(j);
+  op.stage_seconds[3] = lap();
   user_checks();
+  op.stage_seconds[4] = lap();
   pack(op);
+  htab.clear();
+  op.stage_seconds[5] = lap();
   // Operator-level data for the near field and the C ABI.
   op.cfg = cfg;
   op.N = N;

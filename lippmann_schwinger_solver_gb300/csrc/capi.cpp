@@ -145,6 +145,7 @@ ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
   o->matvec_flops = 8LL * far + 8LL * nnz_near * h.rank * h.rank;
   o->device_bytes = d.device_bytes;
   o->assemble_seconds = h.assemble_seconds;
+  for (int i = 0; i < LS_ASSEMBLE_STAGES; ++i) o->assemble_stage_seconds[i] = h.stage_seconds[i];
   o->max_rank = h.max_rank;
   // double-float: the near field takes a GEMM and a gather kernel
   o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 1 : 0);

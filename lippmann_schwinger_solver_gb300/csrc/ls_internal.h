@@ -72,6 +72,7 @@ struct HostOperator {
   std::vector<int> skeleton_dump;
   int max_rank = 0;
   double assemble_seconds = 0.0;
+  double stage_seconds[LS_ASSEMBLE_STAGES] = {};  // ls_op_info_t::assemble_stage_seconds
 };
 
 // assemble.cpp

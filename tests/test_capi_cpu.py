@@ -78,6 +78,10 @@ def test_host_only_operator_refuses_device_calls(ls):
     info = op.info
     assert info["far_entries"] > 0 and info["matvec_flops"] > 8 * info["far_entries"]
     assert info["m2l_entries"] <= info["far_entries"]
+    # Stage times: six non-negative laps that add up to the total.
+    stages = info["assemble_stage_seconds"]
+    assert len(stages) == 6 and min(stages) >= 0.0 and stages[3] > 0.0
+    assert sum(stages) == pytest.approx(info["assemble_seconds"], rel=1e-3, abs=1e-3)
     op.close()
 
 
