@@ -387,6 +387,8 @@ def run_ours(args):
                    "achieved_gbs": info["matvec_bytes"] / (ms * 1e-3) / 1e9,
                    "achieved_fp64_tflops": info["matvec_flops"] / (ms * 1e-3) / 1e12,
                    "assemble_s": info["assemble_seconds"], "device_bytes": info["device_bytes"],
+                   "assemble_stages_s": dict(zip(("geometry", "precompute", "lists", "nca", "checks", "pack"),
+                                                 (round(t, 3) for t in info["assemble_stage_seconds"]))),
                    "far_entries": info["far_entries"], "max_rank": info["max_rank"]},
         "clocks": clk.summary(),
         "other_f64_kernels": alt,
