@@ -1122,15 +1122,46 @@ void Builder::user_checks() {
 }
 
 // Appends a row-major block (rows x K) with its gather list to a phase.
-static void add_task(GemvPhase& ph, const std::vector<cd>& rowmajor, int rows, int K, const std::vector<int>& idx,
-                     int out_off) {
-  if (rows <= 0 || K <= 0) return;
-  const long long a0 = (long long)ph.stageA.size();
-  const int i0 = (int)ph.stageIdx.size();
-  ph.stageA.insert(ph.stageA.end(), rowmajor.begin(), rowmajor.begin() + (size_t)rows * K);
-  ph.stageIdx.insert(ph.stageIdx.end(), idx.begin(), idx.end());
-  for (int r = 0; r < rows; ++r) ph.rows.push_back({a0 + (long long)r * K, K, i0, out_off + r});
-  ph.nnz += (long long)rows * K;
+// Appends blocks to a phase's staging arrays, in the order t = 0..n-1:
+// get(t) gives block t (rows x K, row major; nidx >= K gather indices; its
+// first row writes output element `out`), rows or K = 0 skips it. Offsets
+// come from a prefix sum, so the copies run in parallel; done(t) runs after
+// block t is copied (to free it).
+struct BlockView {
+  const cd* A;
+  int rows, K;
+  const int* idx;
+  int nidx;
+  int out;
+};
+template <class Get, class Done>
+static void stage_blocks(GemvPhase& ph, int n, Get get, Done done) {
+  std::vector<long long> ao((size_t)n + 1), io((size_t)n + 1), ro((size_t)n + 1);
+  ao[0] = (long long)ph.stageA.size();
+  io[0] = (long long)ph.stageIdx.size();
+  ro[0] = (long long)ph.rows.size();
+  for (int t = 0; t < n; ++t) {
+    const BlockView v = get(t);
+    const bool use = v.rows > 0 && v.K > 0;
+    ao[t + 1] = ao[t] + (use ? (long long)v.rows * v.K : 0);
+    io[t + 1] = io[t] + (use ? v.nidx : 0);
+    ro[t + 1] = ro[t] + (use ? v.rows : 0);
+  }
+  ph.nnz += ao[n] - ao[0];
+  ph.stageA.resize((size_t)ao[n]);
+  ph.stageIdx.resize((size_t)io[n]);
+  ph.rows.resize((size_t)ro[n]);
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int t = 0; t < n; ++t) {
+    const BlockView v = get(t);
+    if (v.rows > 0 && v.K > 0) {
+      std::copy(v.A, v.A + (size_t)v.rows * v.K, ph.stageA.begin() + ao[t]);
+      std::copy(v.idx, v.idx + v.nidx, ph.stageIdx.begin() + io[t]);
+      for (int r = 0; r < v.rows; ++r)
+        ph.rows[(size_t)(ro[t] + r)] = {ao[t] + (long long)r * v.K, v.K, (int)io[t], v.out + r};
+    }
+    done(t);
+  }
 }
 
 // Packs the staged blocks into warp tiles (see GemvTile). A tile holds R
@@ -1188,9 +1219,10 @@ static void finalize(GemvPhase& ph, const char* kind) {
   const long long want_tiles = 152LL * kn.warps;
   int r_max = kn.rows;
   while (r_max > 1 && (long long)ph.rows.size() < want_tiles * r_max) r_max >>= 1;
-  struct T { size_t r0; int rows, S, qmax, K; };
+  struct T { size_t r0; int rows, S, qmax, K; long long off, ioff; int row_base; };
   std::vector<T> tl;
   long long total = 0, total_idx = 0;
+  int total_rows = 0;
   for (const Block& b : blocks) {
     const int r_min = std::min(kTileLanes, pow2_ceil((128 + b.K - 1) / b.K));
     const int rcap = std::max(r_max, r_min);
@@ -1202,9 +1234,10 @@ static void finalize(GemvPhase& ph, const char* kind) {
       const int rows = std::min(R, rem);
       const int S = kTileLanes / R;
       const int qmax = (b.K + S - 1) / S;
-      tl.push_back({b.r0 + (size_t)done, rows, S, qmax, b.K});
+      tl.push_back({b.r0 + (size_t)done, rows, S, qmax, b.K, total, total_idx, total_rows});
       total += (long long)qmax * kTileLanes;
       total_idx += (long long)qmax * S;
+      total_rows += rows;
       done += rows;
     }
   }
@@ -1212,9 +1245,9 @@ static void finalize(GemvPhase& ph, const char* kind) {
   ph.idx.assign((size_t)total_idx, 0);
   ph.out.assign(ph.rows.size(), 0);
   ph.klen.assign(tl.size() * kTileLanes, 0);
-  ph.tiles.clear();
-  long long off = 0, ioff = 0;
-  int row_base = 0;
+  // Tiles own disjoint ranges of A, idx, klen and out: fill them in parallel.
+  ph.tiles.assign(tl.size(), GemvTile{});
+#pragma omp parallel for schedule(dynamic, 64)
   for (size_t t = 0; t < tl.size(); ++t) {
     const T& d = tl[t];
     const int R = kTileLanes / d.S;
@@ -1224,23 +1257,20 @@ static void finalize(GemvPhase& ph, const char* kind) {
     for (int q = 0; q < d.qmax; ++q)
       for (int sl = 0; sl < d.S; ++sl) {
         const int k = q * d.S + sl;
-        if (k < d.K) ph.idx[(size_t)(ioff + (long long)q * d.S + sl)] = ph.stageIdx[(size_t)first.idx + k];
+        if (k < d.K) ph.idx[(size_t)(d.ioff + (long long)q * d.S + sl)] = ph.stageIdx[(size_t)first.idx + k];
       }
     for (int r = 0; r < d.rows; ++r) {
       const GemvPhase::Row& row = ph.rows[d.r0 + r];
-      ph.out[(size_t)row_base + r] = row.out;
+      ph.out[(size_t)d.row_base + r] = row.out;
       for (int sl = 0; sl < d.S; ++sl) {
         const int lane = sl * R + r;
         int q = 0;
         for (int k = sl; k < row.K; k += d.S, ++q)
-          ph.A[(size_t)(off + (long long)q * kTileLanes + lane)] = ph.stageA[(size_t)(row.a + k)];
+          ph.A[(size_t)(d.off + (long long)q * kTileLanes + lane)] = ph.stageA[(size_t)(row.a + k)];
         ph.klen[t * kTileLanes + lane] = q;
       }
     }
-    ph.tiles.push_back({off, ioff, d.qmax, d.rows, log2s, (int)(t * kTileLanes), row_base});
-    off += (long long)d.qmax * kTileLanes;
-    ioff += (long long)d.qmax * d.S;
-    row_base += d.rows;
+    ph.tiles[t] = {d.off, d.ioff, d.qmax, d.rows, log2s, (int)(t * kTileLanes), d.row_base};
   }
   std::vector<cd>().swap(ph.stageA);
   std::vector<int>().swap(ph.stageIdx);
@@ -1342,9 +1372,14 @@ void Builder::pack(HostOperator& op) {
       T[t] = std::move(Tm);
       src[t] = std::move(s);
     }
-    for (int t = 0; t < nn; ++t)
-      if (!T[t].empty())
-        add_task(ph, T[t], (int)nodes[j][t].out_charge.size(), (int)src[t].size(), src[t], (int)nodes[j][t].own_charge);
+    stage_blocks(
+        ph, nn,
+        [&](int t) {
+          if (T[t].empty()) return BlockView{nullptr, 0, 0, nullptr, 0, 0};
+          return BlockView{T[t].data(), (int)nodes[j][t].out_charge.size(), (int)src[t].size(), src[t].data(),
+                           (int)src[t].size(), (int)nodes[j][t].own_charge};
+        },
+        [&](int t) { std::vector<cd>().swap(T[t]); });
     finalize(ph, "UP");
     op.up.push_back(std::move(ph));
   }
@@ -1386,12 +1421,16 @@ void Builder::pack(HostOperator& op) {
     }
     GemvPhase ph;
     op.m2l_rows = 0;
-    for (auto& tk : tasks) {
-      if (tk.K == 0) continue;
-      op.m2l_rows += tk.rows;
-      add_task(ph, tk.A, tk.rows, tk.K, tk.idx, (int)tk.out);
-      std::vector<cd>().swap(tk.A);
-    }
+    for (auto& tk : tasks)
+      if (tk.K != 0) op.m2l_rows += tk.rows;
+    stage_blocks(
+        ph, (int)tasks.size(),
+        [&](int u) {
+          const Task& tk = tasks[u];
+          if (tk.K == 0) return BlockView{nullptr, 0, 0, nullptr, 0, 0};
+          return BlockView{tk.A.data(), tk.rows, tk.K, tk.idx.data(), (int)tk.idx.size(), (int)tk.out};
+        },
+        [&](int u) { std::vector<cd>().swap(tasks[u].A); });
     finalize(ph, "M2L");
     op.m2l = std::move(ph);
   }
@@ -1481,11 +1520,14 @@ void Builder::pack(HostOperator& op) {
     }
     GemvPhase ph;
     ph.accumulate = 1;
-    for (int t = 0; t < nch; ++t) {
-      if (!tasks[t].any) continue;
-      add_task(ph, tasks[t].A, tasks[t].rows, tasks[t].K, tasks[t].idx, (int)tasks[t].out);
-      std::vector<cd>().swap(tasks[t].A);
-    }
+    stage_blocks(
+        ph, nch,
+        [&](int t) {
+          const Task& tk = tasks[t];
+          if (!tk.any) return BlockView{nullptr, 0, 0, nullptr, 0, 0};
+          return BlockView{tk.A.data(), tk.rows, tk.K, tk.idx.data(), (int)tk.idx.size(), (int)tk.out};
+        },
+        [&](int t) { std::vector<cd>().swap(tasks[t].A); });
     finalize(ph, "DOWN");
     op.down.push_back(std::move(ph));
   }
