@@ -419,7 +419,7 @@ class HankelTable {
       if (sh.keys[p].x == kEmpty) break;
       if (sh.keys[p] == k) return sh.vals[p];
     }
-    if (size_.load(std::memory_order_relaxed) >= kCap) return nullptr;
+    if (size_.load(std::memory_order_relaxed) >= cap_) return nullptr;
     sh.store.push_back(v);
     sh.keys[p] = k;
     sh.vals[p] = sh.store.back().data();
@@ -441,9 +441,15 @@ class HankelTable {
   // The bits of a relative position: never a NaN, so all-ones marks a free slot.
   static constexpr uint64_t kEmpty = ~0ULL;
   static constexpr int kShardBits = 8;
-  // At most 4 million vectors (about 2.1 GB of host memory); beyond that the
-  // tasks keep what they compute to themselves.
-  static constexpr size_t kCap = size_t(1) << 22;
+  // At most 4 million vectors (about 2.1 GB of host memory) unless
+  // LS_HANKEL_TABLE_CAP gives another count; beyond it the tasks keep what
+  // they compute to themselves (same values, computed more than once).
+  static size_t cap_from_env() {
+    const char* v = std::getenv("LS_HANKEL_TABLE_CAP");
+    char* end = nullptr;
+    const long long c = v ? std::strtoll(v, &end, 10) : -1;
+    return (v && end != v && *end == '\0' && c >= 0) ? (size_t)c : (size_t(1) << 22);
+  }
   // Open addressing with linear probing over a deque of vectors, so a rehash
   // moves keys and pointers but never a vector.
   struct Shard {
@@ -469,6 +475,7 @@ class HankelTable {
   };
   Shard shards_[1 << kShardBits];
   std::atomic<size_t> size_{0};
+  const size_t cap_ = cap_from_env();
 };
 
 // ---------------------------------------------------------------- the builder

@@ -28,6 +28,19 @@ def test_library_exports_every_declared_symbol(ls):
     assert b"sm_103a" in L.ls_version()
 
 
+@pytest.mark.parametrize("cap", ["0", "150"])
+def test_hankel_table_overflow_matches_oracle(ls, ora, monkeypatch, cap):
+    """The assembler shares far-field Hankel vectors through a table of
+    bounded size; past the bound (here forced to 0 and 150 vectors) tasks
+    compute and keep their own. Skeletons stay identical to the oracle's,
+    which computes every vector itself."""
+    monkeypatch.setenv("LS_HANKEL_TABLE_CAP", cap)
+    cfg = full_cfg(CFG_HFR)
+    op = ls.Operator(cfg, device=-1)
+    assert np.array_equal(op.skeleton_dump(), ora.Oracle(cfg.as_dict()).skeleton_dump())
+    op.close()
+
+
 @pytest.mark.parametrize("base,over", [
     (CFG_L3_K10, {}),
     (CFG_C1, {}),
