@@ -30,6 +30,7 @@
 #include <cstring>
 #include <deque>
 #include <limits>
+#include <memory>
 #include <mutex>
 #include <unordered_map>
 #include <vector>
@@ -367,14 +368,18 @@ double contrast_fn(const ls_config& c, double x, double y) {
 }
 
 // ---------------------------------------------------------------- Hankel table
-// Far-field Hankel vectors shared by every task of one assembly. A vector is
-// a function of the two doubles (px - lx, py - ly) alone, so the table is
-// keyed on their bit patterns: a hit returns exactly the vector the caller
-// would have computed, and the skeletons and blocks do not depend on which
-// thread filled a slot first. On a uniform tree the leaf centres are dyadic
-// and a Chebyshev node's offset from its leaf centre rounds the same way in
-// every box of one binade, so few distinct keys occur: at level 5 (kappa 40)
-// 178 thousand against 7.4 million vectors that per-task caches compute.
+// Far-field sums shared by every task of one assembly. The far-field entry
+// K(i, j) is a scaling of sum_n M[j mod rank][n] h_n, where the Hankel
+// vector h of target i about leaf(j) is a function of the two doubles
+// (px - lx, py - ly) alone and M is the same for every leaf. So the table is
+// keyed on the bit patterns of that relative position and stores, per key,
+// the sums for all `rank` source nodes of a leaf: a hit returns exactly what
+// the caller would have computed, and skeletons and blocks do not depend on
+// which thread filled a slot first. On a uniform tree the leaf centres are
+// dyadic and a Chebyshev node's offset from its leaf centre rounds the same
+// way in every box of one binade, so few distinct keys occur: at level 5
+// (kappa 40) 178 thousand, where per-task caches computed 7.4 million Hankel
+// vectors and every entry its own 31-term sum.
 using HankelVec = std::array<cd, 2 * kSeries + 1>;
 
 class HankelTable {
@@ -406,10 +411,12 @@ class HankelTable {
       if (sh.keys[p] == k) return sh.vals[p];
     }
   }
-  // Stores `v` under `k` unless the table is full; returns the stored vector
-  // (a concurrent insert of the same key keeps the first, bit-identical one)
-  // or nullptr when full. Pointers stay valid until clear().
-  const cd* insert(const Key& k, const HankelVec& v) {
+  // Records hold `w` complex values; set before the first insert.
+  void set_width(int w) { width_ = (size_t)w; }
+  // Stores the record `v` under `k` unless the table is full; returns the
+  // stored record (a concurrent insert of the same key keeps the first,
+  // bit-identical one) or nullptr when full. Pointers stay valid until clear().
+  const cd* insert(const Key& k, const cd* v) {
     const uint64_t h = hash(k);
     Shard& sh = shards_[h >> (64 - kShardBits)];
     std::lock_guard<std::mutex> lk(sh.mu);
@@ -420,18 +427,22 @@ class HankelTable {
       if (sh.keys[p] == k) return sh.vals[p];
     }
     if (size_.load(std::memory_order_relaxed) >= cap_) return nullptr;
-    sh.store.push_back(v);
+    cd* rec = sh.alloc(width_);
+    std::copy(v, v + width_, rec);
     sh.keys[p] = k;
-    sh.vals[p] = sh.store.back().data();
+    sh.vals[p] = rec;
+    ++sh.used;
     size_.fetch_add(1, std::memory_order_relaxed);
-    if (2 * sh.store.size() > sh.mask) sh.rehash(2 * (sh.mask + 1));
-    return sh.store.back().data();
+    if (2 * sh.used > sh.mask) sh.rehash(2 * (sh.mask + 1));
+    return rec;
   }
   void clear() {
     for (Shard& sh : shards_) {
       std::vector<Key>().swap(sh.keys);
       std::vector<const cd*>().swap(sh.vals);
-      std::deque<HankelVec>().swap(sh.store);
+      std::vector<std::unique_ptr<cd[]>>().swap(sh.chunks);
+      sh.chunk_left = 0;
+      sh.used = 0;
       sh.mask = 0;
     }
     size_.store(0);
@@ -441,23 +452,31 @@ class HankelTable {
   // The bits of a relative position: never a NaN, so all-ones marks a free slot.
   static constexpr uint64_t kEmpty = ~0ULL;
   static constexpr int kShardBits = 8;
-  // At most 4 million vectors (about 2.1 GB of host memory) unless
-  // LS_HANKEL_TABLE_CAP gives another count; beyond it the tasks keep what
-  // they compute to themselves (same values, computed more than once).
+  // At most 4 million records (about 2.4 GB of host memory at 36 nodes per
+  // leaf) unless LS_HANKEL_TABLE_CAP gives another count; beyond it the tasks
+  // keep what they compute to themselves (same values, computed more than
+  // once).
   static size_t cap_from_env() {
     const char* v = std::getenv("LS_HANKEL_TABLE_CAP");
     char* end = nullptr;
     const long long c = v ? std::strtoll(v, &end, 10) : -1;
     return (v && end != v && *end == '\0' && c >= 0) ? (size_t)c : (size_t(1) << 22);
   }
-  // Open addressing with linear probing over a deque of vectors, so a rehash
-  // moves keys and pointers but never a vector.
+  // Open addressing with linear probing; records live in chunks of 4096, so
+  // a rehash moves keys and pointers but never a record.
   struct Shard {
     std::mutex mu;
     std::vector<Key> keys;
     std::vector<const cd*> vals;
-    std::deque<HankelVec> store;
-    size_t mask = 0;
+    std::vector<std::unique_ptr<cd[]>> chunks;
+    size_t chunk_left = 0, used = 0, mask = 0;
+    cd* alloc(size_t w) {
+      if (chunk_left == 0) {
+        chunks.emplace_back(new cd[4096 * w]);
+        chunk_left = 4096;
+      }
+      return chunks.back().get() + (4096 - chunk_left--) * w;
+    }
     void rehash(size_t cap) {
       std::vector<Key> nk(cap, Key{kEmpty, kEmpty});
       std::vector<const cd*> nv(cap, nullptr);
@@ -476,6 +495,7 @@ class HankelTable {
   Shard shards_[1 << kShardBits];
   std::atomic<size_t> size_{0};
   const size_t cap_ = cap_from_env();
+  size_t width_ = 0;
 };
 
 // ---------------------------------------------------------------- the builder
@@ -544,14 +564,35 @@ class Builder {
       h[n + kSeries] = (jn + kI * yn) * std::exp(kI * double(n) * th);
     }
   }
-  // Per-task cache of target i about leaf(j), over the shared table: open
-  // addressing on the key i * 2^20 + leaf (-1 marks a free slot).
+  // Far-field sums of a target at (rx, ry) from a leaf centre for all `rank`
+  // source nodes of the leaf: out[idx] = sum_n M[idx][n] h_n, in real
+  // arithmetic with the operand order of the complex product,
+  // (a + ib)(c + id) = (ac - bd) + i(ad + bc), so each sum equals the
+  // std::complex one bit for bit without its per-product NaN checks.
+  void key_sums(double rx, double ry, cd* out) const {
+    HankelVec h;
+    hankel_rel(rx, ry, h.data());
+    constexpr int nS = 2 * kSeries + 1;
+    for (int idx = 0; idx < rank; ++idx) {
+      const cd* m = &Mleaf[(size_t)idx * nS];
+      double sr = 0.0, si = 0.0;
+      for (int n = 0; n < nS; ++n) {
+        const double a = m[n].real(), b = m[n].imag(), c = h[n].real(), d = h[n].imag();
+        sr += a * c - b * d;
+        si += a * d + b * c;
+      }
+      out[idx] = cd(sr, si);
+    }
+  }
+  // Per-task cache of the far-field sums of target i about leaf(j), over the
+  // shared table: open addressing on the key i * 2^20 + leaf (-1 marks a
+  // free slot).
   struct HCache {
     const Builder* b;
     std::vector<long long> keys;
     std::vector<const cd*> vals;
     size_t used = 0;
-    std::deque<HankelVec> own;  // vectors the full table did not take
+    std::deque<std::vector<cd>> own;  // records the full table did not take
     long long last_key = -1;    // rows and columns visit a leaf's points in runs
     const cd* last = nullptr;
     static size_t slot(long long key, size_t mask) {
@@ -585,11 +626,11 @@ class Builder {
       const HankelTable::Key k = HankelTable::key(rx, ry);
       const cd* h = b->htab.find(k);
       if (!h) {
-        HankelVec v;
-        b->hankel_rel(rx, ry, v.data());
-        h = b->htab.insert(k, v);
+        std::vector<cd> v((size_t)b->rank);
+        b->key_sums(rx, ry, v.data());
+        h = b->htab.insert(k, v.data());
         if (!h) {
-          own.push_back(v);
+          own.push_back(std::move(v));
           h = own.back().data();
         }
       }
@@ -600,20 +641,7 @@ class Builder {
     }
   };
   cd entry(int i, int j, HCache& hc) const {
-    const cd* h = hc.get(i, j / rank);
-    const int idx = j % rank;
-    const int nS = 2 * kSeries + 1;
-    const cd* m = &Mleaf[(size_t)idx * nS];
-    // sum_n M_n h_n in real arithmetic with the operand order of the complex
-    // product, (a + ib)(c + id) = (ac - bd) + i(ad + bc), so the sum equals
-    // the std::complex one bit for bit without its per-product NaN checks.
-    double sr = 0.0, si = 0.0;
-    for (int n = 0; n < nS; ++n) {
-      const double a = m[n].real(), b = m[n].imag(), c = h[n].real(), d = h[n].imag();
-      sr += a * c - b * d;
-      si += a * d + b * c;
-    }
-    cd s(sr, si);
+    cd s = hc.get(i, j / rank)[j % rank];
     s *= kI / 4.0;
     if (cfg.findPhi) {
       s *= kq_[i];
@@ -1563,6 +1591,7 @@ bool Builder::run(HostOperator& op, std::string& err) {
   geometry();
   op.stage_seconds[0] = lap();
   precompute();
+  htab.set_width(rank);
   op.stage_seconds[1] = lap();
   interaction_lists();
   op.stage_seconds[2] = lap();

@@ -42,7 +42,9 @@ def config(level, kappa, bumps, tol_pow=10):
 
 def solve_many(specs, angles=64, tol=1e-8, tol_pow=10, device=0, log=None, keep_solutions=False):
     """Assembles and solves every scatterer; returns per-scatterer records and
-    the totals. Assembly of scatterer k + 1 overlaps the solve of k."""
+    the totals. Assembly of scatterer k + 1 overlaps the solve of k.
+    assemble_s is the operator's creation (host assembly, upload, FP32
+    copy); host_stages_s splits the host assembly by stage."""
     thetas = 2 * np.pi * np.arange(angles) / angles
     recs, sols = [], []
     ready = {}
@@ -73,7 +75,10 @@ def solve_many(specs, angles=64, tol=1e-8, tol_pow=10, device=0, log=None, keep_
         X, nmv, rr, code = op.gmres_mixed_batched(B, max_outer=20, inner_iter=100, tol=tol)
         t_solve = time.perf_counter() - t0
         rec = dict(scatterer=k, level=level, kappa=round(kappa, 3), bumps=len(bumps), N=op.N,
-                   assemble_s=round(t_asm, 3), solve_s=round(t_solve, 4), applies_and_fp64_products=nmv,
+                   assemble_s=round(t_asm, 3),
+                   host_stages_s=dict(zip(("geometry", "precompute", "lists", "nca", "checks", "pack"),
+                                          (round(t, 3) for t in op.info["assemble_stage_seconds"]))),
+                   solve_s=round(t_solve, 4), applies_and_fp64_products=nmv,
                    max_true_residual=float(np.max(rr)), converged=code == LS_OK)
         recs.append(rec)
         if keep_solutions:
