@@ -640,8 +640,8 @@ class Builder {
       return last = h;
     }
   };
-  cd entry(int i, int j, HCache& hc) const {
-    cd s = hc.get(i, j / rank)[j % rank];
+  // K(i, j) from its far-field sum.
+  cd scale(int i, int j, cd s) const {
     s *= kI / 4.0;
     if (cfg.findPhi) {
       s *= kq_[i];
@@ -649,6 +649,7 @@ class Builder {
     }
     return s;
   }
+  cd entry(int i, int j, HCache& hc) const { return scale(i, j, hc.get(i, j / rank)[j % rank]); }
   // Row-major block K(rows, cols).
   void fill(const std::vector<int>& rows, const std::vector<int>& cols, HCache& hc, cd* out, int ld) const {
     for (size_t a = 0; a < rows.size(); ++a)
@@ -693,10 +694,27 @@ static double norm2(const std::vector<cd>& v) {
   for (const cd& z : v) s += std::norm(z);
   return std::sqrt(s);
 }
+// sum_i conj(a_i) b_i. conj(x + iy) (c + id) = (xc - (-y)d) + i(xd + (-y)c),
+// and p - (-q) is the same IEEE operation as p + q, so the real form below
+// equals the std::complex one bit for bit, without its NaN checks.
 static cd cdot(const std::vector<cd>& a, const std::vector<cd>& b) {
-  cd s(0.0, 0.0);
-  for (size_t i = 0; i < a.size(); ++i) s += std::conj(a[i]) * b[i];
-  return s;
+  double sr = 0.0, si = 0.0;
+  for (size_t i = 0; i < a.size(); ++i) {
+    const double x = a[i].real(), y = a[i].imag(), c = b[i].real(), d = b[i].imag();
+    sr += x * c + y * d;
+    si += x * d - y * c;
+  }
+  return cd(sr, si);
+}
+// v[s] -= f * w[s] for all s, with the operand order of the complex product
+// (a + ib)(c + id) = (ac - bd) + i(ad + bc): equal to the std::complex
+// update bit for bit.
+static void sub_scaled(std::vector<cd>& v, cd f, const std::vector<cd>& w) {
+  const double a = f.real(), b = f.imag();
+  for (size_t s = 0; s < w.size(); ++s) {
+    const double c = w[s].real(), d = w[s].imag();
+    v[s] = cd(v[s].real() - (a * c - b * d), v[s].imag() - (a * d + b * c));
+  }
 }
 
 // Partially pivoted cross approximation that keeps only the pivots
@@ -709,7 +727,26 @@ int Builder::aca(const std::vector<int>& rows, const std::vector<int>& cols, dou
   std::vector<std::vector<cd>> U, V, piv_rows;
   std::vector<cd> row(n2), col(n1), u, v;
   auto get_row = [&](int r) { std::vector<cd> o(n2); for (int k = 0; k < n2; ++k) o[k] = entry(rows[r], cols[k], hc); return o; };
-  auto get_col = [&](int c) { std::vector<cd> o(n1); for (int k = 0; k < n1; ++k) o[k] = entry(rows[k], cols[c], hc); return o; };
+  // Columns in one source leaf share the far-field records of every row:
+  // keep them per leaf, indexed by row position.
+  std::vector<std::pair<int, std::vector<const cd*>>> col_leaf;
+  auto get_col = [&](int c) {
+    std::vector<cd> o(n1);
+    const int j = cols[c], leaf = j / rank, node = j % rank;
+    std::vector<const cd*>* P = nullptr;
+    for (auto& e : col_leaf)
+      if (e.first == leaf) P = &e.second;
+    if (!P) {
+      col_leaf.emplace_back(leaf, std::vector<const cd*>(n1, nullptr));
+      P = &col_leaf.back().second;
+    }
+    for (int k = 0; k < n1; ++k) {
+      const cd*& h = (*P)[k];
+      if (!h) h = hc.get(rows[k], leaf);
+      o[k] = scale(rows[k], j, h[node]);
+    }
+    return o;
+  };
   int rk = 0, ri = 0, ci = 0;
   const double thr = eps * std::pow(10, -1.0 * 0);
   if (n1 < n2) {
@@ -736,14 +773,12 @@ int Builder::aca(const std::vector<int>& rows, const std::vector<int>& cols, dou
       rb.push_back(ri);
       row = get_row(ri);
       const std::vector<cd> raw = row;
-      for (int a = 0; a < rk; ++a)
-        for (size_t s = 0; s < V[a].size(); ++s) row[s] -= U[a][ri] * V[a][s];
+      for (int a = 0; a < rk; ++a) sub_scaled(row, U[a][ri], V[a]);
       ci = argmax_remaining(row, cused);
       cb.push_back(ci);
       for (size_t s = 0; s < row.size(); ++s) v[s] = row[s] / row[ci];
       col = get_col(ci);
-      for (int a = 0; a < rk; ++a)
-        for (size_t s = 0; s < U[a].size(); ++s) col[s] -= V[a][ci] * U[a][s];
+      for (int a = 0; a < rk; ++a) sub_scaled(col, V[a][ci], U[a]);
       u = col;
       if (norm2(u) < 1e-8 || norm2(v) < 1e-8) { rb.pop_back(); cb.pop_back(); break; }
       U.push_back(u); V.push_back(v); piv_rows.push_back(raw);
@@ -778,15 +813,13 @@ int Builder::aca(const std::vector<int>& rows, const std::vector<int>& cols, dou
     while (std::abs(row[ci]) > thr && std::abs(col[ri]) > eps && std::abs(prev - nS) >= eps * prev && rk < mn) {
       cb.push_back(ci);
       col = get_col(ci);
-      for (int a = 0; a < rk; ++a)
-        for (size_t s = 0; s < V[a].size(); ++s) col[s] -= U[a][ci] * V[a][s];
+      for (int a = 0; a < rk; ++a) sub_scaled(col, U[a][ci], V[a]);
       ri = argmax_remaining(col, rused);
       rb.push_back(ri);
       for (size_t s = 0; s < col.size(); ++s) v[s] = col[s] / col[ri];
       row = get_row(ri);
       const std::vector<cd> raw = row;
-      for (int a = 0; a < rk; ++a)
-        for (size_t s = 0; s < U[a].size(); ++s) row[s] -= V[a][ri] * U[a][s];
+      for (int a = 0; a < rk; ++a) sub_scaled(row, V[a][ri], U[a]);
       u = row;
       if (norm2(u) < 1e-8 || norm2(v) < 1e-8) { cb.pop_back(); rb.pop_back(); break; }
       U.push_back(u); V.push_back(v); piv_rows.push_back(raw);
