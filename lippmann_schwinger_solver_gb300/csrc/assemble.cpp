@@ -679,11 +679,29 @@ class Builder {
 // reference dereferences begin() of an empty std::set, which reads the
 // set's element count (0) with libstdc++: index 0, after which the ACA loop
 // ends on rank == min(rows, cols).
+//
+// |v| is std::abs (hypot), which is costly, so a first pass finds the
+// largest re^2 + im^2 = Q. Both forms are within a few ulps of the true
+// magnitude: every index whose |v| equals the largest one has
+// re^2 + im^2 >= Q (1 - 1e-12), and every other index has a strictly
+// smaller |v|. The rule above, run on those candidates alone, therefore
+// picks the same index as a scan of all of them.
 static int argmax_remaining(const std::vector<cd>& v, const std::vector<char>& used) {
+  const int n = (int)v.size();
+  double Q = -1.0;
+  for (int i = 0; i < n; ++i) {
+    if (used[i]) continue;
+    const double q = v[i].real() * v[i].real() + v[i].imag() * v[i].imag();
+    if (q > Q) Q = q;
+  }
+  if (Q < 0.0) return 0;  // every index used
+  const double cut = Q * (1.0 - 1e-12);
   int idx = -1;
   double mx = 0.0;
-  for (int i = 0; i < (int)v.size(); ++i) {
+  for (int i = 0; i < n; ++i) {
     if (used[i]) continue;
+    const double q = v[i].real() * v[i].real() + v[i].imag() * v[i].imag();
+    if (!(q >= cut)) continue;
     if (idx < 0) { idx = i; mx = std::abs(v[i]); continue; }
     if (std::abs(v[i]) > mx) { idx = i; mx = std::abs(v[idx]); }
   }
