@@ -1208,45 +1208,28 @@ void Builder::user_checks() {
 }
 
 // Appends a row-major block (rows x K) with its gather list to a phase.
-// Appends blocks to a phase's staging arrays, in the order t = 0..n-1:
-// get(t) gives block t (rows x K, row major; nidx >= K gather indices; its
-// first row writes output element `out`), rows or K = 0 skips it. Offsets
-// come from a prefix sum, so the copies run in parallel; done(t) runs after
-// block t is copied (to free it).
+// Hands blocks to a phase for packing, in the order t = 0..n-1: get(t)
+// gives block t (A: rows x K, row major; idx: at least K gather indices;
+// its first row writes output element `out`); rows or K = 0 skips it. The
+// phase takes the two vectors over (a move, no copy) and records one row
+// per block row.
 struct BlockView {
-  const cd* A;
+  std::vector<cd>* A;
   int rows, K;
-  const int* idx;
-  int nidx;
+  std::vector<int>* idx;
   int out;
 };
-template <class Get, class Done>
-static void stage_blocks(GemvPhase& ph, int n, Get get, Done done) {
-  std::vector<long long> ao((size_t)n + 1), io((size_t)n + 1), ro((size_t)n + 1);
-  ao[0] = (long long)ph.stageA.size();
-  io[0] = (long long)ph.stageIdx.size();
-  ro[0] = (long long)ph.rows.size();
+template <class Get>
+static void stage_blocks(GemvPhase& ph, int n, Get get) {
   for (int t = 0; t < n; ++t) {
     const BlockView v = get(t);
-    const bool use = v.rows > 0 && v.K > 0;
-    ao[t + 1] = ao[t] + (use ? (long long)v.rows * v.K : 0);
-    io[t + 1] = io[t] + (use ? v.nidx : 0);
-    ro[t + 1] = ro[t] + (use ? v.rows : 0);
-  }
-  ph.nnz += ao[n] - ao[0];
-  ph.stageA.resize((size_t)ao[n]);
-  ph.stageIdx.resize((size_t)io[n]);
-  ph.rows.resize((size_t)ro[n]);
-#pragma omp parallel for schedule(dynamic, 8)
-  for (int t = 0; t < n; ++t) {
-    const BlockView v = get(t);
-    if (v.rows > 0 && v.K > 0) {
-      std::copy(v.A, v.A + (size_t)v.rows * v.K, ph.stageA.begin() + ao[t]);
-      std::copy(v.idx, v.idx + v.nidx, ph.stageIdx.begin() + io[t]);
-      for (int r = 0; r < v.rows; ++r)
-        ph.rows[(size_t)(ro[t] + r)] = {ao[t] + (long long)r * v.K, v.K, (int)io[t], v.out + r};
-    }
-    done(t);
+    if (v.rows <= 0 || v.K <= 0) continue;
+    ph.stageA.push_back(std::move(*v.A));
+    ph.stageIdx.push_back(std::move(*v.idx));
+    const cd* a = ph.stageA.back().data();
+    const int* ix = ph.stageIdx.back().data();
+    for (int r = 0; r < v.rows; ++r) ph.rows.push_back({a + (size_t)r * v.K, v.K, ix, v.out + r});
+    ph.nnz += (long long)v.rows * v.K;
   }
 }
 
@@ -1343,7 +1326,7 @@ static void finalize(GemvPhase& ph, const char* kind) {
     for (int q = 0; q < d.qmax; ++q)
       for (int sl = 0; sl < d.S; ++sl) {
         const int k = q * d.S + sl;
-        if (k < d.K) ph.idx[(size_t)(d.ioff + (long long)q * d.S + sl)] = ph.stageIdx[(size_t)first.idx + k];
+        if (k < d.K) ph.idx[(size_t)(d.ioff + (long long)q * d.S + sl)] = first.idx[k];
       }
     for (int r = 0; r < d.rows; ++r) {
       const GemvPhase::Row& row = ph.rows[d.r0 + r];
@@ -1352,14 +1335,14 @@ static void finalize(GemvPhase& ph, const char* kind) {
         const int lane = sl * R + r;
         int q = 0;
         for (int k = sl; k < row.K; k += d.S, ++q)
-          ph.A[(size_t)(d.off + (long long)q * kTileLanes + lane)] = ph.stageA[(size_t)(row.a + k)];
+          ph.A[(size_t)(d.off + (long long)q * kTileLanes + lane)] = row.a[k];
         ph.klen[t * kTileLanes + lane] = q;
       }
     }
     ph.tiles[t] = {d.off, d.ioff, d.qmax, d.rows, log2s, (int)(t * kTileLanes), d.row_base};
   }
-  std::vector<cd>().swap(ph.stageA);
-  std::vector<int>().swap(ph.stageIdx);
+  std::vector<std::vector<cd>>().swap(ph.stageA);
+  std::vector<std::vector<int>>().swap(ph.stageIdx);
   std::vector<GemvPhase::Row>().swap(ph.rows);
 }
 
@@ -1458,14 +1441,11 @@ void Builder::pack(HostOperator& op) {
       T[t] = std::move(Tm);
       src[t] = std::move(s);
     }
-    stage_blocks(
-        ph, nn,
-        [&](int t) {
-          if (T[t].empty()) return BlockView{nullptr, 0, 0, nullptr, 0, 0};
-          return BlockView{T[t].data(), (int)nodes[j][t].out_charge.size(), (int)src[t].size(), src[t].data(),
-                           (int)src[t].size(), (int)nodes[j][t].own_charge};
-        },
-        [&](int t) { std::vector<cd>().swap(T[t]); });
+    stage_blocks(ph, nn, [&](int t) {
+      if (T[t].empty()) return BlockView{nullptr, 0, 0, nullptr, 0};
+      return BlockView{&T[t], (int)nodes[j][t].out_charge.size(), (int)src[t].size(), &src[t],
+                       (int)nodes[j][t].own_charge};
+    });
     finalize(ph, "UP");
     op.up.push_back(std::move(ph));
   }
@@ -1509,14 +1489,11 @@ void Builder::pack(HostOperator& op) {
     op.m2l_rows = 0;
     for (auto& tk : tasks)
       if (tk.K != 0) op.m2l_rows += tk.rows;
-    stage_blocks(
-        ph, (int)tasks.size(),
-        [&](int u) {
-          const Task& tk = tasks[u];
-          if (tk.K == 0) return BlockView{nullptr, 0, 0, nullptr, 0, 0};
-          return BlockView{tk.A.data(), tk.rows, tk.K, tk.idx.data(), (int)tk.idx.size(), (int)tk.out};
-        },
-        [&](int u) { std::vector<cd>().swap(tasks[u].A); });
+    stage_blocks(ph, (int)tasks.size(), [&](int u) {
+      Task& tk = tasks[u];
+      if (tk.K == 0) return BlockView{nullptr, 0, 0, nullptr, 0};
+      return BlockView{&tk.A, tk.rows, tk.K, &tk.idx, (int)tk.out};
+    });
     finalize(ph, "M2L");
     op.m2l = std::move(ph);
   }
@@ -1606,14 +1583,11 @@ void Builder::pack(HostOperator& op) {
     }
     GemvPhase ph;
     ph.accumulate = 1;
-    stage_blocks(
-        ph, nch,
-        [&](int t) {
-          const Task& tk = tasks[t];
-          if (!tk.any) return BlockView{nullptr, 0, 0, nullptr, 0, 0};
-          return BlockView{tk.A.data(), tk.rows, tk.K, tk.idx.data(), (int)tk.idx.size(), (int)tk.out};
-        },
-        [&](int t) { std::vector<cd>().swap(tasks[t].A); });
+    stage_blocks(ph, nch, [&](int t) {
+      Task& tk = tasks[t];
+      if (!tk.any) return BlockView{nullptr, 0, 0, nullptr, 0};
+      return BlockView{&tk.A, tk.rows, tk.K, &tk.idx, (int)tk.out};
+    });
     finalize(ph, "DOWN");
     op.down.push_back(std::move(ph));
   }

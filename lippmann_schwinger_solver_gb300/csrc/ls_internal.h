@@ -43,10 +43,12 @@ struct GemvPhase {
   std::vector<GemvTile> tiles;
   int accumulate = 0;           // 0: overwrite, 1: accumulate into dst
   long long nnz = 0;            // true (unpadded) block entries
-  // Staging before packing: blocks row major, one record per row.
-  struct Row { long long a; int K; int idx; int out; };
-  std::vector<cd> stageA;
-  std::vector<int> stageIdx;
+  // Staging before packing: the phase owns its blocks (row major) and their
+  // gather lists until they are packed; one record per block row points
+  // into them.
+  struct Row { const cd* a; int K; const int* idx; int out; };
+  std::vector<std::vector<cd>> stageA;
+  std::vector<std::vector<int>> stageIdx;
   std::vector<Row> rows;
   long long entries() const { return nnz; }
 };
