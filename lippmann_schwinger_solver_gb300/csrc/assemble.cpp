@@ -400,7 +400,7 @@ class HankelTable {
     h *= 0xBF58476D1CE4E5B9ULL;
     return h ^ (h >> 29);
   }
-  // Stored vector for `k`, or nullptr.
+  // Stored record for `k`, or nullptr.
   const cd* find(const Key& k) {
     const uint64_t h = hash(k);
     Shard& sh = shards_[h >> (64 - kShardBits)];
@@ -441,6 +441,7 @@ class HankelTable {
       std::vector<Key>().swap(sh.keys);
       std::vector<const cd*>().swap(sh.vals);
       std::vector<std::unique_ptr<cd[]>>().swap(sh.chunks);
+      sh.chunk_cap = 0;
       sh.chunk_left = 0;
       sh.used = 0;
       sh.mask = 0;
@@ -462,20 +463,22 @@ class HankelTable {
     const long long c = v ? std::strtoll(v, &end, 10) : -1;
     return (v && end != v && *end == '\0' && c >= 0) ? (size_t)c : (size_t(1) << 22);
   }
-  // Open addressing with linear probing; records live in chunks of 4096, so
-  // a rehash moves keys and pointers but never a record.
+  // Open addressing with linear probing; records live in chunks (64 records
+  // at first, doubling up to 4096, so small tables stay small), and a rehash
+  // moves keys and pointers but never a record.
   struct Shard {
     std::mutex mu;
     std::vector<Key> keys;
     std::vector<const cd*> vals;
     std::vector<std::unique_ptr<cd[]>> chunks;
-    size_t chunk_left = 0, used = 0, mask = 0;
+    size_t chunk_cap = 0, chunk_left = 0, used = 0, mask = 0;
     cd* alloc(size_t w) {
       if (chunk_left == 0) {
-        chunks.emplace_back(new cd[4096 * w]);
-        chunk_left = 4096;
+        chunk_cap = chunk_cap == 0 ? 64 : std::min<size_t>(2 * chunk_cap, 4096);
+        chunks.emplace_back(new cd[chunk_cap * w]);
+        chunk_left = chunk_cap;
       }
-      return chunks.back().get() + (4096 - chunk_left--) * w;
+      return chunks.back().get() + (chunk_cap - chunk_left--) * w;
     }
     void rehash(size_t cap) {
       std::vector<Key> nk(cap, Key{kEmpty, kEmpty});
