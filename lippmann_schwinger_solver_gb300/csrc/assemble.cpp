@@ -47,6 +47,7 @@ const cd kI(0.0, 1.0);
 constexpr int kSeries = 15;                 // FarFieldInteraction.hpp:55
 constexpr double kQuadEps = 1e-7;           // FarFieldInteraction.hpp:37, NearFieldInteraction1.hpp:199
 constexpr int kQuadOrder = 10;              // 10x10 Gauss-Legendre per panel
+constexpr int kMaxChebOrder = 15;           // basis orders: degreeOfBases <= 10 (checked with nChebNodes <= 8)
 
 // ---------------------------------------------------------------- special functions
 // J_n(x), Y_n(x) for n = 0 .. nmax (nmax < 64) for the far-field Hankel
@@ -973,13 +974,21 @@ void Builder::precompute() {
   static const double ncy[9] = {-2, -2, -2, 0, 2, 2, 2, 0, 0};
   const double rA = radius[nL], rB = radius[nL];
   std::vector<cd> V((size_t)9 * rank * nb);
+  int max_order = 0;
+  for (const auto& ab : bases) max_order = std::max(max_order, std::max(ab.first, ab.second));
 #pragma omp parallel for schedule(dynamic, 1)
   for (int t = 0; t < 9 * rank; ++t) {
     const int q = t / rank, i = t % rank;
     const double bx = ncx[q] * rA, by = ncy[q] * rA;
     const double ax = rA * cheb1[i % n1] + 0.0, ay = rA * cheb1[i / n1] + 0.0;
     const double Xx = (ax - bx) / rB, Xy = (ay - by) / rB;
-    std::unordered_map<unsigned long long, cd> memo;
+    // Per quadrature point: H0 and the Chebyshev values of every order the
+    // bases use, computed once and shared by all bases of this target.
+    struct PointVals {
+      cd H;
+      double tx[kMaxChebOrder + 1], ty[kMaxChebOrder + 1];
+    };
+    std::unordered_map<unsigned long long, PointVals> memo;
     auto key = [](double a, double b) {
       unsigned long long ka, kb;
       std::memcpy(&ka, &a, 8);
@@ -991,17 +1000,20 @@ void Builder::precompute() {
       auto f = [&](double x, double y) -> cd {
         const unsigned long long kk = key(x, y);
         auto it = memo.find(kk);
-        cd H;
-        if (it != memo.end()) {
-          H = it->second;
-        } else {
+        if (it == memo.end()) {
+          PointVals pv;
           const double R2 = (Xx - x) * (Xx - x) + (Xy - y) * (Xy - y);
           const double R = std::sqrt(R2);
           const double arg = kappa * rB * R;
-          H = bes_j(0, arg) + kI * bes_y(0, arg);
-          memo.emplace(kk, H);
+          pv.H = bes_j(0, arg) + kI * bes_y(0, arg);
+          for (int o = 0; o <= max_order; ++o) {
+            pv.tx[o] = cheb_t(x, o);
+            pv.ty[o] = cheb_t(y, o);
+          }
+          it = memo.emplace(kk, pv).first;
         }
-        return H * cheb_t(x, a) * cheb_t(y, b);
+        const PointVals& pv = it->second;
+        return pv.H * pv.tx[a] * pv.ty[b];
       };
       V[((size_t)q * rank + i) * nb + l] = quad2d(f, gln, glw);
     }
