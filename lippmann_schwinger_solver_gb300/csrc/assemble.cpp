@@ -502,6 +502,24 @@ class HankelTable {
   size_t width_ = 0;
 };
 
+// Recently used table records of one thread, direct-mapped and lock-free,
+// in front of the shared table: neighbouring boxes see the same relative
+// positions (translation invariance), so a thread meets the same keys task
+// after task. Entries carry the id of the assembly that stored them; a
+// record pointer is only returned to that assembly, whose table is alive.
+struct ThreadRecent {
+  static constexpr int kBits = 15;
+  struct Slot {
+    HankelTable::Key k;
+    const cd* v;
+    uint64_t owner;
+  };
+  std::vector<Slot> slots = std::vector<Slot>(size_t(1) << kBits, Slot{{0, 0}, nullptr, 0});
+  Slot& at(const HankelTable::Key& k) { return slots[HankelTable::hash(k) & ((size_t(1) << kBits) - 1)]; }
+};
+thread_local ThreadRecent t_recent;
+std::atomic<uint64_t> g_assembly_id{0};
+
 // ---------------------------------------------------------------- the builder
 struct Node {
   bool out_active = false, in_active = false;
@@ -541,6 +559,7 @@ class Builder {
   std::vector<std::vector<std::vector<int>>> nbrs;  // [level][box] same-level neighbours
   std::vector<std::vector<Node>> nodes;             // [level][node]
   mutable HankelTable htab;                         // shared by NCA and block fills
+  const uint64_t id = ++g_assembly_id;              // tags thread-local table entries
 
   bool is_lfr(int j) const { return j >= level_LFR; }
   int nodes_at(int j) const { return is_lfr(j) ? (1 << (2 * j)) : (1 << (2 * j)) * nCones[j]; }
@@ -628,16 +647,20 @@ class Builder {
         if (keys[p] == key) return last = vals[p];
       const double rx = b->gx_[i] - b->cx[b->nL][leaf], ry = b->gy_[i] - b->cy[b->nL][leaf];
       const HankelTable::Key k = HankelTable::key(rx, ry);
-      const cd* h = b->htab.find(k);
+      ThreadRecent::Slot& rs = t_recent.at(k);
+      const cd* h = (rs.owner == b->id && rs.k == k) ? rs.v : b->htab.find(k);
+      bool shared = h != nullptr;  // a table record, alive until the assembly ends
       if (!h) {
         std::vector<cd> v((size_t)b->rank);
         b->key_sums(rx, ry, v.data());
         h = b->htab.insert(k, v.data());
+        shared = h != nullptr;
         if (!h) {
           own.push_back(std::move(v));
           h = own.back().data();
         }
       }
+      if (shared) rs = {k, h, b->id};
       keys[p] = key;
       vals[p] = h;
       ++used;
