@@ -321,7 +321,7 @@ def run_ours(args):
                  "f32_matvec_per_s": 1e3 / ms32, "f32_m2l_ms": m2l32}
         # The learned preconditioner: mixed-precision flexible GMRES with the
         # trained spectral neural operator as initial guess and right
-        # preconditioner (the BASELINE metric's NN-FGMRES leg).
+        # preconditioner (the NN-FGMRES leg of the solve-time metric).
         if not args.no_nn and os.path.exists(FNO_WEIGHTS):
             net = ls.FNO.load(FNO_WEIGHTS, device=local)
             nn = {"weights": os.path.relpath(FNO_WEIGHTS, ROOT), "params": net.n_params}

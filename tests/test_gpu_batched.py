@@ -1,6 +1,6 @@
 """Many right-hand sides on one operator (ls_gmres_mixed_batched).
 
-Each column is judged by its own FP64 true residual, like ls_gmres_mixed;
+Each column stops on its own FP64 true residual, like ls_gmres_mixed;
 the batched solution must agree with the single-vector FP64 GMRES solution
 to the accuracy both solves carry (residual 1e-8, relative solution
 difference bound 1e-5 written below).
