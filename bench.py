@@ -138,30 +138,82 @@ def replica_throughput(world, ms_per_step):
     return world * 1e3 / ms_per_step
 
 
-def cpu_baseline(ls, cfg, budget_s=25.0, threads=None):
-    """Times the oracle's matvec (CPU restatement of the reference phases)
-    on the same operator: as many matvecs as fit in budget_s, at least one."""
+def cpu_model():
+    """The host CPU's model name (lscpu), or the machine type."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+
+    return platform.machine()
+
+
+def _timed_matvecs(o, x, budget_s, cap):
+    """matvec/s of the oracle: as many matvecs as fit in budget_s (>= 1)."""
+    n, t = 0, 0.0
+    while n < 1 or (t < budget_s and n < cap):
+        t1 = time.perf_counter()
+        o.matvec(x)
+        t += time.perf_counter() - t1
+        n += 1
+    return n / t, n
+
+
+def c1_config(ls):
+    """The reference's CPU-runnable configuration: uniform level 4 (N=9,216),
+    kappa 10, Gaussian contrast 1.5 exp(-160|x|^2), NCA tolerance 1e-8."""
+    return ls.Config(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, TOL_POW=8, degreeOfBases=6, nLevelsUniform=4,
+                     Qchoice=0, findPhi=1, reference_rounding=1, L=1.0, kappa=10.0)
+
+
+def oracle_leg(ls, cfg, y_gpu, skel_gpu, budget_s=20.0):
+    """The CPU restatement of the reference (oracle/) on the machine's host cores:
+    its matvec/s with all threads and with one, its GMRES solve time to a
+    relative residual of 1e-8 at this workload and at the 9,216-point C1
+    configuration, and the GPU product's parity with it on the same input
+    (relative L2 distance and skeleton equality)."""
     from oracle import oracle as ora
 
     ora.build()
-    ncores = threads or os.cpu_count() or 1
+    ncores = os.cpu_count() or 1
     ora.set_threads(ncores)
     t0 = time.time()
     o = ora.Oracle(cfg.as_dict())
     t_asm = time.time() - t0
     x = input_vector(o.N)
-    o.matvec(x)  # warm-up
-    n, t = 0, 0.0
-    while n < 1 or t < budget_s:
-        t1 = time.perf_counter()
-        o.matvec(x)
-        t += time.perf_counter() - t1
-        n += 1
-        if n >= 200:
-            break
+    yo = o.matvec(x)  # also the warm-up
+    parity = {"rel_l2_vs_oracle": float(np.linalg.norm(y_gpu - yo) / np.linalg.norm(yo)),
+              "skeletons_equal": bool(np.array_equal(skel_gpu, o.skeleton_dump())),
+              "tolerance": 1e-10, "input": "seeded x (re, im ~ U[-1,1], seed %d)" % (SEED + 1)}
+    v_all, n_all = _timed_matvecs(o, x, budget_s, 200)
+    ora.set_threads(1)
+    v_one, n_one = _timed_matvecs(o, x, min(6.0, budget_s), 50)
+    ora.set_threads(ncores)
+    b = o.rhs()
+    t1 = time.perf_counter()
+    xs, hist, it = o.gmres(b, max_iter=400, tol=1e-8)
+    t_solve = time.perf_counter() - t1
+    rr = float(np.linalg.norm(b - o.matvec(xs)) / np.linalg.norm(b))
     o.close()
-    return {"value": n / t, "unit": "matvec/s", "cores": ncores, "kind": "port",
-            "sample": f"{n} oracle matvecs of the full workload operator (assembly {t_asm:.0f} s not timed)"}
+    o1 = ora.Oracle(c1_config(ls).as_dict())
+    b1 = o1.rhs()
+    t1 = time.perf_counter()
+    x1, _, it1 = o1.gmres(b1, max_iter=400, tol=1e-8)
+    t_solve1 = time.perf_counter() - t1
+    rr1 = float(np.linalg.norm(b1 - o1.matvec(x1)) / np.linalg.norm(b1))
+    o1.close()
+    cpu = {"value": v_all, "unit": "matvec/s", "cores": ncores, "kind": "port", "cpu_model": cpu_model(),
+           "sample": f"{n_all} oracle matvecs of the full workload operator with {ncores} threads, {n_one} with 1 "
+                     f"(assembly {t_asm:.0f} s not timed)",
+           "one_thread": {"value": v_one, "unit": "matvec/s", "cores": 1},
+           "solve_s": {"workload": t_solve, "workload_iters": it, "workload_true_residual": rr,
+                       "c1": t_solve1, "c1_iters": it1, "c1_true_residual": rr1, "tol": 1e-8,
+                       "method": "oracle GMRES (x0 = 0, Givens residual estimate), all threads"}}
+    return cpu, parity
 
 
 def run_reference(args):
@@ -179,7 +231,8 @@ def run_reference(args):
     ora.set_threads(ncores)
     o = ora.Oracle(cfg.as_dict())
     x = input_vector(o.N)
-    for _ in range(max(1, min(args.warmup, 2))):
+    warmup = max(1, args.warmup)
+    for _ in range(warmup):
         o.matvec(x)
     steps = max(1, args.steps)
     t0 = time.perf_counter()
@@ -188,13 +241,13 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     v = steps / dt
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+            "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
             "config": {"workload": "uniform level %d, N=%d, kappa=40, 3 seeded bumps (seed %d), NCA tol 1e-10"
                                    % (args.level, o.N, SEED), "parallelism": "CPU threads"},
-            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": ncores, "kind": "port",
-                             "sample": f"{steps} matvecs of the full workload operator; reference build "
-                                       "unavailable (Eigen/Boost headers missing)"},
+            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": ncores, "kind": "port", "cpu_model": cpu_model(),
+                             "sample": f"{steps} matvecs of the full workload operator after {warmup} warm-ups; "
+                                       "reference build unavailable (Eigen/Boost headers missing)"},
             "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -310,15 +363,27 @@ def run_ours(args):
             t0 = time.perf_counter()
             r = fn()
             return time.perf_counter() - t0, r
-        t64, (_, hist64, it64, rr64, code64) = timed(lambda: op.gmres(b, max_iter=args.max_iter, tol=1e-8))
+        t64, (x64, hist64, it64, rr64, code64) = timed(lambda: op.gmres(b, max_iter=args.max_iter, tol=1e-8))
         op.enable_f32()
         ms32, m2l32 = op.time_matvec(warmup=3, iters=max(5, args.steps), precision=ls.LS_PREC_F32)
-        tm, (_, histm, nmv, rrm, codem) = timed(
+        tm, (xm, histm, nmv, rrm, codem) = timed(
             lambda: op.gmres_mixed(b, max_outer=20, inner_iter=args.max_iter, tol=1e-8))
+
+        def err_vs_fp64(xv):
+            return float(np.linalg.norm(xv - x64) / np.linalg.norm(x64))
         solve = {"tol": 1e-8, "fp64_gmres_s": t64, "fp64_iters": it64, "fp64_true_residual": rr64,
-                 "fp64_converged": code64 == 0, "mixed_s": tm, "mixed_matvecs": nmv, "mixed_true_residual": rrm,
+                 "fp64_converged": code64 == 0, "fp64_history": [float(v) for v in hist64],
+                 "mixed_s": tm, "mixed_matvecs": nmv, "mixed_true_residual": rrm,
                  "mixed_converged": codem == 0, "speedup_mixed_vs_fp64": t64 / tm if tm > 0 else None,
+                 "mixed_rel_err_vs_fp64": err_vs_fp64(xm), "mixed_history": [float(v) for v in histm],
                  "f32_matvec_per_s": 1e3 / ms32, "f32_m2l_ms": m2l32}
+        # The same solves at the 9,216-point C1 configuration (GPU side of the
+        # CPU solve times in cpu_baseline.solve_s).
+        op1 = ls.Operator(c1_config(ls), device=local)
+        b1 = op1.rhs()
+        t64_1, (_, _, it64_1, rr64_1, _) = timed(lambda: op1.gmres(b1, max_iter=args.max_iter, tol=1e-8))
+        solve["c1"] = {"fp64_gmres_s": t64_1, "fp64_iters": it64_1, "fp64_true_residual": rr64_1, "N": op1.N}
+        op1.close()
         # The learned preconditioner: mixed-precision flexible GMRES with the
         # trained spectral neural operator as initial guess and right
         # preconditioner (the NN-FGMRES leg of the solve-time metric).
@@ -327,9 +392,10 @@ def run_ours(args):
             nn = {"weights": os.path.relpath(FNO_WEIGHTS, ROOT), "params": net.n_params}
             for name, flags in (("nn", ls.LS_NN_GUESS | ls.LS_NN_PRECOND), ("nn_guess_only", ls.LS_NN_GUESS),
                                 ("nn_precond_only", ls.LS_NN_PRECOND)):
-                tn, (_, hn, rep, coden) = timed(
+                tn, (xn, hn, rep, coden) = timed(
                     lambda: op.fgmres_nn(net, b, flags=flags, max_outer=20, inner_iter=args.max_iter, tol=1e-8))
                 nn[name] = {"s": tn, "converged": coden == 0, "true_residual": rep["rel_residual"],
+                            "rel_err_vs_fp64": err_vs_fp64(xn),
                             "fp32_applies_and_fp64_products": rep["n_matvec"], "network_applies": rep["n_precond"],
                             "guess_residual": rep["guess_residual"], "fell_back": bool(rep["fell_back"]),
                             "history": [float(v) for v in hn]}
@@ -363,9 +429,22 @@ def run_ours(args):
     peak, peak_kind = load_peaks()
     achieved = info["m2l_bytes"] / (ms_m2l * 1e-3) / 1e9
     traffic = traffic_per_launch(args.f64_kernels)
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(ls, cfg, budget_s=args.cpu_budget)
+        cpu, parity = oracle_leg(ls, cfg, y_main, op.skeleton_dump(), budget_s=args.cpu_budget)
+        if not (parity["rel_l2_vs_oracle"] <= parity["tolerance"] and parity["skeletons_equal"]):
+            raise SystemExit("bench: GPU matvec differs from the oracle at the benchmark size: " + json.dumps(parity))
+    # Measured FP64 FMA peak: the roof of the native FP64 kernels.
+    fp64_peak = ls.measure_fma_peak(local, "fp64")
+    fp32_peak = ls.measure_fma_peak(local, "fp32")
+    phases = op.time_matvec_phases(warmup=3, iters=max(5, args.steps))
+    d_bases = cfg.degreeOfBases
+    n_bases = (d_bases + 1) * (d_bases + 2) // 2
+    side = int(round(info["n_leaves"] ** 0.5))
+    pairs = (3 * side - 2) ** 2  # (leaf, colleague) pairs of a uniform side x side leaf grid
+    # FP64 flops of the factored native near field: c = Q+ x per leaf (real x
+    # complex) and Vt_q c per (leaf, colleague) and row (complex).
+    near_f64_flops = 4 * info["n_leaves"] * n_bases * info["rank"] + 8 * pairs * info["rank"] * n_bases
     line = {
         "metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -382,7 +461,19 @@ def run_ours(args):
         "gpu_launches": info["n_kernels_per_matvec"] * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_kind, "kernel": ("gemv_df_kernel<1> (M2L)" if df_kernels else "gemv_tiles_kernel<double2, 1> (M2L)"),
-                     "kernel_ms": ms_m2l, "kernel_gflops_fp64": info["m2l_flops"] / (ms_m2l * 1e-3) / 1e9},
+                     "kernel_ms": ms_m2l, "kernel_gflops_fp64": info["m2l_flops"] / (ms_m2l * 1e-3) / 1e9,
+                     "fp64_pipe": {"peak_tflops": fp64_peak, "peak_source": "measured (ls_measure_fma_peak, DFMA chains)",
+                                   "fp32_peak_tflops": fp32_peak,
+                                   "m2l_tflops": info["m2l_flops"] / (ms_m2l * 1e-3) / 1e12,
+                                   "m2l_frac": info["m2l_flops"] / (ms_m2l * 1e-3) / 1e12 / fp64_peak,
+                                   "near_field_ms": phases["near"], "near_field_fp64_flops": near_f64_flops,
+                                   "near_field_frac": (near_f64_flops / (phases["near"] * 1e-3) / 1e12 / fp64_peak
+                                                       if not df_kernels else None),
+                                   "matvec_fp64_flops": 8 * info["far_entries"] + near_f64_flops,
+                                   "matvec_frac": ((8 * info["far_entries"] + near_f64_flops) / (ms * 1e-3) / 1e12
+                                                   / fp64_peak if not df_kernels else None)}},
+        "phases_ms": phases,
+        "parity": parity,
         "matvec": {"bytes": info["matvec_bytes"], "flops_fp64": info["matvec_flops"],
                    "achieved_gbs": info["matvec_bytes"] / (ms * 1e-3) / 1e9,
                    "achieved_fp64_tflops": info["matvec_flops"] / (ms * 1e-3) / 1e12,

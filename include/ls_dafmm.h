@@ -143,10 +143,13 @@ ls_status ls_op_set_f64_kernels(ls_op* op, int kernels);
  * doubles (16 MiB) that every GPU loading the library reserves until exit;
  * nothing is allocated or freed per call. x, y and the operator stay
  * caller-provided as in ls_matvec. Operators that need more scratch are
- * rejected with LS_E_INVALID. The first call on a device looks up the
- * array's device address (make it before any stream capture). All calls
- * share the array: calls that overlap on the GPU race and must be
- * serialised by the caller.
+ * rejected with LS_E_INVALID (checked before anything else, so a host-only
+ * operator gets the same answer). It always runs the native FP64 kernels,
+ * with the unfactored near-field blocks, whatever ls_op_set_f64_kernels
+ * selected. The first call on a device looks up the array's device address
+ * in the current CUDA context (make it before any stream capture); a call
+ * after cudaDeviceReset looks it up again. All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
  */
 #define LS_STATIC_SCRATCH_ELEMS (1LL << 20)
 ls_status ls_matvec_noalloc(ls_op* op, const double* x, double* y, void* stream);
@@ -194,6 +197,23 @@ ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_o
 ls_status ls_time_matvec(ls_op* op, int precision, int warmup, int iters, float* ms_matvec,
                          float* ms_m2l);
 
+/* Same timing split by phase, each the mean over `iters` matvecs, in ms:
+ * ms[0] whole matvec, ms[1] load of x and the upward (M2M) phases, ms[2] M2L,
+ * ms[3] downward (L2L) phases, ms[4] near field and output. The events
+ * between the phases stop consecutive kernels from overlapping, so ms[1..4]
+ * add up to slightly more than an unmarked matvec. No counterpart in the
+ * reference. */
+ls_status ls_time_matvec_phases(ls_op* op, int precision, int warmup, int iters, float* ms);
+
+/*
+ * Measured arithmetic peak of `device`: a kernel of independent fused
+ * multiply-add chains (2 flops each) over every SM, best of a few timed
+ * launches with CUDA events. kind 0: FP64 (DFMA), 1: FP32 (FFMA). Writes
+ * TFLOP/s. The denominator of the FP64-pipe roofline of the native kernels.
+ * No counterpart in the reference.
+ */
+ls_status ls_measure_fma_peak(int device, int kind, double* tflops);
+
 /*
  * Density at arbitrary points by the reference's Chebyshev-Q+ interpolation
  * (GMRES_Hybrid/LippmannSchwinger/main/hybridTrueValidation_gmres.cpp:
@@ -218,6 +238,17 @@ long ls_op_skeleton_dump(const ls_op* op, int* buf, long cap);
 /* Leaf-level far-field moments M (rank x 31, complex) and colleague near
  * blocks (9 x rank x rank, complex, row major) as used by the matvec. */
 ls_status ls_op_precomputations(const ls_op* op, double* M, double* near);
+
+/*
+ * Launch mode of the matvec and Krylov kernel chains. No counterpart in the
+ * reference (a CPU code). 1 (the default): programmatic dependent launch,
+ * each kernel scheduled while its predecessor runs and waiting in hardware
+ * for its results; 0: plain stream-ordered launches. Results are bitwise
+ * identical in both modes. LS_PDL=0 in the environment selects 0 at load.
+ * Process-wide; applies to launches queued after the call.
+ */
+ls_status ls_set_pdl(int on);
+int ls_get_pdl(void);
 
 const char* ls_last_error(void);
 const char* ls_version(void);

@@ -44,7 +44,7 @@ EXPORTED_SYMBOLS = (
     "ls_matvec", "ls_matvec_f32", "ls_op_enable_f32", "ls_matvec_host", "ls_gmres", "ls_gmres_restarted",
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
-    "ls_write_result",
+    "ls_write_result", "ls_set_pdl", "ls_get_pdl", "ls_time_matvec_phases", "ls_measure_fma_peak",
 )
 # Every symbol declared in include/ls_fno.h (learned preconditioner).
 FNO_SYMBOLS = (
@@ -209,6 +209,10 @@ def lib():
         L.ls_write_result.argtypes = [ctypes.c_char_p, ctypes.c_int, dp]
         L.ls_last_error.restype = ctypes.c_char_p
         L.ls_version.restype = ctypes.c_char_p
+        L.ls_set_pdl.argtypes = [ctypes.c_int]
+        L.ls_time_matvec_phases.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+        L.ls_measure_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, dp]
+        L.ls_get_pdl.argtypes = []
         fp = ctypes.POINTER(ctypes.c_float)
         L.ls_fno_create.argtypes = [ctypes.POINTER(_FnoConfig), ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
         L.ls_fno_destroy.argtypes = [vp]
@@ -229,6 +233,26 @@ def lib():
                 getattr(L, n).restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+def measure_fma_peak(device=0, kind="fp64"):
+    """Measured FMA throughput of the device in TFLOP/s (ls_measure_fma_peak):
+    kind "fp64" (DFMA) or "fp32" (FFMA)."""
+    v = ctypes.c_double()
+    _check(lib().ls_measure_fma_peak(int(device), 0 if kind == "fp64" else 1, ctypes.byref(v)),
+           "ls_measure_fma_peak")
+    return v.value
+
+
+def set_pdl(on):
+    """Launch the matvec and Krylov kernel chains with programmatic dependent
+    launch (True, the default) or as plain stream-ordered launches
+    (ls_set_pdl). Results are bitwise identical either way."""
+    _check(lib().ls_set_pdl(1 if on else 0), "ls_set_pdl")
+
+
+def get_pdl():
+    return bool(lib().ls_get_pdl())
 
 
 def _check(code, what):
@@ -385,6 +409,13 @@ class Operator:
         _check(lib().ls_time_matvec(self._h, int(precision), int(warmup), int(iters), ctypes.byref(a),
                                     ctypes.byref(b)), "ls_time_matvec")
         return a.value, b.value
+
+    def time_matvec_phases(self, warmup=3, iters=20, precision=LS_PREC_F64):
+        """Mean ms per matvec by phase: dict with total, up, m2l, down, near."""
+        ms = (ctypes.c_float * 5)()
+        _check(lib().ls_time_matvec_phases(self._h, int(precision), int(warmup), int(iters), ms),
+               "ls_time_matvec_phases")
+        return dict(zip(("total", "up", "m2l", "down", "near"), (float(v) for v in ms)))
 
     def interpolate(self, xy, phi):
         """The density phi (nodes) at the points xy (n x 2) by the

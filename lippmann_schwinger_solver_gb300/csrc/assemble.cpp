@@ -712,7 +712,10 @@ class Builder {
 // magnitude: every index whose |v| equals the largest one has
 // re^2 + im^2 >= Q (1 - 1e-12), and every other index has a strictly
 // smaller |v|. The rule above, run on those candidates alone, therefore
-// picks the same index as a scan of all of them.
+// picks the same index as a scan of all of them. That bound needs the
+// squares to carry full relative precision: below |v| ~ 1e-145 they are
+// subnormal (or zero), so when Q < 1e-290 every unused index goes through
+// hypot.
 static int argmax_remaining(const std::vector<cd>& v, const std::vector<char>& used) {
   const int n = (int)v.size();
   double Q = -1.0;
@@ -722,7 +725,7 @@ static int argmax_remaining(const std::vector<cd>& v, const std::vector<char>& u
     if (q > Q) Q = q;
   }
   if (Q < 0.0) return 0;  // every index used
-  const double cut = Q * (1.0 - 1e-12);
+  const double cut = Q < 1e-290 ? -1.0 : Q * (1.0 - 1e-12);
   int idx = -1;
   double mx = 0.0;
   for (int i = 0; i < n; ++i) {

@@ -161,9 +161,9 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
       const float2 a0 = __ldcs(a + 32 * q), a1 = __ldcs(a + 32 * (q + 1));
       float4 v0[NV], v1[NV];
 #pragma unroll
-      for (int p = 0; p < NV; ++p) v0[p] = src4[(size_t)i0 * NV + p];
+      for (int p = 0; p < NV; ++p) v0[p] = ld_chain(src4 + (size_t)i0 * NV + p);
 #pragma unroll
-      for (int p = 0; p < NV; ++p) v1[p] = src4[(size_t)i1 * NV + p];
+      for (int p = 0; p < NV; ++p) v1[p] = ld_chain(src4 + (size_t)i1 * NV + p);
 #pragma unroll
       for (int p = 0; p < NV; ++p) {
         cmac32(sr[2 * p], si[2 * p], a0, v0[p].x, v0[p].y);
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
       const float2 a0 = __ldcs(a + 32 * q);
 #pragma unroll
       for (int p = 0; p < NV; ++p) {
-        const float4 v = src4[(size_t)i0 * NV + p];
+        const float4 v = ld_chain(src4 + (size_t)i0 * NV + p);
         cmac32(sr[2 * p], si[2 * p], a0, v.x, v.y);
         cmac32(sr[2 * p + 1], si[2 * p + 1], a0, v.z, v.w);
       }
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
       for (int p = 0; p < NV; ++p) {
         float4 v = make_float4(sr[2 * p], si[2 * p], sr[2 * p + 1], si[2 * p + 1]);
         if (accumulate) {
-          const float4 u = o4[p];
+          const float4 u = ld_chain(o4 + p);
           v.x += u.x;
           v.y += u.y;
           v.z += u.z;
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(352, 2) near_gemm_block_kernel(int n_leaves, i
   const int tot = NS * rank * NV;
   for (int i = threadIdx.x; i < tot; i += blockDim.x) {
     const int s = i / (rank * NV);
-    sx4[i] = s0 + s < n_leaves ? reinterpret_cast<const float4*>(x)[(size_t)s0 * rank * NV + i]
+    sx4[i] = s0 + s < n_leaves ? ld_chain(reinterpret_cast<const float4*>(x) + (size_t)s0 * rank * NV + i)
                                : make_float4(0.f, 0.f, 0.f, 0.f);
   }
   __syncthreads();
@@ -276,14 +276,14 @@ __global__ void __launch_bounds__(256) near_gather_block_kernel(int n_out, int r
   for (int q = 0; q < 9; ++q) {
     const int nbx = coll[leaf * 9 + q];
     if (nbx < 0) continue;
-    const float2 z = Z[((size_t)nbx * per + (size_t)q * rank + row) * NR + j];
+    const float2 z = ld_chain(Z + ((size_t)nbx * per + (size_t)q * rank + row) * NR + j);
     ar += z.x;
     ai += z.y;
   }
-  const float2 p = P[e];
+  const float2 p = ld_chain(P + e);
   if (find_phi) {
     const float s = kq[t];
-    const float2 xs = x[e];
+    const float2 xs = ld_chain(x + e);
     y[e] = make_float2(p.x + s * ar + xs.x, p.y + s * ai + xs.y);
   } else {
     y[e] = make_float2(p.x + ar, p.y + ai);
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kBDotThreads) multidot_block_kernel(const floa
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
 #pragma unroll
     for (int p = 0; p < NV; ++p) {
-      const float4 a = v4[(size_t)i * NV + p], b = w4[(size_t)i * NV + p];
+      const float4 a = ld_chain(v4 + (size_t)i * NV + p), b = ld_chain(w4 + (size_t)i * NV + p);
       ar[2 * p] = fmaf(a.x, b.x, fmaf(a.y, b.y, ar[2 * p]));
       ai[2 * p] = fmaf(a.x, b.y, fmaf(-a.y, b.x, ai[2 * p]));
       ar[2 * p + 1] = fmaf(a.z, b.z, fmaf(a.w, b.w, ar[2 * p + 1]));
@@ -353,7 +353,7 @@ __global__ void reduce_block_partials_kernel(const double2* __restrict__ partial
   if (c >= nent) return;
   double a = 0.0, b = 0.0;
   for (int k = lane; k < nb; k += 32) {
-    const double2 p = partial[(size_t)c * nb + k];
+    const double2 p = ld_chain(partial + (size_t)c * nb + k);
     a += p.x;
     b += p.y;
   }
@@ -379,18 +379,18 @@ __global__ void __launch_bounds__(256, 4) multi_axpy_block_kernel(float2* __rest
     for (; c + 4 <= ncols; c += 4) {
       float2 v[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = V[(size_t)(c + u) * stride + e];
+      for (int u = 0; u < 4; ++u) v[u] = ld_chain(V + (size_t)(c + u) * stride + e);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const double2 hc = h[(size_t)(c + u) * NR + j];
+        const double2 hc = ld_chain(h + (size_t)(c + u) * NR + j);
         cmac32(sr, si, v[u], (float)hc.x, (float)hc.y);
       }
     }
     for (; c < ncols; ++c) {
-      const double2 hc = h[(size_t)c * NR + j];
-      cmac32(sr, si, V[(size_t)c * stride + e], (float)hc.x, (float)hc.y);
+      const double2 hc = ld_chain(h + (size_t)c * NR + j);
+      cmac32(sr, si, ld_chain(V + (size_t)c * stride + e), (float)hc.x, (float)hc.y);
     }
-    float2 o = w[e];
+    float2 o = ld_chain(w + e);
     o.x += sign * sr;
     o.y += sign * si;
     w[e] = o;
@@ -404,7 +404,7 @@ __global__ void scale_block_kernel(const float2* __restrict__ a, float2* __restr
   pdl_enter();
   __shared__ float f[NR];
   if (threadIdx.x < NR) {
-    const double nn = nrm[threadIdx.x].x;
+    const double nn = ld_chain(nrm + threadIdx.x).x;
     f[threadIdx.x] = nn > 0.0 ? (float)(1.0 / sqrt(nn)) : 0.f;
   }
   __syncthreads();
@@ -412,7 +412,8 @@ __global__ void scale_block_kernel(const float2* __restrict__ a, float2* __restr
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (long long)gridDim.x * blockDim.x) {
     const float s = f[e % NR];
-    b[e] = make_float2(a[e].x * s, a[e].y * s);
+    const float2 v = ld_chain(a + e);
+    b[e] = make_float2(v.x * s, v.y * s);
   }
 }
 
@@ -424,7 +425,7 @@ __global__ void pack_block_kernel(const double2* __restrict__ r, float2* __restr
        e += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(e / NR), j = (int)(e % NR);
     if ((active >> j) & 1u) {
-      const double2 v = r[(size_t)j * n + i];
+      const double2 v = ld_chain(r + (size_t)j * n + i);
       r32[e] = make_float2((float)v.x, (float)v.y);
     } else {
       r32[e] = make_float2(0.f, 0.f);
@@ -441,17 +442,21 @@ __global__ void unpack_add_block_kernel(double2* __restrict__ x, const float2* _
        e += (long long)gridDim.x * blockDim.x) {
     const int j = (int)(e / n), i = (int)(e % n);
     if (!((active >> j) & 1u)) continue;
-    const float2 d = dx[(size_t)i * NR + j];
-    x[e].x += (double)d.x;
-    x[e].y += (double)d.y;
+    const float2 d = ld_chain(dx + (size_t)i * NR + j);
+    double2 u = ld_chain(x + e);
+    u.x += (double)d.x;
+    u.y += (double)d.y;
+    x[e] = u;
   }
 }
 
 __global__ void sub64_kernel(const double2* __restrict__ a, const double2* __restrict__ b, double2* __restrict__ c,
                              int n) {
   pdl_enter();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    c[i] = make_double2(a[i].x - b[i].x, a[i].y - b[i].y);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 u = ld_chain(a + i), v = ld_chain(b + i);
+    c[i] = make_double2(u.x - v.x, u.y - v.y);
+  }
 }
 
 // partial[col * gridDim.x + block] = |A[:, col]|^2 over the block's rows (FP64 columns, leading dimension n).
@@ -465,7 +470,7 @@ __global__ void __launch_bounds__(kBDotThreads) colnorm_kernel(const double2* __
   const double2* __restrict__ a = A + (size_t)blockIdx.y * n + r0;
   double s = 0.0;
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
-    const double2 v = a[i];
+    const double2 v = ld_chain(a + i);
     s = fma(v.x, v.x, fma(v.y, v.y, s));
   }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);

@@ -2,7 +2,9 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -42,6 +44,21 @@ struct ls_fno {
 namespace lsg {
 static thread_local std::string t_last_error;
 void set_error(const std::string& msg) { t_last_error = msg; }
+
+// Programmatic dependent launch of the kernel chains (launch.h): read from
+// LS_PDL on first use (0 turns it off), then set by ls_set_pdl.
+static std::atomic<int> g_pdl{-1};
+int pdl_enabled() {
+  int v = g_pdl.load(std::memory_order_relaxed);
+  if (v < 0) {
+    const char* e = std::getenv("LS_PDL");
+    v = (e && e[0] == '0') ? 0 : 1;
+    int expected = -1;
+    if (!g_pdl.compare_exchange_strong(expected, v)) v = expected;
+  }
+  return v;
+}
+void set_pdl_enabled(int on) { g_pdl.store(on ? 1 : 0); }
 }  // namespace lsg
 
 using namespace lsg;
@@ -222,12 +239,12 @@ ls_status ls_matvec_f32(ls_op* op, const double* x, double* y, void* stream) {
 
 ls_status ls_matvec_noalloc(ls_op* op, const double* x, double* y, void* stream) {
   if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_noalloc: null argument");
-  if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_noalloc: operator was assembled without a device");
-  const long long need = op->dev.charges_len + op->dev.pots_len;
+  const long long need = op->host.charges_len + op->host.pots_len;
   if (need > LS_STATIC_SCRATCH_ELEMS)
     return fail(LS_E_INVALID, "ls_matvec_noalloc: operator needs " + std::to_string(need) +
                                   " complex scratch entries, the static array holds " +
                                   std::to_string((long long)LS_STATIC_SCRATCH_ELEMS));
+  if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_noalloc: operator was assembled without a device");
   cudaError_t e = dev_matvec_static(op->dev, (const double2*)x, (double2*)y, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_noalloc");
   return LS_OK;
@@ -384,6 +401,48 @@ ls_status ls_time_matvec(ls_op* op, int precision, int warmup, int iters, float*
   cudaEventDestroy(b);
   if (ms_matvec) *ms_matvec = total / iters;
   if (ms_m2l) *ms_m2l = m2l_total / iters;
+  return LS_OK;
+}
+
+ls_status ls_time_matvec_phases(ls_op* op, int precision, int warmup, int iters, float* ms) {
+  if (!op || iters < 1 || warmup < 0 || !ms) return fail(LS_E_INVALID, "ls_time_matvec_phases: bad argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_time_matvec_phases: operator was assembled without a device");
+  DevOperator& d = op->dev;
+  if (precision == LS_PREC_F32 && !d.has_f32)
+    return fail(LS_E_STATE, "ls_time_matvec_phases: FP32 operator not enabled");
+  cudaSetDevice(d.device);
+  const bool f32 = precision == LS_PREC_F32;
+  cudaError_t e;
+  for (int i = 0; i < warmup; ++i) {
+    e = f32 ? dev_matvec_f32(d, d.xbuf, d.ybuf, d.stream, false) : dev_matvec(d, d.xbuf, d.ybuf, d.stream, false);
+    if (e != cudaSuccess) return cuda_fail(e, "ls_time_matvec_phases warmup");
+  }
+  cudaEvent_t a, b;
+  if ((e = cudaEventCreate(&a)) != cudaSuccess) return cuda_fail(e, "ls_time_matvec_phases event");
+  if ((e = cudaEventCreate(&b)) != cudaSuccess) {
+    cudaEventDestroy(a);
+    return cuda_fail(e, "ls_time_matvec_phases event");
+  }
+  double acc[5] = {0, 0, 0, 0, 0};
+  const cudaEvent_t m0 = f32 ? d.ev[2] : d.ev[0], m1 = f32 ? d.ev[3] : d.ev[1], m2 = d.ev_down[f32 ? 1 : 0];
+  for (int i = 0; i < iters && e == cudaSuccess; ++i) {
+    cudaEventRecord(a, d.stream);
+    e = f32 ? dev_matvec_f32(d, d.xbuf, d.ybuf, d.stream, true) : dev_matvec(d, d.xbuf, d.ybuf, d.stream, true);
+    if (e != cudaSuccess) break;
+    cudaEventRecord(b, d.stream);
+    if ((e = cudaEventSynchronize(b)) != cudaSuccess) break;
+    float t[5] = {0, 0, 0, 0, 0};
+    cudaEventElapsedTime(&t[0], a, b);
+    cudaEventElapsedTime(&t[1], a, m0);
+    cudaEventElapsedTime(&t[2], m0, m1);
+    cudaEventElapsedTime(&t[3], m1, m2);
+    cudaEventElapsedTime(&t[4], m2, b);
+    for (int k = 0; k < 5; ++k) acc[k] += t[k];
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_time_matvec_phases");
+  for (int k = 0; k < 5; ++k) ms[k] = (float)(acc[k] / iters);
   return LS_OK;
 }
 
@@ -641,6 +700,12 @@ ls_status ls_fgmres_nn(ls_op* op, ls_fno* net, const double* b, int flags, int m
   if (!(rr <= tol)) return fail(LS_E_NOT_CONVERGED, "ls_fgmres_nn: tolerance not reached");
   return LS_OK;
 }
+
+ls_status ls_set_pdl(int on) {
+  set_pdl_enabled(on);
+  return LS_OK;
+}
+int ls_get_pdl(void) { return pdl_enabled(); }
 
 const char* ls_last_error(void) { return t_last_error.c_str(); }
 const char* ls_version(void) { return "lsdafmm-gb300 0.1 (sm_103a)"; }

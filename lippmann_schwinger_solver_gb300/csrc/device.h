@@ -81,6 +81,9 @@ struct DevOperator {
   BatchWorkspace* bws = nullptr;
   // events for phase timing
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // recorded after the downward phases (before the near field) when phases
+  // are marked: [0] FP64 operator, [1] FP32 operator
+  cudaEvent_t ev_down[2] = {nullptr, nullptr};
   long long device_bytes = 0;
   int launches_per_matvec = 0;
 };

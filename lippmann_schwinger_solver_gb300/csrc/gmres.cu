@@ -190,11 +190,11 @@ __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restri
 #pragma unroll
   for (int j = 0; j < kDotCols; ++j) ar[j] = ai[j] = R(0);
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
-    const T b = w[r0 + i];
+    const T b = ld_chain(w + r0 + i);
     T a[kDotCols];
 #pragma unroll
     for (int j = 0; j < kDotCols; ++j)  // all loads first, so that they are in flight together
-      a[j] = j < nc ? V[(size_t)(c0 + j) * ldv + r0 + i] : Cx<T>::make(R(0), R(0));
+      a[j] = j < nc ? ld_chain(V + (size_t)(c0 + j) * ldv + r0 + i) : Cx<T>::make(R(0), R(0));
 #pragma unroll
     for (int j = 0; j < kDotCols; ++j) {
       ar[j] = fma(a[j].x, b.x, ar[j]);
@@ -258,7 +258,7 @@ __global__ void reduce_partials_kernel(const double2* __restrict__ partial, int 
   if (col >= ncols) return;
   double a = 0.0, b = 0.0;
   for (int k = lane; k < nb; k += 32) {
-    const double2 p = partial[(size_t)col * nb + k];
+    const double2 p = ld_chain(partial + (size_t)col * nb + k);
     a += p.x;
     b += p.y;
   }
@@ -283,10 +283,11 @@ __global__ void __launch_bounds__(256) multi_axpy_kernel(T* __restrict__ w, cons
     for (; c + 4 <= ncols; c += 4) {
       T v[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) v[j] = V[(size_t)(c + j) * ldv + i];
+      for (int j = 0; j < 4; ++j) v[j] = ld_chain(V + (size_t)(c + j) * ldv + i);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const R hx = (R)h[c + j].x, hy = (R)h[c + j].y;
+        const double2 hc = ld_chain(h + c + j);
+        const R hx = (R)hc.x, hy = (R)hc.y;
         sr = fma(v[j].x, hx, sr);
         sr = fma(-v[j].y, hy, sr);
         si = fma(v[j].x, hy, si);
@@ -294,14 +295,15 @@ __global__ void __launch_bounds__(256) multi_axpy_kernel(T* __restrict__ w, cons
       }
     }
     for (; c < ncols; ++c) {
-      const T v = V[(size_t)c * ldv + i];
-      const R hx = (R)h[c].x, hy = (R)h[c].y;
+      const T v = ld_chain(V + (size_t)c * ldv + i);
+      const double2 hc = ld_chain(h + c);
+      const R hx = (R)hc.x, hy = (R)hc.y;
       sr = fma(v.x, hx, sr);
       sr = fma(-v.y, hy, sr);
       si = fma(v.x, hy, si);
       si = fma(v.y, hx, si);
     }
-    T o = w[i];
+    T o = ld_chain(w + i);
     o.x += (R)sign * sr;
     o.y += (R)sign * si;
     w[i] = o;
@@ -312,8 +314,10 @@ template <class T>
 __global__ void scale_kernel(const T* __restrict__ a, T* __restrict__ b, double s, int n) {
   pdl_enter();
   using R = typename Cx<T>::R;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = Cx<T>::make(a[i].x * (R)s, a[i].y * (R)s);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const T v = ld_chain(a + i);
+    b[i] = Cx<T>::make(v.x * (R)s, v.y * (R)s);
+  }
 }
 
 // b = a / sqrt(nrm->x), or zeros when the norm is zero (breakdown; the
@@ -325,34 +329,43 @@ __global__ void scale_by_norm_kernel(const T* __restrict__ a, T* __restrict__ b,
   using R = typename Cx<T>::R;
   __shared__ R f;  // formed once per thread block (FP64 divides are slow on GB300)
   if (threadIdx.x == 0) {
-    const double nn = nrm->x;
+    const double nn = ld_chain(nrm).x;
     f = nn > 0.0 ? (R)(1.0 / sqrt(nn)) : R(0);
   }
   __syncthreads();
   const R s = f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = Cx<T>::make(a[i].x * s, a[i].y * s);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const T v = ld_chain(a + i);
+    b[i] = Cx<T>::make(v.x * s, v.y * s);
+  }
 }
 
 template <class T>
 __global__ void sub_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ c, int n) {
   pdl_enter();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    c[i] = Cx<T>::make(a[i].x - b[i].x, a[i].y - b[i].y);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const T u = ld_chain(a + i), v = ld_chain(b + i);
+    c[i] = Cx<T>::make(u.x - v.x, u.y - v.y);
+  }
 }
 
 __global__ void to_f32_kernel(const double2* __restrict__ a, float2* __restrict__ b, int n) {
   pdl_enter();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    b[i] = make_float2((float)a[i].x, (float)a[i].y);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 v = ld_chain(a + i);
+    b[i] = make_float2((float)v.x, (float)v.y);
+  }
 }
 
 // a += b, with b widened to FP64
 __global__ void add_f32_kernel(double2* __restrict__ a, const float2* __restrict__ b, int n) {
   pdl_enter();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    a[i].x += (double)b[i].x;
-    a[i].y += (double)b[i].y;
+    double2 u = ld_chain(a + i);
+    const float2 v = ld_chain(b + i);
+    u.x += (double)v.x;
+    u.y += (double)v.y;
+    a[i] = u;
   }
 }
 

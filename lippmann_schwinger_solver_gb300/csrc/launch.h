@@ -13,6 +13,21 @@
 // predecessor's completion and memory. The wait is the hardware's grid
 // dependency, released when the predecessor grid completes; a kernel
 // launched without the attribute passes through both instructions.
+//
+// Completion is transitive (a kernel cannot finish before its own wait
+// returned), but residency is not: because each kernel releases its
+// successor before it waits, kernel K can become resident on an SM while
+// K-2 or an earlier kernel of the chain still runs there. Lines that such
+// an earlier kernel loads into that SM's L1 / read-only cache after K
+// arrived are not refreshed when K-1 later rewrites the data from other
+// SMs. So every read of data that some kernel of a chain writes (charges,
+// potentials, Krylov vectors, coefficients) goes through ld_chain(), an
+// L2-coherent load (ld.global.cg) that never hits a stale L1 line; only the
+// operator's own blocks and index lists, which nothing rewrites while an
+// operator lives, use the cached or streaming paths.
+//
+// The chains can be launched without the attribute (plain stream order):
+// LS_PDL=0 in the environment, or ls_set_pdl(0) (include/ls_dafmm.h).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -26,8 +41,19 @@ __device__ __forceinline__ void pdl_enter() {
 #endif
 }
 
+// L2-coherent loads of chain-produced data (see above).
+__device__ __forceinline__ double2 ld_chain(const double2* p) { return __ldcg(p); }
+__device__ __forceinline__ float2 ld_chain(const float2* p) { return __ldcg(p); }
+__device__ __forceinline__ float4 ld_chain(const float4* p) { return __ldcg(p); }
+__device__ __forceinline__ double ld_chain(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ld_chain(const float* p) { return __ldcg(p); }
+
+// 1: chains use programmatic dependent launch (default), 0: plain launches.
+int pdl_enabled();
+void set_pdl_enabled(int on);
+
 // kernel<<<grid, block, smem, s>>>(args...) with programmatic stream
-// serialization allowed.
+// serialization allowed (unless turned off, see pdl_enabled()).
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
                               Args... args) {
@@ -40,7 +66,7 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 

@@ -17,6 +17,7 @@
 // block, so every output element is written by exactly one warp and the
 // sums are deterministic (no atomics).
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,6 +26,7 @@
 #include <string>
 #include <vector>
 
+#include "context_cache.h"
 #include "device.h"
 #include "launch.h"
 
@@ -69,7 +71,7 @@ __global__ void __launch_bounds__(256, 3) gemv_tiles_kernel(const GemvTile* __re
       const int i0 = ix[S * q], i1 = ix[S * (q + 1)], i2 = ix[S * (q + 2)], i3 = ix[S * (q + 3)];
       const C a0 = ld_stream(a + 32 * q), a1 = ld_stream(a + 32 * (q + 1));
       const C a2 = ld_stream(a + 32 * (q + 2)), a3 = ld_stream(a + 32 * (q + 3));
-      const C x0 = src[i0], x1 = src[i1], x2 = src[i2], x3 = src[i3];
+      const C x0 = ld_chain(src + i0), x1 = ld_chain(src + i1), x2 = ld_chain(src + i2), x3 = ld_chain(src + i3);
       sr = fma(a0.x, x0.x, sr); sr = fma(-a0.y, x0.y, sr); si = fma(a0.x, x0.y, si); si = fma(a0.y, x0.x, si);
       sr = fma(a1.x, x1.x, sr); sr = fma(-a1.y, x1.y, sr); si = fma(a1.x, x1.y, si); si = fma(a1.y, x1.x, si);
       sr = fma(a2.x, x2.x, sr); sr = fma(-a2.y, x2.y, sr); si = fma(a2.x, x2.y, si); si = fma(a2.y, x2.x, si);
@@ -77,7 +79,7 @@ __global__ void __launch_bounds__(256, 3) gemv_tiles_kernel(const GemvTile* __re
     }
     for (; q < ql; ++q) {
       const C a0 = ld_stream(a + 32 * q);
-      const C x0 = src[ix[S * q]];
+      const C x0 = ld_chain(src + ix[S * q]);
       sr = fma(a0.x, x0.x, sr); sr = fma(-a0.y, x0.y, sr); si = fma(a0.x, x0.y, si); si = fma(a0.y, x0.x, si);
     }
     // Combine the slices: lanes r, r + R, r + 2R, ... (R = 32 >> log2s).
@@ -88,7 +90,7 @@ __global__ void __launch_bounds__(256, 3) gemv_tiles_kernel(const GemvTile* __re
     if (lane < t.rows) {
       C* o = dst + out[t.row_base + lane];
       if (accumulate) {
-        C v = *o;
+        C v = ld_chain(o);
         v.x += sr;
         v.y += si;
         *o = v;
@@ -155,7 +157,7 @@ __global__ void __launch_bounds__(256) near_coeff_kernel(int n_leaves, int rank,
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = n_leaves * rank;
   for (int i = t; i < n; i += gridDim.x * blockDim.x) {
-    const double2 xv = x[i];
+    const double2 xv = ld_chain(x + i);
     x32[i] = make_float2((float)xv.x, (float)xv.y);
   }
   if (t >= n_leaves * nb) return;
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(256) near_coeff_kernel(int n_leaves, int rank,
   double cr = 0.0, ci = 0.0;
   for (int i = 0; i < rank; ++i) {
     const double w = q[i];
-    const double2 v = xs[i];
+    const double2 v = ld_chain(xs + i);
     cr = fma(w, v.x, cr);
     ci = fma(w, v.y, ci);
   }
@@ -196,7 +198,7 @@ __global__ void __launch_bounds__(256, 4) near_factored_kernel(int n_out, int ra
     const double2* __restrict__ cc = c + (size_t)nbx * nb;
     for (int l = 0; l < nb; ++l) {
       const double2 a = v[(size_t)l * rank];
-      const double2 b = cc[l];
+      const double2 b = ld_chain(cc + l);
       ar = fma(a.x, b.x, ar);
       ar = fma(-a.y, b.y, ar);
       ai = fma(a.x, b.y, ai);
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(256, 4) near_factored_kernel(int n_out, int ra
     float er = 0.0f, ei = 0.0f;
     for (int k = 0; k < rank; ++k) {
       const float2 a = e[(size_t)k * rank];
-      const float2 b = xs[k];
+      const float2 b = ld_chain(xs + k);
       er = fmaf(a.x, b.x, er);
       er = fmaf(-a.y, b.y, er);
       ei = fmaf(a.x, b.y, ei);
@@ -216,10 +218,10 @@ __global__ void __launch_bounds__(256, 4) near_factored_kernel(int n_out, int ra
     ar += (double)er;
     ai += (double)ei;
   }
-  const double2 p = P[t];
+  const double2 p = ld_chain(P + t);
   if (find_phi) {
     const double s = kq[t];
-    const double2 xs = x[t];
+    const double2 xs = ld_chain(x + t);
     y[t] = make_double2(p.x + s * ar + xs.x, p.y + s * ai + xs.y);
   } else {
     y[t] = make_double2(p.x + ar, p.y + ai);
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(576, 1) near_gemm32_kernel(int n_leaves, int r
   const int s0 = blockIdx.x * NS;
   for (int i = threadIdx.x; i < NS * rank; i += blockDim.x) {
     const int j = i / rank;
-    sx32[i] = s0 + j < n_leaves ? x[(size_t)s0 * rank + i] : make_float2(0.f, 0.f);
+    sx32[i] = s0 + j < n_leaves ? ld_chain(x + (size_t)s0 * rank + i) : make_float2(0.f, 0.f);
   }
   __syncthreads();
   const int qr = threadIdx.x;
@@ -292,14 +294,14 @@ __global__ void __launch_bounds__(256) near_gather32_kernel(int n_out, int rank,
   for (int q = 0; q < 9; ++q) {
     const int nbx = coll[leaf * 9 + q];
     if (nbx < 0) continue;
-    const float2 z = Z[(size_t)nbx * per + (size_t)q * rank + row];
+    const float2 z = ld_chain(Z + (size_t)nbx * per + (size_t)q * rank + row);
     ar += z.x;
     ai += z.y;
   }
-  const float2 p = P[t];
+  const float2 p = ld_chain(P + t);
   if (find_phi) {
     const float s = kq[t];
-    const float2 xs = x[t];
+    const float2 xs = ld_chain(x + t);
     store_out(y, t, p.x + s * ar + xs.x, p.y + s * ai + xs.y);
   } else {
     store_out(y, t, p.x + ar, p.y + ai);
@@ -327,7 +329,7 @@ __global__ void load_zero_kernel(const X* __restrict__ x, C* __restrict__ S, lon
   pdl_enter();
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride)
-    S[i] = conv(x[i], (C*)nullptr);
+    S[i] = conv(ld_chain(x + i), (C*)nullptr);
   C z;
   z.x = 0;
   z.y = 0;
@@ -408,6 +410,8 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
     return false;
   }
   for (auto& ev : d.ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) { err = "cudaEventCreate"; return false; }
+  for (auto& ev : d.ev_down)
     if (cudaEventCreate(&ev) != cudaSuccess) { err = "cudaEventCreate"; return false; }
   d.N = h.N;
   d.n_leaves = h.n_leaves;
@@ -494,6 +498,7 @@ void dev_free(DevOperator& d) {
   dev_free_gmres(d);
   dev_free_batch(d);
   for (auto& ev : d.ev) if (ev) cudaEventDestroy(ev);
+  for (auto& ev : d.ev_down) if (ev) cudaEventDestroy(ev);
   if (d.stream) cudaStreamDestroy(d.stream);
   d = DevOperator();
 }
@@ -545,6 +550,7 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
   launch_gemv<1>(d.m2l, (const double2*)d.S, d.P, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down) launch_gemv<2>(ph, (const double2*)d.P, d.P, s, d.device);
+  if (mark_m2l) cudaEventRecord(d.ev_down[0], s);
   launch_pdl(near_coeff_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
              d.n_bases, d.Qp, d.S, d.cbuf, d.x32);
   launch_pdl(near_factored_kernel, (unsigned)((d.N + 255) / 256), 256, 0, s, d.N, d.rank, d.n_bases, d.nearVt,
@@ -560,6 +566,7 @@ static cudaError_t f32_phases(DevOperator& d, Y* y, cudaStream_t s, bool mark_m2
   launch_gemv<1>(d.m2l32, (const float2*)d.S32, d.P32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[3], s);
   for (auto& ph : d.down32) launch_gemv<2>(ph, (const float2*)d.P32, d.P32, s, d.device);
+  if (mark_m2l) cudaEventRecord(d.ev_down[1], s);
   const int nthr = (9 * d.rank + 31) / 32 * 32;
   launch_pdl(near_gemm32_kernel, (unsigned)((d.n_leaves + kNearSources32 - 1) / kNearSources32), (unsigned)nthr,
              (size_t)kNearSources32 * d.rank * sizeof(float2), s, d.n_leaves, d.rank, d.nearB32, d.S32, d.Z32);
@@ -604,33 +611,64 @@ cudaError_t dev_matvec_f32v(DevOperator& d, const float2* x, float2* y, cudaStre
 
 namespace {
 
-constexpr int kMaxScratchDevices = 64;
-
 static __device__ __align__(256) double2 g_static_scratch[kStaticScratchElems];
 
-std::mutex g_scratch_mu;
-double2* g_scratch_ptr[kMaxScratchDevices] = {};
+// Unique ID of the calling thread's current CUDA context (0 when there is
+// none). The driver entry points are fetched through the runtime, so the
+// library does not link libcuda itself.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+cudaError_t current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  if (!get_current || !get_id) return cudaErrorNotSupported;
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  if (!ctx) {
+    *id = 0;
+    return cudaSuccess;
+  }
+  return get_id(ctx, id) == CUDA_SUCCESS ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
+
+ContextCache<double2*> g_scratch_cache;
 
 // Device address of g_static_scratch on `device`. In host code the symbol
-// is only a host-side stand-in, so the address is looked up once per device
-// with that device current (the first call on a device does this set-up and
-// should come before any stream capture).
+// is only a host-side stand-in, so the address is looked up with that
+// device current, once per device and context (the first call on a device
+// does this set-up and should come before any stream capture; a call after
+// cudaDeviceReset looks it up again in the new context).
 cudaError_t static_scratch_address(int device, double2** out) {
-  if (device < 0 || device >= kMaxScratchDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[device]) {
-    int cur = -1;
-    cudaError_t e = cudaGetDevice(&cur);
-    if (e != cudaSuccess) return e;
-    if (cur != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (cur != device) cudaSetDevice(cur);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[device] = static_cast<double2*>(p);
+  int cur = -1;
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e != cudaSuccess) return e;
+  if (cur != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
+  unsigned long long ctx = 0;
+  e = current_context_id(&ctx);
+  if (e == cudaSuccess) {
+    const int rc = g_scratch_cache.get(device, ctx, [](double2** v) {
+      void* p = nullptr;
+      const cudaError_t ge = cudaGetSymbolAddress(&p, g_static_scratch);
+      *v = static_cast<double2*>(p);
+      return (int)ge;
+    }, out);
+    e = rc < 0 ? cudaErrorInvalidDevice : (cudaError_t)rc;
   }
-  *out = g_scratch_ptr[device];
-  return cudaSuccess;
+  if (cur != device) cudaSetDevice(cur);
+  return e;
 }
 
 }  // namespace

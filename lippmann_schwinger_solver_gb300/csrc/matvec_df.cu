@@ -100,7 +100,7 @@ __global__ void split_zero_kernel(const double2* __restrict__ x, float4* __restr
                                   float4* __restrict__ P, long long np) {
   pdl_enter();
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) S[i] = split(x[i]);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) S[i] = split(ld_chain(x + i));
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += stride)
     P[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
@@ -134,13 +134,13 @@ __global__ void __launch_bounds__(256, 3) gemv_df_kernel(const GemvTile* __restr
       const int i0 = ix[S * q], i1 = ix[S * (q + 1)], i2 = ix[S * (q + 2)], i3 = ix[S * (q + 3)];
       const float4 a0 = __ldcs(a + 32 * q), a1 = __ldcs(a + 32 * (q + 1));
       const float4 a2 = __ldcs(a + 32 * (q + 2)), a3 = __ldcs(a + 32 * (q + 3));
-      const float4 x0 = src[i0], x1 = src[i1], x2 = src[i2], x3 = src[i3];
+      const float4 x0 = ld_chain(src + i0), x1 = ld_chain(src + i1), x2 = ld_chain(src + i2), x3 = ld_chain(src + i3);
       cmac(rh, rl, ih, il, a0, x0);
       cmac(rh, rl, ih, il, a1, x1);
       cmac(rh, rl, ih, il, a2, x2);
       cmac(rh, rl, ih, il, a3, x3);
     }
-    for (; q < ql; ++q) cmac(rh, rl, ih, il, __ldcs(a + 32 * q), src[ix[S * q]]);
+    for (; q < ql; ++q) cmac(rh, rl, ih, il, __ldcs(a + 32 * q), ld_chain(src + ix[S * q]));
     for (int o = 16; o >= (32 >> t.log2s); o >>= 1) {
       const float rh2 = __shfl_xor_sync(0xffffffffu, rh, o), rl2 = __shfl_xor_sync(0xffffffffu, rl, o);
       const float ih2 = __shfl_xor_sync(0xffffffffu, ih, o), il2 = __shfl_xor_sync(0xffffffffu, il, o);
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256, 3) gemv_df_kernel(const GemvTile* __restr
     if (lane < t.rows) {
       float4* o = dst + out[t.row_base + lane];
       if (accumulate) {
-        const float4 v = *o;
+        const float4 v = ld_chain(o);
         dd_add(rh, rl, v.x, v.z);
         dd_add(ih, il, v.y, v.w);
       }
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) near_coeff_df_kernel(int n_leaves, int ra
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = n_leaves * rank;
   for (int i = t; i < n; i += gridDim.x * blockDim.x) {
-    const float4 v = x[i];
+    const float4 v = ld_chain(x + i);
     x32[i] = make_float2(v.x, v.y);
   }
   if (t >= n_leaves * nb) return;
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(256) near_coeff_df_kernel(int n_leaves, int ra
   float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
   for (int i = 0; i < rank; ++i) {
     const float2 w = q[i];
-    const float4 v = xs[i];
+    const float4 v = ld_chain(xs + i);
     dd_mac(rh, rl, w.x, w.y, v.x, v.z);
     dd_mac(ih, il, w.x, w.y, v.y, v.w);
   }
@@ -216,11 +216,11 @@ __global__ void __launch_bounds__(kNearThreads, kNearMinBlocks) near_gemm_df_ker
   const int s0 = blockIdx.x * NS;
   for (int i = threadIdx.x; i < NS * nb; i += blockDim.x) {
     const int j = i / nb;
-    sc[i] = s0 + j < n_leaves ? c[(size_t)s0 * nb + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    sc[i] = s0 + j < n_leaves ? ld_chain(c + (size_t)s0 * nb + i) : make_float4(0.f, 0.f, 0.f, 0.f);
   }
   for (int i = threadIdx.x; i < NS * rank; i += blockDim.x) {
     const int j = i / rank;
-    sx[i] = s0 + j < n_leaves ? x32[(size_t)s0 * rank + i] : make_float2(0.f, 0.f);
+    sx[i] = s0 + j < n_leaves ? ld_chain(x32 + (size_t)s0 * rank + i) : make_float2(0.f, 0.f);
   }
   __syncthreads();
   for (int qr = threadIdx.x; qr < 9 * rank; qr += blockDim.x) {
@@ -281,19 +281,19 @@ __global__ void __launch_bounds__(256) near_gather_df_kernel(int n_out, int rank
     const int nbx = coll[leaf * 9 + q];
     if (nbx < 0) continue;
     const size_t o = (size_t)nbx * per + (size_t)q * rank + row;
-    const float4 z = Z[o];
+    const float4 z = ld_chain(Z + o);
     dd_add(rh, rl, z.x, z.z);
     dd_add(ih, il, z.y, z.w);
-    const float2 w = ZE[o];
+    const float2 w = ld_chain(ZE + o);
     er += w.x;
     ei += w.y;
   }
   const double ar = ((double)rh + (double)rl) + (double)er;
   const double ai = ((double)ih + (double)il) + (double)ei;
-  const double2 p = join(P[t]);
+  const double2 p = join(ld_chain(P + t));
   if (find_phi) {
     const double s = kq[t];
-    const double2 xs = x[t];
+    const double2 xs = ld_chain(x + t);
     y[t] = make_double2(p.x + s * ar + xs.x, p.y + s * ai + xs.y);
   } else {
     y[t] = make_double2(p.x + ar, p.y + ai);
@@ -399,6 +399,7 @@ cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStre
   launch_df<1>(d.m2l_df, (const float4*)d.S_df, d.P_df, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down_df) launch_df<2>(ph, (const float4*)d.P_df, d.P_df, s, d.device);
+  if (mark_m2l) cudaEventRecord(d.ev_down[0], s);
   launch_pdl(near_coeff_df_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
              d.n_bases, d.Qp_df, d.S_df, d.c_df, d.x32);
   {

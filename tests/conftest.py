@@ -35,6 +35,9 @@ CFG_L3_K10 = dict(nLevelsUniform=3, kappa=10.0, TOL_POW=8, Qchoice=0)
 CFG_C1 = dict(nLevelsUniform=4, kappa=10.0, TOL_POW=8, Qchoice=0)
 CFG_HFR = dict(nLevelsUniform=4, kappa=24.0, TOL_POW=10, Qchoice=3)  # level_LFR 3, HFR cones at level 2
 CFG_BUMPS = dict(nLevelsUniform=4, kappa=40.0, TOL_POW=10, Qchoice=6)
+# Level 5 at kappa 40: level_LFR 4, so HFR runs at levels 3 (16 cones) and
+# 2 (32 cones) and the cone-to-cone M2M and the HFR-to-HFR L2L are used.
+CFG_L5_BUMPS = dict(nLevelsUniform=5, kappa=40.0, TOL_POW=10, Qchoice=6)
 
 
 def full_cfg(d, **over):

@@ -52,18 +52,21 @@ int main() {
     const double R = std::exp(20.0 * u(g));
     for (int i = 0; i < n; ++i) {
       used[i] = (g() % 4) == 0;
-      switch (t % 6) {
+      switch (t % 8) {
         case 0: v[i] = cd(u(g), u(g)); break;
         case 1: v[i] = std::polar(R, ph(g)); break;  // equal magnitudes, many phases
         case 2: v[i] = std::polar(R * (1.0 + 1e-16 * (double)(g() % 7)), ph(g)); break;
         case 3: { const double x = u(g); v[i] = (g() % 2) ? cd(x, 0.0) : cd(0.0, std::nextafter(x, 2.0)); } break;
         case 4: v[i] = (g() % 3 == 0) ? cd(0.0, 0.0) : cd(std::nextafter(R, 0.0) * ((g() % 2) ? 1.0 : -1.0), 0.0); break;
-        default: v[i] = cd((g() % 2) ? -0.0 : 0.0, (g() % 2) ? -0.0 : u(g) * 1e-300); break;  // zeros and tiny values
+        case 5: v[i] = cd((g() % 2) ? -0.0 : 0.0, (g() % 2) ? -0.0 : u(g) * 1e-300); break;  // zeros and tiny values
+        case 6: v[i] = std::polar(1e-160 * (1.0 + 1e-7 * (double)(g() % 5)), ph(g)); break;  // subnormal squares
+        default: v[i] = std::polar(std::exp(-345.0 - 15.0 * std::fabs(u(g))), ph(g)); break;  // squares near underflow
+
       }
     }
     if (lsg::argmax_remaining(v, used) != full_scan(v, used)) ++bad_pivot;
     std::vector<cd> w(n);
-    for (int i = 0; i < n; ++i) w[i] = (t % 6 == 5) ? cd(-0.0, u(g)) : cd(u(g) * R, u(g));
+    for (int i = 0; i < n; ++i) w[i] = (t % 8 == 5) ? cd(-0.0, u(g)) : cd(u(g) * R, u(g));
     if (!same_bits(lsg::cdot(v, w), plain_cdot(v, w))) ++bad_dot;
     const cd f(u(g), (t % 3 == 0) ? -0.0 : u(g));
     std::vector<cd> a = v, b = v;

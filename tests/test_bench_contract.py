@@ -39,7 +39,7 @@ def test_reference_arm_contract():
 
 @pytest.mark.gpu
 def test_our_arm_contract():
-    r = _run(["--level", "4", "--steps", "5", "--warmup", "3", "--no-cpu-baseline", "--no-batch", "--no-nn"])
+    r = _run(["--level", "4", "--steps", "5", "--warmup", "3", "--cpu-budget", "1", "--no-batch", "--no-nn"])
     _common(r)
     assert r["n_gpus"] == 1 and r["gpu_launches"] > 0
     rf = r["roofline"]
@@ -48,3 +48,11 @@ def test_our_arm_contract():
     assert 0 < rf["frac"] < 1.5 and rf["unit"] == "GB/s"
     assert r["e2e"]["h2d_bytes_per_step"] == 16 * int(r["config"]["workload"].split("N=")[1].split(",")[0])
     assert "sm_mhz" in r["clocks"] and r["solve"]["fp64_converged"] and r["solve"]["mixed_converged"]
+    # parity with the oracle on the benchmark input, and the CPU baseline's parts
+    assert r["parity"]["skeletons_equal"] and r["parity"]["rel_l2_vs_oracle"] <= 1e-10
+    cb = r["cpu_baseline"]
+    assert cb["one_thread"]["cores"] == 1 and cb["cpu_model"] and cb["solve_s"]["workload_true_residual"] <= 1e-8
+    fp = rf["fp64_pipe"]
+    assert fp["peak_tflops"] > 0 and 0 < fp["m2l_frac"] < 1.5 and 0 < fp["near_field_frac"] < 1.5
+    assert set(r["phases_ms"]) == {"total", "up", "m2l", "down", "near"}
+    assert r["solve"]["mixed_rel_err_vs_fp64"] < 1e-6

@@ -134,3 +134,20 @@ def test_null_handles_do_not_crash(ls):
     assert L.ls_op_info(None, None) == ls.LS_E_INVALID
     assert L.ls_matvec(None, None, None, None) == ls.LS_E_INVALID
     assert L.ls_op_skeleton_dump(None, None, 0) == -1
+
+
+def test_noalloc_rejects_operators_larger_than_its_static_array(ls):
+    """The allocation-free matvec checks the operator's scratch size first:
+    a level-7 operator needs more than LS_STATIC_SCRATCH_ELEMS (2^20)
+    complex entries and is rejected with LS_E_INVALID, also when it was
+    assembled on the host only."""
+    import ctypes
+
+    op = ls.Operator(ls.Config(nLevelsUniform=7, kappa=10.0, TOL_POW=4, Qchoice=0), device=-1)
+    rc = ls.lib().ls_matvec_noalloc(op._h, ctypes.c_void_p(16), ctypes.c_void_p(16), None)
+    assert rc == ls.LS_E_INVALID
+    assert b"static array holds 1048576" in ls.lib().ls_last_error()
+    small = ls.Operator(ls.Config(nLevelsUniform=3, kappa=10.0, TOL_POW=8, Qchoice=0), device=-1)
+    assert ls.lib().ls_matvec_noalloc(small._h, ctypes.c_void_p(16), ctypes.c_void_p(16), None) == ls.LS_E_STATE
+    op.close()
+    small.close()

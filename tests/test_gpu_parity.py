@@ -6,7 +6,7 @@ the reference DAFMM (same seeded inputs, same skeletons).
 import numpy as np
 import pytest
 
-from conftest import CFG_BUMPS, CFG_C1, CFG_HFR, CFG_L3_K10, full_cfg
+from conftest import CFG_BUMPS, CFG_C1, CFG_HFR, CFG_L3_K10, CFG_L5_BUMPS, full_cfg
 
 pytestmark = pytest.mark.gpu
 
@@ -120,4 +120,35 @@ def test_matvec_matches_golden_fixtures(ls, name):
     op = ls.Operator(ls.Config(**{k: v for k, v in d.items()}), device=0)
     assert np.array_equal(op.skeleton_dump(), g["skeleton"])
     assert _rel(op.matvec(g["x"]), g["y"]) <= TOL_PARITY
+    op.close()
+
+
+def test_two_hfr_levels_match_oracle(ls, ora):
+    """Level 5, kappa 40, three seeded bumps, NCA tolerance 1e-10 (the
+    benchmark operator one level down): HFR at levels 3 and 2, so the
+    cone-to-cone M2M (HFR_M2M_ILActiveTrue, G_FMM2DTree.hpp:3624-3710) and
+    the HFR-to-HFR L2L (HFR_L2L_ILActiveTrue, :4021-4121), both folded
+    through Atilde^-1 on the host, run on the GPU. Native FP64 and
+    double-float kernels against the oracle's per-box QR solves, plus the
+    FP32 operator's error bound."""
+    torch = pytest.importorskip("torch")
+    cfg = full_cfg(CFG_L5_BUMPS)
+    op = ls.Operator(cfg, device=0)
+    ref = ora.Oracle(cfg.as_dict())
+    assert op.info["n_levels"] == 5 and op.info["level_LFR"] == 4
+    assert np.array_equal(op.skeleton_dump(), ref.skeleton_dump())
+    for seed in (11, 12):
+        x = _x(op.N, seed)
+        yo = ref.matvec(x)
+        assert _rel(op.matvec(x), yo) <= TOL_PARITY
+        op.set_f64_kernels(ls.LS_F64_DOUBLE_FLOAT)
+        assert _rel(op.matvec(x), yo) <= TOL_PARITY
+        op.set_f64_kernels(ls.LS_F64_NATIVE)
+    op.enable_f32()
+    x = _x(op.N, 13)
+    xt = torch.from_numpy(x).cuda()
+    y32 = torch.empty_like(xt)
+    op.matvec_device(xt.data_ptr(), y32.data_ptr(), 0, precision=ls.LS_PREC_F32)
+    torch.cuda.synchronize()
+    assert 1e-12 < _rel(y32.cpu().numpy(), ref.matvec(x)) <= 5e-5
     op.close()
