@@ -377,6 +377,16 @@ def run_ours(args):
                  "mixed_converged": codem == 0, "speedup_mixed_vs_fp64": t64 / tm if tm > 0 else None,
                  "mixed_rel_err_vs_fp64": err_vs_fp64(xm), "mixed_history": [float(v) for v in histm],
                  "f32_matvec_per_s": 1e3 / ms32, "f32_m2l_ms": m2l32}
+        # The same refinement with the inner Krylov basis and its Gram-Schmidt
+        # in FP32 (the default above keeps them in FP64).
+        op.set_inner_basis(ls.LS_INNER_BASIS_F32)
+        tm32, (xm32, histm32, nmv32, rrm32, codem32) = timed(
+            lambda: op.gmres_mixed(b, max_outer=20, inner_iter=args.max_iter, tol=1e-8))
+        op.set_inner_basis(ls.LS_INNER_BASIS_F64)
+        solve["mixed_inner_basis"] = "fp64"
+        solve["mixed_fp32_basis"] = {"s": tm32, "matvecs": nmv32, "true_residual": rrm32, "converged": codem32 == 0,
+                                     "rel_err_vs_fp64": err_vs_fp64(xm32), "speedup_vs_fp64": t64 / tm32,
+                                     "history": [float(v) for v in histm32]}
         # The same solves at the 9,216-point C1 configuration (GPU side of the
         # CPU solve times in cpu_baseline.solve_s).
         op1 = ls.Operator(c1_config(ls), device=local)
@@ -439,7 +449,7 @@ def run_ours(args):
     fp32_peak = ls.measure_fma_peak(local, "fp32")
     phases = op.time_matvec_phases(warmup=3, iters=max(5, args.steps))
     d_bases = cfg.degreeOfBases
-    n_bases = (d_bases + 1) * (d_bases + 2) // 2
+    n_bases = d_bases * (d_bases + 1) // 2  # Chebyshev T_a(x) T_b(y) with a + b < degreeOfBases
     side = int(round(info["n_leaves"] ** 0.5))
     pairs = (3 * side - 2) ** 2  # (leaf, colleague) pairs of a uniform side x side leaf grid
     # FP64 flops of the factored native near field: c = Q+ x per leaf (real x

@@ -170,11 +170,21 @@ ls_status ls_gmres(ls_op* op, const double* b, int max_iter, double tol, double*
 /* Fixed-m restarted GMRES (GMRES/GMRES.cpp:257-319, RestartedGMRES). */
 ls_status ls_gmres_restarted(ls_op* op, const double* b, int m, int restarts, double* x);
 
-/* Mixed precision: FP64 flexible GMRES whose inner solves use the FP32
- * operator (needs ls_op_enable_f32). Stops on the FP64 true residual. */
+/* Mixed precision: FP64 iterative refinement whose inner GMRES solves use
+ * the FP32 operator (needs ls_op_enable_f32). Stops on the FP64 true
+ * residual. The inner Krylov basis, its Gram-Schmidt and the Givens
+ * rotations are FP64 unless ls_op_set_inner_basis selected FP32. */
 ls_status ls_gmres_mixed(ls_op* op, const double* b, int max_outer, int inner_iter,
                          double tol, double* x, double* history, int* n_matvec,
                          double* rel_residual);
+/* Element type of the inner Krylov basis of ls_gmres_mixed and
+ * ls_fgmres_nn. LS_INNER_BASIS_F64 (default): Arnoldi vectors, classical
+ * Gram-Schmidt and Givens in FP64 around the FP32 operator apply;
+ * LS_INNER_BASIS_F32: the basis and its orthogonalisation in FP32 as well
+ * (half the basis memory and traffic). No counterpart in the reference. */
+#define LS_INNER_BASIS_F64 0
+#define LS_INNER_BASIS_F32 1
+ls_status ls_op_set_inner_basis(ls_op* op, int basis);
 
 /*
  * Many right-hand sides on one operator (e.g. the incident fields of many

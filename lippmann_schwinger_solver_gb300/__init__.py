@@ -37,6 +37,8 @@ LS_PREC_F64 = 0
 LS_PREC_F32 = 1
 LS_F64_NATIVE = 0
 LS_F64_DOUBLE_FLOAT = 1
+LS_INNER_BASIS_F64 = 0
+LS_INNER_BASIS_F32 = 1
 
 # Every symbol declared in include/ls_dafmm.h.
 EXPORTED_SYMBOLS = (
@@ -210,6 +212,7 @@ def lib():
         L.ls_last_error.restype = ctypes.c_char_p
         L.ls_version.restype = ctypes.c_char_p
         L.ls_set_pdl.argtypes = [ctypes.c_int]
+        L.ls_op_set_inner_basis.argtypes = [vp, ctypes.c_int]
         L.ls_time_matvec_phases.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.ls_measure_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, dp]
         L.ls_get_pdl.argtypes = []
@@ -341,6 +344,11 @@ class Operator:
 
     def enable_f32(self):
         _check(lib().ls_op_enable_f32(self._h), "ls_op_enable_f32")
+
+    def set_inner_basis(self, basis):
+        """Inner Krylov basis of the mixed-precision solvers: LS_INNER_BASIS_F64
+        (default: FP64 Gram-Schmidt and Givens) or LS_INNER_BASIS_F32."""
+        _check(lib().ls_op_set_inner_basis(self._h, int(basis)), "ls_op_set_inner_basis")
 
     def set_f64_kernels(self, kernels):
         """LS_F64_NATIVE or LS_F64_DOUBLE_FLOAT behind every FP64 entry point."""

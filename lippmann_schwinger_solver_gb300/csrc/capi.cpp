@@ -228,6 +228,15 @@ ls_status ls_op_set_f64_kernels(ls_op* op, int kernels) {
   return LS_OK;
 }
 
+ls_status ls_op_set_inner_basis(ls_op* op, int basis) {
+  if (!op) return fail(LS_E_INVALID, "ls_op_set_inner_basis: null argument");
+  if (basis != LS_INNER_BASIS_F64 && basis != LS_INNER_BASIS_F32)
+    return fail(LS_E_INVALID, "ls_op_set_inner_basis: unknown basis " + std::to_string(basis));
+  if (!op->on_device) return fail(LS_E_STATE, "ls_op_set_inner_basis: operator was assembled without a device");
+  op->dev.inner_basis = basis;
+  return LS_OK;
+}
+
 ls_status ls_matvec_f32(ls_op* op, const double* x, double* y, void* stream) {
   if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_f32: null argument");
   if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_f32: operator was assembled without a device");

@@ -64,6 +64,9 @@ struct DevOperator {
   // f64_kernels selects what the FP64 entry points run: LS_F64_NATIVE or
   // LS_F64_DOUBLE_FLOAT.
   int f64_kernels = LS_F64_NATIVE;
+  // Element type of the inner Krylov basis of the mixed-precision solvers
+  // (LS_INNER_BASIS_F64: FP64 Gram-Schmidt and Givens over the FP32 operator).
+  int inner_basis = LS_INNER_BASIS_F64;
   bool has_df = false;
   std::vector<DevPhase<float4>> up_df, down_df;
   DevPhase<float4> m2l_df;

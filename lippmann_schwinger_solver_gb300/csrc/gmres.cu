@@ -96,6 +96,11 @@ struct GmresWorkspace {
   double2* res = nullptr;
   float2* res32 = nullptr;
   float2* dx32 = nullptr;
+  // FP64 inner basis over the FP32 operator: the correction, and the FP32
+  // copies of a direction and its preconditioned image.
+  double2* dx64 = nullptr;
+  float2* pv32 = nullptr;
+  float2* pz32 = nullptr;
   // Coefficients: per-block partial sums, CGS passes, |w|^2 (all FP64).
   double2* partial = nullptr;
   double2* h = nullptr;
@@ -106,8 +111,9 @@ struct GmresWorkspace {
   int n = 0, cap = -1;
   void release_small() {
     cudaFree(res); cudaFree(res32); cudaFree(dx32); cudaFree(partial); cudaFree(h); cudaFree(h2); cudaFree(nrm);
-    res = partial = h = h2 = nrm = nullptr;
-    res32 = dx32 = nullptr;
+    cudaFree(dx64); cudaFree(pv32); cudaFree(pz32);
+    res = partial = h = h2 = nrm = dx64 = nullptr;
+    res32 = dx32 = pv32 = pz32 = nullptr;
     if (copied) cudaEventDestroy(copied);
     copied = nullptr;
     if (pinned) cudaFreeHost(pinned);
@@ -128,6 +134,9 @@ struct GmresWorkspace {
     cudaError_t e = cudaMalloc(&res, (size_t)n_ * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&res32, (size_t)n_ * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&dx32, (size_t)n_ * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&dx64, (size_t)n_ * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&pv32, (size_t)n_ * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMalloc(&pz32, (size_t)n_ * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&partial, (size_t)kDotBlocks * (m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&h, (size_t)(m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&h2, (size_t)(m + 2) * sizeof(double2));
@@ -369,6 +378,26 @@ __global__ void add_f32_kernel(double2* __restrict__ a, const float2* __restrict
   }
 }
 
+__global__ void to_f64_kernel(const float2* __restrict__ a, double2* __restrict__ b, int n) {
+  pdl_enter();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float2 v = ld_chain(a + i);
+    b[i] = make_double2((double)v.x, (double)v.y);
+  }
+}
+
+// a += b (FP64)
+__global__ void add_kernel(double2* __restrict__ a, const double2* __restrict__ b, int n) {
+  pdl_enter();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 u = ld_chain(a + i);
+    const double2 v = ld_chain(b + i);
+    u.x += v.x;
+    u.y += v.y;
+    a[i] = u;
+  }
+}
+
 using cdh = std::complex<double>;
 
 int grid_for(int n) { return std::min((n + 255) / 256, 152 * 8); }
@@ -393,21 +422,33 @@ cudaError_t vnorm(const T* w, int n, GmresWorkspace& ws, cudaStream_t s, double&
   return cudaSuccess;
 }
 
-// y = A x with the operator that matches the basis element type: the FP64
-// operator (native or double-float kernels) for double2, the FP32 operator
-// for float2.
-cudaError_t apply(DevOperator& d, const double2* x, double2* y, cudaStream_t s) {
-  return dev_matvec(d, x, y, s, false);
+// y = A x. An FP32 basis always uses the FP32 operator. An FP64 basis uses
+// the FP64 operator (native or double-float kernels), or, with f32_op, the
+// FP32 operator on FP64 vectors (x rounded to FP32 on load, y widened on
+// store): the inner solves of the mixed-precision refinement with their
+// Gram-Schmidt and Givens algebra in FP64.
+cudaError_t apply(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool f32_op) {
+  return f32_op ? dev_matvec_f32(d, x, y, s, false) : dev_matvec(d, x, y, s, false);
 }
-cudaError_t apply(DevOperator& d, const float2* x, float2* y, cudaStream_t s) {
+cudaError_t apply(DevOperator& d, const float2* x, float2* y, cudaStream_t s, bool) {
   return dev_matvec_f32v(d, x, y, s);
 }
 
 Basis<double2>& basis(GmresWorkspace& ws, const double2*) { return ws.b64; }
 Basis<float2>& basis(GmresWorkspace& ws, const float2*) { return ws.b32; }
 
-cudaError_t precondition(Precond32* M, const float2* v, float2* z, cudaStream_t s) { return M->apply(v, z, s); }
-cudaError_t precondition(Precond32*, const double2*, double2*, cudaStream_t) { return cudaErrorNotSupported; }
+// z = M(v): M works on FP32 vectors, so an FP64 direction is rounded to FP32
+// first and the result widened back.
+cudaError_t precondition(Precond32* M, GmresWorkspace&, const float2* v, float2* z, int, cudaStream_t s) {
+  return M->apply(v, z, s);
+}
+cudaError_t precondition(Precond32* M, GmresWorkspace& ws, const double2* v, double2* z, int n, cudaStream_t s) {
+  launch_pdl(to_f32_kernel, grid_for(n), 256, 0, s, v, ws.pv32, n);
+  cudaError_t e = M->apply(ws.pv32, ws.pz32, s);
+  if (e != cudaSuccess) return e;
+  launch_pdl(to_f64_kernel, grid_for(n), 256, 0, s, (const float2*)ws.pz32, z, n);
+  return cudaGetLastError();
+}
 
 // One Arnoldi cycle from x0 (device, may be null for x0 = 0). Writes the
 // updated solution into x. tol < 0 disables the residual stop; breakdown
@@ -417,7 +458,7 @@ cudaError_t precondition(Precond32*, const double2*, double2*, cudaStream_t) { r
 template <class T>
 cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const T* x0, T* x, int m, double tol,
                           double brk, double bnorm, std::vector<double>* hist, int& iters, bool& converged,
-                          Precond32* M = nullptr) {
+                          Precond32* M = nullptr, bool f32_op = false) {
   Basis<T>& B = basis(ws, b);
   cudaStream_t s = d.stream;
   const int n = d.N;
@@ -426,14 +467,14 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
   // w = A v_k, or w = A M(v_k) with z_k kept.
   auto product = [&](int k) -> cudaError_t {
     const T* v = B.V + (size_t)k * n;
-    if (!M) return apply(d, v, B.w, s);
+    if (!M) return apply(d, v, B.w, s, f32_op);
     T* z = B.Z + (size_t)k * n;
-    cudaError_t pe = precondition(M, v, z, s);
-    return pe != cudaSuccess ? pe : apply(d, z, B.w, s);
+    cudaError_t pe = precondition(M, ws, v, z, n, s);
+    return pe != cudaSuccess ? pe : apply(d, z, B.w, s, f32_op);
   };
   // r = b - A x0
   if (x0) {
-    if ((e = apply(d, x0, B.w, s)) != cudaSuccess) return e;
+    if ((e = apply(d, x0, B.w, s, f32_op)) != cudaSuccess) return e;
     launch_pdl(sub_kernel<T>, grid_for(n), 256, 0, s, b, B.w, B.r, n);
   } else {
     cudaMemcpyAsync(B.r, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, s);
@@ -577,19 +618,25 @@ cudaError_t dev_gmres_restarted(DevOperator& d, const double2* b, double2* x, in
 }
 
 // Iterative refinement in FP64 around GMRES on the FP32 operator:
-//   r = b - A64 x ; solve A32 d = r in FP32 to a loose tolerance ; x += d
-// until |b - A64 x| / |b| <= tol. The residual is always the FP64 one; the
-// inner Arnoldi basis and its orthogonalisation are FP32. With a right
-// preconditioner M the inner solves are flexible GMRES on A32 M, and with
-// guess the iteration starts from x0 = guess(b) instead of 0.
+//   r = b - A64 x ; solve A32 d = r to a loose tolerance ; x += d
+// until |b - A64 x| / |b| <= tol. The residual is always the FP64 one. The
+// inner Arnoldi basis, its Gram-Schmidt and the Givens algebra are FP64 by
+// default (d.inner_basis = LS_INNER_BASIS_F64): only the operator apply is
+// FP32, with its vectors rounded on load and widened on store. With
+// LS_INNER_BASIS_F32 the basis and its orthogonalisation are FP32 too
+// (half the basis traffic). With a right preconditioner M the inner solves
+// are flexible GMRES on A32 M, and with guess the iteration starts from
+// x0 = guess(b) instead of 0.
 cudaError_t dev_gmres_mixed_flex(DevOperator& d, const double2* b, double2* x, Precond32* M, Precond32* guess,
                                  int max_outer, int inner, double tol, std::vector<double>& hist, FlexReport& rep,
                                  double& relres) {
   const int n = d.N;
+  const bool f64_basis = d.inner_basis == LS_INNER_BASIS_F64;
   GmresWorkspace& ws = workspace(d);
   cudaError_t e = ws.ensure(n, inner);
-  if (e == cudaSuccess) e = ws.b32.ensure(n, inner);
-  if (e == cudaSuccess && ws.b64.n != n) e = ws.b64.ensure(n, 1);
+  if (e == cudaSuccess && !f64_basis) e = ws.b32.ensure(n, inner);
+  if (e == cudaSuccess && (ws.b64.n != n || (f64_basis && ws.b64.cap < inner)))
+    e = ws.b64.ensure(n, f64_basis ? inner : 1);
   if (e != cudaSuccess) return e;
   double2* r = ws.res;
   double bn = 0.0;
@@ -634,13 +681,20 @@ cudaError_t dev_gmres_mixed_flex(DevOperator& d, const double2* b, double2* x, P
     const double inner_tol = std::max(tol / std::max(relres, 1e-300), 1e-6);
     Precond32* Mo = (rep.fell_back || inner_tol >= kFlexPlainTol) ? nullptr : M;
     const int m_inner = Mo ? std::min(inner, kFlexInner) : inner;
-    launch_pdl(to_f32_kernel, grid_for(n), 256, 0, d.stream, r, ws.res32, n);
-    if ((e = arnoldi_cycle<float2>(d, ws, ws.res32, nullptr, ws.dx32, m_inner, inner_tol, 1e-300,
-                                   std::max(relres * bn, 1e-300), nullptr, it, conv, Mo)) != cudaSuccess)
-      return e;
+    if (f64_basis) {
+      if ((e = arnoldi_cycle<double2>(d, ws, r, nullptr, ws.dx64, m_inner, inner_tol, 1e-300,
+                                      std::max(relres * bn, 1e-300), nullptr, it, conv, Mo, true)) != cudaSuccess)
+        return e;
+      launch_pdl(add_kernel, grid_for(n), 256, 0, d.stream, x, (const double2*)ws.dx64, n);
+    } else {
+      launch_pdl(to_f32_kernel, grid_for(n), 256, 0, d.stream, r, ws.res32, n);
+      if ((e = arnoldi_cycle<float2>(d, ws, ws.res32, nullptr, ws.dx32, m_inner, inner_tol, 1e-300,
+                                     std::max(relres * bn, 1e-300), nullptr, it, conv, Mo)) != cudaSuccess)
+        return e;
+      launch_pdl(add_f32_kernel, grid_for(n), 256, 0, d.stream, x, ws.dx32, n);
+    }
     rep.n_matvec += it;
     if (Mo) rep.n_precond += it;
-    launch_pdl(add_f32_kernel, grid_for(n), 256, 0, d.stream, x, ws.dx32, n);
     if ((e = dev_matvec(d, x, ws.b64.w, d.stream, false)) != cudaSuccess) return e;
     ++rep.n_matvec;
     launch_pdl(sub_kernel<double2>, grid_for(n), 256, 0, d.stream, b, ws.b64.w, r, n);
