@@ -420,6 +420,17 @@ def run_ours(args):
         op.enable_f32()
         thetas = 2 * np.pi * np.arange(args.angles) / args.angles
         B = op.rhs_angles(thetas)
+        # FP32 block applies with resident inputs: 64 right-hand sides on the
+        # tensor cores against 8 on the CUDA-core block kernels.
+        ms_tc = op.time_block_apply(64, warmup=3, iters=10)
+        ms_cc = op.time_block_apply(8, warmup=3, iters=10)
+        op.set_batch_width(8)
+        op.gmres_mixed_batched(B[:, :8], max_outer=20, inner_iter=100, tol=1e-8)  # warm-up: workspace
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Xb8, nmvb8, rrb8, codeb8 = op.gmres_mixed_batched(B, max_outer=20, inner_iter=100, tol=1e-8)
+        tb8 = time.perf_counter() - t0
+        op.set_batch_width(64)
         op.gmres_mixed_batched(B[:, :8], max_outer=20, inner_iter=100, tol=1e-8)  # warm-up: workspace
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -435,7 +446,14 @@ def run_ours(args):
                  "batched_s": tb, "batched_per_rhs_ms": tb / B.shape[1] * 1e3, "batched_block_applies_and_fp64_products": nmvb,
                  "batched_max_true_residual": float(np.max(rrb)), "batched_converged": codeb == 0,
                  "sequential_mixed_s": ts, "sequential_max_true_residual": float(np.max(rr_seq)),
-                 "speedup_batched_vs_sequential": ts / tb}
+                 "speedup_batched_vs_sequential": ts / tb, "block_width": 64,
+                 "block_apply": {"tensor_core_64_ms": ms_tc, "tensor_core_per_rhs_us": ms_tc / 64 * 1e3,
+                                 "cuda_core_8_ms": ms_cc, "cuda_core_per_rhs_us": ms_cc / 8 * 1e3,
+                                 "speedup_per_rhs": (ms_cc / 8) / (ms_tc / 64)},
+                 "width8": {"s": tb8, "block_applies_and_fp64_products": nmvb8,
+                            "max_true_residual": float(np.max(rrb8)), "converged": codeb8 == 0,
+                            "max_rel_diff_vs_width64": float(max(np.linalg.norm(Xb[:, j] - Xb8[:, j]) /
+                                                                 np.linalg.norm(Xb8[:, j]) for j in range(B.shape[1])))}}
     peak, peak_kind = load_peaks()
     achieved = info["m2l_bytes"] / (ms_m2l * 1e-3) / 1e9
     traffic = traffic_per_launch(args.f64_kernels)

@@ -201,6 +201,24 @@ ls_status ls_op_set_inner_basis(ls_op* op, int basis);
  */
 ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_outer, int inner_iter, double tol,
                                  double* X, int* n_matvec, double* rel_residuals);
+/* Right-hand sides per block of ls_gmres_mixed_batched: 64 (the default)
+ * carries each block through the FP32 operator on the tensor cores
+ * (tcgen05, TF32 inputs split into three products for FP32 accuracy, FP32
+ * accumulation), whose tensor-core form is built on the device on first
+ * use (about twice the FP32 blocks' memory); 8 uses the CUDA-core block
+ * kernels. A tensor-core pipeline wait that gives up returns LS_E_TIMEOUT.
+ * No counterpart in the reference. */
+ls_status ls_op_set_batch_width(ls_op* op, int width);
+/* Y = A32 X for nrhs columns of N complex values (host arrays, column j at
+ * 2 * N * j doubles), 64 columns per pass on the tensor cores: the block
+ * apply of ls_gmres_mixed_batched with width 64. Needs ls_op_enable_f32.
+ * No counterpart in the reference. */
+ls_status ls_matvec_f32_many(ls_op* op, int nrhs, const double* X, double* Y);
+/* Mean ms of one FP32 block apply of `width` resident right-hand sides (8:
+ * CUDA-core block kernels, 64: tensor cores), CUDA events on the
+ * operator's stream after `warmup` untimed applies. No counterpart in the
+ * reference. */
+ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float* ms);
 /* Times `iters` device matvecs (inputs resident) with CUDA events on the
  * operator's stream after `warmup` untimed ones; writes the mean ms per
  * matvec and the mean ms of the dominant kernel (M2L). precision: LS_PREC_*. */

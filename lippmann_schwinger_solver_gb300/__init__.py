@@ -47,6 +47,7 @@ EXPORTED_SYMBOLS = (
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
     "ls_write_result", "ls_set_pdl", "ls_get_pdl", "ls_time_matvec_phases", "ls_measure_fma_peak", "ls_op_set_inner_basis",
+    "ls_op_set_batch_width", "ls_matvec_f32_many", "ls_time_block_apply",
 )
 # Every symbol declared in include/ls_fno.h (learned preconditioner).
 FNO_SYMBOLS = (
@@ -213,6 +214,9 @@ def lib():
         L.ls_version.restype = ctypes.c_char_p
         L.ls_set_pdl.argtypes = [ctypes.c_int]
         L.ls_op_set_inner_basis.argtypes = [vp, ctypes.c_int]
+        L.ls_op_set_batch_width.argtypes = [vp, ctypes.c_int]
+        L.ls_matvec_f32_many.argtypes = [vp, ctypes.c_int, dp, dp]
+        L.ls_time_block_apply.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.ls_time_matvec_phases.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.ls_measure_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, dp]
         L.ls_get_pdl.argtypes = []
@@ -344,6 +348,29 @@ class Operator:
 
     def enable_f32(self):
         _check(lib().ls_op_enable_f32(self._h), "ls_op_enable_f32")
+
+    def set_batch_width(self, width):
+        """Right-hand sides per block of gmres_mixed_batched: 64 (tensor-core
+        block apply, the default) or 8 (CUDA-core block kernels)."""
+        _check(lib().ls_op_set_batch_width(self._h, int(width)), "ls_op_set_batch_width")
+
+    def matvec_f32_many(self, X):
+        """Y = A32 X for the columns of X (N x nrhs), 64 per pass on the
+        tensor cores (ls_matvec_f32_many)."""
+        X = np.asfortranarray(X, dtype=np.complex128)
+        if X.ndim != 2 or X.shape[0] != self.N:
+            raise ValueError(f"X must have shape ({self.N}, nrhs)")
+        Y = np.empty_like(X, order="F")
+        _check(lib().ls_matvec_f32_many(self._h, X.shape[1], _dp(X), _dp(Y)), "ls_matvec_f32_many")
+        return Y
+
+    def time_block_apply(self, width=64, warmup=3, iters=10):
+        """Mean ms of one FP32 block apply of `width` resident right-hand sides
+        (8: CUDA cores, 64: tensor cores)."""
+        ms = ctypes.c_float()
+        _check(lib().ls_time_block_apply(self._h, int(width), int(warmup), int(iters), ctypes.byref(ms)),
+               "ls_time_block_apply")
+        return ms.value
 
     def set_inner_basis(self, basis):
         """Inner Krylov basis of the mixed-precision solvers: LS_INNER_BASIS_F64

@@ -1333,7 +1333,13 @@ static void finalize(GemvPhase& ph, const char* kind) {
   std::vector<T> tl;
   long long total = 0, total_idx = 0;
   int total_rows = 0;
+  ph.blk_tile0.clear();
+  ph.blk_rows.clear();
+  ph.blk_K.clear();
   for (const Block& b : blocks) {
+    ph.blk_tile0.push_back((int)tl.size());
+    ph.blk_rows.push_back(b.rows);
+    ph.blk_K.push_back(b.K);
     const int r_min = std::min(kTileLanes, pow2_ceil((128 + b.K - 1) / b.K));
     const int rcap = std::max(r_max, r_min);
     for (int done = 0; done < b.rows;) {
@@ -1351,6 +1357,7 @@ static void finalize(GemvPhase& ph, const char* kind) {
       done += rows;
     }
   }
+  ph.blk_tile0.push_back((int)tl.size());
   ph.A.assign((size_t)total, cd(0.0, 0.0));
   ph.idx.assign((size_t)total_idx, 0);
   ph.out.assign(ph.rows.size(), 0);

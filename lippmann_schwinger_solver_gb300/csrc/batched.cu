@@ -14,6 +14,11 @@
 // Hessenberg and Givens rotations, its own stopping test), all of them
 // sharing each operator apply and each orthogonalisation launch; the
 // residuals are formed with the FP64 operator one column at a time.
+//
+// Two block widths share this solver (template parameter NR): kBatchRhs (8)
+// right-hand sides with the CUDA-core block apply below, and kTcRhs (64)
+// with the tensor-core block apply of batched_tc.cu, where 64 columns make
+// every operator block a dense contraction.
 
 #include <cuda_runtime.h>
 
@@ -28,16 +33,17 @@
 namespace lsg {
 
 namespace {
-constexpr int NR = kBatchRhs;
+constexpr int NR8 = kBatchRhs;  // width of the CUDA-core block kernels
 constexpr int kBDotThreads = 128;
 constexpr int kBDotBlocks = 304;
 }  // namespace
 
+template <int NR>
 struct BatchWorkspace {
   // FP32 operator work vectors of one block.
-  float2* S = nullptr;   // charges_len x NR
+  float2* S = nullptr;   // (charges_len + 1) x NR; the last row stays zero
   float2* P = nullptr;   // pots_len x NR
-  float2* Z = nullptr;   // near field, pass 1: n_leaves x 9 x rank x NR
+  float2* Z = nullptr;   // near field, pass 1: n_leaves x 9 x rank x NR (CUDA-core apply only)
   // Block Arnoldi: V [step][point][rhs], w, right-hand side, correction.
   float2* V = nullptr;
   float2* w = nullptr;
@@ -54,6 +60,7 @@ struct BatchWorkspace {
   double2* res = nullptr;      // N x NR
   double2* tmp = nullptr;      // N
   int n = 0, cap = -1;
+  long long mem = 0;           // device bytes held
   bool vec_ready = false;
   void release() {
     cudaFree(S); cudaFree(P); cudaFree(Z); cudaFree(V); cudaFree(w); cudaFree(rhs); cudaFree(dx);
@@ -70,9 +77,10 @@ struct BatchWorkspace {
   }
   cudaError_t ensure_vectors(const DevOperator& d) {
     if (vec_ready) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&S, (size_t)d.charges_len * NR * sizeof(float2));
+    cudaError_t e = cudaMalloc(&S, (size_t)(d.charges_len + 1) * NR * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemset(S, 0, (size_t)(d.charges_len + 1) * NR * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&P, (size_t)d.pots_len * NR * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMalloc(&Z, (size_t)d.n_leaves * 9 * d.rank * NR * sizeof(float2));
+    if (e == cudaSuccess && NR == NR8) e = cudaMalloc(&Z, (size_t)d.n_leaves * 9 * d.rank * NR * sizeof(float2));
     if (e != cudaSuccess) return e;
     vec_ready = true;
     return cudaSuccess;
@@ -109,9 +117,14 @@ struct BatchWorkspace {
   }
 };
 
-static BatchWorkspace& batch_ws(DevOperator& d) {
-  if (!d.bws) d.bws = new BatchWorkspace();
+template <int NR> BatchWorkspace<NR>& batch_ws(DevOperator& d);
+template <> BatchWorkspace<kBatchRhs>& batch_ws<kBatchRhs>(DevOperator& d) {
+  if (!d.bws) d.bws = new BatchWorkspace<kBatchRhs>();
   return *d.bws;
+}
+template <> BatchWorkspace<kTcRhs>& batch_ws<kTcRhs>(DevOperator& d) {
+  if (!d.bws_tc) d.bws_tc = new BatchWorkspace<kTcRhs>();
+  return *d.bws_tc;
 }
 
 void dev_free_batch(DevOperator& d) {
@@ -119,6 +132,11 @@ void dev_free_batch(DevOperator& d) {
     d.bws->release();
     delete d.bws;
     d.bws = nullptr;
+  }
+  if (d.bws_tc) {
+    d.bws_tc->release();
+    delete d.bws_tc;
+    d.bws_tc = nullptr;
   }
 }
 
@@ -142,7 +160,7 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
                                                             const float2* __restrict__ src, float2* __restrict__ dst,
                                                             int accumulate) {
   pdl_enter();
-  constexpr int NV = NR / 2;  // float4 per gathered point
+  constexpr int NV = NR8 / 2;  // float4 per gathered point
   const int lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   const float4* __restrict__ src4 = reinterpret_cast<const float4*>(src);
@@ -152,9 +170,9 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
     const int S = 1 << t.log2s;
     const float2* __restrict__ a = A + t.a_off + lane;
     const int* __restrict__ ix = idx + t.i_off + (lane >> (5 - t.log2s));
-    float sr[NR], si[NR];
+    float sr[NR8], si[NR8];
 #pragma unroll
-    for (int j = 0; j < NR; ++j) sr[j] = si[j] = 0.f;
+    for (int j = 0; j < NR8; ++j) sr[j] = si[j] = 0.f;
     int q = 0;
     for (; q + 2 <= ql; q += 2) {
       const int i0 = ix[S * q], i1 = ix[S * (q + 1)];
@@ -184,7 +202,7 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
     }
     for (int o = 16; o >= (32 >> t.log2s); o >>= 1) {
 #pragma unroll
-      for (int j = 0; j < NR; ++j) {
+      for (int j = 0; j < NR8; ++j) {
         sr[j] += __shfl_xor_sync(0xffffffffu, sr[j], o);
         si[j] += __shfl_xor_sync(0xffffffffu, si[j], o);
       }
@@ -209,8 +227,8 @@ __global__ void __launch_bounds__(256, 2) gemv_block_kernel(const GemvTile* __re
 
 // Near field for a block, pass 1 (as near_gemm32_kernel, matvec.cu):
 // Z[s][q][row][j] = B_q(row, :) x_s[:, j]. A thread block takes two
-// leaves (their NR columns staged in shared memory); thread (q, row) keeps
-// 2 x NR sums, so every block entry it loads serves 16 products.
+// leaves (their NR8 columns staged in shared memory); thread (q, row) keeps
+// 2 x NR8 sums, so every block entry it loads serves 16 products.
 constexpr int kBatchNearSources = 2;
 
 __global__ void __launch_bounds__(352, 2) near_gemm_block_kernel(int n_leaves, int rank,
@@ -219,7 +237,7 @@ __global__ void __launch_bounds__(352, 2) near_gemm_block_kernel(int n_leaves, i
                                                                  float2* __restrict__ Z) {
   pdl_enter();
   constexpr int NS = kBatchNearSources;
-  constexpr int NV = NR / 2;
+  constexpr int NV = NR8 / 2;
   extern __shared__ float4 sx4[];  // [s][k][p]
   const int s0 = blockIdx.x * NS;
   const int tot = NS * rank * NV;
@@ -231,11 +249,11 @@ __global__ void __launch_bounds__(352, 2) near_gemm_block_kernel(int n_leaves, i
   __syncthreads();
   for (int qr = threadIdx.x; qr < 9 * rank; qr += blockDim.x) {
     const int q = qr / rank, row = qr - q * rank;
-    float ar[NS][NR], ai[NS][NR];
+    float ar[NS][NR8], ai[NS][NR8];
 #pragma unroll
     for (int s = 0; s < NS; ++s)
 #pragma unroll
-      for (int j = 0; j < NR; ++j) ar[s][j] = ai[s][j] = 0.f;
+      for (int j = 0; j < NR8; ++j) ar[s][j] = ai[s][j] = 0.f;
     const float2* __restrict__ b = BT + (size_t)q * rank * rank + row;
     for (int k = 0; k < rank; ++k) {
       const float2 a = b[(size_t)k * rank];
@@ -267,8 +285,8 @@ __global__ void __launch_bounds__(256) near_gather_block_kernel(int n_out, int r
                                                                 float2* __restrict__ y, int find_phi) {
   pdl_enter();
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (long long)n_out * NR) return;
-  const int t = (int)(e / NR), j = (int)(e - (long long)t * NR);
+  if (e >= (long long)n_out * NR8) return;
+  const int t = (int)(e / NR8), j = (int)(e - (long long)t * NR8);
   const int leaf = t / rank, row = t - leaf * rank;
   float ar = 0.f, ai = 0.f;
   const size_t per = (size_t)9 * rank;
@@ -276,7 +294,7 @@ __global__ void __launch_bounds__(256) near_gather_block_kernel(int n_out, int r
   for (int q = 0; q < 9; ++q) {
     const int nbx = coll[leaf * 9 + q];
     if (nbx < 0) continue;
-    const float2 z = ld_chain(Z + ((size_t)nbx * per + (size_t)q * rank + row) * NR + j);
+    const float2 z = ld_chain(Z + ((size_t)nbx * per + (size_t)q * rank + row) * NR8 + j);
     ar += z.x;
     ai += z.y;
   }
@@ -291,54 +309,37 @@ __global__ void __launch_bounds__(256) near_gather_block_kernel(int n_out, int r
 }
 
 // partial[((col * NR) + j) * gridDim.x + block] = sum_{rows of block}
-// conj(V[col][row][j]) * w[row][j] for the NR right-hand sides; reduced in
-// a fixed order (deterministic).
+// conj(V[col][row][j]) * w[row][j] for the NR right-hand sides. Thread t
+// owns right-hand side t % NR and every (128 / NR)-th row of the block's
+// chunk, so a warp reads 256 contiguous bytes per step; the row groups are
+// summed in shared memory in a fixed order (deterministic).
+template <int NR>
 __global__ void __launch_bounds__(kBDotThreads) multidot_block_kernel(const float2* __restrict__ V, int n,
                                                                       const float2* __restrict__ w,
                                                                       double2* __restrict__ partial) {
   pdl_enter();
-  constexpr int NV = NR / 2;
-  __shared__ float red[kBDotThreads / 32][2 * NR];
+  constexpr int G = kBDotThreads / NR;
+  __shared__ float2 red[G][NR];
   const int chunk = (n + gridDim.x - 1) / gridDim.x;
   const int r0 = blockIdx.x * chunk;
   const int len = max(0, min(chunk, n - r0));
   const int col = blockIdx.y;
-  const float4* __restrict__ v4 = reinterpret_cast<const float4*>(V + (size_t)col * n * NR) + (size_t)r0 * NV;
-  const float4* __restrict__ w4 = reinterpret_cast<const float4*>(w) + (size_t)r0 * NV;
-  float ar[NR], ai[NR];
-#pragma unroll
-  for (int j = 0; j < NR; ++j) ar[j] = ai[j] = 0.f;
-  for (int i = threadIdx.x; i < len; i += blockDim.x) {
-#pragma unroll
-    for (int p = 0; p < NV; ++p) {
-      const float4 a = ld_chain(v4 + (size_t)i * NV + p), b = ld_chain(w4 + (size_t)i * NV + p);
-      ar[2 * p] = fmaf(a.x, b.x, fmaf(a.y, b.y, ar[2 * p]));
-      ai[2 * p] = fmaf(a.x, b.y, fmaf(-a.y, b.x, ai[2 * p]));
-      ar[2 * p + 1] = fmaf(a.z, b.z, fmaf(a.w, b.w, ar[2 * p + 1]));
-      ai[2 * p + 1] = fmaf(a.z, b.w, fmaf(-a.w, b.z, ai[2 * p + 1]));
-    }
+  const int j = threadIdx.x % NR, grp = threadIdx.x / NR;
+  const float2* __restrict__ v = V + ((size_t)col * n + r0) * NR + j;
+  const float2* __restrict__ wv = w + (size_t)r0 * NR + j;
+  float ar = 0.f, ai = 0.f;
+  for (int i = grp; i < len; i += G) {
+    const float2 a = ld_chain(v + (size_t)i * NR), b = ld_chain(wv + (size_t)i * NR);
+    ar = fmaf(a.x, b.x, fmaf(a.y, b.y, ar));
+    ai = fmaf(a.x, b.y, fmaf(-a.y, b.x, ai));
   }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < NR; ++j) {
-    for (int o = 16; o > 0; o >>= 1) {
-      ar[j] += __shfl_xor_sync(0xffffffffu, ar[j], o);
-      ai[j] += __shfl_xor_sync(0xffffffffu, ai[j], o);
-    }
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int j = 0; j < NR; ++j) {
-      red[wid][2 * j] = ar[j];
-      red[wid][2 * j + 1] = ai[j];
-    }
-  }
+  red[grp][j] = make_float2(ar, ai);
   __syncthreads();
   if (threadIdx.x < NR) {
     double a = 0.0, b = 0.0;
-    for (int k = 0; k < kBDotThreads / 32; ++k) {
-      a += (double)red[k][2 * threadIdx.x];
-      b += (double)red[k][2 * threadIdx.x + 1];
+    for (int k = 0; k < G; ++k) {
+      a += (double)red[k][threadIdx.x].x;
+      b += (double)red[k][threadIdx.x].y;
     }
     partial[((size_t)col * NR + threadIdx.x) * gridDim.x + blockIdx.x] = make_double2(a, b);
   }
@@ -365,6 +366,7 @@ __global__ void reduce_block_partials_kernel(const double2* __restrict__ partial
 }
 
 // w[i][j] += sign * sum_c V[c][i][j] * h[c][j]
+template <int NR>
 __global__ void __launch_bounds__(256, 4) multi_axpy_block_kernel(float2* __restrict__ w, const float2* __restrict__ V,
                                                                int n, int ncols, const double2* __restrict__ h,
                                                                float sign) {
@@ -399,6 +401,7 @@ __global__ void __launch_bounds__(256, 4) multi_axpy_block_kernel(float2* __rest
 
 // b[i][j] = a[i][j] / sqrt(nrm[j]), zero for a zero norm. The NR factors
 // are formed once per thread block (FP64 divides are slow on GB300).
+template <int NR>
 __global__ void scale_block_kernel(const float2* __restrict__ a, float2* __restrict__ b,
                                    const double2* __restrict__ nrm, int n) {
   pdl_enter();
@@ -418,13 +421,15 @@ __global__ void scale_block_kernel(const float2* __restrict__ a, float2* __restr
 }
 
 // r32[i][j] = (float) r[j * n + i] for active columns, 0 otherwise.
-__global__ void pack_block_kernel(const double2* __restrict__ r, float2* __restrict__ r32, int n, unsigned active) {
+template <int NR>
+__global__ void pack_block_kernel(const double2* __restrict__ r, float2* __restrict__ r32, int n,
+                                  unsigned long long active) {
   pdl_enter();
   const long long tot = (long long)n * NR;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(e / NR), j = (int)(e % NR);
-    if ((active >> j) & 1u) {
+    if ((active >> j) & 1ull) {
       const double2 v = ld_chain(r + (size_t)j * n + i);
       r32[e] = make_float2((float)v.x, (float)v.y);
     } else {
@@ -434,14 +439,15 @@ __global__ void pack_block_kernel(const double2* __restrict__ r, float2* __restr
 }
 
 // x[j * n + i] += dx[i][j] for active columns.
+template <int NR>
 __global__ void unpack_add_block_kernel(double2* __restrict__ x, const float2* __restrict__ dx, int n, int ncols,
-                                        unsigned active) {
+                                        unsigned long long active) {
   pdl_enter();
   const long long tot = (long long)n * ncols;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < tot;
        e += (long long)gridDim.x * blockDim.x) {
     const int j = (int)(e / n), i = (int)(e % n);
-    if (!((active >> j) & 1u)) continue;
+    if (!((active >> j) & 1ull)) continue;
     const float2 d = ld_chain(dx + (size_t)i * NR + j);
     double2 u = ld_chain(x + e);
     u.x += (double)d.x;
@@ -486,6 +492,12 @@ __global__ void __launch_bounds__(kBDotThreads) colnorm_kernel(const double2* __
 
 int grid_n(long long n) { return (int)std::min<long long>((n + 255) / 256, 152 * 8); }
 
+__global__ void zero_f2_block_kernel(float2* __restrict__ p, long long n) {
+  pdl_enter();
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = make_float2(0.f, 0.f);
+}
+
 int sms_b(int dev) {
   static int v = 0;
   if (v == 0) {
@@ -505,7 +517,8 @@ void launch_block(const DevPhase<float2>& ph, const float2* src, float2* dst, cu
 }
 
 // |columns|^2 of an n x ncols FP64 array into out (host), ncols <= NR.
-cudaError_t colnorms(const double2* A, int n, int ncols, BatchWorkspace& B, cudaStream_t s, double* out) {
+template <int NR>
+cudaError_t colnorms(const double2* A, int n, int ncols, BatchWorkspace<NR>& B, cudaStream_t s, double* out) {
   launch_pdl(colnorm_kernel, dim3(kBDotBlocks, ncols), kBDotThreads, 0, s, A, n, B.partial);
   launch_pdl(reduce_block_partials_kernel, (ncols * 32 + 255) / 256, 256, 0, s, B.partial, kBDotBlocks, ncols, B.nrm);
   std::vector<double2> v(ncols);
@@ -516,9 +529,10 @@ cudaError_t colnorms(const double2* A, int n, int ncols, BatchWorkspace& B, cuda
   return cudaSuccess;
 }
 
-void block_multidot(const float2* V, int n, int ncols, const float2* w, BatchWorkspace& B, double2* h,
+template <int NR>
+void block_multidot(const float2* V, int n, int ncols, const float2* w, BatchWorkspace<NR>& B, double2* h,
                     cudaStream_t s) {
-  launch_pdl(multidot_block_kernel, dim3(kBDotBlocks, ncols), kBDotThreads, 0, s, V, n, w, B.partial);
+  launch_pdl(multidot_block_kernel<NR>, dim3(kBDotBlocks, ncols), kBDotThreads, 0, s, V, n, w, B.partial);
   launch_pdl(reduce_block_partials_kernel, (ncols * NR * 32 + 255) / 256, 256, 0, s, B.partial, kBDotBlocks, ncols * NR, h);
 }
 
@@ -533,10 +547,23 @@ struct RhsState {
   bool done = false;
 };
 
+// y = A32 x for one block of NR right-hand sides.
+template <int NR> cudaError_t block_apply(DevOperator& d, BatchWorkspace<NR>& B, const float2* x, float2* y,
+                                          cudaStream_t s);
+template <> cudaError_t block_apply<kBatchRhs>(DevOperator& d, BatchWorkspace<kBatchRhs>&, const float2* x, float2* y,
+                                               cudaStream_t s) {
+  return dev_matvec_f32_batch(d, x, y, s);
+}
+template <> cudaError_t block_apply<kTcRhs>(DevOperator& d, BatchWorkspace<kTcRhs>& B, const float2* x, float2* y,
+                                            cudaStream_t s) {
+  return dev_matvec_f32_wide(d, x, y, B.S, B.P, s);
+}
+
 // Block Arnoldi (FP32 basis, one GMRES per column sharing the launches):
 // solves A32 x_j = rhs_j for the columns with rs[j].done == false, x = 0
 // start. Returns the block operator applies made.
-cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<RhsState>& rs, int& applies) {
+template <int NR>
+cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace<NR>& B, int m, std::vector<RhsState>& rs, int& applies) {
   cudaStream_t s = d.stream;
   const int n = d.N;
   const size_t blk = (size_t)n * NR;
@@ -559,8 +586,8 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<
   }
   cudaMemsetAsync(B.dx, 0, blk * sizeof(float2), s);
   if (!any) return cudaStreamSynchronize(s);
-  launch_pdl(scale_block_kernel, grid_n((long long)blk), 256, 0, s, B.rhs, B.V, B.nrm, n);
-  if ((e = dev_matvec_f32_batch(d, B.V, B.w, s)) != cudaSuccess) return e;
+  launch_pdl(scale_block_kernel<NR>, grid_n((long long)blk), 256, 0, s, B.rhs, B.V, B.nrm, n);
+  if ((e = block_apply<NR>(d, B, B.V, B.w, s)) != cudaSuccess) return e;
   ++applies;
   double2* hp = B.pinned;
   double2* hp2 = B.pinned + (size_t)(m + 2) * NR;
@@ -569,17 +596,17 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<
   for (int k = 0; k < m; ++k) {
     const float2* Vk = B.V;
     block_multidot(Vk, n, k + 1, B.w, B, B.h, s);
-    launch_pdl(multi_axpy_block_kernel, grid_n((long long)blk), 256, 0, s, B.w, B.V, n, k + 1, B.h, -1.f);
+    launch_pdl(multi_axpy_block_kernel<NR>, grid_n((long long)blk), 256, 0, s, B.w, B.V, n, k + 1, B.h, -1.f);
     block_multidot(Vk, n, k + 1, B.w, B, B.h2, s);
-    launch_pdl(multi_axpy_block_kernel, grid_n((long long)blk), 256, 0, s, B.w, B.V, n, k + 1, B.h2, -1.f);
+    launch_pdl(multi_axpy_block_kernel<NR>, grid_n((long long)blk), 256, 0, s, B.w, B.V, n, k + 1, B.h2, -1.f);
     block_multidot(B.w, n, 1, B.w, B, B.nrm, s);
-    launch_pdl(scale_block_kernel, grid_n((long long)blk), 256, 0, s, B.w, B.V + (size_t)(k + 1) * blk, B.nrm, n);
+    launch_pdl(scale_block_kernel<NR>, grid_n((long long)blk), 256, 0, s, B.w, B.V + (size_t)(k + 1) * blk, B.nrm, n);
     cudaMemcpyAsync(hp, B.h, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hp2, B.h2, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(np, B.nrm, (size_t)NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
     if ((e = cudaEventRecord(B.copied, s)) != cudaSuccess) return e;
     if (k + 1 < m) {
-      if ((e = dev_matvec_f32_batch(d, B.V + (size_t)(k + 1) * blk, B.w, s)) != cudaSuccess) return e;
+      if ((e = block_apply<NR>(d, B, B.V + (size_t)(k + 1) * blk, B.w, s)) != cudaSuccess) return e;
       ++applies;
     }
     if ((e = cudaEventSynchronize(B.copied)) != cudaSuccess) return e;
@@ -630,7 +657,7 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<
   }
   if (kmax > 0) {
     cudaMemcpyAsync(B.h, y.data(), y.size() * sizeof(double2), cudaMemcpyHostToDevice, s);
-    launch_pdl(multi_axpy_block_kernel, grid_n((long long)blk), 256, 0, s, B.dx, B.V, n, kmax, B.h, 1.f);
+    launch_pdl(multi_axpy_block_kernel<NR>, grid_n((long long)blk), 256, 0, s, B.dx, B.V, n, kmax, B.h, 1.f);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   return cudaStreamSynchronize(s);
@@ -641,29 +668,40 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace& B, int m, std::vector<
 cudaError_t dev_matvec_f32_batch(DevOperator& d, const float2* x, float2* y, cudaStream_t s) {
   if (!d.has_f32) return cudaErrorInvalidValue;
   if (!s) s = d.stream;
-  BatchWorkspace& B = batch_ws(d);
+  BatchWorkspace<kBatchRhs>& B = batch_ws<kBatchRhs>(d);
   cudaError_t e = B.ensure_vectors(d);
   if (e != cudaSuccess) return e;
-  cudaMemcpyAsync(B.S, x, (size_t)d.N * NR * sizeof(float2), cudaMemcpyDeviceToDevice, s);
-  cudaMemsetAsync(B.P, 0, (size_t)d.pots_len * NR * sizeof(float2), s);
+  cudaMemcpyAsync(B.S, x, (size_t)d.N * NR8 * sizeof(float2), cudaMemcpyDeviceToDevice, s);
+  cudaMemsetAsync(B.P, 0, (size_t)d.pots_len * NR8 * sizeof(float2), s);
   for (auto& ph : d.up32) launch_block<0>(ph, (const float2*)B.S, B.S, s, d.device);
   launch_block<1>(d.m2l32, (const float2*)B.S, B.P, s, d.device);
   for (auto& ph : d.down32) launch_block<2>(ph, (const float2*)B.P, B.P, s, d.device);
   const int NS = kBatchNearSources;
-  launch_pdl(near_gemm_block_kernel, (d.n_leaves + NS - 1) / NS, 352, (size_t)NS * d.rank * NR * sizeof(float2), s, 
+  launch_pdl(near_gemm_block_kernel, (d.n_leaves + NS - 1) / NS, 352, (size_t)NS * d.rank * NR8 * sizeof(float2), s, 
       d.n_leaves, d.rank, d.nearB32, B.S, B.Z);
-  launch_pdl(near_gather_block_kernel, (int)(((long long)d.N * NR + 255) / 256), 256, 0, s, d.N, d.rank, B.Z, d.kq32,
+  launch_pdl(near_gather_block_kernel, (int)(((long long)d.N * NR8 + 255) / 256), 256, 0, s, d.N, d.rank, B.Z, d.kq32,
                                                                                    d.colleague, B.S, B.P, y,
                                                                                    d.find_phi);
   return cudaGetLastError();
 }
 
-cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, double2* x, int max_outer, int inner,
-                                  double tol, int& n_matvec, std::vector<double>& relres) {
-  if (!d.has_f32) return cudaErrorInvalidValue;
+cudaError_t dev_matvec_f32_wide_ws(DevOperator& d, const float2* x, float2* y, cudaStream_t s) {
+  if (!d.tc) return cudaErrorInvalidValue;
+  if (!s) s = d.stream;
+  BatchWorkspace<kTcRhs>& B = batch_ws<kTcRhs>(d);
+  cudaError_t e = B.ensure_vectors(d);
+  if (e != cudaSuccess) return e;
+  return dev_matvec_f32_wide(d, x, y, B.S, B.P, s);
+}
+
+namespace {
+
+template <int NR>
+cudaError_t gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, double2* x, int max_outer, int inner,
+                              double tol, int& n_matvec, std::vector<double>& relres) {
   const int n = d.N;
   cudaStream_t s = d.stream;
-  BatchWorkspace& B = batch_ws(d);
+  BatchWorkspace<NR>& B = batch_ws<NR>(d);
   cudaError_t e = B.ensure_vectors(d);
   if (e == cudaSuccess) e = B.ensure_basis(n, inner);
   if (e != cudaSuccess) return e;
@@ -673,8 +711,8 @@ cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, do
     const int nb = std::min(NR, nrhs - j0);
     const double2* bb = b + (size_t)j0 * n;
     double2* xb = x + (size_t)j0 * n;
-    double bn2[NR] = {};
-    if ((e = colnorms(bb, n, nb, B, s, bn2)) != cudaSuccess) return e;
+    std::vector<double> bn2(NR, 0.0);
+    if ((e = colnorms(bb, n, nb, B, s, bn2.data())) != cudaSuccess) return e;
     std::vector<double> bn(NR, 0.0), rel(NR, 0.0);
     cudaMemsetAsync(xb, 0, (size_t)n * nb * sizeof(double2), s);
     cudaMemcpyAsync(B.res, bb, (size_t)n * nb * sizeof(double2), cudaMemcpyDeviceToDevice, s);
@@ -684,9 +722,9 @@ cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, do
     }
     std::vector<RhsState> rs(NR);
     for (int o = 0; o < max_outer; ++o) {
-      unsigned active = 0;
+      unsigned long long active = 0;
       for (int j = 0; j < nb; ++j)
-        if (rel[j] > tol) active |= 1u << j;
+        if (rel[j] > tol) active |= 1ull << j;
       if (!active) break;
       for (int j = 0; j < NR; ++j) {
         rs[j].done = !((active >> j) & 1u);
@@ -694,26 +732,95 @@ cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, do
         rs[j].tol = rs[j].done ? 0.0 : std::max(tol / std::max(rel[j], 1e-300), 1e-6);
         rs[j].bnorm = rs[j].done ? 1.0 : std::max(rel[j] * bn[j], 1e-300);
       }
-      launch_pdl(pack_block_kernel, grid_n((long long)n * NR), 256, 0, s, B.res, B.rhs, n, active);
+      launch_pdl(pack_block_kernel<NR>, grid_n((long long)n * NR), 256, 0, s, B.res, B.rhs, n, active);
       int applies = 0;
       if ((e = block_arnoldi(d, B, inner, rs, applies)) != cudaSuccess) return e;
       n_matvec += applies;
-      launch_pdl(unpack_add_block_kernel, grid_n((long long)n * nb), 256, 0, s, xb, B.dx, n, nb, active);
+      launch_pdl(unpack_add_block_kernel<NR>, grid_n((long long)n * nb), 256, 0, s, xb, B.dx, n, nb, active);
       // FP64 residuals of the active columns.
       for (int j = 0; j < nb; ++j) {
-        if (!((active >> j) & 1u)) continue;
+        if (!((active >> j) & 1ull)) continue;
         if ((e = dev_matvec(d, xb + (size_t)j * n, B.tmp, s, false)) != cudaSuccess) return e;
         ++n_matvec;
         launch_pdl(sub64_kernel, grid_n(n), 256, 0, s, bb + (size_t)j * n, B.tmp, B.res + (size_t)j * n, n);
       }
-      double rn2[NR] = {};
-      if ((e = colnorms(B.res, n, nb, B, s, rn2)) != cudaSuccess) return e;
+      std::vector<double> rn2(NR, 0.0);
+      if ((e = colnorms(B.res, n, nb, B, s, rn2.data())) != cudaSuccess) return e;
       for (int j = 0; j < nb; ++j)
-        if ((active >> j) & 1u) rel[j] = bn[j] > 0.0 ? std::sqrt(rn2[j]) / bn[j] : 0.0;
+        if ((active >> j) & 1ull) rel[j] = bn[j] > 0.0 ? std::sqrt(rn2[j]) / bn[j] : 0.0;
     }
     for (int j = 0; j < nb; ++j) relres[j0 + j] = rel[j];
   }
   return cudaStreamSynchronize(s);
+}
+
+}  // namespace
+
+cudaError_t dev_matvec_f32_many(DevOperator& d, int nrhs, const double2* X, double2* Y) {
+  if (!d.tc) return cudaErrorInvalidValue;
+  cudaStream_t s = d.stream;
+  const int n = d.N;
+  BatchWorkspace<kTcRhs>& B = batch_ws<kTcRhs>(d);
+  cudaError_t e = B.ensure_vectors(d);
+  if (e == cudaSuccess) e = B.ensure_basis(n, 1);
+  if (e != cudaSuccess) return e;
+  cudaMemsetAsync(Y, 0, (size_t)n * nrhs * sizeof(double2), s);
+  for (int j0 = 0; j0 < nrhs; j0 += kTcRhs) {
+    const int nb = std::min(kTcRhs, nrhs - j0);
+    const unsigned long long active = nb == 64 ? ~0ull : ((1ull << nb) - 1);
+    launch_pdl(pack_block_kernel<kTcRhs>, grid_n((long long)n * kTcRhs), 256, 0, s, X + (size_t)j0 * n, B.rhs, n,
+               active);
+    if ((e = dev_matvec_f32_wide(d, B.rhs, B.w, B.S, B.P, s)) != cudaSuccess) return e;
+    launch_pdl(unpack_add_block_kernel<kTcRhs>, grid_n((long long)n * nb), 256, 0, s, Y + (size_t)j0 * n,
+               (const float2*)B.w, n, nb, active);
+  }
+  return cudaStreamSynchronize(s);
+}
+
+namespace {
+template <int NR>
+cudaError_t time_block_apply(DevOperator& d, int warmup, int iters, float* ms) {
+  cudaStream_t s = d.stream;
+  BatchWorkspace<NR>& B = batch_ws<NR>(d);
+  cudaError_t e = B.ensure_vectors(d);
+  if (e == cudaSuccess) e = B.ensure_basis(d.N, 1);
+  if (e != cudaSuccess) return e;
+  launch_pdl(zero_f2_block_kernel, grid_n((long long)d.N * NR), 256, 0, s, B.rhs, (long long)d.N * NR);
+  for (int i = 0; i < warmup && e == cudaSuccess; ++i) e = block_apply<NR>(d, B, B.rhs, B.w, s);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, s);
+  for (int i = 0; i < iters && e == cudaSuccess; ++i) e = block_apply<NR>(d, B, B.rhs, B.w, s);
+  cudaEventRecord(b, s);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = t / iters;
+  return e;
+}
+}  // namespace
+
+cudaError_t dev_time_block_apply(DevOperator& d, int width, int warmup, int iters, float* ms) {
+  if (!d.has_f32) return cudaErrorInvalidValue;
+  if (width == kTcRhs) {
+    if (!d.tc) return cudaErrorInvalidValue;
+    return time_block_apply<kTcRhs>(d, warmup, iters, ms);
+  }
+  return time_block_apply<kBatchRhs>(d, warmup, iters, ms);
+}
+
+cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, double2* x, int max_outer, int inner,
+                                  double tol, int& n_matvec, std::vector<double>& relres) {
+  if (!d.has_f32) return cudaErrorInvalidValue;
+  if (d.batch_width == kTcRhs) {
+    if (!d.tc) return cudaErrorInvalidValue;
+    return gmres_mixed_batch<kTcRhs>(d, nrhs, b, x, max_outer, inner, tol, n_matvec, relres);
+  }
+  return gmres_mixed_batch<kBatchRhs>(d, nrhs, b, x, max_outer, inner, tol, n_matvec, relres);
 }
 
 }  // namespace lsg

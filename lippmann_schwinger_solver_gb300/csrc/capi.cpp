@@ -340,6 +340,70 @@ ls_status ls_gmres_mixed(ls_op* op, const double* b, int max_outer, int inner_it
   return LS_OK;
 }
 
+ls_status ls_op_set_batch_width(ls_op* op, int width) {
+  if (!op) return fail(LS_E_INVALID, "ls_op_set_batch_width: null argument");
+  if (width != 8 && width != 64)
+    return fail(LS_E_INVALID, "ls_op_set_batch_width: width must be 8 or 64, not " + std::to_string(width));
+  if (!op->on_device) return fail(LS_E_STATE, "ls_op_set_batch_width: operator was assembled without a device");
+  op->dev.batch_width = width;
+  return LS_OK;
+}
+
+namespace {
+// Builds the tensor-core form of the FP32 operator on first use.
+ls_status ensure_tc(ls_op* op, const char* who) {
+  DevOperator& d = op->dev;
+  if (d.tc) return LS_OK;
+  std::string err;
+  if (!dev_enable_tc(d, op->host, err)) return fail(LS_E_CUDA, std::string(who) + ": " + err);
+  d.device_bytes += dev_tc_operator_bytes(d);
+  return LS_OK;
+}
+ls_status tc_status(ls_op* op, const char* who) {
+  unsigned flag = 0;
+  cudaError_t e = dev_tc_error(op->dev, &flag);
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  if (flag) return fail(LS_E_TIMEOUT, std::string(who) + ": a tensor-core pipeline wait gave up");
+  return LS_OK;
+}
+}  // namespace
+
+ls_status ls_matvec_f32_many(ls_op* op, int nrhs, const double* X, double* Y) {
+  if (!op || !X || !Y || nrhs < 1) return fail(LS_E_INVALID, "ls_matvec_f32_many: bad argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_f32_many: operator was assembled without a device");
+  if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_matvec_f32_many: call ls_op_enable_f32 first");
+  DevOperator& d = op->dev;
+  cudaSetDevice(d.device);
+  ls_status st = ensure_tc(op, "ls_matvec_f32_many");
+  if (st != LS_OK) return st;
+  const size_t bytes = (size_t)d.N * nrhs * sizeof(double2);
+  double2 *dx = nullptr, *dy = nullptr;
+  cudaError_t e = cudaMalloc(&dx, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&dy, bytes);
+  if (e == cudaSuccess) e = cudaMemcpy(dx, X, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = dev_matvec_f32_many(d, nrhs, dx, dy);
+  if (e == cudaSuccess) e = cudaMemcpy(Y, dy, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(dy);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_f32_many");
+  return tc_status(op, "ls_matvec_f32_many");
+}
+
+ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float* ms) {
+  if (!op || !ms || iters < 1 || warmup < 0 || (width != 8 && width != 64))
+    return fail(LS_E_INVALID, "ls_time_block_apply: bad argument");
+  if (!op->on_device) return fail(LS_E_STATE, "ls_time_block_apply: operator was assembled without a device");
+  if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_time_block_apply: call ls_op_enable_f32 first");
+  cudaSetDevice(op->dev.device);
+  if (width == 64) {
+    ls_status st = ensure_tc(op, "ls_time_block_apply");
+    if (st != LS_OK) return st;
+  }
+  cudaError_t e = dev_time_block_apply(op->dev, width, warmup, iters, ms);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_time_block_apply");
+  return width == 64 ? tc_status(op, "ls_time_block_apply") : LS_OK;
+}
+
 ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_outer, int inner_iter, double tol,
                                  double* X, int* n_matvec, double* rel_residuals) {
   if (!op || !B || !X) return fail(LS_E_INVALID, "ls_gmres_mixed_batched: null argument");
@@ -349,6 +413,10 @@ ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_o
   if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_gmres_mixed_batched: call ls_op_enable_f32 first");
   DevOperator& d = op->dev;
   cudaSetDevice(d.device);
+  if (d.batch_width == 64) {
+    ls_status st = ensure_tc(op, "ls_gmres_mixed_batched");
+    if (st != LS_OK) return st;
+  }
   const size_t bytes = (size_t)d.N * nrhs * sizeof(double2);
   double2 *db = nullptr, *dx = nullptr;
   cudaError_t e = cudaMalloc(&db, bytes);
@@ -366,6 +434,10 @@ ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_o
   cudaFree(db);
   cudaFree(dx);
   if (e != cudaSuccess) return cuda_fail(e, "ls_gmres_mixed_batched");
+  if (d.tc) {
+    ls_status st = tc_status(op, "ls_gmres_mixed_batched");
+    if (st != LS_OK) return st;
+  }
   if (n_matvec) *n_matvec = nmv;
   bool ok = true;
   for (int j = 0; j < nrhs; ++j) {

@@ -25,10 +25,14 @@ struct DevPhase {
 };
 
 struct GmresWorkspace;  // gmres.cu: Krylov basis and scratch, kept between solves
+template <int NR>
 struct BatchWorkspace;  // batched.cu: state of the many-right-hand-side solver
+struct TcOperator;      // batched_tc.cu: the FP32 operator in tensor-core form
 
-// Right-hand sides handled together by the batched solver (batched.cu).
+// Right-hand sides handled together by the batched solver (batched.cu):
+// 8 with the CUDA-core block apply, 64 with the tensor-core one.
 constexpr int kBatchRhs = 8;
+constexpr int kTcRhs = 64;
 
 struct DevOperator {
   int device = 0;
@@ -81,7 +85,12 @@ struct DevOperator {
   double2* xbuf = nullptr;
   double2* ybuf = nullptr;
   GmresWorkspace* gws = nullptr;
-  BatchWorkspace* bws = nullptr;
+  BatchWorkspace<kBatchRhs>* bws = nullptr;
+  BatchWorkspace<kTcRhs>* bws_tc = nullptr;
+  TcOperator* tc = nullptr;
+  // Right-hand sides per block of the batched solver: kBatchRhs (CUDA-core
+  // block apply) or kTcRhs (tensor-core block apply, built on first use).
+  int batch_width = kTcRhs;
   // events for phase timing
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   // recorded after the downward phases (before the near field) when phases
@@ -112,6 +121,16 @@ bool dev_enable_df(DevOperator& d, std::string& err);
 void dev_free_df(DevOperator& d);
 cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l);
 
+// batched_tc.cu
+bool dev_enable_tc(DevOperator& d, const HostOperator& h, std::string& err);
+void dev_free_tc(DevOperator& d);
+// y = A32 x for kTcRhs right-hand sides stored rhs-minor, on the tensor
+// cores; S (charges_len + 1 rows, the last one zero) and P (pots_len rows)
+// are the block's work buffers.
+cudaError_t dev_matvec_f32_wide(DevOperator& d, const float2* x, float2* y, float2* S, float2* P, cudaStream_t s);
+cudaError_t dev_tc_error(DevOperator& d, unsigned* flag);
+long long dev_tc_operator_bytes(const DevOperator& d);
+
 // batched.cu
 void dev_free_batch(DevOperator& d);
 // y_j = A32 x_j for the kBatchRhs vectors of a block stored rhs-minor
@@ -121,8 +140,18 @@ cudaError_t dev_matvec_f32_batch(DevOperator& d, const float2* x, float2* y, cud
 // column j at b + j * N), solved kBatchRhs at a time with a shared FP32
 // operator apply. n_matvec counts FP32 block applies and FP64 residual
 // products; relres gets each column's final FP64 relative residual.
+// d.batch_width selects the block width (the tensor-core form must have
+// been enabled for kTcRhs).
 cudaError_t dev_gmres_mixed_batch(DevOperator& d, int nrhs, const double2* b, double2* x, int max_outer, int inner,
                                   double tol, int& n_matvec, std::vector<double>& relres);
+// Same apply on kTcRhs vectors through the block solver's work buffers.
+cudaError_t dev_matvec_f32_wide_ws(DevOperator& d, const float2* x, float2* y, cudaStream_t s);
+// Y = A32 X for nrhs FP64 columns (column j at j * N), kTcRhs at a time on
+// the tensor cores; synchronises the operator's stream.
+cudaError_t dev_matvec_f32_many(DevOperator& d, int nrhs, const double2* X, double2* Y);
+// Mean ms of one block apply of `width` (kBatchRhs or kTcRhs) resident
+// right-hand sides, CUDA events on the operator's stream.
+cudaError_t dev_time_block_apply(DevOperator& d, int width, int warmup, int iters, float* ms);
 
 // gmres.cu
 void dev_free_gmres(DevOperator& d);

@@ -43,6 +43,12 @@ struct GemvPhase {
   std::vector<GemvTile> tiles;
   int accumulate = 0;           // 0: overwrite, 1: accumulate into dst
   long long nnz = 0;            // true (unpadded) block entries
+  // Block structure of the tiles: block b is tiles [blk_tile0[b],
+  // blk_tile0[b + 1]) with blk_rows[b] rows and blk_K[b] columns; its rows
+  // are consecutive in `out` from the first tile's row_base and its gather
+  // list is the first tile's idx range (column k at i_off + k). Read by the
+  // tensor-core form of the phase (batched_tc.cu).
+  std::vector<int> blk_tile0, blk_rows, blk_K;
   // Staging before packing: the phase owns its blocks (row major) and their
   // gather lists until they are packed; one record per block row points
   // into them.

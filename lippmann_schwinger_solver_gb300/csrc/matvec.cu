@@ -497,6 +497,7 @@ void dev_free(DevOperator& d) {
   dev_free_df(d);
   dev_free_gmres(d);
   dev_free_batch(d);
+  dev_free_tc(d);
   for (auto& ev : d.ev) if (ev) cudaEventDestroy(ev);
   for (auto& ev : d.ev_down) if (ev) cudaEventDestroy(ev);
   if (d.stream) cudaStreamDestroy(d.stream);

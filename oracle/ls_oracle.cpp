@@ -1049,51 +1049,7 @@ int ora_gmres(void* h, const double* bd, int max_iter, double tol, double* xd, d
 // column-pivoted QR, x = x0 + V y, repeated `restarts` times.
 int ora_gmres_restarted(void* h, const double* bd, int m, int restarts, double* xd) {
   Oracle* o = (Oracle*)h;
-  const int N = o->N;
-  const cd* b = (const cd*)bd;
-  cd* x = (cd*)xd;
-  std::vector<cd> x0(N, cd(0.0, 0.0)), out(N);
-  for (int rs = 0; rs < restarts; ++rs) {
-    int mm = m;
-    o->matvec(x0.data(), out.data());
-    std::vector<cd> r0(N);
-    for (int i = 0; i < N; ++i) r0[i] = b[i] - out[i];
-    double beta = 0.0;
-    for (int i = 0; i < N; ++i) beta += std::norm(r0[i]);
-    beta = std::sqrt(beta);
-    std::vector<std::vector<cd>> V(1, std::vector<cd>(N));
-    for (int i = 0; i < N; ++i) V[0][i] = r0[i] / beta;
-    CMat Hm(m + 1, m);
-    std::vector<cd> w(N);
-    for (int j = 0; j < m; ++j) {
-      o->matvec(V[j].data(), w.data());
-      for (int i = 0; i <= j; ++i) {
-        cd s(0.0, 0.0);
-        for (int t = 0; t < N; ++t) s += std::conj(V[i][t]) * w[t];
-        Hm(i, j) = s;
-        for (int t = 0; t < N; ++t) w[t] -= s * V[i][t];
-      }
-      double wn = 0.0;
-      for (int t = 0; t < N; ++t) wn += std::norm(w[t]);
-      Hm(j + 1, j) = std::sqrt(wn);
-      if (std::abs(Hm(j + 1, j)) < 1e-8) { mm = j + 1; break; }
-      V.push_back(std::vector<cd>(N));
-      for (int t = 0; t < N; ++t) V[j + 1][t] = w[t] / Hm(j + 1, j);
-    }
-    CMat Hs(mm + 1, mm);
-    for (int a = 0; a <= mm; ++a) for (int c = 0; c < mm; ++c) Hs(a, c) = Hm(a, c);
-    std::vector<cd> be1(mm + 1, cd(0.0, 0.0)), ym(mm);
-    be1[0] = beta;
-    ColPivQR qr;
-    qr.compute(Hs);
-    qr.solve(be1.data(), ym.data());
-    for (int t = 0; t < N; ++t) {
-      cd s = x0[t];
-      for (int c = 0; c < mm; ++c) s += V[c][t] * ym[c];
-      x[t] = s;
-    }
-    for (int t = 0; t < N; ++t) x0[t] = x[t];
-  }
+  restarted_gmres(o->N, [o](const cd* x, cd* y) { o->matvec(x, y); }, (const cd*)bd, m, restarts, (cd*)xd);
   return 0;
 }
 

@@ -23,6 +23,9 @@
 
 #include <omp.h>
 
+#include <map>
+#include <tuple>
+
 namespace ora {
 namespace adaptive {
 // Far-field Bessel orders: one library call per order (the reference's
@@ -37,6 +40,14 @@ struct Cone {
   std::vector<Pair> IL;
   std::vector<int> oc, ochk, ic, ichk;  // outgoing charge/check, incoming charge/check points
   int o_rows = 0, o_cols = 0, o_rank = -1, i_rows = 0, i_cols = 0, i_rank = -1;  // for the printed statistics
+  // operator (FMM2DCone, GMRES/G_FMM2DTree.hpp:119-149)
+  bool out_active = false, in_active = false;  // outgoing_ILActive / incoming_ILActive
+  std::vector<int> uc;                          // user_checkPoints
+  CMat M2M;
+  ColPivQR out_A, in_A;                         // outgoing / incoming Atilde
+  std::vector<CMat> M2L;
+  CMat L2L[4];
+  std::vector<cd> out_charges, in_charges, in_potential;
 };
 
 struct ABox {
@@ -49,6 +60,16 @@ struct ABox {
   std::vector<int> chargeLoc;
   std::vector<int> oc, ochk, ic, ichk;
   int o_rows = 0, o_cols = 0, o_rank = -1, i_rows = 0, i_cols = 0, i_rank = -1;
+  // operator (FMM2DBox, GMRES/G_FMM2DTree.hpp:153-227)
+  bool out_active = false, in_active = false;
+  std::vector<int> uc;
+  CMat out_Ar, L2L;
+  ColPivQR out_A, in_A;
+  std::vector<CMat> M2L;
+  std::vector<cd> multipoles, out_charges, in_charges, in_potential;
+  // near neighbours of a leaf (getNeighbors :1500-1748): tree indices at
+  // level j, j+1, j+1, j-1
+  int colleague[9], fine[12], sepfine[20], coarse[12];
 };
 
 struct LevelStat {
@@ -60,6 +81,7 @@ struct LevelStat {
 struct AOracle {
   ora_cfg cfg;
   int treeAdaptivity = 5;
+  bool with_operator = false;  // also form Ar and the Atilde factorisations (for the matvec)
   double kappa = 0, L = 1, epsTree = 1e-5;
   int n1 = 6, rank = 36, nb = 21, S = 15, nLevels = 0, level_LFR = 2;
   std::vector<std::vector<ABox>> tree;
@@ -73,6 +95,12 @@ struct AOracle {
   std::vector<Pt> grid;
   std::vector<CMat> M;         // per level: (2S+1) x rank
   std::vector<LevelStat> stats;
+  std::vector<double> Qp;      // nb x rank: Q^+ (FarFieldInteraction::evaluateQ)
+  std::vector<Pair> nbases;    // (a, b) of the Chebyshev bases T_a(x) T_b(y)
+  // near blocks by (level, kind, index): kind 0 colleague, 1 fine,
+  // 2 separated fine, 3 coarse (readNeighborInteractions :1913-1950)
+  std::map<std::tuple<int, int, int>, CMat> nearBlk;
+  int unmatched_neighbors = 0;
 
   double contrast(Pt r) const { return contrast_value(cfg, r); }
   int child_index(int J, int boxNumber) const {
@@ -299,12 +327,13 @@ struct AOracle {
     for (int d = 0; d < cfg.degreeOfBases; ++d)
       for (int a = 0; a < d + 1; ++a) bases.push_back({a, d - a});
     nb = (int)bases.size();
+    nbases = bases;
     CMat Q(rank, nb);
     for (int i = 0; i < rank; ++i)
       for (int l = 0; l < nb; ++l) Q(i, l) = cd(chebT(chebStd[i].x, bases[l].x) * chebT(chebStd[i].y, bases[l].y), 0.0);
     ColPivQR qr;
     qr.compute(Q);
-    std::vector<double> Qp((size_t)nb * rank);
+    Qp.assign((size_t)nb * rank, 0.0);
     std::vector<cd> e(rank), xs(nb);
     for (int i = 0; i < rank; ++i) {
       std::fill(e.begin(), e.end(), cd(0.0, 0.0));
@@ -387,6 +416,14 @@ struct AOracle {
     return s;
   }
 
+  // getMatrix (GMRES/G_FMM2DTree.hpp:660-672): K(rows, cols).
+  CMat getMatrix(const std::vector<int>& rows, const std::vector<int>& cols, HCache& hc) const {
+    CMat A((int)rows.size(), (int)cols.size());
+    for (size_t b = 0; b < cols.size(); ++b)
+      for (size_t a = 0; a < rows.size(); ++a) A((int)a, (int)b) = entry(rows[a], cols[b], hc);
+    return A;
+  }
+
   // ---- node sets (getParticlesFromChildren*) -------------------------------
   bool lfr_child(int J, int K) const { return J >= level_LFR || (J < level_LFR && tree[J][K].leaf); }
   template <class Get>
@@ -435,24 +472,30 @@ struct AOracle {
       B.o_rows = (int)far.size();
       B.o_cols = (int)own.size();
       if (!far.empty() && !own.empty()) {
-        B.o_rank = aca_nodes(far, own, tol, rb, cb, nullptr, E);
+        B.out_active = true;
+        B.o_rank = aca_nodes(far, own, tol, rb, cb, with_operator ? &B.out_Ar : nullptr, E);
         if (B.o_rank > 0) {
           for (int r : rb) B.ochk.push_back(far[r]);
           for (int c : cb) B.oc.push_back(own[c]);
+          if (with_operator) B.out_A.compute(getMatrix(B.ochk, B.oc, hc));
         }
       } else {
+        B.out_active = false;
         B.oc = own;
       }
     } else {
       B.i_rows = (int)own.size();
       B.i_cols = (int)far.size();
       if (!far.empty() && !own.empty()) {
+        B.in_active = true;
         B.i_rank = aca_nodes(own, far, tol, rb, cb, nullptr, E);
         if (B.i_rank > 0) {
           for (int r : rb) B.ichk.push_back(own[r]);
           for (int c : cb) B.ic.push_back(far[c]);
+          if (with_operator && !B.leaf) B.in_A.compute(getMatrix(B.ichk, B.ic, hc));
         }
       } else {
+        B.in_active = false;
         B.ichk = own;
       }
     }
@@ -476,24 +519,30 @@ struct AOracle {
       C.o_rows = (int)far.size();
       C.o_cols = (int)own.size();
       if (!far.empty() && !own.empty()) {
+        C.out_active = true;
         C.o_rank = aca_nodes(far, own, tol, rb, cb, nullptr, E);
         if (C.o_rank > 0) {
           for (int r : rb) C.ochk.push_back(far[r]);
           for (int c : cb) C.oc.push_back(own[c]);
+          if (with_operator) C.out_A.compute(getMatrix(C.ochk, C.oc, hc));
         }
       } else {
+        C.out_active = false;
         C.oc = own;
       }
     } else {
       C.i_rows = (int)own.size();
       C.i_cols = (int)far.size();
       if (!far.empty() && !own.empty()) {
+        C.in_active = true;
         C.i_rank = aca_nodes(own, far, tol, rb, cb, nullptr, E);
         if (C.i_rank > 0) {
           for (int r : rb) C.ichk.push_back(own[r]);
           for (int c : cb) C.ic.push_back(far[c]);
+          if (with_operator) C.in_A.compute(getMatrix(C.ichk, C.ic, hc));
         }
       } else {
+        C.in_active = false;
         C.ichk = own;
       }
     }
@@ -529,6 +578,445 @@ struct AOracle {
       }
     }
     stats.push_back({dir, j, (int)tree[j].size(), kmax, rows_cp, cols_cp, rankPerLevel, hfr_level});
+  }
+
+  // ---- operator for the matvec ---------------------------------------------
+  int child(int j, int k, int c) const { return child_index(j + 1, 4 * tree[j][k].boxNumber + c); }
+  // Cone of box (jA, kA) that points at box (j, k) (fmod(arg + 2 pi, 2 pi),
+  // :2524-2526, :3860-3862).
+  int cone_towards(int j, int k, int jA, int kA) const {
+    const double arg = std::atan2(tree[j][k].c.y - tree[jA][kA].c.y, tree[j][k].c.x - tree[jA][kA].c.x);
+    return int(std::fmod(arg + 2 * PI, 2 * PI) / ConeAperture[jA]);
+  }
+
+  // getUserCheckPoints (:3146-3230).
+  void user_checks() {
+    for (int j = nLevels; j >= level_LFR; --j)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) B.uc = B.chargeLoc;
+        else if (B.in_active) B.uc = B.ichk;
+        else for (int c = 0; c < 4; ++c) { const auto& v = tree[j + 1][child(j, k, c)].uc; B.uc.insert(B.uc.end(), v.begin(), v.end()); }
+      }
+    for (int j = level_LFR - 1; j >= 2; --j)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) { B.uc = B.chargeLoc; continue; }
+        for (int cone = 0; cone < nCones[j]; ++cone) {
+          Cone& C = B.cones[cone];
+          if (C.in_active) { C.uc = C.ichk; continue; }
+          for (int c = 0; c < 4; ++c) {
+            const ABox& ch = tree[j + 1][child(j, k, c)];
+            const auto& v = (ch.leaf || j + 1 == level_LFR) ? ch.uc : ch.cones[cone / 2].uc;
+            C.uc.insert(C.uc.end(), v.begin(), v.end());
+          }
+        }
+      }
+  }
+
+  // Assemble_HFR_M2M :3573-3622, :3804; Assemble_HFR_M2L :3829; Assemble_LFR_M2L
+  // :2502; Assemble_LFR_L2L :2653, :2824; Assemble_HFR_L2L :3944, :4183.
+  void assemble() {
+    for (int j = level_LFR - 1; j >= 2; --j) {
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) continue;
+        HCache hc{this, {}};
+        for (int cone = 0; cone < nCones[j]; ++cone) {
+          Cone& C = B.cones[cone];
+          if (!C.out_active) continue;
+          std::vector<int> src;
+          for (int c = 0; c < 4; ++c) {
+            const ABox& ch = tree[j + 1][child(j, k, c)];
+            const auto& v = (j == level_LFR - 1 || ch.leaf) ? ch.oc : ch.cones[cone / 2].oc;
+            src.insert(src.end(), v.begin(), v.end());
+          }
+          if (!C.ochk.empty() && !src.empty()) C.M2M = getMatrix(C.ochk, src, hc);
+        }
+      }
+    }
+    for (int j = 2; j < level_LFR; ++j) {
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) continue;
+        HCache hc{this, {}};
+        for (int cone = 0; cone < nCones[j]; ++cone) {
+          Cone& C = B.cones[cone];
+          if (!C.in_active) continue;
+          for (const Pair& p : C.IL) {
+            const ABox& O = tree[p.x][p.y];
+            if (O.leaf) C.M2L.push_back(getMatrix(C.uc, O.oc, hc));
+            else C.M2L.push_back(getMatrix(C.uc, O.cones[cone_towards(j, k, p.x, p.y)].oc, hc));
+          }
+        }
+      }
+    }
+    for (int j = 2; j <= nLevels; ++j) {
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if ((j < level_LFR && !B.leaf) || !B.in_active) continue;
+        HCache hc{this, {}};
+        const std::vector<int>& rows = B.leaf ? B.chargeLoc : B.uc;
+        for (const Pair& p : B.IL) {
+          const ABox& O = tree[p.x][p.y];
+          if (p.x < level_LFR && !O.leaf) B.M2L.push_back(getMatrix(rows, O.cones[cone_towards(j, k, p.x, p.y)].oc, hc));
+          else B.M2L.push_back(getMatrix(rows, O.oc, hc));
+        }
+      }
+    }
+    for (int j = 2; j < nLevels; ++j) {
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf || j < level_LFR || !B.in_active) continue;
+        HCache hc{this, {}};
+        for (int c = 0; c < 4; ++c) {
+          ABox& ch = tree[j + 1][child(j, k, c)];
+          ch.L2L = getMatrix(ch.leaf ? ch.chargeLoc : ch.uc, B.ic, hc);
+        }
+      }
+    }
+    for (int j = 2; j < level_LFR; ++j) {
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) continue;
+        HCache hc{this, {}};
+        for (int cone = 0; cone < nCones[j]; ++cone) {
+          Cone& C = B.cones[cone];
+          if (!C.in_active) continue;
+          for (int c = 0; c < 4; ++c) {
+            const ABox& ch = tree[j + 1][child(j, k, c)];
+            const std::vector<int>* rows;
+            if (j == level_LFR - 1) rows = (level_LFR != nLevels && !ch.leaf) ? &ch.uc : &ch.chargeLoc;
+            else rows = ch.leaf ? &ch.uc : &ch.cones[cone / 2].uc;
+            if (!rows->empty() && !C.ic.empty()) C.L2L[c] = getMatrix(*rows, C.ic, hc);
+          }
+        }
+      }
+    }
+  }
+
+  // ---- near field -------------------------------------------------------------
+  // Neighbour offsets in units of the leaf's radius (the N_centers,
+  // FN_centers, SFN_centers, CN_centers tables, :19-72): colleagues at
+  // the same level (the self box last), fine and separated-fine neighbours one
+  // level finer, coarse neighbours one level coarser.
+  std::vector<Pt> offsets(int kind) const {
+    std::vector<Pt> v;
+    if (kind == 0) {
+      for (int a = -1; a <= 1; ++a)
+        for (int b = -1; b <= 1; ++b)
+          if (a || b) v.push_back({2.0 * a, 2.0 * b});
+      v.push_back({0.0, 0.0});
+    } else if (kind == 1) {
+      const double e[4] = {-1.5, -0.5, 0.5, 1.5};
+      for (double x : e)
+        for (double y : e)
+          if (std::fabs(x) == 1.5 || std::fabs(y) == 1.5) v.push_back({x, y});
+    } else if (kind == 2) {
+      const double e[6] = {-2.5, -1.5, -0.5, 0.5, 1.5, 2.5};
+      for (double x : e)
+        for (double y : e)
+          if (std::fabs(x) == 2.5 || std::fabs(y) == 2.5) v.push_back({x, y});
+    } else {
+      const double e[4] = {-3.0, -1.0, 1.0, 3.0};
+      for (double x : e)
+        for (double y : e)
+          if (std::fabs(x) == 3.0 || std::fabs(y) == 3.0) v.push_back({x, y});
+    }
+    return v;
+  }
+  // getNeighbors (:1500-1748): sorts each leaf's neighbour list by level and
+  // offset. Separated fine neighbours are the finer ones farther than 2.5
+  // radii (find_distance, :1350).
+  void classify_neighbors() {
+    const std::vector<Pt> tab[4] = {offsets(0), offsets(1), offsets(2), offsets(3)};
+    for (const Pair& lf : leafNodes) {
+      ABox& B = tree[lf.x][lf.y];
+      std::fill(B.colleague, B.colleague + 9, -1);
+      std::fill(B.fine, B.fine + 12, -1);
+      std::fill(B.sepfine, B.sepfine + 20, -1);
+      std::fill(B.coarse, B.coarse + 12, -1);
+      const double r = boxRadius[lf.x];
+      for (const Pair& p : B.nbrs) {
+        const ABox& O = tree[p.x][p.y];
+        const double dx = (O.c.x - B.c.x) / r, dy = (O.c.y - B.c.y) / r;
+        int kind;
+        if (p.x == lf.x) kind = 0;
+        else if (p.x == lf.x + 1) kind = std::sqrt(dx * dx + dy * dy) > 2.5 ? 2 : 1;
+        else if (p.x == lf.x - 1) kind = 3;
+        else { ++unmatched_neighbors; continue; }
+        int* slot = kind == 0 ? B.colleague : kind == 1 ? B.fine : kind == 2 ? B.sepfine : B.coarse;
+        int found = -1;
+        for (size_t t = 0; t < tab[kind].size(); ++t)
+          if (std::fabs(tab[kind][t].x - dx) < 1e-8 && std::fabs(tab[kind][t].y - dy) < 1e-8) found = (int)t;
+        if (found < 0) { ++unmatched_neighbors; continue; }
+        slot[found] = p.y;
+      }
+    }
+  }
+  // getOperator (:1773-1806) with NearFieldInteraction1::evaluateV
+  // (NearFieldInteraction1.hpp:98-128): target box A of radius rA at the
+  // origin, source box B of radius rB centred at (cx, cy):
+  // B(i, :) = (i rB^2 / 4) V(i, :) Q^+, V(i, l) = int H0(kappa rB |X_i - p|)
+  // T_a(p_x) T_b(p_y) dp over [-1, 1]^2, X_i = (node_i - c_B) / rB; the
+  // 6-digit text round trip when reference_rounding is set.
+  CMat near_block(double rA, double rB, double cx, double cy) const {
+    std::vector<double> gln, glw;
+    gauss_legendre(10, gln, glw);
+    CMat V(rank, nb);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < rank; ++i) {
+      const double Xx = (rA * chebStd[i].x - cx) / rB, Xy = (rA * chebStd[i].y - cy) / rB;
+      for (int l = 0; l < nb; ++l) {
+        const int a = nbases[l].x, b = nbases[l].y;
+        auto f = [&](double px, double py) -> cd {
+          const double R2 = (Xx - px) * (Xx - px) + (Xy - py) * (Xy - py);
+          const double R = std::sqrt(R2);
+          const double arg = kappa * rB * R;
+          return (besselJ(0, arg) + I * besselY(0, arg)) * chebT(px, a) * chebT(py, b);
+        };
+        V(i, l) = adaptive_quad(f, gln, glw, 1e-7);
+      }
+    }
+    CMat Bk(rank, rank);
+    for (int i = 0; i < rank; ++i)
+      for (int k = 0; k < rank; ++k) {
+        cd s(0.0, 0.0);
+        for (int l = 0; l < nb; ++l) s += V(i, l) * I * rB * rB / 4.0 * Qp[(size_t)l * rank + k];
+        Bk(i, k) = cfg.reference_rounding ? round6(s) : s;
+      }
+    return Bk;
+  }
+  // The near blocks the leaves use (writeNeighborInteractionsForLevel
+  // :1815-1911, computed here only for the (level, kind, index) that occur).
+  void precompute_near() {
+    const std::vector<Pt> tab[4] = {offsets(0), offsets(1), offsets(2), offsets(3)};
+    const int dl[4] = {0, 1, 1, -1};
+    for (const Pair& lf : leafNodes) {
+      const ABox& B = tree[lf.x][lf.y];
+      const int* slots[4] = {B.colleague, B.fine, B.sepfine, B.coarse};
+      const int cnt[4] = {9, 12, 20, 12};
+      for (int kind = 0; kind < 4; ++kind)
+        for (int t = 0; t < cnt[kind]; ++t) {
+          if (slots[kind][t] < 0) continue;
+          const auto key = std::make_tuple(lf.x, kind, t);
+          if (nearBlk.count(key)) continue;
+          const double rA = boxRadius[lf.x], rB = boxRadius[lf.x + dl[kind]];
+          nearBlk[key] = near_block(rA, rB, tab[kind][t].x * rA, tab[kind][t].y * rA);
+        }
+    }
+  }
+
+  void build_operator() {
+    user_checks();
+    assemble();
+    classify_neighbors();
+    precompute_near();
+  }
+
+  // ---- the matvec: DFMM::MatVecProduct, GMRES/GMRES.cpp:201-254 ------------------
+  static std::vector<cd> solve(const ColPivQR& qr, const std::vector<cd>& u, int n) {
+    std::vector<cd> x(n, cd(0.0, 0.0));
+    qr.solve(u.data(), x.data());
+    return x;
+  }
+  static std::vector<cd> gemv(const CMat& A, const std::vector<cd>& x) {
+    std::vector<cd> y(A.r, cd(0.0, 0.0));
+    if (A.c == (int)x.size()) gemv_acc(A, x.data(), y.data());
+    return y;
+  }
+  static void add_gemv(const CMat& A, const std::vector<cd>& x, std::vector<cd>& y) {
+    if (A.r == (int)y.size() && A.c == (int)x.size() && A.r > 0 && A.c > 0) gemv_acc(A, x.data(), y.data());
+  }
+  void matvec(const cd* x, cd* y) {
+    // assignLeafCharges :1139
+    for (size_t t = 0; t < leafNodes.size(); ++t)
+      tree[leafNodes[t].x][leafNodes[t].y].multipoles.assign(x + t * rank, x + (t + 1) * rank);
+    // LFR_M2M :2472 (leaves of HFR levels included)
+    for (int j = nLevels; j >= 2; --j) {
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (j < level_LFR && !B.leaf) continue;
+        std::vector<cd> src;
+        if (B.leaf) src = B.multipoles;
+        else for (int c = 0; c < 4; ++c) { const auto& v = tree[j + 1][child(j, k, c)].out_charges; src.insert(src.end(), v.begin(), v.end()); }
+        if (B.out_active) {
+          if (!B.oc.empty()) B.out_charges = solve(B.out_A, gemv(B.out_Ar, src), (int)B.oc.size());
+        } else {
+          B.out_charges = src;
+        }
+      }
+    }
+    // HFR_M2M :3772
+    for (int j = level_LFR - 1; j >= 2; --j) {
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) continue;
+        for (int cone = 0; cone < nCones[j]; ++cone) {
+          Cone& C = B.cones[cone];
+          std::vector<cd> src;
+          for (int c = 0; c < 4; ++c) {
+            const ABox& ch = tree[j + 1][child(j, k, c)];
+            const auto& v = (j == level_LFR - 1 || ch.leaf) ? ch.out_charges : ch.cones[cone / 2].out_charges;
+            src.insert(src.end(), v.begin(), v.end());
+          }
+          if (C.out_active) {
+            if (!C.oc.empty() && !C.ochk.empty() && !src.empty())
+              C.out_charges = solve(C.out_A, gemv(C.M2M, src), (int)C.oc.size());
+          } else {
+            C.out_charges = src;
+          }
+        }
+      }
+    }
+    // LFR_M2L :2577
+    for (int j = 2; j <= nLevels; ++j) {
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (j < level_LFR && !B.leaf) continue;
+        B.in_potential.assign(B.leaf ? B.chargeLoc.size() : B.uc.size(), cd(0.0, 0.0));
+        if (!B.in_active) continue;
+        for (size_t l = 0; l < B.IL.size(); ++l) {
+          const Pair p = B.IL[l];
+          const ABox& O = tree[p.x][p.y];
+          if (p.x < level_LFR && !O.leaf) {
+            const Cone& S = O.cones[cone_towards(j, k, p.x, p.y)];
+            if (!S.out_charges.empty()) add_gemv(B.M2L[l], S.out_charges, B.in_potential);
+          } else {
+            add_gemv(B.M2L[l], O.out_charges, B.in_potential);
+          }
+        }
+      }
+    }
+    // HFR_M2L :3882
+    for (int j = 2; j < level_LFR; ++j) {
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) continue;
+        for (int cone = 0; cone < nCones[j]; ++cone) {
+          Cone& C = B.cones[cone];
+          C.in_potential.assign(C.uc.size(), cd(0.0, 0.0));
+          if (!C.in_active) continue;
+          for (size_t l = 0; l < C.IL.size(); ++l) {
+            const Pair p = C.IL[l];
+            const ABox& O = tree[p.x][p.y];
+            const std::vector<cd>& src = O.leaf ? O.out_charges : O.cones[cone_towards(j, k, p.x, p.y)].out_charges;
+            if (!src.empty()) add_gemv(C.M2L[l], src, C.in_potential);
+          }
+        }
+      }
+    }
+    // HFR_L2L :4208 (cones of one box in order, so that no two threads
+    // update the same child)
+    for (int j = 2; j < level_LFR; ++j) {
+#pragma omp parallel for schedule(dynamic, 1)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf) continue;
+        for (int cone = 0; cone < nCones[j]; ++cone) {
+          Cone& C = B.cones[cone];
+          if (C.in_active) {
+            if (C.ic.empty()) continue;
+            C.in_charges = solve(C.in_A, C.in_potential, (int)C.ic.size());
+            for (int c = 0; c < 4; ++c) {
+              ABox& ch = tree[j + 1][child(j, k, c)];
+              std::vector<cd>& pot = (j == level_LFR - 1 || ch.leaf) ? ch.in_potential : ch.cones[cone / 2].in_potential;
+              add_gemv(C.L2L[c], C.in_charges, pot);
+            }
+          } else {
+            int off = 0;
+            for (int c = 0; c < 4; ++c) {
+              ABox& ch = tree[j + 1][child(j, k, c)];
+              std::vector<cd>* pot;
+              int len;
+              if (j == level_LFR - 1) {
+                pot = &ch.in_potential;
+                len = (level_LFR != nLevels && !ch.leaf) ? (int)ch.uc.size() : (int)ch.chargeLoc.size();
+              } else if (ch.leaf) {
+                pot = &ch.in_potential;
+                len = (int)ch.uc.size();
+              } else {
+                pot = &ch.cones[cone / 2].in_potential;
+                len = (int)ch.cones[cone / 2].uc.size();
+              }
+              for (int i = 0; i < len && off + i < (int)C.in_potential.size() && i < (int)pot->size(); ++i)
+                (*pot)[i] += C.in_potential[off + i];
+              off += len;
+            }
+          }
+        }
+      }
+    }
+    // LFR_L2L :2800
+    for (int j = 2; j < nLevels; ++j) {
+#pragma omp parallel for schedule(dynamic, 4)
+      for (int k = 0; k < (int)tree[j].size(); ++k) {
+        ABox& B = tree[j][k];
+        if (B.leaf || j < level_LFR) continue;
+        if (B.in_active) {
+          if (B.ic.empty()) continue;
+          B.in_charges = solve(B.in_A, B.in_potential, (int)B.ic.size());
+          for (int c = 0; c < 4; ++c) {
+            ABox& ch = tree[j + 1][child(j, k, c)];
+            add_gemv(ch.L2L, B.in_charges, ch.in_potential);
+          }
+        } else {
+          int off = 0;
+          for (int c = 0; c < 4; ++c) {
+            ABox& ch = tree[j + 1][child(j, k, c)];
+            const int len = ch.leaf ? (int)ch.chargeLoc.size() : (int)ch.uc.size();
+            for (int i = 0; i < len && off + i < (int)B.in_potential.size(); ++i) ch.in_potential[i] += B.in_potential[off + i];
+            off += len;
+          }
+        }
+      }
+    }
+    // evaluate_NearField_Using_Precomputations_LS :2884-2960: per leaf,
+    // box operator diag(kappa^2 q) B (+ I for the self block) times the
+    // neighbour's multipoles, for colleague, fine, separated-fine and coarse
+    // neighbours.
+    const int dl[4] = {0, 1, 1, -1};
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int t = 0; t < (int)leafNodes.size(); ++t) {
+      const int j = leafNodes[t].x, k = leafNodes[t].y;
+      ABox& B = tree[j][k];
+      std::vector<double> cv(rank);
+      for (int i = 0; i < rank; ++i) cv[i] = kappa * kappa * contrast(grid[B.chargeLoc[i]]);
+      const int* slots[4] = {B.colleague, B.fine, B.sepfine, B.coarse};
+      const int cnt[4] = {9, 12, 20, 12};
+      for (int kind = 0; kind < 4; ++kind)
+        for (int n = 0; n < cnt[kind]; ++n) {
+          const int nk = slots[kind][n];
+          if (nk < 0) continue;
+          const CMat& Bk = nearBlk.at(std::make_tuple(j, kind, n));
+          const std::vector<cd>& src = tree[j + dl[kind]][nk].multipoles;
+          CMat Op(rank, rank);
+          for (int c = 0; c < rank; ++c)
+            for (int i = 0; i < rank; ++i) {
+              cd v = Bk(i, c);
+              if (cfg.findPhi) {
+                v = cv[i] * v;
+                if (kind == 0 && n == 8 && i == c) v += 1.0;
+              }
+              Op(i, c) = v;
+            }
+          add_gemv(Op, src, B.in_potential);
+        }
+    }
+    // collectPotential :3045
+    for (size_t t = 0; t < leafNodes.size(); ++t) {
+      const ABox& B = tree[leafNodes[t].x][leafNodes[t].y];
+      for (int i = 0; i < rank; ++i) y[t * rank + i] = B.in_potential[i];
+    }
   }
 
   void run() {
@@ -687,6 +1175,46 @@ long ora_adaptive_skeletons(const ora_cfg* cfg, int treeAdaptivity, int* buf, lo
       }
     }
   return n;
+}
+
+// The adaptive-tree operator for the matvec (the reference's default path,
+// GMRES/GMRES.cpp:164-199): tree, NCA, blocks and near-field
+// precomputations. Returns a handle, or null for a bad configuration.
+void* ora_adaptive_create(const ora_cfg* cfg, int treeAdaptivity) {
+  using namespace ora::adaptive;
+  if (!cfg || cfg->nChebNodes < 2) return nullptr;
+  AOracle* o = new AOracle();
+  o->cfg = *cfg;
+  o->treeAdaptivity = treeAdaptivity;
+  o->with_operator = true;
+  o->run();
+  o->build_operator();
+  return o;
+}
+void ora_adaptive_destroy(void* h) { delete (ora::adaptive::AOracle*)h; }
+int ora_adaptive_N(void* h) { return (int)((ora::adaptive::AOracle*)h)->grid.size(); }
+int ora_adaptive_unmatched_neighbors(void* h) { return ((ora::adaptive::AOracle*)h)->unmatched_neighbors; }
+void ora_adaptive_points(void* h, double* xy) {
+  const auto* o = (ora::adaptive::AOracle*)h;
+  for (size_t i = 0; i < o->grid.size(); ++i) { xy[2 * i] = o->grid[i].x; xy[2 * i + 1] = o->grid[i].y; }
+}
+// RHSFunction (GMRES/GMRES.cpp:118-125, 361-364): b = -kappa^2 q(x) exp(i kappa x1).
+void ora_adaptive_rhs(void* h, double* b) {
+  auto* o = (ora::adaptive::AOracle*)h;
+  for (size_t i = 0; i < o->grid.size(); ++i) {
+    const ora::Pt r = o->grid[i];
+    const ora::cd v = -1.0 * o->kappa * o->kappa * o->contrast(r) * std::exp(ora::I * o->kappa * r.x);
+    b[2 * i] = v.real();
+    b[2 * i + 1] = v.imag();
+  }
+}
+void ora_adaptive_matvec(void* h, const double* x, double* y) {
+  ((ora::adaptive::AOracle*)h)->matvec((const ora::cd*)x, (ora::cd*)y);
+}
+void ora_adaptive_gmres_restarted(void* h, const double* b, int m, int restarts, double* x) {
+  auto* o = (ora::adaptive::AOracle*)h;
+  ora::restarted_gmres((int)o->grid.size(), [o](const ora::cd* xx, ora::cd* yy) { o->matvec(xx, yy); },
+                       (const ora::cd*)b, m, restarts, (ora::cd*)x);
 }
 
 }  // extern "C"

@@ -78,6 +78,17 @@ def lib():
         L.ora_adaptive_report.restype = ctypes.c_int
         L.ora_adaptive_report.argtypes = [ctypes.POINTER(OraCfg), ctypes.c_int, ip, ip, ctypes.c_int]
         L.ora_bessel_jy_orders.argtypes = [ctypes.c_int, ctypes.c_double, dp, dp]
+        L.ora_adaptive_create.restype = vp
+        L.ora_adaptive_create.argtypes = [ctypes.POINTER(OraCfg), ctypes.c_int]
+        L.ora_adaptive_destroy.argtypes = [vp]
+        for name in ("ora_adaptive_N", "ora_adaptive_unmatched_neighbors"):
+            getattr(L, name).restype = ctypes.c_int
+            getattr(L, name).argtypes = [vp]
+        for name in ("ora_adaptive_points", "ora_adaptive_rhs"):
+            getattr(L, name).argtypes = [vp, dp]
+        L.ora_adaptive_matvec.argtypes = [vp, dp, dp]
+        L.ora_adaptive_gmres_restarted.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, dp]
+        L.ora_adaptive_set_per_order_bessel.argtypes = [ctypes.c_int]
         L.ora_bessel_jy_orders.restype = None
         L.ora_adaptive_set_per_order_bessel.argtypes = [ctypes.c_int]
         L.ora_adaptive_set_per_order_bessel.restype = None
@@ -191,6 +202,59 @@ class Oracle:
         b = np.ascontiguousarray(b, dtype=np.complex128)
         x = np.empty_like(b)
         lib().ora_gmres_restarted(self._h, _dp(b), m, restarts, _dp(x))
+        return x
+
+
+class AdaptiveOracle:
+    """The adaptive-tree restatement with its full operator: createTree with
+    resolveContrast, the 2:1 level restriction, mixed-level interaction lists,
+    NCA, the ten matvec phases with leaves on several levels and the
+    colleague / fine / separated-fine / coarse near blocks, and the
+    reference's RestartedGMRES (oracle/ls_oracle_adaptive.cpp).
+    treeAdaptivity >= 0: the adaptive tree with epsilonTree 10^-treeAdaptivity
+    (the reference's default path); < 0: the uniform tree of nLevelsUniform
+    levels."""
+
+    def __init__(self, cfg, treeAdaptivity=5, per_order_bessel=False):
+        lib().ora_adaptive_set_per_order_bessel(1 if per_order_bessel else 0)
+        c = make_cfg(cfg)
+        self._h = lib().ora_adaptive_create(ctypes.byref(c), int(treeAdaptivity))
+        if not self._h:
+            raise ValueError("bad configuration")
+        self.N = lib().ora_adaptive_N(self._h)
+        self.unmatched_neighbors = lib().ora_adaptive_unmatched_neighbors(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ora_adaptive_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def points(self):
+        a = np.empty((self.N, 2))
+        lib().ora_adaptive_points(self._h, _dp(a))
+        return a
+
+    def rhs(self):
+        b = np.empty(self.N, dtype=np.complex128)
+        lib().ora_adaptive_rhs(self._h, _dp(b))
+        return b
+
+    def matvec(self, x):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.empty_like(x)
+        lib().ora_adaptive_matvec(self._h, _dp(x), _dp(y))
+        return y
+
+    def gmres_restarted(self, b, m, restarts):
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.empty_like(b)
+        lib().ora_adaptive_gmres_restarted(self._h, _dp(b), int(m), int(restarts), _dp(x))
         return x
 
 
