@@ -768,33 +768,18 @@ static void sub_scaled(std::vector<cd>& v, cd f, const std::vector<cd>& w) {
 // Partially pivoted cross approximation that keeps only the pivots
 // (ACA_only_nodes, ACA.hpp:253-481). Row-first when there are fewer rows
 // than columns, column-first otherwise; ties go to the lowest index.
-int Builder::aca(const std::vector<int>& rows, const std::vector<int>& cols, double eps, std::vector<int>& rb,
-                 std::vector<int>& cb, std::vector<cd>* Ar, HCache& hc) const {
-  const int n1 = (int)rows.size(), n2 = (int)cols.size(), mn = std::min(n1, n2);
+// ACA_only_nodes (GMRES/ACA.hpp:253-481) over a rows x cols block given by
+// its row and column fetchers: pivot search, rank-1 updates, the norm
+// estimate and the stopping rules in the reference's order. Returns the
+// rank; rb / cb get the pivot rows / columns and Ar (if given) the pivot
+// rows of the block, row major rank x n2.
+template <class GetRow, class GetCol>
+static int aca_core(int n1, int n2, double eps, std::vector<int>& rb, std::vector<int>& cb, std::vector<cd>* Ar,
+                    GetRow get_row, GetCol get_col) {
+  const int mn = std::min(n1, n2);
   std::vector<char> rused(n1, 0), cused(n2, 0);
   std::vector<std::vector<cd>> U, V, piv_rows;
   std::vector<cd> row(n2), col(n1), u, v;
-  auto get_row = [&](int r) { std::vector<cd> o(n2); for (int k = 0; k < n2; ++k) o[k] = entry(rows[r], cols[k], hc); return o; };
-  // Columns in one source leaf share the far-field records of every row:
-  // keep them per leaf, indexed by row position.
-  std::vector<std::pair<int, std::vector<const cd*>>> col_leaf;
-  auto get_col = [&](int c) {
-    std::vector<cd> o(n1);
-    const int j = cols[c], leaf = j / rank, node = j % rank;
-    std::vector<const cd*>* P = nullptr;
-    for (auto& e : col_leaf)
-      if (e.first == leaf) P = &e.second;
-    if (!P) {
-      col_leaf.emplace_back(leaf, std::vector<const cd*>(n1, nullptr));
-      P = &col_leaf.back().second;
-    }
-    for (int k = 0; k < n1; ++k) {
-      const cd*& h = (*P)[k];
-      if (!h) h = hc.get(rows[k], leaf);
-      o[k] = scale(rows[k], j, h[node]);
-    }
-    return o;
-  };
   int rk = 0, ri = 0, ci = 0;
   const double thr = eps * std::pow(10, -1.0 * 0);
   if (n1 < n2) {
@@ -886,6 +871,34 @@ int Builder::aca(const std::vector<int>& rows, const std::vector<int>& cols, dou
       for (int b = 0; b < n2; ++b) (*Ar)[(size_t)a * n2 + b] = piv_rows[a][b];
   }
   return rk;
+}
+
+
+int Builder::aca(const std::vector<int>& rows, const std::vector<int>& cols, double eps, std::vector<int>& rb,
+                 std::vector<int>& cb, std::vector<cd>* Ar, HCache& hc) const {
+  const int n1 = (int)rows.size(), n2 = (int)cols.size();
+  auto get_row = [&](int r) { std::vector<cd> o(n2); for (int k = 0; k < n2; ++k) o[k] = entry(rows[r], cols[k], hc); return o; };
+  // Columns in one source leaf share the far-field records of every row:
+  // keep them per leaf, indexed by row position.
+  std::vector<std::pair<int, std::vector<const cd*>>> col_leaf;
+  auto get_col = [&](int c) {
+    std::vector<cd> o(n1);
+    const int j = cols[c], leaf = j / rank, node = j % rank;
+    std::vector<const cd*>* P = nullptr;
+    for (auto& e : col_leaf)
+      if (e.first == leaf) P = &e.second;
+    if (!P) {
+      col_leaf.emplace_back(leaf, std::vector<const cd*>(n1, nullptr));
+      P = &col_leaf.back().second;
+    }
+    for (int k = 0; k < n1; ++k) {
+      const cd*& h = (*P)[k];
+      if (!h) h = hc.get(rows[k], leaf);
+      o[k] = scale(rows[k], j, h[node]);
+    }
+    return o;
+  };
+  return aca_core(n1, n2, eps, rb, cb, Ar, get_row, get_col);
 }
 
 void Builder::geometry() {

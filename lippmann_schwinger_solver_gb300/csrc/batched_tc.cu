@@ -18,10 +18,14 @@
 //
 // Precision: FP32 operands through TF32 tensor cores in three products,
 // hi*hi + hi*lo + lo*hi with hi the TF32 truncation of a value and lo the
-// FP32 remainder (lo*lo, about 2^-22 relative, is dropped), accumulated in
-// FP32 in tensor memory: the accuracy of the FP32 operator.
+// FP32 remainder (lo*lo, about 2^-22 relative, is dropped). The tensor
+// core's FP32 accumulation is not round-to-nearest over long sums (measured:
+// 3x the error of the CUDA-core FP32 form on blocks of ~1,000 columns), so
+// each accumulator covers kChunkStages stages (128 real columns) and is then
+// promoted into FP32 registers, round-to-nearest; two tensor-memory slots
+// alternate so that the tensor core keeps working while a slot is read.
 //
-// Kernel structure (tc_gemm_kernel): a persistent grid, 128 threads per CTA
+// Kernel structure (tc_gemm_kernel): a persistent grid of two CTAs per SM, 128 threads per CTA
 // (four warps, one per 32-lane quarter of tensor memory). Blocks of the
 // phase are dealt round-robin. Per block the K columns are walked in stages
 // of 16 complex columns through two shared-memory buffers: all threads
@@ -29,9 +33,11 @@
 // copy the operator stage (split hi/lo); one thread issues the 12 MMAs of a
 // stage (4 K-steps x 3 products) and commits them to the buffer's mbarrier,
 // which the threads wait on before they refill that buffer two stages later.
-// After the last stage the four warps read the accumulator out of tensor
-// memory (tcgen05.ld 32x32b) and write, add to, or combine it into the
-// destination. Every mbarrier wait is bounded; a wait that gives up sets
+// The last stage of a chunk is also committed to its accumulator slot's
+// mbarrier; before a slot is reused the four warps read it out of tensor
+// memory (tcgen05.ld 32x32b, each warp its 32 lanes) and add it to their
+// registers. After the last chunk they write, add to, or combine the
+// registers into the destination. Every mbarrier wait is bounded; a wait that gives up sets
 // the error flag, the CTA skips its remaining work and still frees its
 // tensor memory.
 
@@ -54,7 +60,9 @@ constexpr int kStageCols = 16;                 // complex columns per stage (32 
 constexpr int kRowGroupBytes = 8 * 128;        // stride between 8-row core-matrix groups (SBO)
 constexpr int kXBytes = 128 * 128;             // one plane (hi or lo) of the 128-row operand
 constexpr long long kWaitLimit = 20000000;     // mbarrier polls before a wait gives up
-constexpr int kTmemCols = 256;
+constexpr int kMaxRows = 64;                   // block rows per MMA tile (N <= 64; larger blocks are split)
+constexpr int kChunkStages = 4;                // stages accumulated in tensor memory before promotion
+constexpr int kTmemCols = 2 * kMaxRows;        // two accumulator slots
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -74,7 +82,13 @@ __host__ __device__ __forceinline__ int canon(int row, int cc) {
   return ((row & 7) * 16 + (row >> 3) * kRowGroupBytes + (cc >> 1) * 128 + (cc & 1) * 8) >> 3;
 }
 
-__device__ __forceinline__ float tf32_hi(float v) { return __uint_as_float(__float_as_uint(v) & 0xFFFFE000u); }
+// v rounded to the nearest TF32 value (10 explicit mantissa bits; ties away
+// from zero). Both parts of the split are rounded, so that the tensor
+// core's truncation of its TF32 inputs changes neither: v - hi - lo is then
+// below 2^-22 |v|.
+__device__ __forceinline__ float tf32_rn(float v) {
+  return __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
+}
 
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile("{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p; }" ::
@@ -98,7 +112,7 @@ struct TcBlock {
   long long a_off;  // first float2 of the block's operator stages (stage s at a_off + s * npad * 16)
   int i_off;        // gather list: column k at idx[i_off + k]
   int o_off;        // output rows: row n at out[o_off + n]
-  int rows;         // block rows (<= npad)
+  int rows;         // block rows (<= npad <= kMaxRows)
   int npad;         // rows padded to a multiple of 16 (MMA N)
   int K;            // complex columns
   int nst;          // stages of kStageCols columns
@@ -108,14 +122,15 @@ namespace {
 
 // mode 0: dst rows = D; 1: dst rows += D; 2 (near field and output):
 // y = P + s D + x with s = kappa^2 q of the row (find_phi) or 1.
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 2)
     tc_gemm_kernel(const TcBlock* __restrict__ blocks, int n_blocks, const float2* __restrict__ A,
                    const int* __restrict__ idx, const int* __restrict__ out, const float2* __restrict__ src,
                    float2* __restrict__ dst, int mode, const float2* __restrict__ P, const float* __restrict__ kq,
                    int find_phi, int npad_max, unsigned* __restrict__ err) {
   pdl_enter();
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t bar[2];
+  __shared__ uint64_t bar[2];     // per stage buffer: its MMAs completed
+  __shared__ uint64_t accbar[2];  // per accumulator slot: its chunk completed
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   const int t = threadIdx.x, warp = t >> 5;
@@ -129,6 +144,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (t == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar[0])), "r"(1));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar[1])), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&accbar[0])), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&accbar[1])), "r"(1));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
   }
@@ -142,108 +159,168 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // 2-column core-matrix slice per step, so their shared stores hit 32
   // distinct banks; their loads are 2 x 64 contiguous bytes.
   const int l16 = t & 15, hw = t >> 4, j8 = l16 & 7, cpar = l16 >> 3;
-  long long g = 0;  // stages issued by this CTA (buffer g & 1, use g >> 1)
+  long long g = 0;   // stages issued by this CTA (buffer g & 1, use g >> 1)
+  long long gc = 0;  // chunks issued by this CTA (accumulator slot gc & 1, use gc >> 1)
+  float acc[kMaxRows];
+  // acc[n] += the accumulator slot's column n (this thread's lane).
+  auto promote = [&](int slot, int npad) {
+#pragma unroll
+    for (int c0 = 0; c0 < kMaxRows; c0 += 8) {
+      if (c0 < npad) {
+        uint32_t r[8];
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                     : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(slot * kMaxRows + c0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[c0 + i] += __uint_as_float(r[i]);
+      }
+    }
+  };
   for (int b = blockIdx.x; b < n_blocks; b += gridDim.x) {
     const TcBlock blk = blocks[b];
     const uint32_t idesc = idesc_base | ((uint32_t)(blk.npad >> 3) << 17);
+#pragma unroll
+    for (int n = 0; n < kMaxRows; ++n) acc[n] = 0.f;
+    const long long gc0 = gc;
+    const int nchunks = (blk.nst + kChunkStages - 1) / kChunkStages;
+    // Loads of stage st: 8 gathered right-hand-side values and up to 4
+    // operator vectors per thread. Stage st + 1's loads are issued before
+    // stage st is stored, so every thread has two stages of loads in flight.
+    float2 xv[8], xn[8];
+    float4 av[4], an[4];
+    auto load_stage = [&](int st, float2* x, float4* a) {
+      const int k0 = st * kStageCols;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int ci = hw * 8 + i;
+        const int jj = (ci & 7) * 8 + j8, cc = 2 * (ci >> 3) + cpar;
+        const int k = k0 + cc;
+        x[i] = make_float2(0.f, 0.f);
+        if (k < blk.K) x[i] = ld_chain(src + (size_t)__ldg(idx + blk.i_off + k) * 64 + jj);
+      }
+      // npad rows x 16 complex columns in the canonical layout: npad * 8 <= 512 float4.
+      const float4* As = reinterpret_cast<const float4*>(A + blk.a_off + (long long)st * blk.npad * kStageCols);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int u = t + q * kTcThreads;
+        a[q] = u < blk.npad * 8 ? __ldcs(As + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    };
+    if (blk.nst > 0) load_stage(0, xv, av);
     for (int st = 0; st < blk.nst; ++st, ++g) {
       const int buf = (int)(g & 1);
+      const long long G = gc0 + st / kChunkStages;  // chunk of this stage
+      const bool chunk_start = st % kChunkStages == 0;
+      const bool chunk_end = st % kChunkStages == kChunkStages - 1 || st == blk.nst - 1;
       uint8_t* base = smem + buf * buf_bytes;
       float2* Xh = reinterpret_cast<float2*>(base);
       float2* Xl = reinterpret_cast<float2*>(base + kXBytes);
       float4* Ah = reinterpret_cast<float4*>(base + 2 * kXBytes);
       float4* Al = reinterpret_cast<float4*>(base + 2 * kXBytes + a_plane);
+      if (st + 1 < blk.nst) load_stage(st + 1, xn, an);
       if (g >= 2 && !mbar_wait(&bar[buf], (uint32_t)(((g >> 1) - 1) & 1))) {
         atomicOr(err, 1u);
         abort_flag = 1;
       }
       __syncthreads();
       if (abort_flag) break;
-      // Gathered right-hand sides: columns k0 .. k0 + 15 of the block.
-      const int k0 = st * kStageCols;
-#pragma unroll 2
+#pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int ci = hw * 8 + i;
         const int jj = (ci & 7) * 8 + j8, cc = 2 * (ci >> 3) + cpar;
-        const int k = k0 + cc;
-        float2 v = make_float2(0.f, 0.f);
-        if (k < blk.K) v = ld_chain(src + (size_t)__ldg(idx + blk.i_off + k) * 64 + jj);
-        const float hx = tf32_hi(v.x), hy = tf32_hi(v.y);
+        const float2 v = xv[i];
+        const float hx = tf32_rn(v.x), hy = tf32_rn(v.y);
+        const float lx = tf32_rn(v.x - hx), ly = tf32_rn(v.y - hy);
         const int o_re = canon(jj, cc), o_im = canon(64 + jj, cc);
         Xh[o_re] = make_float2(hx, hy);
-        Xl[o_re] = make_float2(v.x - hx, v.y - hy);
+        Xl[o_re] = make_float2(lx, ly);
         Xh[o_im] = make_float2(hy, -hx);
-        Xl[o_im] = make_float2(v.y - hy, hx - v.x);
+        Xl[o_im] = make_float2(ly, -lx);
       }
-      // Operator stage: npad rows x 16 complex columns, already in the
-      // canonical layout.
-      const float4* As = reinterpret_cast<const float4*>(A + blk.a_off + (long long)st * blk.npad * kStageCols);
-      for (int u = t; u < blk.npad * 8; u += kTcThreads) {
-        const float4 v = __ldcs(As + u);
-        const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-        Ah[u] = h;
-        Al[u] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int u = t + q * kTcThreads;
+        if (u < blk.npad * 8) {
+          const float4 v = av[q];
+          const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+          Ah[u] = h;
+          Al[u] = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
+        }
       }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) xv[i] = xn[i];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) av[q] = an[q];
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      // Slot G & 1 still holds chunk G - 2 of this block: add it to the
+      // registers before the slot is reused (its commit is the slot's latest).
+      if (chunk_start && G - 2 >= gc0) {
+        if (!mbar_wait(&accbar[G & 1], (uint32_t)(((G - 2) >> 1) & 1))) {
+          atomicOr(err, 1u);
+          abort_flag = 1;
+        } else {
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          promote((int)(G & 1), blk.npad);
+        }
+      }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
+      if (abort_flag) break;
       if (t == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t xh = smem_u32(Xh), xl = smem_u32(Xl), ah = smem_u32(Ah), al = smem_u32(Al);
+        const uint32_t dt = tmem + (uint32_t)((G & 1) * kMaxRows);
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks) {
           const uint32_t o = ks * 256;
           const uint64_t dxh = sdesc(xh + o, 128, kRowGroupBytes), dxl = sdesc(xl + o, 128, kRowGroupBytes);
           const uint64_t dah = sdesc(ah + o, 128, kRowGroupBytes), dal = sdesc(al + o, 128, kRowGroupBytes);
-          mma_tf32(tmem, dxh, dah, idesc, (st > 0 || ks > 0) ? 1u : 0u);
-          mma_tf32(tmem, dxh, dal, idesc, 1u);
-          mma_tf32(tmem, dxl, dah, idesc, 1u);
+          mma_tf32(dt, dxh, dah, idesc, (!chunk_start || ks > 0) ? 1u : 0u);
+          mma_tf32(dt, dxh, dal, idesc, 1u);
+          mma_tf32(dt, dxl, dah, idesc, 1u);
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_u32(&bar[buf]))
                      : "memory");
+        if (chunk_end)
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&accbar[G & 1]))
+                       : "memory");
       }
     }
     if (abort_flag) break;
-    // Accumulator complete once the block's last stage has committed (a
-    // block without columns has none and contributes zeros).
-    const bool empty = blk.nst == 0;
-    const long long gl = g - 1;
-    if (!empty && !mbar_wait(&bar[gl & 1], (uint32_t)((gl >> 1) & 1))) {
-      atomicOr(err, 1u);
-      abort_flag = 1;
+    gc = gc0 + nchunks;
+    // The last one or two chunks are still in tensor memory.
+    for (long long G = (gc - 2 > gc0 ? gc - 2 : gc0); G < gc; ++G) {
+      if (!mbar_wait(&accbar[G & 1], (uint32_t)((G >> 1) & 1))) {
+        atomicOr(err, 1u);
+        abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      promote((int)(G & 1), blk.npad);
     }
     __syncthreads();
     if (abort_flag) break;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int m = t, part = m >> 6, j = m & 63;
-    for (int c0 = 0; c0 < blk.rows; c0 += 8) {
-      uint32_t r[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (!empty) {
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                     : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      }
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int n = c0 + i;
-        if (n >= blk.rows) break;
-        const int orow = __ldg(out + blk.o_off + n);
-        const size_t e = ((size_t)orow * 64 + j) * 2 + part;
-        float* dp = reinterpret_cast<float*>(dst) + e;
-        const float v = __uint_as_float(r[i]);
-        if (mode == 0) {
-          *dp = v;
-        } else if (mode == 1) {
-          *dp = ld_chain(dp) + v;
-        } else {
-          const float p = ld_chain(reinterpret_cast<const float*>(P) + e);
-          if (find_phi)
-            *dp = p + __ldg(kq + orow) * v + ld_chain(reinterpret_cast<const float*>(src) + e);
-          else
-            *dp = p + v;
-        }
+    for (int n = 0; n < kMaxRows; ++n) {
+      if (n >= blk.rows) break;
+      const int orow = __ldg(out + blk.o_off + n);
+      const size_t e = ((size_t)orow * 64 + j) * 2 + part;
+      float* dp = reinterpret_cast<float*>(dst) + e;
+      const float v = acc[n];
+      if (mode == 0) {
+        *dp = v;
+      } else if (mode == 1) {
+        *dp = ld_chain(dp) + v;
+      } else {
+        const float p = ld_chain(reinterpret_cast<const float*>(P) + e);
+        if (find_phi)
+          *dp = p + __ldg(kq + orow) * v + ld_chain(reinterpret_cast<const float*>(src) + e);
+        else
+          *dp = p + v;
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -255,7 +332,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 // Far-field phase -> tensor-core form: one warp per tile writes its
-// elements, conjugated, into the block's canonical stages.
+// elements, conjugated, into the canonical stages of the part of its block
+// that holds the row (tile_block: the block's first part; parts are
+// consecutive, kMaxRows rows each).
 __global__ void tc_build_far_kernel(const GemvTile* __restrict__ tiles, int n_tiles, const int* __restrict__ tile_block,
                                     const int* __restrict__ tile_row0, const TcBlock* __restrict__ blocks,
                                     const float2* __restrict__ A32, float2* __restrict__ Atc) {
@@ -263,17 +342,18 @@ __global__ void tc_build_far_kernel(const GemvTile* __restrict__ tiles, int n_ti
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n_tiles; w += nw) {
     const GemvTile tl = tiles[w];
-    const TcBlock blk = blocks[tile_block[w]];
     const int R = 32 >> tl.log2s, S = 1 << tl.log2s;
     const int r = lane % R, s = lane / R;
     if (r >= tl.rows) continue;
     const int row = tile_row0[w] + r;
+    const TcBlock blk = blocks[tile_block[w] + row / kMaxRows];
+    const int prow = row % kMaxRows;
     for (int q = 0; q < tl.qmax; ++q) {
       const int k = q * S + s;
       if (k >= blk.K) break;
       const float2 a = A32[tl.a_off + 32LL * q + lane];
       const int st = k / kStageCols, cc = k % kStageCols;
-      Atc[blk.a_off + (long long)st * blk.npad * kStageCols + canon(row, cc)] = make_float2(a.x, -a.y);
+      Atc[blk.a_off + (long long)st * blk.npad * kStageCols + canon(prow, cc)] = make_float2(a.x, -a.y);
     }
   }
 }
@@ -357,33 +437,33 @@ cudaError_t build_far(TcOperator& T, const GemvPhase& h, const DevPhase<float2>&
   out.accumulate = d32.accumulate;
   out.entries = d32.entries;
   const int nb = (int)h.blk_rows.size();
-  out.n_blocks = nb;
-  if (nb == 0 || d32.n_tiles == 0) {
-    out.n_blocks = 0;
-    return cudaSuccess;
-  }
-  std::vector<TcBlock> blocks(nb);
+  out.n_blocks = 0;
+  if (nb == 0 || d32.n_tiles == 0) return cudaSuccess;
+  // Blocks of more than kMaxRows rows become several parts with the same
+  // gather list.
+  std::vector<TcBlock> blocks;
   std::vector<int> tile_block(h.tiles.size()), tile_row0(h.tiles.size());
   long long a = 0;
   for (int b = 0; b < nb; ++b) {
     const int t0 = h.blk_tile0[b], t1 = h.blk_tile0[b + 1];
     const int rows = h.blk_rows[b], K = h.blk_K[b];
-    if (rows > kTmemCols) {
-      err = "tensor-core form: a block has " + std::to_string(rows) + " rows (at most 256)";
-      return cudaErrorInvalidValue;
-    }
-    const int npad = std::max(16, (rows + 15) / 16 * 16);
     const int nst = (K + kStageCols - 1) / kStageCols;
-    blocks[b] = TcBlock{a, (int)h.tiles[t0].i_off, h.tiles[t0].row_base, rows, npad, K, nst};
-    out.npad_max = std::max(out.npad_max, npad);
-    a += (long long)nst * npad * kStageCols;
+    const int first = (int)blocks.size();
+    for (int r0 = 0; r0 < rows; r0 += kMaxRows) {
+      const int pr = std::min(kMaxRows, rows - r0);
+      const int npad = std::max(16, (pr + 15) / 16 * 16);
+      blocks.push_back(TcBlock{a, (int)h.tiles[t0].i_off, h.tiles[t0].row_base + r0, pr, npad, K, nst});
+      out.npad_max = std::max(out.npad_max, npad);
+      a += (long long)nst * npad * kStageCols;
+    }
     int r0 = 0;
     for (int tt = t0; tt < t1; ++tt) {
-      tile_block[tt] = b;
+      tile_block[tt] = first;
       tile_row0[tt] = r0;
       r0 += h.tiles[tt].rows;
     }
   }
+  out.n_blocks = (int)blocks.size();
   out.a_elems = a;
   int *dtb = nullptr, *dtr = nullptr;
   cudaError_t e = dalloc(T, &out.A, (size_t)a);
@@ -407,7 +487,7 @@ cudaError_t build_far(TcOperator& T, const GemvPhase& h, const DevPhase<float2>&
 cudaError_t launch_tc(const TcOperator& T, const TcPhase& ph, const float2* src, float2* dst, int mode,
                       const float2* P, const float* kq, int find_phi, cudaStream_t s) {
   if (ph.n_blocks == 0) return cudaSuccess;
-  const int grid = std::min(ph.n_blocks, T.sms);
+  const int grid = std::min(ph.n_blocks, 2 * T.sms);  // two CTAs per SM (96 KB shared memory, 128 TMEM columns each)
   return launch_pdl(tc_gemm_kernel, grid, kTcThreads, (size_t)smem_for(ph.npad_max), s, (const TcBlock*)ph.blocks,
                     ph.n_blocks, (const float2*)ph.A, ph.idx, ph.out, src, dst, mode, P, kq, find_phi, ph.npad_max,
                     T.err);
@@ -443,12 +523,16 @@ bool dev_enable_tc(DevOperator& d, const HostOperator& h, std::string& err) {
   if (e == cudaSuccess) {
     TcPhase& nr = T->near;
     const int K = 9 * d.rank;
+    if (d.rank > kMaxRows) {
+      err = "tensor-core form: more than 64 points per leaf";
+      e = cudaErrorInvalidValue;
+    }
     nr.npad_max = std::max(16, (d.rank + 15) / 16 * 16);
     const int nst = (K + kStageCols - 1) / kStageCols;
     nr.a_elems = (long long)nst * nr.npad_max * kStageCols;
     nr.n_blocks = d.n_leaves;
     nr.entries = 9LL * d.rank * d.rank;
-    e = dalloc(*T, &nr.A, (size_t)nr.a_elems);
+    if (e == cudaSuccess) e = dalloc(*T, &nr.A, (size_t)nr.a_elems);
     if (e == cudaSuccess) e = dalloc(*T, &nr.blocks, (size_t)d.n_leaves);
     if (e == cudaSuccess) e = dalloc(*T, &T->near_idx, (size_t)d.n_leaves * K);
     if (e == cudaSuccess) e = dalloc(*T, &T->near_out, (size_t)d.N);
