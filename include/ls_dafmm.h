@@ -70,6 +70,16 @@ typedef struct {
   double bump_cy[LS_MAX_BUMPS];
   double bump_a[LS_MAX_BUMPS];
   double bump_w[LS_MAX_BUMPS];
+  /* Tree: 0 (zero-initialised) = the uniform quadtree of nLevelsUniform
+   * levels (createUniformTree, G_FMM2DTree.hpp:917); 1 = the adaptive
+   * quadtree of the reference's default path (createAdaptiveTree +
+   * makeLevelRestriction_Tree, GMRES/GMRES.cpp:165-166): boxes split until
+   * q is resolved to 10^-treeAdaptivity and no box spans more than one
+   * wavelength, then 2:1 balanced. Adaptive operators support the FP64 and
+   * FP32 matvecs and the GMRES solvers; the batched, allocation-free,
+   * interpolation and network entry points return LS_E_STATE for them. */
+  int tree_adaptive;
+  int treeAdaptivity;
 } ls_config;
 
 typedef struct {

@@ -87,6 +87,8 @@ class _Config(ctypes.Structure):
         ("bump_cy", ctypes.c_double * MAX_BUMPS),
         ("bump_a", ctypes.c_double * MAX_BUMPS),
         ("bump_w", ctypes.c_double * MAX_BUMPS),
+        ("tree_adaptive", ctypes.c_int),
+        ("treeAdaptivity", ctypes.c_int),
     ]
 
 
@@ -137,11 +139,13 @@ class Config:
     L: float = 1.0
     kappa: float = 10.0
     bumps: tuple = ()  # ((cx, cy, a, w), ...) for Qchoice 6
+    tree_adaptive: int = 0   # 1: the reference's adaptive quadtree (createAdaptiveTree + 2:1 balance)
+    treeAdaptivity: int = 5  # adaptive: boxes split until q is resolved to 10^-treeAdaptivity
 
     def to_c(self):
         c = _Config()
         for f in ("nCones_LFR", "nChebNodes", "yes2DFMM", "TOL_POW", "degreeOfBases", "nLevelsUniform",
-                  "Qchoice", "findPhi", "reference_rounding"):
+                  "Qchoice", "findPhi", "reference_rounding", "tree_adaptive", "treeAdaptivity"):
             setattr(c, f, int(getattr(self, f)))
         c.L = float(self.L)
         c.kappa = float(self.kappa)

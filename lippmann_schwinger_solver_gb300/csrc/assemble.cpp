@@ -30,8 +30,11 @@
 #include <cstring>
 #include <deque>
 #include <limits>
+#include <map>
 #include <memory>
 #include <mutex>
+#include <set>
+#include <tuple>
 #include <unordered_map>
 #include <vector>
 
@@ -1749,10 +1752,16 @@ bool Builder::run(HostOperator& op, std::string& err) {
   return true;
 }
 
+#include "assemble_adaptive.h"
+
 }  // namespace
 
 bool assemble(const ls_config& cfg, HostOperator& op, std::string& err) {
   try {
+    if (cfg.tree_adaptive) {
+      AdaptiveBuilder b(cfg);
+      return b.run(op, err);
+    }
     Builder b(cfg);
     return b.run(op, err);
   } catch (const std::bad_alloc&) {

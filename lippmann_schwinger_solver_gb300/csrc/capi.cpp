@@ -74,6 +74,12 @@ ls_status cuda_fail(cudaError_t e, const char* where) {
   return fail(LS_E_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// Entry points built on the uniform tree's leaf grid and colleague table.
+bool adaptive(const ls_op* op) { return op->host.generic_near; }
+ls_status adaptive_refused(const char* who) {
+  return fail(LS_E_STATE, std::string(who) + ": not available for operators on adaptive trees");
+}
+
 }  // namespace
 
 extern "C" {
@@ -113,6 +119,7 @@ ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
   for (auto& p : op->host.up) drop(p);
   for (auto& p : op->host.down) drop(p);
   drop(op->host.m2l);
+  drop(op->host.nearph);
   *out = op;
   return LS_OK;
 }
@@ -150,16 +157,17 @@ ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
     for (auto& p : h.down) far += p.entries();
   }
   o->far_entries = far;
-  o->near_entries = 9LL * h.rank * h.rank;
+  o->near_entries = h.generic_near ? (op->on_device ? d.nearph.entries : h.nearph.entries()) : 9LL * h.rank * h.rank;
   // Algorithmic bytes of one FP64 matvec: every far block once, the shared
   // near blocks once, x read and y written once, every skeleton charge and
   // potential written and read once, kappa^2 q read once.
   const long long sk = (h.charges_len - h.N) + (h.pots_len - h.N);
   o->matvec_bytes = 16LL * far + 16LL * o->near_entries + 16LL * 2 * h.N + 16LL * 2 * sk + 8LL * h.N;
   long long nnz_near = 0;
-  for (int t = 0; t < h.n_leaves; ++t)
-    for (int q = 0; q < 9; ++q) nnz_near += h.colleague[(size_t)t * 9 + q] >= 0;
-  o->matvec_flops = 8LL * far + 8LL * nnz_near * h.rank * h.rank;
+  if (!h.generic_near)
+    for (int t = 0; t < h.n_leaves; ++t)
+      for (int q = 0; q < 9; ++q) nnz_near += h.colleague[(size_t)t * 9 + q] >= 0;
+  o->matvec_flops = 8LL * far + (h.generic_near ? 8LL * o->near_entries : 8LL * nnz_near * h.rank * h.rank);
   o->device_bytes = d.device_bytes;
   o->assemble_seconds = h.assemble_seconds;
   for (int i = 0; i < LS_ASSEMBLE_STAGES; ++i) o->assemble_stage_seconds[i] = h.stage_seconds[i];
@@ -248,6 +256,7 @@ ls_status ls_matvec_f32(ls_op* op, const double* x, double* y, void* stream) {
 
 ls_status ls_matvec_noalloc(ls_op* op, const double* x, double* y, void* stream) {
   if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_noalloc: null argument");
+  if (adaptive(op)) return adaptive_refused("ls_matvec_noalloc");
   const long long need = op->host.charges_len + op->host.pots_len;
   if (need > LS_STATIC_SCRATCH_ELEMS)
     return fail(LS_E_INVALID, "ls_matvec_noalloc: operator needs " + std::to_string(need) +
@@ -370,6 +379,7 @@ ls_status tc_status(ls_op* op, const char* who) {
 
 ls_status ls_matvec_f32_many(ls_op* op, int nrhs, const double* X, double* Y) {
   if (!op || !X || !Y || nrhs < 1) return fail(LS_E_INVALID, "ls_matvec_f32_many: bad argument");
+  if (adaptive(op)) return adaptive_refused("ls_matvec_f32_many");
   if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_f32_many: operator was assembled without a device");
   if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_matvec_f32_many: call ls_op_enable_f32 first");
   DevOperator& d = op->dev;
@@ -392,6 +402,7 @@ ls_status ls_matvec_f32_many(ls_op* op, int nrhs, const double* X, double* Y) {
 ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float* ms) {
   if (!op || !ms || iters < 1 || warmup < 0 || (width != 8 && width != 64))
     return fail(LS_E_INVALID, "ls_time_block_apply: bad argument");
+  if (adaptive(op)) return adaptive_refused("ls_time_block_apply");
   if (!op->on_device) return fail(LS_E_STATE, "ls_time_block_apply: operator was assembled without a device");
   if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_time_block_apply: call ls_op_enable_f32 first");
   cudaSetDevice(op->dev.device);
@@ -407,6 +418,7 @@ ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float
 ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_outer, int inner_iter, double tol,
                                  double* X, int* n_matvec, double* rel_residuals) {
   if (!op || !B || !X) return fail(LS_E_INVALID, "ls_gmres_mixed_batched: null argument");
+  if (adaptive(op)) return adaptive_refused("ls_gmres_mixed_batched");
   if (!op->on_device) return fail(LS_E_STATE, "ls_gmres_mixed_batched: operator was assembled without a device");
   if (nrhs < 1 || max_outer < 1 || inner_iter < 1)
     return fail(LS_E_INVALID, "ls_gmres_mixed_batched: nrhs and iteration counts must be >= 1");
@@ -539,6 +551,7 @@ long ls_op_skeleton_dump(const ls_op* op, int* buf, long cap) {
 
 ls_status ls_op_precomputations(const ls_op* op, double* M, double* near) {
   if (!op) return fail(LS_E_INVALID, "ls_op_precomputations: null argument");
+  if (adaptive(op)) return adaptive_refused("ls_op_precomputations");
   if (M) std::memcpy(M, op->host.M.data(), op->host.M.size() * sizeof(cd));
   if (near) std::memcpy(near, op->host.nearB.data(), op->host.nearB.size() * sizeof(cd));
   return LS_OK;
@@ -547,6 +560,7 @@ ls_status ls_op_precomputations(const ls_op* op, double* M, double* near) {
 ls_status ls_op_interpolate(const ls_op* op, int npts, const double* xy, const double* phi, double* psi) {
   if (!op || npts < 0 || (npts > 0 && (!xy || !phi || !psi)))
     return fail(LS_E_INVALID, "ls_op_interpolate: bad argument");
+  if (adaptive(op)) return adaptive_refused("ls_op_interpolate");
   const HostOperator& h = op->host;
   const double L = h.cfg.L;
   for (int i = 0; i < npts; ++i)
@@ -697,6 +711,7 @@ bool valid_grid(int g) { return g >= 8 && g <= 1024 && (g & (g - 1)) == 0; }
 
 ls_status ls_op_grid_weights(const ls_op* op, int grid, float* w, int* leaf) {
   if (!op || !w || !leaf) return fail(LS_E_INVALID, "ls_op_grid_weights: null argument");
+  if (adaptive(op)) return adaptive_refused("ls_op_grid_weights");
   if (!valid_grid(grid)) return fail(LS_E_INVALID, "ls_op_grid_weights: grid must be a power of two in [8, 1024]");
   std::vector<float> hw;
   std::vector<int> hl;
@@ -708,6 +723,7 @@ ls_status ls_op_grid_weights(const ls_op* op, int grid, float* w, int* leaf) {
 
 ls_status ls_op_grid_contrast(const ls_op* op, int grid, float* q) {
   if (!op || !q) return fail(LS_E_INVALID, "ls_op_grid_contrast: null argument");
+  if (adaptive(op)) return adaptive_refused("ls_op_grid_contrast");
   if (!valid_grid(grid)) return fail(LS_E_INVALID, "ls_op_grid_contrast: grid must be a power of two in [8, 1024]");
   std::vector<float> hq;
   grid_contrast(op->host.cfg, grid, hq);
@@ -717,6 +733,7 @@ ls_status ls_op_grid_contrast(const ls_op* op, int grid, float* q) {
 
 ls_status ls_op_grid_sample(ls_op* op, int grid, int nvec, const double* x, float* out, void* stream) {
   if (!op || !x || !out) return fail(LS_E_INVALID, "ls_op_grid_sample: null argument");
+  if (adaptive(op)) return adaptive_refused("ls_op_grid_sample");
   if (!op->on_device) return fail(LS_E_STATE, "ls_op_grid_sample: operator was assembled without a device");
   if (!valid_grid(grid) || nvec < 1 || nvec > 65535)
     return fail(LS_E_INVALID, "ls_op_grid_sample: bad grid or vector count");
@@ -736,6 +753,7 @@ ls_status ls_op_grid_sample(ls_op* op, int grid, int nvec, const double* x, floa
 ls_status ls_fgmres_nn(ls_op* op, ls_fno* net, const double* b, int flags, int max_outer, int inner_iter, double tol,
                        double* x, double* history, ls_nn_report* report) {
   if (!op || !b || !x) return fail(LS_E_INVALID, "ls_fgmres_nn: null argument");
+  if (adaptive(op)) return adaptive_refused("ls_fgmres_nn");
   if (!op->on_device) return fail(LS_E_STATE, "ls_fgmres_nn: operator was assembled without a device");
   if (max_outer < 1 || inner_iter < 1 || flags < 0 || flags > (LS_NN_GUESS | LS_NN_PRECOND))
     return fail(LS_E_INVALID, "ls_fgmres_nn: bad iteration counts or flags");

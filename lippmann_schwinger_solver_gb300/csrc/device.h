@@ -40,6 +40,12 @@ struct DevOperator {
   int N = 0, n_leaves = 0, rank = 0;
   int find_phi = 1;
   long long charges_len = 0, pots_len = 0;
+  // Adaptive trees: the near field as a gather-GEMV phase accumulating into
+  // P[0:N), then y = P[0:N) (HostOperator::generic_near).
+  bool generic_near = false;
+  DevPhase<double2> nearph;
+  DevPhase<float2> nearph32;
+  DevPhase<float4> nearph_df;
   // FP64 operator
   std::vector<DevPhase<double2>> up, down;
   DevPhase<double2> m2l;

@@ -77,6 +77,12 @@ struct HostOperator {
   GemvPhase m2l;                     // all levels in one launch
   long long m2l_rows = 0;            // potential rows written by M2L
   std::vector<GemvPhase> down;       // L2L, coarse to fine
+  // Adaptive trees: the near field as one more accumulating phase into the
+  // leaf potentials P[0:N) (diag(kappa^2 q) B of every neighbour, + I on the
+  // self block), after which the output is P[0:N). Uniform trees use the
+  // factored colleague blocks instead (generic_near false).
+  GemvPhase nearph;
+  bool generic_near = false;
   std::vector<int> skeleton_dump;
   int max_rank = 0;
   double assemble_seconds = 0.0;

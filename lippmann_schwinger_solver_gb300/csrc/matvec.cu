@@ -319,6 +319,9 @@ __global__ void near_transpose32_kernel(const double2* __restrict__ B, float2* _
 
 // First kernel of a matvec: S[0:n) = x (converted to the operator's type)
 // and P = 0.
+__device__ __forceinline__ double2 conv_out(double2 v, double2*) { return v; }
+__device__ __forceinline__ double2 conv_out(float2 v, double2*) { return make_double2((double)v.x, (double)v.y); }
+__device__ __forceinline__ float2 conv_out(float2 v, float2*) { return v; }
 __device__ __forceinline__ double2 conv(double2 v, double2*) { return v; }
 __device__ __forceinline__ float2 conv(double2 v, float2*) { return make_float2((float)v.x, (float)v.y); }
 __device__ __forceinline__ float2 conv(float2 v, float2*) { return v; }
@@ -334,6 +337,16 @@ __global__ void load_zero_kernel(const X* __restrict__ x, C* __restrict__ S, lon
   z.x = 0;
   z.y = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < np; i += stride) P[i] = z;
+}
+
+// y = P[0:n) (adaptive trees: the near-field phase has accumulated into P).
+template <class C, class Y>
+__global__ void copy_out_kernel(const C* __restrict__ P, Y* __restrict__ y, int n) {
+  pdl_enter();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const C v = ld_chain(P + i);
+    y[i] = conv_out(v, (Y*)nullptr);
+  }
 }
 
 __global__ void d2f_kernel(const double2* __restrict__ a, float2* __restrict__ b, long long n) {
@@ -425,6 +438,8 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
   if (!upload_phase(h.m2l, d.m2l, tot, err)) return false;
   d.down.resize(h.down.size());
   for (size_t i = 0; i < h.down.size(); ++i) if (!upload_phase(h.down[i], d.down[i], tot, err)) return false;
+  d.generic_near = h.generic_near;
+  if (h.generic_near && !upload_phase(h.nearph, d.nearph, tot, err)) return false;
   if (!dmalloc(&d.S, (size_t)h.charges_len, tot, err)) return false;
   if (!dmalloc(&d.P, (size_t)h.pots_len, tot, err)) return false;
   if (!dmalloc(&d.nearB, h.nearB.size(), tot, err)) return false;
@@ -435,8 +450,10 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
   cudaMemcpy(d.nearB, h.nearB.data(), h.nearB.size() * sizeof(double2), cudaMemcpyHostToDevice);
   cudaMemcpy(d.kq, h.kq.data(), h.kq.size() * sizeof(double), cudaMemcpyHostToDevice);
   cudaMemcpy(d.colleague, h.colleague.data(), h.colleague.size() * sizeof(int), cudaMemcpyHostToDevice);
-  {
-    d.n_bases = h.n_bases;
+  d.n_bases = h.n_bases;
+  // The factored near field of a uniform tree; an adaptive tree's near
+  // interactions are the generic near phase uploaded above.
+  if (!h.generic_near) {
     // Device layouts are transposed so that the threads of one leaf (one per
     // row) read consecutive words: Vt as [q][l][row], E as [q][k][row].
     const int R = h.rank, NB = h.n_bases;
@@ -463,7 +480,7 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
   cudaMemset(d.ybuf, 0, (size_t)h.N * sizeof(double2));
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { err = std::string("upload: ") + cudaGetErrorString(e); return false; }
-  int launches = 3;  // load of x, near coefficients, near field
+  int launches = 3;  // load of x, near coefficients and near field (or near phase and copy-out)
   for (auto& p : d.up) launches += p.n_tiles > 0;
   launches += d.m2l.n_tiles > 0;
   for (auto& p : d.down) launches += p.n_tiles > 0;
@@ -486,6 +503,8 @@ void dev_free(DevOperator& d) {
   for (auto& p : d.up) free_phase(p);
   for (auto& p : d.down) free_phase(p);
   free_phase(d.m2l);
+  free_phase(d.nearph);
+  cudaFree(d.nearph32.A);
   // FP32 phases share idx / out / klen / tiles with the FP64 phases; only A is theirs.
   for (auto& p : d.up32) cudaFree(p.A);
   for (auto& p : d.down32) cudaFree(p.A);
@@ -527,14 +546,17 @@ bool dev_enable_f32(DevOperator& d, std::string& err) {
   if (!f32_phase(d.m2l, d.m2l32, tot, err)) return false;
   d.down32.resize(d.down.size());
   for (size_t i = 0; i < d.down.size(); ++i) if (!f32_phase(d.down[i], d.down32[i], tot, err)) return false;
+  if (d.generic_near && !f32_phase(d.nearph, d.nearph32, tot, err)) return false;
   if (!dmalloc(&d.S32, (size_t)d.charges_len, tot, err)) return false;
   if (!dmalloc(&d.P32, (size_t)d.pots_len, tot, err)) return false;
-  const long long nb = 9LL * d.rank * d.rank;
-  if (!dmalloc(&d.nearB32, (size_t)nb, tot, err)) return false;
   if (!dmalloc(&d.kq32, (size_t)d.N, tot, err)) return false;
-  if (!dmalloc(&d.Z32, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
-  near_transpose32_kernel<<<64, 256>>>(d.nearB, d.nearB32, d.rank);
   d2f_real_kernel<<<256, 256>>>(d.kq, d.kq32, d.N);
+  if (!d.generic_near) {  // FP32 copy of the uniform tree's shared near blocks
+    const long long nb = 9LL * d.rank * d.rank;
+    if (!dmalloc(&d.nearB32, (size_t)nb, tot, err)) return false;
+    if (!dmalloc(&d.Z32, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
+    near_transpose32_kernel<<<64, 256>>>(d.nearB, d.nearB32, d.rank);
+  }
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { err = std::string("enable_f32: ") + cudaGetErrorString(e); return false; }
   d.has_f32 = true;
@@ -552,6 +574,11 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down) launch_gemv<2>(ph, (const double2*)d.P, d.P, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev_down[0], s);
+  if (d.generic_near) {
+    launch_gemv<3>(d.nearph, (const double2*)d.S, d.P, s, d.device);
+    launch_pdl(copy_out_kernel<double2, double2>, (unsigned)((d.N + 255) / 256), 256, 0, s, (const double2*)d.P, y, d.N);
+    return cudaGetLastError();
+  }
   launch_pdl(near_coeff_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
              d.n_bases, d.Qp, d.S, d.cbuf, d.x32);
   launch_pdl(near_factored_kernel, (unsigned)((d.N + 255) / 256), 256, 0, s, d.N, d.rank, d.n_bases, d.nearVt,
@@ -568,6 +595,11 @@ static cudaError_t f32_phases(DevOperator& d, Y* y, cudaStream_t s, bool mark_m2
   if (mark_m2l) cudaEventRecord(d.ev[3], s);
   for (auto& ph : d.down32) launch_gemv<2>(ph, (const float2*)d.P32, d.P32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev_down[1], s);
+  if (d.generic_near) {
+    launch_gemv<3>(d.nearph32, (const float2*)d.S32, d.P32, s, d.device);
+    launch_pdl(copy_out_kernel<float2, Y>, (unsigned)((d.N + 255) / 256), 256, 0, s, (const float2*)d.P32, y, d.N);
+    return cudaGetLastError();
+  }
   const int nthr = (9 * d.rank + 31) / 32 * 32;
   launch_pdl(near_gemm32_kernel, (unsigned)((d.n_leaves + kNearSources32 - 1) / kNearSources32), (unsigned)nthr,
              (size_t)kNearSources32 * d.rank * sizeof(float2), s, d.n_leaves, d.rank, d.nearB32, d.S32, d.Z32);

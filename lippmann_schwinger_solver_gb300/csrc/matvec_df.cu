@@ -310,6 +310,12 @@ int sms(int dev) {
   return g_sms;
 }
 
+// y = P[0:n) joined to FP64 (adaptive trees, after the near-field phase).
+__global__ void join_out_kernel(const float4* __restrict__ P, double2* __restrict__ y, int n) {
+  pdl_enter();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = join(ld_chain(P + i));
+}
+
 template <int PHASE>
 void launch_df(const DevPhase<float4>& ph, const float4* src, float4* dst, cudaStream_t s, int dev) {
   if (ph.n_tiles == 0) return;
@@ -357,17 +363,20 @@ bool dev_enable_df(DevOperator& d, std::string& err) {
   if (!df_phase(d.m2l, d.m2l_df, tot, err)) return false;
   d.down_df.resize(d.down.size());
   for (size_t i = 0; i < d.down.size(); ++i) if (!df_phase(d.down[i], d.down_df[i], tot, err)) return false;
+  if (d.generic_near && !df_phase(d.nearph, d.nearph_df, tot, err)) return false;
   if (!dalloc(&d.S_df, (size_t)d.charges_len, tot, err)) return false;
   if (!dalloc(&d.P_df, (size_t)d.pots_len, tot, err)) return false;
-  const long long nvt = 9LL * d.rank * d.n_bases;
-  const long long nqp = (long long)d.n_bases * d.rank;
-  if (!dalloc(&d.Vt_df, (size_t)nvt, tot, err)) return false;
-  if (!dalloc(&d.Qp_df, (size_t)nqp, tot, err)) return false;
-  if (!dalloc(&d.c_df, (size_t)d.n_leaves * d.n_bases, tot, err)) return false;
-  if (!dalloc(&d.Z_df, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
-  if (!dalloc(&d.ZE_df, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
-  split_kernel<<<64, 256>>>(d.nearVt, d.Vt_df, nvt);
-  split_real_kernel<<<16, 256>>>(d.Qp, d.Qp_df, nqp);
+  if (!d.generic_near) {  // the uniform tree's factored near field
+    const long long nvt = 9LL * d.rank * d.n_bases;
+    const long long nqp = (long long)d.n_bases * d.rank;
+    if (!dalloc(&d.Vt_df, (size_t)nvt, tot, err)) return false;
+    if (!dalloc(&d.Qp_df, (size_t)nqp, tot, err)) return false;
+    if (!dalloc(&d.c_df, (size_t)d.n_leaves * d.n_bases, tot, err)) return false;
+    if (!dalloc(&d.Z_df, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
+    if (!dalloc(&d.ZE_df, (size_t)d.n_leaves * 9 * d.rank, tot, err)) return false;
+    split_kernel<<<64, 256>>>(d.nearVt, d.Vt_df, nvt);
+    split_real_kernel<<<16, 256>>>(d.Qp, d.Qp_df, nqp);
+  }
   const cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { err = std::string("enable double-float: ") + cudaGetErrorString(e); return false; }
   d.has_df = true;
@@ -378,6 +387,8 @@ void dev_free_df(DevOperator& d) {
   for (auto& p : d.up_df) cudaFree(p.A);
   for (auto& p : d.down_df) cudaFree(p.A);
   cudaFree(d.m2l_df.A);
+  cudaFree(d.nearph_df.A);
+  d.nearph_df = DevPhase<float4>();
   cudaFree(d.S_df); cudaFree(d.P_df); cudaFree(d.Vt_df); cudaFree(d.Qp_df); cudaFree(d.c_df);
   cudaFree(d.Z_df); cudaFree(d.ZE_df);
   d.up_df.clear();
@@ -400,6 +411,11 @@ cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStre
   if (mark_m2l) cudaEventRecord(d.ev[1], s);
   for (auto& ph : d.down_df) launch_df<2>(ph, (const float4*)d.P_df, d.P_df, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev_down[0], s);
+  if (d.generic_near) {
+    launch_df<3>(d.nearph_df, (const float4*)d.S_df, d.P_df, s, d.device);
+    launch_pdl(join_out_kernel, (unsigned)((n + 255) / 256), 256, 0, s, (const float4*)d.P_df, y, n);
+    return cudaGetLastError();
+  }
   launch_pdl(near_coeff_df_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
              d.n_bases, d.Qp_df, d.S_df, d.c_df, d.x32);
   {
