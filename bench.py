@@ -170,6 +170,50 @@ def c1_config(ls):
                      Qchoice=0, findPhi=1, reference_rounding=1, L=1.0, kappa=10.0)
 
 
+def readme_adaptive_config(ls):
+    """The reference's published run (GMRES/Readme.md:43): adaptive quadtree
+    (tolerance 1e-5, 5 levels, N=5,328), nCones_LFR 16, 6x6 nodes, L = 0.5,
+    kappa 40, NCA tolerance 1e-8, Gaussian contrast."""
+    return ls.Config(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, TOL_POW=8, degreeOfBases=6, nLevelsUniform=5,
+                     Qchoice=0, findPhi=1, reference_rounding=1, L=0.5, kappa=40.0, tree_adaptive=1,
+                     treeAdaptivity=5)
+
+
+# Residuals the reference prints for RestartedGMRES(m = 10) after 1 and 2
+# restarts at that configuration (GMRES/Readme.md:64-65, 84-85).
+README_RESIDUALS = {1: 4.59412e-06, 2: 1.28443e-10}
+
+
+def adaptive_leg(ls, local, timed, max_iter):
+    """The adaptive operator at the README configuration: matvec time,
+    RestartedGMRES(10) with 1 and 2 restarts against the published
+    residuals, and the solves to 1e-8."""
+    opa = ls.Operator(readme_adaptive_config(ls), device=local)
+    info = opa.info
+    ms_a, _ = opa.time_matvec(warmup=3, iters=20, precision=ls.LS_PREC_F64)
+    ba = opa.rhs()
+    out = {"config": "adaptive quadtree (GMRES/Readme.md:43), N=%d, %d levels" % (opa.N, info["n_levels"]),
+           "N": opa.N, "assemble_s": info["assemble_seconds"],
+           "assemble_stages_s": dict(zip(("geometry", "precompute", "lists", "nca", "checks", "pack"),
+                                         (round(t, 3) for t in info["assemble_stage_seconds"]))),
+           "far_entries": info["far_entries"], "near_entries": info["near_entries"],
+           "matvec_ms": ms_a, "matvec_per_s": 1e3 / ms_a, "restarted_gmres_m10": {}}
+    nb = np.linalg.norm(ba)
+    for restarts, published in README_RESIDUALS.items():
+        t, xr = timed(lambda: opa.gmres_restarted(ba, 10, restarts))
+        res = float(np.linalg.norm(ba - opa.matvec(xr)) / nb)
+        out["restarted_gmres_m10"][str(restarts)] = {"s": t, "residual": res, "published": published,
+                                                     "rel_diff": abs(res / published - 1.0)}
+    t64, (x64, _, it64, rr64, code64) = timed(lambda: opa.gmres(ba, max_iter=max_iter, tol=1e-8))
+    opa.enable_f32()
+    tm, (xm, _, nmv, rrm, codem) = timed(lambda: opa.gmres_mixed(ba, max_outer=20, inner_iter=max_iter, tol=1e-8))
+    out.update({"fp64_gmres_s": t64, "fp64_iters": it64, "fp64_true_residual": rr64, "fp64_converged": code64 == 0,
+                "mixed_s": tm, "mixed_matvecs": nmv, "mixed_true_residual": rrm, "mixed_converged": codem == 0,
+                "mixed_rel_err_vs_fp64": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))})
+    opa.close()
+    return out
+
+
 def oracle_leg(ls, cfg, y_gpu, skel_gpu, budget_s=20.0):
     """The CPU restatement of the reference (oracle/) on the machine's host cores:
     its matvec/s with all threads and with one, its GMRES solve time to a
@@ -413,6 +457,9 @@ def run_ours(args):
             nn["speedup_nn_vs_mixed"] = tm / nn["nn"]["s"]
             solve["nn_fgmres"] = nn
             net.close()
+    # The reference's default (adaptive) tree at its published configuration.
+    if solve is not None and not args.no_adaptive:
+        solve["adaptive_readme"] = adaptive_leg(ls, local, timed, args.max_iter)
     # Many incidence directions on the scatterer (64 plane waves): the
     # batched mixed-precision solve against the same solves one at a time.
     batch = None
@@ -561,6 +608,7 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the many-direction batched solve")
     ap.add_argument("--no-nn", action="store_true", help="skip the learned-preconditioner solve")
+    ap.add_argument("--no-adaptive", action="store_true", help="skip the adaptive-tree operator at the README run")
     ap.add_argument("--angles", type=int, default=64, help="incidence directions of the batched solve")
     ap.add_argument("--max-iter", type=int, default=400)
     ap.add_argument("--f64-kernels", default="native", choices=["native", "double-float"],

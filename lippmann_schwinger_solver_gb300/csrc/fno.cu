@@ -549,15 +549,17 @@ __global__ void features_kernel(int G, int B, int S, const float* __restrict__ Q
 // work). The network is walked in alternating phases separated by grid-wide
 // barriers:
 //   row phase p (one grid row x per block): for p = 0 the lift of the row;
-//     for p >= 1 the y-synthesis of G1 + pointwise path + bias (+ GELU) of
-//     layer p-1; then, while p < L, the y-DFT of the new row into H1, and at
+//     for p >= 1 the x-synthesis of the row's G1 values from the mixed
+//     spectrum O of layer p-1, then the y-synthesis + pointwise path + bias
+//     (+ GELU); then, while p < L, the y-DFT of the new row into H1, and at
 //     p = L the projection of the row's points.
-//   column phase p (one kept ky per block): x-DFT of the H1 column, the
-//     per-mode channel mixing of layer p, and the x-synthesis into G1.
-// A row needs only its own previous values and G1 row, and a column only
+//   column phase p (one kept ky and kMixGroup kept kx per work item, so
+//     that M * 2M / kMixGroup blocks share it): the x-DFT of the H1 column
+//     at those kx and their per-mode channel mixing of layer p into O.
+// A row needs only its own previous values and O, and a column item only
 // its H1 column, so one barrier after each phase suffices (2 L in all).
 // Same arithmetic as the separate kernels above, in the same order per
-// output, except that the x-DFT sums run unsplit.
+// output, except that the x-DFT sums run in two halves.
 struct Fwd1Args {
   int G, M, L, PW;
   const float* in;    // [G*G][6]
@@ -566,6 +568,7 @@ struct Fwd1Args {
   float* h;           // [G*G][32], updated row by row
   float2* H1;         // [G][M][32]
   float2* G1;         // [G][M][32]
+  float2* O;          // [2M][M][32]: mixed spectrum of the layer
   const float2* tw;
   const float* lift_w;
   const float* lift_b;
@@ -579,6 +582,7 @@ struct Fwd1Args {
 };
 
 constexpr int kF1Threads = 512;
+constexpr int kMixGroup = 8;  // kept kx per column work item of the fused pass
 
 // Shared floats of the fused kernel: twiddles, then the larger of the row
 // phase (two rows, a G1 row, pointwise weights, projection weights) and the
@@ -626,12 +630,20 @@ __global__ void __launch_bounds__(kF1Threads, 1) forward1_kernel(Fwd1Args a) {
       } else {
         const int l = p - 1;
         for (int i = tid; i < G * 32; i += nt) hs_old[i] = a.h[row0 * 32 + i];
+        // x-synthesis of this row (x = r) from the layer's mixed spectrum.
         for (int i = tid; i < M * 32; i += nt) {
-          float2 g = a.G1[(long long)r * M * 32 + i];
-          const float sk = ((i >> 5) ? 2.f : 1.f) / GG;
-          g.x *= sk;
-          g.y *= sk;
-          gs[i] = g;
+          const int ky = i >> 5, c = i & 31;
+          float ar = 0.f, ai = 0.f;
+#pragma unroll 8
+          for (int m = 0; m < NM2; ++m) {
+            const int f = m < M ? m : G - 2 * M + m;
+            const float2 t = ts[(f * r) & (G - 1)];
+            const float2 v = __ldcg(a.O + ((long long)m * M + ky) * 32 + c);
+            ar = fmaf(t.x, v.x, fmaf(-t.y, v.y, ar));
+            ai = fmaf(t.x, v.y, fmaf(t.y, v.x, ai));
+          }
+          const float sk = (ky ? 2.f : 1.f) / GG;
+          gs[i] = make_float2(ar * sk, ai * sk);
         }
         for (int i = tid; i < 1024; i += nt) ps[(i >> 5) * 33 + (i & 31)] = a.pw_w[l][i];
         if (p == L) {
@@ -719,51 +731,52 @@ __global__ void __launch_bounds__(kF1Threads, 1) forward1_kernel(Fwd1Args a) {
     }
     if (p == L) break;
     grid.sync();
-    // ---------------- column phase (layer p)
-    for (int ky = blockIdx.x; ky < M; ky += gridDim.x) {
-      float2* ins = reinterpret_cast<float2*>(region);  // [G][32]
-      float2* h2s = ins + G * 32;                          // [2M][32]
-      float2* os = h2s + NM2 * 32;                         // [2M][32]
-      for (int i = tid; i < G * 32; i += nt) ins[i] = a.H1[((long long)(i >> 5) * M + ky) * 32 + (i & 31)];
+    // ---------------- column phase (layer p): x-DFT and mixing of one kept
+    // ky for a group of kMixGroup kept kx, so that M * ceil(2M / kMixGroup)
+    // blocks share the work; the x-synthesis runs in the next row phase.
+    const int ngrp = (NM2 + kMixGroup - 1) / kMixGroup;
+    for (int item = blockIdx.x; item < M * ngrp; item += gridDim.x) {
+      const int ky = item / ngrp, m0 = (item % ngrp) * kMixGroup;
+      float2* ins = reinterpret_cast<float2*>(region);   // [G][32]
+      float2* part = ins + G * 32;                        // [2][kMixGroup][32]
+      float2* h2s = part + 2 * kMixGroup * 32;            // [kMixGroup][32]
+      for (int i = tid; i < G * 32; i += nt) ins[i] = __ldcg(a.H1 + ((long long)(i >> 5) * M + ky) * 32 + (i & 31));
       __syncthreads();
-      for (int item = tid; item < NM2 * 32; item += nt) {
-        const int m = item >> 5, c = item & 31;
-        const int f = m < M ? m : G - 2 * M + m;
+      // each output's sum over x in two halves (independent chains)
+      for (int it = tid; it < 2 * kMixGroup * 32; it += nt) {
+        const int half = it / (kMixGroup * 32), rem = it - half * kMixGroup * 32;
+        const int mm = rem >> 5, c = rem & 31, m = m0 + mm;
         float ar = 0.f, ai = 0.f;
-        for (int x = 0; x < G; ++x) {
-          const float2 t = ts[(f * x) & (G - 1)];
-          const float2 v = ins[x * 32 + c];
-          ar = fmaf(t.x, v.x, fmaf(t.y, v.y, ar));
-          ai = fmaf(t.x, v.y, fmaf(-t.y, v.x, ai));
+        if (m < NM2) {
+          const int f = m < M ? m : G - 2 * M + m;
+          for (int x = half * (G >> 1); x < (half + 1) * (G >> 1); ++x) {
+            const float2 t = ts[(f * x) & (G - 1)];
+            const float2 v = ins[x * 32 + c];
+            ar = fmaf(t.x, v.x, fmaf(t.y, v.y, ar));
+            ai = fmaf(t.x, v.y, fmaf(-t.y, v.x, ai));
+          }
         }
-        h2s[item] = make_float2(ar, ai);
+        part[it] = make_float2(ar, ai);
       }
       __syncthreads();
-      for (int item = tid; item < NM2 * 32; item += nt) {
-        const int m = item >> 5, o = item & 31;
+      for (int it = tid; it < kMixGroup * 32; it += nt) {
+        const float2 u = part[it], v = part[kMixGroup * 32 + it];
+        h2s[it] = make_float2(u.x + v.x, u.y + v.y);
+      }
+      __syncthreads();
+      for (int it = tid; it < kMixGroup * 32; it += nt) {
+        const int mm = it >> 5, o = it & 31, m = m0 + mm;
+        if (m >= NM2) continue;
         const float2* wm = a.spec[p] + (long long)(m * M + ky) * 1024 + o;
         float ar = 0.f, ai = 0.f;
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
-          const float2 v = h2s[m * 32 + i];
+          const float2 v = h2s[mm * 32 + i];
           const float2 w = wm[i * 32];
           ar = fmaf(v.x, w.x, fmaf(-v.y, w.y, ar));
           ai = fmaf(v.x, w.y, fmaf(v.y, w.x, ai));
         }
-        os[item] = make_float2(ar, ai);
-      }
-      __syncthreads();
-      for (int item = tid; item < G * 32; item += nt) {
-        const int x = item >> 5, c = item & 31;
-        float ar = 0.f, ai = 0.f;
-        for (int m = 0; m < NM2; ++m) {
-          const int f = m < M ? m : G - 2 * M + m;
-          const float2 t = ts[(f * x) & (G - 1)];
-          const float2 v = os[m * 32 + c];
-          ar = fmaf(t.x, v.x, fmaf(-t.y, v.y, ar));
-          ai = fmaf(t.x, v.y, fmaf(t.y, v.x, ai));
-        }
-        a.G1[((long long)x * M + ky) * 32 + c] = make_float2(ar, ai);
+        a.O[((long long)m * M + ky) * 32 + o] = make_float2(ar, ai);
       }
       __syncthreads();
     }
@@ -980,6 +993,7 @@ cudaError_t FnoNet::forward1(const float* in, float* outp, const float* ssq, cud
   a.h = h[0];
   a.H1 = H1;
   a.G1 = G1;
+  a.O = O;
   a.tw = tw;
   a.lift_w = params + lay.lift_w;
   a.lift_b = params + lay.lift_b;

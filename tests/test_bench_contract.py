@@ -56,3 +56,8 @@ def test_our_arm_contract():
     assert fp["peak_tflops"] > 0 and 0 < fp["m2l_frac"] < 1.5 and 0 < fp["near_field_frac"] < 1.5
     assert set(r["phases_ms"]) == {"total", "up", "m2l", "down", "near"}
     assert r["solve"]["mixed_rel_err_vs_fp64"] < 1e-6
+    # the adaptive operator at the reference's published run reproduces its residuals
+    ad = r["solve"]["adaptive_readme"]
+    assert ad["N"] == 5328 and ad["fp64_converged"] and ad["mixed_converged"]
+    for restarts in ("1", "2"):
+        assert ad["restarted_gmres_m10"][restarts]["rel_diff"] <= 2e-5, ad["restarted_gmres_m10"]
