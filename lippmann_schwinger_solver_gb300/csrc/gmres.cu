@@ -33,6 +33,10 @@ namespace lsg {
 constexpr int kDotThreads = 128;
 constexpr int kDotBlocks = 304;  // row chunks: partial sums per column (2 per SM)
 constexpr int kDotCols = 8;      // columns per multi-dot block
+constexpr int kAxpyBlocksMax = 152 * 8;  // grid_for()'s cap: per-block norm partials
+// DGKS criterion of the conditional second Gram-Schmidt pass: it runs only
+// when the first pass removed more than half of |w|^2 (|w'| < |w| / sqrt 2).
+constexpr double kReorthRatio = 0.5;
 constexpr int kFlexInner = 24;   // steps of a right-preconditioned inner cycle
 // Inner targets at or above this relative reduction are left to plain
 // GMRES: a few unpreconditioned steps reach them for less than the
@@ -89,6 +93,9 @@ struct Basis {
   }
 };
 
+// Column groups of a multi-dot over up to m + 1 basis vectors and w.
+inline int n_counters(int m) { return (m + 2 + kDotCols - 1) / kDotCols; }
+
 struct GmresWorkspace {
   Basis<double2> b64;
   Basis<float2> b32;
@@ -105,14 +112,19 @@ struct GmresWorkspace {
   double2* partial = nullptr;
   double2* h = nullptr;
   double2* h2 = nullptr;
-  double2* nrm = nullptr;
+  double2* nrm = nullptr;   // [0] |w|^2 of the new direction, [1] before and [2] after the first pass
+  double* npartial = nullptr;  // per-block partial norms of the fused corrections
+  unsigned* counters = nullptr;  // finished blocks per column group, + one for the corrections
   cudaEvent_t copied = nullptr;  // a step's coefficients are on the host
   double2* pinned = nullptr;     // host: h (m+2), h2 (m+2), |w|^2; page-locked so copies stay asynchronous
   int n = 0, cap = -1;
+  int n_groups() const { return n_counters(cap); }
   void release_small() {
     cudaFree(res); cudaFree(res32); cudaFree(dx32); cudaFree(partial); cudaFree(h); cudaFree(h2); cudaFree(nrm);
-    cudaFree(dx64); cudaFree(pv32); cudaFree(pz32);
+    cudaFree(dx64); cudaFree(pv32); cudaFree(pz32); cudaFree(npartial); cudaFree(counters);
     res = partial = h = h2 = nrm = dx64 = nullptr;
+    npartial = nullptr;
+    counters = nullptr;
     res32 = dx32 = pv32 = pz32 = nullptr;
     if (copied) cudaEventDestroy(copied);
     copied = nullptr;
@@ -140,7 +152,10 @@ struct GmresWorkspace {
     if (e == cudaSuccess) e = cudaMalloc(&partial, (size_t)kDotBlocks * (m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&h, (size_t)(m + 2) * sizeof(double2));
     if (e == cudaSuccess) e = cudaMalloc(&h2, (size_t)(m + 2) * sizeof(double2));
-    if (e == cudaSuccess) e = cudaMalloc(&nrm, sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&nrm, 3 * sizeof(double2));
+    if (e == cudaSuccess) e = cudaMalloc(&npartial, kAxpyBlocksMax * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&counters, (size_t)(n_counters(m) + 1) * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(counters, 0, (size_t)(n_counters(m) + 1) * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost(&pinned, (size_t)(2 * (m + 2) + 1) * sizeof(double2));
     if (e != cudaSuccess) {
@@ -175,26 +190,49 @@ __device__ __forceinline__ void shfl_add(R& x, R& y, R kx, R ky, int o) {
   y = ky + __shfl_xor_sync(0xffffffffu, y, o);
 }
 
-// partial[col * gridDim.x + block] = sum_{rows of block} conj(V[row, col]) * w[row].
+// True when the second Gram-Schmidt pass is not needed (DGKS): the first
+// pass left at least kReorthRatio of |w|^2.
+__device__ __forceinline__ bool reorth_skipped(const double2* nrm_w, const double2* nrm_r) {
+  return ld_chain(nrm_r).x >= kReorthRatio * ld_chain(nrm_w).x;
+}
+
+// out[c] = sum_rows conj(V[row, c]) * w[row] for c < ncols and, with
+// nrm_out, *nrm_out = |w|^2 (w taken as one more column).
 // Block (x, y) owns a contiguous chunk of rows and the columns
 // 8y .. 8y+7: each thread keeps eight sums, so it has eight independent
-// loads of V in flight per row. GB300's FP64 pipe is narrow, so the warp
+// loads in flight per row. GB300's FP64 pipe is narrow, so the warp
 // reduction of the eight sums is a transposing butterfly: at each of the
 // first three shuffle steps a lane keeps half of its columns and adds the
 // partner's half, which leaves each group of four lanes one column (18
-// adds per lane instead of 80). All orders are fixed: deterministic.
+// adds per lane instead of 80). Each block leaves its sums in partial; the
+// last block of a column group to finish (counted in counters[y]) adds the
+// group's partials in a fixed order and resets the counter for the next
+// launch, so the dot products take one launch and stay deterministic.
+// With gate_w / gate_r (the second, conditional pass) the kernel writes
+// zeros instead when reorth_skipped().
 template <class T>
-__global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restrict__ V, long long ldv, int ncols,
-                                                               const T* __restrict__ w, int n,
-                                                               double2* __restrict__ partial) {
+__global__ void __launch_bounds__(kDotThreads) gs_dot_kernel(const T* __restrict__ V, long long ldv, int ncols,
+                                                             const T* __restrict__ w, int n,
+                                                             double2* __restrict__ partial,
+                                                             unsigned* __restrict__ counters,
+                                                             double2* __restrict__ out, double2* __restrict__ nrm_out,
+                                                             const double2* __restrict__ gate_w,
+                                                             const double2* __restrict__ gate_r) {
   pdl_enter();
   using R = typename Cx<T>::R;
   __shared__ T red[kDotThreads / 32][kDotCols];
+  __shared__ unsigned ticket;
+  const int nv = ncols + (nrm_out ? 1 : 0);
+  const int c0 = blockIdx.y * kDotCols;
+  const int nc = min(kDotCols, nv - c0);
+  if (gate_w && reorth_skipped(gate_w, gate_r)) {
+    if (blockIdx.x == 0 && (int)threadIdx.x < nc && c0 + (int)threadIdx.x < ncols)
+      out[c0 + threadIdx.x] = make_double2(0.0, 0.0);
+    return;
+  }
   const int chunk = (n + gridDim.x - 1) / gridDim.x;
   const int r0 = blockIdx.x * chunk;
   const int len = max(0, min(chunk, n - r0));
-  const int c0 = blockIdx.y * kDotCols;
-  const int nc = min(kDotCols, ncols - c0);
   R ar[kDotCols], ai[kDotCols];
 #pragma unroll
   for (int j = 0; j < kDotCols; ++j) ar[j] = ai[j] = R(0);
@@ -203,7 +241,8 @@ __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restri
     T a[kDotCols];
 #pragma unroll
     for (int j = 0; j < kDotCols; ++j)  // all loads first, so that they are in flight together
-      a[j] = j < nc ? ld_chain(V + (size_t)(c0 + j) * ldv + r0 + i) : Cx<T>::make(R(0), R(0));
+      a[j] = c0 + j < ncols ? ld_chain(V + (size_t)(c0 + j) * ldv + r0 + i)
+                            : (j < nc ? b : Cx<T>::make(R(0), R(0)));
 #pragma unroll
     for (int j = 0; j < kDotCols; ++j) {
       ar[j] = fma(a[j].x, b.x, ar[j]);
@@ -247,7 +286,7 @@ __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restri
   if ((lane & 3) == 0)
     red[wid][((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1)] = Cx<T>::make(ar[0], ai[0]);
   __syncthreads();
-  if (threadIdx.x < nc) {
+  if ((int)threadIdx.x < nc) {
     double a = 0.0, b = 0.0;
     for (int k = 0; k < kDotThreads / 32; ++k) {
       a += (double)red[k][threadIdx.x].x;
@@ -255,27 +294,112 @@ __global__ void __launch_bounds__(kDotThreads) multidot_kernel(const T* __restri
     }
     partial[(size_t)(c0 + threadIdx.x) * gridDim.x + blockIdx.x] = make_double2(a, b);
   }
+  // The last block of the group adds the group's partial sums.
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) ticket = atomicAdd(counters + blockIdx.y, 1u);
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  __threadfence();
+  for (int t = wid; t < nc; t += kDotThreads / 32) {
+    double a = 0.0, b = 0.0;
+    for (int k = lane; k < (int)gridDim.x; k += 32) {
+      const double2 p = __ldcg(partial + (size_t)(c0 + t) * gridDim.x + k);
+      a += p.x;
+      b += p.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      double2* d = c0 + t < ncols ? out + c0 + t : nrm_out;
+      *d = make_double2(a, b);
+    }
+  }
+  if (threadIdx.x == 0) counters[blockIdx.y] = 0;
 }
 
-// out[col] = sum_b partial[col * nb + b]: one warp per column, lanes stride
-// over the partials, then a fixed shuffle tree (deterministic).
-__global__ void reduce_partials_kernel(const double2* __restrict__ partial, int nb, int ncols,
-                                       double2* __restrict__ out) {
+// One Gram-Schmidt correction fused with the norm that follows it:
+// w[i] -= sum_c V[i, c] * h[c], then *nrm_out = |w|^2 (the per-block
+// partial norms added in a fixed order by the last block to finish, as in
+// gs_dot_kernel). With gate_w / gate_r (the second, conditional pass) a
+// skipped pass leaves w unchanged and copies *gate_r to *nrm_out.
+template <class T>
+__global__ void __launch_bounds__(256) axpy_norm_kernel(T* __restrict__ w, const T* __restrict__ V, long long ldv,
+                                                        int ncols, const double2* __restrict__ h, int n,
+                                                        double* __restrict__ npartial, unsigned* __restrict__ counter,
+                                                        double2* __restrict__ nrm_out,
+                                                        const double2* __restrict__ gate_w,
+                                                        const double2* __restrict__ gate_r) {
   pdl_enter();
-  const int col = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (col >= ncols) return;
-  double a = 0.0, b = 0.0;
-  for (int k = lane; k < nb; k += 32) {
-    const double2 p = ld_chain(partial + (size_t)col * nb + k);
-    a += p.x;
-    b += p.y;
+  using R = typename Cx<T>::R;
+  __shared__ double red[8];
+  __shared__ unsigned ticket;
+  if (gate_w && reorth_skipped(gate_w, gate_r)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nrm_out = ld_chain(gate_r);
+    return;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    R sr = R(0), si = R(0);
+    int c = 0;
+    for (; c + 4 <= ncols; c += 4) {
+      T v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = ld_chain(V + (size_t)(c + j) * ldv + i);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const double2 hc = ld_chain(h + c + j);
+        const R hx = (R)hc.x, hy = (R)hc.y;
+        sr = fma(v[j].x, hx, sr);
+        sr = fma(-v[j].y, hy, sr);
+        si = fma(v[j].x, hy, si);
+        si = fma(v[j].y, hx, si);
+      }
+    }
+    for (; c < ncols; ++c) {
+      const T v = ld_chain(V + (size_t)c * ldv + i);
+      const double2 hc = ld_chain(h + c);
+      const R hx = (R)hc.x, hy = (R)hc.y;
+      sr = fma(v.x, hx, sr);
+      sr = fma(-v.y, hy, sr);
+      si = fma(v.x, hy, si);
+      si = fma(v.y, hx, si);
+    }
+    const T o = ld_chain(w + i);
+    const R nx = o.x - sr, ny = o.y - si;
+    w[i] = Cx<T>::make(nx, ny);
+    acc = fma((double)nx, (double)nx, acc);
+    acc = fma((double)ny, (double)ny, acc);
   }
-  if (lane == 0) out[col] = make_double2(a, b);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) red[wid] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    npartial[blockIdx.x] = t;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  __threadfence();
+  double t = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) t += __ldcg(npartial + k);
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  __syncthreads();
+  if (lane == 0) red[wid] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double u = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) u += red[k];
+    *nrm_out = make_double2(u, 0.0);
+    *counter = 0;
+  }
 }
 
 // w[i] += sign * sum_c V[i, c] * h[c]; the column loop is unrolled by 4 so
@@ -402,18 +526,27 @@ using cdh = std::complex<double>;
 
 int grid_for(int n) { return std::min((n + 255) / 256, 152 * 8); }
 
-// h_dev[0:ncols) = V[:, 0:ncols)^H w
+// h_dev[0:ncols) = V[:, 0:ncols)^H w and, with nrm_dev, *nrm_dev = |w|^2;
+// with gate_w / gate_r the conditional second pass.
 template <class T>
-void multidot(const T* V, long long ldv, int ncols, const T* w, int n, double2* partial, double2* h_dev,
-              cudaStream_t s) {
-  launch_pdl(multidot_kernel<T>, dim3(kDotBlocks, (ncols + kDotCols - 1) / kDotCols), kDotThreads, 0, s, V, ldv, ncols, w, n,
-                                                                                                 partial);
-  launch_pdl(reduce_partials_kernel, (ncols * 32 + 255) / 256, 256, 0, s, partial, kDotBlocks, ncols, h_dev);
+void multidot(const T* V, long long ldv, int ncols, const T* w, int n, GmresWorkspace& ws, double2* h_dev,
+              double2* nrm_dev, const double2* gate_w, const double2* gate_r, cudaStream_t s) {
+  const int nv = ncols + (nrm_dev ? 1 : 0);
+  launch_pdl(gs_dot_kernel<T>, dim3(kDotBlocks, (nv + kDotCols - 1) / kDotCols), kDotThreads, 0, s, V, ldv, ncols, w,
+             n, ws.partial, ws.counters, h_dev, nrm_dev, gate_w, gate_r);
+}
+
+// w -= V[:, 0:ncols) h_dev, then *nrm_dev = |w|^2 (see axpy_norm_kernel).
+template <class T>
+void correct(T* w, const T* V, long long ldv, int ncols, const double2* h_dev, int n, GmresWorkspace& ws,
+             double2* nrm_dev, const double2* gate_w, const double2* gate_r, cudaStream_t s) {
+  launch_pdl(axpy_norm_kernel<T>, grid_for(n), 256, 0, s, w, V, ldv, ncols, h_dev, n, ws.npartial,
+             ws.counters + (ws.n_groups()), nrm_dev, gate_w, gate_r);
 }
 
 template <class T>
 cudaError_t vnorm(const T* w, int n, GmresWorkspace& ws, cudaStream_t s, double& out) {
-  multidot(w, n, 1, w, n, ws.partial, ws.nrm, s);
+  multidot(static_cast<const T*>(nullptr), n, 0, w, n, ws, nullptr, ws.nrm, nullptr, nullptr, s);
   double2 hv;
   cudaError_t e = cudaMemcpyAsync(&hv, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return e;
@@ -505,12 +638,17 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
   double2* hp2 = ws.pinned + (m + 2);
   double2* np = ws.pinned + 2 * (m + 2);
   for (int k = 0; k < m; ++k) {
-    // CGS2, both passes and the norm on the device; one copy back per step.
-    multidot(B.V, n, k + 1, B.w, n, ws.partial, ws.h, s);
-    launch_pdl(multi_axpy_kernel<T>, grid_for(n), 256, 0, s, B.w, B.V, n, k + 1, ws.h, n, -1.0);
-    multidot(B.V, n, k + 1, B.w, n, ws.partial, ws.h2, s);
-    launch_pdl(multi_axpy_kernel<T>, grid_for(n), 256, 0, s, B.w, B.V, n, k + 1, ws.h2, n, -1.0);
-    multidot(B.w, n, 1, B.w, n, ws.partial, ws.nrm, s);
+    // Classical Gram-Schmidt with a conditional second pass (DGKS), all on
+    // the device; one copy back per step. Pass 1: h = V^H w with |w|^2, then
+    // w' = w - V h with |w'|^2. Pass 2 (h2 = V^H w', w'' = w' - V h2 with
+    // |w''|^2) runs only when |w'|^2 < kReorthRatio |w|^2; otherwise both
+    // of its kernels return at once, h2 = 0 and |w''|^2 = |w'|^2.
+    double2* nrm_w = ws.nrm + 1;
+    double2* nrm_1 = ws.nrm + 2;
+    multidot(B.V, n, k + 1, B.w, n, ws, ws.h, nrm_w, nullptr, nullptr, s);
+    correct(B.w, B.V, n, k + 1, ws.h, n, ws, nrm_1, nullptr, nullptr, s);
+    multidot(B.V, n, k + 1, B.w, n, ws, ws.h2, nullptr, nrm_w, nrm_1, s);
+    correct(B.w, B.V, n, k + 1, ws.h2, n, ws, ws.nrm, nrm_w, nrm_1, s);
     launch_pdl(scale_by_norm_kernel<T>, grid_for(n), 256, 0, s, B.w, B.V + (size_t)(k + 1) * n, ws.nrm, n);
     cudaMemcpyAsync(hp, ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hp2, ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
