@@ -50,8 +50,13 @@ struct inputsToDFMM {
   int yes2DFMM = 1;
   int TOL_POW = 8;
   int degreeOfBases = 6;
-  int treeAdaptivity = 5;  // unused: the tree is uniform
-  int nLevelsUniform = 4;
+  int treeAdaptivity = 5;  // adaptive tree: contrast resolved to 10^-treeAdaptivity
+  int nLevelsUniform = 4;  // uniform tree: its depth
+  // 1: the adaptive quadtree that GMRES/GMRES.cpp:164-165 builds
+  // (createAdaptiveTree + makeLevelRestriction_Tree); 0: the uniform tree
+  // of createUniformTree (the line the reference leaves commented out),
+  // which the benchmark workloads use.
+  int treeAdaptive = 0;
 };
 
 // Contrast plugin: Qchoice 0..5 as in the reference, 6 = Gaussian bumps.
@@ -87,6 +92,8 @@ class DFMM {
     c.TOL_POW = inputs.TOL_POW;
     c.degreeOfBases = inputs.degreeOfBases;
     c.nLevelsUniform = inputs.nLevelsUniform;
+    c.tree_adaptive = inputs.treeAdaptive;
+    c.treeAdaptivity = inputs.treeAdaptivity;
     c.Qchoice = kernel.Qchoice;
     c.findPhi = findPhi ? 1 : 0;
     c.reference_rounding = 1;

@@ -530,6 +530,9 @@ class inputsToDFMM:  # noqa: N801 - reference name (GMRES/GMRES.cpp:129-138)
     degreeOfBases: int = 6
     treeAdaptivity: int = 5
     nLevelsUniform: int = 4
+    # 1: the adaptive quadtree GMRES/GMRES.cpp:164-165 builds; 0: the uniform
+    # tree (createUniformTree) of the benchmark workloads.
+    treeAdaptive: int = 0
 
 
 class userkernel:  # noqa: N801 - reference name (GMRES/GMRES.cpp:100-127)
@@ -552,7 +555,8 @@ class DFMM:
                           TOL_POW=inputs.TOL_POW, degreeOfBases=inputs.degreeOfBases,
                           nLevelsUniform=inputs.nLevelsUniform, Qchoice=kernel.Qchoice, findPhi=int(findPhi),
                           reference_rounding=int(reference_rounding), L=inputs.L, kappa=kernel.kappa,
-                          bumps=kernel.bumps)
+                          bumps=kernel.bumps, tree_adaptive=int(inputs.treeAdaptive),
+                          treeAdaptivity=int(inputs.treeAdaptivity))
         self.device = device
         self.K = None
 

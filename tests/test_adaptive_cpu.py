@@ -32,7 +32,12 @@ def _oracle_skeletons(ora, d, adaptivity):
 
 
 def test_adaptive_host_assembly_matches_oracle_skeletons(ls, ora):
-    op = ls.Operator(ls.Config(**README), device=-1)
+    # through the reference-shaped mirror (inputsToDFMM / userkernel / DFMM)
+    inputs = ls.inputsToDFMM(nCones_LFR=16, nChebNodes=6, L=0.5, yes2DFMM=1, TOL_POW=8, degreeOfBases=6,
+                             treeAdaptivity=5, treeAdaptive=1)
+    S = ls.DFMM(inputs, ls.userkernel(kappa=40.0, Qchoice=0), device=-1)
+    S.FMMTreeInitialisation()
+    op = S.K
     assert op.N == 5328 and op.info["n_levels"] == 5 and op.info["level_LFR"] == 4
     assert np.array_equal(op.skeleton_dump(), _oracle_skeletons(ora, README, 5))
     a = ora.AdaptiveOracle(README, treeAdaptivity=5)
