@@ -501,6 +501,17 @@ def run_ours(args):
                             "max_true_residual": float(np.max(rrb8)), "converged": codeb8 == 0,
                             "max_rel_diff_vs_width64": float(max(np.linalg.norm(Xb[:, j] - Xb8[:, j]) /
                                                                  np.linalg.norm(Xb8[:, j]) for j in range(B.shape[1])))}}
+    # BASELINE config 4: 32 seeded scatterers of uneven size (levels 4-6,
+    # kappa U[10, 60], 1-4 bumps) x 64 directions, host assembly of the next
+    # scatterer overlapped with the GPU solve of the current one.
+    many = None
+    if not args.no_solve and not args.no_batch and args.scatterers > 0:
+        from lippmann_schwinger_solver_gb300 import scatterers as scat
+        specs = scat.scatterer_specs(args.scatterers, SEED)
+        recs, many, _ = scat.solve_many(specs, args.angles, 1e-8, 10, device=local)
+        many["levels"] = {str(lv): sum(1 for r in recs if r["level"] == lv) for lv in (4, 5, 6)}
+        many["host_stages_s"] = {k: round(sum(r["host_stages_s"][k] for r in recs), 2)
+                                 for k in recs[0]["host_stages_s"]}
     peak, peak_kind = load_peaks()
     achieved = info["m2l_bytes"] / (ms_m2l * 1e-3) / 1e9
     traffic = traffic_per_launch(args.f64_kernels)
@@ -560,6 +571,7 @@ def run_ours(args):
         "other_f64_kernels": alt,
         "solve": solve,
         "batched_solve": batch,
+        "many_scatterers": many,
         "cpu_baseline": cpu,
     }
     if rank == 0:
@@ -596,6 +608,47 @@ def run_fno_forward(args):
     net.close()
 
 
+def run_block_apply(args):
+    """Times `--steps` FP32 block applies of `args.block_apply` right-hand
+    sides (64: tensor cores, 8: CUDA cores) on the workload operator at
+    `--level`, inputs resident; one JSON line. Also the command that the
+    tensor-core kernel's ncu captures profile."""
+    import lippmann_schwinger_solver_gb300 as ls
+    op = ls.Operator(workload_config(ls, args.level), device=0)
+    op.enable_f32()
+    ms = op.time_block_apply(args.block_apply, warmup=max(3, args.warmup), iters=max(1, args.steps))
+    print(json.dumps({"metric": "FP32 block apply", "unit": "ms", "value": ms, "width": args.block_apply,
+                      "per_rhs_us": ms / args.block_apply * 1e3, "N": op.N, "level": args.level}), flush=True)
+    op.close()
+
+
+def run_profile_solve(args):
+    """One FP64 GMRES and one mixed-precision solve to 1e-8 on the workload
+    operator at `--level`, after an untimed pair, inside a CUDA profiler range
+    (ncu --profile-from-start off captures just them); one JSON line."""
+    import torch
+
+    import lippmann_schwinger_solver_gb300 as ls
+    op = ls.Operator(workload_config(ls, args.level), device=0)
+    op.enable_f32()
+    b = op.rhs()
+    op.gmres(b, max_iter=args.max_iter, tol=1e-8)
+    op.gmres_mixed(b, max_outer=20, inner_iter=args.max_iter, tol=1e-8)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    t0 = time.perf_counter()
+    _, _, it, rr, _ = op.gmres(b, max_iter=args.max_iter, tol=1e-8)
+    t1 = time.perf_counter()
+    _, _, nmv, rrm, _ = op.gmres_mixed(b, max_outer=20, inner_iter=args.max_iter, tol=1e-8)
+    t2 = time.perf_counter()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"metric": "solve to 1e-8 inside a profiler range", "fp64_gmres_s": t1 - t0, "fp64_iters": it,
+                      "fp64_true_residual": rr, "mixed_s": t2 - t1, "mixed_matvecs": nmv, "mixed_true_residual": rrm,
+                      "N": op.N, "level": args.level}), flush=True)
+    op.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -610,6 +663,8 @@ def main():
     ap.add_argument("--no-nn", action="store_true", help="skip the learned-preconditioner solve")
     ap.add_argument("--no-adaptive", action="store_true", help="skip the adaptive-tree operator at the README run")
     ap.add_argument("--angles", type=int, default=64, help="incidence directions of the batched solve")
+    ap.add_argument("--scatterers", type=int, default=32,
+                    help="scatterers of the many-scatterer batched workload (0 skips it)")
     ap.add_argument("--max-iter", type=int, default=400)
     ap.add_argument("--f64-kernels", default="native", choices=["native", "double-float"],
                     help="kernels behind the FP64 operator: FP64 arithmetic, or FP32 hi/lo pairs with "
@@ -618,9 +673,17 @@ def main():
                     help="operator precision of the timed loop (f32: profiling run of the FP32 operator)")
     ap.add_argument("--fno-forward", type=int, default=0,
                     help="only time this many batch-1 forward passes of the trained network")
+    ap.add_argument("--block-apply", type=int, default=0,
+                    help="only time FP32 block applies of this many right-hand sides (64 or 8)")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="only run one FP64 and one mixed solve inside a CUDA profiler range")
     args = ap.parse_args()
     if args.fno_forward > 0:
         run_fno_forward(args)
+    elif args.block_apply > 0:
+        run_block_apply(args)
+    elif args.profile_solve:
+        run_profile_solve(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

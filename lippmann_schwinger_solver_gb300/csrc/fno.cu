@@ -1008,7 +1008,9 @@ cudaError_t FnoNet::forward1(const float* in, float* outp, const float* ssq, cud
   a.p2_b = params + lay.p2_b;
   void* args[] = {&a};
   const size_t smem = fwd1_smem_floats(shape.grid, shape.modes) * sizeof(float);
-  const int blocks = std::min(fused_blocks, std::max(shape.grid, shape.modes));
+  // one block per grid row and per column work item (a kept ky and a group of kMixGroup kept kx)
+  const int col_items = shape.modes * ((2 * shape.modes + kMixGroup - 1) / kMixGroup);
+  const int blocks = std::min(fused_blocks, std::max(shape.grid, col_items));
   launches = 1;
   return cudaLaunchCooperativeKernel((const void*)forward1_kernel, dim3((unsigned)blocks), dim3(kF1Threads), args,
                                      smem, s);

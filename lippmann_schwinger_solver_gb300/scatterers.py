@@ -4,8 +4,8 @@ Each scatterer (uniform tree of level 4-6, kappa ~ U[10, 60], 1 to 4
 Gaussian bumps with centres U[-0.6, 0.6]^2, amplitudes U[0.5, 1.5], widths
 U[0.05, 0.2], all seeded) is assembled on the host, uploaded, and solved for
 `angles` plane-wave incidences theta_m = 2 pi m / angles by the batched
-mixed-precision solver (ls_gmres_mixed_batched: eight directions per FP32
-operator apply, FP64 true residual per direction). The host assembly of the
+mixed-precision solver (ls_gmres_mixed_batched: 64 directions per FP32
+operator apply on the tensor cores, FP64 true residual per direction). The host assembly of the
 next scatterer runs in a second thread while the GPU solves the current one:
 ctypes releases the interpreter lock during each library call.
 
