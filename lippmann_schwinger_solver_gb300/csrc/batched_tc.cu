@@ -186,18 +186,27 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     const int nchunks = (blk.nst + kChunkStages - 1) / kChunkStages;
     // Loads of stage st: 8 gathered right-hand-side values and up to 4
     // operator vectors per thread. Stage st + 1's loads are issued before
-    // stage st is stored, so every thread has two stages of loads in flight.
+    // stage st is stored, so every thread has two stages of loads in flight;
+    // the gather indices are loaded one stage earlier still, so the
+    // dependent index load is off the critical path.
     float2 xv[8], xn[8];
     float4 av[4], an[4];
-    auto load_stage = [&](int st, float2* x, float4* a) {
+    int ixv[8], ixn[8];  // gather sources of the next stage and of the one after (-1: past K)
+    auto load_idx = [&](int st, int* ix) {
       const int k0 = st * kStageCols;
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int ci = hw * 8 + i;
-        const int jj = (ci & 7) * 8 + j8, cc = 2 * (ci >> 3) + cpar;
-        const int k = k0 + cc;
-        x[i] = make_float2(0.f, 0.f);
-        if (k < blk.K) x[i] = ld_chain(src + (size_t)__ldg(idx + blk.i_off + k) * 64 + jj);
+        const int k = k0 + 2 * (ci >> 3) + cpar;
+        ix[i] = k < blk.K ? __ldg(idx + blk.i_off + k) : -1;
+      }
+    };
+    auto load_stage = [&](int st, const int* ix, float2* x, float4* a) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int ci = hw * 8 + i;
+        const int jj = (ci & 7) * 8 + j8;
+        x[i] = ix[i] >= 0 ? ld_chain(src + (size_t)ix[i] * 64 + jj) : make_float2(0.f, 0.f);
       }
       // npad rows x 16 complex columns in the canonical layout: npad * 8 <= 512 float4.
       const float4* As = reinterpret_cast<const float4*>(A + blk.a_off + (long long)st * blk.npad * kStageCols);
@@ -207,7 +216,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         a[q] = u < blk.npad * 8 ? __ldcs(As + u) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
     };
-    if (blk.nst > 0) load_stage(0, xv, av);
+    if (blk.nst > 0) {
+      load_idx(0, ixv);
+      load_stage(0, ixv, xv, av);
+    }
+    if (blk.nst > 1) load_idx(1, ixv);
     for (int st = 0; st < blk.nst; ++st, ++g) {
       const int buf = (int)(g & 1);
       const long long G = gc0 + st / kChunkStages;  // chunk of this stage
@@ -218,7 +231,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       float2* Xl = reinterpret_cast<float2*>(base + kXBytes);
       float4* Ah = reinterpret_cast<float4*>(base + 2 * kXBytes);
       float4* Al = reinterpret_cast<float4*>(base + 2 * kXBytes + a_plane);
-      if (st + 1 < blk.nst) load_stage(st + 1, xn, an);
+      if (st + 1 < blk.nst) load_stage(st + 1, ixv, xn, an);
+      if (st + 2 < blk.nst) load_idx(st + 2, ixn);
       if (g >= 2 && !mbar_wait(&bar[buf], (uint32_t)(((g >> 1) - 1) & 1))) {
         atomicOr(err, 1u);
         abort_flag = 1;
@@ -249,7 +263,10 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         }
       }
 #pragma unroll
-      for (int i = 0; i < 8; ++i) xv[i] = xn[i];
+      for (int i = 0; i < 8; ++i) {
+        xv[i] = xn[i];
+        ixv[i] = ixn[i];
+      }
 #pragma unroll
       for (int q = 0; q < 4; ++q) av[q] = an[q];
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

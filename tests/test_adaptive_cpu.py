@@ -56,8 +56,19 @@ def test_adaptive_operator_refuses_uniform_only_entry_points(ls):
     op.close()
 
 
+# Further adaptive trees: the scattered-field operator (findPhi = 0) at
+# kappa 20; a shallower tree (treeAdaptivity 4) at NCA tolerance 1e-10; 5 x 5
+# nodes per leaf. Skeletons equal the oracle's in all of them; the TOL 1e-10
+# tree sits at ~1e-11 from the oracle (measured 1.2e-11 and 1.6e-11), the
+# rounding of the folded Atilde^-1 blocks against the oracle's per-box solves.
+OTHER = [(dict(README, kappa=20.0, findPhi=0), 1e-12),
+         (dict(README, kappa=20.0, TOL_POW=10, treeAdaptivity=4), 1e-10),
+         (dict(README, nChebNodes=5, degreeOfBases=5), 1e-10)]
+
+
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
-def test_adaptive_packed_program_in_bounds_and_equal_to_oracle(ls, ora, tmp_path):
+@pytest.mark.parametrize("cfg,bound", [(README, 1e-12)] + OTHER)
+def test_adaptive_packed_program_in_bounds_and_equal_to_oracle(ls, ora, tmp_path, cfg, bound):
     """The packed gather-GEMV program of the adaptive operator -- every tile,
     gather index and output row the device kernels touch -- run on the host
     by tests/cpp/packed_program_check.cpp: all accesses in bounds, no output
@@ -69,8 +80,8 @@ def test_adaptive_packed_program_in_bounds_and_equal_to_oracle(ls, ora, tmp_path
                     src, "-o", exe], check=True, capture_output=True, timeout=600)
     cfg_path, x_path, y_path = (str(tmp_path / n) for n in ("cfg.bin", "x.bin", "y.bin"))
     with open(cfg_path, "wb") as f:
-        f.write(bytes(ls.Config(**README).to_c()))
-    a = ora.AdaptiveOracle(README, treeAdaptivity=5)
+        f.write(bytes(ls.Config(**cfg).to_c()))
+    a = ora.AdaptiveOracle(cfg, treeAdaptivity=cfg["treeAdaptivity"])
     rng = np.random.default_rng(3)
     x = rng.uniform(-1, 1, a.N) + 1j * rng.uniform(-1, 1, a.N)
     x.astype(np.complex128).tofile(x_path)
@@ -79,4 +90,4 @@ def test_adaptive_packed_program_in_bounds_and_equal_to_oracle(ls, ora, tmp_path
     y = np.fromfile(y_path, dtype=np.complex128)
     ya = a.matvec(x)
     a.close()
-    assert np.linalg.norm(y - ya) / np.linalg.norm(ya) <= 1e-12
+    assert np.linalg.norm(y - ya) / np.linalg.norm(ya) <= bound

@@ -41,6 +41,28 @@ def test_adaptive_matvec_matches_oracle(ls, pair):
         op.set_f64_kernels(ls.LS_F64_NATIVE)
 
 
+@pytest.mark.parametrize("over", [dict(kappa=20.0, findPhi=0), dict(kappa=20.0, TOL_POW=10, treeAdaptivity=4)])
+def test_adaptive_matvec_matches_oracle_on_other_trees(ls, ora, over):
+    cfg = dict(README, **over)
+    op = ls.Operator(ls.Config(**cfg), device=0)
+    a = ora.AdaptiveOracle(cfg, treeAdaptivity=cfg["treeAdaptivity"])
+    rng = np.random.default_rng(7)
+    x = rng.uniform(-1, 1, op.N) + 1j * rng.uniform(-1, 1, op.N)
+    ya = a.matvec(x)
+    assert _rel(op.matvec(x), ya) <= 1e-10
+    op.set_f64_kernels(ls.LS_F64_DOUBLE_FLOAT)
+    assert _rel(op.matvec(x), ya) <= 1e-10
+    op.enable_f32()
+    torch = pytest.importorskip("torch")
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.empty_like(xt)
+    op.matvec_device(xt.data_ptr(), yt.data_ptr(), 0, precision=ls.LS_PREC_F32)
+    torch.cuda.synchronize()
+    assert _rel(yt.cpu().numpy(), ya) <= 5e-5  # the FP32 operator's bound
+    op.close()
+    a.close()
+
+
 def test_gpu_restarted_gmres_reproduces_readme_residuals(ls, pair):
     op, a = pair
     b = a.rhs()
