@@ -558,8 +558,8 @@ __global__ void features_kernel(int G, int B, int S, const float* __restrict__ Q
 //     at those kx and their per-mode channel mixing of layer p into O.
 // A row needs only its own previous values and O, and a column item only
 // its H1 column, so one barrier after each phase suffices (2 L in all).
-// Same arithmetic as the separate kernels above, in the same order per
-// output, except that the x-DFT sums run in two halves.
+// Same arithmetic as the separate kernels above, except that the DFT sums
+// run as several interleaved partial sums (independent FMA chains).
 struct Fwd1Args {
   int G, M, L, PW;
   const float* in;    // [G*G][6]
@@ -630,20 +630,25 @@ __global__ void __launch_bounds__(kF1Threads, 1) forward1_kernel(Fwd1Args a) {
       } else {
         const int l = p - 1;
         for (int i = tid; i < G * 32; i += nt) hs_old[i] = a.h[row0 * 32 + i];
-        // x-synthesis of this row (x = r) from the layer's mixed spectrum.
-        for (int i = tid; i < M * 32; i += nt) {
-          const int ky = i >> 5, c = i & 31;
-          float ar = 0.f, ai = 0.f;
-#pragma unroll 8
+        // x-synthesis of this row (x = r) from the layer's mixed spectrum:
+        // two channels per thread (one 16-byte load per mode), so that the
+        // M * 16 items take one round and 16 loads are in flight per thread.
+        for (int i = tid; i < M * 16; i += nt) {
+          const int ky = i >> 4, c2 = (i & 15) * 2;
+          float ar0 = 0.f, ai0 = 0.f, ar1 = 0.f, ai1 = 0.f;
+#pragma unroll 16
           for (int m = 0; m < NM2; ++m) {
             const int f = m < M ? m : G - 2 * M + m;
             const float2 t = ts[(f * r) & (G - 1)];
-            const float2 v = __ldcg(a.O + ((long long)m * M + ky) * 32 + c);
-            ar = fmaf(t.x, v.x, fmaf(-t.y, v.y, ar));
-            ai = fmaf(t.x, v.y, fmaf(t.y, v.x, ai));
+            const float4 v = __ldcg(reinterpret_cast<const float4*>(a.O + ((long long)m * M + ky) * 32 + c2));
+            ar0 = fmaf(t.x, v.x, fmaf(-t.y, v.y, ar0));
+            ai0 = fmaf(t.x, v.y, fmaf(t.y, v.x, ai0));
+            ar1 = fmaf(t.x, v.z, fmaf(-t.y, v.w, ar1));
+            ai1 = fmaf(t.x, v.w, fmaf(t.y, v.z, ai1));
           }
           const float sk = (ky ? 2.f : 1.f) / GG;
-          gs[i] = make_float2(ar * sk, ai * sk);
+          gs[ky * 32 + c2] = make_float2(ar0 * sk, ai0 * sk);
+          gs[ky * 32 + c2 + 1] = make_float2(ar1 * sk, ai1 * sk);
         }
         for (int i = tid; i < 1024; i += nt) ps[(i >> 5) * 33 + (i & 31)] = a.pw_w[l][i];
         if (p == L) {
@@ -685,14 +690,19 @@ __global__ void __launch_bounds__(kF1Threads, 1) forward1_kernel(Fwd1Args a) {
         for (int i = tid; i < G * 32; i += nt) a.h[row0 * 32 + i] = hs_new[i];
         for (int item = tid; item < M * 32; item += nt) {
           const int ky = item >> 5, c = item & 31;
-          float ar = 0.f, ai = 0.f;
-          for (int y = 0; y < G; ++y) {
-            const float2 t = ts[(ky * y) & (G - 1)];
-            const float v = hs_new[y * 32 + c];
-            ar = fmaf(t.x, v, ar);
-            ai = fmaf(-t.y, v, ai);
+          // four interleaved partial sums (independent FMA chains)
+          float ar[4] = {0.f, 0.f, 0.f, 0.f}, ai[4] = {0.f, 0.f, 0.f, 0.f};
+          for (int y = 0; y < G; y += 4) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const float2 t = ts[(ky * (y + u)) & (G - 1)];
+              const float v = hs_new[(y + u) * 32 + c];
+              ar[u] = fmaf(t.x, v, ar[u]);
+              ai[u] = fmaf(-t.y, v, ai[u]);
+            }
           }
-          a.H1[((long long)r * M + ky) * 32 + c] = make_float2(ar, ai);
+          a.H1[((long long)r * M + ky) * 32 + c] = make_float2((ar[0] + ar[1]) + (ar[2] + ar[3]),
+                                                               (ai[0] + ai[1]) + (ai[2] + ai[3]));
         }
       } else {
         const int nk = PW >> 5;
@@ -746,17 +756,20 @@ __global__ void __launch_bounds__(kF1Threads, 1) forward1_kernel(Fwd1Args a) {
       for (int it = tid; it < 2 * kMixGroup * 32; it += nt) {
         const int half = it / (kMixGroup * 32), rem = it - half * kMixGroup * 32;
         const int mm = rem >> 5, c = rem & 31, m = m0 + mm;
-        float ar = 0.f, ai = 0.f;
+        float ar[2] = {0.f, 0.f}, ai[2] = {0.f, 0.f};
         if (m < NM2) {
           const int f = m < M ? m : G - 2 * M + m;
-          for (int x = half * (G >> 1); x < (half + 1) * (G >> 1); ++x) {
-            const float2 t = ts[(f * x) & (G - 1)];
-            const float2 v = ins[x * 32 + c];
-            ar = fmaf(t.x, v.x, fmaf(t.y, v.y, ar));
-            ai = fmaf(t.x, v.y, fmaf(-t.y, v.x, ai));
+          for (int x = half * (G >> 1); x < (half + 1) * (G >> 1); x += 2) {
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {  // two interleaved partial sums
+              const float2 t = ts[(f * (x + u)) & (G - 1)];
+              const float2 v = ins[(x + u) * 32 + c];
+              ar[u] = fmaf(t.x, v.x, fmaf(t.y, v.y, ar[u]));
+              ai[u] = fmaf(t.x, v.y, fmaf(-t.y, v.x, ai[u]));
+            }
           }
         }
-        part[it] = make_float2(ar, ai);
+        part[it] = make_float2(ar[0] + ar[1], ai[0] + ai[1]);
       }
       __syncthreads();
       for (int it = tid; it < kMixGroup * 32; it += nt) {
