@@ -22,22 +22,24 @@
 // core's FP32 accumulation is not round-to-nearest over long sums (measured:
 // 3x the error of the CUDA-core FP32 form on blocks of ~1,000 columns), so
 // each accumulator covers kChunkStages stages (128 real columns) and is then
-// promoted into FP32 registers, round-to-nearest; two tensor-memory slots
-// alternate so that the tensor core keeps working while a slot is read.
+// added to running FP32 sums (round-to-nearest) that are also kept in tensor
+// memory, next to the two accumulator slots, which alternate so that the
+// tensor core keeps working while a slot is read.
 //
 // Kernel structure (tc_gemm_kernel): a persistent grid of two CTAs per SM, 128 threads per CTA
 // (four warps, one per 32-lane quarter of tensor memory). Blocks of the
 // phase are dealt round-robin. Per block the K columns are walked in stages
 // of 16 complex columns through two shared-memory buffers: all threads
 // gather the 64-wide source rows (split hi/lo, two MMA rows per value) and
-// copy the operator stage (split hi/lo); one thread issues the 12 MMAs of a
-// stage (4 K-steps x 3 products) and commits them to the buffer's mbarrier,
-// which the threads wait on before they refill that buffer two stages later.
-// The last stage of a chunk is also committed to its accumulator slot's
-// mbarrier; before a slot is reused the four warps read it out of tensor
-// memory (tcgen05.ld 32x32b, each warp its 32 lanes) and add it to their
-// registers. After the last chunk they write, add to, or combine the
-// registers into the destination. Every mbarrier wait is bounded; a wait that gives up sets
+// copy the operator stage (split hi/lo), with the loads of the next two
+// stages in flight; one thread issues the 12 MMAs of a stage (4 K-steps x 3
+// products) and commits them to the buffer's mbarrier, which the threads
+// wait on before they refill that buffer two stages later. The last stage
+// of a chunk is also committed to its accumulator slot's mbarrier; before a
+// slot is reused the four warps read it out of tensor memory (tcgen05.ld
+// 32x32b, each warp its 32 lanes) and add it to the sums (tcgen05.st).
+// After the last chunk they write, add to, or combine the sums into the
+// destination, eight rows at a time with their loads batched. Every mbarrier wait is bounded; a wait that gives up sets
 // the error flag, the CTA skips its remaining work and still frees its
 // tensor memory.
 
@@ -62,7 +64,8 @@ constexpr int kXBytes = 128 * 128;             // one plane (hi or lo) of the 12
 constexpr long long kWaitLimit = 20000000;     // mbarrier polls before a wait gives up
 constexpr int kMaxRows = 64;                   // block rows per MMA tile (N <= 64; larger blocks are split)
 constexpr int kChunkStages = 4;                // stages accumulated in tensor memory before promotion
-constexpr int kTmemCols = 2 * kMaxRows;        // two accumulator slots
+constexpr int kSumCol = 2 * kMaxRows;          // tensor-memory columns of the running FP32 sums
+constexpr int kTmemCols = 256;                 // two accumulator slots and the sums (a power of two)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -133,6 +136,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   __shared__ uint64_t accbar[2];  // per accumulator slot: its chunk completed
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
+  __shared__ int orows[kMaxRows];  // the current block's output rows
   const int t = threadIdx.x, warp = t >> 5;
   const int a_plane = npad_max * 128;               // bytes of one operator plane
   const int buf_bytes = 2 * kXBytes + 2 * a_plane;  // Xh, Xl, Ah, Al
@@ -161,52 +165,70 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   const int l16 = t & 15, hw = t >> 4, j8 = l16 & 7, cpar = l16 >> 3;
   long long g = 0;   // stages issued by this CTA (buffer g & 1, use g >> 1)
   long long gc = 0;  // chunks issued by this CTA (accumulator slot gc & 1, use gc >> 1)
-  float acc[kMaxRows];
-  // acc[n] += the accumulator slot's column n (this thread's lane).
-  auto promote = [&](int slot, int npad) {
+  // The running FP32 sums of a block live in tensor memory next to the two
+  // accumulator slots (columns kSumCol + n, this thread's lane), which
+  // leaves the registers to the loads in flight.
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+  auto tld8 = [&](uint32_t col, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(lane_base + col));
+  };
+  // sums[n] (+)= the accumulator slot's column n, round-to-nearest FP32;
+  // the first chunk of a block sets the sums.
+  auto promote = [&](int slot, int npad, bool first) {
 #pragma unroll
     for (int c0 = 0; c0 < kMaxRows; c0 += 8) {
       if (c0 < npad) {
-        uint32_t r[8];
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                     : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(slot * kMaxRows + c0)));
+        uint32_t r[8], q[8];
+        tld8((uint32_t)(slot * kMaxRows + c0), r);
+        if (!first) tld8((uint32_t)(kSumCol + c0), q);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (!first) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) acc[c0 + i] += __uint_as_float(r[i]);
+          for (int i = 0; i < 8; ++i) r[i] = __float_as_uint(__uint_as_float(q[i]) + __uint_as_float(r[i]));
+        }
+        asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(
+                         lane_base + (uint32_t)(kSumCol + c0)),
+                     "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+                     : "memory");
       }
     }
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
   };
   for (int b = blockIdx.x; b < n_blocks; b += gridDim.x) {
     const TcBlock blk = blocks[b];
     const uint32_t idesc = idesc_base | ((uint32_t)(blk.npad >> 3) << 17);
-#pragma unroll
-    for (int n = 0; n < kMaxRows; ++n) acc[n] = 0.f;
     const long long gc0 = gc;
+    // Output rows of the block, loaded now so that they have arrived by the
+    // epilogue (the barriers of the stage loop order the shared stores before
+    // their reads there).
+    if (t < blk.rows) orows[t] = __ldg(out + blk.o_off + t);
     const int nchunks = (blk.nst + kChunkStages - 1) / kChunkStages;
     // Loads of stage st: 8 gathered right-hand-side values and up to 4
-    // operator vectors per thread. Stage st + 1's loads are issued before
-    // stage st is stored, so every thread has two stages of loads in flight;
-    // the gather indices are loaded one stage earlier still, so the
-    // dependent index load is off the critical path.
-    float2 xv[8], xn[8];
-    float4 av[4], an[4];
-    int ixv[8], ixn[8];  // gather sources of the next stage and of the one after (-1: past K)
-    auto load_idx = [&](int st, int* ix) {
+    // operator vectors per thread. The loads of stages st + 1 and st + 2 are
+    // in flight while stage st is stored (x0/a0: stage st, x1/a1: st + 1,
+    // x2/a2: st + 2), and the gather indices are loaded a stage earlier
+    // still (ix: stage st + 3), so the dependent index load is off the
+    // critical path.
+    float2 x0[8], x1[8], x2[8];
+    float4 a0[4], a1[4], a2[4];
+    int ix[8];  // gather sources of a stage not yet loaded (-1: past K)
+    auto load_idx = [&](int st, int* ixp) {
       const int k0 = st * kStageCols;
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int ci = hw * 8 + i;
         const int k = k0 + 2 * (ci >> 3) + cpar;
-        ix[i] = k < blk.K ? __ldg(idx + blk.i_off + k) : -1;
+        ixp[i] = k < blk.K ? __ldg(idx + blk.i_off + k) : -1;
       }
     };
-    auto load_stage = [&](int st, const int* ix, float2* x, float4* a) {
+    auto load_stage = [&](int st, const int* ixp, float2* x, float4* a) {
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int ci = hw * 8 + i;
         const int jj = (ci & 7) * 8 + j8;
-        x[i] = ix[i] >= 0 ? ld_chain(src + (size_t)ix[i] * 64 + jj) : make_float2(0.f, 0.f);
+        x[i] = ixp[i] >= 0 ? ld_chain(src + (size_t)ixp[i] * 64 + jj) : make_float2(0.f, 0.f);
       }
       // npad rows x 16 complex columns in the canonical layout: npad * 8 <= 512 float4.
       const float4* As = reinterpret_cast<const float4*>(A + blk.a_off + (long long)st * blk.npad * kStageCols);
@@ -217,10 +239,14 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       }
     };
     if (blk.nst > 0) {
-      load_idx(0, ixv);
-      load_stage(0, ixv, xv, av);
+      load_idx(0, ix);
+      load_stage(0, ix, x0, a0);
     }
-    if (blk.nst > 1) load_idx(1, ixv);
+    if (blk.nst > 1) {
+      load_idx(1, ix);
+      load_stage(1, ix, x1, a1);
+    }
+    if (blk.nst > 2) load_idx(2, ix);
     for (int st = 0; st < blk.nst; ++st, ++g) {
       const int buf = (int)(g & 1);
       const long long G = gc0 + st / kChunkStages;  // chunk of this stage
@@ -231,8 +257,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       float2* Xl = reinterpret_cast<float2*>(base + kXBytes);
       float4* Ah = reinterpret_cast<float4*>(base + 2 * kXBytes);
       float4* Al = reinterpret_cast<float4*>(base + 2 * kXBytes + a_plane);
-      if (st + 1 < blk.nst) load_stage(st + 1, ixv, xn, an);
-      if (st + 2 < blk.nst) load_idx(st + 2, ixn);
+      if (st + 2 < blk.nst) load_stage(st + 2, ix, x2, a2);
+      if (st + 3 < blk.nst) load_idx(st + 3, ix);
       if (g >= 2 && !mbar_wait(&bar[buf], (uint32_t)(((g >> 1) - 1) & 1))) {
         atomicOr(err, 1u);
         abort_flag = 1;
@@ -243,7 +269,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       for (int i = 0; i < 8; ++i) {
         const int ci = hw * 8 + i;
         const int jj = (ci & 7) * 8 + j8, cc = 2 * (ci >> 3) + cpar;
-        const float2 v = xv[i];
+        const float2 v = x0[i];
         const float hx = tf32_rn(v.x), hy = tf32_rn(v.y);
         const float lx = tf32_rn(v.x - hx), ly = tf32_rn(v.y - hy);
         const int o_re = canon(jj, cc), o_im = canon(64 + jj, cc);
@@ -256,7 +282,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       for (int q = 0; q < 4; ++q) {
         const int u = t + q * kTcThreads;
         if (u < blk.npad * 8) {
-          const float4 v = av[q];
+          const float4 v = a0[q];
           const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
           Ah[u] = h;
           Al[u] = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
@@ -264,11 +290,14 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       }
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        xv[i] = xn[i];
-        ixv[i] = ixn[i];
+        x0[i] = x1[i];
+        x1[i] = x2[i];
       }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) av[q] = an[q];
+      for (int q = 0; q < 4; ++q) {
+        a0[q] = a1[q];
+        a1[q] = a2[q];
+      }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       // Slot G & 1 still holds chunk G - 2 of this block: add it to the
       // registers before the slot is reused (its commit is the slot's latest).
@@ -278,7 +307,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           abort_flag = 1;
         } else {
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          promote((int)(G & 1), blk.npad);
+          promote((int)(G & 1), blk.npad, G - 2 == gc0);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -316,28 +345,52 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      promote((int)(G & 1), blk.npad);
+      promote((int)(G & 1), blk.npad, G == gc0);
     }
     __syncthreads();
     if (abort_flag) break;
+    // Epilogue, eight rows at a time: their output indices and old values
+    // are all loaded before any of them is written (the rows of a phase are
+    // distinct), so a group costs one round trip, not eight.
     const int m = t, part = m >> 6, j = m & 63;
+    float* dstf = reinterpret_cast<float*>(dst);
+    for (int c0 = 0; c0 < blk.rows; c0 += 8) {
+      uint32_t r[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};  // a block without columns sums to zero
+      if (nchunks > 0) tld8((uint32_t)(kSumCol + c0), r);
+      size_t e[8];
+      float base[8], extra[8], scale[8];
 #pragma unroll
-    for (int n = 0; n < kMaxRows; ++n) {
-      if (n >= blk.rows) break;
-      const int orow = __ldg(out + blk.o_off + n);
-      const size_t e = ((size_t)orow * 64 + j) * 2 + part;
-      float* dp = reinterpret_cast<float*>(dst) + e;
-      const float v = acc[n];
-      if (mode == 0) {
-        *dp = v;
-      } else if (mode == 1) {
-        *dp = ld_chain(dp) + v;
-      } else {
-        const float p = ld_chain(reinterpret_cast<const float*>(P) + e);
-        if (find_phi)
-          *dp = p + __ldg(kq + orow) * v + ld_chain(reinterpret_cast<const float*>(src) + e);
+      for (int i = 0; i < 8; ++i) {
+        const int orow = c0 + i < blk.rows ? orows[c0 + i] : 0;
+        e[i] = ((size_t)orow * 64 + j) * 2 + part;
+        scale[i] = (mode == 2 && find_phi) ? __ldg(kq + orow) : 1.f;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        base[i] = extra[i] = 0.f;
+        if (c0 + i < blk.rows) {
+          if (mode == 1) {
+            base[i] = ld_chain(dstf + e[i]);
+          } else if (mode == 2) {
+            base[i] = ld_chain(reinterpret_cast<const float*>(P) + e[i]);
+            if (find_phi) extra[i] = ld_chain(reinterpret_cast<const float*>(src) + e[i]);
+          }
+        }
+      }
+      if (nchunks > 0) asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        if (c0 + i >= blk.rows) break;
+        const float v = __uint_as_float(r[i]);
+        // mode 0: v; mode 1: old + v; mode 2: P + s v, + x with find_phi
+        if (mode == 0)
+          dstf[e[i]] = v;
+        else if (mode == 1)
+          dstf[e[i]] = base[i] + v;
+        else if (find_phi)
+          dstf[e[i]] = base[i] + scale[i] * v + extra[i];
         else
-          *dp = p + v;
+          dstf[e[i]] = base[i] + v;
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
