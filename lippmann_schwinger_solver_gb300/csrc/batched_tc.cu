@@ -17,7 +17,7 @@
 // 16 complex columns after another, so that staging it is a linear copy.
 //
 // Precision: FP32 operands through TF32 tensor cores in three products,
-// hi*hi + hi*lo + lo*hi with hi the TF32 truncation of a value and lo the
+// hi*hi + hi*lo + lo*hi with hi a value rounded to TF32 and lo the
 // FP32 remainder (lo*lo, about 2^-22 relative, is dropped). The tensor
 // core's FP32 accumulation is not round-to-nearest over long sums (measured:
 // 3x the error of the CUDA-core FP32 form on blocks of ~1,000 columns), so
