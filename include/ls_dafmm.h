@@ -164,7 +164,10 @@ ls_status ls_op_set_f64_kernels(ls_op* op, int kernels);
 #define LS_STATIC_SCRATCH_ELEMS (1LL << 20)
 ls_status ls_matvec_noalloc(ls_op* op, const double* x, double* y, void* stream);
 /* Host-buffer convenience: copies x in, runs ls_matvec, copies y out, syncs.
- * This is the call a reference-style driver makes (Vec in, Vec out). */
+ * This is the call a reference-style driver makes (Vec in, Vec out). When x
+ * and y are distinct page-locked buffers (cudaMallocHost, cudaHostRegister)
+ * the matvec reads x from and writes y to host memory directly, without
+ * separate copies; the result is the same. */
 ls_status ls_matvec_host(ls_op* op, const double* x, double* y);
 
 /*

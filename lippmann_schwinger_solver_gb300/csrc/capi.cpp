@@ -268,11 +268,33 @@ ls_status ls_matvec_noalloc(ls_op* op, const double* x, double* y, void* stream)
   return LS_OK;
 }
 
+// Device address of a page-locked host buffer (cudaMallocHost,
+// cudaHostRegister, torch pin_memory), or nullptr for any other pointer.
+static void* pinned_device_address(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 ls_status ls_matvec_host(ls_op* op, const double* x, double* y) {
   if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec_host: null argument");
   if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_host: operator was assembled without a device");
   DevOperator& d = op->dev;
   cudaSetDevice(d.device);
+  // Page-locked buffers: the matvec's first kernel reads x from host memory
+  // and its output kernel writes y there, so the transfers overlap the
+  // kernels instead of running as separate copies.
+  void* xd = pinned_device_address(x);
+  void* yd = xd ? pinned_device_address(y) : nullptr;
+  if (xd && yd && xd != yd) {
+    cudaError_t e = dev_matvec(d, (const double2*)xd, (double2*)yd, d.stream, false);
+    if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_host");
+    if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_matvec_host sync");
+    return LS_OK;
+  }
   const size_t bytes = (size_t)d.N * sizeof(double2);
   cudaError_t e = cudaMemcpyAsync(d.xbuf, x, bytes, cudaMemcpyHostToDevice, d.stream);
   if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_host H2D");
