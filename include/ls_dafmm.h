@@ -80,6 +80,15 @@ typedef struct {
    * interpolation and network entry points return LS_E_STATE for them. */
   int tree_adaptive;
   int treeAdaptivity;
+  /* 1: the precomputation quadratures (far moments M and near blocks) run on
+   * the operator's GPU; 0 (zero-initialised, the default): on the host
+   * cores, as the reference does. The GPU's values differ from the host's in
+   * the last bits; M entries that are zero by symmetry then carry other
+   * round-off, and NCA pivots among entries at that noise level change, so
+   * the operator is no longer the oracle's bit for bit (its matvec stays
+   * within about 1e-7 of it on the tested trees). Operators assembled
+   * without a device always integrate on the host. */
+  int precompute_on_gpu;
 } ls_config;
 
 typedef struct {

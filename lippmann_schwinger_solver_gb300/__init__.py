@@ -89,6 +89,7 @@ class _Config(ctypes.Structure):
         ("bump_w", ctypes.c_double * MAX_BUMPS),
         ("tree_adaptive", ctypes.c_int),
         ("treeAdaptivity", ctypes.c_int),
+        ("precompute_on_gpu", ctypes.c_int),
     ]
 
 
@@ -141,11 +142,13 @@ class Config:
     bumps: tuple = ()  # ((cx, cy, a, w), ...) for Qchoice 6
     tree_adaptive: int = 0   # 1: the reference's adaptive quadtree (createAdaptiveTree + 2:1 balance)
     treeAdaptivity: int = 5  # adaptive: boxes split until q is resolved to 10^-treeAdaptivity
+    precompute_on_gpu: int = 0  # 1: precomputation quadratures on the operator's GPU (not bit-exact with the host)
 
     def to_c(self):
         c = _Config()
         for f in ("nCones_LFR", "nChebNodes", "yes2DFMM", "TOL_POW", "degreeOfBases", "nLevelsUniform",
-                  "Qchoice", "findPhi", "reference_rounding", "tree_adaptive", "treeAdaptivity"):
+                  "Qchoice", "findPhi", "reference_rounding", "tree_adaptive", "treeAdaptivity",
+                  "precompute_on_gpu"):
             setattr(c, f, int(getattr(self, f)))
         c.L = float(self.L)
         c.kappa = float(self.kappa)

@@ -17,7 +17,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CXX_SOURCES = ["assemble.cpp", "capi.cpp"]
-CU_SOURCES = ["matvec.cu", "matvec_df.cu", "gmres.cu", "batched.cu", "fno.cu", "nn_precond.cu", "peaks.cu", "batched_tc.cu"]
+CU_SOURCES = ["matvec.cu", "matvec_df.cu", "gmres.cu", "batched.cu", "fno.cu", "nn_precond.cu", "peaks.cu", "batched_tc.cu",
+              "quadrature.cu"]
 
 
 def _nvcc():

@@ -195,6 +195,11 @@ cd quad2d(const F& f, const std::vector<double>& gx, const std::vector<double>& 
   return total;
 }
 
+thread_local int t_assembly_device = -1;
+// Device for the precomputation quadratures of an assembly with cfg: its GPU
+// when cfg asks for it (and there is one), else none.
+int quadrature_device(const ls_config& cfg) { return cfg.precompute_on_gpu ? t_assembly_device : -1; }
+
 // ---------------------------------------------------------------- small dense QR
 // Column-pivoted Householder QR (xGEQP3 with norm downdating); solve()
 // returns the basic least-squares solution on the nonzero pivots.
@@ -987,10 +992,28 @@ void Builder::precompute() {
   }
   const int nS = 2 * kSeries + 1;
   const double rj = radius[nL];
+  static const double ncx[9] = {-2, 0, 2, 2, 2, 0, -2, -2, 0};
+  static const double ncy[9] = {-2, -2, -2, 0, 2, 2, 2, 0, 0};
+  const double rA = radius[nL], rB = radius[nL];
+  // The quadratures below (far moments, then near integrals) run on the
+  // operator's GPU when it has one; otherwise, or if that fails, on the host.
+  std::vector<QuadTask> tasks;
+  tasks.reserve((size_t)nS * nb + (size_t)9 * rank * nb);
+  for (int t = 0; t < nS * nb; ++t)
+    tasks.push_back({0.0, 0.0, kappa * rj, bases[t % nb].first, bases[t % nb].second, t / nb - kSeries, 1});
+  for (int t = 0; t < 9 * rank; ++t) {
+    const int q = t / rank, i = t % rank;
+    const double Xx = (rA * cheb1[i % n1] + 0.0 - ncx[q] * rA) / rB, Xy = (rA * cheb1[i / n1] + 0.0 - ncy[q] * rA) / rB;
+    for (int l = 0; l < nb; ++l) tasks.push_back({Xx, Xy, kappa * rB, bases[l].first, bases[l].second, 0, 0});
+  }
+  std::vector<cd> qv;
+  const bool on_gpu = gpu_quadrature(quadrature_device(cfg), tasks, gln, glw, qv);
   // Far moments C (2S+1) x nb, then M = C Q^+ rounded like the text cache.
   std::vector<cd> C((size_t)nS * nb);
+  if (on_gpu)
+    for (int t = 0; t < nS * nb; ++t) C[t] = rj * rj * qv[t];
 #pragma omp parallel for schedule(dynamic, 1)
-  for (int t = 0; t < nS * nb; ++t) {
+  for (int t = 0; t < (on_gpu ? 0 : nS * nb); ++t) {
     const int n = t / nb - kSeries, l = t % nb;
     const int a = bases[l].first, b = bases[l].second;
     auto f = [&](double x, double y) -> cd {
@@ -1012,14 +1035,13 @@ void Builder::precompute() {
     }
   // Colleague near blocks: V(i,l) = int H0(k r |X_i - P|) T_a T_b dP, then
   // V (i r^2 / 4) Q^+.
-  static const double ncx[9] = {-2, 0, 2, 2, 2, 0, -2, -2, 0};
-  static const double ncy[9] = {-2, -2, -2, 0, 2, 2, 2, 0, 0};
-  const double rA = radius[nL], rB = radius[nL];
   std::vector<cd> V((size_t)9 * rank * nb);
+  if (on_gpu)
+    for (size_t t = 0; t < V.size(); ++t) V[t] = qv[(size_t)nS * nb + t];
   int max_order = 0;
   for (const auto& ab : bases) max_order = std::max(max_order, std::max(ab.first, ab.second));
 #pragma omp parallel for schedule(dynamic, 1)
-  for (int t = 0; t < 9 * rank; ++t) {
+  for (int t = 0; t < (on_gpu ? 0 : 9 * rank); ++t) {
     const int q = t / rank, i = t % rank;
     const double bx = ncx[q] * rA, by = ncy[q] * rA;
     const double ax = rA * cheb1[i % n1] + 0.0, ay = rA * cheb1[i / n1] + 0.0;
@@ -1774,5 +1796,14 @@ bool assemble(const ls_config& cfg, HostOperator& op, std::string& err) {
 }
 
 double contrast_at(const ls_config& cfg, double x, double y) { return contrast_fn(cfg, x, y); }
+
+void set_assembly_device(int device) { t_assembly_device = device; }
+
+// The GPU quadrature (csrc/quadrature.cu) replaces this stub in the library;
+// a host-only build keeps it and integrates on the host.
+__attribute__((weak)) bool gpu_quadrature(int, const std::vector<QuadTask>&, const std::vector<double>&,
+                                          const std::vector<double>&, std::vector<cd>&) {
+  return false;
+}
 
 }  // namespace lsg

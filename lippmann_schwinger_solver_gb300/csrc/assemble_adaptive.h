@@ -299,6 +299,11 @@ class AdaptiveBuilder {
       };
       C[(size_t)(n + kSeries) * nb + l] = rj * rj * quad2d(f, gln, glw);
     }
+    finish_M(j, C);
+  }
+  // M = C Q^+ of leaf level j, rounded like the text cache.
+  void finish_M(int j, const std::vector<cd>& C) {
+    const int nS = 2 * kSeries + 1;
     std::vector<cd> M((size_t)nS * rank);
     for (int n = 0; n < nS; ++n)
       for (int i = 0; i < rank; ++i) {
@@ -556,6 +561,10 @@ class AdaptiveBuilder {
         V[(size_t)i * nb + l] = quad2d(f, gln, glw);
       }
     }
+    return finish_near(rB, V);
+  }
+  // Bk = V (i rB^2 / 4) Q^+, rounded like the text cache.
+  std::vector<cd> finish_near(double rB, const std::vector<cd>& V) const {
     std::vector<cd> Bk((size_t)rank * rank);
     for (int i = 0; i < rank; ++i)
       for (int k = 0; k < rank; ++k) {
@@ -564,6 +573,54 @@ class AdaptiveBuilder {
         Bk[(size_t)i * rank + k] = cfg.reference_rounding ? cd(round6(s.real()), round6(s.imag())) : s;
       }
     return Bk;
+  }
+  // Every leaf level's far moments and every near block in one GPU batch
+  // (csrc/quadrature.cu); false when there is no GPU for it (the host
+  // routines above then run).
+  bool precompute_on_gpu(const std::set<int>& leaf_levels) {
+    const int dev = quadrature_device(cfg);
+    if (dev < 0) return false;
+    const int nS = 2 * kSeries + 1;
+    std::vector<QuadTask> tasks;
+    for (int j : leaf_levels)
+      for (int t = 0; t < nS * nb; ++t)
+        tasks.push_back({0.0, 0.0, kappa * radius[j], bases[t % nb].first, bases[t % nb].second, t / nb - kSeries, 1});
+    std::vector<std::pair<double, double>> tab[4] = {offsets(0), offsets(1), offsets(2), offsets(3)};
+    struct NearKey { std::tuple<int, int, int> key; double rB; };
+    std::vector<NearKey> keys;
+    std::set<std::tuple<int, int, int>> seen;
+    for (const Ref& lf : leaves) {
+      const ABox& B = box(lf);
+      for (int kind = 0; kind < 4; ++kind)
+        for (int t = 0; t < kNbrCount[kind]; ++t) {
+          if (B.nbr[kind][t] < 0) continue;
+          const auto key = std::make_tuple(lf.first, kind, t);
+          if (!seen.insert(key).second) continue;
+          const double rA = radius[lf.first], rB = radius[lf.first + kNbrLevel[kind]];
+          const double cx = tab[kind][t].first * rA, cy = tab[kind][t].second * rA;
+          keys.push_back({key, rB});
+          for (int i = 0; i < rank; ++i) {
+            const double Xx = (rA * cheb1[i % n1] - cx) / rB, Xy = (rA * cheb1[i / n1] - cy) / rB;
+            for (int l = 0; l < nb; ++l) tasks.push_back({Xx, Xy, kappa * rB, bases[l].first, bases[l].second, 0, 0});
+          }
+        }
+    }
+    std::vector<cd> qv;
+    if (!gpu_quadrature(dev, tasks, gln, glw, qv)) return false;
+    size_t o = 0;
+    for (int j : leaf_levels) {
+      const double rj = radius[j];
+      std::vector<cd> C((size_t)nS * nb);
+      for (int t = 0; t < nS * nb; ++t) C[t] = rj * rj * qv[o + t];
+      o += (size_t)nS * nb;
+      finish_M(j, C);
+    }
+    for (const NearKey& k : keys) {
+      std::vector<cd> V(qv.begin() + o, qv.begin() + o + (size_t)rank * nb);
+      o += (size_t)rank * nb;
+      nearBlk[k.key] = finish_near(k.rB, V);
+    }
+    return true;
   }
   void precompute_near() {
     std::vector<std::pair<double, double>> tab[4] = {offsets(0), offsets(1), offsets(2), offsets(3)};
@@ -1011,10 +1068,12 @@ bool AdaptiveBuilder::run(HostOperator& op, std::string& err) {
   precompute_Q();
   std::set<int> leaf_levels;
   for (const Ref& lf : leaves) leaf_levels.insert(lf.first);
-  for (int j : leaf_levels) precompute_M(j);
   classify_neighbors();
   if (unmatched) { err = "adaptive tree: " + std::to_string(unmatched) + " near neighbours of unexpected level or offset"; return false; }
-  precompute_near();
+  if (!precompute_on_gpu(leaf_levels)) {
+    for (int j : leaf_levels) precompute_M(j);
+    precompute_near();
+  }
   op.stage_seconds[1] = lap();
   op.stage_seconds[2] = lap();
   nca();

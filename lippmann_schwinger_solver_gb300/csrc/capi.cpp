@@ -96,7 +96,10 @@ ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
   ls_op* op = new (std::nothrow) ls_op();
   if (!op) return fail(LS_E_NOMEM, "ls_op_create: out of host memory");
   std::string err;
-  if (!assemble(*cfg, op->host, err)) {
+  set_assembly_device(device);  // the precomputation quadratures may use this GPU
+  const bool assembled = assemble(*cfg, op->host, err);
+  set_assembly_device(-1);
+  if (!assembled) {
     delete op;
     return fail(LS_E_INVALID, "ls_op_create: " + err);
   }

@@ -89,8 +89,29 @@ struct HostOperator {
   double stage_seconds[LS_ASSEMBLE_STAGES] = {};  // ls_op_info_t::assemble_stage_seconds
 };
 
+// One adaptive quadrature of the assembly's precomputations over [-1,1]^2:
+// kind 0 the near-field integral of H0(k |X - p|) T_a(p_x) T_b(p_y) for a
+// target X = (xx, xy); kind 1 the far moment of J_n(k |p|) e^{-i n arg p}
+// T_a(p_x) T_b(p_y).
+struct QuadTask {
+  double xx, xy, k;
+  int a, b, n, kind;
+};
+// Integrates the tasks on the GPU `device` with the host's adaptive
+// 10 x 10 panel rule (gx, gw: its Gauss-Legendre nodes and weights);
+// returns false, out untouched, when that is not possible (no device, or
+// a bounded integral that did not finish), and the caller integrates on
+// the host. csrc/quadrature.cu; a host-only build (tests/cpp) gets a stub
+// that returns false.
+bool gpu_quadrature(int device, const std::vector<QuadTask>& tasks, const std::vector<double>& gx,
+                    const std::vector<double>& gw, std::vector<cd>& out);
+
 // assemble.cpp
 bool assemble(const ls_config& cfg, HostOperator& op, std::string& err);
+// The GPU that the calling thread's assemblies may use for their
+// precomputation quadratures (-1: none), set by ls_op_create around
+// assemble().
+void set_assembly_device(int device);
 // The contrast plugin q(x, y) selected by cfg (userkernel::ContrastFunction).
 double contrast_at(const ls_config& cfg, double x, double y);
 

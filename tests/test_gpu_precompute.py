@@ -1,0 +1,78 @@
+"""Precomputation quadratures on the GPU (csrc/quadrature.cu,
+ls_config.precompute_on_gpu = 1) against the same operator integrated on
+the host cores (the default, bit-exact with the oracle).
+
+The GPU values differ from the host's in the last bits. After the
+reference's 6-digit rounding the far moments M and the near blocks are
+equal but for entries that are zero by symmetry (round-off noise near
+1e-36 of the largest) and rare rounding ties; the NCA pivots among entries
+at that noise level then differ, so the GPU-integrated operator is not the
+oracle's bit for bit. The bars below: M and the near blocks within one unit
+of the 6th digit of their largest entry, the matvec within 1e-6 of the
+oracle (measured 2e-8 to 7e-8), and the precomputation faster on the GPU.
+Also the adaptive tree of the reference's README run, whose precomputation
+(53 near blocks per leaf level) dominates its host assembly."""
+import numpy as np
+import pytest
+
+from conftest import CFG_C1, CFG_L5_BUMPS, full_cfg
+
+pytestmark = pytest.mark.gpu
+
+README = dict(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, TOL_POW=8, degreeOfBases=6, nLevelsUniform=5, Qchoice=0,
+              findPhi=1, reference_rounding=1, L=0.5, kappa=40.0, tree_adaptive=1, treeAdaptivity=5)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _skeleton_agreement(a, b):
+    n = min(len(a), len(b))
+    return float(np.mean(a[:n] == b[:n])) if n else 1.0
+
+
+@pytest.mark.parametrize("base", [CFG_C1, CFG_L5_BUMPS])
+def test_gpu_precomputations_against_host_ones(ls, ora, base):
+    cfg = full_cfg(base)
+    host = ls.Operator(cfg, device=0)
+    gpu = ls.Operator(full_cfg(base, precompute_on_gpu=1), device=0)
+    t_gpu, t_host = gpu.info["assemble_stage_seconds"][1], host.info["assemble_stage_seconds"][1]
+    Mg, Bg = gpu.precomputations()
+    Mh, Bh = host.precomputations()
+    o = ora.Oracle(cfg.as_dict())
+    rng = np.random.default_rng(13)
+    x = rng.uniform(-1, 1, gpu.N) + 1j * rng.uniform(-1, 1, gpu.N)
+    e_gpu = _rel(gpu.matvec(x), o.matvec(x))
+    agree = _skeleton_agreement(gpu.skeleton_dump(), host.skeleton_dump())
+    print(f"precompute stage: GPU {t_gpu:.3f} s, host {t_host:.3f} s; matvec vs oracle {e_gpu:.2e}; "
+          f"skeleton agreement {agree:.4f}; M entries differing {np.count_nonzero(Mg != Mh)} of {Mh.size}")
+    assert np.max(np.abs(Mg - Mh)) <= 1e-5 * np.max(np.abs(Mh))
+    assert np.max(np.abs(Bg - Bh)) <= 1e-5 * np.max(np.abs(Bh))
+    assert e_gpu <= 1e-6
+    assert np.array_equal(host.skeleton_dump(), o.skeleton_dump())  # the default stays the oracle's
+    assert t_gpu < t_host
+    o.close()
+    gpu.close()
+    host.close()
+
+
+def test_gpu_precomputations_of_the_adaptive_readme_tree(ls, ora):
+    host = ls.Operator(ls.Config(**README), device=0)
+    gpu = ls.Operator(ls.Config(**dict(README, precompute_on_gpu=1)), device=0)
+    t_gpu, t_host = gpu.info["assemble_stage_seconds"][1], host.info["assemble_stage_seconds"][1]
+    rng = np.random.default_rng(17)
+    x = rng.uniform(-1, 1, gpu.N) + 1j * rng.uniform(-1, 1, gpu.N)
+    a = ora.AdaptiveOracle(README, treeAdaptivity=5)
+    ya = a.matvec(x)
+    e_gpu, e_host = _rel(gpu.matvec(x), ya), _rel(host.matvec(x), ya)
+    print(f"adaptive precompute stage: GPU {t_gpu:.3f} s, host {t_host:.3f} s; matvec vs oracle: "
+          f"GPU-integrated {e_gpu:.2e}, host-integrated {e_host:.2e}")
+    assert e_host <= 1e-10 and e_gpu <= 1e-6
+    b = gpu.rhs()
+    xs, hist, it, rr, code = gpu.gmres(b, 200, 1e-10)
+    assert code == ls.LS_OK and rr <= 2e-10
+    assert t_gpu < t_host
+    a.close()
+    gpu.close()
+    host.close()
