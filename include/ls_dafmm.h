@@ -76,8 +76,9 @@ typedef struct {
    * makeLevelRestriction_Tree, GMRES/GMRES.cpp:165-166): boxes split until
    * q is resolved to 10^-treeAdaptivity and no box spans more than one
    * wavelength, then 2:1 balanced. Adaptive operators support the FP64 and
-   * FP32 matvecs and the GMRES solvers; the batched, allocation-free,
-   * interpolation and network entry points return LS_E_STATE for them. */
+   * FP32 matvecs, the GMRES solvers and the batched ones; the
+   * allocation-free, interpolation and network entry points return
+   * LS_E_STATE for them. */
   int tree_adaptive;
   int treeAdaptivity;
   /* 1: the precomputation quadratures (far moments M and near blocks) run on

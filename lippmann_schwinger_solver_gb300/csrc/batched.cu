@@ -676,6 +676,11 @@ cudaError_t dev_matvec_f32_batch(DevOperator& d, const float2* x, float2* y, cud
   for (auto& ph : d.up32) launch_block<0>(ph, (const float2*)B.S, B.S, s, d.device);
   launch_block<1>(d.m2l32, (const float2*)B.S, B.P, s, d.device);
   for (auto& ph : d.down32) launch_block<2>(ph, (const float2*)B.P, B.P, s, d.device);
+  if (d.generic_near) {  // adaptive trees: the near phase accumulates into P[0:N), which is y
+    launch_block<3>(d.nearph32, (const float2*)B.S, B.P, s, d.device);
+    cudaMemcpyAsync(y, B.P, (size_t)d.N * NR8 * sizeof(float2), cudaMemcpyDeviceToDevice, s);
+    return cudaGetLastError();
+  }
   const int NS = kBatchNearSources;
   launch_pdl(near_gemm_block_kernel, (d.n_leaves + NS - 1) / NS, 352, (size_t)NS * d.rank * NR8 * sizeof(float2), s, 
       d.n_leaves, d.rank, d.nearB32, B.S, B.Z);

@@ -590,7 +590,10 @@ bool dev_enable_tc(DevOperator& d, const HostOperator& h, std::string& err) {
   T->down.resize(d.down32.size());
   for (size_t i = 0; i < d.down32.size() && e == cudaSuccess; ++i)
     e = build_far(*T, h.down[i], d.down32[i], T->down[i], err);
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess && d.generic_near) {
+    // adaptive trees: the near phase is one more gather-GEMV phase
+    e = build_far(*T, h.nearph, d.nearph32, T->near, err);
+  } else if (e == cudaSuccess) {
     TcPhase& nr = T->near;
     const int K = 9 * d.rank;
     if (d.rank > kMaxRows) {
@@ -646,7 +649,13 @@ cudaError_t dev_matvec_f32_wide(DevOperator& d, const float2* x, float2* y, floa
   if (e == cudaSuccess) e = launch_tc(T, T.m2l, S, P, 0, nullptr, nullptr, 0, s);
   for (const auto& ph : T.down)
     if (e == cudaSuccess) e = launch_tc(T, ph, P, P, 1, nullptr, nullptr, 0, s);
-  if (e == cudaSuccess) e = launch_tc(T, T.near, S, y, 2, P, d.kq32, d.find_phi, s);
+  if (d.generic_near) {  // adaptive trees: the near phase accumulates into P[0:N), which is y
+    if (e == cudaSuccess) e = launch_tc(T, T.near, S, P, 1, nullptr, nullptr, 0, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(y, P, (size_t)d.N * kTcRhs * sizeof(float2), cudaMemcpyDeviceToDevice, s);
+  } else if (e == cudaSuccess) {
+    e = launch_tc(T, T.near, S, y, 2, P, d.kq32, d.find_phi, s);
+  }
   return e == cudaSuccess ? cudaGetLastError() : e;
 }
 

@@ -404,7 +404,6 @@ ls_status tc_status(ls_op* op, const char* who) {
 
 ls_status ls_matvec_f32_many(ls_op* op, int nrhs, const double* X, double* Y) {
   if (!op || !X || !Y || nrhs < 1) return fail(LS_E_INVALID, "ls_matvec_f32_many: bad argument");
-  if (adaptive(op)) return adaptive_refused("ls_matvec_f32_many");
   if (!op->on_device) return fail(LS_E_STATE, "ls_matvec_f32_many: operator was assembled without a device");
   if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_matvec_f32_many: call ls_op_enable_f32 first");
   DevOperator& d = op->dev;
@@ -427,7 +426,6 @@ ls_status ls_matvec_f32_many(ls_op* op, int nrhs, const double* X, double* Y) {
 ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float* ms) {
   if (!op || !ms || iters < 1 || warmup < 0 || (width != 8 && width != 64))
     return fail(LS_E_INVALID, "ls_time_block_apply: bad argument");
-  if (adaptive(op)) return adaptive_refused("ls_time_block_apply");
   if (!op->on_device) return fail(LS_E_STATE, "ls_time_block_apply: operator was assembled without a device");
   if (!op->dev.has_f32) return fail(LS_E_STATE, "ls_time_block_apply: call ls_op_enable_f32 first");
   cudaSetDevice(op->dev.device);
@@ -443,7 +441,6 @@ ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float
 ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_outer, int inner_iter, double tol,
                                  double* X, int* n_matvec, double* rel_residuals) {
   if (!op || !B || !X) return fail(LS_E_INVALID, "ls_gmres_mixed_batched: null argument");
-  if (adaptive(op)) return adaptive_refused("ls_gmres_mixed_batched");
   if (!op->on_device) return fail(LS_E_STATE, "ls_gmres_mixed_batched: operator was assembled without a device");
   if (nrhs < 1 || max_outer < 1 || inner_iter < 1)
     return fail(LS_E_INVALID, "ls_gmres_mixed_batched: nrhs and iteration counts must be >= 1");
