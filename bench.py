@@ -667,6 +667,33 @@ def run_profile_solve(args):
     op.close()
 
 
+def run_adaptive_matvecs(args):
+    """Times `args.adaptive_matvecs` FP64 matvecs of the adaptive operator of
+    the reference's README run with CUDA events (device-resident x); one
+    JSON line. Also the command that its launch lists profile."""
+    import torch
+
+    import lippmann_schwinger_solver_gb300 as ls
+    op = ls.Operator(readme_adaptive_config(ls), device=0)
+    x = torch.from_numpy(input_vector(op.N)).cuda()
+    y = torch.empty_like(x)
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(max(3, args.warmup)):
+        op.matvec_device(x.data_ptr(), y.data_ptr(), st)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(args.adaptive_matvecs):
+        op.matvec_device(x.data_ptr(), y.data_ptr(), st)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.adaptive_matvecs
+    print(json.dumps({"metric": "FP64 matvec, adaptive README tree", "unit": "matvec/s", "value": 1e3 / ms,
+                      "ms": ms, "N": op.N, "launches_per_matvec": op.info["n_kernels_per_matvec"],
+                      "matvec_bytes": op.info["matvec_bytes"]}), flush=True)
+    op.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -693,6 +720,8 @@ def main():
                     help="only time this many batch-1 forward passes of the trained network")
     ap.add_argument("--block-apply", type=int, default=0,
                     help="only time FP32 block applies of this many right-hand sides (64 or 8)")
+    ap.add_argument("--adaptive-matvecs", type=int, default=0,
+                    help="only time this many FP64 matvecs of the adaptive README-run operator")
     ap.add_argument("--profile-solve", action="store_true",
                     help="only run one FP64 and one mixed solve inside a CUDA profiler range")
     args = ap.parse_args()
@@ -702,6 +731,8 @@ def main():
         run_block_apply(args)
     elif args.profile_solve:
         run_profile_solve(args)
+    elif args.adaptive_matvecs > 0:
+        run_adaptive_matvecs(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
