@@ -185,13 +185,32 @@ def readme_adaptive_config(ls):
 README_RESIDUALS = {1: 4.59412e-06, 2: 1.28443e-10}
 
 
+def _device_matvec_ms(op, iters, warmup):
+    """Mean time of back-to-back FP64 matvecs with device-resident x on
+    torch's current stream (CUDA events around the whole loop)."""
+    import torch
+    x = torch.from_numpy(input_vector(op.N)).cuda()
+    y = torch.empty_like(x)
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(warmup):
+        op.matvec_device(x.data_ptr(), y.data_ptr(), st)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(iters):
+        op.matvec_device(x.data_ptr(), y.data_ptr(), st)
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / iters
+
+
 def adaptive_leg(ls, local, timed, max_iter):
     """The adaptive operator at the README configuration: matvec time,
     RestartedGMRES(10) with 1 and 2 restarts against the published
     residuals, and the solves to 1e-8."""
     opa = ls.Operator(readme_adaptive_config(ls), device=local)
     info = opa.info
-    ms_a, _ = opa.time_matvec(warmup=3, iters=20, precision=ls.LS_PREC_F64)
+    ms_a = _device_matvec_ms(opa, 200, 5)
     ba = opa.rhs()
     out = {"config": "adaptive quadtree (GMRES/Readme.md:43), N=%d, %d levels" % (opa.N, info["n_levels"]),
            "N": opa.N, "assemble_s": info["assemble_seconds"],
@@ -671,23 +690,9 @@ def run_adaptive_matvecs(args):
     """Times `args.adaptive_matvecs` FP64 matvecs of the adaptive operator of
     the reference's README run with CUDA events (device-resident x); one
     JSON line. Also the command that its launch lists profile."""
-    import torch
-
     import lippmann_schwinger_solver_gb300 as ls
     op = ls.Operator(readme_adaptive_config(ls), device=0)
-    x = torch.from_numpy(input_vector(op.N)).cuda()
-    y = torch.empty_like(x)
-    st = torch.cuda.current_stream().cuda_stream
-    for _ in range(max(3, args.warmup)):
-        op.matvec_device(x.data_ptr(), y.data_ptr(), st)
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(args.adaptive_matvecs):
-        op.matvec_device(x.data_ptr(), y.data_ptr(), st)
-    b.record()
-    torch.cuda.synchronize()
-    ms = a.elapsed_time(b) / args.adaptive_matvecs
+    ms = _device_matvec_ms(op, args.adaptive_matvecs, max(3, args.warmup))
     print(json.dumps({"metric": "FP64 matvec, adaptive README tree", "unit": "matvec/s", "value": 1e3 / ms,
                       "ms": ms, "N": op.N, "launches_per_matvec": op.info["n_kernels_per_matvec"],
                       "matvec_bytes": op.info["matvec_bytes"]}), flush=True)
