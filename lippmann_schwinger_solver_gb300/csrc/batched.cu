@@ -55,6 +55,8 @@ struct BatchWorkspace {
   double2* nrm = nullptr;      // NR
   double2* pinned = nullptr;   // host: h, h2 ((m + 2) x NR each), nrm (NR)
   cudaEvent_t copied = nullptr;
+  cudaEvent_t orthogonalised = nullptr;  // a step's Gram-Schmidt kernels are done
+  cudaStream_t side = nullptr;           // the coefficient copies, off the operator's stream
   // FP64 outer loop: residual columns, one product, right-hand sides and
   // solutions of a call (device copies of the caller's host arrays).
   double2* res = nullptr;      // N x NR
@@ -70,7 +72,10 @@ struct BatchWorkspace {
     if (pinned) cudaFreeHost(pinned);
     pinned = nullptr;
     if (copied) cudaEventDestroy(copied);
-    copied = nullptr;
+    if (orthogonalised) cudaEventDestroy(orthogonalised);
+    if (side) cudaStreamDestroy(side);
+    copied = orthogonalised = nullptr;
+    side = nullptr;
     n = 0;
     cap = -1;
     vec_ready = false;
@@ -94,7 +99,10 @@ struct BatchWorkspace {
     if (pinned) cudaFreeHost(pinned);
     pinned = nullptr;
     if (copied) cudaEventDestroy(copied);
-    copied = nullptr;
+    if (orthogonalised) cudaEventDestroy(orthogonalised);
+    if (side) cudaStreamDestroy(side);
+    copied = orthogonalised = nullptr;
+    side = nullptr;
     n = 0;
     cap = -1;
     const size_t blk = (size_t)n_ * NR * sizeof(float2);
@@ -110,6 +118,8 @@ struct BatchWorkspace {
     if (e == cudaSuccess) e = cudaMalloc(&tmp, (size_t)n_ * sizeof(double2));
     if (e == cudaSuccess) e = cudaMallocHost(&pinned, (size_t)(2 * (m + 2) * NR + NR) * sizeof(double2));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&orthogonalised, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
     if (e != cudaSuccess) return e;
     n = n_;
     cap = m;
@@ -601,10 +611,14 @@ cudaError_t block_arnoldi(DevOperator& d, BatchWorkspace<NR>& B, int m, std::vec
     launch_pdl(multi_axpy_block_kernel<NR>, grid_n((long long)blk), 256, 0, s, B.w, B.V, n, k + 1, B.h2, -1.f);
     block_multidot(B.w, n, 1, B.w, B, B.nrm, s);
     launch_pdl(scale_block_kernel<NR>, grid_n((long long)blk), 256, 0, s, B.w, B.V + (size_t)(k + 1) * blk, B.nrm, n);
-    cudaMemcpyAsync(hp, B.h, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(hp2, B.h2, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(np, B.nrm, (size_t)NR * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    if ((e = cudaEventRecord(B.copied, s)) != cudaSuccess) return e;
+    // Coefficients to the host on a side stream (as in the single-vector
+    // Arnoldi step of gmres.cu): the next block apply follows directly.
+    if ((e = cudaEventRecord(B.orthogonalised, s)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(B.side, B.orthogonalised, 0)) != cudaSuccess) return e;
+    cudaMemcpyAsync(hp, B.h, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, B.side);
+    cudaMemcpyAsync(hp2, B.h2, (size_t)(k + 1) * NR * sizeof(double2), cudaMemcpyDeviceToHost, B.side);
+    cudaMemcpyAsync(np, B.nrm, (size_t)NR * sizeof(double2), cudaMemcpyDeviceToHost, B.side);
+    if ((e = cudaEventRecord(B.copied, B.side)) != cudaSuccess) return e;
     if (k + 1 < m) {
       if ((e = block_apply<NR>(d, B, B.V + (size_t)(k + 1) * blk, B.w, s)) != cudaSuccess) return e;
       ++applies;

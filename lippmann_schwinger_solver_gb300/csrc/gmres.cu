@@ -116,6 +116,8 @@ struct GmresWorkspace {
   double* npartial = nullptr;  // per-block partial norms of the fused corrections
   unsigned* counters = nullptr;  // finished blocks per column group, + one for the corrections
   cudaEvent_t copied = nullptr;  // a step's coefficients are on the host
+  cudaEvent_t orthogonalised = nullptr;  // a step's Gram-Schmidt kernels are done
+  cudaStream_t side = nullptr;  // the coefficient copies, off the operator's stream
   double2* pinned = nullptr;     // host: h (m+2), h2 (m+2), |w|^2; page-locked so copies stay asynchronous
   int n = 0, cap = -1;
   int n_groups() const { return n_counters(cap); }
@@ -127,7 +129,10 @@ struct GmresWorkspace {
     counters = nullptr;
     res32 = dx32 = pv32 = pz32 = nullptr;
     if (copied) cudaEventDestroy(copied);
-    copied = nullptr;
+    if (orthogonalised) cudaEventDestroy(orthogonalised);
+    if (side) cudaStreamDestroy(side);
+    copied = orthogonalised = nullptr;
+    side = nullptr;
     if (pinned) cudaFreeHost(pinned);
     pinned = nullptr;
     n = 0;
@@ -157,6 +162,8 @@ struct GmresWorkspace {
     if (e == cudaSuccess) e = cudaMalloc(&counters, (size_t)(n_counters(m) + 1) * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(counters, 0, (size_t)(n_counters(m) + 1) * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&orthogonalised, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&pinned, (size_t)(2 * (m + 2) + 1) * sizeof(double2));
     if (e != cudaSuccess) {
       release_small();
@@ -650,10 +657,16 @@ cudaError_t arnoldi_cycle(DevOperator& d, GmresWorkspace& ws, const T* b, const 
     multidot(B.V, n, k + 1, B.w, n, ws, ws.h2, nullptr, nrm_w, nrm_1, s);
     correct(B.w, B.V, n, k + 1, ws.h2, n, ws, ws.nrm, nrm_w, nrm_1, s);
     launch_pdl(scale_by_norm_kernel<T>, grid_for(n), 256, 0, s, B.w, B.V + (size_t)(k + 1) * n, ws.nrm, n);
-    cudaMemcpyAsync(hp, ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(hp2, ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(np, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, s);
-    if ((e = cudaEventRecord(ws.copied, s)) != cudaSuccess) return e;
+    // The coefficients go to the host on a side stream, so that the next
+    // operator apply follows the Gram-Schmidt kernels directly on the
+    // operator's stream. The host waits for these copies before it queues the
+    // next step's Gram-Schmidt kernels, the next writers of h, h2 and nrm.
+    if ((e = cudaEventRecord(ws.orthogonalised, s)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(ws.side, ws.orthogonalised, 0)) != cudaSuccess) return e;
+    cudaMemcpyAsync(hp, ws.h, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, ws.side);
+    cudaMemcpyAsync(hp2, ws.h2, (size_t)(k + 1) * sizeof(double2), cudaMemcpyDeviceToHost, ws.side);
+    cudaMemcpyAsync(np, ws.nrm, sizeof(double2), cudaMemcpyDeviceToHost, ws.side);
+    if ((e = cudaEventRecord(ws.copied, ws.side)) != cudaSuccess) return e;
     if (k + 1 < m && (e = product(k + 1)) != cudaSuccess) return e;
     if ((e = cudaEventSynchronize(ws.copied)) != cudaSuccess) return e;
     std::vector<cdh> hk(k + 2);
