@@ -91,3 +91,24 @@ def test_adaptive_packed_program_in_bounds_and_equal_to_oracle(ls, ora, tmp_path
     ya = a.matvec(x)
     a.close()
     assert np.linalg.norm(y - ya) / np.linalg.norm(ya) <= bound
+
+
+@pytest.mark.parametrize("over,message", [
+    (dict(treeAdaptivity=0), "treeAdaptivity"),
+    (dict(treeAdaptivity=13), "treeAdaptivity"),
+    (dict(nChebNodes=9), "nChebNodes"),
+    (dict(degreeOfBases=12, nChebNodes=4), "degreeOfBases"),
+    (dict(L=0.0), "L must be"),
+    (dict(kappa=-1.0), "kappa"),
+    (dict(TOL_POW=17), "TOL_POW"),
+    (dict(Qchoice=7), "Qchoice"),
+    # q resolved at once and kappa 0: a tree of fewer than 3 levels
+    (dict(Qchoice=3, kappa=0.0, treeAdaptivity=1), "levels"),
+])
+def test_adaptive_config_rejections(ls, over, message):
+    """Invalid adaptive configurations fail with LS_E_INVALID and a message
+    naming the field, before any tree is built."""
+    with pytest.raises(ls.LSError) as ei:
+        ls.Operator(ls.Config(**dict(README, **over)), device=-1)
+    assert ei.value.code == ls.LS_E_INVALID
+    assert message in str(ei.value)
