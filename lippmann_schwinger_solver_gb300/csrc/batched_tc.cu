@@ -47,6 +47,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -120,6 +121,17 @@ struct TcBlock {
   int K;            // complex columns
   int nst;          // stages of kStageCols columns
 };
+
+// One stage of a CTA's stage program (80 bytes): what the loader of
+// tc_ws_kernel copies for it and how the stage sits in its block.
+struct TcStage {
+  int rows[16];  // gather source row of each column (ncols used)
+  int a256;      // first float2 of the operator stage / 256
+  int ncols;     // columns present (1..16)
+  int npad;      // block rows padded to a multiple of 16
+  int flags;     // 1: first stage of an accumulator chunk, 2: last stage of a chunk
+};
+static_assert(sizeof(TcStage) == 80, "stage record");
 
 namespace {
 
@@ -401,6 +413,490 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
 }
 
+// Warp-specialized form of tc_gemm_kernel (same operands, accumulation
+// order and epilogue modes), one CTA per SM in four roles:
+//   - a loader warp streams the raw stages (the 16 gathered source rows of
+//     64 right-hand sides, 512 bytes each, and the operator stage) into a
+//     ring of kWsRaw shared-memory slots with per-lane cp.async (16 bytes a
+//     lane per row, then the contiguous operator stage), each lane's copies
+//     one arrival on the slot's `raw_full` mbarrier (small bulk copies of
+//     single rows would queue on the copy engine one by one).
+//     What it copies comes from the CTA's stage program (one
+//     TcStage record per stage, built once per phase), itself streamed into
+//     shared memory kProgChunk records at a time, kProgRing chunks ahead, so
+//     no dependent global load sits on the loader's path;
+//   - eight converter warps read a raw stage, split it into the TF32 hi/lo
+//     planes of the MMA layout in one of kWsCan canonical slots, release
+//     the raw slot (`raw_empty`) and arrive on the canonical slot's `full`;
+//   - an MMA warp whose elected thread waits on `full`, issues the stage's
+//     12 MMAs into the chunk's accumulator slot and commits them to the
+//     canonical slot's `empty` and, at a chunk's end, to the accumulator
+//     slot's `accfull`;
+//   - four epilogue warps (one per 32-lane quarter of tensor memory) add
+//     each finished chunk into the block's running FP32 sums, free the
+//     accumulator slot (`accempty`), and after the block's last chunk
+//     combine sums + last chunk with the destination. Their block records
+//     are read 32 blocks ahead, their output rows copied (cp.async) two
+//     blocks ahead.
+// A stage's column count, padding and chunk flags travel with it: the
+// loader writes them beside the raw slot, the converters beside the
+// canonical slot. Chunks rotate over kWsAcc accumulator slots, so the
+// tensor core runs up to six chunks ahead of the epilogue warps and no role
+// waits for another at a block boundary. Every wait is bounded: one that
+// gives up sets the error flag and the abort flag and every role leaves its
+// loops; the loader waits (bounded) for its copies in flight and the MMA
+// thread for its MMAs before the tensor memory is freed.
+constexpr int kWsCan = 3;
+constexpr int kWsRaw = 4;
+constexpr int kWsTmemCols = 512;                   // all of an SM's tensor memory (one CTA per SM)
+constexpr int kWsAcc = 7;                          // accumulator slots (columns 64 s .. 64 s + 63)
+constexpr int kWsSumCol = kWsAcc * kMaxRows;       // the running sums (448 .. 511)
+constexpr int kWsConv = 256;                       // converter threads (warps 0-7)
+constexpr int kWsMmaWarp = 8, kWsLoadWarp = 9, kWsEpiWarp0 = 10;
+constexpr int kWsEpi = 128;                        // epilogue threads (warps 10-13)
+constexpr int kWsThreads = kWsConv + 64 + kWsEpi;
+constexpr int kRowBytes = 64 * 8;                  // one gathered source row (64 complex FP32)
+constexpr int kRawXBytes = kStageCols * kRowBytes;
+constexpr int kProgChunk = 8, kProgRing = 4;       // stage records per program copy; copies in the ring
+static_assert(kWsSumCol + kMaxRows <= kWsTmemCols, "tensor-memory columns");
+
+__host__ __device__ constexpr int ws_can_bytes(int npad_max) { return kWsCan * (2 * kXBytes + 2 * npad_max * 128); }
+__host__ __device__ constexpr int ws_raw_slot(int npad_max) { return kRawXBytes + npad_max * 128; }
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+// Named barrier 1 of the epilogue warps that also ORs a flag over them, so
+// that every epilogue warp takes the same branch after it.
+__device__ __forceinline__ bool epilogue_sync_or(bool v) {
+  int r;
+  asm volatile("{ .reg .pred p, q; setp.ne.s32 p, %1, 0; bar.red.or.pred q, 1, %2, p; selp.s32 %0, 1, 0, q; }"
+               : "=r"(r)
+               : "r"((int)v), "n"(kWsEpi)
+               : "memory");
+  return r != 0;
+}
+
+__global__ void __launch_bounds__(kWsThreads, 1)
+    tc_ws_kernel(const TcBlock* __restrict__ blocks, int n_blocks, const TcStage* __restrict__ prog,
+                 const int* __restrict__ prog_off, const float2* __restrict__ A, const int* __restrict__ out,
+                 const float2* __restrict__ src, float2* __restrict__ dst, int mode, const float2* __restrict__ P,
+                 const float* __restrict__ kq, int find_phi, int npad_max, unsigned* __restrict__ err) {
+  pdl_enter();
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t full[kWsCan], empty[kWsCan], raw_full[kWsRaw], raw_empty[kWsRaw], prog_full[kProgRing];
+  __shared__ uint64_t accfull[kWsAcc], accempty[kWsAcc], drained;
+  __shared__ __align__(16) TcStage prog_ring[kProgRing][kProgChunk];
+  __shared__ int raw_hdr[kWsRaw][3];    // ncols, npad, flags of the raw slot's stage
+  __shared__ int can_hdr[kWsCan][2];    // npad, flags of the canonical slot's stage
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int abort_flag;
+  __shared__ int orows[4][kMaxRows];    // output rows of the epilogue's blocks k .. k + 2 (slot k & 3)
+  __shared__ float oscale[2][kMaxRows]; // mode 2 with find_phi: kappa^2 q of the output row
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int a_plane = npad_max * 128;
+  const int can_slot = 2 * kXBytes + 2 * a_plane;
+  const int raw_slot = ws_raw_slot(npad_max);
+  uint8_t* const raw_base = smem + ws_can_bytes(npad_max);
+  const int s_begin = __ldg(prog_off + blockIdx.x), n_st = __ldg(prog_off + blockIdx.x + 1) - s_begin;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(kWsTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (t == 0) {
+    auto init = [](uint64_t* bar, int count) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+    };
+    for (int i = 0; i < kWsCan; ++i) {
+      init(&full[i], kWsConv / 32);
+      init(&empty[i], 1);
+    }
+    for (int i = 0; i < kWsRaw; ++i) {
+      init(&raw_full[i], 33);  // the loader's 32 lanes (their copies) + lane 0's header arrival
+      init(&raw_empty[i], kWsConv / 32);
+    }
+    for (int i = 0; i < kProgRing; ++i) init(&prog_full[i], 1);
+    for (int i = 0; i < kWsAcc; ++i) {
+      init(&accfull[i], 1);
+      init(&accempty[i], kWsEpi / 32);
+    }
+    init(&drained, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  auto fail = [&]() {
+    atomicOr(err, 1u);
+    abort_flag = 1;
+  };
+
+  if (warp == kWsLoadWarp) {
+    // ---------------- loader warp
+    auto fetch = [&](int q) {  // program chunk q into ring slot q % kProgRing
+      const int first = q * kProgChunk;
+      if (first >= n_st || lane != 0) return;
+      const uint32_t bytes = (uint32_t)(min(kProgChunk, n_st - first) * (int)sizeof(TcStage));
+      mbar_expect_tx(&prog_full[q % kProgRing], bytes);
+      bulk_copy(prog_ring[q % kProgRing], prog + s_begin + first, bytes, &prog_full[q % kProgRing]);
+    };
+    for (int q = 0; q < kProgRing; ++q) fetch(q);
+    int g = 0;
+    for (; g < n_st; ++g) {
+      const int q = g / kProgChunk, w = g % kProgChunk, rs = g % kWsRaw;
+      const bool waited = (w != 0 || mbar_wait(&prog_full[q % kProgRing], (uint32_t)((q / kProgRing) & 1))) &&
+                          (g < kWsRaw || mbar_wait(&raw_empty[rs], (uint32_t)(((g / kWsRaw) - 1) & 1)));
+      if (!__all_sync(0xffffffffu, waited && !abort_flag)) {
+        if (lane == 0 && !waited) fail();
+        break;
+      }
+      const TcStage& rec = prog_ring[q % kProgRing][w];
+      const int ncols = rec.ncols, npad = rec.npad, flags = rec.flags;
+      const float4* As = reinterpret_cast<const float4*>(A + (long long)rec.a256 * 256);
+      int rows[kStageCols];  // all read before the first copy is issued
+#pragma unroll
+      for (int c = 0; c < kStageCols; ++c) rows[c] = rec.rows[c];
+      uint8_t* raw = raw_base + rs * raw_slot;
+      // 16 bytes of each gathered row per lane, then the contiguous operator
+      // stage in 16-byte pieces (cp.async through L2); the slot's mbarrier
+      // counts each lane's copies
+#pragma unroll
+      for (int c = 0; c < kStageCols; ++c)
+        if (c < ncols) cp_async16(raw + c * kRowBytes + 16 * lane, src + (size_t)rows[c] * 64 + 2 * lane);
+      for (int u = lane; u < npad * 8; u += 32) cp_async16(raw + kRawXBytes + 16 * u, As + u);
+      if (lane == 0) {
+        raw_hdr[rs][0] = ncols;
+        raw_hdr[rs][1] = npad;
+        raw_hdr[rs][2] = flags;
+      }
+      asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(&raw_full[rs])) : "memory");
+      if (lane == 0) mbar_arrive(&raw_full[rs]);  // publishes the stage's header
+      if (w == kProgChunk - 1) {  // chunk q is read: its slot takes chunk q + kProgRing
+        __syncwarp();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fetch(q + kProgRing);
+      }
+    }
+    // the copies of the last stages issued have landed before the shared
+    // memory is released (after a normal run these phases are long complete)
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (lane == 0)
+      for (int s = (g > kWsRaw ? g - kWsRaw : 0); s < g; ++s)
+        if (!mbar_wait(&raw_full[s % kWsRaw], (uint32_t)((s / kWsRaw) & 1))) {
+          fail();
+          break;
+        }
+    __syncwarp();
+  } else if (warp == kWsMmaWarp) {
+    // ---------------- MMA warp: one elected thread issues and commits.
+    if (lane == 0) {
+      const uint32_t idesc_base = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(128 >> 4) << 24);
+      int g = 0;
+      long long G = -1;  // chunks started
+      for (; g < n_st; ++g) {
+        const int slot = g % kWsCan;
+        if (!mbar_wait(&full[slot], (uint32_t)((g / kWsCan) & 1))) {
+          fail();
+          break;
+        }
+        const int npad = can_hdr[slot][0], flags = can_hdr[slot][1];
+        const bool chunk_start = flags & 1, chunk_end = flags & 2;
+        if (chunk_start) ++G;
+        const int as = (int)(G % kWsAcc);
+        if (chunk_start && G >= kWsAcc && !mbar_wait(&accempty[as], (uint32_t)(((G / kWsAcc) - 1) & 1))) {
+          fail();
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t idesc = idesc_base | ((uint32_t)(npad >> 3) << 17);
+        uint8_t* base = smem + slot * can_slot;
+        const uint32_t xh = smem_u32(base), xl = smem_u32(base + kXBytes);
+        const uint32_t ah = smem_u32(base + 2 * kXBytes), al = smem_u32(base + 2 * kXBytes + a_plane);
+        const uint32_t dt = tmem + (uint32_t)(as * kMaxRows);
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks) {
+          const uint32_t o = ks * 256;
+          const uint64_t dxh = sdesc(xh + o, 128, kRowGroupBytes), dxl = sdesc(xl + o, 128, kRowGroupBytes);
+          const uint64_t dah = sdesc(ah + o, 128, kRowGroupBytes), dal = sdesc(al + o, 128, kRowGroupBytes);
+          mma_tf32(dt, dxh, dah, idesc, (!chunk_start || ks > 0) ? 1u : 0u);
+          mma_tf32(dt, dxh, dal, idesc, 1u);
+          mma_tf32(dt, dxl, dah, idesc, 1u);
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&empty[slot]))
+                     : "memory");
+        if (chunk_end)
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&accfull[as]))
+                       : "memory");
+      }
+      // every MMA issued (g stages) has completed before the tensor memory is freed
+      if (g > 0) {
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&drained))
+                     : "memory");
+        if (!mbar_wait(&drained, 0u)) fail();
+      }
+    }
+    __syncwarp();
+  } else if (warp < kWsMmaWarp) {
+    // ---------------- converter warps
+    // Thread (kk, m): source column kk of the stage, right-hand sides 2m,
+    // 2m + 1, 2m + 32, 2m + 33. Eight consecutive lanes read 128
+    // contiguous bytes of a raw row; the 16 lanes of a half-warp cover the
+    // eight rows of a core matrix and both column parities, so the 8-byte
+    // canonical stores are free of bank conflicts.
+    const int m = (t & 7) | (((t >> 4) & 1) << 3);
+    const int kk = ((t >> 5) << 1) | ((t >> 3) & 1);
+    const int rot = (t >> 2) & 1;
+    for (int g = 0; g < n_st; ++g) {
+      const int rs = g % kWsRaw, cs = g % kWsCan;
+      const bool waited = mbar_wait(&raw_full[rs], (uint32_t)((g / kWsRaw) & 1)) &&
+                          (g < kWsCan || mbar_wait(&empty[cs], (uint32_t)(((g / kWsCan) - 1) & 1)));
+      if (!__all_sync(0xffffffffu, waited && !abort_flag)) {
+        if (lane == 0 && !waited) fail();
+        break;
+      }
+      const int ncols = raw_hdr[rs][0], npad = raw_hdr[rs][1], flags = raw_hdr[rs][2];
+      const uint8_t* raw = raw_base + rs * raw_slot;
+      float4 x0 = make_float4(0.f, 0.f, 0.f, 0.f), x1 = x0, a[2];
+      if (kk < ncols) {  // columns past the block's last are zero
+        const float4* row = reinterpret_cast<const float4*>(raw + kk * kRowBytes);
+        x0 = row[m];
+        x1 = row[m + 16];
+      }
+      const float4* Ar = reinterpret_cast<const float4*>(raw + kRawXBytes);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int u = t + q * kWsConv;
+        a[q] = u < npad * 8 ? Ar[u] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      uint8_t* base = smem + cs * can_slot;
+      float2* Xh = reinterpret_cast<float2*>(base);
+      float2* Xl = reinterpret_cast<float2*>(base + kXBytes);
+      float4* Ah = reinterpret_cast<float4*>(base + 2 * kXBytes);
+      float4* Al = reinterpret_cast<float4*>(base + 2 * kXBytes + a_plane);
+      // value ii of the thread: right-hand side 2m + (ii & 1) + 32 (ii >> 1);
+      // store i takes ii = i ^ rot
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int ii = i ^ rot;
+        const float4 h2 = (ii & 2) ? x1 : x0;
+        const float vx = (ii & 1) ? h2.z : h2.x, vy = (ii & 1) ? h2.w : h2.y;
+        const int j = 2 * m + (ii & 1) + 32 * (ii >> 1);
+        const float hx = tf32_rn(vx), hy = tf32_rn(vy);
+        const float lx = tf32_rn(vx - hx), ly = tf32_rn(vy - hy);
+        const int o_re = canon(j, kk), o_im = canon(64 + j, kk);
+        Xh[o_re] = make_float2(hx, hy);
+        Xl[o_re] = make_float2(lx, ly);
+        Xh[o_im] = make_float2(hy, -hx);
+        Xl[o_im] = make_float2(ly, -lx);
+      }
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int u = t + q * kWsConv;
+        if (u < npad * 8) {
+          const float4 v = a[q];
+          const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+          Ah[u] = h;
+          Al[u] = make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
+        }
+      }
+      if (t == 0) {  // read by the MMA thread after `full`
+        can_hdr[cs][0] = npad;
+        can_hdr[cs][1] = flags;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&full[cs]);
+        mbar_arrive(&raw_empty[rs]);
+      }
+    }
+  } else {
+    // ---------------- epilogue warps
+    const int e = t - kWsEpiWarp0 * 32;              // 0..127
+    const int quarter = warp & 3;                    // tensor-memory lanes 32 quarter .. + 31
+    const int mrow = quarter * 32 + lane, part = mrow >> 6, j = mrow & 63;
+    const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+    auto tld16 = [&](uint32_t col, uint32_t* r) {
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(lane_base + col));
+    };
+    auto tst16 = [&](uint32_t col, const uint32_t* r) {
+      asm volatile(
+          "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+              lane_base + col),
+          "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+          "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+          : "memory");
+    };
+    auto wait_chunk = [&](long long G) -> bool {  // warp-uniform: the loads after it are warp-collective
+      const bool done = __all_sync(0xffffffffu, mbar_wait(&accfull[G % kWsAcc], (uint32_t)((G / kWsAcc) & 1)));
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      return done;
+    };
+    auto free_chunk = [&](long long G) {
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[G % kWsAcc]);
+    };
+    // Block k of this CTA is block blockIdx.x + k grid. Its record (rows,
+    // npad, nst, o_off) sits in lane k & 31 of a window of 32 records; the
+    // next window is loaded a window ahead.
+    const int n_mine = (n_blocks - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    auto load_rec = [&](int k) -> int4 {
+      if (k >= n_mine) return make_int4(0, 0, 0, 0);
+      const TcBlock* B = blocks + blockIdx.x + (size_t)k * gridDim.x;
+      return make_int4(B->rows, B->npad, B->nst, B->o_off);
+    };
+    auto rec_of = [&](int k, const int4& cur, const int4& nxt, int base) -> int4 {  // warp-uniform k
+      const int4 w = (k - base) < 32 ? cur : nxt;
+      const int l = k & 31;
+      return make_int4(__shfl_sync(0xffffffffu, w.x, l), __shfl_sync(0xffffffffu, w.y, l),
+                       __shfl_sync(0xffffffffu, w.z, l), __shfl_sync(0xffffffffu, w.w, l));
+    };
+    // output rows of block k into orows[k & 3] (cp.async, one group per block)
+    auto copy_rows = [&](int k, const int4& r) {
+      if (k < n_mine && e < r.x) {
+        const uint32_t d = smem_u32(&orows[k & 3][e]);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(out + r.w + e) : "memory");
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    int4 wcur = load_rec(lane), wnxt = load_rec(32 + lane);
+    int wbase = 0;  // block of wcur's lane 0
+    copy_rows(0, rec_of(0, wcur, wnxt, wbase));
+    copy_rows(1, rec_of(1, wcur, wnxt, wbase));
+    long long gc = 0;
+    for (int k = 0; k < n_mine; ++k) {
+      if (k - wbase == 32) {
+        wcur = wnxt;
+        wbase += 32;
+        wnxt = load_rec(wbase + 32 + lane);
+      }
+      const int4 r = rec_of(k, wcur, wnxt, wbase);
+      const int rows = r.x, npad = r.y, nst = r.z;
+      copy_rows(k + 2, rec_of(k + 2, wcur, wnxt, wbase));
+      asm volatile("cp.async.wait_group 2;" ::: "memory");  // this thread's rows of block k have landed
+      const int ob = k & 3, sb = k & 1;
+      const long long gc0 = gc;
+      const int nchunks = (nst + kChunkStages - 1) / kChunkStages;
+      gc = gc0 + nchunks;
+      bool ok = true;
+      // sums = chunk 0 + chunk 1 + ... (round-to-nearest FP32, in order), all but the last chunk
+      for (long long G = gc0; G + 1 < gc; ++G) {
+        if (!wait_chunk(G)) {
+          ok = false;
+          break;
+        }
+        const uint32_t acol = (uint32_t)((G % kWsAcc) * kMaxRows);
+        for (int c0 = 0; c0 < npad; c0 += 16) {
+          uint32_t ra[16], q[16];
+          tld16(acol + c0, ra);
+          if (G > gc0) tld16((uint32_t)(kWsSumCol + c0), q);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (G > gc0) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) ra[i] = __float_as_uint(__uint_as_float(q[i]) + __uint_as_float(ra[i]));
+          }
+          tst16((uint32_t)(kWsSumCol + c0), ra);
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        free_chunk(G);
+      }
+      if (ok && nchunks > 0 && !wait_chunk(gc - 1)) ok = false;
+      if (!ok && lane == 0) fail();
+      if (mode == 2 && find_phi && e < rows) oscale[sb][e] = __ldg(kq + orows[ob][e]);
+      // output rows visible; the same decision in every epilogue warp
+      if (epilogue_sync_or(!ok || abort_flag)) break;
+      // y = sums + last chunk, combined with the destination; all old values
+      // of a 16-row group are loaded before any of them is written (the rows
+      // of a phase are distinct)
+      const uint32_t lcol = (uint32_t)(((gc - 1) % kWsAcc) * kMaxRows);
+      float* dstf = reinterpret_cast<float*>(dst);
+      for (int c0 = 0; c0 < rows; c0 += 16) {
+        uint32_t ra[16], q[16];
+        if (nchunks > 0) {
+          tld16(lcol + c0, ra);
+          if (nchunks > 1) tld16((uint32_t)(kWsSumCol + c0), q);
+        }
+        float basev[16], extra[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          basev[i] = extra[i] = 0.f;
+          if (c0 + i < rows) {
+            const size_t el = ((size_t)orows[ob][c0 + i] * 64 + j) * 2 + part;
+            if (mode == 1) {
+              basev[i] = ld_chain(dstf + el);
+            } else if (mode == 2) {
+              basev[i] = ld_chain(reinterpret_cast<const float*>(P) + el);
+              if (find_phi) extra[i] = ld_chain(reinterpret_cast<const float*>(src) + el);
+            }
+          }
+        }
+        if (nchunks > 0) asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          if (c0 + i < rows) {
+            const size_t el = ((size_t)orows[ob][c0 + i] * 64 + j) * 2 + part;
+            float v = 0.f;  // a block without columns sums to zero
+            if (nchunks > 1)
+              v = __uint_as_float(q[i]) + __uint_as_float(ra[i]);
+            else if (nchunks == 1)
+              v = __uint_as_float(ra[i]);
+            // mode 0: v; mode 1: old + v; mode 2: P + s v, + x with find_phi
+            dstf[el] = mode == 0 ? v
+                                 : (mode == 2 && find_phi ? basev[i] + oscale[sb][c0 + i] * v + extra[i]
+                                                          : basev[i] + v);
+          }
+        }
+      }
+      if (nchunks > 0) free_chunk(gc - 1);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");  // no copy into shared memory outlives the CTA
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kWsTmemCols));
+}
+
+// Stage program of a phase: the stages of block b in order, blocks dealt
+// to the CTAs round-robin (CTA c: blocks c, c + grid, ...); one thread per
+// stage record.
+__global__ void tc_program_kernel(const int2* __restrict__ stage_of, int n, const TcBlock* __restrict__ blocks,
+                                  const int* __restrict__ idx, TcStage* __restrict__ prog) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const TcBlock blk = blocks[stage_of[s].x];
+    const int st = stage_of[s].y;
+    TcStage r;
+    r.ncols = min(kStageCols, blk.K - st * kStageCols);
+    for (int c = 0; c < kStageCols; ++c) r.rows[c] = c < r.ncols ? idx[blk.i_off + st * kStageCols + c] : 0;
+    r.a256 = (int)((blk.a_off + (long long)st * blk.npad * kStageCols) >> 8);
+    r.npad = blk.npad;
+    r.flags = (st % kChunkStages == 0 ? 1 : 0) | (st % kChunkStages == kChunkStages - 1 || st == blk.nst - 1 ? 2 : 0);
+    prog[s] = r;
+  }
+}
+
 // Far-field phase -> tensor-core form: one warp per tile writes its
 // elements, conjugated, into the canonical stages of the part of its block
 // that holds the row (tile_block: the block's first part; parts are
@@ -476,6 +972,9 @@ struct TcPhase {
   int accumulate = 0;
   long long a_elems = 0;
   long long entries = 0;  // true complex entries
+  TcStage* prog = nullptr;  // stage program of tc_ws_kernel (CTA c: prog[prog_off[c] .. prog_off[c + 1]))
+  int* prog_off = nullptr;
+  int prog_grid = 0;
 };
 
 struct TcOperator {
@@ -496,6 +995,37 @@ template <class T>
 cudaError_t dalloc(TcOperator& t, T** p, size_t n) {
   cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
   if (e == cudaSuccess) t.owned.push_back(*p);
+  return e;
+}
+
+// Stage program of a phase whose blocks (nst per block on the host) and
+// gather lists are on the device: blocks dealt round-robin to
+// min(n_blocks, sms) CTAs, each CTA's stages contiguous.
+cudaError_t build_program(TcOperator& T, TcPhase& ph, const std::vector<int>& nst) {
+  const int nb = ph.n_blocks;
+  if (nb == 0) return cudaSuccess;
+  const int grid = std::min(nb, T.sms);
+  std::vector<int> off(grid + 1, 0);
+  std::vector<int2> stage_of;
+  for (int c = 0; c < grid; ++c) {
+    off[c] = (int)stage_of.size();
+    for (int b = c; b < nb; b += grid)
+      for (int st = 0; st < nst[b]; ++st) stage_of.push_back(make_int2(b, st));
+  }
+  off[grid] = (int)stage_of.size();
+  ph.prog_grid = grid;
+  int2* d_of = nullptr;
+  cudaError_t e = dalloc(T, &ph.prog, stage_of.size());
+  if (e == cudaSuccess) e = dalloc(T, &ph.prog_off, off.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d_of, std::max<size_t>(stage_of.size(), 1) * sizeof(int2));
+  if (e == cudaSuccess) e = cudaMemcpy(ph.prog_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !stage_of.empty())
+    e = cudaMemcpy(d_of, stage_of.data(), stage_of.size() * sizeof(int2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !stage_of.empty()) {
+    tc_program_kernel<<<512, 256>>>(d_of, (int)stage_of.size(), ph.blocks, ph.idx, ph.prog);
+    e = cudaDeviceSynchronize();
+  }
+  cudaFree(d_of);
   return e;
 }
 
@@ -550,13 +1080,34 @@ cudaError_t build_far(TcOperator& T, const GemvPhase& h, const DevPhase<float2>&
   }
   cudaFree(dtb);
   cudaFree(dtr);
+  if (e == cudaSuccess) {
+    std::vector<int> nst(blocks.size());
+    for (size_t b = 0; b < blocks.size(); ++b) nst[b] = blocks[b].nst;
+    e = build_program(T, out, nst);
+  }
   if (e != cudaSuccess) err = std::string("tensor-core form: ") + cudaGetErrorString(e);
   return e;
+}
+
+int ws_smem_for(int npad_max) { return ws_can_bytes(npad_max) + kWsRaw * ws_raw_slot(npad_max); }
+
+// LS_TC_WS=1 selects the warp-specialized kernel (read once).
+bool use_ws() {
+  static const bool ws = [] {
+    const char* v = std::getenv("LS_TC_WS");
+    return v && std::atoi(v) != 0;
+  }();
+  return ws;
 }
 
 cudaError_t launch_tc(const TcOperator& T, const TcPhase& ph, const float2* src, float2* dst, int mode,
                       const float2* P, const float* kq, int find_phi, cudaStream_t s) {
   if (ph.n_blocks == 0) return cudaSuccess;
+  if (use_ws()) {  // one CTA per SM, the grid its stage program was dealt to
+    return launch_pdl(tc_ws_kernel, ph.prog_grid, kWsThreads, (size_t)ws_smem_for(ph.npad_max), s,
+                      (const TcBlock*)ph.blocks, ph.n_blocks, (const TcStage*)ph.prog, (const int*)ph.prog_off,
+                      (const float2*)ph.A, ph.out, src, dst, mode, P, kq, find_phi, ph.npad_max, T.err);
+  }
   const int grid = std::min(ph.n_blocks, 2 * T.sms);  // two CTAs per SM (96 KB shared memory, 128 TMEM columns each)
   return launch_pdl(tc_gemm_kernel, grid, kTcThreads, (size_t)smem_for(ph.npad_max), s, (const TcBlock*)ph.blocks,
                     ph.n_blocks, (const float2*)ph.A, ph.idx, ph.out, src, dst, mode, P, kq, find_phi, ph.npad_max,
@@ -618,12 +1169,15 @@ bool dev_enable_tc(DevOperator& d, const HostOperator& h, std::string& err) {
                                           nr.blocks, nr.npad_max, nst);
       e = cudaDeviceSynchronize();
     }
+    if (e == cudaSuccess) e = build_program(*T, nr, std::vector<int>((size_t)d.n_leaves, nst));
   }
-  int need = 0;
-  for (auto& p : T->up) need = std::max(need, smem_for(p.npad_max));
-  for (auto& p : T->down) need = std::max(need, smem_for(p.npad_max));
-  need = std::max(need, std::max(smem_for(T->m2l.npad_max), smem_for(T->near.npad_max)));
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, need);
+  int npad = std::max(T->m2l.npad_max, T->near.npad_max);
+  for (auto& p : T->up) npad = std::max(npad, p.npad_max);
+  for (auto& p : T->down) npad = std::max(npad, p.npad_max);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_for(npad));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(tc_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ws_smem_for(npad));
   if (e != cudaSuccess) {
     if (err.empty()) err = std::string("tensor-core form: ") + cudaGetErrorString(e);
     for (void* p : T->owned) cudaFree(p);
