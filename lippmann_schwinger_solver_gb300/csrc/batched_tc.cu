@@ -26,6 +26,10 @@
 // memory, next to the two accumulator slots, which alternate so that the
 // tensor core keeps working while a slot is read.
 //
+// Two kernels implement this: tc_ws_kernel (the default, described at its
+// definition: one CTA per SM with loader, converter, MMA and epilogue warps
+// fed by a per-CTA stage program) and tc_gemm_kernel (LS_TC_WS=0).
+//
 // Kernel structure (tc_gemm_kernel): a persistent grid of two CTAs per SM, 128 threads per CTA
 // (four warps, one per 32-lane quarter of tensor memory). Blocks of the
 // phase are dealt round-robin. Per block the K columns are walked in stages
@@ -1091,11 +1095,12 @@ cudaError_t build_far(TcOperator& T, const GemvPhase& h, const DevPhase<float2>&
 
 int ws_smem_for(int npad_max) { return ws_can_bytes(npad_max) + kWsRaw * ws_raw_slot(npad_max); }
 
-// LS_TC_WS=1 selects the warp-specialized kernel (read once).
+// The warp-specialized kernel runs unless LS_TC_WS=0 selects the two-CTA
+// kernel (read once).
 bool use_ws() {
   static const bool ws = [] {
     const char* v = std::getenv("LS_TC_WS");
-    return v && std::atoi(v) != 0;
+    return !(v && std::atoi(v) == 0);
   }();
   return ws;
 }
