@@ -50,6 +50,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <queue>
 #include <cstdint>
 #include <cstdlib>
 #include <string>
@@ -494,8 +495,9 @@ __device__ __forceinline__ bool epilogue_sync_or(bool v) {
 }
 
 __global__ void __launch_bounds__(kWsThreads, 1)
-    tc_ws_kernel(const TcBlock* __restrict__ blocks, int n_blocks, const TcStage* __restrict__ prog,
-                 const int* __restrict__ prog_off, const float2* __restrict__ A, const int* __restrict__ out,
+    tc_ws_kernel(const TcBlock* __restrict__ blocks, const int* __restrict__ blk_list, const int* __restrict__ blk_off,
+                 const TcStage* __restrict__ prog, const int* __restrict__ prog_off, const float2* __restrict__ A,
+                 const int* __restrict__ out,
                  const float2* __restrict__ src, float2* __restrict__ dst, int mode, const float2* __restrict__ P,
                  const float* __restrict__ kq, int find_phi, int npad_max, unsigned* __restrict__ err) {
   pdl_enter();
@@ -763,13 +765,13 @@ __global__ void __launch_bounds__(kWsThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&accempty[G % kWsAcc]);
     };
-    // Block k of this CTA is block blockIdx.x + k grid. Its record (rows,
-    // npad, nst, o_off) sits in lane k & 31 of a window of 32 records; the
-    // next window is loaded a window ahead.
-    const int n_mine = (n_blocks - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    // Block k of this CTA is blocks[blk_list[blk_off[cta] + k]]. Its record
+    // (rows, npad, nst, o_off) sits in lane k & 31 of a window of 32
+    // records; the next window is loaded a window ahead.
+    const int b_first = __ldg(blk_off + blockIdx.x), n_mine = __ldg(blk_off + blockIdx.x + 1) - b_first;
     auto load_rec = [&](int k) -> int4 {
       if (k >= n_mine) return make_int4(0, 0, 0, 0);
-      const TcBlock* B = blocks + blockIdx.x + (size_t)k * gridDim.x;
+      const TcBlock* B = blocks + __ldg(blk_list + b_first + k);
       return make_int4(B->rows, B->npad, B->nst, B->o_off);
     };
     auto rec_of = [&](int k, const int4& cur, const int4& nxt, int base) -> int4 {  // warp-uniform k
@@ -849,9 +851,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           basev[i] = extra[i] = 0.f;
           if (c0 + i < rows) {
             const size_t el = ((size_t)orows[ob][c0 + i] * 64 + j) * 2 + part;
-            if (mode == 1) {
-              basev[i] = ld_chain(dstf + el);
-            } else if (mode == 2) {
+            if (mode == 2) {
               basev[i] = ld_chain(reinterpret_cast<const float*>(P) + el);
               if (find_phi) extra[i] = ld_chain(reinterpret_cast<const float*>(src) + el);
             }
@@ -867,10 +867,13 @@ __global__ void __launch_bounds__(kWsThreads, 1)
               v = __uint_as_float(q[i]) + __uint_as_float(ra[i]);
             else if (nchunks == 1)
               v = __uint_as_float(ra[i]);
-            // mode 0: v; mode 1: old + v; mode 2: P + s v, + x with find_phi
-            dstf[el] = mode == 0 ? v
-                                 : (mode == 2 && find_phi ? basev[i] + oscale[sb][c0 + i] * v + extra[i]
-                                                          : basev[i] + v);
+            // mode 0: v; mode 1: old + v (an L2 reduction: one FP32 add, no
+            // round trip); mode 2: P + s v, + x with find_phi
+            if (mode == 1)
+              asm volatile("red.global.add.f32 [%0], %1;" ::"l"(dstf + el), "f"(v) : "memory");
+            else
+              dstf[el] = mode == 0 ? v
+                                   : (find_phi ? basev[i] + oscale[sb][c0 + i] * v + extra[i] : basev[i] + v);
           }
         }
       }
@@ -978,6 +981,8 @@ struct TcPhase {
   long long entries = 0;  // true complex entries
   TcStage* prog = nullptr;  // stage program of tc_ws_kernel (CTA c: prog[prog_off[c] .. prog_off[c + 1]))
   int* prog_off = nullptr;
+  int* blk_list = nullptr;  // CTA c's blocks: blk_list[blk_off[c] .. blk_off[c + 1])
+  int* blk_off = nullptr;
   int prog_grid = 0;
 };
 
@@ -1003,24 +1008,46 @@ cudaError_t dalloc(TcOperator& t, T** p, size_t n) {
 }
 
 // Stage program of a phase whose blocks (nst per block on the host) and
-// gather lists are on the device: blocks dealt round-robin to
-// min(n_blocks, sms) CTAs, each CTA's stages contiguous.
+// gather lists are on the device. The blocks are dealt to min(n_blocks, sms)
+// CTAs longest first, each to the CTA with the least work so far (a block
+// costs its stages plus about two stages of pipeline fill and epilogue);
+// each CTA's stages are contiguous, in the order of its block list.
 cudaError_t build_program(TcOperator& T, TcPhase& ph, const std::vector<int>& nst) {
   const int nb = ph.n_blocks;
   if (nb == 0) return cudaSuccess;
   const int grid = std::min(nb, T.sms);
-  std::vector<int> off(grid + 1, 0);
+  std::vector<int> order(nb);
+  for (int b = 0; b < nb; ++b) order[b] = b;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nst[a] > nst[b]; });
+  std::priority_queue<std::pair<long long, int>, std::vector<std::pair<long long, int>>, std::greater<>> least;
+  for (int c = 0; c < grid; ++c) least.push({0, c});
+  std::vector<std::vector<int>> mine(grid);
+  for (int b : order) {
+    const auto [work, c] = least.top();
+    least.pop();
+    mine[c].push_back(b);
+    least.push({work + nst[b] + 2, c});
+  }
+  std::vector<int> off(grid + 1, 0), boff(grid + 1, 0), list;
   std::vector<int2> stage_of;
   for (int c = 0; c < grid; ++c) {
     off[c] = (int)stage_of.size();
-    for (int b = c; b < nb; b += grid)
+    boff[c] = (int)list.size();
+    for (int b : mine[c]) {
+      list.push_back(b);
       for (int st = 0; st < nst[b]; ++st) stage_of.push_back(make_int2(b, st));
+    }
   }
   off[grid] = (int)stage_of.size();
+  boff[grid] = (int)list.size();
   ph.prog_grid = grid;
   int2* d_of = nullptr;
   cudaError_t e = dalloc(T, &ph.prog, stage_of.size());
   if (e == cudaSuccess) e = dalloc(T, &ph.prog_off, off.size());
+  if (e == cudaSuccess) e = dalloc(T, &ph.blk_list, list.size());
+  if (e == cudaSuccess) e = dalloc(T, &ph.blk_off, boff.size());
+  if (e == cudaSuccess) e = cudaMemcpy(ph.blk_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(ph.blk_off, boff.data(), boff.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&d_of, std::max<size_t>(stage_of.size(), 1) * sizeof(int2));
   if (e == cudaSuccess) e = cudaMemcpy(ph.prog_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && !stage_of.empty())
@@ -1110,8 +1137,9 @@ cudaError_t launch_tc(const TcOperator& T, const TcPhase& ph, const float2* src,
   if (ph.n_blocks == 0) return cudaSuccess;
   if (use_ws()) {  // one CTA per SM, the grid its stage program was dealt to
     return launch_pdl(tc_ws_kernel, ph.prog_grid, kWsThreads, (size_t)ws_smem_for(ph.npad_max), s,
-                      (const TcBlock*)ph.blocks, ph.n_blocks, (const TcStage*)ph.prog, (const int*)ph.prog_off,
-                      (const float2*)ph.A, ph.out, src, dst, mode, P, kq, find_phi, ph.npad_max, T.err);
+                      (const TcBlock*)ph.blocks, (const int*)ph.blk_list, (const int*)ph.blk_off,
+                      (const TcStage*)ph.prog, (const int*)ph.prog_off, (const float2*)ph.A, ph.out, src, dst, mode,
+                      P, kq, find_phi, ph.npad_max, T.err);
   }
   const int grid = std::min(ph.n_blocks, 2 * T.sms);  // two CTAs per SM (96 KB shared memory, 128 TMEM columns each)
   return launch_pdl(tc_gemm_kernel, grid, kTcThreads, (size_t)smem_for(ph.npad_max), s, (const TcBlock*)ph.blocks,
