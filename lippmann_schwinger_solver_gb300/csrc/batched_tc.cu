@@ -86,6 +86,27 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
   return d;
 }
 
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte
+// swizzle layout: 128-byte rows, 8-row atoms of 1024 bytes (SBO), the
+// 16-byte chunk c of row r stored at chunk c ^ (r & 7); descriptor version
+// 1, layout type 2 (128-byte swizzle). A K-step starts 32 bytes further
+// into the rows of the atom.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;               // LBO (unused by swizzled K-major operands)
+  d |= (uint64_t)(1024 >> 4) << 32;     // SBO
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// Float2 index of (row, complex column cc) of a stage plane in the 128-byte
+// swizzle layout (one 128-byte row = the stage's 16 complex columns).
+__host__ __device__ __forceinline__ int canon_sw128(int row, int cc) {
+  return ((row >> 3) * 1024 + (row & 7) * 128 + ((((cc >> 1) ^ (row & 7))) << 4) + (cc & 1) * 8) >> 3;
+}
+
 // Float2 index of (row, complex column cc) inside one stage plane.
 __host__ __device__ __forceinline__ int canon(int row, int cc) {
   return ((row & 7) * 16 + (row >> 3) * kRowGroupBytes + (cc >> 1) * 128 + (cc & 1) * 8) >> 3;
@@ -637,7 +658,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks) {
           const uint32_t o = ks * 256;
-          const uint64_t dxh = sdesc(xh + o, 128, kRowGroupBytes), dxl = sdesc(xl + o, 128, kRowGroupBytes);
+          const uint64_t dxh = sdesc_sw128(xh + 32 * ks), dxl = sdesc_sw128(xl + 32 * ks);
           const uint64_t dah = sdesc(ah + o, 128, kRowGroupBytes), dal = sdesc(al + o, 128, kRowGroupBytes);
           mma_tf32(dt, dxh, dah, idesc, (!chunk_start || ks > 0) ? 1u : 0u);
           mma_tf32(dt, dxh, dal, idesc, 1u);
@@ -707,7 +728,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
         const int j = 2 * m + (ii & 1) + 32 * (ii >> 1);
         const float hx = tf32_rn(vx), hy = tf32_rn(vy);
         const float lx = tf32_rn(vx - hx), ly = tf32_rn(vy - hy);
-        const int o_re = canon(j, kk), o_im = canon(64 + j, kk);
+        const int o_re = canon_sw128(j, kk), o_im = canon_sw128(64 + j, kk);
         Xh[o_re] = make_float2(hx, hy);
         Xl[o_re] = make_float2(lx, ly);
         Xh[o_im] = make_float2(hy, -hx);
