@@ -501,6 +501,14 @@ def run_ours(args):
         # tensor cores against 8 on the CUDA-core block kernels.
         ms_tc = op.time_block_apply(64, warmup=3, iters=10)
         ms_cc = op.time_block_apply(8, warmup=3, iters=10)
+        # The tensor-core apply's roofline: 12 TF32 MMAs (N <= 64) per stage,
+        # each costing a fixed issue time below N = 128 (measured).
+        tc_stages = op.tc_stages()
+        mma_cycles = ls.measure_mma_issue(local, 48)
+        sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+        clk_now = clk.summary()
+        sm_mhz = clk_now.get("sm_mhz") or clk_now.get("sm_max_mhz") or 2070.0
+        tc_floor_ms = tc_stages * 12 * mma_cycles / sm_count / (sm_mhz * 1e6) * 1e3
         op.set_batch_width(8)
         op.gmres_mixed_batched(B[:, :8], max_outer=20, inner_iter=100, tol=1e-8)  # warm-up: workspace
         torch.cuda.synchronize()
@@ -526,7 +534,11 @@ def run_ours(args):
                  "speedup_batched_vs_sequential": ts / tb, "block_width": 64,
                  "block_apply": {"tensor_core_64_ms": ms_tc, "tensor_core_per_rhs_us": ms_tc / 64 * 1e3,
                                  "cuda_core_8_ms": ms_cc, "cuda_core_per_rhs_us": ms_cc / 8 * 1e3,
-                                 "speedup_per_rhs": (ms_cc / 8) / (ms_tc / 64)},
+                                 "speedup_per_rhs": (ms_cc / 8) / (ms_tc / 64),
+                                 "issue_roofline": {"bound": "tensor-core MMA issue", "stages": tc_stages,
+                                                    "mmas": 12 * tc_stages, "cycles_per_mma": mma_cycles,
+                                                    "sm_mhz": sm_mhz, "floor_ms": tc_floor_ms,
+                                                    "frac": tc_floor_ms / ms_tc}},
                  "width8": {"s": tb8, "block_applies_and_fp64_products": nmvb8,
                             "max_true_residual": float(np.max(rrb8)), "converged": codeb8 == 0,
                             "max_rel_diff_vs_width64": float(max(np.linalg.norm(Xb[:, j] - Xb8[:, j]) /
@@ -655,7 +667,8 @@ def run_block_apply(args):
     op.enable_f32()
     ms = op.time_block_apply(args.block_apply, warmup=max(3, args.warmup), iters=max(1, args.steps))
     print(json.dumps({"metric": "FP32 block apply", "unit": "ms", "value": ms, "width": args.block_apply,
-                      "per_rhs_us": ms / args.block_apply * 1e3, "N": op.N, "level": args.level}), flush=True)
+                      "per_rhs_us": ms / args.block_apply * 1e3, "N": op.N, "level": args.level,
+                      "tensor_core_stages": op.tc_stages()}), flush=True)
     op.close()
 
 

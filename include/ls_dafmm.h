@@ -242,6 +242,10 @@ ls_status ls_matvec_f32_many(ls_op* op, int nrhs, const double* X, double* Y);
  * operator's stream after `warmup` untimed applies. No counterpart in the
  * reference. */
 ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float* ms);
+/* Stages (16 complex columns of one block) of one 64-wide tensor-core block
+ * apply, all phases; 0 before the tensor-core form is built (by the first
+ * 64-wide apply). Each stage is 12 MMAs. No counterpart in the reference. */
+ls_status ls_op_tc_stages(const ls_op* op, long long* stages);
 /* Times `iters` device matvecs (inputs resident) with CUDA events on the
  * operator's stream after `warmup` untimed ones; writes the mean ms per
  * matvec and the mean ms of the dominant kernel (M2L). precision: LS_PREC_*. */
@@ -264,6 +268,15 @@ ls_status ls_time_matvec_phases(ls_op* op, int precision, int warmup, int iters,
  * No counterpart in the reference.
  */
 ls_status ls_measure_fma_peak(int device, int kind, double* tflops);
+/*
+ * Issue cost of one TF32 tensor-core MMA (M = 128, N = n, K = 8) on `device`:
+ * one CTA per SM issues 512 back-to-back MMAs into one accumulator; writes
+ * the mean SM cycles per MMA over the SMs (second of two launches). n is a
+ * multiple of 16 in [16, 256]. Below n = 128 the cost does not depend on n:
+ * the floor of the tensor-core block apply (12 MMAs per stage). No
+ * counterpart in the reference.
+ */
+ls_status ls_measure_mma_issue(int device, int n, double* clocks_per_mma);
 
 /*
  * Density at arbitrary points by the reference's Chebyshev-Q+ interpolation

@@ -47,7 +47,7 @@ EXPORTED_SYMBOLS = (
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
     "ls_write_result", "ls_set_pdl", "ls_get_pdl", "ls_time_matvec_phases", "ls_measure_fma_peak", "ls_op_set_inner_basis",
-    "ls_op_set_batch_width", "ls_matvec_f32_many", "ls_time_block_apply",
+    "ls_op_set_batch_width", "ls_matvec_f32_many", "ls_time_block_apply", "ls_op_tc_stages", "ls_measure_mma_issue",
 )
 # Every symbol declared in include/ls_fno.h (learned preconditioner).
 FNO_SYMBOLS = (
@@ -226,6 +226,8 @@ def lib():
         L.ls_time_block_apply.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.ls_time_matvec_phases.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.ls_measure_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, dp]
+        L.ls_measure_mma_issue.argtypes = [ctypes.c_int, ctypes.c_int, dp]
+        L.ls_op_tc_stages.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.ls_get_pdl.argtypes = []
         fp = ctypes.POINTER(ctypes.c_float)
         L.ls_fno_create.argtypes = [ctypes.POINTER(_FnoConfig), ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
@@ -255,6 +257,14 @@ def measure_fma_peak(device=0, kind="fp64"):
     v = ctypes.c_double()
     _check(lib().ls_measure_fma_peak(int(device), 0 if kind == "fp64" else 1, ctypes.byref(v)),
            "ls_measure_fma_peak")
+    return v.value
+
+
+def measure_mma_issue(device=0, n=48):
+    """SM cycles per TF32 tensor-core MMA (M = 128, N = n, K = 8) issued back to
+    back (ls_measure_mma_issue): the floor of the tensor-core block apply."""
+    v = ctypes.c_double()
+    _check(lib().ls_measure_mma_issue(int(device), int(n), ctypes.byref(v)), "ls_measure_mma_issue")
     return v.value
 
 
@@ -370,6 +380,13 @@ class Operator:
         Y = np.empty_like(X, order="F")
         _check(lib().ls_matvec_f32_many(self._h, X.shape[1], _dp(X), _dp(Y)), "ls_matvec_f32_many")
         return Y
+
+    def tc_stages(self):
+        """Stages of one 64-wide tensor-core block apply (12 MMAs each); 0
+        before the first 64-wide apply builds the tensor-core form."""
+        v = ctypes.c_longlong()
+        _check(lib().ls_op_tc_stages(self._h, ctypes.byref(v)), "ls_op_tc_stages")
+        return v.value
 
     def time_block_apply(self, width=64, warmup=3, iters=10):
         """Mean ms of one FP32 block apply of `width` resident right-hand sides

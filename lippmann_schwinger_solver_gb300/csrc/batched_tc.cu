@@ -1005,6 +1005,7 @@ struct TcPhase {
   int* blk_list = nullptr;  // CTA c's blocks: blk_list[blk_off[c] .. blk_off[c + 1])
   int* blk_off = nullptr;
   int prog_grid = 0;
+  long long prog_stages = 0;  // stages of the phase (all CTAs)
 };
 
 struct TcOperator {
@@ -1062,6 +1063,7 @@ cudaError_t build_program(TcOperator& T, TcPhase& ph, const std::vector<int>& ns
   off[grid] = (int)stage_of.size();
   boff[grid] = (int)list.size();
   ph.prog_grid = grid;
+  ph.prog_stages = (long long)stage_of.size();
   int2* d_of = nullptr;
   cudaError_t e = dalloc(T, &ph.prog, stage_of.size());
   if (e == cudaSuccess) e = dalloc(T, &ph.prog_off, off.size());
@@ -1271,6 +1273,19 @@ cudaError_t dev_tc_error(DevOperator& d, unsigned* flag) {
   *flag = 0;
   if (!d.tc) return cudaSuccess;
   return cudaMemcpy(flag, d.tc->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+}
+
+long long dev_tc_stages(const DevOperator& d) {
+  if (!d.tc) return 0;
+  long long n = 0;
+  auto add = [&](const TcPhase& p) {
+    if (p.n_blocks) n += p.prog_stages;
+  };
+  for (auto& p : d.tc->up) add(p);
+  add(d.tc->m2l);
+  for (auto& p : d.tc->down) add(p);
+  add(d.tc->near);
+  return n;
 }
 
 long long dev_tc_operator_bytes(const DevOperator& d) {

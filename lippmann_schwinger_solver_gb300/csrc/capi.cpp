@@ -438,6 +438,12 @@ ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float
   return width == 64 ? tc_status(op, "ls_time_block_apply") : LS_OK;
 }
 
+ls_status ls_op_tc_stages(const ls_op* op, long long* stages) {
+  if (!op || !stages) return fail(LS_E_INVALID, "ls_op_tc_stages: null argument");
+  *stages = op->on_device ? dev_tc_stages(op->dev) : 0;
+  return LS_OK;
+}
+
 ls_status ls_gmres_mixed_batched(ls_op* op, int nrhs, const double* B, int max_outer, int inner_iter, double tol,
                                  double* X, int* n_matvec, double* rel_residuals) {
   if (!op || !B || !X) return fail(LS_E_INVALID, "ls_gmres_mixed_batched: null argument");

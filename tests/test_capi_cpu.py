@@ -88,6 +88,7 @@ def test_host_only_operator_refuses_device_calls(ls):
     with pytest.raises(ls.LSError) as ei:
         op.gmres_mixed_batched(np.zeros((op.N, 3), dtype=np.complex128))
     assert ei.value.code == ls.LS_E_STATE
+    assert op.tc_stages() == 0  # no tensor-core form without a device
     info = op.info
     assert info["far_entries"] > 0 and info["matvec_flops"] > 8 * info["far_entries"]
     assert info["m2l_entries"] <= info["far_entries"]
@@ -134,6 +135,16 @@ def test_null_handles_do_not_crash(ls):
     assert L.ls_op_info(None, None) == ls.LS_E_INVALID
     assert L.ls_matvec(None, None, None, None) == ls.LS_E_INVALID
     assert L.ls_op_skeleton_dump(None, None, 0) == -1
+    assert L.ls_op_tc_stages(None, None) == ls.LS_E_INVALID
+
+
+@pytest.mark.parametrize("n", [0, 8, 24, 272])
+def test_mma_issue_measure_rejects_shapes_before_any_device_call(ls, n):
+    """N must be a multiple of 16 in [16, 256]; the check comes before the
+    device lookup, so it answers without a GPU."""
+    with pytest.raises(ls.LSError) as ei:
+        ls.measure_mma_issue(0, n)
+    assert ei.value.code == ls.LS_E_INVALID
 
 
 def test_noalloc_rejects_operators_larger_than_its_static_array(ls):

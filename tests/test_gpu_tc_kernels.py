@@ -14,7 +14,7 @@ import sys
 import numpy as np
 import pytest
 
-from conftest import CFG_HFR, CFG_L5_BUMPS, ROOT, full_cfg
+from conftest import CFG_C1, CFG_HFR, CFG_L5_BUMPS, ROOT, full_cfg
 
 pytestmark = pytest.mark.gpu
 
@@ -56,3 +56,19 @@ def test_warp_specialized_kernel_equals_two_cta_kernel(tmp_path, cfg):
     print(f"max |warp-specialized - two-CTA| / max |y| = {diff:.2e}")
     assert np.all(np.isfinite(y_ws))
     assert np.array_equal(y_ws, y_2c)
+
+
+def test_mma_issue_cost_and_stage_count(ls):
+    """ls_measure_mma_issue: below N = 128 one TF32 MMA costs the same
+    whatever N (the floor of the block apply), at N = 256 the tensor rate
+    makes it dearer; ls_op_tc_stages counts the stages of the tensor-core
+    form once the first 64-wide apply has built it."""
+    c16, c64, c256 = (ls.measure_mma_issue(0, n) for n in (16, 64, 256))
+    print(f"cycles per MMA: N=16 {c16:.1f}, N=64 {c64:.1f}, N=256 {c256:.1f}")
+    assert 5.0 < c16 < 1000.0 and c64 < 1.5 * c16 and c256 > 1.5 * c16
+    op = ls.Operator(full_cfg(CFG_C1), device=0)
+    op.enable_f32()
+    assert op.tc_stages() == 0
+    op.time_block_apply(64, warmup=0, iters=1)
+    assert op.tc_stages() > 0
+    op.close()
