@@ -246,6 +246,13 @@ ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float
  * apply, all phases; 0 before the tensor-core form is built (by the first
  * 64-wide apply). Each stage is 12 MMAs. No counterpart in the reference. */
 ls_status ls_op_tc_stages(const ls_op* op, long long* stages);
+/* The bounded-wait path of the tensor-core kernels, on its own: one CTA
+ * allocates tensor memory, waits `polls` polls (1 .. 1e8) on an mbarrier
+ * that nothing arrives on, records that the wait gave up as the kernels do
+ * (the flag behind LS_E_TIMEOUT), frees the tensor memory and exits; writes
+ * *gave_up = 1. The context stays usable. For tests of failure detection
+ * without a GPU fault. No counterpart in the reference. */
+ls_status ls_tc_wait_probe(int device, long long polls, int* gave_up);
 /* Times `iters` device matvecs (inputs resident) with CUDA events on the
  * operator's stream after `warmup` untimed ones; writes the mean ms per
  * matvec and the mean ms of the dominant kernel (M2L). precision: LS_PREC_*. */

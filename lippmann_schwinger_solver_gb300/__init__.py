@@ -48,6 +48,7 @@ EXPORTED_SYMBOLS = (
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
     "ls_write_result", "ls_set_pdl", "ls_get_pdl", "ls_time_matvec_phases", "ls_measure_fma_peak", "ls_op_set_inner_basis",
     "ls_op_set_batch_width", "ls_matvec_f32_many", "ls_time_block_apply", "ls_op_tc_stages", "ls_measure_mma_issue",
+    "ls_tc_wait_probe",
 )
 # Every symbol declared in include/ls_fno.h (learned preconditioner).
 FNO_SYMBOLS = (
@@ -228,6 +229,7 @@ def lib():
         L.ls_measure_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int, dp]
         L.ls_measure_mma_issue.argtypes = [ctypes.c_int, ctypes.c_int, dp]
         L.ls_op_tc_stages.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+        L.ls_tc_wait_probe.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int)]
         L.ls_get_pdl.argtypes = []
         fp = ctypes.POINTER(ctypes.c_float)
         L.ls_fno_create.argtypes = [ctypes.POINTER(_FnoConfig), ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
@@ -266,6 +268,15 @@ def measure_mma_issue(device=0, n=48):
     v = ctypes.c_double()
     _check(lib().ls_measure_mma_issue(int(device), int(n), ctypes.byref(v)), "ls_measure_mma_issue")
     return v.value
+
+
+def tc_wait_probe(device=0, polls=100000):
+    """Runs the tensor-core kernels' bounded mbarrier wait on a barrier that
+    nothing arrives on (ls_tc_wait_probe); True when the wait gave up and
+    recorded it."""
+    v = ctypes.c_int()
+    _check(lib().ls_tc_wait_probe(int(device), int(polls), ctypes.byref(v)), "ls_tc_wait_probe")
+    return bool(v.value)
 
 
 def set_pdl(on):

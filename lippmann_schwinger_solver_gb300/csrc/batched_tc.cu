@@ -125,15 +125,16 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b
                    "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, long long limit) {
   uint32_t done = 0;
-  for (long long it = 0; it < kWaitLimit && !done; ++it)
+  for (long long it = 0; it < limit && !done; ++it)
     asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
                  : "=r"(done)
                  : "r"(smem_u32(bar)), "r"(parity)
                  : "memory");
   return done != 0;
 }
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) { return mbar_wait_n(bar, parity, kWaitLimit); }
 
 }  // namespace
 
@@ -907,6 +908,34 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kWsTmemCols));
 }
 
+// The bounded-wait path of the tensor-core kernels on its own: the CTA
+// allocates its tensor memory, every thread waits on an mbarrier that
+// nothing arrives on with the kernels' wait (`polls` polls), a wait that
+// gives up sets the error flag as the kernels' do, and the tensor memory is
+// freed before the CTA exits.
+__global__ void tc_wait_probe_kernel(long long polls, unsigned* __restrict__ err) {
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tbase;
+  const int t = threadIdx.x;
+  if (t < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tbase)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tm = tbase;
+  if (!mbar_wait_n(&bar, 0u, polls)) atomicOr(err, 1u);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (t < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tm), "r"(kTmemCols));
+}
+
 // Stage program of a phase: the stages of block b in order, blocks dealt
 // to the CTAs round-robin (CTA c: blocks c, c + grid, ...); one thread per
 // stage record.
@@ -1273,6 +1302,22 @@ cudaError_t dev_tc_error(DevOperator& d, unsigned* flag) {
   *flag = 0;
   if (!d.tc) return cudaSuccess;
   return cudaMemcpy(flag, d.tc->err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+}
+
+cudaError_t dev_tc_wait_probe(int device, long long polls, unsigned* gave_up) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return e;
+  unsigned* err = nullptr;
+  if ((e = cudaMalloc(&err, sizeof(unsigned))) != cudaSuccess) return e;
+  e = cudaMemset(err, 0, sizeof(unsigned));
+  if (e == cudaSuccess) {
+    tc_wait_probe_kernel<<<1, 128>>>(polls, err);
+    e = cudaDeviceSynchronize();
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(gave_up, err, sizeof(unsigned), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  return e;
 }
 
 long long dev_tc_stages(const DevOperator& d) {

@@ -438,6 +438,18 @@ ls_status ls_time_block_apply(ls_op* op, int width, int warmup, int iters, float
   return width == 64 ? tc_status(op, "ls_time_block_apply") : LS_OK;
 }
 
+ls_status ls_tc_wait_probe(int device, long long polls, int* gave_up) {
+  if (!gave_up || polls < 1 || polls > 100000000LL) return fail(LS_E_INVALID, "ls_tc_wait_probe: bad argument");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return fail(LS_E_CUDA, "ls_tc_wait_probe: no such CUDA device");
+  unsigned flag = 0;
+  const cudaError_t e = dev_tc_wait_probe(device, polls, &flag);
+  if (e != cudaSuccess) return cuda_fail(e, "ls_tc_wait_probe");
+  *gave_up = flag ? 1 : 0;
+  return LS_OK;
+}
+
 ls_status ls_op_tc_stages(const ls_op* op, long long* stages) {
   if (!op || !stages) return fail(LS_E_INVALID, "ls_op_tc_stages: null argument");
   *stages = op->on_device ? dev_tc_stages(op->dev) : 0;

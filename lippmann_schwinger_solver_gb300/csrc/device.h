@@ -136,7 +136,8 @@ void dev_free_tc(DevOperator& d);
 cudaError_t dev_matvec_f32_wide(DevOperator& d, const float2* x, float2* y, float2* S, float2* P, cudaStream_t s);
 cudaError_t dev_tc_error(DevOperator& d, unsigned* flag);
 long long dev_tc_operator_bytes(const DevOperator& d);
-long long dev_tc_stages(const DevOperator& d);  // stages of one tensor-core block apply (0 before it is built)
+long long dev_tc_stages(const DevOperator& d);
+cudaError_t dev_tc_wait_probe(int device, long long polls, unsigned* gave_up);  // stages of one tensor-core block apply (0 before it is built)
 
 // batched.cu
 void dev_free_batch(DevOperator& d);

@@ -1,6 +1,7 @@
 """The C ABI library without a GPU: it loads, exports every symbol declared
 in include/ls_dafmm.h, and its host assembly (device < 0) reproduces the
 oracle's precomputations and NCA skeletons exactly. No compute call runs."""
+import ctypes
 import os
 import re
 
@@ -136,6 +137,9 @@ def test_null_handles_do_not_crash(ls):
     assert L.ls_matvec(None, None, None, None) == ls.LS_E_INVALID
     assert L.ls_op_skeleton_dump(None, None, 0) == -1
     assert L.ls_op_tc_stages(None, None) == ls.LS_E_INVALID
+    assert L.ls_tc_wait_probe(0, 1000, None) == ls.LS_E_INVALID
+    v = ctypes.c_int()
+    assert L.ls_tc_wait_probe(0, 0, ctypes.byref(v)) == ls.LS_E_INVALID
 
 
 @pytest.mark.parametrize("n", [0, 8, 24, 272])

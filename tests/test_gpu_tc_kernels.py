@@ -72,3 +72,15 @@ def test_mma_issue_cost_and_stage_count(ls):
     op.time_block_apply(64, warmup=0, iters=1)
     assert op.tc_stages() > 0
     op.close()
+
+
+def test_bounded_wait_gives_up_and_the_context_survives(ls):
+    """Failure detection without a GPU fault: the tensor-core kernels' bounded
+    mbarrier wait, run on a barrier that nothing arrives on (a short poll
+    limit), gives up and records it; the probe frees its tensor memory, and
+    the same process then runs a tensor-core block apply normally."""
+    assert ls.tc_wait_probe(0, polls=100000)
+    op = ls.Operator(full_cfg(CFG_C1), device=0)
+    op.enable_f32()
+    assert op.time_block_apply(64, warmup=1, iters=2) > 0.0
+    op.close()
