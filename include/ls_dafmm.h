@@ -320,6 +320,19 @@ ls_status ls_op_precomputations(const ls_op* op, double* M, double* near);
  */
 ls_status ls_set_pdl(int on);
 int ls_get_pdl(void);
+/*
+ * Near-field schedule of the native FP64 matvec on uniform trees. No
+ * counterpart in the reference. 1 (the default): the near field (Q+ x per
+ * leaf and the factored colleague blocks) runs on a second stream of the
+ * same priority beside the upward, M2L and downward phases, whose latency-bound
+ * launches leave FP64 issue slots free, and one kernel adds it to the
+ * potentials at the end; 0: after them, in one stream. Results are bitwise
+ * identical in both modes. LS_NEAR_OVERLAP=0 in the environment selects 0 at
+ * load. Process-wide; applies to matvecs queued after the call. Phase timing
+ * (ls_time_matvec_phases) always runs the near field after the far field.
+ */
+ls_status ls_set_near_overlap(int on);
+int ls_get_near_overlap(void);
 
 const char* ls_last_error(void);
 const char* ls_version(void);

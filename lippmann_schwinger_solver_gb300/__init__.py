@@ -48,7 +48,7 @@ EXPORTED_SYMBOLS = (
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
     "ls_write_result", "ls_set_pdl", "ls_get_pdl", "ls_time_matvec_phases", "ls_measure_fma_peak", "ls_op_set_inner_basis",
     "ls_op_set_batch_width", "ls_matvec_f32_many", "ls_time_block_apply", "ls_op_tc_stages", "ls_measure_mma_issue",
-    "ls_tc_wait_probe",
+    "ls_tc_wait_probe", "ls_set_near_overlap", "ls_get_near_overlap",
 )
 # Every symbol declared in include/ls_fno.h (learned preconditioner).
 FNO_SYMBOLS = (
@@ -231,6 +231,8 @@ def lib():
         L.ls_op_tc_stages.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.ls_tc_wait_probe.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int)]
         L.ls_get_pdl.argtypes = []
+        L.ls_set_near_overlap.argtypes = [ctypes.c_int]
+        L.ls_get_near_overlap.argtypes = []
         fp = ctypes.POINTER(ctypes.c_float)
         L.ls_fno_create.argtypes = [ctypes.POINTER(_FnoConfig), ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
         L.ls_fno_destroy.argtypes = [vp]
@@ -277,6 +279,16 @@ def tc_wait_probe(device=0, polls=100000):
     v = ctypes.c_int()
     _check(lib().ls_tc_wait_probe(int(device), int(polls), ctypes.byref(v)), "ls_tc_wait_probe")
     return bool(v.value)
+
+
+def set_near_overlap(on):
+    """Run the native FP64 matvec's near field beside its far-field chain
+    (1, the default) or after it (0) (ls_set_near_overlap); bitwise identical."""
+    lib().ls_set_near_overlap(1 if on else 0)
+
+
+def get_near_overlap():
+    return bool(lib().ls_get_near_overlap())
 
 
 def set_pdl(on):

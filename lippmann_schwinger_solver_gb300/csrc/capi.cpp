@@ -59,6 +59,19 @@ int pdl_enabled() {
   return v;
 }
 void set_pdl_enabled(int on) { g_pdl.store(on ? 1 : 0); }
+
+std::atomic<int> g_near_overlap{-1};
+int near_overlap_enabled() {
+  int v = g_near_overlap.load(std::memory_order_relaxed);
+  if (v < 0) {
+    const char* e = std::getenv("LS_NEAR_OVERLAP");
+    v = (e && e[0] == '0') ? 0 : 1;
+    int expected = -1;
+    if (!g_near_overlap.compare_exchange_strong(expected, v)) v = expected;
+  }
+  return v;
+}
+void set_near_overlap_enabled(int on) { g_near_overlap.store(on ? 1 : 0); }
 }  // namespace lsg
 
 using namespace lsg;
@@ -176,7 +189,8 @@ ls_status ls_op_info(const ls_op* op, ls_op_info_t* o) {
   for (int i = 0; i < LS_ASSEMBLE_STAGES; ++i) o->assemble_stage_seconds[i] = h.stage_seconds[i];
   o->max_rank = h.max_rank;
   // double-float: the near field takes a GEMM and a gather kernel
-  o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 1 : 0);
+  o->n_kernels_per_matvec = d.launches_per_matvec + (d.f64_kernels == LS_F64_DOUBLE_FLOAT ? 1 : 0) +
+                            (d.f64_kernels == LS_F64_NATIVE && dev_near_overlap(d) ? 1 : 0);
   // M2L: every block once (16 B per complex entry), every source charge of
   // the charge buffer once, every potential it writes once.
   o->m2l_entries = op->on_device ? d.m2l.entries : h.m2l.entries();
@@ -845,6 +859,12 @@ ls_status ls_set_pdl(int on) {
   return LS_OK;
 }
 int ls_get_pdl(void) { return pdl_enabled(); }
+
+ls_status ls_set_near_overlap(int on) {
+  set_near_overlap_enabled(on);
+  return LS_OK;
+}
+int ls_get_near_overlap(void) { return near_overlap_enabled(); }
 
 const char* ls_last_error(void) { return t_last_error.c_str(); }
 const char* ls_version(void) { return "lsdafmm-gb300 0.1 (sm_103a)"; }

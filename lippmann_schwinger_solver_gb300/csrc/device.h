@@ -61,6 +61,12 @@ struct DevOperator {
   float2* nearE = nullptr;   // [q][k][row]: 9 x rank x rank (FP32, transposed)
   double2* cbuf = nullptr;   // n_leaves x n_bases: Q^+ x per leaf
   float2* x32 = nullptr;     // N: x in FP32 for the E_q term
+  // The factored near field overlapped with the upward, M2L and downward
+  // phases: its contribution goes to Zn on near_stream (the same priority),
+  // forked after the load of x and joined before the combine with P.
+  cudaStream_t near_stream = nullptr;
+  cudaEvent_t near_fork = nullptr, near_join = nullptr;
+  double2* Zn = nullptr;     // N: the near-field contribution
   // FP32 operator (mixed precision), built on request
   bool has_f32 = false;
   std::vector<DevPhase<float2>> up32, down32;
@@ -137,6 +143,7 @@ cudaError_t dev_matvec_f32_wide(DevOperator& d, const float2* x, float2* y, floa
 cudaError_t dev_tc_error(DevOperator& d, unsigned* flag);
 long long dev_tc_operator_bytes(const DevOperator& d);
 long long dev_tc_stages(const DevOperator& d);
+bool dev_near_overlap(const DevOperator& d);  // the native matvec overlaps its near field (see ls_set_near_overlap)
 cudaError_t dev_tc_wait_probe(int device, long long polls, unsigned* gave_up);  // stages of one tensor-core block apply (0 before it is built)
 
 // batched.cu

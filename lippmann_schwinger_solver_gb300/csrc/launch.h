@@ -51,6 +51,10 @@ __device__ __forceinline__ float ld_chain(const float* p) { return __ldcg(p); }
 // 1: chains use programmatic dependent launch (default), 0: plain launches.
 int pdl_enabled();
 void set_pdl_enabled(int on);
+// Whether the native FP64 matvec runs its near field beside the far-field
+// chain (LS_NEAR_OVERLAP=0 in the environment: after it).
+int near_overlap_enabled();
+void set_near_overlap_enabled(int on);
 
 // kernel<<<grid, block, smem, s>>>(args...) with programmatic stream
 // serialization allowed (unless turned off, see pdl_enabled()).

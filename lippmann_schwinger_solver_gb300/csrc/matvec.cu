@@ -228,6 +228,71 @@ __global__ void __launch_bounds__(256, 4) near_factored_kernel(int n_out, int ra
   }
 }
 
+// The same near field split at P, for the overlapped schedule (ls_set_near_overlap):
+// near_part_kernel writes the colleague sum of every output row to Z (the
+// loop of near_factored_kernel, unchanged), near_combine_kernel forms
+// y = P + kappa^2 q Z + x (find_phi) or P + Z with the same expressions, so
+// both schedules give the same bits.
+__global__ void __launch_bounds__(256, 4) near_part_kernel(int n_out, int rank, int nb, const double2* __restrict__ Vt,
+                                                        const float2* __restrict__ E, const int* __restrict__ coll,
+                                                        const double2* __restrict__ c, const float2* __restrict__ x32,
+                                                        double2* __restrict__ Z) {
+  pdl_enter();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_out) return;
+  const int leaf = t / rank, row = t - leaf * rank;
+  double ar = 0.0, ai = 0.0;
+#pragma unroll 1
+  for (int n = 0; n < 9; ++n) {
+    const int nbx = coll[leaf * 9 + n];
+    if (nbx < 0) continue;
+    const double2* __restrict__ v = Vt + (size_t)n * nb * rank + row;
+    const double2* __restrict__ cc = c + (size_t)nbx * nb;
+    for (int l = 0; l < nb; ++l) {
+      const double2 a = v[(size_t)l * rank];
+      const double2 b = ld_chain(cc + l);
+      ar = fma(a.x, b.x, ar);
+      ar = fma(-a.y, b.y, ar);
+      ai = fma(a.x, b.y, ai);
+      ai = fma(a.y, b.x, ai);
+    }
+    const float2* __restrict__ e = E + (size_t)n * rank * rank + row;
+    const float2* __restrict__ xs = x32 + (size_t)nbx * rank;
+    float er = 0.0f, ei = 0.0f;
+    for (int k = 0; k < rank; ++k) {
+      const float2 a = e[(size_t)k * rank];
+      const float2 b = ld_chain(xs + k);
+      er = fmaf(a.x, b.x, er);
+      er = fmaf(-a.y, b.y, er);
+      ei = fmaf(a.x, b.y, ei);
+      ei = fmaf(a.y, b.x, ei);
+    }
+    ar += (double)er;
+    ai += (double)ei;
+  }
+  Z[t] = make_double2(ar, ai);
+}
+
+__global__ void __launch_bounds__(256) near_combine_kernel(int n_out, const double* __restrict__ kq,
+                                                           const double2* __restrict__ Z,
+                                                           const double2* __restrict__ x,
+                                                           const double2* __restrict__ P, double2* __restrict__ y,
+                                                           int find_phi) {
+  pdl_enter();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_out) return;
+  const double2 z = ld_chain(Z + t);
+  const double ar = z.x, ai = z.y;
+  const double2 p = ld_chain(P + t);
+  if (find_phi) {
+    const double s = kq[t];
+    const double2 xs = ld_chain(x + t);
+    y[t] = make_double2(p.x + s * ar + xs.x, p.y + s * ai + xs.y);
+  } else {
+    y[t] = make_double2(p.x + ar, p.y + ai);
+  }
+}
+
 // Near field of the FP32 operator in two passes (as the double-float path,
 // matvec_df.cu). Pass 1: Z32[s][q][row] = B_q(row, :) x_s for every leaf s
 // and direction q; a block takes kNearSources32 leaves (their x staged in
@@ -472,6 +537,16 @@ bool dev_upload(const HostOperator& h, DevOperator& d, std::string& err) {
     if (!dmalloc(&d.nearE, e32.size(), tot, err)) return false;
     if (!dmalloc(&d.cbuf, (size_t)h.n_leaves * h.n_bases, tot, err)) return false;
     if (!dmalloc(&d.x32, (size_t)h.N, tot, err)) return false;
+    if (!dmalloc(&d.Zn, (size_t)h.N, tot, err)) return false;
+    // The same (default) priority as the far-field chain: measured, a
+    // higher-priority chain starves the near field onto the critical path
+    // (0.660 ms per matvec against 0.601 at equal priority, level 6).
+    if ((e = cudaStreamCreateWithFlags(&d.near_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&d.near_fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&d.near_join, cudaEventDisableTiming)) != cudaSuccess) {
+      err = std::string("near-field stream: ") + cudaGetErrorString(e);
+      return false;
+    }
     cudaMemcpy(d.nearVt, vt.data(), vt.size() * sizeof(double2), cudaMemcpyHostToDevice);
     cudaMemcpy(d.Qp, h.Qpinv.data(), h.Qpinv.size() * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(d.nearE, e32.data(), e32.size() * sizeof(float2), cudaMemcpyHostToDevice);
@@ -510,7 +585,10 @@ void dev_free(DevOperator& d) {
   for (auto& p : d.down32) cudaFree(p.A);
   cudaFree(d.m2l32.A);
   cudaFree(d.S); cudaFree(d.P); cudaFree(d.nearB); cudaFree(d.kq); cudaFree(d.colleague);
-  cudaFree(d.nearVt); cudaFree(d.Qp); cudaFree(d.nearE); cudaFree(d.cbuf); cudaFree(d.x32);
+  cudaFree(d.nearVt); cudaFree(d.Qp); cudaFree(d.nearE); cudaFree(d.cbuf); cudaFree(d.x32); cudaFree(d.Zn);
+  if (d.near_fork) cudaEventDestroy(d.near_fork);
+  if (d.near_join) cudaEventDestroy(d.near_join);
+  if (d.near_stream) cudaStreamDestroy(d.near_stream);
   cudaFree(d.S32); cudaFree(d.P32); cudaFree(d.nearB32); cudaFree(d.kq32); cudaFree(d.Z32);
   cudaFree(d.xbuf); cudaFree(d.ybuf);
   dev_free_df(d);
@@ -563,11 +641,27 @@ bool dev_enable_f32(DevOperator& d, std::string& err) {
   return true;
 }
 
+bool dev_near_overlap(const DevOperator& d) {
+  return !d.generic_near && d.near_stream && near_overlap_enabled();
+}
+
 cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_t s, bool mark_m2l) {
   if (d.f64_kernels == LS_F64_DOUBLE_FLOAT) return dev_matvec_df(d, x, y, s, mark_m2l);
   if (!s) s = d.stream;
   launch_pdl(load_zero_kernel<double2, double2>, (unsigned)sm_count(d.device) * 4, 256, 0, s, x, d.S, (long long)d.N,
              d.P, d.pots_len);
+  // Overlapped near field (not when the phases are being timed apart): it
+  // needs only x, so it forks here and joins before the combine with P.
+  const bool overlap = !mark_m2l && dev_near_overlap(d);
+  if (overlap) {
+    cudaEventRecord(d.near_fork, s);
+    cudaStreamWaitEvent(d.near_stream, d.near_fork, 0);
+    launch_pdl(near_coeff_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, d.near_stream, d.n_leaves,
+               d.rank, d.n_bases, d.Qp, d.S, d.cbuf, d.x32);
+    launch_pdl(near_part_kernel, (unsigned)((d.N + 255) / 256), 256, 0, d.near_stream, d.N, d.rank, d.n_bases,
+               d.nearVt, d.nearE, d.colleague, d.cbuf, d.x32, d.Zn);
+    cudaEventRecord(d.near_join, d.near_stream);
+  }
   for (auto& ph : d.up) launch_gemv<0>(ph, (const double2*)d.S, d.S, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[0], s);
   launch_gemv<1>(d.m2l, (const double2*)d.S, d.P, s, d.device);
@@ -577,6 +671,12 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
   if (d.generic_near) {
     launch_gemv<3>(d.nearph, (const double2*)d.S, d.P, s, d.device);
     launch_pdl(copy_out_kernel<double2, double2>, (unsigned)((d.N + 255) / 256), 256, 0, s, (const double2*)d.P, y, d.N);
+    return cudaGetLastError();
+  }
+  if (overlap) {
+    cudaStreamWaitEvent(s, d.near_join, 0);
+    launch_pdl(near_combine_kernel, (unsigned)((d.N + 255) / 256), 256, 0, s, d.N, d.kq, (const double2*)d.Zn,
+               (const double2*)d.S, (const double2*)d.P, y, d.find_phi);
     return cudaGetLastError();
   }
   launch_pdl(near_coeff_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
@@ -589,6 +689,18 @@ cudaError_t dev_matvec(DevOperator& d, const double2* x, double2* y, cudaStream_
 // Phases of the FP32 operator after x has been placed in S32.
 template <class Y>
 static cudaError_t f32_phases(DevOperator& d, Y* y, cudaStream_t s, bool mark_m2l) {
+  const int nthr = (9 * d.rank + 31) / 32 * 32;
+  const size_t near_smem = (size_t)kNearSources32 * d.rank * sizeof(float2);
+  const unsigned near_blocks = (unsigned)((d.n_leaves + kNearSources32 - 1) / kNearSources32);
+  // near-field pass 1 beside the far-field chain (ls_set_near_overlap)
+  const bool overlap = !mark_m2l && dev_near_overlap(d);
+  if (overlap) {
+    cudaEventRecord(d.near_fork, s);
+    cudaStreamWaitEvent(d.near_stream, d.near_fork, 0);
+    launch_pdl(near_gemm32_kernel, near_blocks, (unsigned)nthr, near_smem, d.near_stream, d.n_leaves, d.rank,
+               d.nearB32, d.S32, d.Z32);
+    cudaEventRecord(d.near_join, d.near_stream);
+  }
   for (auto& ph : d.up32) launch_gemv<0>(ph, (const float2*)d.S32, d.S32, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[2], s);
   launch_gemv<1>(d.m2l32, (const float2*)d.S32, d.P32, s, d.device);
@@ -600,9 +712,11 @@ static cudaError_t f32_phases(DevOperator& d, Y* y, cudaStream_t s, bool mark_m2
     launch_pdl(copy_out_kernel<float2, Y>, (unsigned)((d.N + 255) / 256), 256, 0, s, (const float2*)d.P32, y, d.N);
     return cudaGetLastError();
   }
-  const int nthr = (9 * d.rank + 31) / 32 * 32;
-  launch_pdl(near_gemm32_kernel, (unsigned)((d.n_leaves + kNearSources32 - 1) / kNearSources32), (unsigned)nthr,
-             (size_t)kNearSources32 * d.rank * sizeof(float2), s, d.n_leaves, d.rank, d.nearB32, d.S32, d.Z32);
+  if (overlap)
+    cudaStreamWaitEvent(s, d.near_join, 0);
+  else
+    launch_pdl(near_gemm32_kernel, near_blocks, (unsigned)nthr, near_smem, s, d.n_leaves, d.rank, d.nearB32, d.S32,
+               d.Z32);
   launch_pdl(near_gather32_kernel<Y>, (unsigned)((d.N + 255) / 256), 256, 0, s, d.N, d.rank, d.Z32, d.kq32,
              d.colleague, d.S32, d.P32, y, d.find_phi);
   return cudaGetLastError();

@@ -405,6 +405,19 @@ cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStre
   const int n = d.N;
   launch_pdl(split_zero_kernel, (unsigned)sms(d.device) * 4, 256, 0, s, x, d.S_df, (long long)n, d.P_df,
              d.pots_len);
+  const size_t near_smem = (size_t)kNearSources * (d.n_bases * sizeof(float4) + d.rank * sizeof(float2));
+  const unsigned near_blocks = (unsigned)((d.n_leaves + kNearSources - 1) / kNearSources);
+  // near-field coefficients and pass 1 beside the far-field chain (ls_set_near_overlap)
+  const bool overlap = !mark_m2l && dev_near_overlap(d);
+  if (overlap) {
+    cudaEventRecord(d.near_fork, s);
+    cudaStreamWaitEvent(d.near_stream, d.near_fork, 0);
+    launch_pdl(near_coeff_df_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, d.near_stream,
+               d.n_leaves, d.rank, d.n_bases, d.Qp_df, d.S_df, d.c_df, d.x32);
+    launch_pdl(near_gemm_df_kernel, near_blocks, kNearThreads, near_smem, d.near_stream, d.n_leaves, d.rank,
+               d.n_bases, d.Vt_df, d.nearE, d.c_df, d.x32, d.Z_df, d.ZE_df);
+    cudaEventRecord(d.near_join, d.near_stream);
+  }
   for (auto& ph : d.up_df) launch_df<0>(ph, (const float4*)d.S_df, d.S_df, s, d.device);
   if (mark_m2l) cudaEventRecord(d.ev[0], s);
   launch_df<1>(d.m2l_df, (const float4*)d.S_df, d.P_df, s, d.device);
@@ -416,15 +429,16 @@ cudaError_t dev_matvec_df(DevOperator& d, const double2* x, double2* y, cudaStre
     launch_pdl(join_out_kernel, (unsigned)((n + 255) / 256), 256, 0, s, (const float4*)d.P_df, y, n);
     return cudaGetLastError();
   }
-  launch_pdl(near_coeff_df_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
-             d.n_bases, d.Qp_df, d.S_df, d.c_df, d.x32);
-  {
-    const size_t smem = (size_t)kNearSources * (d.n_bases * sizeof(float4) + d.rank * sizeof(float2));
-    launch_pdl(near_gemm_df_kernel, (unsigned)((d.n_leaves + kNearSources - 1) / kNearSources), kNearThreads, smem, s,
-               d.n_leaves, d.rank, d.n_bases, d.Vt_df, d.nearE, d.c_df, d.x32, d.Z_df, d.ZE_df);
-    launch_pdl(near_gather_df_kernel, (unsigned)((n + 255) / 256), 256, 0, s, n, d.rank, d.Z_df, d.ZE_df, d.kq,
-               d.colleague, x, d.P_df, y, d.find_phi);
+  if (overlap) {
+    cudaStreamWaitEvent(s, d.near_join, 0);
+  } else {
+    launch_pdl(near_coeff_df_kernel, (unsigned)((d.n_leaves * d.n_bases + 255) / 256), 256, 0, s, d.n_leaves, d.rank,
+               d.n_bases, d.Qp_df, d.S_df, d.c_df, d.x32);
+    launch_pdl(near_gemm_df_kernel, near_blocks, kNearThreads, near_smem, s, d.n_leaves, d.rank, d.n_bases, d.Vt_df,
+               d.nearE, d.c_df, d.x32, d.Z_df, d.ZE_df);
   }
+  launch_pdl(near_gather_df_kernel, (unsigned)((n + 255) / 256), 256, 0, s, n, d.rank, d.Z_df, d.ZE_df, d.kq,
+             d.colleague, x, d.P_df, y, d.find_phi);
   return cudaGetLastError();
 }
 

@@ -85,3 +85,30 @@ def test_pdl_and_plain_launches_are_bitwise_equal_at_level6(ls):
     for k, (a, b) in enumerate(zip(with_pdl, plain)):
         assert np.array_equal(a, b), f"result {k} differs between PDL and plain launches"
     op.close()
+
+
+def test_overlapped_and_serial_near_field_are_bitwise_equal_at_level6(ls):
+    """The native FP64 matvec with its near field on a second stream beside
+    the far-field chain (the default) and after it (ls_set_near_overlap(0)):
+    back-to-back matvecs on different inputs, restarted GMRES and the
+    mixed-precision solve give the same bits; with PDL on and off."""
+    op = ls.Operator(_workload(ls), device=0)
+    op.enable_f32()
+    rng = np.random.default_rng(7)
+    xs = [rng.uniform(-1, 1, op.N) + 1j * rng.uniform(-1, 1, op.N) for _ in range(3)]
+    was, was_pdl = ls.get_near_overlap(), ls.get_pdl()
+    try:
+        runs = {}
+        for pdl in (True, False):
+            ls.set_pdl(pdl)
+            for overlap in (True, False):
+                ls.set_near_overlap(overlap)
+                runs[(pdl, overlap)] = _run_all(ls, op, xs)
+    finally:
+        ls.set_near_overlap(was)
+        ls.set_pdl(was_pdl)
+    ref = runs[(True, False)]
+    for key, res in runs.items():
+        for k, (a, b) in enumerate(zip(res, ref)):
+            assert np.array_equal(a, b), f"result {k} differs (pdl, overlap) = {key}"
+    op.close()
