@@ -307,7 +307,37 @@ ls_status ls_matvec_host(ls_op* op, const double* x, double* y) {
   void* xd = pinned_device_address(x);
   void* yd = xd ? pinned_device_address(y) : nullptr;
   if (xd && yd && xd != yd) {
-    cudaError_t e = dev_matvec(d, (const double2*)xd, (double2*)yd, d.stream, false);
+    // One call is synchronous, so the host's enqueueing of the matvec's
+    // launches and events would sit on its path: the sequence is captured
+    // once into a CUDA graph (programmatic launches and the near-field
+    // fork/join become its edges) and launched as one operation.
+    const int key = d.f64_kernels * 4 + near_overlap_enabled() * 2 + pdl_enabled();
+    if (!(d.mv_graph && d.mv_x == xd && d.mv_y == yd && d.mv_key == key)) {
+      if (d.mv_graph) cudaGraphExecDestroy(d.mv_graph);
+      d.mv_graph = nullptr;
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        const cudaError_t em = dev_matvec(d, (const double2*)xd, (double2*)yd, d.stream, false);
+        e = cudaStreamEndCapture(d.stream, &g);
+        if (e == cudaSuccess) e = em;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&d.mv_graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {  // not capturable here: launch the sequence directly
+        if (d.mv_graph) cudaGraphExecDestroy(d.mv_graph);
+        d.mv_graph = nullptr;
+        cudaGetLastError();
+        e = dev_matvec(d, (const double2*)xd, (double2*)yd, d.stream, false);
+        if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_host");
+        if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_matvec_host sync");
+        return LS_OK;
+      }
+      d.mv_x = xd;
+      d.mv_y = yd;
+      d.mv_key = key;
+    }
+    cudaError_t e = cudaGraphLaunch(d.mv_graph, d.stream);
     if (e != cudaSuccess) return cuda_fail(e, "ls_matvec_host");
     if ((e = cudaStreamSynchronize(d.stream)) != cudaSuccess) return cuda_fail(e, "ls_matvec_host sync");
     return LS_OK;

@@ -67,6 +67,13 @@ struct DevOperator {
   cudaStream_t near_stream = nullptr;
   cudaEvent_t near_fork = nullptr, near_join = nullptr;
   double2* Zn = nullptr;     // N: the near-field contribution
+  // The matvec on page-locked host buffers as one CUDA graph (ls_matvec_host),
+  // captured for one (x, y, kernel family, schedule) and launched as one
+  // operation; recaptured when any of them changes.
+  cudaGraphExec_t mv_graph = nullptr;
+  const void* mv_x = nullptr;
+  const void* mv_y = nullptr;
+  int mv_key = -1;
   // FP32 operator (mixed precision), built on request
   bool has_f32 = false;
   std::vector<DevPhase<float2>> up32, down32;

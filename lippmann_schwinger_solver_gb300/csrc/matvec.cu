@@ -586,6 +586,7 @@ void dev_free(DevOperator& d) {
   cudaFree(d.m2l32.A);
   cudaFree(d.S); cudaFree(d.P); cudaFree(d.nearB); cudaFree(d.kq); cudaFree(d.colleague);
   cudaFree(d.nearVt); cudaFree(d.Qp); cudaFree(d.nearE); cudaFree(d.cbuf); cudaFree(d.x32); cudaFree(d.Zn);
+  if (d.mv_graph) cudaGraphExecDestroy(d.mv_graph);
   if (d.near_fork) cudaEventDestroy(d.near_fork);
   if (d.near_join) cudaEventDestroy(d.near_join);
   if (d.near_stream) cudaStreamDestroy(d.near_stream);
