@@ -244,6 +244,30 @@ def adaptive_leg(ls, local, timed, max_iter):
     return out
 
 
+def gpu_assembly_leg(ls, cfg, x, y_host, skel_host, device):
+    """The workload's operator assembled with its far field on the GPU
+    (ls_config.far_on_gpu 1: sum table; 2: table and NCA; then also the
+    precomputation quadratures) against the default host-assembled one,
+    which the oracle leg pins: assembly stages, the matvec's distance and
+    the fraction of skeleton nodes that agree."""
+    names = ("geometry", "precompute", "lists", "nca", "checks", "pack")
+    out = {"tolerance": 10.0 ** (1 - cfg.TOL_POW)}
+    for name, over in (("far_table", dict(far_on_gpu=1)), ("far_table_and_nca", dict(far_on_gpu=2)),
+                       ("far_and_precompute", dict(far_on_gpu=2, precompute_on_gpu=1))):
+        t0 = time.perf_counter()
+        opg = ls.Operator(dataclasses.replace(cfg, **over), device=device)
+        wall = time.perf_counter() - t0
+        y = opg.matvec(x)
+        ig = opg.info
+        out[name] = {"assemble_s": ig["assemble_seconds"], "operator_create_s": wall,
+                     "assemble_stages_s": dict(zip(names, (round(t, 3) for t in ig["assemble_stage_seconds"]))),
+                     "rel_l2_vs_host_operator": float(np.linalg.norm(y - y_host) / np.linalg.norm(y_host)),
+                     "skeleton_nodes_equal": ls.skeleton_agreement(opg.skeleton_dump(), skel_host),
+                     "max_rank": ig["max_rank"]}
+        opg.close()
+    return out
+
+
 def oracle_leg(ls, cfg, y_gpu, skel_gpu, budget_s=20.0):
     """The CPU restatement of the reference (oracle/) on the machine's host cores:
     its matvec/s with all threads and with one, its GMRES solve time to a
@@ -573,6 +597,9 @@ def run_ours(args):
         many_g["host_stages_s"] = {k: round(sum(r["host_stages_s"][k] for r in recs_g), 2)
                                    for k in recs_g[0]["host_stages_s"]}
         many["gpu_precompute"] = many_g
+    far_gpu = None
+    if rank == 0 and not args.no_gpu_assembly:
+        far_gpu = gpu_assembly_leg(ls, cfg, x, y_main, op.skeleton_dump(), local)
     peak, peak_kind = load_peaks()
     achieved = info["m2l_bytes"] / (ms_m2l * 1e-3) / 1e9
     traffic = traffic_per_launch(args.f64_kernels)
@@ -627,7 +654,8 @@ def run_ours(args):
                    "assemble_s": info["assemble_seconds"], "device_bytes": info["device_bytes"],
                    "assemble_stages_s": dict(zip(("geometry", "precompute", "lists", "nca", "checks", "pack"),
                                                  (round(t, 3) for t in info["assemble_stage_seconds"]))),
-                   "far_entries": info["far_entries"], "max_rank": info["max_rank"]},
+                   "far_entries": info["far_entries"], "max_rank": info["max_rank"],
+                   "far_on_gpu": far_gpu},
         "clocks": clk.summary(),
         "other_f64_kernels": alt,
         "solve": solve,
@@ -724,6 +752,26 @@ def run_adaptive_matvecs(args):
     op.close()
 
 
+def run_far_assembly(args):
+    """Only the far-field-on-GPU assemblies of the workload against the host
+    assembly (one JSON line)."""
+    import lippmann_schwinger_solver_gb300 as ls
+
+    ls.build()
+    cfg = workload_config(ls, args.level)
+    op = ls.Operator(cfg, device=0)
+    x = input_vector(op.N)
+    y = op.matvec(x)
+    ih = op.info
+    line = {"workload": "uniform level %d, N=%d, kappa=40, 3 seeded bumps, NCA tol 1e-10" % (args.level, op.N),
+            "host_assemble_s": ih["assemble_seconds"],
+            "host_stages_s": dict(zip(("geometry", "precompute", "lists", "nca", "checks", "pack"),
+                                      (round(t, 3) for t in ih["assemble_stage_seconds"]))),
+            "far_on_gpu": gpu_assembly_leg(ls, cfg, x, y, op.skeleton_dump(), 0)}
+    print(json.dumps(line), flush=True)
+    op.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -737,6 +785,10 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the many-direction batched solve")
     ap.add_argument("--no-nn", action="store_true", help="skip the learned-preconditioner solve")
     ap.add_argument("--no-adaptive", action="store_true", help="skip the adaptive-tree operator at the README run")
+    ap.add_argument("--no-gpu-assembly", action="store_true",
+                    help="skip the operators assembled with their far field on the GPU")
+    ap.add_argument("--far-assembly", action="store_true",
+                    help="only compare the GPU far-field assemblies with the host one at this level")
     ap.add_argument("--angles", type=int, default=64, help="incidence directions of the batched solve")
     ap.add_argument("--scatterers", type=int, default=32,
                     help="scatterers of the many-scatterer batched workload (0 skips it)")
@@ -763,6 +815,8 @@ def main():
         run_profile_solve(args)
     elif args.adaptive_matvecs > 0:
         run_adaptive_matvecs(args)
+    elif args.far_assembly:
+        run_far_assembly(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

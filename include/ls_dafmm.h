@@ -90,6 +90,20 @@ typedef struct {
    * within about 1e-7 of it on the tested trees). Operators assembled
    * without a device always integrate on the host. */
   int precompute_on_gpu;
+  /* Far-field assembly of a uniform tree (getMatrixEntry,
+   * G_FMM2DTree.hpp:603-658; ACA_only_nodes, GMRES/ACA.hpp:253-481):
+   * 0 (the default): on the host cores, entries from a cache of Hankel sums
+   * filled on demand, bit-exact with the reference's algorithm;
+   * 1: the far-field sums of every distinct relative position are tabulated
+   * on the operator's GPU (on the host cores when it has no device) and the
+   * host's NCA and block fills read them from that table;
+   * 2: as 1, and the NCA skeleton search of every box runs on the GPU as
+   * well (one warp per box; the host redoes any box whose rank passes the
+   * GPU's capacity).
+   * GPU values differ from the host's in the last bits, which can move an
+   * NCA pivot among near-equal candidates; the matvec stays within the NCA
+   * tolerance of the host-assembled operator's. Adaptive trees ignore it. */
+  int far_on_gpu;
 } ls_config;
 
 typedef struct {

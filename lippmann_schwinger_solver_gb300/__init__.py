@@ -91,6 +91,7 @@ class _Config(ctypes.Structure):
         ("tree_adaptive", ctypes.c_int),
         ("treeAdaptivity", ctypes.c_int),
         ("precompute_on_gpu", ctypes.c_int),
+        ("far_on_gpu", ctypes.c_int),
     ]
 
 
@@ -144,12 +145,13 @@ class Config:
     tree_adaptive: int = 0   # 1: the reference's adaptive quadtree (createAdaptiveTree + 2:1 balance)
     treeAdaptivity: int = 5  # adaptive: boxes split until q is resolved to 10^-treeAdaptivity
     precompute_on_gpu: int = 0  # 1: precomputation quadratures on the operator's GPU (not bit-exact with the host)
+    far_on_gpu: int = 0  # 1: far-field sum table on the GPU; 2: and the NCA skeleton search (uniform trees)
 
     def to_c(self):
         c = _Config()
         for f in ("nCones_LFR", "nChebNodes", "yes2DFMM", "TOL_POW", "degreeOfBases", "nLevelsUniform",
                   "Qchoice", "findPhi", "reference_rounding", "tree_adaptive", "treeAdaptivity",
-                  "precompute_on_gpu"):
+                  "precompute_on_gpu", "far_on_gpu"):
             setattr(c, f, int(getattr(self, f)))
         c.L = float(self.L)
         c.kappa = float(self.kappa)
@@ -180,6 +182,31 @@ def seeded_bumps(seed, n=3):
 
 
 _lib = None
+
+
+def skeleton_nodes(dump):
+    """Per-node skeletons of an ls_op_skeleton_dump array: {(level, box,
+    cone or -1): (out_active, in_active, out_charge, out_check, in_charge,
+    in_check, user_check)} with the lists as tuples of point indices."""
+    d = [int(v) for v in dump]
+    out, p = {}, 0
+    while p < len(d):
+        key, flags = (d[p], d[p + 1], d[p + 2]), (d[p + 3], d[p + 4])
+        p += 5
+        lists = []
+        for _ in range(5):
+            n = d[p]
+            lists.append(tuple(d[p + 1:p + 1 + n]))
+            p += 1 + n
+        out[key] = flags + tuple(lists)
+    return out
+
+
+def skeleton_agreement(dump_a, dump_b):
+    """Fraction of the nodes of dump_b whose skeletons (flags and all five
+    lists) are the same in dump_a."""
+    a, b = skeleton_nodes(dump_a), skeleton_nodes(dump_b)
+    return sum(1 for k, v in b.items() if a.get(k) == v) / max(1, len(b))
 
 
 def build(verbose=False):

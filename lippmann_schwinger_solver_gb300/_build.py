@@ -18,7 +18,10 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CXX_SOURCES = ["assemble.cpp", "capi.cpp"]
 CU_SOURCES = ["matvec.cu", "matvec_df.cu", "gmres.cu", "batched.cu", "fno.cu", "nn_precond.cu", "peaks.cu", "batched_tc.cu",
-              "quadrature.cu"]
+              "quadrature.cu", "far_gpu.cu"]
+# The far-field assembly on the GPU rounds every product and sum on its own,
+# as the host assembler (-ffp-contract=off) does.
+CU_EXTRA = {"far_gpu.cu": ["--fmad=false"]}
 
 
 def _nvcc():
@@ -37,7 +40,7 @@ def _cmds():
     for s in CU_SOURCES:
         o = os.path.join(OBJ, s + ".o")
         cmds.append((o, [_nvcc(), "-O3", "-std=c++17", ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
-                         "-Xptxas", "-v" if os.environ.get("LS_PTXAS_VERBOSE") else "-O3"] + inc +
+                         "-Xptxas", "-v" if os.environ.get("LS_PTXAS_VERBOSE") else "-O3"] + CU_EXTRA.get(s, []) + inc +
                      ["-c", os.path.join(CSRC, s), "-o", o], [os.path.join(CSRC, s)]))
     return cmds
 

@@ -199,6 +199,11 @@ thread_local int t_assembly_device = -1;
 // Device for the precomputation quadratures of an assembly with cfg: its GPU
 // when cfg asks for it (and there is one), else none.
 int quadrature_device(const ls_config& cfg) { return cfg.precompute_on_gpu ? t_assembly_device : -1; }
+// Largest far-field sum table tabulated for far_on_gpu (host and device copies).
+constexpr size_t kFarTableMaxBytes = size_t(4) << 30;
+// Rank capacity of a GPU NCA block (its scratch holds this many pivot
+// vectors); the host redoes the rare block that passes it.
+constexpr int kNcaRankCap = 48;
 
 // ---------------------------------------------------------------- small dense QR
 // Column-pivoted Householder QR (xGEQP3 with norm downdating); solve()
@@ -544,6 +549,9 @@ struct Node {
 class Builder {
  public:
   explicit Builder(const ls_config& c) : cfg(c) {}
+  ~Builder() { gpu_far_close(gfar); }
+  Builder(const Builder&) = delete;
+  Builder& operator=(const Builder&) = delete;
   bool run(HostOperator& op, std::string& err);
 
  private:
@@ -568,6 +576,21 @@ class Builder {
   std::vector<std::vector<Node>> nodes;             // [level][node]
   mutable HankelTable htab;                         // shared by NCA and block fills
   const uint64_t id = ++g_assembly_id;              // tags thread-local table entries
+  // far_on_gpu: the far-field sums of every distinct relative position
+  // (FarTables); a target's record about a leaf is dense_rec(i, leaf).
+  FarTables ft;
+  struct FreeDeleter {
+    void operator()(cd* p) const { std::free(p); }
+  };
+  std::unique_ptr<cd[], FreeDeleter> dS;
+  bool dense = false;
+  int dny = 0;
+  GpuFar* gfar = nullptr;
+  const cd* dense_rec(int i, int leaf) const {
+    const int xi = ft.xid[(size_t)ft.xrow[i] * ft.ncol + ft.lcol[leaf]];
+    const int yi = ft.yid[(size_t)ft.yrow[i] * ft.ncol + ft.lrow[leaf]];
+    return dS.get() + ((size_t)xi * dny + yi) * rank;
+  }
 
   bool is_lfr(int j) const { return j >= level_LFR; }
   int nodes_at(int j) const { return is_lfr(j) ? (1 << (2 * j)) : (1 << (2 * j)) * nCones[j]; }
@@ -645,6 +668,7 @@ class Builder {
       vals.swap(nv);
     }
     const cd* get(int i, int leaf) {
+      if (b->dense) return b->dense_rec(i, leaf);
       const long long key = (long long)i * 1048576LL + leaf;
       if (key == last_key) return last;
       last_key = key;
@@ -700,9 +724,21 @@ class Builder {
   int aca(const std::vector<int>& rows, const std::vector<int>& cols, double eps, std::vector<int>& rb,
           std::vector<int>& cb, std::vector<cd>* Ar, HCache& hc) const;
 
+  // One NCA block: out (outgoing) has the far checks as rows and the
+  // box's own charges as columns, in the box's own checks as rows and the
+  // far charges as columns.
+  struct NcaJob {
+    Node* nd = nullptr;
+    bool out = false;
+    std::vector<int> rows, cols, rb, cb;
+    int rank = 0;
+  };
+
   void geometry();
   void precompute();
   void interaction_lists();
+  void far_tables();
+  void run_nca(std::vector<NcaJob>& jobs);
   void nca_level_lfr(int j);
   void nca_level_hfr(int j);
   void user_checks();
@@ -1158,62 +1194,235 @@ static inline int cone_towards(const std::vector<double>& cxj, const std::vector
   return int(a / ap);
 }
 
-void Builder::nca_level_lfr(int j) {
-  const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
-  const int nbx = 1 << (2 * j);
-  const bool leaf = (j == nL);
-  // outgoing
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int k = 0; k < nbx; ++k) {
-    HCache hc{this, {}};
-    Node& nd = lfr(j, k);
-    std::vector<int> own, far;
-    if (leaf) for (int i = 0; i < rank; ++i) own.push_back(k * rank + i);
-    else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * k + c).out_charge; own.insert(own.end(), v.begin(), v.end()); }
-    for (int b : nd.IL) {
-      if (leaf) for (int i = 0; i < rank; ++i) far.push_back(b * rank + i);
-      else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * b + c).in_check; far.insert(far.end(), v.begin(), v.end()); }
-    }
-    if (!far.empty() && !own.empty()) {
-      nd.out_active = true;
-      std::vector<int> rb, cb;
-      if (aca(far, own, tol, rb, cb, &nd.Ar, hc) > 0) {
-        for (int r : rb) nd.out_check.push_back(far[r]);
-        for (int c : cb) nd.out_charge.push_back(own[c]);
+// Tables for far_on_gpu (see FarTables). Leaf centres of one column share
+// their x bits (every box of a column is reached by the same halvings), so
+// fl(gx_i - cx_leaf) is a function of (x node of i, column of i's leaf,
+// column of the leaf). The sums are tabulated on the operator's GPU, or on
+// the host cores when the operator has no device; a GPU that cannot do it
+// leaves the assembly on the default path. Every record the host reads
+// here is key_sums of the same (rx, ry) bits that the default path keys its
+// cache on, so a host-tabulated assembly is the default one bit for bit.
+void Builder::far_tables() {
+  dense = false;
+  if (!cfg.far_on_gpu || !(kappa > 0.0)) return;
+  const int n1 = cfg.nChebNodes, nleaf = 1 << (2 * nL), ncol = 1 << nL;
+  std::vector<double> xs(cx[nL]), ys(cy[nL]);
+  std::sort(xs.begin(), xs.end());
+  std::sort(ys.begin(), ys.end());
+  xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
+  ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
+  if ((int)xs.size() != ncol || (int)ys.size() != ncol) return;
+  FarTables t;
+  t.rank = rank;
+  t.ncol = ncol;
+  t.findPhi = cfg.findPhi;
+  t.kappa = kappa;
+  t.lcol.resize(nleaf);
+  t.lrow.resize(nleaf);
+  for (int l = 0; l < nleaf; ++l) {
+    t.lcol[l] = (int)(std::lower_bound(xs.begin(), xs.end(), cx[nL][l]) - xs.begin());
+    t.lrow[l] = (int)(std::lower_bound(ys.begin(), ys.end(), cy[nL][l]) - ys.begin());
+  }
+  // Coordinates of each (node, column) row, checked bit for bit against
+  // every point of the row.
+  std::vector<double> gxr((size_t)n1 * ncol), gyr((size_t)n1 * ncol);
+  std::vector<char> seenx(gxr.size(), 0), seeny(gyr.size(), 0);
+  t.xrow.resize(N);
+  t.yrow.resize(N);
+  for (int i = 0; i < N; ++i) {
+    const int l = i / rank, c = (i % rank) % n1, r = (i % rank) / n1;
+    const int xr = c * ncol + t.lcol[l], yr = r * ncol + t.lrow[l];
+    t.xrow[i] = xr;
+    t.yrow[i] = yr;
+    for (int axis = 0; axis < 2; ++axis) {
+      std::vector<double>& g = axis ? gyr : gxr;
+      std::vector<char>& seen = axis ? seeny : seenx;
+      const int row = axis ? yr : xr;
+      const double v = axis ? gy_[i] : gx_[i];
+      if (!seen[row]) {
+        g[row] = v;
+        seen[row] = 1;
+      } else if (std::memcmp(&g[row], &v, sizeof(double)) != 0) {
+        return;
       }
-    } else {
-      nd.out_active = false;
-      nd.out_charge = own;
     }
   }
-  // incoming
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int k = 0; k < nbx; ++k) {
-    HCache hc{this, {}};
-    Node& nd = lfr(j, k);
-    std::vector<int> own, far;
-    if (leaf) for (int i = 0; i < rank; ++i) own.push_back(k * rank + i);
-    else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * k + c).in_check; own.insert(own.end(), v.begin(), v.end()); }
-    for (int b : nd.IL) {
-      if (leaf) for (int i = 0; i < rank; ++i) far.push_back(b * rank + i);
-      else for (int c = 0; c < 4; ++c) { const auto& v = lfr(j + 1, 4 * b + c).out_charge; far.insert(far.end(), v.begin(), v.end()); }
+  auto distinct = [&](const std::vector<double>& g, const std::vector<double>& cs, std::vector<double>& u,
+                      std::vector<int>& id) {
+    std::unordered_map<uint64_t, int> at;
+    id.resize(g.size() * cs.size());
+    for (size_t row = 0; row < g.size(); ++row)
+      for (size_t lc = 0; lc < cs.size(); ++lc) {
+        const double v = g[row] - cs[lc];
+        uint64_t bits;
+        std::memcpy(&bits, &v, sizeof(double));
+        auto it = at.find(bits);
+        if (it == at.end()) {
+          it = at.emplace(bits, (int)u.size()).first;
+          u.push_back(v);
+        }
+        id[row * cs.size() + lc] = it->second;
+      }
+  };
+  distinct(gxr, xs, t.ux, t.xid);
+  distinct(gyr, ys, t.uy, t.yid);
+  const size_t nkeys = t.ux.size() * t.uy.size();
+  if (nkeys * rank * sizeof(cd) > kFarTableMaxBytes) return;
+  t.kq = kq_;
+  t.M = Mleaf;
+  ft = std::move(t);
+  dny = (int)ft.uy.size();
+  // The host copy, allocated without a serial fill and first touched by
+  // all threads (its pages then spread over the threads that read them).
+  const size_t nrec = nkeys * rank;
+  dS.reset(static_cast<cd*>(std::malloc(nrec * sizeof(cd))));
+  if (!dS) return;
+  cd* S = dS.get();
+#pragma omp parallel for schedule(static)
+  for (long long key = 0; key < (long long)nkeys; ++key)
+    for (int r = 0; r < rank; ++r) S[(size_t)key * rank + r] = cd(0.0, 0.0);
+  const int device = t_assembly_device;
+  if (device >= 0) {
+    gfar = gpu_far_open(device, ft, S);
+    if (!gfar) {
+      dS.reset();
+      return;
     }
-    if (!far.empty() && !own.empty()) {
-      nd.in_active = true;
-      std::vector<int> rb, cb;
-      if (aca(own, far, tol, rb, cb, nullptr, hc) > 0) {
-        for (int r : rb) nd.in_check.push_back(own[r]);
-        for (int c : cb) nd.in_charge.push_back(far[c]);
+  } else {
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long key = 0; key < (long long)nkeys; ++key) {
+      const double rx = ft.ux[key / dny], ry = ft.uy[key % dny];
+      if (rx == 0.0 && ry == 0.0) continue;  // coincident points: never a far-field pair
+      key_sums(rx, ry, S + (size_t)key * rank);
+    }
+  }
+  dense = true;
+}
+
+// The NCA of a batch of blocks (ACA_only_nodes per block). With far_on_gpu
+// = 2 the blocks run on the GPU, and the host keeps only those the GPU
+// marked (rank capacity) or could not run; the outgoing blocks' pivot rows
+// (Ar) of GPU results are filled from the table. Then the results go to
+// their nodes: an empty side leaves the node inactive with its own list
+// passed through.
+void Builder::run_nca(std::vector<NcaJob>& jobs) {
+  const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
+  const int nj = (int)jobs.size();
+  std::vector<char> on_gpu(nj, 0);
+  if (gfar && cfg.far_on_gpu == 2) {
+    std::vector<NcaTask> tasks;
+    std::vector<int> which, idx;
+    int piv_off = 0;
+    for (int t = 0; t < nj; ++t) {
+      const NcaJob& jb = jobs[t];
+      if (jb.rows.empty() || jb.cols.empty()) continue;
+      NcaTask tk;
+      tk.idx_off = (long long)idx.size();
+      tk.n1 = (int)jb.rows.size();
+      tk.n2 = (int)jb.cols.size();
+      tk.R = std::min(std::min(tk.n1, tk.n2), kNcaRankCap);
+      tk.out_off = piv_off;
+      piv_off += 2 * tk.R;
+      idx.insert(idx.end(), jb.rows.begin(), jb.rows.end());
+      idx.insert(idx.end(), jb.cols.begin(), jb.cols.end());
+      tasks.push_back(tk);
+      which.push_back(t);
+    }
+    std::vector<int> ranks, piv, status;
+    if (!tasks.empty() && gpu_far_nca(gfar, tasks, idx, tol, ranks, piv, status)) {
+      for (size_t u = 0; u < tasks.size(); ++u) {
+        if (status[u] != 0) continue;
+        NcaJob& jb = jobs[which[u]];
+        const NcaTask& tk = tasks[u];
+        jb.rank = ranks[u];
+        jb.rb.assign(piv.begin() + tk.out_off, piv.begin() + tk.out_off + jb.rank);
+        jb.cb.assign(piv.begin() + tk.out_off + tk.R, piv.begin() + tk.out_off + tk.R + jb.rank);
+        on_gpu[which[u]] = 1;
+      }
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int t = 0; t < nj; ++t) {
+    NcaJob& jb = jobs[t];
+    if (jb.rows.empty() || jb.cols.empty()) continue;
+    HCache hc{this, {}};
+    if (!on_gpu[t]) {
+      jb.rank = aca(jb.rows, jb.cols, tol, jb.rb, jb.cb, jb.out ? &jb.nd->Ar : nullptr, hc);
+    } else if (jb.out && jb.rank > 0) {
+      std::vector<int> prow(jb.rank);
+      for (int a = 0; a < jb.rank; ++a) prow[a] = jb.rows[jb.rb[a]];
+      jb.nd->Ar.assign((size_t)jb.rank * jb.cols.size(), cd(0.0, 0.0));
+      fill(prow, jb.cols, hc, jb.nd->Ar.data(), (int)jb.cols.size());
+    }
+  }
+  for (NcaJob& jb : jobs) {
+    Node& nd = *jb.nd;
+    const bool active = !jb.rows.empty() && !jb.cols.empty();
+    if (jb.out) {
+      nd.out_active = active;
+      if (!active) {
+        nd.out_charge = jb.cols;
+      } else if (jb.rank > 0) {
+        for (int r : jb.rb) nd.out_check.push_back(jb.rows[r]);
+        for (int c : jb.cb) nd.out_charge.push_back(jb.cols[c]);
       }
     } else {
-      nd.in_active = false;
-      nd.in_check = own;
+      nd.in_active = active;
+      if (!active) {
+        nd.in_check = jb.rows;
+      } else if (jb.rank > 0) {
+        for (int r : jb.rb) nd.in_check.push_back(jb.rows[r]);
+        for (int c : jb.cb) nd.in_charge.push_back(jb.cols[c]);
+      }
     }
   }
 }
 
+// NCA of the LFR level j (G_FMM2DTree.hpp:2062-2386): the outgoing block of
+// a box pairs the far checks (its interaction list's, leaves: all their
+// points; else their children's incoming checks) with its own charges
+// (leaves: its points; else its children's outgoing charges); the incoming
+// block pairs its own checks with the far charges.
+void Builder::nca_level_lfr(int j) {
+  const int nbx = 1 << (2 * j);
+  const bool leaf = (j == nL);
+  std::vector<NcaJob> jobs(2 * (size_t)nbx);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int t = 0; t < 2 * nbx; ++t) {
+    const int k = t % nbx;
+    NcaJob& jb = jobs[t];
+    jb.out = t < nbx;
+    jb.nd = &lfr(j, k);
+    std::vector<int>& own = jb.out ? jb.cols : jb.rows;
+    std::vector<int>& far = jb.out ? jb.rows : jb.cols;
+    if (leaf) {
+      for (int i = 0; i < rank; ++i) own.push_back(k * rank + i);
+    } else {
+      for (int c = 0; c < 4; ++c) {
+        const Node& ch = lfr(j + 1, 4 * k + c);
+        const auto& v = jb.out ? ch.out_charge : ch.in_check;
+        own.insert(own.end(), v.begin(), v.end());
+      }
+    }
+    for (int b : jb.nd->IL) {
+      if (leaf) {
+        for (int i = 0; i < rank; ++i) far.push_back(b * rank + i);
+      } else {
+        for (int c = 0; c < 4; ++c) {
+          const Node& ch = lfr(j + 1, 4 * b + c);
+          const auto& v = jb.out ? ch.in_check : ch.out_charge;
+          far.insert(far.end(), v.begin(), v.end());
+        }
+      }
+    }
+  }
+  run_nca(jobs);
+}
+
+// NCA of the HFR level j (G_FMM2DTree.hpp:3232-3571), per box and cone:
+// own charges / checks from the children's nodes for that cone, far ones
+// from the interaction list's boxes through the cone that faces this box.
 void Builder::nca_level_hfr(int j) {
-  const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
   const int nbx = 1 << (2 * j), nc = nCones[j];
   auto gather = [&](int jj, int kk, int cn, bool charges, std::vector<int>& dst) {
     for (int c = 0; c < 4; ++c) {
@@ -1222,46 +1431,20 @@ void Builder::nca_level_hfr(int j) {
       dst.insert(dst.end(), v.begin(), v.end());
     }
   };
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int t = 0; t < nbx * nc; ++t) {
-    const int k = t / nc, cn = t % nc;
-    HCache hc{this, {}};
-    Node& nd = cone(j, k, cn);
-    std::vector<int> own, far;
-    gather(j, k, cn, true, own);
-    for (int b : nd.IL) gather(j, b, cone_towards(cx[j], cy[j], k, b, aperture[j]), false, far);
-    if (!far.empty() && !own.empty()) {
-      nd.out_active = true;
-      std::vector<int> rb, cb;
-      if (aca(far, own, tol, rb, cb, &nd.Ar, hc) > 0) {
-        for (int r : rb) nd.out_check.push_back(far[r]);
-        for (int c : cb) nd.out_charge.push_back(own[c]);
-      }
-    } else {
-      nd.out_active = false;
-      nd.out_charge = own;
-    }
+  const int nn = nbx * nc;
+  std::vector<NcaJob> jobs(2 * (size_t)nn);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int t = 0; t < 2 * nn; ++t) {
+    const int u = t % nn, k = u / nc, cn = u % nc;
+    NcaJob& jb = jobs[t];
+    jb.out = t < nn;
+    jb.nd = &cone(j, k, cn);
+    std::vector<int>& own = jb.out ? jb.cols : jb.rows;
+    std::vector<int>& far = jb.out ? jb.rows : jb.cols;
+    gather(j, k, cn, jb.out, own);
+    for (int b : jb.nd->IL) gather(j, b, cone_towards(cx[j], cy[j], k, b, aperture[j]), !jb.out, far);
   }
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int t = 0; t < nbx * nc; ++t) {
-    const int k = t / nc, cn = t % nc;
-    HCache hc{this, {}};
-    Node& nd = cone(j, k, cn);
-    std::vector<int> own, far;
-    gather(j, k, cn, false, own);
-    for (int b : nd.IL) gather(j, b, cone_towards(cx[j], cy[j], k, b, aperture[j]), true, far);
-    if (!far.empty() && !own.empty()) {
-      nd.in_active = true;
-      std::vector<int> rb, cb;
-      if (aca(own, far, tol, rb, cb, nullptr, hc) > 0) {
-        for (int r : rb) nd.in_check.push_back(own[r]);
-        for (int c : cb) nd.in_charge.push_back(far[c]);
-      }
-    } else {
-      nd.in_active = false;
-      nd.in_check = own;
-    }
-  }
+  run_nca(jobs);
 }
 
 void Builder::user_checks() {
@@ -1706,6 +1889,7 @@ bool Builder::run(HostOperator& op, std::string& err) {
   op.stage_seconds[1] = lap();
   interaction_lists();
   op.stage_seconds[2] = lap();
+  far_tables();
   for (int j = nL; j >= level_LFR; --j) nca_level_lfr(j);
   for (int j = level_LFR - 1; j >= 2; --j) nca_level_hfr(j);
   op.stage_seconds[3] = lap();
@@ -1713,6 +1897,10 @@ bool Builder::run(HostOperator& op, std::string& err) {
   op.stage_seconds[4] = lap();
   pack(op);
   htab.clear();
+  gpu_far_close(gfar);
+  gfar = nullptr;
+  dense = false;
+  dS.reset();
   op.stage_seconds[5] = lap();
   // Operator-level data for the near field and the C ABI.
   op.cfg = cfg;
@@ -1801,6 +1989,12 @@ void set_assembly_device(int device) { t_assembly_device = device; }
 
 // The GPU quadrature (csrc/quadrature.cu) replaces this stub in the library;
 // a host-only build keeps it and integrates on the host.
+__attribute__((weak)) GpuFar* gpu_far_open(int, const FarTables&, cd*) { return nullptr; }
+__attribute__((weak)) bool gpu_far_nca(GpuFar*, const std::vector<NcaTask>&, const std::vector<int>&, double,
+                                       std::vector<int>&, std::vector<int>&, std::vector<int>&) {
+  return false;
+}
+__attribute__((weak)) void gpu_far_close(GpuFar*) {}
 __attribute__((weak)) bool gpu_quadrature(int, const std::vector<QuadTask>&, const std::vector<double>&,
                                           const std::vector<double>&, std::vector<cd>&) {
   return false;

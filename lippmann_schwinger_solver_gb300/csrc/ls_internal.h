@@ -106,11 +106,47 @@ struct QuadTask {
 bool gpu_quadrature(int device, const std::vector<QuadTask>& tasks, const std::vector<double>& gx,
                     const std::vector<double>& gw, std::vector<cd>& out);
 
+// The far-field entry tables of a uniform tree (the x and y parts of
+// p_i - c_leaf take few distinct values): ux / uy the distinct values;
+// xid[xrow * ncol + lcol] the index in ux of fl(gx_i - cx_leaf) for a point
+// of x row xrow (x node * ncol + x column of its leaf) and a leaf of x
+// column lcol; likewise yid. A far-field entry's 31-term sums then sit at
+// S[(xid * ny + yid) * rank + node].
+struct FarTables {
+  int rank = 0, ncol = 0, findPhi = 0;
+  double kappa = 0.0;
+  std::vector<double> ux, uy;
+  std::vector<int> xid, yid;    // (nChebNodes * ncol) x ncol
+  std::vector<int> xrow, yrow;  // per point
+  std::vector<int> lcol, lrow;  // per leaf
+  std::vector<double> kq;       // kappa^2 q per point
+  std::vector<cd> M;            // rank x 31, the leaf moments
+};
+// One NCA block for the GPU: rows idx[idx_off, +n1), columns
+// idx[idx_off + n1, +n2) (point indices); pivots up to R = min(n1, n2, cap):
+// rows at piv[out_off, +R), columns at piv[out_off + R, +R).
+struct NcaTask {
+  long long idx_off;
+  int n1, n2, R, out_off;
+};
+// csrc/far_gpu.cu. gpu_far_open builds the far-field sum table on `device`
+// and copies it into S_host (ux.size() * uy.size() * rank elements);
+// nullptr when that is not possible. gpu_far_nca runs the NCA of a batch
+// of blocks with tolerance eps (status 1 marks a block whose rank reached
+// R < min(n1, n2)); false when the batch could not run. gpu_far_close
+// frees the device state. A host-only build gets stubs that fail, and the
+// host does the work.
+struct GpuFar;
+GpuFar* gpu_far_open(int device, const FarTables& t, cd* S_host);
+bool gpu_far_nca(GpuFar* f, const std::vector<NcaTask>& tasks, const std::vector<int>& idx, double eps,
+                 std::vector<int>& ranks, std::vector<int>& piv, std::vector<int>& status);
+void gpu_far_close(GpuFar* f);
+
 // assemble.cpp
 bool assemble(const ls_config& cfg, HostOperator& op, std::string& err);
 // The GPU that the calling thread's assemblies may use for their
-// precomputation quadratures (-1: none), set by ls_op_create around
-// assemble().
+// precomputation quadratures and far field (-1: none), set by ls_op_create
+// around assemble().
 void set_assembly_device(int device);
 // The contrast plugin q(x, y) selected by cfg (userkernel::ContrastFunction).
 double contrast_at(const ls_config& cfg, double x, double y);
