@@ -17,16 +17,17 @@
 // libstdc++'s and glibc's, in the last bits. The file is compiled without
 // FMA contraction, as the host's assembler is.
 //
-// NCA. One warp per task (a box's outgoing or incoming block: rows, cols,
-// tolerance), tasks taken from an atomic counter. The steps are the host's
-// aca_core in the same order: pivot search with ties to the lowest index,
-// the rank-1 updates element by element in the same operand order, the
-// norm estimate and the stopping rules. Norms and dot products are warp
-// reductions (another summation order than the host's loop), so a stopping
-// decision taken within rounding of its threshold can differ. A task whose
-// rank would pass the scratch's rank capacity is marked and the host redoes
-// it. Every loop is bounded by the task's sizes; nothing waits on another
-// thread beyond __syncwarp.
+// NCA. One CTA per task (a box's outgoing or incoming block: rows, cols,
+// tolerance; 128 threads on levels with few blocks, 32 on levels with many),
+// tasks taken from an atomic counter. The steps are
+// the host's aca_core in the same order: pivot search with ties to the
+// lowest index, the rank-1 updates element by element in the same operand
+// order, the norm estimate and the stopping rules. Norms and dot products
+// are block reductions (another summation order than the host's loop), so
+// a stopping decision taken within rounding of its threshold can differ. A
+// task whose rank would pass the scratch's rank capacity is marked and the
+// host redoes it. Every loop is bounded by the task's sizes; threads wait
+// on nothing but the CTA's own barriers.
 
 #include <cuda_runtime.h>
 
@@ -45,7 +46,6 @@ namespace {
 constexpr int kSeriesG = 15;                 // FarFieldInteraction.hpp:55
 constexpr int kTerms = 2 * kSeriesG + 1;
 constexpr int kTableKeys = 128;              // keys (threads) per block of the table kernel
-constexpr int kNcaWarpsPerBlock = 4;
 constexpr int kNcaRankCapG = 64;             // largest NcaTask::R the kernel takes
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -158,16 +158,49 @@ __device__ __forceinline__ double2 far_entry(const NcaGeomDev& g, int i, int j) 
   return make_double2(re, im);
 }
 
+// Threads of one NCA block (a CTA of NT threads, 32 or 128): vectors are
+// split over all of them; norms, dot products and the pivot search are
+// block reductions.
+template <int NT>
+struct NcaShared {
+  static constexpr int kWarps = NT / 32;
+  double2 coef[kNcaRankCapG];  // coefficients of the current rank-1 updates
+  double red[4][kWarps];       // per-warp partial sums
+  int redi[kWarps];            // per-warp pivot candidates
+  int task;
+};
+
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
   return v;
 }
 
+// Sums v[0..K) over the block; every thread gets the same bits (the warp
+// sums are combined in warp order by each thread).
+template <int K, int NT>
+__device__ __forceinline__ void block_sum(double (&v)[K], NcaShared<NT>& sh) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < K; ++j) v[j] = warp_sum(v[j]);
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < K; ++j) sh.red[j][warp] = v[j];
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    double t = 0.0;
+    for (int w = 0; w < NT / 32; ++w) t += sh.red[j][w];
+    v[j] = t;
+  }
+  __syncthreads();
+}
+
 // First index of the largest |v| among the unused ones, 0 when all are used.
-__device__ int warp_argmax(const double2* v, const unsigned char* used, int n, int lane) {
+template <int NT>
+__device__ int block_argmax(const double2* v, const unsigned char* used, int n, NcaShared<NT>& sh) {
   double best = -1.0;
   int bi = INT_MAX;
-  for (int k = lane; k < n; k += 32) {
+  for (int k = threadIdx.x; k < n; k += NT) {
     if (used[k]) continue;
     const double a = hypot(v[k].x, v[k].y);
     if (a > best) {
@@ -183,6 +216,23 @@ __device__ int warp_argmax(const double2* v, const unsigned char* used, int n, i
       bi = oi;
     }
   }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sh.red[0][warp] = best;
+    sh.redi[warp] = bi;
+  }
+  __syncthreads();
+  best = -1.0;
+  bi = INT_MAX;
+  for (int w = 0; w < NT / 32; ++w) {
+    const double ob = sh.red[0][w];
+    const int oi = sh.redi[w];
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+  }
+  __syncthreads();
   return best < 0.0 ? 0 : bi;
 }
 
@@ -198,43 +248,30 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
   return make_double2((a.x * r + a.y) / den, (a.y * r - a.x) / den);
 }
 
-__device__ __forceinline__ double warp_norm(const double2* v, int n, int lane) {
-  double s = 0.0;
-  for (int k = lane; k < n; k += 32) s += v[k].x * v[k].x + v[k].y * v[k].y;
-  return sqrt(warp_sum(s));
-}
-
-// sum_k conj(a_k) b_k
-__device__ __forceinline__ double2 warp_cdot(const double2* a, const double2* b, int n, int lane) {
-  double sr = 0.0, si = 0.0;
-  for (int k = lane; k < n; k += 32) {
-    const double x = a[k].x, y = a[k].y, c = b[k].x, d = b[k].y;
-    sr += x * c + y * d;
-    si += x * d - y * c;
-  }
-  return make_double2(warp_sum(sr), warp_sum(si));
-}
-
 // as_row: out[k] = K(rows[fixed], cols[k]), k < n2; else out[k] = K(rows[k], cols[fixed]), k < n1.
+template <int NT>
 __device__ __forceinline__ void fetch(const NcaGeomDev& g, const int* __restrict__ rows,
                                       const int* __restrict__ cols, int n1, int n2, bool as_row, int fixed,
-                                      double2* __restrict__ out, int lane) {
+                                      double2* __restrict__ out) {
   if (as_row) {
     const int i = rows[fixed];
 #pragma unroll 4
-    for (int k = lane; k < n2; k += 32) out[k] = far_entry(g, i, cols[k]);
+    for (int k = threadIdx.x; k < n2; k += NT) out[k] = far_entry(g, i, cols[k]);
   } else {
     const int j = cols[fixed];
 #pragma unroll 4
-    for (int k = lane; k < n1; k += 32) out[k] = far_entry(g, rows[k], j);
+    for (int k = threadIdx.x; k < n1; k += NT) out[k] = far_entry(g, rows[k], j);
   }
 }
 
-// One NCA task by one warp. The first vector fetched lives on domain D1
+// One NCA task by one block. The first vector fetched lives on domain D1
 // (columns when the block has fewer rows than columns, rows otherwise),
 // the second on D2; V holds the normalised D1 vectors, U the D2 ones.
+// Every branch below depends only on values all threads hold alike.
+template <int NT>
 __device__ void aca_task(const NcaGeomDev& g, const NcaTask& tk, const int* idx, double eps, double2* scr,
-                         unsigned char* used, int* piv, int* rank_out, int* status_out, double2* coef, int lane) {
+                         unsigned char* used, int* piv, int* rank_out, int* status_out, NcaShared<NT>& sh) {
+  const int tid = threadIdx.x;
   const int n1 = tk.n1, n2 = tk.n2, R = tk.R;
   const int* rows = idx + tk.idx_off;
   const int* cols = rows + n1;
@@ -251,19 +288,19 @@ __device__ void aca_task(const NcaGeomDev& g, const NcaTask& tk, const int* idx,
   int* cb = rb + R;
   int* list1 = rowfirst ? cb : rb;         // pivots on D1
   int* list2 = rowfirst ? rb : cb;         // pivots on D2
-  for (int k = lane; k < d1 + d2; k += 32) used[k] = 0;
-  __syncwarp();
+  for (int k = tid; k < d1 + d2; k += NT) used[k] = 0;
+  __syncthreads();
   int i1 = 0, i2 = 0, l = 0;
   for (; l < d2; ++l) {
     i2 = l;
-    __syncwarp();  // every lane has read p[i1] before p is refetched
-    fetch(g, rows, cols, n1, n2, rowfirst, i2, p, lane);
-    __syncwarp();
-    i1 = warp_argmax(p, used1, d1, lane);
+    __syncthreads();  // every thread has read p[i1] before p is refetched
+    fetch<NT>(g, rows, cols, n1, n2, rowfirst, i2, p);
+    __syncthreads();
+    i1 = block_argmax(p, used1, d1, sh);
     if (cmag(p[i1]) > eps) break;
   }
   if (l == d2) {
-    if (lane == 0) {
+    if (tid == 0) {
       *rank_out = 0;
       *status_out = 0;
     }
@@ -271,67 +308,70 @@ __device__ void aca_task(const NcaGeomDev& g, const NcaTask& tk, const int* idx,
   }
   {
     const double2 pv = p[i1];
-    for (int k = lane; k < d1; k += 32) V[k] = cdiv(p[k], pv);
+    for (int k = tid; k < d1; k += NT) V[k] = cdiv(p[k], pv);
   }
-  fetch(g, rows, cols, n1, n2, !rowfirst, i1, q, lane);
-  __syncwarp();
-  for (int k = lane; k < d2; k += 32) U[k] = q[k];
-  if (lane == 0) {
+  fetch<NT>(g, rows, cols, n1, n2, !rowfirst, i1, q);
+  __syncthreads();
+  for (int k = tid; k < d2; k += NT) U[k] = q[k];
+  if (tid == 0) {
     list1[0] = i1;
     list2[0] = i2;
     used1[i1] = 1;
     used2[i2] = 1;
   }
-  __syncwarp();
+  __syncthreads();
   int rk = 1, status = 0;
   double nS = 0.0, prev = 1000.0;
-  i2 = warp_argmax(q, used2, d2, lane);
+  i2 = block_argmax(q, used2, d2, sh);
   while (cmag(p[i1]) > eps && cmag(q[i2]) > eps && fabs(prev - nS) >= eps * prev && rk < mn) {
     if (rk >= R) {
       status = 1;
       break;
     }
-    __syncwarp();  // every lane has read p[i1] and q[i2] before they are refetched
-    fetch(g, rows, cols, n1, n2, rowfirst, i2, p, lane);
+    __syncthreads();  // every thread has read p[i1] and q[i2] before they are refetched
+    fetch<NT>(g, rows, cols, n1, n2, rowfirst, i2, p);
     // p[k] -= U[a][i2] V[a][k], a = 0..rk-1 in order (the host's sub_scaled
     // sequence for every element); the coefficients staged in shared memory.
-    for (int a = lane; a < rk; a += 32) coef[a] = U[(size_t)a * d2 + i2];
-    __syncwarp();
-    for (int k = lane; k < d1; k += 32) {
+    for (int a = tid; a < rk; a += NT) sh.coef[a] = U[(size_t)a * d2 + i2];
+    __syncthreads();
+    for (int k = tid; k < d1; k += NT) {
       double2 x = p[k];
 #pragma unroll 4
       for (int a = 0; a < rk; ++a) {
-        const double2 f = coef[a], w = V[(size_t)a * d1 + k];
+        const double2 f = sh.coef[a], w = V[(size_t)a * d1 + k];
         x = make_double2(x.x - (f.x * w.x - f.y * w.y), x.y - (f.x * w.y + f.y * w.x));
       }
       p[k] = x;
     }
-    __syncwarp();
-    const int n_i1 = warp_argmax(p, used1, d1, lane);
-    double2* Vr = V + (size_t)rk * d1;
+    __syncthreads();
+    const int n_i1 = block_argmax(p, used1, d1, sh);
+    double2* __restrict__ Vr = V + (size_t)rk * d1;
     {
       const double2 pv = p[n_i1];
-      for (int k = lane; k < d1; k += 32) Vr[k] = cdiv(p[k], pv);
+      for (int k = tid; k < d1; k += NT) Vr[k] = cdiv(p[k], pv);
     }
-    fetch(g, rows, cols, n1, n2, !rowfirst, n_i1, q, lane);
-    for (int a = lane; a < rk; a += 32) coef[a] = V[(size_t)a * d1 + n_i1];
-    __syncwarp();
+    fetch<NT>(g, rows, cols, n1, n2, !rowfirst, n_i1, q);
+    for (int a = tid; a < rk; a += NT) sh.coef[a] = V[(size_t)a * d1 + n_i1];
+    __syncthreads();
     double2* __restrict__ Ur = U + (size_t)rk * d2;
-    for (int k = lane; k < d2; k += 32) {
+    double nn[2] = {0.0, 0.0};
+    for (int k = tid; k < d2; k += NT) {
       double2 x = q[k];
 #pragma unroll 4
       for (int a = 0; a < rk; ++a) {
-        const double2 f = coef[a], w = U[(size_t)a * d2 + k];
+        const double2 f = sh.coef[a], w = U[(size_t)a * d2 + k];
         x = make_double2(x.x - (f.x * w.x - f.y * w.y), x.y - (f.x * w.y + f.y * w.x));
       }
       q[k] = x;
       Ur[k] = x;
+      nn[0] += x.x * x.x + x.y * x.y;
     }
-    __syncwarp();
-    const double nu = warp_norm(Ur, d2, lane), nv = warp_norm(Vr, d1, lane);
+    for (int k = tid; k < d1; k += NT) nn[1] += Vr[k].x * Vr[k].x + Vr[k].y * Vr[k].y;
+    block_sum<2>(nn, sh);  // also orders the writes of q, Ur before the reads below
+    const double nu = sqrt(nn[0]), nv = sqrt(nn[1]);
     if (nu < 1e-8 || nv < 1e-8) break;
     i1 = n_i1;
-    if (lane == 0) {
+    if (tid == 0) {
       list1[rk] = i1;
       list2[rk] = i2;
       used1[i1] = 1;
@@ -341,68 +381,87 @@ __device__ void aca_task(const NcaGeomDev& g, const NcaTask& tk, const int* idx,
     if (rk != 2) prev = nS;
     nS = nS * nS + (nu * nv) * (nu * nv);
     for (int a = 0; a < rk; ++a) {
-      const double2 cu = warp_cdot(U + (size_t)a * d2, Ur, d2, lane);
-      const double2 cv = warp_cdot(V + (size_t)a * d1, Vr, d1, lane);
-      const double2 pr = make_double2(cu.x * cv.x - cu.y * cv.y, cu.x * cv.y + cu.y * cv.x);
-      nS += 2 * hypot(pr.x, pr.y);
+      // cu = sum conj(U[a]) Ur, cv = sum conj(V[a]) Vr
+      double d4[4] = {0.0, 0.0, 0.0, 0.0};
+      const double2* Ua = U + (size_t)a * d2;
+      const double2* Va = V + (size_t)a * d1;
+      for (int k = tid; k < d2; k += NT) {
+        const double x = Ua[k].x, y = Ua[k].y, c = Ur[k].x, d = Ur[k].y;
+        d4[0] += x * c + y * d;
+        d4[1] += x * d - y * c;
+      }
+      for (int k = tid; k < d1; k += NT) {
+        const double x = Va[k].x, y = Va[k].y, c = Vr[k].x, d = Vr[k].y;
+        d4[2] += x * c + y * d;
+        d4[3] += x * d - y * c;
+      }
+      block_sum<4>(d4, sh);
+      const double prr = d4[0] * d4[2] - d4[1] * d4[3], pri = d4[0] * d4[3] + d4[1] * d4[2];
+      nS += 2 * hypot(prr, pri);
     }
     nS = sqrt(nS);
-    __syncwarp();
-    i2 = warp_argmax(q, used2, d2, lane);
+    __syncthreads();
+    i2 = block_argmax(q, used2, d2, sh);
   }
-  if (lane == 0) {
+  if (tid == 0) {
     *rank_out = rk;
     *status_out = status;
   }
 }
 
-__global__ void __launch_bounds__(kNcaWarpsPerBlock * 32) nca_kernel(NcaGeomDev g, const NcaTask* __restrict__ tasks,
-                                                                    int ntasks, const int* __restrict__ idx, double eps,
-                                                                    int* next, int* piv, int* ranks, int* status,
-                                                                    double2* scratch, long long warp_scr,
-                                                                    unsigned char* flags, long long warp_flags) {
-  __shared__ double2 coef_all[kNcaWarpsPerBlock][kNcaRankCapG];
-  const int lane = threadIdx.x & 31;
-  double2* coef = coef_all[threadIdx.x >> 5];
-  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  double2* scr = scratch + w * warp_scr;
-  unsigned char* used = flags + w * warp_flags;
+template <int NT>
+__global__ void __launch_bounds__(NT) nca_kernel(NcaGeomDev g, const NcaTask* __restrict__ tasks, int ntasks,
+                                                         const int* __restrict__ idx, double eps, int* next, int* piv,
+                                                         int* ranks, int* status, double2* scratch,
+                                                         long long blk_scr, unsigned char* flags,
+                                                         long long blk_flags) {
+  __shared__ NcaShared<NT> sh;
+  double2* scr = scratch + (long long)blockIdx.x * blk_scr;
+  unsigned char* used = flags + (long long)blockIdx.x * blk_flags;
   for (int iter = 0; iter <= ntasks; ++iter) {
-    int t = 0;
-    if (lane == 0) t = atomicAdd(next, 1);
-    t = __shfl_sync(kFull, t, 0);
+    if (threadIdx.x == 0) sh.task = atomicAdd(next, 1);
+    __syncthreads();
+    const int t = sh.task;
+    __syncthreads();
     if (t >= ntasks) break;
-    aca_task(g, tasks[t], idx, eps, scr, used, piv, ranks + t, status + t, coef, lane);
-    __syncwarp();
+    aca_task<NT>(g, tasks[t], idx, eps, scr, used, piv, ranks + t, status + t, sh);
+    __syncthreads();
   }
 }
 
 template <class T>
-bool upload(T** d, const std::vector<T>& h) {
+bool upload(T** d, const std::vector<T>& h, cudaStream_t s) {
   *d = nullptr;
   if (h.empty()) return true;
-  return cudaMalloc(d, sizeof(T) * h.size()) == cudaSuccess &&
-         cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  return cudaMallocAsync(reinterpret_cast<void**>(d), sizeof(T) * h.size(), s) == cudaSuccess &&
+         cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s) == cudaSuccess;
+}
+
+template <class T>
+bool alloc(T** d, size_t n, cudaStream_t s) {
+  *d = nullptr;
+  return cudaMallocAsync(reinterpret_cast<void**>(d), sizeof(T) * std::max<size_t>(n, 1), s) == cudaSuccess;
 }
 
 }  // namespace
 
+// Device state of one assembly. Everything runs on a stream of its own with
+// stream-ordered allocations, so an assembly on a host thread overlaps GPU
+// work that other streams of the process (a solve) have in flight.
 struct GpuFar {
   int device = -1;
+  cudaStream_t stream = nullptr;
   NcaGeomDev g{};
   double2* S = nullptr;
   int *xid = nullptr, *yid = nullptr, *xrow = nullptr, *yrow = nullptr, *lcol = nullptr, *lrow = nullptr;
   double* kq = nullptr;
-  double seconds_table = 0.0;
   ~GpuFar() {
-    cudaFree(S);
-    cudaFree(xid);
-    cudaFree(yid);
-    cudaFree(xrow);
-    cudaFree(yrow);
-    cudaFree(lcol);
-    cudaFree(lrow);
-    cudaFree(kq);
+    if (stream) {
+      for (void* p : {(void*)S, (void*)xid, (void*)yid, (void*)xrow, (void*)yrow, (void*)lcol, (void*)lrow, (void*)kq})
+        if (p) cudaFreeAsync(p, stream);
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
     cudaGetLastError();
   }
 };
@@ -418,29 +477,35 @@ GpuFar* gpu_far_open(int device, const FarTables& t, cd* S_host) {
   }
   GpuFar* f = new GpuFar();
   f->device = device;
+  if (cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    f->stream = nullptr;
+    delete f;
+    return nullptr;
+  }
+  cudaStream_t s = f->stream;
   const size_t sbytes = sizeof(double2) * (size_t)nkeys * t.rank;
   double *dux = nullptr, *duy = nullptr;
   double2* dM = nullptr;
   std::vector<double2> Mh(t.M.size());
   for (size_t i = 0; i < Mh.size(); ++i) Mh[i] = make_double2(t.M[i].real(), t.M[i].imag());
   const size_t smem = sizeof(double2) * ((size_t)t.rank * kTerms + (size_t)kTableKeys * kTerms);
-  bool ok = upload(&dux, t.ux) && upload(&duy, t.uy) && upload(&dM, Mh) && cudaMalloc(&f->S, sbytes) == cudaSuccess &&
+  bool ok = upload(&dux, t.ux, s) && upload(&duy, t.uy, s) && upload(&dM, Mh, s) &&
+            alloc(&f->S, (size_t)nkeys * t.rank, s) &&
             cudaFuncSetAttribute(far_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
                 cudaSuccess;
   if (ok) {
     const long long blocks = (nkeys + kTableKeys - 1) / kTableKeys;
-    far_table_kernel<<<(unsigned)blocks, kTableKeys, smem>>>(dux, duy, (int)ny, nkeys, t.kappa, dM, t.rank, f->S);
-    ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
-  }
-  if (ok) {
+    far_table_kernel<<<(unsigned)blocks, kTableKeys, smem, s>>>(dux, duy, (int)ny, nkeys, t.kappa, dM, t.rank, f->S);
     static_assert(sizeof(cd) == sizeof(double2), "complex layout");
-    ok = cudaMemcpy(S_host, f->S, sbytes, cudaMemcpyDeviceToHost) == cudaSuccess;
+    ok = cudaGetLastError() == cudaSuccess &&
+         cudaMemcpyAsync(S_host, f->S, sbytes, cudaMemcpyDeviceToHost, s) == cudaSuccess;
   }
-  ok = ok && upload(&f->xid, t.xid) && upload(&f->yid, t.yid) && upload(&f->xrow, t.xrow) &&
-       upload(&f->yrow, t.yrow) && upload(&f->lcol, t.lcol) && upload(&f->lrow, t.lrow) && upload(&f->kq, t.kq);
-  cudaFree(dux);
-  cudaFree(duy);
-  cudaFree(dM);
+  ok = ok && upload(&f->xid, t.xid, s) && upload(&f->yid, t.yid, s) && upload(&f->xrow, t.xrow, s) &&
+       upload(&f->yrow, t.yrow, s) && upload(&f->lcol, t.lcol, s) && upload(&f->lrow, t.lrow, s) &&
+       upload(&f->kq, t.kq, s);
+  for (void* p : {(void*)dux, (void*)duy, (void*)dM})
+    if (p) cudaFreeAsync(p, s);
+  ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
   if (!ok) {
     cudaGetLastError();
     delete f;
@@ -457,55 +522,60 @@ bool gpu_far_nca(GpuFar* f, const std::vector<NcaTask>& tasks, const std::vector
     cudaGetLastError();
     return false;
   }
+  cudaStream_t s = f->stream;
   const int nt = (int)tasks.size();
-  long long warp_scr = 0, warp_flags = 0, npiv = 0;
+  long long blk_scr = 0, blk_flags = 0, npiv = 0;
   for (const NcaTask& t : tasks) {
     if (t.R < 1 || t.R > kNcaRankCapG) return false;
     const long long d = (long long)t.n1 + t.n2;
-    warp_scr = std::max(warp_scr, (long long)t.R * d + d);
-    warp_flags = std::max(warp_flags, d);
+    blk_scr = std::max(blk_scr, (long long)t.R * d + d);
+    blk_flags = std::max(blk_flags, d);
     npiv = std::max(npiv, (long long)t.out_off + 2LL * t.R);
   }
-  warp_flags = (warp_flags + 15) / 16 * 16;
-  // Warps: one per task up to the GPU's resident warps and an 8 GB scratch.
-  int sms = 0;
+  blk_flags = (blk_flags + 15) / 16 * 16;
+  // Threads per block: 128 when the level's blocks fill the GPU's CTAs of
+  // 128 at most twice (few large blocks: the latency of each matters), else
+  // 32 (many blocks: more of them in flight). CTAs: one per task up to the
+  // resident ones (CTAs beyond those would find the task counter
+  // exhausted) and an 8 GB scratch.
+  int sms = 0, per128 = 0, per32 = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, f->device);
-  long long warps = std::min<long long>(nt, (long long)std::max(sms, 1) * 48);
+  sms = std::max(sms, 1);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per128, nca_kernel<128>, 128, 0) != cudaSuccess) per128 = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per32, nca_kernel<32>, 32, 0) != cudaSuccess) per32 = 1;
+  const bool wide = nt <= 2LL * sms * std::max(per128, 1);
+  long long blocks = std::min<long long>(nt, (long long)sms * std::max(wide ? per128 : per32, 1));
   const long long budget = 8LL << 30;
-  warps = std::max(1LL, std::min(warps, budget / std::max(1LL, warp_scr * (long long)sizeof(double2))));
-  warps = (warps + kNcaWarpsPerBlock - 1) / kNcaWarpsPerBlock * kNcaWarpsPerBlock;
+  blocks = std::max(1LL, std::min(blocks, budget / std::max(1LL, blk_scr * (long long)sizeof(double2))));
   NcaTask* dt = nullptr;
   int *didx = nullptr, *dnext = nullptr, *dpiv = nullptr, *drank = nullptr, *dstat = nullptr;
   double2* dscr = nullptr;
   unsigned char* dflags = nullptr;
-  bool ok = upload(&dt, tasks) && upload(&didx, idx) && cudaMalloc(&dnext, sizeof(int)) == cudaSuccess &&
-            cudaMemset(dnext, 0, sizeof(int)) == cudaSuccess &&
-            cudaMalloc(&dpiv, sizeof(int) * (size_t)std::max(1LL, npiv)) == cudaSuccess &&
-            cudaMalloc(&drank, sizeof(int) * (size_t)nt) == cudaSuccess &&
-            cudaMalloc(&dstat, sizeof(int) * (size_t)nt) == cudaSuccess &&
-            cudaMalloc(&dscr, sizeof(double2) * (size_t)(warps * warp_scr)) == cudaSuccess &&
-            cudaMalloc(&dflags, (size_t)(warps * warp_flags)) == cudaSuccess;
+  bool ok = upload(&dt, tasks, s) && upload(&didx, idx, s) && alloc(&dnext, 1, s) &&
+            cudaMemsetAsync(dnext, 0, sizeof(int), s) == cudaSuccess && alloc(&dpiv, (size_t)npiv, s) &&
+            alloc(&drank, (size_t)nt, s) && alloc(&dstat, (size_t)nt, s) &&
+            alloc(&dscr, (size_t)(blocks * blk_scr), s) && alloc(&dflags, (size_t)(blocks * blk_flags), s);
   if (ok) {
-    nca_kernel<<<(unsigned)(warps / kNcaWarpsPerBlock), kNcaWarpsPerBlock * 32>>>(
-        f->g, dt, nt, didx, eps, dnext, dpiv, drank, dstat, dscr, warp_scr, dflags, warp_flags);
-    ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+    if (wide)
+      nca_kernel<128><<<(unsigned)blocks, 128, 0, s>>>(f->g, dt, nt, didx, eps, dnext, dpiv, drank, dstat, dscr,
+                                                       blk_scr, dflags, blk_flags);
+    else
+      nca_kernel<32><<<(unsigned)blocks, 32, 0, s>>>(f->g, dt, nt, didx, eps, dnext, dpiv, drank, dstat, dscr,
+                                                     blk_scr, dflags, blk_flags);
+    ok = cudaGetLastError() == cudaSuccess;
   }
   if (ok) {
     ranks.resize(nt);
     status.resize(nt);
     piv.resize((size_t)std::max(1LL, npiv));
-    ok = cudaMemcpy(ranks.data(), drank, sizeof(int) * nt, cudaMemcpyDeviceToHost) == cudaSuccess &&
-         cudaMemcpy(status.data(), dstat, sizeof(int) * nt, cudaMemcpyDeviceToHost) == cudaSuccess &&
-         cudaMemcpy(piv.data(), dpiv, sizeof(int) * piv.size(), cudaMemcpyDeviceToHost) == cudaSuccess;
+    ok = cudaMemcpyAsync(ranks.data(), drank, sizeof(int) * nt, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+         cudaMemcpyAsync(status.data(), dstat, sizeof(int) * nt, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+         cudaMemcpyAsync(piv.data(), dpiv, sizeof(int) * npiv, cudaMemcpyDeviceToHost, s) == cudaSuccess;
   }
-  cudaFree(dt);
-  cudaFree(didx);
-  cudaFree(dnext);
-  cudaFree(dpiv);
-  cudaFree(drank);
-  cudaFree(dstat);
-  cudaFree(dscr);
-  cudaFree(dflags);
+  for (void* p : {(void*)dt, (void*)didx, (void*)dnext, (void*)dpiv, (void*)drank, (void*)dstat, (void*)dscr,
+                  (void*)dflags})
+    if (p) cudaFreeAsync(p, s);
+  ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
   cudaGetLastError();
   return ok;
 }

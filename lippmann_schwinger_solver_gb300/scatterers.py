@@ -35,18 +35,18 @@ def scatterer_specs(n, seed, levels=(4, 5, 6), kappa_lo=10.0, kappa_hi=60.0):
     return out
 
 
-def config(level, kappa, bumps, tol_pow=10, precompute_on_gpu=0):
+def config(level, kappa, bumps, tol_pow=10, precompute_on_gpu=0, far_on_gpu=0):
     return Config(nCones_LFR=16, nChebNodes=6, yes2DFMM=1, TOL_POW=tol_pow, degreeOfBases=6, nLevelsUniform=level,
                   Qchoice=6, findPhi=1, reference_rounding=1, L=1.0, kappa=kappa, bumps=bumps,
-                  precompute_on_gpu=precompute_on_gpu)
+                  precompute_on_gpu=precompute_on_gpu, far_on_gpu=far_on_gpu)
 
 
 def solve_many(specs, angles=64, tol=1e-8, tol_pow=10, device=0, log=None, keep_solutions=False,
-               precompute_on_gpu=0):
+               precompute_on_gpu=0, far_on_gpu=0):
     """Assembles and solves every scatterer; returns per-scatterer records and
     the totals. Assembly of scatterer k + 1 overlaps the solve of k. With
-    precompute_on_gpu the precomputation quadratures run on the GPU (see
-    ls_config.precompute_on_gpu).
+    precompute_on_gpu the precomputation quadratures run on the GPU, with
+    far_on_gpu the far-field table (1) and NCA (2) (see ls_config).
     assemble_s is the operator's creation (host assembly, upload, FP32
     copy); host_stages_s splits the host assembly by stage."""
     thetas = 2 * np.pi * np.arange(angles) / angles
@@ -56,7 +56,8 @@ def solve_many(specs, angles=64, tol=1e-8, tol_pow=10, device=0, log=None, keep_
     def build(k):
         t0 = time.perf_counter()
         try:
-            op = Operator(config(*specs[k], tol_pow=tol_pow, precompute_on_gpu=precompute_on_gpu), device=device)
+            op = Operator(config(*specs[k], tol_pow=tol_pow, precompute_on_gpu=precompute_on_gpu,
+                                 far_on_gpu=far_on_gpu), device=device)
             op.enable_f32()
             ready[k] = (op, time.perf_counter() - t0, None)
         except Exception as e:  # reported with the scatterer, not raised from the thread
@@ -109,9 +110,12 @@ def main(argv=None):
     ap.add_argument("--tol-pow", type=int, default=10)
     ap.add_argument("--levels", default="4,5,6")
     ap.add_argument("--gpu-precompute", action="store_true", help="precomputation quadratures on the GPU")
+    ap.add_argument("--gpu-far", type=int, default=0, choices=[0, 1, 2],
+                    help="far-field table (1) and NCA skeleton search (2) on the GPU")
     a = ap.parse_args(argv)
     specs = scatterer_specs(a.n, a.seed, levels=tuple(int(v) for v in a.levels.split(",")))
-    _, total, _ = solve_many(specs, a.angles, a.tol, a.tol_pow, log=print, precompute_on_gpu=int(a.gpu_precompute))
+    _, total, _ = solve_many(specs, a.angles, a.tol, a.tol_pow, log=print, precompute_on_gpu=int(a.gpu_precompute),
+                             far_on_gpu=a.gpu_far)
     print(json.dumps(total))
 
 
