@@ -100,9 +100,11 @@ typedef struct {
    * 2: as 1, and the NCA skeleton search of every box runs on the GPU as
    * well (one warp per box; the host redoes any box whose rank passes the
    * GPU's capacity).
-   * GPU values differ from the host's in the last bits, which can move an
-   * NCA pivot among near-equal candidates; the matvec stays within the NCA
-   * tolerance of the host-assembled operator's. Adaptive trees ignore it. */
+   * GPU values differ from the host's in the last bits, which moves NCA
+   * pivots among candidates equal in magnitude up to such bits (mirror-image
+   * positions of a uniform tree): the skeletons are other valid choices, and
+   * the matvec moves by less than the host-assembled operator itself moves
+   * when the NCA tolerance is tightened tenfold. Adaptive trees ignore it. */
   int far_on_gpu;
 } ls_config;
 
