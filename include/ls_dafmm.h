@@ -98,8 +98,8 @@ typedef struct {
    * on the operator's GPU (on the host cores when it has no device) and the
    * host's NCA and block fills read them from that table;
    * 2: as 1, and the NCA skeleton search of every box runs on the GPU as
-   * well (one warp per box; the host redoes any box whose rank passes the
-   * GPU's capacity).
+   * well (one thread block per box and direction; the host redoes any box
+   * whose rank passes the GPU's capacity).
    * GPU values differ from the host's in the last bits, which moves NCA
    * pivots among candidates equal in magnitude up to such bits (mirror-image
    * positions of a uniform tree): the skeletons are other valid choices, and
@@ -153,6 +153,12 @@ ls_status ls_op_points(const ls_op* op, double* xy);
 ls_status ls_op_contrast(const ls_op* op, double* q);
 /* b_i = -kappa^2 q(x_i) exp(i kappa x_i1); userkernel::RHSFunction (GMRES/GMRES.cpp:122-125). */
 ls_status ls_op_rhs(const ls_op* op, double* b);
+/* Right-hand sides of n incidence directions: column t of b (N x n complex,
+ * column major) is -kappa^2 q(x_i) exp(i kappa (x_i1 cos th_t + x_i2 sin th_t)),
+ * the reference's RHSFunction (GMRES/GMRES.cpp:122-125) turned by th_t
+ * (th_t = 0 gives ls_op_rhs bit for bit). Host threads; the many-direction
+ * workload forms its right-hand sides with it. */
+ls_status ls_op_rhs_angles(const ls_op* op, const double* thetas, int n, double* b);
 
 /*
  * y = A x on the device. x and y are device pointers to N complex values

@@ -42,7 +42,7 @@ LS_INNER_BASIS_F32 = 1
 
 # Every symbol declared in include/ls_dafmm.h.
 EXPORTED_SYMBOLS = (
-    "ls_op_create", "ls_op_destroy", "ls_op_info", "ls_op_points", "ls_op_contrast", "ls_op_rhs",
+    "ls_op_create", "ls_op_destroy", "ls_op_info", "ls_op_points", "ls_op_contrast", "ls_op_rhs", "ls_op_rhs_angles",
     "ls_matvec", "ls_matvec_f32", "ls_op_enable_f32", "ls_matvec_host", "ls_gmres", "ls_gmres_restarted",
     "ls_gmres_mixed", "ls_time_matvec", "ls_op_skeleton_dump", "ls_op_precomputations", "ls_last_error",
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
@@ -228,6 +228,7 @@ def lib():
         L.ls_op_info.argtypes = [vp, ctypes.POINTER(_Info)]
         for n in ("ls_op_points", "ls_op_contrast", "ls_op_rhs"):
             getattr(L, n).argtypes = [vp, dp]
+        L.ls_op_rhs_angles.argtypes = [vp, dp, ctypes.c_int, dp]
         for n in ("ls_matvec", "ls_matvec_f32", "ls_matvec_noalloc"):
             getattr(L, n).argtypes = [vp, vp, vp, vp]
         L.ls_op_enable_f32.argtypes = [vp]
@@ -505,13 +506,12 @@ class Operator:
 
     def rhs_angles(self, thetas):
         """Right-hand sides -kappa^2 q exp(i kappa (x cos t + y sin t)) for the
-        incidence directions t (GMRES/GMRES.cpp:119-126 for t = 0), N x len(t)."""
-        xy = self.points()
-        q = self.contrast()
-        k = self.cfg.kappa
-        t = np.asarray(thetas, dtype=float)
-        phase = np.outer(xy[:, 0], np.cos(t)) + np.outer(xy[:, 1], np.sin(t))
-        return np.asfortranarray(-(k * k) * q[:, None] * np.exp(1j * k * phase))
+        incidence directions t (GMRES/GMRES.cpp:119-126 for t = 0), N x len(t),
+        formed by ls_op_rhs_angles on the host threads."""
+        t = np.ascontiguousarray(np.asarray(thetas, dtype=float).ravel())
+        B = np.empty((self.N, len(t)), dtype=np.complex128, order="F")
+        _check(lib().ls_op_rhs_angles(self._h, _dp(t), len(t), _dp(B)), "ls_op_rhs_angles")
+        return B
 
     def time_matvec(self, warmup=3, iters=20, precision=LS_PREC_F64):
         a, b = ctypes.c_float(), ctypes.c_float()

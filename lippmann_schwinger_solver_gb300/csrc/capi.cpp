@@ -224,6 +224,25 @@ ls_status ls_op_rhs(const ls_op* op, double* b) {
   return LS_OK;
 }
 
+ls_status ls_op_rhs_angles(const ls_op* op, const double* thetas, int n, double* b) {
+  if (!op || !thetas || !b) return fail(LS_E_INVALID, "ls_op_rhs_angles: null argument");
+  if (n < 1) return fail(LS_E_INVALID, "ls_op_rhs_angles: n must be >= 1");
+  const HostOperator& h = op->host;
+  const double k = h.cfg.kappa;
+  const long long N = h.N;
+#pragma omp parallel for schedule(static)
+  for (long long u = 0; u < N * n; ++u) {
+    const int t = (int)(u / N);
+    const long long i = u - (long long)t * N;
+    const double phase = h.px[i] * std::cos(thetas[t]) + h.py[i] * std::sin(thetas[t]);
+    const cd inc = std::exp(cd(0.0, k * phase));
+    const cd v = -1.0 * k * k * h.q[i] * inc;
+    b[2 * u] = v.real();
+    b[2 * u + 1] = v.imag();
+  }
+  return LS_OK;
+}
+
 ls_status ls_matvec(ls_op* op, const double* x, double* y, void* stream) {
   if (!op || !x || !y) return fail(LS_E_INVALID, "ls_matvec: null argument");
   if (!op->on_device) return fail(LS_E_STATE, "ls_matvec: operator was assembled without a device");

@@ -166,3 +166,24 @@ def test_noalloc_rejects_operators_larger_than_its_static_array(ls):
     assert ls.lib().ls_matvec_noalloc(small._h, ctypes.c_void_p(16), ctypes.c_void_p(16), None) == ls.LS_E_STATE
     op.close()
     small.close()
+
+
+def test_rhs_angles_is_the_turned_reference_rhs(ls):
+    """ls_op_rhs_angles: column t is -kappa^2 q exp(i kappa (x cos t + y sin t))
+    (GMRES/GMRES.cpp:122-125 turned by t), the t = 0 column is ls_op_rhs bit
+    for bit, and bad arguments are rejected."""
+    op = ls.Operator(full_cfg(CFG_L3_K10), device=-1)
+    th = np.array([0.0, 0.7, np.pi, 5.9])
+    B = op.rhs_angles(th)
+    assert B.shape == (op.N, 4) and B.flags["F_CONTIGUOUS"]
+    assert np.array_equal(B[:, 0], op.rhs())
+    xy, q, k = op.points(), op.contrast(), op.cfg.kappa
+    ref = -(k * k) * q[:, None] * np.exp(1j * k * (np.outer(xy[:, 0], np.cos(th)) + np.outer(xy[:, 1], np.sin(th))))
+    assert np.max(np.abs(B - ref)) <= 1e-14 * np.max(np.abs(ref))
+    L = ls.lib()
+    out = np.empty(2 * op.N)
+    t0 = np.zeros(1)
+    assert L.ls_op_rhs_angles(op._h, None, 1, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == ls.LS_E_INVALID
+    assert L.ls_op_rhs_angles(op._h, t0.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 0,
+                              out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == ls.LS_E_INVALID
+    op.close()
