@@ -1579,7 +1579,7 @@ static void finalize(GemvPhase& ph, const char* kind) {
     }
   }
   ph.blk_tile0.push_back((int)tl.size());
-  ph.A.assign((size_t)total, cd(0.0, 0.0));
+  ph.A.resize((size_t)total);  // uninitialised: each tile zeroes and fills its own range below
   ph.idx.assign((size_t)total_idx, 0);
   ph.out.assign(ph.rows.size(), 0);
   ph.klen.assign(tl.size() * kTileLanes, 0);
@@ -1592,6 +1592,7 @@ static void finalize(GemvPhase& ph, const char* kind) {
     int log2s = 0;
     while ((1 << log2s) < d.S) ++log2s;
     const GemvPhase::Row& first = ph.rows[d.r0];
+    std::fill(ph.A.begin() + d.off, ph.A.begin() + d.off + (long long)d.qmax * kTileLanes, cplx{0.0, 0.0});
     for (int q = 0; q < d.qmax; ++q)
       for (int sl = 0; sl < d.S; ++sl) {
         const int k = q * d.S + sl;
@@ -1604,7 +1605,7 @@ static void finalize(GemvPhase& ph, const char* kind) {
         const int lane = sl * R + r;
         int q = 0;
         for (int k = sl; k < row.K; k += d.S, ++q)
-          ph.A[(size_t)(d.off + (long long)q * kTileLanes + lane)] = row.a[k];
+          ph.A[(size_t)(d.off + (long long)q * kTileLanes + lane)] = cplx{row.a[k].real(), row.a[k].imag()};
         ph.klen[t * kTileLanes + lane] = q;
       }
     }

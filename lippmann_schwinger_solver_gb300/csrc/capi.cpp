@@ -129,7 +129,7 @@ ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
   }
   // Host copies of the tiles are no longer needed.
   auto drop = [](GemvPhase& p) {
-    std::vector<cd>().swap(p.A);
+    PackedBlocks().swap(p.A);
     std::vector<int>().swap(p.idx);
   };
   for (auto& p : op->host.up) drop(p);

@@ -3,8 +3,12 @@
 #pragma once
 
 #include <complex>
+#include <cstddef>
 #include <cstdint>
+#include <memory>
+#include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/ls_dafmm.h"
@@ -12,6 +16,40 @@
 namespace lsg {
 
 using cd = std::complex<double>;
+
+// A complex double as two plain doubles, and a vector of them whose
+// elements are left uninitialised on resize: the packed operator (hundreds
+// of MB) is then first touched by the threads that fill it, in parallel,
+// instead of zeroed by one thread (std::complex always zero-initialises).
+struct cplx {
+  double re, im;
+};
+template <class T>
+struct NoInitAllocator {
+  using value_type = T;
+  NoInitAllocator() = default;
+  template <class U>
+  NoInitAllocator(const NoInitAllocator<U>&) noexcept {}
+  T* allocate(size_t n) { return std::allocator<T>().allocate(n); }
+  void deallocate(T* p, size_t n) noexcept { std::allocator<T>().deallocate(p, n); }
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new (static_cast<void*>(p)) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+  }
+  template <class U>
+  bool operator==(const NoInitAllocator<U>&) const noexcept {
+    return true;
+  }
+  template <class U>
+  bool operator!=(const NoInitAllocator<U>&) const noexcept {
+    return false;
+  }
+};
+using PackedBlocks = std::vector<cplx, NoInitAllocator<cplx>>;
 
 // One warp tile of a gather-GEMV phase: R = 32 / S rows of one block, each
 // split into S interleaved column slices, so lane l = s * R + r sums the
@@ -36,7 +74,7 @@ constexpr int kTileLanes = 32;
 
 // A phase (or one tree level of a phase) in device-ready form.
 struct GemvPhase {
-  std::vector<cd> A;            // tiles, column interleaved (zero padded)
+  PackedBlocks A;               // tiles, column interleaved (zero padded)
   std::vector<int> idx;         // gather indices, one per tile, step and slice
   std::vector<int> out;         // output element of each row
   std::vector<int> klen;        // steps of each lane (32 per tile)

@@ -56,7 +56,8 @@ bool run_phase(const GemvPhase& ph, const std::vector<cd>& src, std::vector<cd>&
         const int i = ph.idx[T.i_off + (long long)S * q + sl];
         if (i < 0 || i >= (long long)src.size()) return fail(name, "gather index", (long long)t, i);
         read[i] = 1;
-        s += ph.A[T.a_off + (long long)L * q + lane] * src[i];
+        const lsg::cplx a = ph.A[T.a_off + (long long)L * q + lane];
+        s += cd(a.re, a.im) * src[i];
       }
       lane_sum[lane] = s;
     }
