@@ -356,6 +356,25 @@ int ls_get_pdl(void);
 ls_status ls_set_near_overlap(int on);
 int ls_get_near_overlap(void);
 
+/*
+ * Cache of the assembly's precomputations (the far moments M of a leaf size
+ * and the near-field blocks), replacing the reference's text files
+ * (writeMToFile / writeNeighborInteractionsForLevel and their readers,
+ * G_FMM2DTree.hpp:1264-1270, 1868-1950), which hold the values at 6
+ * significant digits and are recomputed on every run. A record holds the
+ * exact values an assembly computed and is keyed on every input they depend
+ * on (kappa, the leaf radii and neighbour offsets, nChebNodes,
+ * degreeOfBases, reference_rounding, host or GPU integration), so an
+ * assembly that reads it is the same bit for bit. dir NULL: off (the
+ * default); "": records kept in memory for the process; a directory: also
+ * stored there as binary files (one per record, shared between processes;
+ * a file that does not match its key is ignored). Process-wide; setting it
+ * drops the records held in memory. ls_precompute_cache_stats: records
+ * found and not found since the process started.
+ */
+ls_status ls_set_precompute_cache(const char* dir);
+ls_status ls_precompute_cache_stats(long long* hits, long long* misses);
+
 const char* ls_last_error(void);
 const char* ls_version(void);
 

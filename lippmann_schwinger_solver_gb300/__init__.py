@@ -48,7 +48,8 @@ EXPORTED_SYMBOLS = (
     "ls_version", "ls_matvec_noalloc", "ls_op_set_f64_kernels", "ls_gmres_mixed_batched", "ls_op_interpolate",
     "ls_write_result", "ls_set_pdl", "ls_get_pdl", "ls_time_matvec_phases", "ls_measure_fma_peak", "ls_op_set_inner_basis",
     "ls_op_set_batch_width", "ls_matvec_f32_many", "ls_time_block_apply", "ls_op_tc_stages", "ls_measure_mma_issue",
-    "ls_tc_wait_probe", "ls_set_near_overlap", "ls_get_near_overlap",
+    "ls_tc_wait_probe", "ls_set_near_overlap", "ls_get_near_overlap", "ls_set_precompute_cache",
+    "ls_precompute_cache_stats",
 )
 # Every symbol declared in include/ls_fno.h (learned preconditioner).
 FNO_SYMBOLS = (
@@ -260,6 +261,8 @@ def lib():
         L.ls_tc_wait_probe.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int)]
         L.ls_get_pdl.argtypes = []
         L.ls_set_near_overlap.argtypes = [ctypes.c_int]
+        L.ls_set_precompute_cache.argtypes = [ctypes.c_char_p]
+        L.ls_precompute_cache_stats.argtypes = [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
         L.ls_get_near_overlap.argtypes = []
         fp = ctypes.POINTER(ctypes.c_float)
         L.ls_fno_create.argtypes = [ctypes.POINTER(_FnoConfig), ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
@@ -313,6 +316,19 @@ def set_near_overlap(on):
     """Run the native FP64 matvec's near field beside its far-field chain
     (1, the default) or after it (0) (ls_set_near_overlap); bitwise identical."""
     lib().ls_set_near_overlap(1 if on else 0)
+
+
+def set_precompute_cache(dir):
+    """Cache of the assembly's precomputations (ls_set_precompute_cache):
+    None off, "" in memory, a directory path also as binary files there."""
+    lib().ls_set_precompute_cache(None if dir is None else os.fsencode(dir))
+
+
+def precompute_cache_stats():
+    """(hits, misses) of the precomputation cache since the process started."""
+    h, m = ctypes.c_longlong(), ctypes.c_longlong()
+    _check(lib().ls_precompute_cache_stats(ctypes.byref(h), ctypes.byref(m)), "ls_precompute_cache_stats")
+    return h.value, m.value
 
 
 def get_near_overlap():

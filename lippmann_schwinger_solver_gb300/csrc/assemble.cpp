@@ -34,6 +34,7 @@
 #include <memory>
 #include <mutex>
 #include <set>
+#include <thread>
 #include <tuple>
 #include <unordered_map>
 #include <vector>
@@ -199,6 +200,135 @@ thread_local int t_assembly_device = -1;
 // Device for the precomputation quadratures of an assembly with cfg: its GPU
 // when cfg asks for it (and there is one), else none.
 int quadrature_device(const ls_config& cfg) { return cfg.precompute_on_gpu ? t_assembly_device : -1; }
+
+// ---------------------------------------------------------------- precomputation cache
+// The reference writes M and the near blocks to text files at 6 digits and
+// reads them back (writeMToFile / writeNeighborInteractionsForLevel,
+// G_FMM2DTree.hpp:1264-1270, 1868-1950), recomputing them on every run.
+// Here a record holds the exact values an assembly computed, keyed on every
+// input they depend on (the kind of record, kappa, radii and offsets as
+// bits, Chebyshev nodes, basis degree, rounding, host or GPU integration),
+// so an assembly that reads one is the same bit for bit. Files: "LSPC",
+// format version, key length and bytes, value count, values (native
+// doubles); written to a temporary name and renamed, checked key for key
+// on reading (a file that does not match is a miss).
+class PrecomputeCache {
+ public:
+  void set(const char* dir) {
+    std::lock_guard<std::mutex> lk(mu_);
+    on_ = dir != nullptr;
+    dir_ = dir ? dir : "";
+    mem_.clear();
+  }
+  bool enabled() {
+    std::lock_guard<std::mutex> lk(mu_);
+    return on_;
+  }
+  bool get(const std::string& key, std::vector<cd>& out) {
+    std::string dir;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!on_) return false;
+      auto it = mem_.find(key);
+      if (it != mem_.end()) {
+        out = it->second;
+        ++hits_;
+        return true;
+      }
+      dir = dir_;
+    }
+    if (!dir.empty() && read_file(dir, key, out)) {
+      std::lock_guard<std::mutex> lk(mu_);
+      mem_[key] = out;
+      ++hits_;
+      return true;
+    }
+    std::lock_guard<std::mutex> lk(mu_);
+    ++misses_;
+    return false;
+  }
+  void put(const std::string& key, const std::vector<cd>& v) {
+    std::string dir;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!on_) return;
+      mem_[key] = v;
+      dir = dir_;
+    }
+    if (!dir.empty()) write_file(dir, key, v);
+  }
+  void stats(long long& h, long long& m) {
+    std::lock_guard<std::mutex> lk(mu_);
+    h = hits_;
+    m = misses_;
+  }
+
+ private:
+  static constexpr uint32_t kVersion = 1;
+  static std::string path(const std::string& dir, const std::string& key) {
+    uint64_t h = 1469598103934665603ULL;  // FNV-1a
+    for (unsigned char c : key) h = (h ^ c) * 1099511628211ULL;
+    char name[40];
+    std::snprintf(name, sizeof(name), "/%016llx.lspc", (unsigned long long)h);
+    return dir + name;
+  }
+  static bool read_file(const std::string& dir, const std::string& key, std::vector<cd>& out) {
+    FILE* f = std::fopen(path(dir, key).c_str(), "rb");
+    if (!f) return false;
+    char magic[4];
+    uint32_t ver = 0;
+    uint64_t klen = 0, n = 0;
+    bool ok = std::fread(magic, 1, 4, f) == 4 && std::memcmp(magic, "LSPC", 4) == 0 &&
+              std::fread(&ver, sizeof(ver), 1, f) == 1 && ver == kVersion && std::fread(&klen, sizeof(klen), 1, f) == 1 &&
+              klen == key.size();
+    std::string k;
+    if (ok) {
+      k.resize(klen);
+      ok = std::fread(&k[0], 1, klen, f) == klen && k == key && std::fread(&n, sizeof(n), 1, f) == 1 &&
+           n <= (uint64_t(1) << 32);
+    }
+    if (ok) {
+      std::vector<cd> v((size_t)n);
+      ok = std::fread(v.data(), sizeof(cd), (size_t)n, f) == n && std::fgetc(f) == EOF;
+      if (ok) out.swap(v);
+    }
+    std::fclose(f);
+    return ok;
+  }
+  static void write_file(const std::string& dir, const std::string& key, const std::vector<cd>& v) {
+    const std::string final_path = path(dir, key);
+    char suffix[64];
+    std::snprintf(suffix, sizeof(suffix), ".tmp%llu", (unsigned long long)std::hash<std::thread::id>()(
+                                                          std::this_thread::get_id()));
+    const std::string tmp = final_path + suffix;
+    FILE* f = std::fopen(tmp.c_str(), "wb");
+    if (!f) return;
+    const uint32_t ver = kVersion;
+    const uint64_t klen = key.size(), n = v.size();
+    const bool ok = std::fwrite("LSPC", 1, 4, f) == 4 && std::fwrite(&ver, sizeof(ver), 1, f) == 1 &&
+                    std::fwrite(&klen, sizeof(klen), 1, f) == 1 && std::fwrite(key.data(), 1, klen, f) == klen &&
+                    std::fwrite(&n, sizeof(n), 1, f) == 1 && std::fwrite(v.data(), sizeof(cd), n, f) == n;
+    if (std::fclose(f) == 0 && ok)
+      std::rename(tmp.c_str(), final_path.c_str());
+    else
+      std::remove(tmp.c_str());
+  }
+  std::mutex mu_;
+  bool on_ = false;
+  std::string dir_;
+  std::map<std::string, std::vector<cd>> mem_;
+  long long hits_ = 0, misses_ = 0;
+};
+PrecomputeCache g_pcache;
+
+// Key of a precomputation record: its kind, then doubles (as bits) and ints.
+std::string pc_key(const char* kind, std::initializer_list<double> ds, std::initializer_list<int> is) {
+  std::string k(kind);
+  k.push_back('\0');
+  for (double d : ds) k.append(reinterpret_cast<const char*>(&d), sizeof(double));
+  for (int i : is) k.append(reinterpret_cast<const char*>(&i), sizeof(int));
+  return k;
+}
 // Largest far-field sum table tabulated for far_on_gpu (host and device copies).
 constexpr size_t kFarTableMaxBytes = size_t(4) << 30;
 // Rank capacity of a GPU NCA block (its scratch holds this many pivot
@@ -1028,6 +1158,23 @@ void Builder::precompute() {
   }
   const int nS = 2 * kSeries + 1;
   const double rj = radius[nL];
+  // A cached record of this leaf size: M, then the near blocks, their
+  // factors and rounding residuals.
+  const size_t nM = (size_t)nS * rank, nB = (size_t)9 * rank * rank, nV = (size_t)9 * rank * nb;
+  auto key = [&](int gpu) {
+    return pc_key("uniform-leaf", {kappa, rj}, {cfg.nChebNodes, cfg.degreeOfBases, cfg.reference_rounding, gpu, kSeries});
+  };
+  {
+    std::vector<cd> rec;
+    if (g_pcache.get(key(quadrature_device(cfg) >= 0), rec) && rec.size() == nM + 2 * nB + nV) {
+      Mleaf.assign(rec.begin(), rec.begin() + nM);
+      near.assign(rec.begin() + nM, rec.begin() + nM + nB);
+      nearVt.assign(rec.begin() + nM + nB, rec.begin() + nM + nB + nV);
+      nearE.assign(rec.begin() + nM + nB + nV, rec.end());
+      Qpinv = Qp;
+      return;
+    }
+  }
   static const double ncx[9] = {-2, 0, 2, 2, 2, 0, -2, -2, 0};
   static const double ncy[9] = {-2, -2, -2, 0, 2, 2, 2, 0, 0};
   const double rA = radius[nL], rB = radius[nL];
@@ -1140,6 +1287,15 @@ void Builder::precompute() {
         nearE[((size_t)q * rank + i) * rank + c] = s - exact;
       }
     }
+  if (g_pcache.enabled()) {
+    std::vector<cd> rec;
+    rec.reserve(nM + 2 * nB + nV);
+    rec.insert(rec.end(), Mleaf.begin(), Mleaf.end());
+    rec.insert(rec.end(), near.begin(), near.end());
+    rec.insert(rec.end(), nearVt.begin(), nearVt.end());
+    rec.insert(rec.end(), nearE.begin(), nearE.end());
+    g_pcache.put(key(on_gpu ? 1 : 0), rec);
+  }
 }
 
 // Interaction lists of the children of every box (assign_Child_Interaction,
@@ -1987,6 +2143,9 @@ bool assemble(const ls_config& cfg, HostOperator& op, std::string& err) {
 double contrast_at(const ls_config& cfg, double x, double y) { return contrast_fn(cfg, x, y); }
 
 void set_assembly_device(int device) { t_assembly_device = device; }
+
+void precompute_cache_set(const char* dir) { g_pcache.set(dir); }
+void precompute_cache_stats(long long& hits, long long& misses) { g_pcache.stats(hits, misses); }
 
 // The GPU quadrature (csrc/quadrature.cu) replaces this stub in the library;
 // a host-only build keeps it and integrates on the host.

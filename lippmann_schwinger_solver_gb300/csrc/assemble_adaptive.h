@@ -582,7 +582,10 @@ class AdaptiveBuilder {
     if (dev < 0) return false;
     const int nS = 2 * kSeries + 1;
     std::vector<QuadTask> tasks;
+    std::vector<int> levels;
     for (int j : leaf_levels)
+      if (!Mlev.count(j)) levels.push_back(j);
+    for (int j : levels)
       for (int t = 0; t < nS * nb; ++t)
         tasks.push_back({0.0, 0.0, kappa * radius[j], bases[t % nb].first, bases[t % nb].second, t / nb - kSeries, 1});
     std::vector<std::pair<double, double>> tab[4] = {offsets(0), offsets(1), offsets(2), offsets(3)};
@@ -595,7 +598,7 @@ class AdaptiveBuilder {
         for (int t = 0; t < kNbrCount[kind]; ++t) {
           if (B.nbr[kind][t] < 0) continue;
           const auto key = std::make_tuple(lf.first, kind, t);
-          if (!seen.insert(key).second) continue;
+          if (nearBlk.count(key) || !seen.insert(key).second) continue;
           const double rA = radius[lf.first], rB = radius[lf.first + kNbrLevel[kind]];
           const double cx = tab[kind][t].first * rA, cy = tab[kind][t].second * rA;
           keys.push_back({key, rB});
@@ -606,9 +609,10 @@ class AdaptiveBuilder {
         }
     }
     std::vector<cd> qv;
+    if (tasks.empty()) return true;
     if (!gpu_quadrature(dev, tasks, gln, glw, qv)) return false;
     size_t o = 0;
-    for (int j : leaf_levels) {
+    for (int j : levels) {
       const double rj = radius[j];
       std::vector<cd> C((size_t)nS * nb);
       for (int t = 0; t < nS * nb; ++t) C[t] = rj * rj * qv[o + t];
@@ -621,6 +625,59 @@ class AdaptiveBuilder {
       nearBlk[k.key] = finish_near(k.rB, V);
     }
     return true;
+  }
+  // Precomputation-cache keys of a leaf level's far moments and of a near
+  // block (level, kind, slot), for host (gpu 0) or GPU (1) integration.
+  std::string m_key(int j, int gpu) const {
+    return pc_key("adaptive-M", {kappa, radius[j]}, {n1, cfg.degreeOfBases, cfg.reference_rounding, gpu, kSeries});
+  }
+  std::string near_key(const std::tuple<int, int, int>& key, const std::vector<std::pair<double, double>>* tab,
+                       int gpu) const {
+    const int j = std::get<0>(key), kind = std::get<1>(key), t = std::get<2>(key);
+    const double rA = radius[j], rB = radius[j + kNbrLevel[kind]];
+    return pc_key("adaptive-near", {kappa, rA, rB, tab[kind][t].first * rA, tab[kind][t].second * rA},
+                  {n1, cfg.degreeOfBases, cfg.reference_rounding, gpu});
+  }
+  // The leaf levels' moments and the near blocks the leaves use: read from
+  // the precomputation cache what it holds, integrate the rest (on the GPU
+  // when so configured, else on the host), and store what was integrated.
+  void precomputations(const std::set<int>& leaf_levels) {
+    std::vector<std::pair<double, double>> tab[4] = {offsets(0), offsets(1), offsets(2), offsets(3)};
+    std::set<std::tuple<int, int, int>> used;
+    for (const Ref& lf : leaves) {
+      const ABox& B = box(lf);
+      for (int kind = 0; kind < 4; ++kind)
+        for (int t = 0; t < kNbrCount[kind]; ++t)
+          if (B.nbr[kind][t] >= 0) used.insert(std::make_tuple(lf.first, kind, t));
+    }
+    const int want_gpu = quadrature_device(cfg) >= 0 ? 1 : 0;
+    std::set<int> cached_m;
+    std::set<std::tuple<int, int, int>> cached_near;
+    if (g_pcache.enabled()) {
+      std::vector<cd> rec;
+      for (int j : leaf_levels)
+        if (g_pcache.get(m_key(j, want_gpu), rec) && rec.size() == (size_t)(2 * kSeries + 1) * rank) {
+          Mlev[j] = rec;
+          cached_m.insert(j);
+        }
+      for (const auto& key : used)
+        if (g_pcache.get(near_key(key, tab, want_gpu), rec) && rec.size() == (size_t)rank * rank) {
+          nearBlk[key] = rec;
+          cached_near.insert(key);
+        }
+    }
+    const bool gpu = precompute_on_gpu(leaf_levels);
+    if (!gpu) {
+      for (int j : leaf_levels)
+        if (!Mlev.count(j)) precompute_M(j);
+      precompute_near();
+    }
+    if (g_pcache.enabled()) {
+      for (int j : leaf_levels)
+        if (!cached_m.count(j)) g_pcache.put(m_key(j, gpu ? 1 : 0), Mlev.at(j));
+      for (const auto& key : used)
+        if (!cached_near.count(key)) g_pcache.put(near_key(key, tab, gpu ? 1 : 0), nearBlk.at(key));
+    }
   }
   void precompute_near() {
     std::vector<std::pair<double, double>> tab[4] = {offsets(0), offsets(1), offsets(2), offsets(3)};
@@ -1070,10 +1127,7 @@ bool AdaptiveBuilder::run(HostOperator& op, std::string& err) {
   for (const Ref& lf : leaves) leaf_levels.insert(lf.first);
   classify_neighbors();
   if (unmatched) { err = "adaptive tree: " + std::to_string(unmatched) + " near neighbours of unexpected level or offset"; return false; }
-  if (!precompute_on_gpu(leaf_levels)) {
-    for (int j : leaf_levels) precompute_M(j);
-    precompute_near();
-  }
+  precomputations(leaf_levels);
   op.stage_seconds[1] = lap();
   op.stage_seconds[2] = lap();
   nca();

@@ -915,6 +915,17 @@ ls_status ls_set_near_overlap(int on) {
 }
 int ls_get_near_overlap(void) { return near_overlap_enabled(); }
 
+ls_status ls_set_precompute_cache(const char* dir) {
+  precompute_cache_set(dir);
+  return LS_OK;
+}
+
+ls_status ls_precompute_cache_stats(long long* hits, long long* misses) {
+  if (!hits || !misses) return fail(LS_E_INVALID, "ls_precompute_cache_stats: null argument");
+  precompute_cache_stats(*hits, *misses);
+  return LS_OK;
+}
+
 const char* ls_last_error(void) { return t_last_error.c_str(); }
 const char* ls_version(void) { return "lsdafmm-gb300 0.1 (sm_103a)"; }
 

@@ -180,7 +180,13 @@ bool gpu_far_nca(GpuFar* f, const std::vector<NcaTask>& tasks, const std::vector
                  std::vector<int>& ranks, std::vector<int>& piv, std::vector<int>& status);
 void gpu_far_close(GpuFar* f);
 
-// assemble.cpp
+// assemble.cpp. Process-wide cache of precomputation records (far
+// moments, near blocks), keyed on every input they depend on: dir nullptr
+// turns it off (the default), "" keeps records in memory, a path also
+// stores them as binary files there (shared between processes).
+void precompute_cache_set(const char* dir);
+void precompute_cache_stats(long long& hits, long long& misses);
+
 bool assemble(const ls_config& cfg, HostOperator& op, std::string& err);
 // The GPU that the calling thread's assemblies may use for their
 // precomputation quadratures and far field (-1: none), set by ls_op_create

@@ -76,3 +76,26 @@ def test_gpu_precomputations_of_the_adaptive_readme_tree(ls, ora):
     a.close()
     gpu.close()
     host.close()
+
+
+def test_gpu_precomputations_through_the_cache(ls):
+    """With the precomputation cache on, a second GPU-integrated assembly of
+    the same tree reads the GPU's records (bit-equal operator), and a
+    host-integrated assembly does not take them (its own key)."""
+    ls.set_precompute_cache("")
+    try:
+        h0, m0 = ls.precompute_cache_stats()
+        a = ls.Operator(full_cfg(CFG_C1, precompute_on_gpu=1), device=0)
+        b = ls.Operator(full_cfg(CFG_C1, precompute_on_gpu=1), device=0)
+        h1, m1 = ls.precompute_cache_stats()
+        assert (h1 - h0, m1 - m0) == (1, 1)
+        Ma, Ba = a.precomputations()
+        Mb, Bb = b.precomputations()
+        assert np.array_equal(Ma, Mb) and np.array_equal(Ba, Bb)
+        assert np.array_equal(a.skeleton_dump(), b.skeleton_dump())
+        c = ls.Operator(full_cfg(CFG_C1), device=0)
+        assert ls.precompute_cache_stats()[1] == m1 + 1
+        for op in (a, b, c):
+            op.close()
+    finally:
+        ls.set_precompute_cache(None)
