@@ -603,6 +603,10 @@ def run_ours(args):
         many_f["host_stages_s"] = {k: round(sum(r["host_stages_s"][k] for r in recs_f), 2)
                                    for k in recs_f[0]["host_stages_s"]}
         many["gpu_precompute_and_far"] = many_f
+        # The same, two scatterers assembled and two solved at a time.
+        _, many_w, _ = scat.solve_many(specs, args.angles, 1e-8, 10, device=local, precompute_on_gpu=1,
+                                       far_on_gpu=2, workers=2)
+        many["gpu_precompute_and_far_2_workers"] = many_w
     far_gpu = None
     if rank == 0 and not args.no_gpu_assembly:
         far_gpu = gpu_assembly_leg(ls, cfg, x, y_main, op.skeleton_dump(), local)

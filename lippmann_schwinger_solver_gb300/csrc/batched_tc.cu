@@ -1260,9 +1260,9 @@ bool dev_enable_tc(DevOperator& d, const HostOperator& h, std::string& err) {
   for (auto& p : T->up) npad = std::max(npad, p.npad_max);
   for (auto& p : T->down) npad = std::max(npad, p.npad_max);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_for(npad));
+    e = raise_smem_limit((const void*)tc_gemm_kernel, smem_for(npad));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(tc_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ws_smem_for(npad));
+    e = raise_smem_limit((const void*)tc_ws_kernel, ws_smem_for(npad));
   if (e != cudaSuccess) {
     if (err.empty()) err = std::string("tensor-core form: ") + cudaGetErrorString(e);
     for (void* p : T->owned) cudaFree(p);

@@ -2,14 +2,18 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/ls_fno.h"
@@ -59,6 +63,18 @@ int pdl_enabled() {
   return v;
 }
 void set_pdl_enabled(int on) { g_pdl.store(on ? 1 : 0); }
+
+cudaError_t raise_smem_limit(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> limit;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  int& cur = limit[{kernel, dev}];
+  cur = std::max(cur, bytes);
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, cur);
+}
 
 std::atomic<int> g_near_overlap{-1};
 int near_overlap_enabled() {

@@ -37,6 +37,7 @@
 #include <string>
 #include <vector>
 
+#include "launch.h"
 #include "ls_internal.h"
 
 namespace lsg {
@@ -491,8 +492,7 @@ GpuFar* gpu_far_open(int device, const FarTables& t, cd* S_host) {
   const size_t smem = sizeof(double2) * ((size_t)t.rank * kTerms + (size_t)kTableKeys * kTerms);
   bool ok = upload(&dux, t.ux, s) && upload(&duy, t.uy, s) && upload(&dM, Mh, s) &&
             alloc(&f->S, (size_t)nkeys * t.rank, s) &&
-            cudaFuncSetAttribute(far_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-                cudaSuccess;
+            raise_smem_limit((const void*)far_table_kernel, (int)smem) == cudaSuccess;
   if (ok) {
     const long long blocks = (nkeys + kTableKeys - 1) / kTableKeys;
     far_table_kernel<<<(unsigned)blocks, kTableKeys, smem, s>>>(dux, duy, (int)ny, nkeys, t.kappa, dM, t.rank, f->S);

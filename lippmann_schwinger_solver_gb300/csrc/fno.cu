@@ -33,6 +33,7 @@
 #include <cstdint>
 
 #include "fno.h"
+#include "launch.h"
 
 namespace lsg {
 
@@ -980,8 +981,7 @@ bool FnoNet::fused_ok() {
     if (shape.grid <= 128 && shape.layers <= 8 && shape.proj <= 128 &&
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) == cudaSuccess && coop &&
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess &&
-        cudaFuncSetAttribute(forward1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-            cudaSuccess &&
+        raise_smem_limit((const void*)forward1_kernel, (int)smem) == cudaSuccess &&
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forward1_kernel, kF1Threads, smem) == cudaSuccess &&
         per_sm >= 1) {
       fused_blocks = nsm * per_sm;

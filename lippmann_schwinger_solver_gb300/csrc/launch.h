@@ -56,6 +56,15 @@ void set_pdl_enabled(int on);
 int near_overlap_enabled();
 void set_near_overlap_enabled(int on);
 
+// Raises the dynamic shared-memory limit of `kernel` on the current device
+// to at least `bytes`. The limit is one setting per kernel and device for
+// the whole process, shared by every operator and network: each call sets
+// it to the largest value any caller has asked for on that device, so a
+// caller that needs less never lowers it under another one's launches (two
+// operators of different sizes used from two threads). Setting it on every
+// call also restores it after a device reset. Thread-safe (capi.cpp).
+cudaError_t raise_smem_limit(const void* kernel, int bytes);
+
 // kernel<<<grid, block, smem, s>>>(args...) with programmatic stream
 // serialization allowed (unless turned off, see pdl_enabled()).
 template <typename... KArgs, typename... Args>

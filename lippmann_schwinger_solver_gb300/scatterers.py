@@ -42,38 +42,28 @@ def config(level, kappa, bumps, tol_pow=10, precompute_on_gpu=0, far_on_gpu=0):
 
 
 def solve_many(specs, angles=64, tol=1e-8, tol_pow=10, device=0, log=None, keep_solutions=False,
-               precompute_on_gpu=0, far_on_gpu=0):
+               precompute_on_gpu=0, far_on_gpu=0, workers=1):
     """Assembles and solves every scatterer; returns per-scatterer records and
-    the totals. Assembly of scatterer k + 1 overlaps the solve of k. With
-    precompute_on_gpu the precomputation quadratures run on the GPU, with
-    far_on_gpu the far-field table (1) and NCA (2) (see ls_config).
+    the totals. With precompute_on_gpu the precomputation quadratures run on
+    the GPU, with far_on_gpu the far-field table (1) and NCA (2) (see
+    ls_config).
+    workers = 1: the assembly of scatterer k + 1 overlaps the solve of k.
+    workers = W > 1: a work queue in scatterer order; W threads assemble
+    (at most 2W operators built and not yet solved) and W threads solve, each
+    on its own operator's streams, so small solves share the GPU.
     assemble_s is the operator's creation (host assembly, upload, FP32
     copy); host_stages_s splits the host assembly by stage."""
     thetas = 2 * np.pi * np.arange(angles) / angles
-    recs, sols = [], []
-    ready = {}
+    n = len(specs)
 
-    def build(k):
+    def create(k):
         t0 = time.perf_counter()
-        try:
-            op = Operator(config(*specs[k], tol_pow=tol_pow, precompute_on_gpu=precompute_on_gpu,
-                                 far_on_gpu=far_on_gpu), device=device)
-            op.enable_f32()
-            ready[k] = (op, time.perf_counter() - t0, None)
-        except Exception as e:  # reported with the scatterer, not raised from the thread
-            ready[k] = (None, time.perf_counter() - t0, e)
+        op = Operator(config(*specs[k], tol_pow=tol_pow, precompute_on_gpu=precompute_on_gpu,
+                             far_on_gpu=far_on_gpu), device=device)
+        op.enable_f32()
+        return op, time.perf_counter() - t0
 
-    t_start = time.perf_counter()
-    th = threading.Thread(target=build, args=(0,))
-    th.start()
-    for k in range(len(specs)):
-        th.join()
-        op, t_asm, err = ready.pop(k)
-        if k + 1 < len(specs):
-            th = threading.Thread(target=build, args=(k + 1,))
-            th.start()
-        if err is not None:
-            raise err
+    def solve(k, op, t_asm):
         level, kappa, bumps = specs[k]
         B = op.rhs_angles(thetas)
         t0 = time.perf_counter()
@@ -85,17 +75,80 @@ def solve_many(specs, angles=64, tol=1e-8, tol_pow=10, device=0, log=None, keep_
                                           (round(t, 3) for t in op.info["assemble_stage_seconds"]))),
                    solve_s=round(t_solve, 4), applies_and_fp64_products=nmv,
                    max_true_residual=float(np.max(rr)), converged=code == LS_OK)
-        recs.append(rec)
-        if keep_solutions:
-            sols.append(X)
         if log:
             log(json.dumps(rec))
         op.close()
+        return rec, (X if keep_solutions else None)
+
+    t_start = time.perf_counter()
+    if workers <= 1:
+        out = []
+        ready = {}
+
+        def build(k):
+            try:
+                ready[k] = create(k) + (None,)
+            except Exception as e:  # reported with the scatterer, not raised from the thread
+                ready[k] = (None, 0.0, e)
+
+        th = threading.Thread(target=build, args=(0,))
+        th.start()
+        for k in range(n):
+            th.join()
+            op, t_asm, err = ready.pop(k)
+            if k + 1 < n:
+                th = threading.Thread(target=build, args=(k + 1,))
+                th.start()
+            if err is not None:
+                raise err
+            out.append(solve(k, op, t_asm))
+    else:
+        from concurrent.futures import ThreadPoolExecutor
+        slots = threading.Semaphore(2 * workers)
+        stop = threading.Event()
+        taken = set()
+
+        def build_q(k):
+            while not slots.acquire(timeout=0.05):
+                if stop.is_set():
+                    raise RuntimeError("stopped")
+            try:
+                if stop.is_set():
+                    raise RuntimeError("stopped")
+                return create(k)
+            except BaseException:
+                slots.release()
+                raise
+
+        def solve_q(k):
+            op, t_asm = futs[k].result()
+            taken.add(k)
+            try:
+                return solve(k, op, t_asm)
+            finally:
+                slots.release()
+
+        with ThreadPoolExecutor(workers) as builders, ThreadPoolExecutor(workers) as solvers:
+            futs = [builders.submit(build_q, k) for k in range(n)]
+            try:
+                out = list(solvers.map(solve_q, range(n)))
+            except BaseException:
+                # A scatterer failed: stop the queue and free the operators
+                # that were built and not taken by a solver.
+                stop.set()
+                for f in futs:
+                    f.cancel()
+                for k, f in enumerate(futs):
+                    if k not in taken and f.done() and not f.cancelled() and f.exception() is None:
+                        f.result()[0].close()
+                raise
     wall = time.perf_counter() - t_start
-    total = dict(scatterers=len(specs), directions=angles, solutions=len(specs) * angles, tol=tol,
+    recs = [r for r, _ in out]
+    sols = [x for _, x in out] if keep_solutions else []
+    total = dict(scatterers=n, directions=angles, solutions=n * angles, tol=tol, workers=workers,
                  wall_s=round(wall, 2), assemble_s=round(sum(r["assemble_s"] for r in recs), 2),
                  solve_s=round(sum(r["solve_s"] for r in recs), 3),
-                 solve_per_direction_ms=round(1e3 * sum(r["solve_s"] for r in recs) / (len(specs) * angles), 3),
+                 solve_per_direction_ms=round(1e3 * sum(r["solve_s"] for r in recs) / (n * angles), 3),
                  all_converged=all(r["converged"] for r in recs),
                  max_true_residual=max(r["max_true_residual"] for r in recs))
     return recs, total, sols
@@ -112,10 +165,12 @@ def main(argv=None):
     ap.add_argument("--gpu-precompute", action="store_true", help="precomputation quadratures on the GPU")
     ap.add_argument("--gpu-far", type=int, default=0, choices=[0, 1, 2],
                     help="far-field table (1) and NCA skeleton search (2) on the GPU")
+    ap.add_argument("--workers", type=int, default=1,
+                    help="scatterers assembled and solved at once (a work queue when > 1)")
     a = ap.parse_args(argv)
     specs = scatterer_specs(a.n, a.seed, levels=tuple(int(v) for v in a.levels.split(",")))
     _, total, _ = solve_many(specs, a.angles, a.tol, a.tol_pow, log=print, precompute_on_gpu=int(a.gpu_precompute),
-                             far_on_gpu=a.gpu_far)
+                             far_on_gpu=a.gpu_far, workers=a.workers)
     print(json.dumps(total))
 
 

@@ -50,16 +50,21 @@ def test_batched_rejects_bad_input(ls):
     op.close()
 
 
-def test_many_scatterers_pipeline(ls):
+@pytest.mark.parametrize("workers", [1, 2])
+def test_many_scatterers_pipeline(ls, workers):
     """Several scatterers of different size and wavenumber, each with many
-    directions; assembly of the next overlaps the solve of the current one.
-    Every direction of every scatterer meets the FP64 tolerance, and the
-    solutions equal those of the same solve run alone."""
+    directions; assembly of the next overlaps the solve of the current one
+    (workers = 1), or a work queue assembles and solves two at a time
+    (workers = 2, solves of different operators in flight together). Every
+    direction of every scatterer meets the FP64 tolerance, and the solutions
+    equal those of the same solve run alone."""
     from lippmann_schwinger_solver_gb300 import scatterers as sc
-    specs = [(3, 12.0, ((0.1, -0.2, 1.0, 0.15),)), (4, 30.0, ((-0.3, 0.2, 0.8, 0.1), (0.4, 0.1, 1.2, 0.07)))]
-    recs, total, sols = sc.solve_many(specs, angles=16, tol=1e-8, keep_solutions=True)
+    specs = [(3, 12.0, ((0.1, -0.2, 1.0, 0.15),)), (4, 30.0, ((-0.3, 0.2, 0.8, 0.1), (0.4, 0.1, 1.2, 0.07))),
+             (3, 20.0, ((0.2, 0.3, 1.1, 0.12),))]
+    recs, total, sols = sc.solve_many(specs, angles=16, tol=1e-8, keep_solutions=True, workers=workers)
     assert total["all_converged"] and total["max_true_residual"] <= 1e-8
-    assert [r["N"] for r in recs] == [2304, 9216]
+    assert [r["N"] for r in recs] == [2304, 9216, 2304]
+    assert [r["scatterer"] for r in recs] == [0, 1, 2]
     op = ls.Operator(sc.config(*specs[1]), device=0)
     op.enable_f32()
     B = op.rhs_angles(2 * np.pi * np.arange(16) / 16)
@@ -67,3 +72,25 @@ def test_many_scatterers_pipeline(ls):
     assert code == ls.LS_OK
     assert np.linalg.norm(X - sols[1]) / np.linalg.norm(X) < 1e-12
     op.close()
+
+
+def test_operators_of_different_sizes_share_the_kernels(ls):
+    """The tensor-core kernels' dynamic shared-memory limit is one setting
+    per kernel for the process: setting up a smaller operator's tensor-core
+    form after a larger one's must not lower it under the larger one's
+    launches (it did, and the larger operator's next batched solve failed
+    with an invalid-argument launch error when two scatterers of different
+    sizes were solved from two threads)."""
+    from conftest import CFG_L5_BUMPS
+    big = ls.Operator(full_cfg(CFG_L5_BUMPS), device=0)
+    big.enable_f32()
+    big.time_block_apply(64, warmup=0, iters=1)
+    small = ls.Operator(full_cfg(CFG_L3_K10), device=0)
+    small.enable_f32()
+    small.time_block_apply(64, warmup=0, iters=1)
+    for op in (big, small):
+        B = op.rhs_angles(2 * np.pi * np.arange(8) / 8)
+        X, nmv, rr, code = op.gmres_mixed_batched(B, max_outer=20, inner_iter=100, tol=1e-8)
+        assert code == ls.LS_OK and np.max(rr) <= 1e-8
+    big.close()
+    small.close()
