@@ -10,6 +10,9 @@
  * (depth-first leaves, 36 Chebyshev nodes per leaf, node = row * n + col).
  * All functions return LS_OK (0) or a negative LS_E_* code and never exit
  * the process; ls_last_error() describes the last failure on this thread.
+ * Threading: an operator serves one call at a time (its device buffers and
+ * stream are its own); distinct operators may be created, solved and
+ * destroyed from different threads at the same time.
  */
 #ifndef LS_DAFMM_H
 #define LS_DAFMM_H
