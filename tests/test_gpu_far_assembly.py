@@ -3,9 +3,9 @@ against the host assembler, which is the oracle's bit for bit.
 
 Mode 1 tabulates the far-field sums of every distinct relative position on
 the GPU and leaves the NCA (ACA_only_nodes, GMRES/ACA.hpp:253-481) on the
-host; mode 2 also runs the NCA on the GPU, one warp per block. The GPU's
-Bessel, trigonometric and hypot values differ from the host's in the last
-bits. On a uniform tree many pivot candidates are equal in magnitude up to
+host; mode 2 also runs the NCA on the GPU, one thread block per NCA block.
+The GPU's Bessel, trigonometric and hypot values differ from the host's in
+the last bits. On a uniform tree many pivot candidates are equal in magnitude up to
 such bits (mirror-image positions), so those ties break differently: the
 skeletons are other valid choices, not the oracle's. The bar is therefore
 the assembly's own sensitivity: the GPU-assembled operator's matvec is no
