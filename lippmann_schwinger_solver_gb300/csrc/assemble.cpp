@@ -1469,20 +1469,29 @@ void Builder::run_nca(std::vector<NcaJob>& jobs) {
     std::vector<NcaTask> tasks;
     std::vector<int> which, idx;
     int piv_off = 0;
+    long long idx_len = 0;
     for (int t = 0; t < nj; ++t) {
       const NcaJob& jb = jobs[t];
       if (jb.rows.empty() || jb.cols.empty()) continue;
       NcaTask tk;
-      tk.idx_off = (long long)idx.size();
+      tk.idx_off = idx_len;
       tk.n1 = (int)jb.rows.size();
       tk.n2 = (int)jb.cols.size();
       tk.R = std::min(std::min(tk.n1, tk.n2), kNcaRankCap);
       tk.out_off = piv_off;
       piv_off += 2 * tk.R;
-      idx.insert(idx.end(), jb.rows.begin(), jb.rows.end());
-      idx.insert(idx.end(), jb.cols.begin(), jb.cols.end());
+      idx_len += (long long)tk.n1 + tk.n2;
       tasks.push_back(tk);
       which.push_back(t);
+    }
+    // Every block's rows then columns, copied in parallel to its offset.
+    idx.resize((size_t)idx_len);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int u = 0; u < (int)tasks.size(); ++u) {
+      const NcaJob& jb = jobs[which[u]];
+      int* dst = idx.data() + tasks[u].idx_off;
+      std::copy(jb.rows.begin(), jb.rows.end(), dst);
+      std::copy(jb.cols.begin(), jb.cols.end(), dst + jb.rows.size());
     }
     std::vector<int> ranks, piv, status;
     if (!tasks.empty() && gpu_far_nca(gfar, tasks, idx, tol, ranks, piv, status)) {
