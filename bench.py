@@ -579,7 +579,7 @@ def run_ours(args):
                             "max_true_residual": float(np.max(rrb8)), "converged": codeb8 == 0,
                             "max_rel_diff_vs_width64": float(max(np.linalg.norm(Xb[:, j] - Xb8[:, j]) /
                                                                  np.linalg.norm(Xb8[:, j]) for j in range(B.shape[1])))}}
-    # BASELINE config 4: 32 seeded scatterers of uneven size (levels 4-6,
+    # The many-scatterer workload: 32 seeded scatterers of uneven size (levels 4-6,
     # kappa U[10, 60], 1-4 bumps) x 64 directions, host assembly of the next
     # scatterer overlapped with the GPU solve of the current one.
     many = None
