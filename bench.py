@@ -246,14 +246,16 @@ def adaptive_leg(ls, local, timed, max_iter):
 
 def gpu_assembly_leg(ls, cfg, x, y_host, skel_host, device):
     """The workload's operator assembled with its far field on the GPU
-    (ls_config.far_on_gpu 1: sum table; 2: table and NCA; then also the
-    precomputation quadratures) against the default host-assembled one,
+    (ls_config.far_on_gpu 1: sum table; 2: table and NCA; 3: and the M2L
+    tiles filled on the device; then also the precomputation quadratures)
+    against the default host-assembled one,
     which the oracle leg pins: assembly stages, the matvec's distance and
     the fraction of skeleton nodes that agree."""
     names = ("geometry", "precompute", "lists", "nca", "checks", "pack")
     out = {"tolerance": 10.0 ** (1 - cfg.TOL_POW)}
     for name, over in (("far_table", dict(far_on_gpu=1)), ("far_table_and_nca", dict(far_on_gpu=2)),
-                       ("far_and_precompute", dict(far_on_gpu=2, precompute_on_gpu=1))):
+                       ("far_table_nca_and_m2l_fill", dict(far_on_gpu=3)),
+                       ("far_and_precompute", dict(far_on_gpu=3, precompute_on_gpu=1))):
         t0 = time.perf_counter()
         opg = ls.Operator(dataclasses.replace(cfg, **over), device=device)
         wall = time.perf_counter() - t0
@@ -599,13 +601,13 @@ def run_ours(args):
         many["gpu_precompute"] = many_g
         # And with the far-field table and NCA on the GPU as well.
         recs_f, many_f, _ = scat.solve_many(specs, args.angles, 1e-8, 10, device=local, precompute_on_gpu=1,
-                                            far_on_gpu=2)
+                                            far_on_gpu=3)
         many_f["host_stages_s"] = {k: round(sum(r["host_stages_s"][k] for r in recs_f), 2)
                                    for k in recs_f[0]["host_stages_s"]}
         many["gpu_precompute_and_far"] = many_f
         # The same, two scatterers assembled and two solved at a time.
         _, many_w, _ = scat.solve_many(specs, args.angles, 1e-8, 10, device=local, precompute_on_gpu=1,
-                                       far_on_gpu=2, workers=2)
+                                       far_on_gpu=3, workers=2)
         many["gpu_precompute_and_far_2_workers"] = many_w
     far_gpu = None
     if rank == 0 and not args.no_gpu_assembly:

@@ -102,7 +102,11 @@ typedef struct {
    * host's NCA and block fills read them from that table;
    * 2: as 1, and the NCA skeleton search of every box runs on the GPU as
    * well (one thread block per box and direction; the host redoes any box
-   * whose rank passes the GPU's capacity).
+   * whose rank passes the GPU's capacity);
+   * 3: as 2, and the M2L blocks (Assemble_LFR_M2L / Assemble_HFR_M2L,
+   * G_FMM2DTree.hpp:2502, 3829) are filled from the table straight into the
+   * device operator's tiles, never formed on the host (without a device, on
+   * the host from the same table).
    * GPU values differ from the host's in the last bits, which moves NCA
    * pivots among candidates equal in magnitude up to such bits (mirror-image
    * positions of a uniform tree): the skeletons are other valid choices, and

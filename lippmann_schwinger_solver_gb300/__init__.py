@@ -146,7 +146,7 @@ class Config:
     tree_adaptive: int = 0   # 1: the reference's adaptive quadtree (createAdaptiveTree + 2:1 balance)
     treeAdaptivity: int = 5  # adaptive: boxes split until q is resolved to 10^-treeAdaptivity
     precompute_on_gpu: int = 0  # 1: precomputation quadratures on the operator's GPU (not bit-exact with the host)
-    far_on_gpu: int = 0  # 1: far-field sum table on the GPU; 2: and the NCA skeleton search (uniform trees)
+    far_on_gpu: int = 0  # 1: far-field sum table on the GPU; 2: and the NCA; 3: and the M2L block fill (uniform trees)
 
     def to_c(self):
         c = _Config()

@@ -868,6 +868,8 @@ class Builder {
   void precompute();
   void interaction_lists();
   void far_tables();
+  void fill_tiles_host(GemvPhase& ph, const std::vector<FillTile>& fl, const std::vector<int>& rowpts,
+                       const std::vector<int>& colpts);
   void run_nca(std::vector<NcaJob>& jobs);
   void nca_level_lfr(int j);
   void nca_level_hfr(int j);
@@ -1455,8 +1457,34 @@ void Builder::far_tables() {
   dense = true;
 }
 
+// Fills the tiles described by fl from the far-field table on the host
+// (far_on_gpu = 3 without a device, or when the device fill failed): the
+// entries the device fill writes, and the values the default packing
+// writes for the same blocks.
+void Builder::fill_tiles_host(GemvPhase& ph, const std::vector<FillTile>& fl, const std::vector<int>& rowpts,
+                              const std::vector<int>& colpts) {
+  ph.A.resize((size_t)ph.dev_A_elems);
+  ph.dev_A_elems = 0;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (size_t t = 0; t < fl.size(); ++t) {
+    const FillTile& f = fl[t];
+    HCache hc{this, {}};
+    const int S = 1 << f.log2s, R = kTileLanes >> f.log2s;
+    for (int q = 0; q < f.qmax; ++q)
+      for (int lane = 0; lane < kTileLanes; ++lane) {
+        const int sl = lane / R, r = lane % R, k = q * S + sl;
+        cplx v{0.0, 0.0};
+        if (r < f.rows && k < f.K) {
+          const cd e = entry(rowpts[(size_t)(f.row_off + r)], colpts[(size_t)(f.col_off + k)], hc);
+          v = cplx{e.real(), e.imag()};
+        }
+        ph.A[(size_t)(f.a_off + (long long)q * kTileLanes + lane)] = v;
+      }
+  }
+}
+
 // The NCA of a batch of blocks (ACA_only_nodes per block). With far_on_gpu
-// = 2 the blocks run on the GPU, and the host keeps only those the GPU
+// >= 2 the blocks run on the GPU, and the host keeps only those the GPU
 // marked (rank capacity) or could not run; the outgoing blocks' pivot rows
 // (Ar) of GPU results are filled from the table. Then the results go to
 // their nodes: an empty side leaves the node inactive with its own list
@@ -1465,7 +1493,7 @@ void Builder::run_nca(std::vector<NcaJob>& jobs) {
   const double tol = std::pow(10, -1.0 * cfg.TOL_POW);
   const int nj = (int)jobs.size();
   std::vector<char> on_gpu(nj, 0);
-  if (gfar && cfg.far_on_gpu == 2) {
+  if (gfar && cfg.far_on_gpu >= 2) {
     std::vector<NcaTask> tasks;
     std::vector<int> which, idx;
     int piv_off = 0;
@@ -1645,17 +1673,27 @@ struct BlockView {
   int rows, K;
   std::vector<int>* idx;
   int out;
+  // A == nullptr: the block is filled from the far-field table, row r from
+  // target point (*rowpts)[r] against the source points *colpts.
+  std::vector<int>* rowpts = nullptr;
+  std::vector<int>* colpts = nullptr;
 };
 template <class Get>
 static void stage_blocks(GemvPhase& ph, int n, Get get) {
   for (int t = 0; t < n; ++t) {
     const BlockView v = get(t);
     if (v.rows <= 0 || v.K <= 0) continue;
-    ph.stageA.push_back(std::move(*v.A));
     ph.stageIdx.push_back(std::move(*v.idx));
-    const cd* a = ph.stageA.back().data();
     const int* ix = ph.stageIdx.back().data();
-    for (int r = 0; r < v.rows; ++r) ph.rows.push_back({a + (size_t)r * v.K, v.K, ix, v.out + r});
+    if (v.A) {
+      ph.stageA.push_back(std::move(*v.A));
+      const cd* a = ph.stageA.back().data();
+      for (int r = 0; r < v.rows; ++r) ph.rows.push_back({a + (size_t)r * v.K, v.K, ix, v.out + r});
+    } else {
+      ph.stageCols.push_back(std::move(*v.colpts));
+      const int* cp = ph.stageCols.back().data();
+      for (int r = 0; r < v.rows; ++r) ph.rows.push_back({nullptr, v.K, ix, v.out + r, (*v.rowpts)[r], cp});
+    }
     ph.nnz += (long long)v.rows * v.K;
   }
 }
@@ -1701,7 +1739,12 @@ static TileKnobs tile_knobs(const char* kind) {
   return k;
 }
 
-static void finalize(GemvPhase& ph, const char* kind) {
+// Rows staged without values (table blocks) leave ph.A empty: the tiles
+// are described in *fill (row points in *frows, each block's source points
+// once in *fcols) and ph.dev_A_elems holds their size, for a fill from the
+// far-field table on the device or on the host.
+static void finalize(GemvPhase& ph, const char* kind, std::vector<FillTile>* fill = nullptr,
+                     std::vector<int>* frows = nullptr, std::vector<int>* fcols = nullptr) {
   struct Block { size_t r0; int rows, K; };
   std::vector<Block> blocks;
   for (size_t r = 0; r < ph.rows.size();) {
@@ -1744,7 +1787,29 @@ static void finalize(GemvPhase& ph, const char* kind) {
     }
   }
   ph.blk_tile0.push_back((int)tl.size());
-  ph.A.resize((size_t)total);  // uninitialised: each tile zeroes and fills its own range below
+  const bool table = !ph.rows.empty() && ph.rows[0].a == nullptr;
+  if (table) {
+    fill->clear();
+    frows->clear();
+    fcols->clear();
+    const int* last_cols = nullptr;
+    long long col_off = 0;
+    for (const T& d : tl) {
+      const GemvPhase::Row& first = ph.rows[d.r0];
+      if (first.cpt != last_cols) {
+        col_off = (long long)fcols->size();
+        fcols->insert(fcols->end(), first.cpt, first.cpt + d.K);
+        last_cols = first.cpt;
+      }
+      int log2s = 0;
+      while ((1 << log2s) < d.S) ++log2s;
+      fill->push_back({d.off, (long long)frows->size(), col_off, d.qmax, d.rows, log2s, d.K});
+      for (int r = 0; r < d.rows; ++r) frows->push_back(ph.rows[d.r0 + r].pt);
+    }
+    ph.dev_A_elems = total;
+  } else {
+    ph.A.resize((size_t)total);  // uninitialised: each tile zeroes and fills its own range below
+  }
   ph.idx.assign((size_t)total_idx, 0);
   ph.out.assign(ph.rows.size(), 0);
   ph.klen.assign(tl.size() * kTileLanes, 0);
@@ -1757,7 +1822,8 @@ static void finalize(GemvPhase& ph, const char* kind) {
     int log2s = 0;
     while ((1 << log2s) < d.S) ++log2s;
     const GemvPhase::Row& first = ph.rows[d.r0];
-    std::fill(ph.A.begin() + d.off, ph.A.begin() + d.off + (long long)d.qmax * kTileLanes, cplx{0.0, 0.0});
+    if (!table)
+      std::fill(ph.A.begin() + d.off, ph.A.begin() + d.off + (long long)d.qmax * kTileLanes, cplx{0.0, 0.0});
     for (int q = 0; q < d.qmax; ++q)
       for (int sl = 0; sl < d.S; ++sl) {
         const int k = q * d.S + sl;
@@ -1770,7 +1836,7 @@ static void finalize(GemvPhase& ph, const char* kind) {
         const int lane = sl * R + r;
         int q = 0;
         for (int k = sl; k < row.K; k += d.S, ++q)
-          ph.A[(size_t)(d.off + (long long)q * kTileLanes + lane)] = cplx{row.a[k].real(), row.a[k].imag()};
+          if (!table) ph.A[(size_t)(d.off + (long long)q * kTileLanes + lane)] = cplx{row.a[k].real(), row.a[k].imag()};
         ph.klen[t * kTileLanes + lane] = q;
       }
     }
@@ -1778,6 +1844,7 @@ static void finalize(GemvPhase& ph, const char* kind) {
   }
   std::vector<std::vector<cd>>().swap(ph.stageA);
   std::vector<std::vector<int>>().swap(ph.stageIdx);
+  std::vector<std::vector<int>>().swap(ph.stageCols);
   std::vector<GemvPhase::Row>().swap(ph.rows);
 }
 
@@ -1885,9 +1952,12 @@ void Builder::pack(HostOperator& op) {
     op.up.push_back(std::move(ph));
   }
 
-  // ---- M2L: one task per node with an incoming interaction list.
+  // ---- M2L: one task per node with an incoming interaction list. With
+  // far_on_gpu = 3 the blocks keep only their target and source points and
+  // their tiles are filled from the far-field table on the device.
   {
-    struct Task { std::vector<cd> A; std::vector<int> idx; int rows = 0, K = 0; long long out = 0; };
+    struct Task { std::vector<cd> A; std::vector<int> idx, rowpts, colpts; int rows = 0, K = 0; long long out = 0; };
+    const bool by_table = dense && cfg.far_on_gpu >= 3;
     std::vector<std::pair<int, int>> all;
     for (int j = 2; j <= nL; ++j)
       for (int t = 0; t < (int)nodes[j].size(); ++t) all.push_back({j, t});
@@ -1909,13 +1979,17 @@ void Builder::pack(HostOperator& op) {
       const int rows = (int)nd.user_check.size();
       HCache hc{this, {}};
       Task& tk = tasks[u];
-      tk.A.resize((size_t)rows * K);
+      if (!by_table) tk.A.resize((size_t)rows * K);
       int c0 = 0;
       for (const Node* s : srcs) {
-        fill(nd.user_check, s->out_charge, hc, tk.A.data() + c0, K);
+        if (by_table)
+          tk.colpts.insert(tk.colpts.end(), s->out_charge.begin(), s->out_charge.end());
+        else
+          fill(nd.user_check, s->out_charge, hc, tk.A.data() + c0, K);
         tk.idx.insert(tk.idx.end(), s->fidx.begin(), s->fidx.end());
         c0 += (int)s->out_charge.size();
       }
+      if (by_table) tk.rowpts = nd.user_check;
       tk.rows = rows;
       tk.K = K;
       tk.out = nd.pot_off;
@@ -1927,9 +2001,18 @@ void Builder::pack(HostOperator& op) {
     stage_blocks(ph, (int)tasks.size(), [&](int u) {
       Task& tk = tasks[u];
       if (tk.K == 0) return BlockView{nullptr, 0, 0, nullptr, 0};
+      if (by_table) return BlockView{nullptr, tk.rows, tk.K, &tk.idx, (int)tk.out, &tk.rowpts, &tk.colpts};
       return BlockView{&tk.A, tk.rows, tk.K, &tk.idx, (int)tk.out};
     });
-    finalize(ph, "M2L");
+    if (by_table) {
+      std::vector<FillTile> fl;
+      std::vector<int> frows, fcols;
+      finalize(ph, "M2L", &fl, &frows, &fcols);
+      ph.dev_A = gfar ? gpu_far_fill(gfar, fl, frows, fcols, ph.dev_A_elems) : nullptr;
+      if (!ph.dev_A) fill_tiles_host(ph, fl, frows, fcols);
+    } else {
+      finalize(ph, "M2L");
+    }
     op.m2l = std::move(ph);
   }
 
@@ -2164,6 +2247,11 @@ __attribute__((weak)) bool gpu_far_nca(GpuFar*, const std::vector<NcaTask>&, con
   return false;
 }
 __attribute__((weak)) void gpu_far_close(GpuFar*) {}
+__attribute__((weak)) void* gpu_far_fill(GpuFar*, const std::vector<FillTile>&, const std::vector<int>&,
+                                         const std::vector<int>&, long long) {
+  return nullptr;
+}
+__attribute__((weak)) void gpu_far_free(void*) {}
 __attribute__((weak)) bool gpu_quadrature(int, const std::vector<QuadTask>&, const std::vector<double>&,
                                           const std::vector<double>&, std::vector<cd>&) {
   return false;

@@ -129,6 +129,7 @@ ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
   const bool assembled = assemble(*cfg, op->host, err);
   set_assembly_device(-1);
   if (!assembled) {
+    gpu_far_free(op->host.m2l.dev_A);
     delete op;
     return fail(LS_E_INVALID, "ls_op_create: " + err);
   }
@@ -139,10 +140,13 @@ ls_status ls_op_create(const ls_config* cfg, int device, ls_op** out) {
   op->on_device = true;
   op->dev.device = device;
   if (!dev_upload(op->host, op->dev, err)) {
+    // Device-filled tiles the upload did not adopt are freed here.
+    if (op->host.m2l.dev_A && op->dev.m2l.A != op->host.m2l.dev_A) gpu_far_free(op->host.m2l.dev_A);
     dev_free(op->dev);
     delete op;
     return fail(LS_E_CUDA, "ls_op_create: " + err);
   }
+  op->host.m2l.dev_A = nullptr;  // owned by the device operator now
   // Host copies of the tiles are no longer needed.
   auto drop = [](GemvPhase& p) {
     PackedBlocks().swap(p.A);

@@ -430,6 +430,28 @@ __global__ void __launch_bounds__(NT) nca_kernel(NcaGeomDev g, const NcaTask* __
   }
 }
 
+// Tiles of a phase from the far-field table (FillTile): one warp per tile,
+// lane l writing column slot l of each 32-wide step, so a step is one
+// contiguous 512-byte row.
+__global__ void __launch_bounds__(256) table_fill_kernel(NcaGeomDev g, const FillTile* __restrict__ tiles,
+                                                         long long ntiles, const int* __restrict__ rowpts,
+                                                         const int* __restrict__ colpts, double2* __restrict__ A) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += nw) {
+    const FillTile f = tiles[t];
+    const int S = 1 << f.log2s, R = 32 >> f.log2s;
+    const int sl = lane / R, r = lane - sl * R;
+    const int i = r < f.rows ? rowpts[f.row_off + r] : 0;
+    for (int q = 0; q < f.qmax; ++q) {
+      const int k = q * S + sl;
+      double2 v = make_double2(0.0, 0.0);
+      if (r < f.rows && k < f.K) v = far_entry(g, i, colpts[f.col_off + k]);
+      A[f.a_off + (long long)q * 32 + lane] = v;
+    }
+  }
+}
+
 template <class T>
 bool upload(T** d, const std::vector<T>& h, cudaStream_t s) {
   *d = nullptr;
@@ -581,5 +603,53 @@ bool gpu_far_nca(GpuFar* f, const std::vector<NcaTask>& tasks, const std::vector
 }
 
 void gpu_far_close(GpuFar* f) { delete f; }
+
+void* gpu_far_fill(GpuFar* f, const std::vector<FillTile>& tiles, const std::vector<int>& rowpts,
+                   const std::vector<int>& colpts, long long elems) {
+  if (!f || tiles.empty() || elems <= 0) return nullptr;
+  // Every tile inside A and its point lists (the kernel does not check).
+  for (const FillTile& t : tiles) {
+    const int R = 32 >> t.log2s;
+    if (t.log2s < 0 || t.log2s > 5 || t.rows < 1 || t.rows > R || t.K < 1 || t.qmax < 1 ||
+        t.qmax != (t.K + (1 << t.log2s) - 1) >> t.log2s || t.a_off < 0 || t.a_off + 32LL * t.qmax > elems ||
+        t.row_off < 0 || t.row_off + t.rows > (long long)rowpts.size() || t.col_off < 0 ||
+        t.col_off + t.K > (long long)colpts.size())
+      return nullptr;
+  }
+  if (cudaSetDevice(f->device) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  cudaStream_t s = f->stream;
+  double2* A = nullptr;
+  if (cudaMalloc(&A, sizeof(double2) * (size_t)elems) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  FillTile* dt = nullptr;
+  int *dr = nullptr, *dc = nullptr;
+  bool ok = upload(&dt, tiles, s) && upload(&dr, rowpts, s) && upload(&dc, colpts, s);
+  if (ok) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, f->device);
+    const long long nt = (long long)tiles.size();
+    const long long blocks = std::max(1LL, std::min((nt + 7) / 8, (long long)std::max(sms, 1) * 16));
+    table_fill_kernel<<<(unsigned)blocks, 256, 0, s>>>(f->g, dt, nt, dr, dc, A);
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  for (void* p : {(void*)dt, (void*)dr, (void*)dc})
+    if (p) cudaFreeAsync(p, s);
+  ok = cudaStreamSynchronize(s) == cudaSuccess && ok;
+  if (!ok) {
+    cudaFree(A);
+    cudaGetLastError();
+    return nullptr;
+  }
+  return A;
+}
+
+void gpu_far_free(void* p) {
+  if (p) cudaFree(p);
+}
 
 }  // namespace lsg

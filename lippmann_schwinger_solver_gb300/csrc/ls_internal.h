@@ -90,10 +90,24 @@ struct GemvPhase {
   // Staging before packing: the phase owns its blocks (row major) and their
   // gather lists until they are packed; one record per block row points
   // into them.
-  struct Row { const cd* a; int K; const int* idx; int out; };
+  // A row staged without values (a == nullptr) is filled from the far-field
+  // table: its target point pt against the block's source points cpt[0, K).
+  struct Row {
+    const cd* a;
+    int K;
+    const int* idx;
+    int out;
+    int pt = -1;
+    const int* cpt = nullptr;
+  };
   std::vector<std::vector<cd>> stageA;
-  std::vector<std::vector<int>> stageIdx;
+  std::vector<std::vector<int>> stageIdx, stageCols;
   std::vector<Row> rows;
+  // The tiles filled on the device (far_on_gpu = 3, M2L): A stays empty on
+  // the host and dev_A (dev_A_elems complex doubles, cudaMalloc'd on the
+  // operator's device) holds them until the device upload adopts it.
+  void* dev_A = nullptr;
+  long long dev_A_elems = 0;
   long long entries() const { return nnz; }
 };
 
@@ -160,6 +174,14 @@ struct FarTables {
   std::vector<double> kq;       // kappa^2 q per point
   std::vector<cd> M;            // rank x 31, the leaf moments
 };
+// One tile of a phase filled from the far-field table: A[a_off + 32 q +
+// lane] for lane = sl * R + r (R = 32 >> log2s rows, sl < 1 << log2s) is
+// K(rowpts[row_off + r], colpts[col_off + q * S + sl]) for r < rows and
+// q * S + sl < K, zero elsewhere (the layout of GemvTile).
+struct FillTile {
+  long long a_off, row_off, col_off;
+  int qmax, rows, log2s, K;
+};
 // One NCA block for the GPU: rows idx[idx_off, +n1), columns
 // idx[idx_off + n1, +n2) (point indices); pivots up to R = min(n1, n2, cap):
 // rows at piv[out_off, +R), columns at piv[out_off + R, +R).
@@ -179,6 +201,11 @@ GpuFar* gpu_far_open(int device, const FarTables& t, cd* S_host);
 bool gpu_far_nca(GpuFar* f, const std::vector<NcaTask>& tasks, const std::vector<int>& idx, double eps,
                  std::vector<int>& ranks, std::vector<int>& piv, std::vector<int>& status);
 void gpu_far_close(GpuFar* f);
+// Fills `elems` complex doubles of tiles from the table on the device;
+// returns the cudaMalloc'd array, or nullptr (the host fills them instead).
+void* gpu_far_fill(GpuFar* f, const std::vector<FillTile>& tiles, const std::vector<int>& rowpts,
+                   const std::vector<int>& colpts, long long elems);
+void gpu_far_free(void* p);
 
 // assemble.cpp. Process-wide cache of precomputation records (far
 // moments, near blocks), keyed on every input they depend on: dir nullptr

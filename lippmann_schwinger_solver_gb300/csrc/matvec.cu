@@ -470,11 +470,19 @@ static bool upload_phase(const GemvPhase& h, DevPhase<double2>& d, long long& to
   d.n_tiles = (int)h.tiles.size();
   d.accumulate = h.accumulate;
   d.entries = h.nnz;
-  d.stored = (long long)h.A.size();
-  if (!dmalloc(&d.A, h.A.size(), total, err)) return false;
-  if (h.A.size() && cudaMemcpy(d.A, h.A.data(), h.A.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess) {
-    err = "upload A";
-    return false;
+  if (h.dev_A) {
+    // Tiles filled on this device during assembly: adopted, not copied.
+    d.A = static_cast<double2*>(h.dev_A);
+    d.stored = h.dev_A_elems;
+    total += h.dev_A_elems * (long long)sizeof(double2);
+  } else {
+    d.stored = (long long)h.A.size();
+    if (!dmalloc(&d.A, h.A.size(), total, err)) return false;
+    if (h.A.size() &&
+        cudaMemcpy(d.A, h.A.data(), h.A.size() * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess) {
+      err = "upload A";
+      return false;
+    }
   }
   return upload(&d.idx, h.idx, total, err) && upload(&d.out, h.out, total, err) &&
          upload(&d.klen, h.klen, total, err) && upload(&d.tiles, h.tiles, total, err);

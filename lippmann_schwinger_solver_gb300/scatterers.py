@@ -45,8 +45,8 @@ def solve_many(specs, angles=64, tol=1e-8, tol_pow=10, device=0, log=None, keep_
                precompute_on_gpu=0, far_on_gpu=0, workers=1):
     """Assembles and solves every scatterer; returns per-scatterer records and
     the totals. With precompute_on_gpu the precomputation quadratures run on
-    the GPU, with far_on_gpu the far-field table (1) and NCA (2) (see
-    ls_config).
+    the GPU, with far_on_gpu the far-field table (1), NCA (2) and M2L block
+    fill (3) (see ls_config).
     workers = 1: the assembly of scatterer k + 1 overlaps the solve of k.
     workers = W > 1: a work queue in scatterer order; W threads assemble
     (at most 2W operators built and not yet solved) and W threads solve, each
@@ -163,8 +163,8 @@ def main(argv=None):
     ap.add_argument("--tol-pow", type=int, default=10)
     ap.add_argument("--levels", default="4,5,6")
     ap.add_argument("--gpu-precompute", action="store_true", help="precomputation quadratures on the GPU")
-    ap.add_argument("--gpu-far", type=int, default=0, choices=[0, 1, 2],
-                    help="far-field table (1) and NCA skeleton search (2) on the GPU")
+    ap.add_argument("--gpu-far", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="far-field table (1), NCA skeleton search (2) and M2L block fill (3) on the GPU")
     ap.add_argument("--workers", type=int, default=1,
                     help="scatterers assembled and solved at once (a work queue when > 1)")
     a = ap.parse_args(argv)

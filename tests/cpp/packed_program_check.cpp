@@ -11,7 +11,10 @@
 //     writes (its tiles run concurrently).
 // Compiled against the assembler source itself (host code only).
 //
-// usage: packed_program_check <ls_config bytes> <x: N complex128> <y out>
+// usage: packed_program_check <ls_config bytes> <x: N complex128> <y out> [--far-only]
+// --far-only: y is the far part alone (the leaf potentials after the upward,
+// M2L and downward phases), for uniform trees, whose near field is not a
+// packed phase.
 // Exit status: 0 = all checks passed and y written; 2 = bad arguments;
 // 3 = assembly failed; 4 = a check failed (reason on stderr).
 #include "../../lippmann_schwinger_solver_gb300/csrc/assemble.cpp"
@@ -81,7 +84,9 @@ bool run_phase(const GemvPhase& ph, const std::vector<cd>& src, std::vector<cd>&
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc != 4) return 2;
+  if (argc != 4 && argc != 5) return 2;
+  const bool far_only = argc == 5 && std::string(argv[4]) == "--far-only";
+  if (argc == 5 && !far_only) return 2;
   ls_config cfg;
   FILE* f = std::fopen(argv[1], "rb");
   if (!f) return 2;
@@ -98,7 +103,7 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "assemble: %s\n", err.c_str());
     return 3;
   }
-  if (!h.generic_near) {
+  if (!h.generic_near && !far_only) {
     std::fprintf(stderr, "the operator has no generic near phase\n");
     return 4;
   }
@@ -114,7 +119,7 @@ int main(int argc, char** argv) {
   if (!run_phase(h.m2l, S, P, false, "m2l")) return 4;
   for (auto& ph : h.down)
     if (!run_phase(ph, P, P, true, "down")) return 4;
-  if (!run_phase(h.nearph, S, P, false, "near")) return 4;
+  if (!far_only && !run_phase(h.nearph, S, P, false, "near")) return 4;
   f = std::fopen(argv[3], "wb");
   if (!f || std::fwrite(P.data(), sizeof(cd), N, f) != (size_t)N) return 2;
   std::fclose(f);

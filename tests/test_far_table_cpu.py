@@ -9,6 +9,8 @@ cone (ACA_only_nodes, GMRES/ACA.hpp:253-481), the same moments and near
 blocks. Mode 2 (NCA on the GPU) without a device runs the host's NCA on the
 table. A wrong index in the tables would change entries and with them the
 skeletons."""
+import os
+
 import numpy as np
 import pytest
 
@@ -59,3 +61,34 @@ def test_skeleton_parser_round_trip(ls):
             moved += [len(lst)] + list(lst)
     assert ls.skeleton_agreement(np.array(moved, dtype=np.int32), dump) == pytest.approx(1.0 - 1.0 / len(nodes))
     op.close()
+
+
+@pytest.mark.parametrize("base", [CFG_C1, CFG_HFR, CFG_L5_BUMPS], ids=["c1", "hfr-cones", "level5-kappa40"])
+def test_table_filled_m2l_tiles_equal_the_default_packing(ls, tmp_path, base):
+    """far_on_gpu = 3 forms the M2L tiles from tile descriptors and the
+    far-field table (on the device, or on the host without one) instead of
+    packing host-filled blocks. Run on the host by
+    tests/cpp/packed_program_check.cpp (every access checked in bounds), the
+    far part of the matvec (upward, M2L, downward phases) equals the
+    default packing's bit for bit."""
+    import subprocess
+    from conftest import ROOT
+    exe = str(tmp_path / "packed_program_check")
+    src = os.path.join(ROOT, "tests", "cpp", "packed_program_check.cpp")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"),
+                    src, "-o", exe], check=True, capture_output=True, timeout=600)
+    rng = np.random.default_rng(3)
+    ys = {}
+    for mode in (0, 3):
+        cfg = full_cfg(base, far_on_gpu=mode)
+        cfg_path, x_path, y_path = (str(tmp_path / f"{n}{mode}.bin") for n in ("cfg", "x", "y"))
+        with open(cfg_path, "wb") as f:
+            f.write(bytes(cfg.to_c()))
+        n = (1 << (2 * cfg.nLevelsUniform)) * cfg.nChebNodes ** 2
+        if mode == 0:
+            x = rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)
+        x.astype(np.complex128).tofile(x_path)
+        out = subprocess.run([exe, cfg_path, x_path, y_path, "--far-only"], capture_output=True, text=True, timeout=600)
+        assert out.returncode == 0, out.stdout + out.stderr
+        ys[mode] = np.fromfile(y_path, dtype=np.complex128)
+    assert np.linalg.norm(ys[0]) > 0 and np.array_equal(ys[3], ys[0])

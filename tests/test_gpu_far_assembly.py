@@ -73,3 +73,29 @@ def test_far_assembly_on_gpu_against_host(ls, ora, base):
     o.close()
     tighter.close()
     host.close()
+
+
+@pytest.mark.parametrize("base", [CFG_C1, CFG_L5_BUMPS], ids=["c1", "level5-kappa40"])
+def test_m2l_tiles_filled_on_the_device(ls, base):
+    """far_on_gpu = 3 fills the M2L tiles from the far-field table on the
+    device and the operator adopts them; far_on_gpu = 2 packs the same
+    entries on the host from the same table. Same skeletons, the same FP64
+    matvec bit for bit, and the forms derived from the device tiles (FP32,
+    double-float, the 64-wide tensor-core apply) agree as well."""
+    rng = np.random.default_rng(31)
+    ops = {m: ls.Operator(full_cfg(base, far_on_gpu=m), device=0) for m in (2, 3)}
+    x = rng.uniform(-1, 1, ops[2].N) + 1j * rng.uniform(-1, 1, ops[2].N)
+    assert np.array_equal(ops[2].skeleton_dump(), ops[3].skeleton_dump())
+    y = {m: op.matvec(x) for m, op in ops.items()}
+    assert np.array_equal(y[2], y[3])
+    for op in ops.values():
+        op.enable_f32()
+        op.set_f64_kernels(ls.LS_F64_DOUBLE_FLOAT)
+    assert np.array_equal(ops[2].matvec(x), ops[3].matvec(x))
+    X = np.asfortranarray(rng.uniform(-1, 1, (ops[2].N, 64)) + 1j * rng.uniform(-1, 1, (ops[2].N, 64)))
+    assert np.array_equal(ops[2].matvec_f32_many(X), ops[3].matvec_f32_many(X))
+    b = ops[3].rhs()
+    xs, hist, it, rr, code = ops[3].gmres(b, 300, 1e-10)
+    assert code == ls.LS_OK and rr <= 2e-10
+    for op in ops.values():
+        op.close()
