@@ -111,7 +111,10 @@ typedef struct {
    * pivots among candidates equal in magnitude up to such bits (mirror-image
    * positions of a uniform tree): the skeletons are other valid choices, and
    * the matvec moves by less than the host-assembled operator itself moves
-   * when the NCA tolerance is tightened tenfold. Adaptive trees ignore it. */
+   * when the NCA tolerance is tightened tenfold. Adaptive trees ignore it,
+   * and so do trees whose table would pass 4 GB (the x and y offsets of a
+   * level-8 tree give about 14 GB; level 7: 2.9 GB): those assemble on the
+   * default path. */
   int far_on_gpu;
 } ls_config;
 
