@@ -92,3 +92,20 @@ def test_table_filled_m2l_tiles_equal_the_default_packing(ls, tmp_path, base):
         assert out.returncode == 0, out.stdout + out.stderr
         ys[mode] = np.fromfile(y_path, dtype=np.complex128)
     assert np.linalg.norm(ys[0]) > 0 and np.array_equal(ys[3], ys[0])
+
+
+@pytest.mark.parametrize("over", [dict(findPhi=0), dict(nChebNodes=4, degreeOfBases=4), dict(reference_rounding=0)],
+                         ids=["bare-helmholtz", "4x4-nodes", "unrounded"])
+def test_host_tabulated_far_field_other_operators(ls, ora, over):
+    """The table's indexing for other node counts (rank 16: x rows of 4
+    nodes), the bare Helmholtz operator (no kappa^2 q scaling) and unrounded
+    moments: the assembly stays the oracle's bit for bit, table fill of the
+    M2L tiles included (mode 3 without a device)."""
+    cfg = full_cfg(CFG_HFR, far_on_gpu=3, **over)
+    op = ls.Operator(cfg, device=-1)
+    ref = ora.Oracle(cfg.as_dict())
+    assert np.array_equal(op.skeleton_dump(), ref.skeleton_dump())
+    M, B = op.precomputations()
+    assert np.array_equal(M, ref.far_moments()) and np.array_equal(B, ref.near_blocks())
+    ref.close()
+    op.close()
