@@ -378,8 +378,10 @@ int ls_get_near_overlap(void);
  * assembly that reads it is the same bit for bit. dir NULL: off (the
  * default); "": records kept in memory for the process; a directory: also
  * stored there as binary files (one per record, shared between processes;
- * a file that does not match its key is ignored). Process-wide; setting it
- * drops the records held in memory. ls_precompute_cache_stats: records
+ * a file that does not match its key is ignored; a directory that cannot
+ * be written costs only the files). Records held in memory are capped at
+ * 2 GB, past which they are dropped (the files still serve). Process-wide;
+ * setting it drops the records held in memory. ls_precompute_cache_stats: records
  * found and not found since the process started.
  */
 ls_status ls_set_precompute_cache(const char* dir);

@@ -219,6 +219,7 @@ class PrecomputeCache {
     on_ = dir != nullptr;
     dir_ = dir ? dir : "";
     mem_.clear();
+    mem_bytes_ = 0;
   }
   bool enabled() {
     std::lock_guard<std::mutex> lk(mu_);
@@ -239,7 +240,14 @@ class PrecomputeCache {
     }
     if (!dir.empty() && read_file(dir, key, out)) {
       std::lock_guard<std::mutex> lk(mu_);
-      mem_[key] = out;
+      if (mem_bytes_ + out.size() * sizeof(cd) > kMemCap) {
+        mem_.clear();
+        mem_bytes_ = 0;
+      }
+      if (!mem_.count(key)) {
+        mem_[key] = out;
+        mem_bytes_ += out.size() * sizeof(cd);
+      }
       ++hits_;
       return true;
     }
@@ -252,7 +260,16 @@ class PrecomputeCache {
     {
       std::lock_guard<std::mutex> lk(mu_);
       if (!on_) return;
+      // Records held in memory are capped: past the cap they are dropped
+      // (files, when there is a directory, still serve them).
+      if (mem_bytes_ + v.size() * sizeof(cd) > kMemCap) {
+        mem_.clear();
+        mem_bytes_ = 0;
+      }
+      auto it = mem_.find(key);
+      if (it != mem_.end()) mem_bytes_ -= it->second.size() * sizeof(cd);
       mem_[key] = v;
+      mem_bytes_ += v.size() * sizeof(cd);
       dir = dir_;
     }
     if (!dir.empty()) write_file(dir, key, v);
@@ -265,6 +282,7 @@ class PrecomputeCache {
 
  private:
   static constexpr uint32_t kVersion = 1;
+  static constexpr size_t kMemCap = size_t(2) << 30;  // bytes of records held in memory
   static std::string path(const std::string& dir, const std::string& key) {
     uint64_t h = 1469598103934665603ULL;  // FNV-1a
     for (unsigned char c : key) h = (h ^ c) * 1099511628211ULL;
@@ -317,6 +335,7 @@ class PrecomputeCache {
   bool on_ = false;
   std::string dir_;
   std::map<std::string, std::vector<cd>> mem_;
+  size_t mem_bytes_ = 0;
   long long hits_ = 0, misses_ = 0;
 };
 PrecomputeCache g_pcache;

@@ -131,3 +131,22 @@ def test_cache_off_by_default_and_stats_checked(ls):
     op.close()
     assert ls.precompute_cache_stats() == (h0, m0)
     assert ls.lib().ls_precompute_cache_stats(None, None) == ls.LS_E_INVALID
+
+
+def test_unwritable_directory_keeps_memory_records(cache, ora, tmp_path):
+    """A cache directory that cannot be written (here: a path below a plain
+    file) costs nothing but the files: assemblies still succeed, stay the
+    oracle's bit for bit, and the records held in memory still hit."""
+    ls = cache
+    blocker = tmp_path / "not_a_dir"
+    blocker.write_text("x")
+    ls.set_precompute_cache(str(blocker / "sub"))
+    cfg = full_cfg(CFG_C1)
+    h0, m0 = ls.precompute_cache_stats()
+    a = ls.Operator(cfg, device=-1)
+    b = ls.Operator(cfg, device=-1)
+    h1, m1 = ls.precompute_cache_stats()
+    assert (h1 - h0, m1 - m0) == (1, 1)
+    assert _same_as_oracle(ls, ora, cfg, b)
+    a.close()
+    b.close()
